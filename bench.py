@@ -1,0 +1,391 @@
+#!/usr/bin/env python
+"""Benchmark: state-applies/s of the Γ-point wavefunction step (H psi + rho + ortho).
+
+One step = rhoofr + vpsi + ortho(Gram-Schmidt) over all states of the cell,
+i.e. the three hot-path routines a CPMD wavefunction-optimisation step calls
+(forces_driver.mod.F90:165-224, updwf_utils.mod.F90:150).
+state-applies/s = nstate * steps / time.
+
+Workload: cubic L = 20.52 bohr, 64 atoms (2x2x2 diamond, +-0.05 bohr seeded
+jitter), 128 states, 70 Ry (ngw = 42736), mesh 120^3; psi and V_loc seeded
+synthetic.  The headline `value` is the mixed-precision path (FP32 FFT and
+V*psi, FP64 accumulation, reductions and ortho); the plain FP64 drop-in is
+measured in the same run (`fp64`).  Inputs (c0, c2: 87.5 MB each) are larger
+than the 129 MB L2 together, so no L2 flush is needed between steps.
+
+--impl reference times the reference's CPU path restated in numpy/scipy (the
+reference itself, Fortran + FFTW + BLAS, cannot be built here) on a bounded
+sample of the same step, on all host cores.
+
+Multi-GPU (torchrun): every rank runs an independent replica (the step does
+not shard across GPUs in this build); value = total over ranks, time = max.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "state-applies/s (Hpsi+rho+ortho), mixed vs FP64 on same GB300 @|dE|<=1e-6 Ha/atom"
+WORKLOAD = "cubic L=20.52 bohr, 64 atoms, 128 states, 70 Ry (ngw=42736), mesh 120^3, Gamma point"
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.stop_ev = threading.Event()
+        self.th = threading.Thread(target=self.run, daemon=True)
+
+    def run(self):
+        while not self.stop_ev.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                vals = [v.strip() for v in out.stdout.strip().split(",")]
+                if len(vals) >= 7:
+                    self.samples.append(vals)
+            except Exception:
+                pass
+            self.stop_ev.wait(0.2)
+
+    def __enter__(self):
+        self.th.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop_ev.set()
+        self.th.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def dist_setup(n_gpus: int):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("GBCP_BENCH_BACKEND", "nccl") == "nccl" else "gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x: float, world: int) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------- CPU reference (oracle port)
+def cpu_reference_sample(cell, n_band: int = 16):
+    """Time the restated reference path on a bounded sample: rhoofr + vpsi on
+    the first n_band states, ortho (Cholesky GS) on all states.  Returns the
+    extrapolated full-step time and a description."""
+    import numpy as np
+    from oracle import cpmd_oracle as O
+    b = cell.basis
+    sub = np.asfortranarray(cell.c0[:, :n_band])
+    f = cell.f[:n_band]
+    t0 = time.perf_counter()
+    O.rhoofr(sub, f, b.mill, b.nr, b.kr, b.omega, b.hg, b.tpiba2, b.geq0)
+    O.vpsi(sub, np.zeros_like(sub), f, cell.vpot, b.mill, b.nr, b.hg, b.tpiba2, b.geq0)
+    t1 = time.perf_counter()
+    O.rgs(cell.c0, b.geq0)
+    t2 = time.perf_counter()
+    n = cell.nstate
+    t_step = (t1 - t0) * (n / n_band) + (t2 - t1)
+    return t_step, (t1 - t0), (t2 - t1)
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from cpmd_gb300.synth import make_cell
+    cell = make_cell("c1")
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_reference_sample(cell, args.ref_states)
+    ts = []
+    for _ in range(args.steps):
+        t_step, tb, to = cpu_reference_sample(cell, args.ref_states)
+        ts.append(t_step)
+    t = sum(ts) / len(ts)
+    value = cell.nstate / t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "state-applies/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "global_batch": cell.nstate, "seq_len": 120 ** 3, "parallelism": "none",
+                   "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": "state-applies/s", "cores": cores, "kind": "port",
+                         "sample": f"numpy/scipy restatement (scipy.fft workers=-1, OpenBLAS): rhoofr+vpsi on "
+                                   f"{args.ref_states} of {cell.nstate} states scaled x{cell.nstate // args.ref_states}"
+                                   f", ortho on all {cell.nstate} states, per step"},
+        "e2e": {"value": value, "unit": "state-applies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def kernel_bytes(name: str, geo: dict, np_: int, s: int) -> float:
+    """Compulsory HBM bytes of one launch (s = bytes per complex of the FFT precision)."""
+    n1, n2, n3 = geo["nr"]
+    ncol, nslot, nent, ngw = geo["ncol"], geo["nslot"], geo["nent"], geo["ngw"]
+    zb = n3 * ncol * s
+    yb = n3 * n2 * nslot * s
+    grid = n1 * n2 * n3
+    if name == "k_zinv":
+        return np_ * (2 * ngw * 16 + zb)
+    if name == "k_yinv":
+        return np_ * (zb + yb)
+    if name == "k_xinv_rho":
+        return np_ * yb + 2 * grid * 8
+    if name == "k_xvx":
+        return np_ * 2 * yb + grid * 8
+    if name == "k_yfwd":
+        return np_ * (yb + zb)
+    if name == "k_zfwd":
+        return np_ * (zb + nent * s)
+    if name == "k_decode":
+        return np_ * (2 * ngw * s + 2 * ngw * 16 + 2 * 2 * ngw * 16)
+    return 0.0
+
+
+def run_gpu(args, rank, world, local):
+    import numpy as np
+    import torch
+    from cpmd_gb300 import Context, kernel_launches
+    from cpmd_gb300.synth import make_cell
+
+    torch.cuda.set_device(local)
+    cell = make_cell("c1")
+    b = cell.basis
+    n = cell.nstate
+    dev = torch.device("cuda", local)
+    c0 = torch.from_numpy(np.ascontiguousarray(cell.c0.T)).to(dev)
+    f = torch.from_numpy(cell.f).to(dev)
+    v = torch.from_numpy(cell.vpot).to(dev)
+    rho = torch.empty(tuple(b.kr[::-1]), dtype=torch.float64, device=dev)
+    c2 = torch.zeros_like(c0)
+
+    def make_step(ctx):
+        def step():
+            ctx.rhoofr(c0, f, rho, energies=False)
+            ctx.vpsi(c0, c2, f, v)
+            ctx.ortho(c0, "gs")
+        return step
+
+    def timed(ctx, steps, warmup, sample_clocks=False):
+        step = make_step(ctx)
+        for _ in range(warmup):
+            step()
+        torch.cuda.synchronize()
+        barrier(world)
+        torch.cuda.synchronize()
+        l0 = kernel_launches()
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        sampler = ClockSampler(local) if sample_clocks else None
+        if sampler:
+            sampler.__enter__()
+        s.record()
+        for _ in range(steps):
+            step()
+        e.record()
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.__exit__()
+        barrier(world)
+        ms = s.elapsed_time(e)
+        return ms, kernel_launches() - l0, (sampler.summary() if sampler else None)
+
+    batch = args.batch
+    ctx_mx = Context(b, "mixed", batch=batch)
+    ctx_64 = Context(b, "fp64", batch=batch)
+    ms_mx, launches, clocks = timed(ctx_mx, args.steps, args.warmup, sample_clocks=True)
+    ms_mx = allreduce_max(ms_mx, world)
+    ms_64, _, _ = timed(ctx_64, args.fp64_steps, max(1, min(args.warmup, 2)))
+    ms_64 = allreduce_max(ms_64, world)
+
+    value = world * n * args.steps / (ms_mx / 1e3)
+    v64 = world * n * args.fp64_steps / (ms_64 / 1e3)
+
+    # accuracy of the mixed step against FP64 on the same inputs: energy E_kin + int V rho
+    rho64, ek64, _, _ = ctx_64.rhoofr(c0, f)
+    rhomx, ekmx, _, _ = ctx_mx.rhoofr(c0, f)
+    dv = b.omega / (b.nr[0] * b.nr[1] * b.nr[2])
+    e64 = ek64 + dv * float((rho64 * v).sum())
+    emx = ekmx + dv * float((rhomx * v).sum())
+    nat = cell.tau.shape[0]
+
+    # live per-kernel timing (CUDA events on the library stream) over profiled steps
+    ctx_mx.profile(True)
+    for _ in range(2):
+        make_step(ctx_mx)()
+    prof = ctx_mx.profile_read()
+    ctx_mx.profile(False)
+    geo = geometry_summary(b)
+    npairs = (n + 1) // 2
+    bt = min(batch, npairs)
+    dom = max(prof.items(), key=lambda kv: kv[1][0])
+    dname, (dms, dcount) = dom
+    hbm, bf16, src = peaks()
+    per_launch_ms = dms / dcount
+    bytes_per_launch = kernel_bytes(dname, geo, bt, 8)
+    achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9 if bytes_per_launch else None
+    step_ms_prof = sum(t for t, _ in prof.values()) / 2
+
+    # end to end through the public API with host (pinned) buffers
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()  # noqa: E731
+    c0h = pin((n, b.ngw), torch.complex128)
+    c0h[:] = cell.c0.T
+    c0h = c0h.T  # Fortran (ngw, n) view of pinned memory
+    c2h = pin((n, b.ngw), torch.complex128)
+    c2h[:] = 0
+    c2h = c2h.T
+    fh = pin((n,), torch.float64)
+    fh[:] = cell.f
+    vh = pin(tuple(b.kr[::-1]), torch.float64)
+    vh[:] = cell.vpot
+    rhoh = pin(tuple(b.kr[::-1]), torch.float64)
+
+    def e2e_step():
+        ctx_mx.rhoofr(c0h, fh, rhoh, energies=False)
+        ctx_mx.vpsi(c0h, c2h, fh, vh)
+        ctx_mx.ortho(c0h, "gs")
+
+    for _ in range(2):
+        e2e_step()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    t_e2e = allreduce_max(time.perf_counter() - t0, world)
+    wfn = b.ngw * n * 16
+    grid = b.nnr1 * 8
+    h2d = 3 * wfn + wfn + 2 * n * 8 + grid
+    d2h = grid + wfn + wfn
+    e2e = world * n * args.e2e_steps / t_e2e
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        ts = [cpu_reference_sample(cell, args.ref_states)[0] for _ in range(2)]
+        cpu = {"value": n / min(ts), "unit": "state-applies/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"numpy/scipy restatement of rhoofr+vpsi on {args.ref_states} of {n} states scaled "
+                         f"x{n // args.ref_states} + ortho on all {n} states; best of 2"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "state-applies/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_mx / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-fft/f64-accum", "data": "synthetic (seeded psi, V_loc)",
+            "config": {"workload": WORKLOAD, "global_batch": n * world, "seq_len": 120 ** 3,
+                       "parallelism": "replicas" if world > 1 else "none", "precision": "mixed",
+                       "pairs_per_batch": bt, "l2": "inputs larger than L2 (c0+c2 = 175 MB)"},
+            "fp64": {"value": v64, "ms_per_step": ms_64 / args.fp64_steps, "steps": args.fp64_steps,
+                     "mixed_over_fp64": value / v64},
+            "accuracy": {"dE_Ha_per_atom_mixed_vs_fp64": abs(emx - e64) / nat, "E_fp64_Ha": e64},
+            "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                         "peak_source": src, "launch_ms": per_launch_ms, "bytes_per_launch": bytes_per_launch,
+                         "kernel_share": dms / 2 / step_ms_prof},
+            "kernels_ms_per_step": {k: round(t / 2, 4) for k, (t, _) in sorted(prof.items(), key=lambda kv: -kv[1][0])},
+            "clocks": clocks,
+            "e2e": {"value": e2e, "unit": "state-applies/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "steps": args.e2e_steps, "path": "C ABI, host (pinned) buffers, GBCP_MEM_HOST"},
+            "gpu_launches": launches,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    ctx_mx.close()
+    ctx_64.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--fp64-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--ref-states", type=int, default=16)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def geometry_summary(basis) -> dict:
+    """Column / slot counts of the pruned FFT (mirrors the context's map build)."""
+    import numpy as np
+    m = basis.mill[: basis.ngw].astype(np.int64)
+    full = np.concatenate([m, -m[1:]]) if basis.geq0 else np.concatenate([m, -m])
+    cols = {}
+    for gx, gy, gz in full.tolist():
+        cols.setdefault((gx, gy), []).append(gz)
+    gxs = sorted({k[0] for k in cols})
+    ncol = 0
+    nent = 0
+    for gx in range(gxs[0], gxs[-1] + 1):
+        gys = [k[1] for k in cols if k[0] == gx]
+        if not gys:
+            continue
+        for gy in range(min(gys), max(gys) + 1):
+            z = cols.get((gx, gy))
+            ncol += 1
+            if z:
+                nent += max(z) - min(z) + 1
+    return {"nr": basis.nr, "ncol": ncol, "nslot": gxs[-1] - gxs[0] + 1, "nent": nent, "ngw": basis.ngw}
+
+
+if __name__ == "__main__":
+    main()

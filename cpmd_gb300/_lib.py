@@ -1,0 +1,81 @@
+"""ctypes binding of ``libcpmd_gb300.so`` (the C ABI in include/cpmd_gb300.h)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libcpmd_gb300.so"
+
+GBCP_OK = 0
+STATUS = {
+    0: "OK", 1: "ERR_ARG", 2: "ERR_NOT_SPD", 3: "ERR_NONFINITE", 4: "ERR_TIMEOUT",
+    5: "ERR_CUDA", 6: "ERR_NOMEM", 7: "ERR_UNSUPPORTED", 8: "ERR_NOT_CONVERGED",
+}
+PREC = {"fp64": 0, "mixed": 1}
+MEM_HOST, MEM_DEVICE = 0, 1
+ORTHO = {"gs": 0, "lowdin": 1}
+
+
+class GbcpError(RuntimeError):
+    def __init__(self, fn: str, code: int, msg: str = ""):
+        super().__init__(f"{fn}: {STATUS.get(code, code)} {msg}".strip())
+        self.code = code
+
+
+class GridDesc(C.Structure):
+    _fields_ = [
+        ("nr1", C.c_int32), ("nr2", C.c_int32), ("nr3", C.c_int32),
+        ("kr1", C.c_int32), ("kr2", C.c_int32), ("kr3", C.c_int32),
+        ("ngw", C.c_int32), ("geq0", C.c_int32),
+        ("omega", C.c_double), ("tpiba2", C.c_double),
+        ("inyh", C.POINTER(C.c_int32)), ("hg", C.POINTER(C.c_double)),
+    ]
+
+
+_P = C.c_void_p
+_I = C.c_int
+_D = C.c_double
+_DP = C.POINTER(C.c_double)
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "gbcp_ctx_create": (_I, [C.POINTER(GridDesc), _I, _I, _P, C.POINTER(_P)]),
+    "gbcp_ctx_destroy": (_I, [_P]),
+    "gbcp_set_precision": (_I, [_P, _I]),
+    "gbcp_synchronize": (_I, [_P]),
+    "gbcp_last_error": (_I, [_P, C.c_char_p, _I]),
+    "gbcp_kernel_launches": (C.c_int64, []),
+    "gbcp_profile_enable": (_I, [_P, _I]),
+    "gbcp_profile_read": (_I, [_P, _I, C.c_char_p, _I, _DP, C.POINTER(C.c_int64)]),
+    "gbcp_rhoofr": (_I, [_P, _P, _I, _I, _P, _P, _DP, _DP, _DP, _I]),
+    "gbcp_vpsi": (_I, [_P, _P, _I, _P, _I, _P, _P, _I, _I]),
+    "gbcp_ortho": (_I, [_P, _P, _I, _I, _I, _DP, _I]),
+    "gbcp_ovlap": (_I, [_P, _P, _I, _I, _P, _I]),
+    "gbcp_invfftn": (_I, [_P, _P, _I]),
+    "gbcp_fwfftn": (_I, [_P, _P, _I]),
+    "gbcp_rnlsm1": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _I]),
+    "gbcp_fnonloc": (_I, [_P, _P, _I, _I, _P, _I, _I, _P, _P, _P, _P, _P, _I]),
+}
+
+_lib = None
+
+
+def load(path: str | os.PathLike | None = None):
+    """Load the CUDA library; raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with cpmd_gb300.build.build() "
+                           "(the hot path has no CPU fallback)")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib

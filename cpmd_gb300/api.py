@@ -1,0 +1,252 @@
+"""Host-side mirror of CPMD's Fortran entry points over the GB300 C ABI.
+
+The reference routines take their grid and basis from module globals; here a
+:class:`Context` holds them (one ``gbcp_ctx``), and each method is the routine
+of the same name:
+
+=================  =========================================  ==============================
+method             reference routine                          file:line
+=================  =========================================  ==============================
+``rhoofr``         rhoofr(c0, rhoe, psi, nstate)              rhoofr_utils.mod.F90:122
+``vpsi``           vpsi(c0, c2, f, vpot, psi, nstate, ...)    vpsi_utils.mod.F90:120
+``ortho``          ortho(nstate, c0, cscr)                    ortho_utils.mod.F90:124
+``ovlap``          ovlap(nstate, a, c1, c2) (c1 == c2)         ovlap_utils.mod.F90:57
+``invfftn``        invfftn(f, sparse=.FALSE., ...)            fftmain_utils.mod.F90:373
+``fwfftn``         fwfftn(f, sparse=.FALSE., ...)             fftmain_utils.mod.F90:403
+``rnlsm``          rnlsm(c0, nstate, ...) -> rnlsm1           rnlsm_utils.mod.F90:23
+``fnonloc``        fnonloc(c2, f, nstate, ...)                fnonloc_utils.mod.F90:55
+=================  =========================================  ==============================
+
+Arrays may be numpy arrays (host memory; the call stages them and
+synchronises) or torch CUDA tensors (device memory; the call is queued on the
+context's stream).  Layouts follow the reference:
+
+* wavefunctions: Fortran ``c0(ngw, nstate)`` complex128 -> numpy
+  ``order='F'`` array of shape (ngw, nstate), or a torch tensor of shape
+  (nstate, ngw) (row-major), i.e. the same bytes;
+* real-space arrays: Fortran ``rhoe(kr1, kr2, kr3)`` -> numpy / torch array
+  of shape (kr3, kr2, kr1);
+* fnl: Fortran ``fnl(nat, ngh, nstate)`` -> shape (nstate, ngh, nat).
+
+Errors raise :class:`GbcpError` (the reference aborts via stopgm).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import MEM_DEVICE, MEM_HOST, ORTHO, PREC, GbcpError
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if _is_torch(x):
+        if not x.is_cuda:
+            raise ValueError("torch tensors must live on a CUDA device (use numpy for host arrays)")
+        if not x.is_contiguous():
+            raise ValueError("torch tensors must be contiguous")
+        return C.c_void_p(x.data_ptr())
+    if not (x.flags["F_CONTIGUOUS"] or x.flags["C_CONTIGUOUS"]):
+        # column-major wavefunction views with a leading dimension are allowed
+        if not (x.ndim == 2 and x.strides[0] == x.itemsize):
+            raise ValueError("numpy arrays must be contiguous")
+    return C.c_void_p(x.ctypes.data)
+
+
+def _mem(*arrs) -> int:
+    kinds = {(_is_torch(a)) for a in arrs if a is not None}
+    if len(kinds) != 1:
+        raise ValueError("all array arguments of one call must be either numpy (host) or torch CUDA (device)")
+    return MEM_DEVICE if kinds.pop() else MEM_HOST
+
+
+def _ld_wfn(c, ngw: int) -> tuple[int, int]:
+    """(leading dimension, nstate) of a wavefunction array."""
+    if _is_torch(c):
+        if c.dim() != 2:
+            raise ValueError("wavefunction tensor must be (nstate, ngw)")
+        import torch
+        if c.dtype != torch.complex128:
+            raise ValueError("wavefunctions are complex128")
+        return int(c.shape[1]), int(c.shape[0])
+    if c.dtype != np.complex128 or c.ndim != 2:
+        raise ValueError("wavefunctions are complex128 (ngw, nstate)")
+    if c.shape[0] < ngw:
+        raise ValueError(f"wavefunction leading dimension {c.shape[0]} < ngw {ngw}")
+    # Fortran column-major, possibly a leading-dimension view c(1:ngw, :) of a larger array
+    if c.shape[1] > 1 and (c.strides[0] != 16 or c.strides[1] % 16 != 0):
+        raise ValueError("numpy wavefunctions must be column-major (ngw, nstate)")
+    ld = c.strides[1] // 16 if c.shape[1] > 1 else c.shape[0]
+    return int(ld), int(c.shape[1])
+
+
+class Context:
+    """One drop-in context: grid + basis + precision + stream."""
+
+    def __init__(self, basis, precision: str = "fp64", batch: int = 0, stream=None):
+        self.lib = _lib.load()
+        self.basis = basis
+        self.ngw = basis.ngw
+        self.kr = tuple(basis.kr)
+        self.nr = tuple(basis.nr)
+        self._inyh = np.ascontiguousarray(basis.inyh[:, : basis.ngw].T.astype(np.int32))  # (ngw, 3) == Fortran (3, ngw)
+        self._hg = np.ascontiguousarray(basis.hg[: basis.ngw], dtype=np.float64)
+        g = _lib.GridDesc()
+        g.nr1, g.nr2, g.nr3 = basis.nr
+        g.kr1, g.kr2, g.kr3 = basis.kr
+        g.ngw = basis.ngw
+        g.geq0 = 1 if basis.geq0 else 0
+        g.omega = basis.omega
+        g.tpiba2 = basis.tpiba2
+        g.inyh = self._inyh.ctypes.data_as(C.POINTER(C.c_int32))
+        g.hg = self._hg.ctypes.data_as(C.POINTER(C.c_double))
+        h = C.c_void_p()
+        st = C.c_void_p(stream) if stream is not None else None
+        rc = self.lib.gbcp_ctx_create(C.byref(g), PREC[precision], int(batch), st, C.byref(h))
+        if rc != 0:
+            raise GbcpError("gbcp_ctx_create", rc)
+        self.h = h
+        self.precision = precision
+
+    # -- housekeeping --------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gbcp_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_precision(self, precision: str):
+        self._check("gbcp_set_precision", self.lib.gbcp_set_precision(self.h, PREC[precision]))
+        self.precision = precision
+
+    def synchronize(self):
+        self._check("gbcp_synchronize", self.lib.gbcp_synchronize(self.h))
+
+    def last_error(self) -> str:
+        buf = C.create_string_buffer(512)
+        self.lib.gbcp_last_error(self.h, buf, 512)
+        return buf.value.decode(errors="replace")
+
+    def profile(self, enable: bool = True):
+        """Start (clear) or stop the per-kernel CUDA-event timers."""
+        self._check("gbcp_profile_enable", self.lib.gbcp_profile_enable(self.h, 1 if enable else 0))
+
+    def profile_read(self) -> dict:
+        """{kernel name: (total ms, launches)} since the last profile(True)."""
+        out = {}
+        i = 0
+        buf = C.create_string_buffer(128)
+        ms = C.c_double()
+        n = C.c_int64()
+        while self.lib.gbcp_profile_read(self.h, i, buf, 128, C.byref(ms), C.byref(n)) == 0:
+            out[buf.value.decode()] = (ms.value, int(n.value))
+            i += 1
+        return out
+
+    def _check(self, fn: str, rc: int):
+        if rc != 0:
+            raise GbcpError(fn, rc, self.last_error())
+
+    # -- hot path ------------------------------------------------------------
+    def rhoofr(self, c0, f, rhoe=None, energies: bool = True):
+        """Density (padded layout) and, if ``energies``, (ekin, csumg, csumr)."""
+        ldc, n = _ld_wfn(c0, self.ngw)
+        if rhoe is None:
+            if _is_torch(c0):
+                import torch
+                rhoe = torch.empty(self.kr[::-1], dtype=torch.float64, device=c0.device)
+            else:
+                rhoe = np.empty(self.kr[::-1])
+        mem = _mem(c0, f, rhoe)
+        ek, cg, cr = C.c_double(), C.c_double(), C.c_double()
+        refs = (C.byref(ek), C.byref(cg), C.byref(cr)) if energies else (None, None, None)
+        self._check("gbcp_rhoofr", self.lib.gbcp_rhoofr(self.h, _ptr(c0), ldc, n, _ptr(f), _ptr(rhoe), *refs, mem))
+        if energies:
+            return rhoe, ek.value, cg.value, cr.value
+        return rhoe
+
+    def vpsi(self, c0, c2, f, vpot):
+        """c2 += -f (1/2 G^2 c0 + [V psi](G)); returns c2."""
+        ldc, n = _ld_wfn(c0, self.ngw)
+        ld2, n2 = _ld_wfn(c2, self.ngw)
+        if n2 != n:
+            raise ValueError("c0 and c2 state counts differ")
+        mem = _mem(c0, c2, f, vpot)
+        self._check("gbcp_vpsi", self.lib.gbcp_vpsi(self.h, _ptr(c0), ldc, _ptr(c2), ld2, _ptr(f), _ptr(vpot), n, mem))
+        return c2
+
+    def ortho(self, c0, method: str = "gs"):
+        """Orthonormalise c0 in place; returns scond = max|S - I| of the input."""
+        ldc, n = _ld_wfn(c0, self.ngw)
+        sc = C.c_double()
+        self._check("gbcp_ortho", self.lib.gbcp_ortho(self.h, _ptr(c0), ldc, n, ORTHO[method], C.byref(sc), _mem(c0)))
+        return sc.value
+
+    def ovlap(self, c0, smat=None):
+        ldc, n = _ld_wfn(c0, self.ngw)
+        if smat is None:
+            if _is_torch(c0):
+                import torch
+                smat = torch.empty((n, n), dtype=torch.float64, device=c0.device)
+            else:
+                smat = np.empty((n, n))
+        self._check("gbcp_ovlap", self.lib.gbcp_ovlap(self.h, _ptr(c0), ldc, n, _ptr(smat), _mem(c0, smat)))
+        return smat
+
+    def invfftn(self, grid):
+        """In-place inverse 3D FFT of a complex grid shaped (nr3, kr2, kr1)."""
+        self._check("gbcp_invfftn", self.lib.gbcp_invfftn(self.h, _ptr(grid), _mem(grid)))
+        return grid
+
+    def fwfftn(self, grid):
+        self._check("gbcp_fwfftn", self.lib.gbcp_fwfftn(self.h, _ptr(grid), _mem(grid)))
+        return grid
+
+    def rnlsm(self, c0, twnl, eigr, nghtol, fnl=None):
+        """fnl (nstate, ngh, nat) == Fortran fnl(nat, ngh, nstate)."""
+        ldc, n = _ld_wfn(c0, self.ngw)
+        ngh = int(len(nghtol))
+        nat = int(eigr.shape[1] if not _is_torch(eigr) else eigr.shape[0])
+        nt = np.ascontiguousarray(np.asarray(nghtol, dtype=np.int32))
+        if fnl is None:
+            if _is_torch(c0):
+                import torch
+                fnl = torch.empty((n, ngh, nat), dtype=torch.float64, device=c0.device)
+            else:
+                fnl = np.empty((n, ngh, nat))
+        mem = _mem(c0, twnl, eigr, fnl)
+        self._check("gbcp_rnlsm1", self.lib.gbcp_rnlsm1(self.h, _ptr(c0), ldc, n, nat, ngh, _ptr(nt), _ptr(twnl),
+                                                        _ptr(eigr), _ptr(fnl), mem))
+        return fnl
+
+    def fnonloc(self, c2, f, fnl, twnl, eigr, nghtol, wsg):
+        ld2, n = _ld_wfn(c2, self.ngw)
+        ngh = int(len(nghtol))
+        nat = int(eigr.shape[1] if not _is_torch(eigr) else eigr.shape[0])
+        nt = np.ascontiguousarray(np.asarray(nghtol, dtype=np.int32))
+        mem = _mem(c2, f, fnl, twnl, eigr, wsg)
+        self._check("gbcp_fnonloc", self.lib.gbcp_fnonloc(self.h, _ptr(c2), ld2, n, _ptr(f), nat, ngh, _ptr(nt),
+                                                          _ptr(twnl), _ptr(eigr), _ptr(fnl), _ptr(wsg), mem))
+        return c2
+
+
+def kernel_launches() -> int:
+    return int(_lib.load().gbcp_kernel_launches())

@@ -1,0 +1,663 @@
+// C ABI of the GB300 wavefunction hot path (declared in include/cpmd_gb300.h).
+//
+// The context replaces the reference's FFT set-up (fftprp_utils.mod.F90:
+// 116-330 builds the ray maps nzh/indz/msp; fftnew_utils.mod.F90:101-170
+// copies them to the device) and the module singletons cp_cufft/cp_curho/
+// cp_cuvpsi (per-stream device buffers).  The maps here describe the
+// sphere column by column for the pruned 3D FFT of band.cu.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/cpmd_gb300.h"
+#include "ctx.h"
+
+namespace gbcp {
+
+std::atomic<long long> g_launches{0};
+
+bool ensure(Ctx& c, Scratch& s, size_t bytes) {
+  if (bytes <= s.cap && s.p) return true;
+  if (s.p) {
+    cudaStreamSynchronize(c.stream);
+    cudaFree(s.p);
+    s.p = nullptr;
+    s.cap = 0;
+  }
+  if (bytes == 0) bytes = 16;
+  if (cudaMalloc(&s.p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    s.p = nullptr;
+    return false;
+  }
+  s.cap = bytes;
+  return true;
+}
+
+static cudaEvent_t pool_event(Ctx& c) {
+  if (!c.prof_pool.empty()) {
+    cudaEvent_t e = c.prof_pool.back();
+    c.prof_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+ProfScope::ProfScope(Ctx& ctx, const char* name) : c(ctx), on(ctx.prof) {
+  if (!on) return;
+  r.name = name;
+  r.a = pool_event(c);
+  r.b = pool_event(c);
+  cudaEventRecord(r.a, c.stream);
+}
+
+ProfScope::~ProfScope() {
+  if (!on) return;
+  cudaEventRecord(r.b, c.stream);
+  c.prof_live.push_back(r);
+}
+
+void prof_fold(Ctx& c) {
+  if (c.prof_live.empty()) return;
+  cudaStreamSynchronize(c.stream);
+  for (ProfRec& r : c.prof_live) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    bool found = false;
+    for (auto& kv : c.prof_acc) {
+      if (kv.first == r.name) {
+        kv.second.ms += ms;
+        kv.second.n += 1;
+        found = true;
+        break;
+      }
+    }
+    if (!found) {
+      ProfAcc a;
+      a.ms = ms;
+      a.n = 1;
+      c.prof_acc.push_back({r.name, a});
+    }
+    c.prof_pool.push_back(r.a);
+    c.prof_pool.push_back(r.b);
+  }
+  c.prof_live.clear();
+}
+
+static void release(Scratch& s) {
+  if (s.p) cudaFree(s.p);
+  s.p = nullptr;
+  s.cap = 0;
+}
+
+// Factor n into radices 8, 5, 4, 3, 2 (largest first).  0 if n has a prime
+// factor above 5 (the reference's own FFT tables hold 2,3,5-smooth sizes only,
+// gfft_utils.mod.F90:39-84).
+static bool make_plan(int n, FftPlan& p) {
+  p.n = n;
+  p.npass = 0;
+  int m = n;
+  const int rad[5] = {8, 5, 4, 3, 2};
+  while (m > 1) {
+    bool found = false;
+    for (int r : rad) {
+      if (m % r == 0) {
+        if (p.npass >= kMaxPasses) return false;
+        p.radix[p.npass++] = r;
+        m /= r;
+        found = true;
+        break;
+      }
+    }
+    if (!found) return false;
+  }
+  if (p.npass == 0) {  // n == 1
+    return false;
+  }
+  return true;
+}
+
+template <typename T> static bool upload(Ctx& c, const std::vector<T>& h, const T*& dptr) {
+  void* p = nullptr;
+  const size_t bytes = std::max<size_t>(sizeof(T) * h.size(), 16);
+  if (cudaMalloc(&p, bytes) != cudaSuccess) return false;
+  if (!h.empty() && cudaMemcpy(p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess) return false;
+  c.dev_allocs.push_back(p);
+  dptr = static_cast<const T*>(p);
+  return true;
+}
+
+static int build_geometry(Ctx& c, const int32_t* inyh, const double* hg) {
+  const int n[3] = {c.nr[0], c.nr[1], c.nr[2]};
+  const int ngw = c.ngw;
+  struct Pt {
+    int gx, gy, gz, ent;
+  };
+  std::vector<Pt> pts;
+  pts.reserve(2 * (size_t)ngw);
+  for (int ig = 0; ig < ngw; ++ig) {
+    int m[3];
+    for (int a = 0; a < 3; ++a) {
+      m[a] = inyh[3 * (size_t)ig + a] - (n[a] / 2 + 1);
+      if (2 * std::abs(m[a]) >= n[a]) {
+        c.err = "inyh: G vector " + std::to_string(ig) + " outside the mesh";
+        return 1;
+      }
+    }
+    pts.push_back({m[0], m[1], m[2], ig + 1});
+    if (m[0] != 0 || m[1] != 0 || m[2] != 0) pts.push_back({-m[0], -m[1], -m[2], -(ig + 1)});
+  }
+  // columns keyed by (gx, gy)
+  std::map<std::pair<int, int>, std::vector<std::pair<int, int>>> cols;
+  for (const Pt& p : pts) cols[{p.gx, p.gy}].push_back({p.gz, p.ent});
+  // slots: gx range and per gx the gy range (dense, holes allowed)
+  std::map<int, std::pair<int, int>> gyr;
+  for (auto& kv : cols) {
+    const int gx = kv.first.first, gy = kv.first.second;
+    auto it = gyr.find(gx);
+    if (it == gyr.end()) gyr[gx] = {gy, gy};
+    else it->second = {std::min(it->second.first, gy), std::max(it->second.second, gy)};
+  }
+  const int gxlo = gyr.begin()->first, gxhi = gyr.rbegin()->first;
+  const int nslot = gxhi - gxlo + 1;
+  std::vector<int> slot_col0(nslot, 0), slot_gylo(nslot, 0), slot_ncol(nslot, 0);
+  std::vector<int> col_start, col_zlo, col_ent, col_slot, col_gy, ent_col;
+  std::vector<int> pos_plus(ngw, -1), pos_minus(ngw, -1);
+  int ncol = 0;
+  for (int s = 0; s < nslot; ++s) {
+    const int gx = gxlo + s;
+    slot_col0[s] = ncol;
+    auto it = gyr.find(gx);
+    if (it == gyr.end()) continue;  // empty slot (hole in gx)
+    slot_gylo[s] = it->second.first;
+    slot_ncol[s] = it->second.second - it->second.first + 1;
+    for (int gy = it->second.first; gy <= it->second.second; ++gy) {
+      col_start.push_back((int)col_ent.size());
+      col_slot.push_back(s);
+      col_gy.push_back(gy);
+      auto ci = cols.find({gx, gy});
+      if (ci == cols.end()) {
+        col_zlo.push_back(0);
+      } else {
+        int zlo = 1 << 30, zhi = -(1 << 30);
+        for (auto& e : ci->second) {
+          zlo = std::min(zlo, e.first);
+          zhi = std::max(zhi, e.first);
+        }
+        col_zlo.push_back(zlo);
+        const int base = (int)col_ent.size();
+        col_ent.resize(base + (zhi - zlo + 1), 0);
+        ent_col.resize(col_ent.size(), ncol);
+        for (auto& e : ci->second) {
+          const int pos = base + (e.first - zlo);
+          if (col_ent[pos] != 0) {
+            c.err = "inyh: duplicate G vector";
+            return 1;
+          }
+          col_ent[pos] = e.second;
+          if (e.second > 0) pos_plus[e.second - 1] = pos;
+          else pos_minus[-e.second - 1] = pos;
+        }
+      }
+      ++ncol;
+    }
+  }
+  col_start.push_back((int)col_ent.size());
+  for (int ig = 0; ig < ngw; ++ig)
+    if (pos_minus[ig] < 0) pos_minus[ig] = pos_plus[ig];  // G = 0 is its own mirror
+  std::vector<double> hgv(hg, hg + ngw);
+  GeoDev& g = c.geo;
+  g.n1 = n[0];
+  g.n2 = n[1];
+  g.n3 = n[2];
+  g.k1 = c.kr[0];
+  g.k2 = c.kr[1];
+  g.ngw = ngw;
+  g.ncol = ncol;
+  g.nslot = nslot;
+  g.gxlo = gxlo;
+  g.nent = (int)col_ent.size();
+  if (!upload(c, col_start, g.col_start) || !upload(c, col_zlo, g.col_zlo) || !upload(c, col_ent, g.col_ent) ||
+      !upload(c, col_slot, g.col_slot) || !upload(c, col_gy, g.col_gy) || !upload(c, ent_col, g.ent_col) ||
+      !upload(c, slot_col0, g.slot_col0) || !upload(c, slot_gylo, g.slot_gylo) ||
+      !upload(c, slot_ncol, g.slot_ncol) || !upload(c, pos_plus, g.pos_plus) || !upload(c, pos_minus, g.pos_minus) ||
+      !upload(c, hgv, g.hg)) {
+    c.err = "geometry upload failed";
+    return 6;
+  }
+  return 0;
+}
+
+static int build_fft(Ctx& c) {
+  for (int a = 0; a < 3; ++a) {
+    if (!make_plan(c.nr[a], c.plan[a])) {
+      c.err = "mesh size " + std::to_string(c.nr[a]) + " is not 2,3,5-smooth";
+      return 7;
+    }
+    const int n = c.nr[a];
+    std::vector<cx<double>> t64(n);
+    std::vector<cx<float>> t32(n);
+    for (int m = 0; m < n; ++m) {
+      // FP64 host trigonometry; the quarter points are set exactly
+      const double ang = 2.0 * M_PI * (double)m / (double)n;
+      t64[m] = mk<double>(std::cos(ang), std::sin(ang));
+      if (4 * m == n) t64[m] = mk<double>(0.0, 1.0);
+      if (2 * m == n) t64[m] = mk<double>(-1.0, 0.0);
+      if (4 * m == 3 * n) t64[m] = mk<double>(0.0, -1.0);
+      t32[m] = mk<float>((float)t64[m].x, (float)t64[m].y);
+    }
+    const cx<double>* d64;
+    const cx<float>* d32;
+    if (!upload(c, t64, d64) || !upload(c, t32, d32)) {
+      c.err = "twiddle upload failed";
+      return 6;
+    }
+    c.tw64[a] = const_cast<cx<double>*>(d64);
+    c.tw32[a] = const_cast<cx<float>*>(d32);
+  }
+  return 0;
+}
+
+}  // namespace gbcp
+
+using gbcp::Ctx;
+using gbcp::cx;
+
+struct gbcp_ctx {
+  Ctx c;
+};
+
+static int set_err(gbcp_ctx* h, int rc, const char* msg) {
+  if (h && msg) h->c.err = msg;
+  return rc;
+}
+
+extern "C" {
+
+int gbcp_ctx_create(const gbcp_grid_desc* grid, int precision, int max_batch, void* stream, gbcp_ctx** out) {
+  if (!grid || !out || !grid->inyh || !grid->hg) return GBCP_ERR_ARG;
+  if (grid->nr1 < 2 || grid->nr2 < 2 || grid->nr3 < 2 || grid->kr1 < grid->nr1 || grid->kr2 < grid->nr2 ||
+      grid->kr3 < grid->nr3 || grid->ngw < 1 || !(grid->omega > 0) || !(grid->tpiba2 > 0))
+    return GBCP_ERR_ARG;
+  if (precision != GBCP_PREC_FP64 && precision != GBCP_PREC_MIXED) return GBCP_ERR_ARG;
+  gbcp_ctx* h = new gbcp_ctx();
+  Ctx& c = h->c;
+  c.nr[0] = grid->nr1;
+  c.nr[1] = grid->nr2;
+  c.nr[2] = grid->nr3;
+  c.kr[0] = grid->kr1;
+  c.kr[1] = grid->kr2;
+  c.kr[2] = grid->kr3;
+  c.ngw = grid->ngw;
+  c.geq0 = grid->geq0 ? 1 : 0;
+  c.omega = grid->omega;
+  c.tpiba2 = grid->tpiba2;
+  c.precision = precision;
+  c.batch = max_batch > 0 ? max_batch : 8;
+  if (stream) {
+    c.stream = static_cast<cudaStream_t>(stream);
+  } else {
+    if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete h;
+      return GBCP_ERR_CUDA;
+    }
+    c.own_stream = true;
+  }
+  int rc = gbcp::build_geometry(c, grid->inyh, grid->hg);
+  if (!rc) rc = gbcp::build_fft(c);
+  if (!rc && cudaMalloc(&c.d_info, 16) != cudaSuccess) rc = GBCP_ERR_NOMEM;
+  if (rc) {
+    fprintf(stderr, "gbcp_ctx_create: %s\n", c.err.c_str());
+    gbcp_ctx_destroy(h);
+    return rc;
+  }
+  *out = h;
+  return GBCP_OK;
+}
+
+int gbcp_ctx_destroy(gbcp_ctx* h) {
+  if (!h) return GBCP_OK;
+  Ctx& c = h->c;
+  if (c.stream) cudaStreamSynchronize(c.stream);
+  for (void* p : c.dev_allocs) cudaFree(p);
+  gbcp::Scratch* all[] = {&c.zbuf, &c.ybuf, &c.qbuf, &c.st_c0, &c.st_c2, &c.st_rho, &c.st_vpot, &c.st_f,
+                          &c.st_misc, &c.st_misc2, &c.red, &c.smat, &c.smat2, &c.smat3, &c.sparts, &c.cscr,
+                          &c.nl_a, &c.nl_b, &c.nl_c, &c.nl_d};
+  for (auto* s : all) gbcp::release(*s);
+  if (c.d_info) cudaFree(c.d_info);
+  gbcp::prof_fold(c);
+  for (cudaEvent_t e : c.prof_pool) cudaEventDestroy(e);
+  if (c.own_stream && c.stream) cudaStreamDestroy(c.stream);
+  delete h;
+  return GBCP_OK;
+}
+
+int gbcp_set_precision(gbcp_ctx* h, int precision) {
+  if (!h || (precision != GBCP_PREC_FP64 && precision != GBCP_PREC_MIXED)) return GBCP_ERR_ARG;
+  h->c.precision = precision;
+  return GBCP_OK;
+}
+
+int gbcp_synchronize(gbcp_ctx* h) {
+  if (!h) return GBCP_ERR_ARG;
+  cudaError_t e = cudaStreamSynchronize(h->c.stream);
+  if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));
+  return GBCP_OK;
+}
+
+int gbcp_last_error(gbcp_ctx* h, char* buf, int len) {
+  if (!h || !buf || len <= 0) return GBCP_ERR_ARG;
+  snprintf(buf, (size_t)len, "%s", h->c.err.c_str());
+  return GBCP_OK;
+}
+
+int64_t gbcp_kernel_launches(void) { return (int64_t)gbcp::g_launches.load(); }
+
+int gbcp_profile_enable(gbcp_ctx* h, int enable) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  gbcp::prof_fold(c);
+  c.prof_acc.clear();
+  c.prof = enable != 0;
+  return GBCP_OK;
+}
+
+int gbcp_profile_read(gbcp_ctx* h, int idx, char* name, int name_len, double* total_ms, int64_t* count) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  gbcp::prof_fold(c);
+  if (idx < 0 || idx >= (int)c.prof_acc.size()) return GBCP_ERR_ARG;
+  const auto& kv = c.prof_acc[(size_t)idx];
+  if (name && name_len > 0) snprintf(name, (size_t)name_len, "%s", kv.first.c_str());
+  if (total_ms) *total_ms = kv.second.ms;
+  if (count) *count = kv.second.n;
+  return GBCP_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+using gbcp::Scratch;
+
+// Stage a host (ngw x n, leading dim ld) complex array into packed device memory.
+int stage_in_cx(Ctx& c, Scratch& s, const double* h, int ld, int rows, int n, cx<double>** d) {
+  const size_t bytes = sizeof(cx<double>) * (size_t)rows * n;
+  if (!gbcp::ensure(c, s, bytes)) return GBCP_ERR_NOMEM;
+  *d = static_cast<cx<double>*>(s.p);
+  if (n > 0) {
+    GBCP_CUDA_TRY(c, cudaMemcpy2DAsync(s.p, sizeof(cx<double>) * rows, h, sizeof(cx<double>) * (size_t)ld,
+                                       sizeof(cx<double>) * rows, n, cudaMemcpyHostToDevice, c.stream));
+  }
+  return 0;
+}
+
+int stage_out_cx(Ctx& c, const cx<double>* d, double* h, int ld, int rows, int n) {
+  if (n > 0) {
+    GBCP_CUDA_TRY(c, cudaMemcpy2DAsync(h, sizeof(cx<double>) * (size_t)ld, d, sizeof(cx<double>) * rows,
+                                       sizeof(cx<double>) * rows, n, cudaMemcpyDeviceToHost, c.stream));
+  }
+  return 0;
+}
+
+int stage_in(Ctx& c, Scratch& s, const void* h, size_t bytes, void** d) {
+  if (!gbcp::ensure(c, s, bytes)) return GBCP_ERR_NOMEM;
+  *d = s.p;
+  if (bytes) GBCP_CUDA_TRY(c, cudaMemcpyAsync(s.p, h, bytes, cudaMemcpyHostToDevice, c.stream));
+  return 0;
+}
+
+int finish(Ctx& c, int rc) {
+  if (rc) {
+    if (c.err.empty()) c.err = "error";
+    return rc;
+  }
+  cudaError_t e = cudaStreamSynchronize(c.stream);
+  if (e != cudaSuccess) {
+    c.err = cudaGetErrorString(e);
+    return GBCP_ERR_CUDA;
+  }
+  return GBCP_OK;
+}
+
+bool bad_mem(int mem) { return mem != GBCP_MEM_HOST && mem != GBCP_MEM_DEVICE; }
+
+}  // namespace
+
+extern "C" {
+
+int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double* f, double* rhoe, double* ekin,
+                double* csumg, double* csumr, int mem) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  if (bad_mem(mem) || nstate < 0 || (nstate > 0 && (!c0 || !f || ldc < c.ngw)) || !rhoe)
+    return set_err(h, GBCP_ERR_ARG, "rhoofr: bad argument");
+  c.err.clear();
+  const size_t nnr1 = (size_t)c.kr[0] * c.kr[1] * c.kr[2];
+  const cx<double>* dc0 = reinterpret_cast<const cx<double>*>(c0);
+  const double* df = f;
+  double* drho = rhoe;
+  int dld = ldc;
+  int rc = 0;
+  if (mem == GBCP_MEM_HOST) {
+    cx<double>* t;
+    void* tf;
+    if ((rc = stage_in_cx(c, c.st_c0, c0, ldc, c.ngw, nstate, &t))) return rc;
+    if ((rc = stage_in(c, c.st_f, f, sizeof(double) * nstate, &tf))) return rc;
+    if (!gbcp::ensure(c, c.st_rho, sizeof(double) * nnr1)) return GBCP_ERR_NOMEM;
+    dc0 = t;
+    df = static_cast<double*>(tf);
+    drho = static_cast<double*>(c.st_rho.p);
+    dld = c.ngw;
+  }
+  rc = gbcp::band_rhoofr(c, dc0, dld, nstate, df, drho);
+  if (!rc && (ekin || csumg) && nstate > 0) rc = gbcp::kin_energy(c, dc0, dld, nstate, df, ekin, csumg);
+  if (!rc && nstate == 0) {
+    if (ekin) *ekin = 0.0;
+    if (csumg) *csumg = 0.0;
+  }
+  if (!rc && csumr) {
+    double s = 0.0;
+    rc = gbcp::rho_sum(c, drho, &s);
+    *csumr = s * c.omega / ((double)c.nr[0] * c.nr[1] * c.nr[2]);
+  }
+  if (!rc && mem == GBCP_MEM_HOST) {
+    cudaError_t e = cudaMemcpyAsync(rhoe, drho, sizeof(double) * nnr1, cudaMemcpyDeviceToHost, c.stream);
+    if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (mem == GBCP_MEM_HOST || rc) return finish(c, rc);
+  return GBCP_OK;
+}
+
+int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, const double* f, const double* vpot,
+              int nstate, int mem) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  if (bad_mem(mem) || nstate < 0 || (nstate > 0 && (!c0 || !c2 || !f || !vpot || ldc < c.ngw || ldc2 < c.ngw)))
+    return set_err(h, GBCP_ERR_ARG, "vpsi: bad argument");
+  c.err.clear();
+  if (nstate == 0) return GBCP_OK;
+  const size_t nnr1 = (size_t)c.kr[0] * c.kr[1] * c.kr[2];
+  const cx<double>* dc0 = reinterpret_cast<const cx<double>*>(c0);
+  cx<double>* dc2 = reinterpret_cast<cx<double>*>(c2);
+  const double* df = f;
+  const double* dv = vpot;
+  int l0 = ldc, l2 = ldc2;
+  int rc = 0;
+  if (mem == GBCP_MEM_HOST) {
+    cx<double>* t0;
+    cx<double>* t2;
+    void* tf;
+    void* tv;
+    if ((rc = stage_in_cx(c, c.st_c0, c0, ldc, c.ngw, nstate, &t0))) return rc;
+    if ((rc = stage_in_cx(c, c.st_c2, c2, ldc2, c.ngw, nstate, &t2))) return rc;
+    if ((rc = stage_in(c, c.st_f, f, sizeof(double) * nstate, &tf))) return rc;
+    if ((rc = stage_in(c, c.st_vpot, vpot, sizeof(double) * nnr1, &tv))) return rc;
+    dc0 = t0;
+    dc2 = t2;
+    df = static_cast<double*>(tf);
+    dv = static_cast<double*>(tv);
+    l0 = l2 = c.ngw;
+  }
+  rc = gbcp::band_vpsi(c, dc0, l0, dc2, l2, df, dv, nstate);
+  if (!rc && mem == GBCP_MEM_HOST) rc = stage_out_cx(c, dc2, c2, ldc2, c.ngw, nstate);
+  if (mem == GBCP_MEM_HOST || rc) return finish(c, rc);
+  return GBCP_OK;
+}
+
+int gbcp_ortho(gbcp_ctx* h, double* c0, int ldc, int nstate, int method, double* scond, int mem) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  if (bad_mem(mem) || nstate < 0 || (nstate > 0 && (!c0 || ldc < c.ngw)) ||
+      (method != GBCP_ORTHO_GS && method != GBCP_ORTHO_LOWDIN))
+    return set_err(h, GBCP_ERR_ARG, "ortho: bad argument");
+  c.err.clear();
+  if (nstate == 0) return GBCP_OK;
+  cx<double>* dc0 = reinterpret_cast<cx<double>*>(c0);
+  int l0 = ldc;
+  int rc = 0;
+  if (mem == GBCP_MEM_HOST) {
+    if ((rc = stage_in_cx(c, c.st_c0, c0, ldc, c.ngw, nstate, &dc0))) return rc;
+    l0 = c.ngw;
+  }
+  rc = method == GBCP_ORTHO_GS ? gbcp::ortho_gs(c, dc0, l0, nstate, scond)
+                               : gbcp::ortho_lowdin(c, dc0, l0, nstate, scond);
+  if (!rc && mem == GBCP_MEM_HOST) rc = stage_out_cx(c, dc0, c0, ldc, c.ngw, nstate);
+  return finish(c, rc);
+}
+
+int gbcp_ovlap(gbcp_ctx* h, const double* c0, int ldc, int nstate, double* smat, int mem) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  if (bad_mem(mem) || nstate <= 0 || !c0 || !smat || ldc < c.ngw) return set_err(h, GBCP_ERR_ARG, "ovlap: bad argument");
+  c.err.clear();
+  const cx<double>* dc0 = reinterpret_cast<const cx<double>*>(c0);
+  int l0 = ldc;
+  double* dS = smat;
+  int rc = 0;
+  if (mem == GBCP_MEM_HOST) {
+    cx<double>* t;
+    if ((rc = stage_in_cx(c, c.st_c0, c0, ldc, c.ngw, nstate, &t))) return rc;
+    dc0 = t;
+    l0 = c.ngw;
+    if (!gbcp::ensure(c, c.st_misc, sizeof(double) * (size_t)nstate * nstate)) return GBCP_ERR_NOMEM;
+    dS = static_cast<double*>(c.st_misc.p);
+  }
+  rc = gbcp::ovlap_gamma(c, dc0, l0, nstate, dS);
+  if (!rc && mem == GBCP_MEM_HOST) {
+    cudaError_t e =
+        cudaMemcpyAsync(smat, dS, sizeof(double) * (size_t)nstate * nstate, cudaMemcpyDeviceToHost, c.stream);
+    if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (mem == GBCP_MEM_HOST || rc) return finish(c, rc);
+  return GBCP_OK;
+}
+
+static int fft_entry(gbcp_ctx* h, double* f, int mem, bool inv) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  if (bad_mem(mem) || !f) return set_err(h, GBCP_ERR_ARG, "fft: bad argument");
+  c.err.clear();
+  const size_t n = (size_t)c.kr[0] * c.kr[1] * c.nr[2];
+  cx<double>* d = reinterpret_cast<cx<double>*>(f);
+  int rc = 0;
+  if (mem == GBCP_MEM_HOST) {
+    void* t;
+    if ((rc = stage_in(c, c.st_misc2, f, sizeof(cx<double>) * n, &t))) return rc;
+    d = static_cast<cx<double>*>(t);
+  }
+  rc = gbcp::dense_fft(c, d, inv);
+  if (!rc && mem == GBCP_MEM_HOST) {
+    cudaError_t e = cudaMemcpyAsync(f, d, sizeof(cx<double>) * n, cudaMemcpyDeviceToHost, c.stream);
+    if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (mem == GBCP_MEM_HOST || rc) return finish(c, rc);
+  return GBCP_OK;
+}
+
+int gbcp_invfftn(gbcp_ctx* h, double* f, int mem) { return fft_entry(h, f, mem, true); }
+int gbcp_fwfftn(gbcp_ctx* h, double* f, int mem) { return fft_entry(h, f, mem, false); }
+
+int gbcp_rnlsm1(gbcp_ctx* h, const double* c0, int ldc, int nstate, int nat, int ngh, const int32_t* nghtol,
+                const double* twnl, const double* eigr, double* fnl, int mem) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  if (bad_mem(mem) || nstate <= 0 || nat <= 0 || ngh <= 0 || !c0 || !nghtol || !twnl || !eigr || !fnl ||
+      ldc < c.ngw)
+    return set_err(h, GBCP_ERR_ARG, "rnlsm1: bad argument");
+  c.err.clear();
+  const cx<double>* dc0 = reinterpret_cast<const cx<double>*>(c0);
+  const double* dtw = twnl;
+  const cx<double>* de = reinterpret_cast<const cx<double>*>(eigr);
+  double* dfnl = fnl;
+  int l0 = ldc;
+  int rc = 0;
+  const size_t nfnl = (size_t)nat * ngh * nstate;
+  if (mem == GBCP_MEM_HOST) {
+    cx<double>* t0;
+    void* t1;
+    void* t2;
+    if ((rc = stage_in_cx(c, c.st_c0, c0, ldc, c.ngw, nstate, &t0))) return rc;
+    if ((rc = stage_in(c, c.nl_b, twnl, sizeof(double) * (size_t)c.ngw * ngh, &t1))) return rc;
+    if ((rc = stage_in(c, c.nl_c, eigr, sizeof(cx<double>) * (size_t)c.ngw * nat, &t2))) return rc;
+    if (!gbcp::ensure(c, c.nl_d, sizeof(double) * nfnl)) return GBCP_ERR_NOMEM;
+    dc0 = t0;
+    dtw = static_cast<double*>(t1);
+    de = static_cast<cx<double>*>(t2);
+    dfnl = static_cast<double*>(c.nl_d.p);
+    l0 = c.ngw;
+  }
+  rc = gbcp::nl_rnlsm1(c, dc0, l0, nstate, nat, ngh, nghtol, dtw, de, dfnl);
+  if (!rc && mem == GBCP_MEM_HOST) {
+    cudaError_t e = cudaMemcpyAsync(fnl, dfnl, sizeof(double) * nfnl, cudaMemcpyDeviceToHost, c.stream);
+    if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (mem == GBCP_MEM_HOST || rc) return finish(c, rc);
+  return GBCP_OK;
+}
+
+int gbcp_fnonloc(gbcp_ctx* h, double* c2, int ldc2, int nstate, const double* f, int nat, int ngh,
+                 const int32_t* nghtol, const double* twnl, const double* eigr, const double* fnl, const double* wsg,
+                 int mem) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  if (bad_mem(mem) || nstate <= 0 || nat <= 0 || ngh <= 0 || !c2 || !f || !nghtol || !twnl || !eigr || !fnl ||
+      !wsg || ldc2 < c.ngw)
+    return set_err(h, GBCP_ERR_ARG, "fnonloc: bad argument");
+  c.err.clear();
+  cx<double>* dc2 = reinterpret_cast<cx<double>*>(c2);
+  const double* df = f;
+  const double* dtw = twnl;
+  const cx<double>* de = reinterpret_cast<const cx<double>*>(eigr);
+  const double* dfnl = fnl;
+  const double* dw = wsg;
+  int l2 = ldc2;
+  int rc = 0;
+  if (mem == GBCP_MEM_HOST) {
+    void *t1, *t2, *t3, *t4, *t5;
+    if ((rc = stage_in_cx(c, c.st_c2, c2, ldc2, c.ngw, nstate, &dc2))) return rc;
+    if ((rc = stage_in(c, c.st_f, f, sizeof(double) * nstate, &t1))) return rc;
+    if ((rc = stage_in(c, c.nl_b, twnl, sizeof(double) * (size_t)c.ngw * ngh, &t2))) return rc;
+    if ((rc = stage_in(c, c.nl_c, eigr, sizeof(cx<double>) * (size_t)c.ngw * nat, &t3))) return rc;
+    if ((rc = stage_in(c, c.nl_d, fnl, sizeof(double) * (size_t)nat * ngh * nstate, &t4))) return rc;
+    if ((rc = stage_in(c, c.st_misc, wsg, sizeof(double) * ngh, &t5))) return rc;
+    df = static_cast<double*>(t1);
+    dtw = static_cast<double*>(t2);
+    de = static_cast<cx<double>*>(t3);
+    dfnl = static_cast<double*>(t4);
+    dw = static_cast<double*>(t5);
+    l2 = c.ngw;
+  }
+  rc = gbcp::nl_fnonloc(c, dc2, l2, nstate, df, nat, ngh, nghtol, dtw, de, dfnl, dw);
+  if (!rc && mem == GBCP_MEM_HOST) rc = stage_out_cx(c, dc2, c2, ldc2, c.ngw, nstate);
+  if (mem == GBCP_MEM_HOST || rc) return finish(c, rc);
+  return GBCP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,148 @@
+// Internal context of the GB300 wavefunction hot path (not part of the ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "fft_core.cuh"
+
+namespace gbcp {
+
+extern std::atomic<long long> g_launches;
+inline void count_launch(int n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// Sphere geometry as seen by the pruned 3D FFT.
+//
+// Columns are the (gx, gy) pairs touched by the full wavefunction sphere
+// (+G and -G of every half-sphere vector), sorted by gx then gy; each column
+// holds the contiguous gz range [col_zlo, col_zlo + len) and its entries
+// col_ent = +(ig+1) for +G, -(ig+1) for -G, 0 for a hole.  A "slot" is one gx
+// value; its columns are consecutive and cover gy in [slot_gylo, +slot_ncol).
+struct GeoDev {
+  int n1, n2, n3;       // mesh
+  int k1, k2;           // leading dims of real-space arrays
+  int ngw;
+  int ncol, nslot, gxlo, nent;
+  const int* col_start;  // ncol+1
+  const int* col_zlo;    // ncol
+  const int* col_ent;    // nent
+  const int* col_slot;   // ncol
+  const int* col_gy;     // ncol
+  const int* ent_col;    // nent
+  const int* slot_col0;  // nslot
+  const int* slot_gylo;  // nslot
+  const int* slot_ncol;  // nslot
+  const int* pos_plus;   // ngw: entry position of +G
+  const int* pos_minus;  // ngw: entry position of -G
+  const double* hg;      // ngw
+};
+
+// Launch shape of one FFT stage: lines per CTA.
+struct StageTune {
+  int zl = 0, yl = 0, xl = 0;  // 0 = derive from target element count
+};
+
+struct Scratch {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+// Per-kernel event timers (the analogue of the reference's tiset/tihalt
+// timers, timer.mod.F90:39-130): when enabled, every launch is bracketed by
+// two events on the context stream; totals are folded on read.
+struct ProfRec {
+  const char* name;
+  cudaEvent_t a, b;
+};
+struct ProfAcc {
+  double ms = 0.0;
+  long long n = 0;
+};
+
+struct Ctx {
+  // grid
+  int nr[3], kr[3], ngw, geq0;
+  double omega, tpiba2;
+  int precision;
+  int batch;  // pairs per batch
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  // geometry
+  GeoDev geo{};
+  std::vector<void*> dev_allocs;  // geometry arrays
+  // fft plans and twiddles per axis
+  FftPlan plan[3];
+  cx<double>* tw64[3] = {nullptr, nullptr, nullptr};
+  cx<float>* tw32[3] = {nullptr, nullptr, nullptr};
+  StageTune tune;
+  // workspaces
+  Scratch zbuf, ybuf, qbuf;
+  Scratch st_c0, st_c2, st_rho, st_vpot, st_f, st_misc, st_misc2;
+  Scratch red;      // reductions
+  Scratch smat, smat2, smat3, sparts, cscr;
+  Scratch nl_a, nl_b, nl_c, nl_d;
+  int* d_info = nullptr;
+  std::string err;
+  // profiling
+  bool prof = false;
+  std::vector<ProfRec> prof_live;
+  std::vector<cudaEvent_t> prof_pool;
+  std::vector<std::pair<std::string, ProfAcc>> prof_acc;
+};
+
+// RAII launch timer; a no-op unless profiling is enabled on the context.
+struct ProfScope {
+  Ctx& c;
+  ProfRec r{};
+  bool on;
+  ProfScope(Ctx& ctx, const char* name);
+  ~ProfScope();
+};
+void prof_fold(Ctx& c);
+
+// grow-only scratch allocation; returns false on cudaMalloc failure
+bool ensure(Ctx& c, Scratch& s, size_t bytes);
+
+// ---- band loop (band.cu) ----
+int band_rhoofr(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho);
+int band_vpsi(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, const double* f, const double* vpot,
+              int nstate);
+int dense_fft(Ctx& c, cx<double>* grid, bool inv);
+int kin_energy(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* ekin, double* csumg);
+int rho_sum(Ctx& c, const double* rho, double* sum);
+
+// ---- linear algebra (linalg.cu) ----
+int ovlap_gamma(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S);
+int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host);
+int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host);
+
+// ---- projectors (nonlocal.cu) ----
+int nl_rnlsm1(Ctx& c, const cx<double>* c0, int ldc, int nstate, int nat, int ngh, const int* nghtol_host,
+              const double* twnl, const cx<double>* eigr, double* fnl);
+int nl_fnonloc(Ctx& c, cx<double>* c2, int ldc2, int nstate, const double* f, int nat, int ngh,
+               const int* nghtol_host, const double* twnl, const cx<double>* eigr, const double* fnl,
+               const double* wsg);
+
+}  // namespace gbcp
+
+#define GBCP_CUDA_TRY(ctx, expr)                                                   \
+  do {                                                                           \
+    cudaError_t e_ = (expr);                                                     \
+    if (e_ != cudaSuccess) {                                                     \
+      (ctx).err = std::string(#expr) + ": " + cudaGetErrorString(e_);           \
+      return 5;                                                                  \
+    }                                                                            \
+  } while (0)
+
+#define GBCP_LAUNCH_CHECK(ctx)                                                    \
+  do {                                                                           \
+    ::gbcp::count_launch();                                                      \
+    cudaError_t e_ = cudaGetLastError();                                         \
+    if (e_ != cudaSuccess) {                                                     \
+      (ctx).err = std::string("launch: ") + cudaGetErrorString(e_) + " at " + __FILE__ + ":" + std::to_string(__LINE__); \
+      return 5;                                                                  \
+    }                                                                            \
+  } while (0)

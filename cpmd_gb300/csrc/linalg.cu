@@ -1,0 +1,480 @@
+// Orthogonalisation of the Γ-point states (FP64 path).
+//
+// Reference: ortho -> rgs (rgs_utils.mod.F90:31-93): S = 2 C^T C - c0 c0^T
+// over the real view of C (dsyrk 'U','T' alpha=2 + dger -1), dpotrf/dtrtri
+// (uinv, l.95-162), C <- C U^{-1} (dtrmm R,U,N,N), zclean.
+// lowdin (lowdin_utils.mod.F90:58-89): the same S via csmat/ovlap, then
+// A = S^{-1/2} and C <- C A.
+//
+// GB300 form:
+//  * S: split-K tiled FP64 GEMM over the real view (K = 2 ngw), upper block
+//    triangle only, partial tiles folded by a second kernel that also applies
+//    the G=0 correction, mirrors the lower triangle and computes max|S-I|.
+//  * U and U^{-1}: one CTA, S resident in L2/L1 (n <= 1024 states).
+//  * S^{-1/2}: coupled Newton-Schulz iteration on GEMMs (Y -> S^{1/2},
+//    Z -> S^{-1/2}); mathematically the same matrix as Z w^{-1/2} Z^T from the
+//    reference's dspevy, reached without an eigensolver.
+//  * C <- C M: tiled FP64 GEMM (triangular skip for U^{-1}) into scratch,
+//    copied back with the zclean fused.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "ctx.h"
+
+namespace gbcp {
+
+namespace {
+
+constexpr int TS = 64;   // output tile
+constexpr int BK = 16;   // K step
+constexpr int NT = 256;  // threads (16 x 16, 4 x 4 outputs each)
+
+// Partial S over one K-chunk for one upper tile pair (bi <= bj).
+// A(k, i) = Ar[k + i*lda]  (real view of C, lda = 2*ldc, K = 2*ngw)
+__global__ void __launch_bounds__(NT) k_syrk_part(const double* __restrict__ Ar, int lda, int K, int n, int ntb,
+                                                  int kchunk, double* __restrict__ part) {
+  __shared__ double As[BK][TS + 1];
+  __shared__ double Bs[BK][TS + 1];
+  // decode tile pair from blockIdx.x over the upper triangle of ntb x ntb tiles
+  int t = blockIdx.x, bi = 0;
+  while (t >= ntb - bi) {
+    t -= ntb - bi;
+    ++bi;
+  }
+  const int bj = bi + t;
+  const int split = blockIdx.y;
+  const int k0 = split * kchunk, k1 = min(K, k0 + kchunk);
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double acc[4][4] = {};
+  const int i0 = bi * TS, j0 = bj * TS;
+  for (int kb = k0; kb < k1; kb += BK) {
+    // load 16 x 64 for both operands: thread -> (k = tid % 16, col = tid / 16 + 16 q)
+    for (int q = 0; q < 4; ++q) {
+      const int kk = threadIdx.x % 16, cc = threadIdx.x / 16 + 16 * q;
+      const int k = kb + kk;
+      const int ci = i0 + cc, cj = j0 + cc;
+      As[kk][cc] = (k < k1 && ci < n) ? Ar[k + (size_t)ci * lda] : 0.0;
+      Bs[kk][cc] = (k < k1 && cj < n) ? Ar[k + (size_t)cj * lda] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        a[u] = As[kk][ty + 16 * u];
+        b[u] = Bs[kk][tx + 16 * u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+  // part[split][i][j] (row-major n x n)
+  double* P = part + (size_t)split * n * n;
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int i = i0 + ty + 16 * u, j = j0 + tx + 16 * v;
+      if (i < n && j < n) P[(size_t)i * n + j] = acc[u][v];
+    }
+}
+
+// S[i][j] = 2 sum_split part - Re c0_i Re c0_j for the upper triangle tiles,
+// mirrored into the lower triangle.  Column-major == row-major (symmetric).
+__global__ void k_syrk_fold(const double* __restrict__ part, int nsplit, int n, int ntb, const double* __restrict__ Ar,
+                            int lda, int geq0, double* __restrict__ S, unsigned long long* __restrict__ scond_bits) {
+  const size_t nn = (size_t)n * n;
+  double mx = 0.0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nn; e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    const int bi = i / TS, bj = j / TS;
+    if (bi > bj) continue;  // lower block triangle handled by mirroring
+    double s = 0.0;
+    for (int p = 0; p < nsplit; ++p) s += part[(size_t)p * nn + e];
+    s *= 2.0;
+    if (geq0) s -= Ar[(size_t)i * lda] * Ar[(size_t)j * lda];
+    S[(size_t)i * n + j] = s;
+    S[(size_t)j * n + i] = s;
+    const double d = fabs(i == j ? s - 1.0 : s);
+    mx = fmax(mx, d);
+  }
+  if (scond_bits) {
+    // non-negative doubles order like their bit patterns
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(scond_bits, (unsigned long long)__double_as_longlong(mx));
+  }
+}
+
+// Cholesky S = U^T U (upper, row-major in place) then X = U^{-1} (upper).
+// One CTA; info = k+1 at the first non-positive pivot, -1 on NaN.
+__global__ void __launch_bounds__(1024) k_potrf_trtri(double* __restrict__ S, double* __restrict__ X, int n,
+                                                      int* __restrict__ info) {
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x == 0) {
+      const double d = S[(size_t)k * n + k];
+      if (!(d > 0.0)) bad = (d != d) ? -1 : k + 1;
+      else S[(size_t)k * n + k] = sqrt(d);
+    }
+    __syncthreads();
+    if (bad) break;
+    const double dk = S[(size_t)k * n + k];
+    for (int j = k + 1 + threadIdx.x; j < n; j += blockDim.x) S[(size_t)k * n + j] /= dk;
+    __syncthreads();
+    const int m = n - k - 1;
+    const long long tot = (long long)m * m;
+    for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
+      const int i = k + 1 + (int)(e / m), j = k + 1 + (int)(e % m);
+      if (j >= i) S[(size_t)i * n + j] -= S[(size_t)k * n + i] * S[(size_t)k * n + j];
+    }
+    __syncthreads();
+  }
+  if (bad) {
+    if (threadIdx.x == 0) *info = bad;
+    return;
+  }
+  // triangular inverse, one column per thread: X[i][j] = -(sum_{k=i+1..j} U[i][k] X[k][j]) / U[i][i]
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    for (int i = j + 1; i < n; ++i) X[(size_t)i * n + j] = 0.0;
+    X[(size_t)j * n + j] = 1.0 / S[(size_t)j * n + j];
+    for (int i = j - 1; i >= 0; --i) {
+      double s = 0.0;
+      for (int k = i + 1; k <= j; ++k) s = fma(S[(size_t)i * n + k], X[(size_t)k * n + j], s);
+      X[(size_t)i * n + j] = -s / S[(size_t)i * n + i];
+    }
+  }
+  if (threadIdx.x == 0) *info = 0;
+}
+
+// Cout = A * M.  A real view (rows = 2 ngw, lda), M (n x n) row-major (M[k][j]).
+// upper != 0: M is upper triangular, column block j only needs k <= j.
+__global__ void __launch_bounds__(NT) k_gemm_right(const double* __restrict__ A, int lda, int rows, int n,
+                                                   const double* __restrict__ M, int upper, double* __restrict__ Cout,
+                                                   int ldo) {
+  __shared__ double As[BK][TS + 1];
+  __shared__ double Ms[BK][TS + 1];
+  const int r0 = blockIdx.x * TS, j0 = blockIdx.y * TS;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double acc[4][4] = {};
+  const int kend = upper ? min(n, j0 + TS) : n;
+  for (int kb = 0; kb < kend; kb += BK) {
+    for (int q = 0; q < 4; ++q) {
+      // A tile: 64 rows x 16 k, coalesced along rows
+      const int rr = threadIdx.x % 64, kk = threadIdx.x / 64 + 4 * q;
+      const int r = r0 + rr, k = kb + kk;
+      As[kk][rr] = (r < rows && k < n) ? A[r + (size_t)k * lda] : 0.0;
+      // M tile: 16 k x 64 cols
+      const int cc = threadIdx.x % 64, km = threadIdx.x / 64 + 4 * q;
+      const int c = j0 + cc, k2 = kb + km;
+      Ms[km][cc] = (c < n && k2 < n) ? M[(size_t)k2 * n + c] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        a[u] = As[kk][tx + 16 * u];
+        b[u] = Ms[kk][ty + 16 * u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int r = r0 + tx + 16 * u, c = j0 + ty + 16 * v;
+      if (r < rows && c < n) Cout[r + (size_t)c * ldo] = acc[u][v];
+    }
+}
+
+// copy the real view back (ngw complex rows per state) and zero Im c(G=0)
+__global__ void k_copy_back(const double* __restrict__ src, int lds, double* __restrict__ dst, int ldd, int rows,
+                            int n, int geq0) {
+  const size_t tot = (size_t)rows * n;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(e % rows), c = (int)(e / rows);
+    double v = src[r + (size_t)c * lds];
+    if (geq0 && r == 1) v = 0.0;
+    dst[r + (size_t)c * ldd] = v;
+  }
+}
+
+// small dense n x n GEMM (row-major): C = alpha A B + beta C + gamma I
+__global__ void __launch_bounds__(NT) k_gemm_nn(const double* __restrict__ A, const double* __restrict__ B,
+                                                double* __restrict__ C, int n, double alpha, double beta,
+                                                double gamma) {
+  __shared__ double As[BK][TS + 1];
+  __shared__ double Bs[BK][TS + 1];
+  const int i0 = blockIdx.y * TS, j0 = blockIdx.x * TS;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double acc[4][4] = {};
+  for (int kb = 0; kb < n; kb += BK) {
+    for (int q = 0; q < 4; ++q) {
+      const int kk = threadIdx.x % 16, ii = threadIdx.x / 16 + 16 * q;
+      As[kk][ii] = (i0 + ii < n && kb + kk < n) ? A[(size_t)(i0 + ii) * n + kb + kk] : 0.0;
+      const int jj = threadIdx.x % 64, k2 = threadIdx.x / 64 + 4 * q;
+      Bs[k2][jj] = (j0 + jj < n && kb + k2 < n) ? B[(size_t)(kb + k2) * n + j0 + jj] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        a[u] = As[kk][ty + 16 * u];
+        b[u] = Bs[kk][tx + 16 * u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int i = i0 + ty + 16 * u, j = j0 + tx + 16 * v;
+      if (i < n && j < n) {
+        double r = alpha * acc[u][v];
+        if (beta != 0.0) r += beta * C[(size_t)i * n + j];
+        if (i == j) r += gamma;
+        C[(size_t)i * n + j] = r;
+      }
+    }
+}
+
+// Newton-Schulz set-up: alpha = max row sum |S| (>= lambda_max), Y = S/alpha, Z = I
+__global__ void k_ns_init(const double* __restrict__ S, int n, double* __restrict__ Y, double* __restrict__ Z,
+                          double* __restrict__ alpha_out) {
+  __shared__ double red[1024];
+  double mx = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < n; ++j) s += fabs(S[(size_t)i * n + j]);
+    mx = fmax(mx, s);
+  }
+  red[threadIdx.x] = mx;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  const double alpha = red[0];
+  for (size_t e = threadIdx.x; e < (size_t)n * n; e += blockDim.x) {
+    Y[e] = S[e] / alpha;
+    Z[e] = ((e / n) == (e % n)) ? 1.0 : 0.0;
+  }
+  if (threadIdx.x == 0) *alpha_out = alpha;
+}
+
+// max |T - I| over an n x n matrix (one CTA)
+__global__ void k_dev_from_identity(const double* __restrict__ T, int n, double* __restrict__ out) {
+  __shared__ double red[1024];
+  double mx = 0.0;
+  for (size_t e = threadIdx.x; e < (size_t)n * n; e += blockDim.x) {
+    const double d = T[e] - (((e / n) == (e % n)) ? 1.0 : 0.0);
+    mx = fmax(mx, fabs(d));
+  }
+  red[threadIdx.x] = mx;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+__global__ void k_scale(double* __restrict__ X, size_t n, const double* __restrict__ alpha, double power) {
+  const double s = pow(*alpha, power);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) X[e] *= s;
+}
+
+}  // namespace
+
+int ovlap_gamma_ex(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, double* scond_host) {
+  const int n = nstate;
+  const int K = 2 * c.ngw;
+  const int lda = 2 * ldc;
+  const int ntb = (n + TS - 1) / TS;
+  const int npairs = ntb * (ntb + 1) / 2;
+  // enough CTAs to fill the GPU: ~4 waves of 152 SMs
+  int nsplit = std::max(1, std::min(1024, (4 * 152 + npairs - 1) / npairs));
+  int kchunk = (K + nsplit - 1) / nsplit;
+  kchunk = ((kchunk + BK - 1) / BK) * BK;
+  nsplit = (K + kchunk - 1) / kchunk;
+  if (!ensure(c, c.sparts, sizeof(double) * (size_t)nsplit * n * n + 16)) return 6;
+  const double* Ar = reinterpret_cast<const double*>(c0);
+  double* part = static_cast<double*>(c.sparts.p);
+  {
+    ProfScope ps_(c, "k_syrk_part");
+    k_syrk_part<<<dim3(npairs, nsplit), NT, 0, c.stream>>>(Ar, lda, K, n, ntb, kchunk, part);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  unsigned long long* bits = reinterpret_cast<unsigned long long*>(part + (size_t)nsplit * n * n);
+  if (scond_host) GBCP_CUDA_TRY(c, cudaMemsetAsync(bits, 0, sizeof(unsigned long long), c.stream));
+  const int fb = std::max(1, std::min(1024, (n * n + 255) / 256));
+  {
+    ProfScope ps_(c, "k_syrk_fold");
+    k_syrk_fold<<<fb, 256, 0, c.stream>>>(part, nsplit, n, ntb, Ar, lda, c.geq0, S, scond_host ? bits : nullptr);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  if (scond_host) {
+    unsigned long long h = 0;
+    GBCP_CUDA_TRY(c, cudaMemcpyAsync(&h, bits, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
+    GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+    double d;
+    memcpy(&d, &h, sizeof(d));
+    *scond_host = d;
+  }
+  return 0;
+}
+
+int ovlap_gamma(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S) {
+  return ovlap_gamma_ex(c, c0, ldc, nstate, S, nullptr);
+}
+
+static int apply_right(Ctx& c, cx<double>* c0, int ldc, int nstate, const double* M, int upper) {
+  const int rows = 2 * c.ngw;
+  const int lda = 2 * ldc;
+  if (!ensure(c, c.cscr, sizeof(double) * (size_t)rows * nstate)) return 6;
+  double* tmp = static_cast<double*>(c.cscr.p);
+  dim3 grid((rows + TS - 1) / TS, (nstate + TS - 1) / TS);
+  {
+    ProfScope ps_(c, "k_gemm_right");
+    k_gemm_right<<<grid, NT, 0, c.stream>>>(reinterpret_cast<const double*>(c0), lda, rows, nstate, M, upper, tmp, rows);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  {
+    ProfScope ps_(c, "k_copy_back");
+    k_copy_back<<<1024, 256, 0, c.stream>>>(tmp, rows, reinterpret_cast<double*>(c0), lda, rows, nstate, c.geq0);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  return 0;
+}
+
+int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host) {
+  const int n = nstate;
+  if (n <= 0) return 0;
+  if (n > 4096) {
+    c.err = "ortho: nstate above 4096 not supported";
+    return 7;
+  }
+  if (!ensure(c, c.smat, sizeof(double) * (size_t)n * n) || !ensure(c, c.smat2, sizeof(double) * (size_t)n * n))
+    return 6;
+  double* S = static_cast<double*>(c.smat.p);
+  double* X = static_cast<double*>(c.smat2.p);
+  int rc = ovlap_gamma_ex(c, c0, ldc, n, S, scond_host);
+  if (rc) return rc;
+  {
+    ProfScope ps_(c, "k_potrf_trtri");
+    k_potrf_trtri<<<1, 1024, 0, c.stream>>>(S, X, n, c.d_info);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  rc = apply_right(c, c0, ldc, n, X, 1);
+  if (rc) return rc;
+  int info = 0;
+  GBCP_CUDA_TRY(c, cudaMemcpyAsync(&info, c.d_info, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  if (info > 0) {
+    c.err = "UINV: leading minor " + std::to_string(info) + " not positive definite (dpotrf)";
+    return 2;
+  }
+  if (info < 0) {
+    c.err = "UINV: non-finite overlap";
+    return 3;
+  }
+  return 0;
+}
+
+int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host) {
+  const int n = nstate;
+  if (n <= 0) return 0;
+  if (n > 4096) {
+    c.err = "ortho: nstate above 4096 not supported";
+    return 7;
+  }
+  const size_t nn = (size_t)n * n;
+  if (!ensure(c, c.smat, sizeof(double) * nn) || !ensure(c, c.smat2, sizeof(double) * nn * 3) ||
+      !ensure(c, c.smat3, sizeof(double) * (nn + 8)))
+    return 6;
+  double* S = static_cast<double*>(c.smat.p);
+  double* Y = static_cast<double*>(c.smat2.p);
+  double* Z = Y + nn;
+  double* T = Z + nn;
+  double* W = static_cast<double*>(c.smat3.p);
+  double* scal = W + nn;  // [0] alpha, [1] residual
+  int rc = ovlap_gamma_ex(c, c0, ldc, n, S, scond_host);
+  if (rc) return rc;
+  {
+    ProfScope ps_(c, "k_ns_init");
+    k_ns_init<<<1, 1024, 0, c.stream>>>(S, n, Y, Z, scal);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  dim3 grid((n + TS - 1) / TS, (n + TS - 1) / TS);
+  double prev = 1e300, res = 1e300;
+  bool ok = false;
+  for (int it = 0; it < 100; ++it) {
+    // T = (3 I - Z Y) / 2 ; Y <- Y T ; Z <- T Z
+    {
+      ProfScope ps_(c, "k_gemm_nn");
+      k_gemm_nn<<<grid, NT, 0, c.stream>>>(Z, Y, T, n, -0.5, 0.0, 1.5);
+      GBCP_LAUNCH_CHECK(c);
+    }
+    {
+      ProfScope ps_(c, "k_gemm_nn");
+      k_gemm_nn<<<grid, NT, 0, c.stream>>>(Y, T, W, n, 1.0, 0.0, 0.0);
+      GBCP_LAUNCH_CHECK(c);
+    }
+    std::swap(Y, W);
+    {
+      ProfScope ps_(c, "k_gemm_nn");
+      k_gemm_nn<<<grid, NT, 0, c.stream>>>(T, Z, W, n, 1.0, 0.0, 0.0);
+      GBCP_LAUNCH_CHECK(c);
+    }
+    std::swap(Z, W);
+    {
+      ProfScope ps_(c, "k_dev_from_identity");
+      k_dev_from_identity<<<1, 1024, 0, c.stream>>>(T, n, scal + 1);
+      GBCP_LAUNCH_CHECK(c);
+    }
+    GBCP_CUDA_TRY(c, cudaMemcpyAsync(&res, scal + 1, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+    if (!std::isfinite(res)) break;
+    // quadratic convergence ends at rounding level: stop when T = I to ~n eps
+    // or when the deviation no longer drops
+    if (res < 1e-15 * std::max(1, n / 16) || (res < 1e-10 && res >= prev)) {
+      ok = true;
+      break;
+    }
+    prev = res;
+  }
+  if (!ok) {
+    c.err = "lowdin: Newton-Schulz iteration for S^-1/2 did not converge (S ill-conditioned or not SPD)";
+    return std::isfinite(res) ? 8 : 3;
+  }
+  // A = Z / sqrt(alpha)
+  {
+    ProfScope ps_(c, "k_scale");
+    k_scale<<<256, 256, 0, c.stream>>>(Z, nn, scal, -0.5);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  return apply_right(c, c0, ldc, n, Z, 0);
+}
+
+}  // namespace gbcp

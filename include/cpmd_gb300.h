@@ -1,0 +1,144 @@
+/*
+ * cpmd_gb300.h -- C ABI of the GB300-native CPMD wavefunction hot path.
+ *
+ * Every entry point replaces one CPMD Fortran routine of the Γ-point,
+ * norm-conserving band loop; a Fortran caller binds them with
+ * ISO_C_BINDING exactly like src/cuuser_interfaces.mod.F90:41-201 binds
+ * CuUser_C_* (pointers as TYPE(C_PTR) by value, integers by value).
+ *
+ * Conventions
+ *  - Complex arrays are interleaved (re, im) FP64, i.e. COMPLEX(real_8),
+ *    column-major with an explicit leading dimension (in complex elements).
+ *  - Real-space arrays (rhoe, vpot) use the reference's padded layout
+ *    (kr1, kr2, kr3) with x fastest (fpar%kr1, kr2s, kr3s; kr = nr + mod(nr+1,2)),
+ *    loadpa_utils.mod.F90:509-525, loadpa_utils.mod.F90:432.
+ *  - `mem` says where ALL array arguments of a call live:
+ *    GBCP_MEM_HOST   -> the call stages through device buffers owned by the
+ *                       context and synchronises before returning;
+ *    GBCP_MEM_DEVICE -> pointers are device pointers; work is queued on the
+ *                       context's stream; the call synchronises only when it
+ *                       returns host scalars (non-NULL scalar outputs).
+ *  - Every call returns a status (GBCP_OK = 0).  The reference aborts through
+ *    stopgm (error_handling.mod.F90:11-53); here the caller decides.
+ *  - A context is not thread-safe; use one per host thread / stream.
+ */
+#ifndef CPMD_GB300_H
+#define CPMD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gbcp_ctx gbcp_ctx;
+
+enum gbcp_status {
+  GBCP_OK = 0,
+  GBCP_ERR_ARG = 1,        /* bad argument (NULL, size, layout) */
+  GBCP_ERR_NOT_SPD = 2,    /* overlap matrix not positive definite (rgs_utils.mod.F90:127-155) */
+  GBCP_ERR_NONFINITE = 3,  /* NaN/Inf detected in an input or a reduction */
+  GBCP_ERR_TIMEOUT = 4,    /* a bounded device-side wait expired */
+  GBCP_ERR_CUDA = 5,       /* CUDA runtime error */
+  GBCP_ERR_NOMEM = 6,      /* device allocation failed */
+  GBCP_ERR_UNSUPPORTED = 7,/* mesh size / option not supported */
+  GBCP_ERR_NOT_CONVERGED = 8 /* iterative Loewdin step did not converge */
+};
+
+enum gbcp_precision {
+  GBCP_PREC_FP64 = 0,  /* plain FP64 drop-in */
+  GBCP_PREC_MIXED = 1  /* FP32 FFT and V*psi, FP64 reductions and accumulation */
+};
+
+enum gbcp_mem { GBCP_MEM_HOST = 0, GBCP_MEM_DEVICE = 1 };
+
+enum gbcp_ortho_method {
+  GBCP_ORTHO_GS = 0,     /* rgs: Cholesky Gram-Schmidt (ortho_utils.mod.F90:256) */
+  GBCP_ORTHO_LOWDIN = 1  /* lowdin (ortho_utils.mod.F90:193) */
+};
+
+/* Grid and basis description: the module globals the reference hot path reads
+ * (system.mod: spar%nr*s, fpar%kr*, ncpw%ngw, parm%omega, parm%tpiba2, geq0;
+ * cppt: inyh, hg). */
+typedef struct gbcp_grid_desc {
+  int32_t nr1, nr2, nr3;  /* FFT mesh */
+  int32_t kr1, kr2, kr3;  /* leading dimensions of real-space arrays */
+  int32_t ngw;            /* wavefunction half-sphere size */
+  int32_t geq0;           /* 1 if entry 0 is G = 0 */
+  double omega;           /* cell volume (bohr^3) */
+  double tpiba2;          /* (2 pi / alat)^2 */
+  const int32_t* inyh;    /* (3, ngw) Fortran order: Miller index + nr/2 + 1 (cppt::inyh) */
+  const double* hg;       /* (ngw) |G|^2 in tpiba2 units (cppt::hg) */
+} gbcp_grid_desc;
+
+/* Context creation: builds the sphere/column maps, FFT plans and twiddles
+ * once (the reference's fft_init/setfftn, fftprp_utils.mod.F90:65-95,
+ * fftnew_utils.mod.F90:101-170).  `stream` is a cudaStream_t or NULL (the
+ * context then creates its own).  `max_batch` is the number of state pairs
+ * transformed per launch (0 = default). */
+int gbcp_ctx_create(const gbcp_grid_desc* grid, int precision, int max_batch, void* stream, gbcp_ctx** out);
+int gbcp_ctx_destroy(gbcp_ctx* ctx);
+int gbcp_set_precision(gbcp_ctx* ctx, int precision);
+int gbcp_synchronize(gbcp_ctx* ctx);
+/* Last error message of this context (NUL-terminated, truncated to len). */
+int gbcp_last_error(gbcp_ctx* ctx, char* buf, int len);
+/* Number of kernels this library has launched in this process (all contexts). */
+int64_t gbcp_kernel_launches(void);
+
+/* Per-kernel timers, the counterpart of the reference's tiset/tihalt wall-clock
+ * table (timer.mod.F90:39-130) and NVTX ranges (cpmd_global.h:93-98).
+ * enable != 0 clears the table and brackets every later launch with CUDA
+ * events on the context stream; gbcp_profile_read synchronises, then returns
+ * entry `idx` (name, total milliseconds, launch count) or GBCP_ERR_ARG past
+ * the last entry. */
+int gbcp_profile_enable(gbcp_ctx* ctx, int enable);
+int gbcp_profile_read(gbcp_ctx* ctx, int idx, char* name, int name_len, double* total_ms, int64_t* count);
+
+/* rhoofr(c0, rhoe, psi, nstate)            rhoofr_utils.mod.F90:122-644
+ * rhoe(kr1,kr2,kr3) = sum_i f_i/omega psi_i(r)^2 (zero in the padding);
+ * ekin = tpiba2 sum_i f_i sum_G hg |c|^2 (kin_energy_utils.mod.F90:93-108);
+ * csumg = sum_i f_i <c_i|c_i>; csumr = sum_r rhoe * omega / (nr1 nr2 nr3)
+ * (rhoofr_utils.mod.F90:607-635).  Scalar outputs may be NULL. */
+int gbcp_rhoofr(gbcp_ctx* ctx, const double* c0, int ldc, int nstate, const double* f, double* rhoe,
+                double* ekin, double* csumg, double* csumr, int mem);
+
+/* vpsi(c0, c2, f, vpot, psi, nstate, ...)  vpsi_utils.mod.F90:120-732 (Γ branch 661-671)
+ * c2 += -f/2 (tpiba2 hg c0 + FFT[V psi]) per state (add_wfn, l.717). */
+int gbcp_vpsi(gbcp_ctx* ctx, const double* c0, int ldc, double* c2, int ldc2, const double* f,
+              const double* vpot, int nstate, int mem);
+
+/* ortho(nstate, c0, cscr)                  ortho_utils.mod.F90:124-272
+ * In-place orthonormalisation in the Γ metric, then zclean.  `scond` (may be
+ * NULL) receives max|S - I| of the input overlap (csmat_utils.mod.F90:82-89). */
+int gbcp_ortho(gbcp_ctx* ctx, double* c0, int ldc, int nstate, int method, double* scond, int mem);
+
+/* Overlap matrix only: S = 2 Re(C^H C) - Re c(0) Re c(0)^T, full n x n
+ * column-major (ovlap_utils.mod.F90:150-165, symmetric branch). */
+int gbcp_ovlap(gbcp_ctx* ctx, const double* c0, int ldc, int nstate, double* smat, int mem);
+
+/* invfftn / fwfftn                          fftmain_utils.mod.F90:373-431
+ * Dense in-place 3D FFT of a complex grid laid out (kr1, kr2, nr3), x fastest,
+ * G stored at FFT index (g mod nr).  inv: e^{+iGr}, unscaled;
+ * fw: e^{-iGr}, scaled 1/(nr1 nr2 nr3). */
+int gbcp_invfftn(gbcp_ctx* ctx, double* f, int mem);
+int gbcp_fwfftn(gbcp_ctx* ctx, double* f, int mem);
+
+/* rnlsm(c0, nstate, ...) -> rnlsm1         rnlsm1_utils.mod.F90:42-193
+ * One species of nat atoms with ngh projectors of angular momentum nghtol[iv]:
+ * fnl(nat, ngh, nstate) = 2 Re sum_G conj((-i)^l twnl(G,iv) eigr(G,ia)) c(G),
+ * with the G = 0 term halved.  twnl(ngw, ngh) real, eigr(ngw, nat) complex. */
+int gbcp_rnlsm1(gbcp_ctx* ctx, const double* c0, int ldc, int nstate, int nat, int ngh, const int32_t* nghtol,
+                const double* twnl, const double* eigr, double* fnl, int mem);
+
+/* fnonloc(c2, f, nstate, ...)               fnonloc_utils.mod.F90:306-354 (BHS/KB branch)
+ * c2(G,i) += sum_iv twnl(G,iv) (-i)^l (-f_i wsg(iv)) sum_ia eigr(G,ia) fnl(ia,iv,i),
+ * f_i < 1e-5 counted as 1. */
+int gbcp_fnonloc(gbcp_ctx* ctx, double* c2, int ldc2, int nstate, const double* f, int nat, int ngh,
+                 const int32_t* nghtol, const double* twnl, const double* eigr, const double* fnl,
+                 const double* wsg, int mem);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CPMD_GB300_H */
