@@ -165,6 +165,19 @@ class Context:
         if rc != 0:
             raise GbcpError(fn, rc, self.last_error())
 
+    def _prep(self, *arrs) -> int:
+        """Memory kind of a call; device calls are queued on torch's current
+        stream so they order with the caller's torch work."""
+        mem = _mem(*arrs)
+        if mem == MEM_DEVICE:
+            import torch
+            # handle 0 is the legacy default stream: pass cudaStreamLegacy (0x1)
+            s = torch.cuda.current_stream().cuda_stream or 1
+        else:
+            s = None
+        self._check("gbcp_set_stream", self.lib.gbcp_set_stream(self.h, C.c_void_p(s) if s else None))
+        return mem
+
     # -- hot path ------------------------------------------------------------
     def rhoofr(self, c0, f, rhoe=None, energies: bool = True):
         """Density (padded layout) and, if ``energies``, (ekin, csumg, csumr)."""
@@ -175,7 +188,7 @@ class Context:
                 rhoe = torch.empty(self.kr[::-1], dtype=torch.float64, device=c0.device)
             else:
                 rhoe = np.empty(self.kr[::-1])
-        mem = _mem(c0, f, rhoe)
+        mem = self._prep(c0, f, rhoe)
         ek, cg, cr = C.c_double(), C.c_double(), C.c_double()
         refs = (C.byref(ek), C.byref(cg), C.byref(cr)) if energies else (None, None, None)
         self._check("gbcp_rhoofr", self.lib.gbcp_rhoofr(self.h, _ptr(c0), ldc, n, _ptr(f), _ptr(rhoe), *refs, mem))
@@ -189,7 +202,7 @@ class Context:
         ld2, n2 = _ld_wfn(c2, self.ngw)
         if n2 != n:
             raise ValueError("c0 and c2 state counts differ")
-        mem = _mem(c0, c2, f, vpot)
+        mem = self._prep(c0, c2, f, vpot)
         self._check("gbcp_vpsi", self.lib.gbcp_vpsi(self.h, _ptr(c0), ldc, _ptr(c2), ld2, _ptr(f), _ptr(vpot), n, mem))
         return c2
 
@@ -197,7 +210,7 @@ class Context:
         """Orthonormalise c0 in place; returns scond = max|S - I| of the input."""
         ldc, n = _ld_wfn(c0, self.ngw)
         sc = C.c_double()
-        self._check("gbcp_ortho", self.lib.gbcp_ortho(self.h, _ptr(c0), ldc, n, ORTHO[method], C.byref(sc), _mem(c0)))
+        self._check("gbcp_ortho", self.lib.gbcp_ortho(self.h, _ptr(c0), ldc, n, ORTHO[method], C.byref(sc), self._prep(c0)))
         return sc.value
 
     def ovlap(self, c0, smat=None):
@@ -208,16 +221,16 @@ class Context:
                 smat = torch.empty((n, n), dtype=torch.float64, device=c0.device)
             else:
                 smat = np.empty((n, n))
-        self._check("gbcp_ovlap", self.lib.gbcp_ovlap(self.h, _ptr(c0), ldc, n, _ptr(smat), _mem(c0, smat)))
+        self._check("gbcp_ovlap", self.lib.gbcp_ovlap(self.h, _ptr(c0), ldc, n, _ptr(smat), self._prep(c0, smat)))
         return smat
 
     def invfftn(self, grid):
         """In-place inverse 3D FFT of a complex grid shaped (nr3, kr2, kr1)."""
-        self._check("gbcp_invfftn", self.lib.gbcp_invfftn(self.h, _ptr(grid), _mem(grid)))
+        self._check("gbcp_invfftn", self.lib.gbcp_invfftn(self.h, _ptr(grid), self._prep(grid)))
         return grid
 
     def fwfftn(self, grid):
-        self._check("gbcp_fwfftn", self.lib.gbcp_fwfftn(self.h, _ptr(grid), _mem(grid)))
+        self._check("gbcp_fwfftn", self.lib.gbcp_fwfftn(self.h, _ptr(grid), self._prep(grid)))
         return grid
 
     def rnlsm(self, c0, twnl, eigr, nghtol, fnl=None):
@@ -232,7 +245,7 @@ class Context:
                 fnl = torch.empty((n, ngh, nat), dtype=torch.float64, device=c0.device)
             else:
                 fnl = np.empty((n, ngh, nat))
-        mem = _mem(c0, twnl, eigr, fnl)
+        mem = self._prep(c0, twnl, eigr, fnl)
         self._check("gbcp_rnlsm1", self.lib.gbcp_rnlsm1(self.h, _ptr(c0), ldc, n, nat, ngh, _ptr(nt), _ptr(twnl),
                                                         _ptr(eigr), _ptr(fnl), mem))
         return fnl
@@ -242,7 +255,7 @@ class Context:
         ngh = int(len(nghtol))
         nat = int(eigr.shape[1] if not _is_torch(eigr) else eigr.shape[0])
         nt = np.ascontiguousarray(np.asarray(nghtol, dtype=np.int32))
-        mem = _mem(c2, f, fnl, twnl, eigr, wsg)
+        mem = self._prep(c2, f, fnl, twnl, eigr, wsg)
         self._check("gbcp_fnonloc", self.lib.gbcp_fnonloc(self.h, _ptr(c2), ld2, n, _ptr(f), nat, ngh, _ptr(nt),
                                                           _ptr(twnl), _ptr(eigr), _ptr(fnl), _ptr(wsg), mem))
         return c2

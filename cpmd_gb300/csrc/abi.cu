@@ -300,15 +300,11 @@ int gbcp_ctx_create(const gbcp_grid_desc* grid, int precision, int max_batch, vo
   c.tpiba2 = grid->tpiba2;
   c.precision = precision;
   c.batch = max_batch > 0 ? max_batch : 8;
-  if (stream) {
-    c.stream = static_cast<cudaStream_t>(stream);
-  } else {
-    if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) {
-      delete h;
-      return GBCP_ERR_CUDA;
-    }
-    c.own_stream = true;
+  if (cudaStreamCreateWithFlags(&c.own, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return GBCP_ERR_CUDA;
   }
+  c.stream = stream ? static_cast<cudaStream_t>(stream) : c.own;
   int rc = gbcp::build_geometry(c, grid->inyh, grid->hg);
   if (!rc) rc = gbcp::build_fft(c);
   if (!rc && cudaMalloc(&c.d_info, 16) != cudaSuccess) rc = GBCP_ERR_NOMEM;
@@ -333,7 +329,10 @@ int gbcp_ctx_destroy(gbcp_ctx* h) {
   if (c.d_info) cudaFree(c.d_info);
   gbcp::prof_fold(c);
   for (cudaEvent_t e : c.prof_pool) cudaEventDestroy(e);
-  if (c.own_stream && c.stream) cudaStreamDestroy(c.stream);
+  if (c.own) {
+    cudaStreamSynchronize(c.own);
+    cudaStreamDestroy(c.own);
+  }
   delete h;
   return GBCP_OK;
 }
@@ -341,6 +340,16 @@ int gbcp_ctx_destroy(gbcp_ctx* h) {
 int gbcp_set_precision(gbcp_ctx* h, int precision) {
   if (!h || (precision != GBCP_PREC_FP64 && precision != GBCP_PREC_MIXED)) return GBCP_ERR_ARG;
   h->c.precision = precision;
+  return GBCP_OK;
+}
+
+int gbcp_set_stream(gbcp_ctx* h, void* stream) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c.own;
+  if (s == c.stream) return GBCP_OK;
+  gbcp::prof_fold(c);
+  c.stream = s;
   return GBCP_OK;
 }
 

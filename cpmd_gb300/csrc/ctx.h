@@ -68,8 +68,8 @@ struct Ctx {
   double omega, tpiba2;
   int precision;
   int batch;  // pairs per batch
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
+  cudaStream_t stream = nullptr;  // stream all work is queued on
+  cudaStream_t own = nullptr;     // the context's own stream
   // geometry
   GeoDev geo{};
   std::vector<void*> dev_allocs;  // geometry arrays

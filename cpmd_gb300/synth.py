@@ -29,13 +29,14 @@ DIAMOND = np.array([
     [0.25, 0.25, 0.25], [0.25, 0.75, 0.75], [0.75, 0.25, 0.75], [0.75, 0.75, 0.25],
 ])
 
-# configurations of the wavefunction hot path (cell edge for the 8-atom cell,
-# supercell repeat, states, cut-off, mesh, jitter)
+# configurations of the wavefunction hot path: edge of the 8-atom diamond
+# cell (the supercell edge is alat * rep), supercell repeat, states, cut-off
+# (Ry), mesh, jitter (bohr)
 CONFIGS = {
-    "c0": dict(alat=10.26, rep=1, nstate=16, ecut=20.0, nr=32, jitter=0.0),
-    "c1": dict(alat=20.52, rep=2, nstate=128, ecut=70.0, nr=120, jitter=0.05),
-    "c2": dict(alat=30.78, rep=3, nstate=432, ecut=50.0, nr=144, jitter=0.1),
-    "c4": dict(alat=41.04, rep=4, nstate=1024, ecut=70.0, nr=240, jitter=0.05, nproj=8),
+    "c0": dict(alat=10.26, rep=1, nstate=16, ecut=20.0, nr=32, jitter=0.0),     # L = 10.26
+    "c1": dict(alat=10.26, rep=2, nstate=128, ecut=70.0, nr=120, jitter=0.05),  # L = 20.52
+    "c2": dict(alat=10.26, rep=3, nstate=432, ecut=50.0, nr=144, jitter=0.1),   # L = 30.78
+    "c4": dict(alat=10.26, rep=4, nstate=1024, ecut=70.0, nr=240, jitter=0.05, nproj=8),  # L = 41.04
 }
 
 

@@ -79,6 +79,11 @@ typedef struct gbcp_grid_desc {
 int gbcp_ctx_create(const gbcp_grid_desc* grid, int precision, int max_batch, void* stream, gbcp_ctx** out);
 int gbcp_ctx_destroy(gbcp_ctx* ctx);
 int gbcp_set_precision(gbcp_ctx* ctx, int precision);
+/* Queue later work on `stream` (a cudaStream_t; NULL = the context's own
+ * stream; the CUDA legacy default stream is cudaStreamLegacy).  Device-pointer calls are ordered only with respect to this stream,
+ * as the reference's GPU path orders work on its thread's stream
+ * (thread_view, vpsi_utils.mod.F90:295). */
+int gbcp_set_stream(gbcp_ctx* ctx, void* stream);
 int gbcp_synchronize(gbcp_ctx* ctx);
 /* Last error message of this context (NUL-terminated, truncated to len). */
 int gbcp_last_error(gbcp_ctx* ctx, char* buf, int len);
