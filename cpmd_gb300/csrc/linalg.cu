@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "ctx.h"
@@ -478,3 +479,76 @@ int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host
 }
 
 }  // namespace gbcp
+
+// ---------------------------------------------------------------------------
+// Allocation-free overlap matrix: gbcp_ovlap_noalloc.
+//
+// Some callers of this library cannot call cudaMalloc: an application whose
+// device memory is owned by its own pool allocator (every byte handed out by
+// that pool), or a time-stepping loop that must not stall every stream on the
+// device with the implicit synchronisation an allocation brings.  For them
+// this entry point computes the same Γ-point overlap matrix as gbcp_ovlap but
+// allocates nothing: the caller passes device pointers for the wavefunctions
+// and the result, and the split-K partial sums live in the fixed device array
+// below.  That array (8 MiB, room for nsplit * nstate^2 <= 2^20 doubles, so
+// nstate <= 1024) is part of the library image: every GPU that loads the
+// library holds it until the process exits.  All calls share it and it keeps
+// the last call's contents; the kernels overwrite every partial they later
+// read, so nothing needs clearing.  Calls whose work overlaps on the GPU
+// (different streams, or several host threads) race on the array.
+namespace gbcp {
+
+static __device__ __align__(256) double g_noalloc_scratch[size_t(1) << 20];
+
+namespace {
+constexpr size_t kNoAllocDoubles = size_t(1) << 20;
+constexpr int kNoAllocMaxDevices = 64;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+std::mutex g_noalloc_mu;
+
+// Device address of the scratch array for the current device.  The host-side
+// name g_noalloc_scratch is only a stand-in for the symbol, not a device
+// address, so it is resolved once per device with cudaGetSymbolAddress.
+int noalloc_scratch(double** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return 5;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return 5;
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return 0;
+}
+}  // namespace
+
+}  // namespace gbcp
+
+extern "C" int gbcp_ovlap_noalloc(const double* c0, int ldc, int ngw, int nstate, int geq0, double* smat,
+                                  void* stream) {
+  using namespace gbcp;
+  if (!c0 || !smat || ngw < 1 || ldc < ngw || nstate < 1) return 1;
+  const int n = nstate;
+  const size_t nn = (size_t)n * n;
+  if (nn > kNoAllocDoubles) return 1;  // nstate above 1024
+  double* scratch = nullptr;
+  if (noalloc_scratch(&scratch)) return 5;
+  const int K = 2 * ngw, lda = 2 * ldc;
+  const int ntb = (n + TS - 1) / TS;
+  const int npairs = ntb * (ntb + 1) / 2;
+  int nsplit = std::max(1, std::min(1024, (4 * 152 + npairs - 1) / npairs));
+  nsplit = std::max(1, std::min(nsplit, (int)(kNoAllocDoubles / nn)));
+  int kchunk = (K + nsplit - 1) / nsplit;
+  kchunk = ((kchunk + BK - 1) / BK) * BK;
+  nsplit = (K + kchunk - 1) / kchunk;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  k_syrk_part<<<dim3(npairs, nsplit), NT, 0, st>>>(c0, lda, K, n, ntb, kchunk, scratch);
+  count_launch();
+  if (cudaGetLastError() != cudaSuccess) return 5;
+  const int fb = std::max(1, std::min(1024, (int)((nn + 255) / 256)));
+  k_syrk_fold<<<fb, 256, 0, st>>>(scratch, nsplit, n, ntb, c0, lda, geq0 ? 1 : 0, smat, nullptr);
+  count_launch();
+  if (cudaGetLastError() != cudaSuccess) return 5;
+  return 0;
+}

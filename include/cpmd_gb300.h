@@ -121,6 +121,22 @@ int gbcp_ortho(gbcp_ctx* ctx, double* c0, int ldc, int nstate, int method, doubl
  * column-major (ovlap_utils.mod.F90:150-165, symmetric branch). */
 int gbcp_ovlap(gbcp_ctx* ctx, const double* c0, int ldc, int nstate, double* smat, int mem);
 
+/* Allocation-free overlap matrix.  No counterpart in the reference: it exists
+ * for callers that cannot call cudaMalloc (an application whose device memory
+ * is all owned by its own pool allocator, or a time-stepping loop that must
+ * not stall the device with an allocation's implicit synchronisation).  Same
+ * S as gbcp_ovlap, from device pointers only, queued on `stream` (a
+ * cudaStream_t; NULL = the legacy default stream); needs no context.
+ * It calls no cudaMalloc/cudaFree: its split-K partial sums live in a fixed
+ * 8 MiB device array inside the library (held by every GPU that loads the
+ * library until the process exits), so nstate <= 1024 (GBCP_ERR_ARG above).
+ * The first call on each device, with that device current, looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture.  All calls share the array: calls whose work overlaps on
+ * the GPU race.  c0: device, complex, leading dimension ldc >= ngw;
+ * smat: device, nstate x nstate. */
+int gbcp_ovlap_noalloc(const double* c0, int ldc, int ngw, int nstate, int geq0, double* smat, void* stream);
+
 /* invfftn / fwfftn                          fftmain_utils.mod.F90:373-431
  * Dense in-place 3D FFT of a complex grid laid out (kr1, kr2, nr3), x fastest,
  * G stored at FFT index (g mod nr).  inv: e^{+iGr}, unscaled;
