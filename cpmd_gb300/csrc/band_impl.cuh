@@ -1,0 +1,496 @@
+// Band loop of the Γ-point hot path: rhoofr and vpsi as a pruned 3D FFT.
+//
+// Reference data flow (rhoofr_utils.mod.F90:305-409, vpsi_utils.mod.F90:376-675):
+// for each pair of states, pack c1 + i c2 on the sphere (state_utils.mod.F90:
+// 165-189), inverse 3D FFT (fftmain_utils.mod.F90:90-104), accumulate density
+// or multiply by V and transform forward (l.122-136), decode.
+//
+// GB300 data flow per batch of pairs (one launch per stage, all pairs of the
+// batch in the grid):
+//   Z stage  gather the sphere column (gx,gy) straight from c0, FFT along z
+//            -> zbuf[pair][z][col]            (only sphere columns exist)
+//   Y stage  per z-plane and gx slot, FFT along y
+//            -> ybuf[pair][z][y][slot]        (only |gx| inside the sphere)
+//   X stage  per (y,z) line, FFT along x, then
+//            rhoofr: rho += f1/omega Re^2 + f2/omega Im^2 (registers, all pairs)
+//            vpsi:   x V(r), forward FFT along x, keep the sphere slots
+// and for vpsi the mirror Y and Z stages forward, then a decode kernel that
+// forms fp/fm from +G/-G and adds the kinetic term into c2.
+// psi(r) never reaches HBM.  The all-to-all of the reference
+// (fftutil_utils.mod.F90:292-319) becomes the layout change between stages.
+//
+// Every stage kernel is a template on the precision T and on NC, the length
+// of the axis it transforms: NC > 0 selects the compile-time plan of
+// fft_ct.cuh (all index arithmetic constant), NC = 0 the run-time plan.
+// This header is included by band64.cu and band32.cu, one per precision.
+#pragma once
+#include <algorithm>
+#include <cmath>
+
+#include "ctx.h"
+#include "fft_ct.cuh"
+
+namespace gbcp {
+namespace band {
+
+constexpr int kThreads = 256;
+constexpr int kElems = 2048;   // complex elements per CTA tile (lines * length)
+constexpr int kMaxAcc = 16;    // density accumulators per thread (run-time plan)
+
+__host__ __device__ constexpr int line_stride(int n) { return (n % 2 == 0) ? n + 1 : n; }
+__host__ __device__ constexpr int ct_lines(int n) { return (kElems / n) > 0 ? (kElems / n) : 1; }
+__device__ __forceinline__ int freq_of(int i, int n) { return (i < (n + 1) / 2) ? i : i - n; }
+__device__ __forceinline__ int idx_of(int g, int n) { return g < 0 ? g + n : g; }
+
+template <typename T>
+__device__ __forceinline__ void load_tw(cx<T>* tw, const cx<T>* __restrict__ twg, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = twg[i];
+}
+
+template <bool INV, typename T, int NC>
+__device__ __forceinline__ cx<T>* run_fft(cx<T>* a, cx<T>* b, int nl, int ls, const FftPlan& p,
+                                          const cx<T>* tw) {
+  if constexpr (NC > 0) {
+    return fft_ct<INV, T, NC, ct_lines(NC), kThreads>(a, b, tw);
+  } else {
+    return fft_lines<INV>(a, b, nl, ls, p, tw);
+  }
+}
+
+// stage geometry: length N, line stride LS, lines per CTA NL
+#define GBCP_STAGE(NAXIS, NLRT)                                   \
+  const int N = (NC > 0) ? NC : (NAXIS);                          \
+  const int ls = (NC > 0) ? line_stride(NC) : line_stride(N);     \
+  const int nl = (NC > 0) ? ct_lines(NC) : (NLRT);                \
+  extern __shared__ __align__(16) unsigned char smem_raw[];       \
+  cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);                 \
+  cx<T>* a = tw + N;                                              \
+  cx<T>* b = a + nl * ls;
+
+// ---------------------------------------------------------------- Z stage (inverse, gather)
+template <typename T, int NC>
+__global__ void __launch_bounds__(kThreads) k_zinv(GeoDev g, FftPlan p, const cx<double>* __restrict__ c0, int ldc,
+                                                  int s0, int nstate, int nlrt, cx<T>* __restrict__ zbuf,
+                                                  const cx<T>* __restrict__ twg) {
+  GBCP_STAGE(g.n3, nlrt)
+  const int pair = blockIdx.y;
+  const int col0 = blockIdx.x * nl;
+  const int is1 = s0 + 2 * pair, is2 = is1 + 1;
+  const bool two = is2 < nstate;
+  const cx<double>* c1 = c0 + (size_t)is1 * ldc;
+  const cx<double>* c2 = c0 + (size_t)(two ? is2 : is1) * ldc;
+  load_tw(tw, twg, N);
+  for (int idx = threadIdx.x; idx < nl * N; idx += kThreads) {
+    const int l = idx / N, z = idx - l * N, col = col0 + l;
+    cx<T> v = mk<T>(0, 0);
+    if (col < g.ncol) {
+      const int st = g.col_start[col], len = g.col_start[col + 1] - st;
+      const int off = freq_of(z, N) - g.col_zlo[col];
+      if (off >= 0 && off < len) {
+        const int e = g.col_ent[st + off];
+        if (e != 0) {
+          const int ig = (e > 0 ? e : -e) - 1;
+          const cx<double> u = c1[ig];
+          const cx<double> w = two ? c2[ig] : mk<double>(0.0, 0.0);
+          // +G: c1 + i c2 ; -G: conj(c1) + i conj(c2)
+          v = (e > 0) ? mk<T>((T)(u.x - w.y), (T)(u.y + w.x)) : mk<T>((T)(u.x + w.y), (T)(w.x - u.y));
+        }
+      }
+    }
+    a[l * ls + z] = v;
+  }
+  __syncthreads();
+  const cx<T>* r = run_fft<true, T, NC>(a, b, nl, ls, p, tw);
+  cx<T>* zb = zbuf + (size_t)pair * N * g.ncol;
+  for (int idx = threadIdx.x; idx < nl * N; idx += kThreads) {
+    const int z = idx / nl, l = idx - z * nl, col = col0 + l;
+    if (col < g.ncol) zb[(size_t)z * g.ncol + col] = r[l * ls + z];
+  }
+}
+
+// ---------------------------------------------------------------- Y stage (inverse)
+template <typename T, int NC>
+__global__ void __launch_bounds__(kThreads) k_yinv(GeoDev g, FftPlan p, const cx<T>* __restrict__ zbuf, int nlrt,
+                                                  cx<T>* __restrict__ ybuf, const cx<T>* __restrict__ twg) {
+  GBCP_STAGE(g.n2, nlrt)
+  const int sb = blockIdx.x * nl, z = blockIdx.y, pair = blockIdx.z;
+  const cx<T>* zrow = zbuf + ((size_t)pair * g.n3 + z) * g.ncol;
+  load_tw(tw, twg, N);
+  for (int idx = threadIdx.x; idx < nl * N; idx += kThreads) {
+    const int l = idx / N, y = idx - l * N, s = sb + l;
+    cx<T> v = mk<T>(0, 0);
+    if (s < g.nslot) {
+      const int off = freq_of(y, N) - g.slot_gylo[s];
+      if (off >= 0 && off < g.slot_ncol[s]) v = zrow[g.slot_col0[s] + off];
+    }
+    a[l * ls + y] = v;
+  }
+  __syncthreads();
+  const cx<T>* r = run_fft<true, T, NC>(a, b, nl, ls, p, tw);
+  cx<T>* yb = ybuf + ((size_t)pair * g.n3 + z) * (size_t)N * g.nslot;
+  for (int idx = threadIdx.x; idx < nl * N; idx += kThreads) {
+    const int y = idx / nl, l = idx - y * nl, s = sb + l;
+    if (s < g.nslot) yb[(size_t)y * g.nslot + s] = r[l * ls + y];
+  }
+}
+
+// Load nl x-lines (y0..y0+nl) of plane z from ybuf, scattering slots to x.
+template <typename T>
+__device__ __forceinline__ void load_xlines(const GeoDev& g, const cx<T>* __restrict__ yb, int y0, int nl, int N,
+                                            int ls, cx<T>* a) {
+  for (int idx = threadIdx.x; idx < nl * N; idx += kThreads) {
+    const int l = idx / N, x = idx - l * N, y = y0 + l;
+    const int s = freq_of(x, N) - g.gxlo;
+    cx<T> v = mk<T>(0, 0);
+    if (y < g.n2 && s >= 0 && s < g.nslot) v = yb[(size_t)y * g.nslot + s];
+    a[l * ls + x] = v;
+  }
+}
+
+// ---------------------------------------------------------------- X stage + density
+template <typename T, int NC>
+__global__ void __launch_bounds__(kThreads) k_xinv_rho(GeoDev g, FftPlan p, const cx<T>* __restrict__ ybuf,
+                                                      int npairs, int s0, int nstate, const double* __restrict__ f,
+                                                      double inv_omega, double* __restrict__ rho, int nlrt,
+                                                      const cx<T>* __restrict__ twg) {
+  GBCP_STAGE(g.n1, nlrt)
+  constexpr int NACC = (NC > 0) ? (ct_lines(NC) * NC + kThreads - 1) / kThreads : kMaxAcc;
+  const int y0 = blockIdx.x * nl, z = blockIdx.y;
+  load_tw(tw, twg, N);
+  double acc[NACC];
+#pragma unroll
+  for (int k = 0; k < NACC; ++k) acc[k] = 0.0;
+  const int tot = nl * N;
+  for (int pair = 0; pair < npairs; ++pair) {
+    const int is1 = s0 + 2 * pair, is2 = is1 + 1;
+    const double f1 = f[is1] * inv_omega;
+    const double f2 = (is2 < nstate) ? f[is2] * inv_omega : 0.0;
+    const cx<T>* yb = ybuf + ((size_t)pair * g.n3 + z) * (size_t)g.n2 * g.nslot;
+    load_xlines(g, yb, y0, nl, N, ls, a);
+    __syncthreads();
+    const cx<T>* r = run_fft<true, T, NC>(a, b, nl, ls, p, tw);
+#pragma unroll
+    for (int k = 0; k < NACC; ++k) {
+      const int e = threadIdx.x + k * kThreads;
+      if (e < tot) {
+        const int l = e / N, x = e - l * N;
+        const cx<T> v = r[l * ls + x];
+        const double vr = (double)v.x, vi = (double)v.y;
+        acc[k] += f1 * vr * vr + f2 * vi * vi;
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int k = 0; k < NACC; ++k) {
+    const int e = threadIdx.x + k * kThreads;
+    if (e < tot) {
+      const int l = e / N, x = e - l * N, y = y0 + l;
+      if (y < g.n2) rho[x + (size_t)g.k1 * (y + (size_t)g.k2 * z)] += acc[k];
+    }
+  }
+}
+
+// ---------------------------------------------------------------- X stage: inverse, x V, forward
+template <typename T, int NC>
+__global__ void __launch_bounds__(kThreads) k_xvx(GeoDev g, FftPlan p, cx<T>* __restrict__ ybuf,
+                                                 const double* __restrict__ vpot, int nlrt,
+                                                 const cx<T>* __restrict__ twg) {
+  GBCP_STAGE(g.n1, nlrt)
+  const int y0 = blockIdx.x * nl, z = blockIdx.y, pair = blockIdx.z;
+  cx<T>* yb = ybuf + ((size_t)pair * g.n3 + z) * (size_t)g.n2 * g.nslot;
+  load_tw(tw, twg, N);
+  load_xlines(g, yb, y0, nl, N, ls, a);
+  __syncthreads();
+  cx<T>* r = run_fft<true, T, NC>(a, b, nl, ls, p, tw);
+  cx<T>* o = (r == a) ? b : a;
+  for (int idx = threadIdx.x; idx < nl * N; idx += kThreads) {
+    const int l = idx / N, x = idx - l * N, y = y0 + l;
+    const T v = (y < g.n2) ? (T)vpot[x + (size_t)g.k1 * (y + (size_t)g.k2 * z)] : (T)0;
+    r[l * ls + x] = scl(r[l * ls + x], v);
+  }
+  __syncthreads();
+  const cx<T>* q = run_fft<false, T, NC>(r, o, nl, ls, p, tw);
+  for (int idx = threadIdx.x; idx < nl * g.nslot; idx += kThreads) {
+    const int l = idx / g.nslot, s = idx - l * g.nslot, y = y0 + l;
+    if (y < g.n2) yb[(size_t)y * g.nslot + s] = q[l * ls + idx_of(g.gxlo + s, N)];
+  }
+}
+
+// ---------------------------------------------------------------- Y stage (forward)
+template <typename T, int NC>
+__global__ void __launch_bounds__(kThreads) k_yfwd(GeoDev g, FftPlan p, const cx<T>* __restrict__ ybuf, int nlrt,
+                                                  cx<T>* __restrict__ zbuf, const cx<T>* __restrict__ twg) {
+  GBCP_STAGE(g.n2, nlrt)
+  const int sb = blockIdx.x * nl, z = blockIdx.y, pair = blockIdx.z;
+  const cx<T>* yb = ybuf + ((size_t)pair * g.n3 + z) * (size_t)N * g.nslot;
+  load_tw(tw, twg, N);
+  for (int idx = threadIdx.x; idx < nl * N; idx += kThreads) {
+    const int y = idx / nl, l = idx - y * nl, s = sb + l;
+    a[l * ls + y] = (s < g.nslot) ? yb[(size_t)y * g.nslot + s] : mk<T>(0, 0);
+  }
+  __syncthreads();
+  const cx<T>* r = run_fft<false, T, NC>(a, b, nl, ls, p, tw);
+  cx<T>* zrow = zbuf + ((size_t)pair * g.n3 + z) * g.ncol;
+  const int send = min(sb + nl, g.nslot);
+  const int cbeg = g.slot_col0[sb];
+  const int cend = g.slot_col0[send - 1] + g.slot_ncol[send - 1];
+  for (int c = cbeg + threadIdx.x; c < cend; c += kThreads) {
+    const int l = g.col_slot[c] - sb;
+    zrow[c] = r[l * ls + idx_of(g.col_gy[c], N)];
+  }
+}
+
+// ---------------------------------------------------------------- Z stage (forward, to sphere entries)
+template <typename T, int NC>
+__global__ void __launch_bounds__(kThreads) k_zfwd(GeoDev g, FftPlan p, const cx<T>* __restrict__ zbuf, int nlrt,
+                                                  T scale, cx<T>* __restrict__ qbuf,
+                                                  const cx<T>* __restrict__ twg) {
+  GBCP_STAGE(g.n3, nlrt)
+  const int col0 = blockIdx.x * nl, pair = blockIdx.y;
+  const cx<T>* zb = zbuf + (size_t)pair * N * g.ncol;
+  load_tw(tw, twg, N);
+  for (int idx = threadIdx.x; idx < nl * N; idx += kThreads) {
+    const int z = idx / nl, l = idx - z * nl, col = col0 + l;
+    a[l * ls + z] = (col < g.ncol) ? zb[(size_t)z * g.ncol + col] : mk<T>(0, 0);
+  }
+  __syncthreads();
+  const cx<T>* r = run_fft<false, T, NC>(a, b, nl, ls, p, tw);
+  const int cend = min(col0 + nl, g.ncol);
+  const int ebeg = g.col_start[col0], eend = g.col_start[cend];
+  cx<T>* qb = qbuf + (size_t)pair * g.nent;
+  for (int e = ebeg + threadIdx.x; e < eend; e += kThreads) {
+    const int col = g.ent_col[e];
+    const int gz = g.col_zlo[col] + (e - g.col_start[col]);
+    qb[e] = scl(r[(col - col0) * ls + idx_of(gz, N)], scale);
+  }
+}
+
+#undef GBCP_STAGE
+
+// ---------------------------------------------------------------- decode + kinetic (vpsi_utils.mod.F90:661-671)
+template <typename T>
+__global__ void k_decode(GeoDev g, const cx<T>* __restrict__ qbuf, const cx<double>* __restrict__ c0, int ldc,
+                         cx<double>* __restrict__ c2, int ldc2, const double* __restrict__ f, int s0, int nstate,
+                         double tpiba2) {
+  const int ig = blockIdx.x * blockDim.x + threadIdx.x;
+  const int pair = blockIdx.y;
+  if (ig >= g.ngw) return;
+  const int is1 = s0 + 2 * pair, is2 = is1 + 1;
+  const cx<T>* qb = qbuf + (size_t)pair * g.nent;
+  const cx<T> qp = qb[g.pos_plus[ig]], qm = qb[g.pos_minus[ig]];
+  const double fpx = (double)qp.x + (double)qm.x, fpy = (double)qp.y + (double)qm.y;
+  const double fmx = (double)qp.x - (double)qm.x, fmy = (double)qp.y - (double)qm.y;
+  const double kin = tpiba2 * g.hg[ig];
+  double fi = f[is1] * 0.5;
+  if (fi == 0.0) fi = 1.0;
+  {
+    const cx<double> c = c0[(size_t)is1 * ldc + ig];
+    cx<double>& o = c2[(size_t)is1 * ldc2 + ig];
+    o.x += -fi * (kin * c.x + fpx);
+    o.y += -fi * (kin * c.y + fmy);
+  }
+  if (is2 < nstate) {
+    double fip1 = f[is2] * 0.5;
+    if (fip1 == 0.0) fip1 = 1.0;
+    const cx<double> c = c0[(size_t)is2 * ldc + ig];
+    cx<double>& o = c2[(size_t)is2 * ldc2 + ig];
+    o.x += -fip1 * (kin * c.x + fpy);
+    o.y += -fip1 * (kin * c.y - fmx);
+  }
+}
+
+// =========================================================================== host side
+
+inline int lines_rt(int n) { return std::max(1, std::min(64, kElems / n)); }
+
+template <typename T> inline size_t stage_smem(int n, int nl) {
+  return sizeof(cx<T>) * ((size_t)n + 2 * (size_t)nl * line_stride(n));
+}
+
+template <typename KernelT> inline void allow_smem(KernelT k, size_t bytes) {
+  if (bytes > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <typename T> inline const cx<T>* tw_of(Ctx& c, int axis);
+template <> inline const cx<double>* tw_of<double>(Ctx& c, int axis) { return c.tw64[axis]; }
+template <> inline const cx<float>* tw_of<float>(Ctx& c, int axis) { return c.tw32[axis]; }
+
+// lines per CTA of a stage (compile-time plan or run-time tile)
+template <int NC> inline int stage_lines(int n) { return NC > 0 ? ct_lines(NC) : lines_rt(n); }
+
+#define GBCP_CT_SIZES(X) X(32) X(36) X(40) X(48) X(60) X(64) X(72) X(80) X(96) X(120) X(144) X(240)
+
+// Dispatch `launch_<name><T, NC>(args...)` on the run-time length n.
+#define GBCP_DISPATCH(FN, T, n, ...)                        \
+  switch (n) {                                              \
+    case 32: return FN<T, 32>(__VA_ARGS__);                 \
+    case 36: return FN<T, 36>(__VA_ARGS__);                 \
+    case 40: return FN<T, 40>(__VA_ARGS__);                 \
+    case 48: return FN<T, 48>(__VA_ARGS__);                 \
+    case 60: return FN<T, 60>(__VA_ARGS__);                 \
+    case 64: return FN<T, 64>(__VA_ARGS__);                 \
+    case 72: return FN<T, 72>(__VA_ARGS__);                 \
+    case 80: return FN<T, 80>(__VA_ARGS__);                 \
+    case 96: return FN<T, 96>(__VA_ARGS__);                 \
+    case 120: return FN<T, 120>(__VA_ARGS__);               \
+    case 144: return FN<T, 144>(__VA_ARGS__);               \
+    case 240: return FN<T, 240>(__VA_ARGS__);               \
+    default: return FN<T, 0>(__VA_ARGS__);                  \
+  }
+
+template <typename T> int ensure_band_buffers(Ctx& c, int npairs) {
+  const GeoDev& g = c.geo;
+  const size_t zb = sizeof(cx<T>) * (size_t)npairs * g.n3 * g.ncol;
+  const size_t yb = sizeof(cx<T>) * (size_t)npairs * g.n3 * g.n2 * g.nslot;
+  const size_t qb = sizeof(cx<T>) * (size_t)npairs * g.nent;
+  if (!ensure(c, c.zbuf, zb) || !ensure(c, c.ybuf, yb) || !ensure(c, c.qbuf, qb)) {
+    c.err = "band workspace allocation failed";
+    return 6;
+  }
+  return 0;
+}
+
+template <typename T, int NC>
+int launch_zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int np) {
+  const GeoDev& g = c.geo;
+  const int nl = stage_lines<NC>(g.n3);
+  const size_t sm = stage_smem<T>(g.n3, nl);
+  allow_smem(k_zinv<T, NC>, sm);
+  ProfScope ps_(c, "k_zinv");
+  k_zinv<T, NC><<<dim3((g.ncol + nl - 1) / nl, np), kThreads, sm, c.stream>>>(
+      g, c.plan[2], c0, ldc, s0, nstate, nl, static_cast<cx<T>*>(c.zbuf.p), tw_of<T>(c, 2));
+  GBCP_LAUNCH_CHECK(c);
+  return 0;
+}
+
+template <typename T, int NC> int launch_yinv(Ctx& c, int np) {
+  const GeoDev& g = c.geo;
+  const int nl = stage_lines<NC>(g.n2);
+  const size_t sm = stage_smem<T>(g.n2, nl);
+  allow_smem(k_yinv<T, NC>, sm);
+  ProfScope ps_(c, "k_yinv");
+  k_yinv<T, NC><<<dim3((g.nslot + nl - 1) / nl, g.n3, np), kThreads, sm, c.stream>>>(
+      g, c.plan[1], static_cast<const cx<T>*>(c.zbuf.p), nl, static_cast<cx<T>*>(c.ybuf.p), tw_of<T>(c, 1));
+  GBCP_LAUNCH_CHECK(c);
+  return 0;
+}
+
+template <typename T, int NC>
+int launch_xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho) {
+  const GeoDev& g = c.geo;
+  int nl = stage_lines<NC>(g.n1);
+  if (NC == 0) {
+    while (nl > 1 && nl * g.n1 > kMaxAcc * kThreads) --nl;
+    if (nl * g.n1 > kMaxAcc * kThreads) {
+      c.err = "mesh too large for the density tile";
+      return 7;
+    }
+  }
+  const size_t sm = stage_smem<T>(g.n1, nl);
+  allow_smem(k_xinv_rho<T, NC>, sm);
+  ProfScope ps_(c, "k_xinv_rho");
+  k_xinv_rho<T, NC><<<dim3((g.n2 + nl - 1) / nl, g.n3), kThreads, sm, c.stream>>>(
+      g, c.plan[0], static_cast<const cx<T>*>(c.ybuf.p), np, s0, nstate, f, 1.0 / c.omega, rho, nl, tw_of<T>(c, 0));
+  GBCP_LAUNCH_CHECK(c);
+  return 0;
+}
+
+template <typename T, int NC> int launch_xvx(Ctx& c, int np, const double* vpot) {
+  const GeoDev& g = c.geo;
+  const int nl = stage_lines<NC>(g.n1);
+  const size_t sm = stage_smem<T>(g.n1, nl);
+  allow_smem(k_xvx<T, NC>, sm);
+  ProfScope ps_(c, "k_xvx");
+  k_xvx<T, NC><<<dim3((g.n2 + nl - 1) / nl, g.n3, np), kThreads, sm, c.stream>>>(
+      g, c.plan[0], static_cast<cx<T>*>(c.ybuf.p), vpot, nl, tw_of<T>(c, 0));
+  GBCP_LAUNCH_CHECK(c);
+  return 0;
+}
+
+template <typename T, int NC> int launch_yfwd(Ctx& c, int np) {
+  const GeoDev& g = c.geo;
+  const int nl = stage_lines<NC>(g.n2);
+  const size_t sm = stage_smem<T>(g.n2, nl);
+  allow_smem(k_yfwd<T, NC>, sm);
+  ProfScope ps_(c, "k_yfwd");
+  k_yfwd<T, NC><<<dim3((g.nslot + nl - 1) / nl, g.n3, np), kThreads, sm, c.stream>>>(
+      g, c.plan[1], static_cast<const cx<T>*>(c.ybuf.p), nl, static_cast<cx<T>*>(c.zbuf.p), tw_of<T>(c, 1));
+  GBCP_LAUNCH_CHECK(c);
+  return 0;
+}
+
+template <typename T, int NC> int launch_zfwd(Ctx& c, int np) {
+  const GeoDev& g = c.geo;
+  const int nl = stage_lines<NC>(g.n3);
+  const size_t sm = stage_smem<T>(g.n3, nl);
+  const T scale = (T)(1.0 / ((double)g.n1 * g.n2 * g.n3));
+  allow_smem(k_zfwd<T, NC>, sm);
+  ProfScope ps_(c, "k_zfwd");
+  k_zfwd<T, NC><<<dim3((g.ncol + nl - 1) / nl, np), kThreads, sm, c.stream>>>(
+      g, c.plan[2], static_cast<const cx<T>*>(c.zbuf.p), nl, scale, static_cast<cx<T>*>(c.qbuf.p),
+      tw_of<T>(c, 2));
+  GBCP_LAUNCH_CHECK(c);
+  return 0;
+}
+
+template <typename T>
+int launch_decode(Ctx& c, int np, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, const double* f, int s0,
+                  int nstate) {
+  const GeoDev& g = c.geo;
+  ProfScope ps_(c, "k_decode");
+  k_decode<T><<<dim3((g.ngw + 255) / 256, np), 256, 0, c.stream>>>(g, static_cast<const cx<T>*>(c.qbuf.p), c0, ldc,
+                                                                     c2, ldc2, f, s0, nstate, c.tpiba2);
+  GBCP_LAUNCH_CHECK(c);
+  return 0;
+}
+
+template <typename T> int zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int np) {
+  GBCP_DISPATCH(launch_zinv, T, c.nr[2], c, c0, ldc, s0, nstate, np)
+}
+template <typename T> int yinv(Ctx& c, int np) { GBCP_DISPATCH(launch_yinv, T, c.nr[1], c, np) }
+template <typename T> int xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho) {
+  GBCP_DISPATCH(launch_xinv_rho, T, c.nr[0], c, np, s0, nstate, f, rho)
+}
+template <typename T> int xvx(Ctx& c, int np, const double* vpot) {
+  GBCP_DISPATCH(launch_xvx, T, c.nr[0], c, np, vpot)
+}
+template <typename T> int yfwd(Ctx& c, int np) { GBCP_DISPATCH(launch_yfwd, T, c.nr[1], c, np) }
+template <typename T> int zfwd(Ctx& c, int np) { GBCP_DISPATCH(launch_zfwd, T, c.nr[2], c, np) }
+
+template <typename T>
+int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho) {
+  const int npairs_total = (nstate + 1) / 2;
+  int rc = ensure_band_buffers<T>(c, std::min(c.batch, npairs_total));
+  if (rc) return rc;
+  for (int p0 = 0; p0 < npairs_total; p0 += c.batch) {
+    const int np = std::min(c.batch, npairs_total - p0);
+    const int s0 = 2 * p0;
+    if ((rc = zinv<T>(c, c0, ldc, s0, nstate, np))) return rc;
+    if ((rc = yinv<T>(c, np))) return rc;
+    if ((rc = xinv_rho<T>(c, np, s0, nstate, f, rho))) return rc;
+  }
+  return 0;
+}
+
+template <typename T>
+int vpsi_t(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, const double* f, const double* vpot,
+           int nstate) {
+  const int npairs_total = (nstate + 1) / 2;
+  int rc = ensure_band_buffers<T>(c, std::min(c.batch, npairs_total));
+  if (rc) return rc;
+  for (int p0 = 0; p0 < npairs_total; p0 += c.batch) {
+    const int np = std::min(c.batch, npairs_total - p0);
+    const int s0 = 2 * p0;
+    if ((rc = zinv<T>(c, c0, ldc, s0, nstate, np))) return rc;
+    if ((rc = yinv<T>(c, np))) return rc;
+    if ((rc = xvx<T>(c, np, vpot))) return rc;
+    if ((rc = yfwd<T>(c, np))) return rc;
+    if ((rc = zfwd<T>(c, np))) return rc;
+    if ((rc = launch_decode<T>(c, np, c0, ldc, c2, ldc2, f, s0, nstate))) return rc;
+  }
+  return 0;
+}
+
+}  // namespace band
+}  // namespace gbcp
