@@ -45,6 +45,7 @@ SIGNATURES = {
     "gbcp_ctx_destroy": (_I, [_P]),
     "gbcp_set_precision": (_I, [_P, _I]),
     "gbcp_set_stream": (_I, [_P, _P]),
+    "gbcp_set_option": (_I, [_P, _I, _I]),
     "gbcp_synchronize": (_I, [_P]),
     "gbcp_last_error": (_I, [_P, C.c_char_p, _I]),
     "gbcp_kernel_launches": (C.c_int64, []),

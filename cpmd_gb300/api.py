@@ -137,6 +137,11 @@ class Context:
         self._check("gbcp_set_precision", self.lib.gbcp_set_precision(self.h, PREC[precision]))
         self.precision = precision
 
+    def set_option(self, key: str, value: int):
+        """key 'gemm' (-1 by precision, 0 FP64 SIMT, 1 tensor cores) or 'batch' (pairs per launch)."""
+        k = {"gemm": 1, "batch": 2}[key]
+        self._check("gbcp_set_option", self.lib.gbcp_set_option(self.h, k, int(value)))
+
     def synchronize(self):
         self._check("gbcp_synchronize", self.lib.gbcp_synchronize(self.h))
 

@@ -343,6 +343,20 @@ int gbcp_set_precision(gbcp_ctx* h, int precision) {
   return GBCP_OK;
 }
 
+int gbcp_set_option(gbcp_ctx* h, int key, int value) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  if (key == GBCP_OPT_GEMM && value >= -1 && value <= 1) {
+    c.gemm_mode = value;
+    return GBCP_OK;
+  }
+  if (key == GBCP_OPT_BATCH && value > 0) {
+    c.batch = value;
+    return GBCP_OK;
+  }
+  return set_err(h, GBCP_ERR_ARG, "set_option: unknown key or value");
+}
+
 int gbcp_set_stream(gbcp_ctx* h, void* stream) {
   if (!h) return GBCP_ERR_ARG;
   Ctx& c = h->c;

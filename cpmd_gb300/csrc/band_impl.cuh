@@ -157,14 +157,17 @@ __global__ void __launch_bounds__(kThreads) k_xinv_rho(GeoDev g, FftPlan p, cons
   constexpr int NACC = (NC > 0) ? (ct_lines(NC) * NC + kThreads - 1) / kThreads : kMaxAcc;
   const int y0 = blockIdx.x * nl, z = blockIdx.y;
   load_tw(tw, twg, N);
-  double acc[NACC];
+  // density of this launch's pairs: FP64 in the FP64 path; FP32 in the mixed path, added once
+  // per launch to the FP64 density (the per-pair FP64 accumulation would occupy the
+  // FP64 pipe for ~4 operations per grid point and pair)
+  T acc[NACC];
 #pragma unroll
-  for (int k = 0; k < NACC; ++k) acc[k] = 0.0;
+  for (int k = 0; k < NACC; ++k) acc[k] = (T)0;
   const int tot = nl * N;
   for (int pair = 0; pair < npairs; ++pair) {
     const int is1 = s0 + 2 * pair, is2 = is1 + 1;
-    const double f1 = f[is1] * inv_omega;
-    const double f2 = (is2 < nstate) ? f[is2] * inv_omega : 0.0;
+    const T f1 = (T)(f[is1] * inv_omega);
+    const T f2 = (T)((is2 < nstate) ? f[is2] * inv_omega : 0.0);
     const cx<T>* yb = ybuf + ((size_t)pair * g.n3 + z) * (size_t)g.n2 * g.nslot;
     load_xlines(g, yb, y0, nl, N, ls, a);
     __syncthreads();
@@ -175,7 +178,7 @@ __global__ void __launch_bounds__(kThreads) k_xinv_rho(GeoDev g, FftPlan p, cons
       if (e < tot) {
         const int l = e / N, x = e - l * N;
         const cx<T> v = r[l * ls + x];
-        const double vr = (double)v.x, vi = (double)v.y;
+        const T vr = v.x, vi = v.y;
         acc[k] += f1 * vr * vr + f2 * vi * vi;
       }
     }
@@ -186,7 +189,7 @@ __global__ void __launch_bounds__(kThreads) k_xinv_rho(GeoDev g, FftPlan p, cons
     const int e = threadIdx.x + k * kThreads;
     if (e < tot) {
       const int l = e / N, x = e - l * N, y = y0 + l;
-      if (y < g.n2) rho[x + (size_t)g.k1 * (y + (size_t)g.k2 * z)] += acc[k];
+      if (y < g.n2) rho[x + (size_t)g.k1 * (y + (size_t)g.k2 * z)] += (double)acc[k];
     }
   }
 }

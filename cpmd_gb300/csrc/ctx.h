@@ -67,7 +67,8 @@ struct Ctx {
   int nr[3], kr[3], ngw, geq0;
   double omega, tpiba2;
   int precision;
-  int batch;  // pairs per batch
+  int batch;           // pairs per batch
+  int gemm_mode = -1;  // overlap GEMM: -1 by precision (mixed -> tensor cores), 0 FP64 SIMT, 1 tensor cores
   cudaStream_t stream = nullptr;  // stream all work is queued on
   cudaStream_t own = nullptr;     // the context's own stream
   // geometry
@@ -116,6 +117,8 @@ int rho_sum(Ctx& c, const double* rho, double* sum);
 
 // ---- linear algebra (linalg.cu) ----
 int ovlap_gamma(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S);
+int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, double* scond_host);
+inline bool use_tc_gemm(const Ctx& c) { return c.gemm_mode == 1 || (c.gemm_mode < 0 && c.precision == 1); }
 int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host);
 int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host);
 

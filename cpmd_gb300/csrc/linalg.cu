@@ -309,6 +309,7 @@ __global__ void k_scale(double* __restrict__ X, size_t n, const double* __restri
 }  // namespace
 
 int ovlap_gamma_ex(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, double* scond_host) {
+  if (use_tc_gemm(c)) return ovlap_tc(c, c0, ldc, nstate, S, scond_host);
   const int n = nstate;
   const int K = 2 * c.ngw;
   const int lda = 2 * ldc;

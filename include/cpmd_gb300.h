@@ -79,6 +79,15 @@ typedef struct gbcp_grid_desc {
 int gbcp_ctx_create(const gbcp_grid_desc* grid, int precision, int max_batch, void* stream, gbcp_ctx** out);
 int gbcp_ctx_destroy(gbcp_ctx* ctx);
 int gbcp_set_precision(gbcp_ctx* ctx, int precision);
+
+/* Options (the reference's &CPMD GPU keywords, control_utils.mod.F90:2856-2894,
+ * become per-context settings):
+ *   GBCP_OPT_GEMM   overlap GEMM engine: -1 = by precision (MIXED -> tensor
+ *                   cores), 0 = FP64 SIMT, 1 = tcgen05 split-precision
+ *                   (FP64-accurate);
+ *   GBCP_OPT_BATCH  state pairs per band-loop launch (> 0). */
+enum gbcp_option { GBCP_OPT_GEMM = 1, GBCP_OPT_BATCH = 2 };
+int gbcp_set_option(gbcp_ctx* ctx, int key, int value);
 /* Queue later work on `stream` (a cudaStream_t; NULL = the context's own
  * stream; the CUDA legacy default stream is cudaStreamLegacy).  Device-pointer calls are ordered only with respect to this stream,
  * as the reference's GPU path orders work on its thread's stream
