@@ -118,6 +118,7 @@ int rho_sum(Ctx& c, const double* rho, double* sum);
 // ---- linear algebra (linalg.cu) ----
 int ovlap_gamma(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S);
 int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, double* scond_host);
+int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout, int ldo);
 inline bool use_tc_gemm(const Ctx& c) { return c.gemm_mode == 1 || (c.gemm_mode < 0 && c.precision == 1); }
 int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host);
 int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host);

@@ -155,6 +155,49 @@ __global__ void __launch_bounds__(1024) k_potrf_trtri(double* __restrict__ S, do
   if (threadIdx.x == 0) *info = 0;
 }
 
+// Same factorisation with S held in shared memory (n <= 160): the trailing
+// updates and the triangular inverse read shared memory instead of L2.
+__global__ void __launch_bounds__(1024) k_potrf_trtri_smem(const double* __restrict__ Sg, double* __restrict__ X,
+                                                           int n, int* __restrict__ info) {
+  extern __shared__ double sS[];
+  __shared__ int bad;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) sS[e] = Sg[e];
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x == 0) {
+      const double d = sS[k * n + k];
+      if (!(d > 0.0)) bad = (d != d) ? -1 : k + 1;
+      else sS[k * n + k] = sqrt(d);
+    }
+    __syncthreads();
+    if (bad) break;
+    const double dk = sS[k * n + k];
+    for (int j = k + 1 + threadIdx.x; j < n; j += blockDim.x) sS[k * n + j] /= dk;
+    __syncthreads();
+    const int m = n - k - 1;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+      const int i = k + 1 + e / m, j = k + 1 + e % m;
+      if (j >= i) sS[i * n + j] -= sS[k * n + i] * sS[k * n + j];
+    }
+    __syncthreads();
+  }
+  if (bad) {
+    if (threadIdx.x == 0) *info = bad;
+    return;
+  }
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    for (int i = j + 1; i < n; ++i) X[(size_t)i * n + j] = 0.0;
+    X[(size_t)j * n + j] = 1.0 / sS[j * n + j];
+    for (int i = j - 1; i >= 0; --i) {
+      double s = 0.0;
+      for (int k = i + 1; k <= j; ++k) s = fma(sS[i * n + k], X[(size_t)k * n + j], s);
+      X[(size_t)i * n + j] = -s / sS[i * n + i];
+    }
+  }
+  if (threadIdx.x == 0) *info = 0;
+}
+
 // Cout = A * M.  A real view (rows = 2 ngw, lda), M (n x n) row-major (M[k][j]).
 // upper != 0: M is upper triangular, column block j only needs k <= j.
 __global__ void __launch_bounds__(NT) k_gemm_right(const double* __restrict__ A, int lda, int rows, int n,
@@ -356,8 +399,11 @@ static int apply_right(Ctx& c, cx<double>* c0, int ldc, int nstate, const double
   const int lda = 2 * ldc;
   if (!ensure(c, c.cscr, sizeof(double) * (size_t)rows * nstate)) return 6;
   double* tmp = static_cast<double*>(c.cscr.p);
-  dim3 grid((rows + TS - 1) / TS, (nstate + TS - 1) / TS);
-  {
+  if (use_tc_gemm(c)) {
+    const int rc = rmul_tc(c, reinterpret_cast<const double*>(c0), lda, rows, nstate, M, upper, tmp, rows);
+    if (rc) return rc;
+  } else {
+    dim3 grid((rows + TS - 1) / TS, (nstate + TS - 1) / TS);
     ProfScope ps_(c, "k_gemm_right");
     k_gemm_right<<<grid, NT, 0, c.stream>>>(reinterpret_cast<const double*>(c0), lda, rows, nstate, M, upper, tmp, rows);
     GBCP_LAUNCH_CHECK(c);
@@ -383,15 +429,26 @@ int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host) {
   double* X = static_cast<double*>(c.smat2.p);
   int rc = ovlap_gamma_ex(c, c0, ldc, n, S, scond_host);
   if (rc) return rc;
-  {
+  if (n <= 160) {
+    const size_t sm = sizeof(double) * (size_t)n * n;
+    if (sm > 48 * 1024)
+      cudaFuncSetAttribute(k_potrf_trtri_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    ProfScope ps_(c, "k_potrf_trtri");
+    k_potrf_trtri_smem<<<1, 1024, sm, c.stream>>>(S, X, n, c.d_info);
+    GBCP_LAUNCH_CHECK(c);
+  } else {
     ProfScope ps_(c, "k_potrf_trtri");
     k_potrf_trtri<<<1, 1024, 0, c.stream>>>(S, X, n, c.d_info);
     GBCP_LAUNCH_CHECK(c);
   }
-  rc = apply_right(c, c0, ldc, n, X, 1);
-  if (rc) return rc;
+  // a failed factorisation leaves c0 untouched
   int info = 0;
   GBCP_CUDA_TRY(c, cudaMemcpyAsync(&info, c.d_info, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  if (info == 0) {
+    rc = apply_right(c, c0, ldc, n, X, 1);
+    if (rc) return rc;
+  }
   GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   if (info > 0) {
     c.err = "UINV: leading minor " + std::to_string(info) + " not positive definite (dpotrf)";

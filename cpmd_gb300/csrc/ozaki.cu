@@ -1,35 +1,37 @@
-// Γ-point overlap matrix S = 2 Re(C^H C) - Re c(0) Re c(0)^T on the tcgen05
-// tensor cores, to FP64 accuracy, by error-free splitting (after Ozaki, Ogita,
-// Oishi and Rump, "Error-free transformations of matrix multiplication by using
-// fast routines of matrix multiplication and its applications", Numer.
-// Algorithms 59, 2012; arranged here for bf16 MMAs with FP32 accumulators).
+// FP64-accurate GEMMs of the ortho step on the tcgen05 tensor cores, by
+// error-free splitting (after Ozaki, Ogita, Oishi and Rump, "Error-free
+// transformations of matrix multiplication by using fast routines of matrix
+// multiplication and its applications", Numer. Algorithms 59, 2012; arranged
+// here for bf16 MMAs with FP32 accumulators and int64 folding).
 //
-// Reference: rgs_utils.mod.F90:63-68 / ovlap_utils.mod.F90:150-165 (dsyrk over
-// the real view of C, K = 2 ngw, then dger for G = 0).
+//  * ovlap_tc: S = 2 Re(C^H C) - Re c(0) Re c(0)^T over the real view of C
+//    (K = 2 ngw) -- rgs_utils.mod.F90:63-68, ovlap_utils.mod.F90:150-165.
+//  * rmul_tc:  C <- C M for an n x n matrix M (U^{-1} of Gram-Schmidt, upper
+//    triangular, rgs_utils.mod.F90:71-73; or S^{-1/2} of Loewdin,
+//    lowdin_utils.mod.F90:81-83).
 //
-// Splitting.  Every state column j has an exponent E_j with |a_kj| < 2^E_j.
-// Each element becomes the 56-bit fixed-point magnitude v = trunc(|a| 2^(56-E_j))
-// cut into 8 signed 7-bit digits m_s (s = 0 most significant), so
-// a = 2^E_j sum_s m_s 2^(-7(s+1)) up to 2^(E_j-56).  A digit is an integer in
-// [-127, 127]: exact in bf16, and a digit product is exact in FP32.
+// Splitting.  Every row of the left operand and every column of the right
+// operand has an exponent E with |x| < 2^E (row/column maxima).  An element
+// becomes the 56-bit fixed-point magnitude v = trunc(|x| 2^(56-E)), cut into 8
+// signed 7-bit digits m_s (s = 0 most significant): x = 2^E sum_s m_s 2^(-7(s+1))
+// up to 2^(E-56).  A digit is an integer in [-127, 127] -- exact in bf16 -- and
+// a digit product is exact in FP32.
 //
-// Products.  For a 128 x 64 output tile the CTA runs, per K-chunk of 128 real
-// rows, the 36 digit-pair products with s + t = d <= 7 (level d), accumulating
-// every pair of one level in one FP32 TMEM accumulator (8 accumulators x 64
-// columns = all 512 TMEM columns).  A level sum is an integer below
-// 8 * 128 * 127^2 < 2^24, so FP32 holds it exactly.  After each chunk the
-// accumulators are read back and folded into two int64 registers per output
-// (H = levels 0-3, Lo = levels 4-7, shifted by 7 bits per level); int64 keeps
-// the sum over all chunks exact.  Split-K partials are added with 64-bit
-// integer atomics, and only the final conversion is FP64:
-//   sum_k a_ki a_kj = 2^(E_i+E_j) (H 2^-35 + Lo 2^-63).
-// Levels above 7 (digit pairs beyond 56 bits) are dropped: < 2^-49 relative to
-// 2^(E_i+E_j) per product term.
+// Products.  For a 128 x 64 output tile the CTA runs, per K-chunk of 128, the
+// 36 digit-pair products with s + t = d <= 7 ("level" d), accumulating all pairs
+// of a level in one FP32 TMEM accumulator (8 levels x 64 columns = the 512 TMEM
+// columns).  A level sum is an integer below 8 * 128 * 127^2 < 2^24, so FP32
+// holds it exactly.  After each chunk the accumulators are read back and folded
+// into two int64 registers per output (H = levels 0-3, Lo = levels 4-7, 7 bits
+// apart); int64 keeps the sum over every chunk exact and only the final
+// conversion is FP64:  sum_k x_ik y_kj = 2^(E_i+E_j) (H 2^-35 + Lo 2^-63).
+// Levels above 7 are dropped (< 2^-49 of 2^(E_i+E_j) per product term).
 //
-// The digits are produced in the kernel from FP64 data with integer
+// The digits are produced in the kernels from FP64 data with integer
 // instructions and stored straight into shared memory in the tensor core's
 // K-major core-matrix layout: no slice matrices in HBM, no FP64 arithmetic in
-// the inner loop.
+// the inner loop.  Every mbarrier wait is bounded; on expiry the kernel flags
+// GBCP_ERR_TIMEOUT, frees its TMEM and returns.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -41,9 +43,9 @@ namespace gbcp {
 
 namespace {
 
-constexpr int OZ_M = 128;      // output rows per CTA (states i)
-constexpr int OZ_N = 64;       // output columns per CTA (states j)
-constexpr int OZ_KS = 32;      // real K rows per sub-chunk (two MMAs of K = 16)
+constexpr int OZ_M = 128;      // output rows per tile
+constexpr int OZ_N = 64;       // output columns per tile
+constexpr int OZ_KS = 32;      // K per sub-chunk (two MMAs of K = 16)
 constexpr int OZ_SUBS = 4;     // sub-chunks per exact accumulation chunk (K = 128)
 constexpr int OZ_SL = 8;       // digit slices
 constexpr int OZ_LEV = 8;      // levels kept (s + t <= 7)
@@ -53,84 +55,137 @@ constexpr int B_SLICE_BYTES = OZ_N * OZ_KS * 2;  // 4 KB
 constexpr int A_BUF_BYTES = OZ_SL * A_SLICE_BYTES;
 constexpr int B_BUF_BYTES = OZ_SL * B_SLICE_BYTES;
 constexpr int OZ_SMEM = 2 * A_BUF_BYTES + 2 * B_BUF_BYTES;  // 192 KB, double-buffered
+constexpr uint32_t kIdesc = tc::idesc_bf16_f32(OZ_M, OZ_N);
 
-// byte offset of (row, k-group) core-matrix row in a K-major no-swizzle tile of 32 K
+// byte offset of the (row, k-group) core-matrix row in a K-major no-swizzle tile of 32 K
 __device__ __forceinline__ int core_off(int row, int kg) { return (((row >> 3) << 2) + kg) * 128 + (row & 7) * 16; }
 
 // signed 7-bit digit -> bf16 bits (exact: |d| <= 127)
 __device__ __forceinline__ uint32_t digit_bf16(int d) { return __float_as_uint((float)d) >> 16; }
 
-// Fixed-point magnitude trunc(|a| 2^(56-E)) (< 2^56) and the sign of a, integer ops only.
-__device__ __forceinline__ unsigned long long fixed56(double a, int E, bool& neg) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(a);
+// exponent E with |x| < 2^E from the bit pattern of max |x|
+__device__ __forceinline__ int exp_of_max(unsigned long long bits) {
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  return (ex == 0) ? -1021 : ex - 1022;
+}
+
+// Fixed-point magnitude trunc(|x| 2^(56-E)) (< 2^56) and the sign, integer ops only.
+__device__ __forceinline__ unsigned long long fixed56(double x, int E, bool& neg) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   neg = (b >> 63) != 0;
   const int ex = (int)((b >> 52) & 0x7FF);
   if (ex == 0) return 0ull;  // zero or subnormal
   const unsigned long long M = (b & ((1ull << 52) - 1)) | (1ull << 52);
   int sh = ex - 1019 - E;  // = (ex - 1023) + 4 - E
-  if (sh > 3) sh = 3;      // cannot happen when |a| < 2^E; keeps v < 2^56
+  if (sh > 3) sh = 3;      // cannot happen when |x| < 2^E; keeps v < 2^56
   if (sh >= 0) return M << sh;
   return (sh <= -64) ? 0ull : (M >> (-sh));
 }
 
-// Produce the 8 digit slices of rows [r0, r0+rows) x K [kb, kb+32) into smem.
-__device__ __forceinline__ void produce(const double* __restrict__ Ar, int lda, int K, int n, int kb, int s0,
-                                        int rows, const int* __restrict__ E, uint8_t* __restrict__ dst,
-                                        int slice_bytes) {
-  // task = (row, kg): 4 k-groups of 8 per row; consecutive threads read consecutive k-groups
-  for (int task = threadIdx.x; task < rows * 4; task += OZ_THREADS) {
-    const int row = task >> 2, kg = task & 3;
-    const int state = s0 + row;
-    const bool valid = state < n;
-    const int e = valid ? E[state] : 0;
-    uint32_t w[OZ_SL][4];
+// Digits of 8 consecutive K elements of one operand row -> 8 slices x 16 bytes in smem.
+__device__ __forceinline__ void store_digits(const double (&x)[8], int E, uint8_t* dst, int slice_bytes, int off) {
+  uint32_t w[OZ_SL][4];
 #pragma unroll
-    for (int q2 = 0; q2 < 4; ++q2) {
-      const int k = kb + kg * 8 + 2 * q2;
-      double2 v2 = make_double2(0.0, 0.0);
-      if (valid && k < K) v2 = *reinterpret_cast<const double2*>(Ar + k + (size_t)state * lda);
-      bool n0, n1;
-      const unsigned long long f0 = fixed56(v2.x, e, n0), f1 = fixed56(v2.y, e, n1);
-#pragma unroll
-      for (int s = 0; s < OZ_SL; ++s) {
-        const int sh = 7 * (OZ_SL - 1 - s);
-        const int d0 = (int)((f0 >> sh) & 127ull), d1 = (int)((f1 >> sh) & 127ull);
-        w[s][q2] = digit_bf16(n0 ? -d0 : d0) | (digit_bf16(n1 ? -d1 : d1) << 16);
-      }
-    }
-    const int off = core_off(row, kg);
+  for (int q2 = 0; q2 < 4; ++q2) {
+    bool n0, n1;
+    const unsigned long long f0 = fixed56(x[2 * q2], E, n0), f1 = fixed56(x[2 * q2 + 1], E, n1);
 #pragma unroll
     for (int s = 0; s < OZ_SL; ++s) {
-      *reinterpret_cast<uint4*>(dst + s * slice_bytes + off) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+      const int sh = 7 * (OZ_SL - 1 - s);
+      const int d0 = (int)((f0 >> sh) & 127ull), d1 = (int)((f1 >> sh) & 127ull);
+      w[s][q2] = digit_bf16(n0 ? -d0 : d0) | (digit_bf16(n1 ? -d1 : d1) << 16);
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < OZ_SL; ++s)
+    *reinterpret_cast<uint4*>(dst + s * slice_bytes + off) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+}
+
+// Issue the 72 MMAs of one sub-chunk (36 digit pairs x 2 K-steps) into the 8
+// level accumulators; `first` restarts the accumulators (chunk start).
+__device__ __forceinline__ void issue_levels(uint32_t tmem, uint32_t a_base, uint32_t b_base, bool first) {
+#pragma unroll 1
+  for (int d = 0; d < OZ_LEV; ++d) {
+    const uint32_t dt = tmem + (uint32_t)(OZ_N * d);
+#pragma unroll 1
+    for (int s = 0; s <= d; ++s) {
+      const int u = d - s;
+#pragma unroll
+      for (int kk = 0; kk < 2; ++kk) {
+        const uint64_t ad = tc::sdesc_kmajor(a_base + s * A_SLICE_BYTES + kk * 256, 128, 512);
+        const uint64_t bd = tc::sdesc_kmajor(b_base + u * B_SLICE_BYTES + kk * 256, 128, 512);
+        tc::mma_f16(dt, ad, bd, kIdesc, (first && s == 0 && kk == 0) ? 0u : 1u);
+      }
     }
   }
 }
 
-// Per-state exponent: E_j = unbiased exponent of max_k |a_kj| + 1 (so |a| < 2^E).
-__global__ void k_col_exp(const double* __restrict__ Ar, int lda, int K, int n, int* __restrict__ E) {
+// Fold the 8 level accumulators of this thread's TMEM lane, 32 columns, into H / Lo.
+__device__ __forceinline__ void fold_levels(uint32_t lane_base, long long (&H)[32], long long (&Lo)[32]) {
+#pragma unroll 1
+  for (int d = 0; d < OZ_LEV; ++d) {
+    uint32_t r[32];
+    tc::tmem_ld32(lane_base + (uint32_t)(OZ_N * d), r);
+    tc::tmem_ld_wait();
+    const long long m = 1ll << (7 * (3 - (d & 3)));
+    if (d < 4) {
+#pragma unroll
+      for (int c = 0; c < 32; ++c) H[c] += (long long)__float2int_rn(__uint_as_float(r[c])) * m;
+    } else {
+#pragma unroll
+      for (int c = 0; c < 32; ++c) Lo[c] += (long long)__float2int_rn(__uint_as_float(r[c])) * m;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- exponent pre-passes
+// column maxima |a_kj| over k (state columns of the real view): bits into cmax[j]
+__global__ void k_col_max(const double* __restrict__ Ar, int lda, int K, int n, int kper,
+                          unsigned long long* __restrict__ cmax) {
   const int j = blockIdx.x;
+  const int k0 = blockIdx.y * kper, k1 = min(K, k0 + kper);
   unsigned long long mx = 0;
-  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+  for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(Ar[k + (size_t)j * lda]) & ~(1ull << 63);
     mx = b > mx ? b : mx;
   }
-  __shared__ unsigned long long red[256];
-  red[threadIdx.x] = mx;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] = red[threadIdx.x] > red[threadIdx.x + s] ? red[threadIdx.x] : red[threadIdx.x + s];
-    __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long v = __shfl_down_sync(0xffffffffu, mx, o);
+    mx = v > mx ? v : mx;
   }
-  if (threadIdx.x == 0) {
-    const int ex = (int)((red[0] >> 52) & 0x7FF);
-    E[j] = (ex == 0) ? -1021 : ex - 1023 + 1;
-  }
+  if ((threadIdx.x & 31) == 0 && mx) atomicMax(cmax + j, mx);
 }
 
+// row maxima of the real view over the n states: bits into rmax[r]
+__global__ void k_row_max(const double* __restrict__ Ar, int lda, int rows, int n,
+                          unsigned long long* __restrict__ rmax) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  unsigned long long mx = 0;
+  for (int k = 0; k < n; ++k) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(Ar[r + (size_t)k * lda]) & ~(1ull << 63);
+    mx = b > mx ? b : mx;
+  }
+  rmax[r] = mx;
+}
+
+// column maxima of a small row-major n x n matrix M over its rows
+__global__ void k_mat_col_max(const double* __restrict__ M, int n, unsigned long long* __restrict__ cmax) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  unsigned long long mx = 0;
+  for (int k = 0; k < n; ++k) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(M[(size_t)k * n + j]) & ~(1ull << 63);
+    mx = b > mx ? b : mx;
+  }
+  cmax[j] = mx;
+}
+
+// ---------------------------------------------------------------- S = C^T C (real view)
 __global__ void __launch_bounds__(OZ_THREADS, 1)
-    k_ozaki_syrk(const double* __restrict__ Ar, int lda, int K, int n, const int* __restrict__ E, int njb,
-                 int subs_per_split, unsigned long long* __restrict__ Hacc, unsigned long long* __restrict__ Lacc,
-                 int* __restrict__ err) {
+    k_ozaki_syrk(const double* __restrict__ Ar, int lda, int K, int n, const unsigned long long* __restrict__ cmax,
+                 int njb, int subs_per_split, unsigned long long* __restrict__ Hacc,
+                 unsigned long long* __restrict__ Lacc, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t sm[];
   uint8_t* sA = sm;
   uint8_t* sB = sm + 2 * A_BUF_BYTES;
@@ -166,6 +221,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_sh;
+  const uint32_t lane_base = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(32 * (warp >> 2));
 
   long long H[32], Lo[32];
 #pragma unroll
@@ -173,7 +229,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     H[c] = 0;
     Lo[c] = 0;
   }
-  constexpr uint32_t idesc = tc::idesc_bf16_f32(OZ_M, OZ_N);
   uint32_t ph[2] = {0u, 0u};
   int pend[2] = {0, 0};
   bool done_ok = true;
@@ -196,28 +251,31 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     const int kb = (sub0 + it) * OZ_KS;
     uint8_t* a_dst = sA + buf * A_BUF_BYTES;
     uint8_t* b_dst = sB + buf * B_BUF_BYTES;
-    produce(Ar, lda, K, n, kb, i0, OZ_M, E, a_dst, A_SLICE_BYTES);
-    produce(Ar, lda, K, n, kb, j0, OZ_N, E, b_dst, B_SLICE_BYTES);
+    // A: 128 state rows, B: 64 state rows; task = (row, k-group of 8), k contiguous in memory
+    for (int task = threadIdx.x; task < (OZ_M + OZ_N) * 4; task += OZ_THREADS) {
+      const bool isA = task < OZ_M * 4;
+      const int tt = isA ? task : task - OZ_M * 4;
+      const int row = tt >> 2, kg = tt & 3;
+      const int state = (isA ? i0 : j0) + row;
+      const bool valid = state < n;
+      const int e = valid ? exp_of_max(cmax[state]) : 0;
+      double x[8];
+#pragma unroll
+      for (int q2 = 0; q2 < 4; ++q2) {
+        const int k = kb + kg * 8 + 2 * q2;
+        double2 v2 = make_double2(0.0, 0.0);
+        if (valid && k < K) v2 = *reinterpret_cast<const double2*>(Ar + k + (size_t)state * lda);
+        x[2 * q2] = v2.x;
+        x[2 * q2 + 1] = v2.y;
+      }
+      store_digits(x, e, isA ? a_dst : b_dst, isA ? A_SLICE_BYTES : B_SLICE_BYTES, core_off(row, kg));
+    }
     tc::fence_proxy_async();
     __syncthreads();
     const int ci = it % OZ_SUBS;
     if (threadIdx.x == 0) {
       tc::fence_after_sync();
-      const uint32_t a_base = tc::smem_u32(a_dst), b_base = tc::smem_u32(b_dst);
-#pragma unroll 1
-      for (int d = 0; d < OZ_LEV; ++d) {
-        const uint32_t dt = tmem + (uint32_t)(OZ_N * d);
-#pragma unroll 1
-        for (int s = 0; s <= d; ++s) {
-          const int u = d - s;
-#pragma unroll
-          for (int kk = 0; kk < 2; ++kk) {
-            const uint64_t ad = tc::sdesc_kmajor(a_base + s * A_SLICE_BYTES + kk * 256, 128, 512);
-            const uint64_t bd = tc::sdesc_kmajor(b_base + u * B_SLICE_BYTES + kk * 256, 128, 512);
-            tc::mma_f16(dt, ad, bd, idesc, (ci == 0 && s == 0 && kk == 0) ? 0u : 1u);
-          }
-        }
-      }
+      issue_levels(tmem, tc::smem_u32(a_dst), tc::smem_u32(b_dst), ci == 0);
       tc::mma_commit(&mbar[buf]);
     }
     pend[buf] = 1;
@@ -240,21 +298,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         break;
       }
       tc::fence_after_sync();
-      const uint32_t lane_base = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(32 * (warp >> 2));
-#pragma unroll 1
-      for (int d = 0; d < OZ_LEV; ++d) {
-        uint32_t r[32];
-        tc::tmem_ld32(lane_base + (uint32_t)(OZ_N * d), r);
-        tc::tmem_ld_wait();
-        const int sh = 7 * (3 - (d & 3));
-        if (d < 4) {
-#pragma unroll
-          for (int c = 0; c < 32; ++c) H[c] += (long long)__float2int_rn(__uint_as_float(r[c])) * (1ll << sh);
-        } else {
-#pragma unroll
-          for (int c = 0; c < 32; ++c) Lo[c] += (long long)__float2int_rn(__uint_as_float(r[c])) * (1ll << sh);
-        }
-      }
+      fold_levels(lane_base, H, Lo);
       tc::fence_before_sync();
       __syncthreads();
     }
@@ -283,14 +327,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 
 // S[i][j] (i <= j, mirrored) = 2 * 2^(E_i+E_j) (H 2^-35 + Lo 2^-63) - Re c0_i Re c0_j
 __global__ void k_ozaki_syrk_finalize(const long long* __restrict__ H, const long long* __restrict__ Lo,
-                                      const int* __restrict__ E, int n, const double* __restrict__ Ar, int lda,
-                                      int geq0, double* __restrict__ S, unsigned long long* __restrict__ scond_bits) {
+                                      const unsigned long long* __restrict__ cmax, int n,
+                                      const double* __restrict__ Ar, int lda, int geq0, double* __restrict__ S,
+                                      unsigned long long* __restrict__ scond_bits) {
   double mx = 0.0;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * n;
        e += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(e / n), j = (int)(e % n);
     if (i > j) continue;
-    const int ee = E[i] + E[j];
+    const int ee = exp_of_max(cmax[i]) + exp_of_max(cmax[j]);
     double v = ldexp((double)H[e], ee - 35) + ldexp((double)Lo[e], ee - 63);
     v *= 2.0;
     if (geq0) v -= Ar[(size_t)i * lda] * Ar[(size_t)j * lda];
@@ -303,6 +348,153 @@ __global__ void k_ozaki_syrk_finalize(const long long* __restrict__ H, const lon
     if ((threadIdx.x & 31) == 0) atomicMax(scond_bits, (unsigned long long)__double_as_longlong(mx));
   }
 }
+
+// ---------------------------------------------------------------- Cout = A M (persistent over tiles)
+// A: real view (rows x n, column-major, lda); M: n x n row-major; Cout column-major (ldo).
+// upper: M is upper triangular, column tile j only needs k < j0 + 64.
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    k_ozaki_rmul(const double* __restrict__ A, int lda, int rows, int n, const double* __restrict__ M, int upper,
+                 const unsigned long long* __restrict__ rmax, const unsigned long long* __restrict__ mcmax,
+                 double* __restrict__ Cout, int ldo, int* __restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t sm[];
+  uint8_t* sA = sm;
+  uint8_t* sB = sm + 2 * A_BUF_BYTES;
+  __shared__ uint64_t mbar[2];
+  __shared__ uint32_t tmem_sh;
+  __shared__ int abort_sh;
+
+  const int nrt = (rows + OZ_M - 1) / OZ_M, nct = (n + OZ_N - 1) / OZ_N;
+  const int ntiles = nrt * nct;
+  if ((int)blockIdx.x >= ntiles) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) {
+    tc::tmem_alloc(&tmem_sh, 512);
+    tc::tmem_relinquish();
+  }
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&mbar[0], 1);
+    tc::mbar_init(&mbar[1], 1);
+    tc::fence_mbar_init();
+    abort_sh = 0;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_sh;
+  const uint32_t lane_base = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(32 * (warp >> 2));
+  uint32_t ph[2] = {0u, 0u};
+  int pend[2] = {0, 0};
+  int it = 0;
+
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    // column tile outer so that consecutive CTAs share the M slices of a column tile
+    const int ct = tile / nrt, rt = tile % nrt;
+    const int r0 = rt * OZ_M, j0 = ct * OZ_N;
+    const int kmax = upper ? min(n, j0 + OZ_N) : n;
+    const int nsub = (kmax + OZ_KS - 1) / OZ_KS;
+    long long H[32], Lo[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) {
+      H[c] = 0;
+      Lo[c] = 0;
+    }
+    for (int s = 0; s < nsub; ++s, ++it) {
+      const int buf = it & 1;
+      if (pend[buf]) {
+        if (!tc::mbar_wait(&mbar[buf], ph[buf])) {
+          abort_sh = 1;
+          atomicExch(err, 4);
+        }
+        ph[buf] ^= 1u;
+        pend[buf] = 0;
+      }
+      __syncthreads();
+      if (abort_sh) break;
+      const int kb = s * OZ_KS;
+      uint8_t* a_dst = sA + buf * A_BUF_BYTES;
+      uint8_t* b_dst = sB + buf * B_BUF_BYTES;
+      // A rows r (consecutive threads -> consecutive r: coalesced), 8 k each
+      for (int task = threadIdx.x; task < OZ_M * 4; task += OZ_THREADS) {
+        const int row = task & (OZ_M - 1), kg = task >> 7;
+        const int r = r0 + row;
+        const bool valid = r < rows;
+        const int e = valid ? exp_of_max(rmax[r]) : 0;
+        double x[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int k = kb + kg * 8 + q;
+          x[q] = (valid && k < n) ? A[r + (size_t)k * lda] : 0.0;
+        }
+        store_digits(x, e, a_dst, A_SLICE_BYTES, core_off(row, kg));
+      }
+      // B rows j = columns of M: B[j][k] = M[k][j]
+      for (int task = threadIdx.x; task < OZ_N * 4; task += OZ_THREADS) {
+        const int row = task & (OZ_N - 1), kg = task >> 6;
+        const int j = j0 + row;
+        const bool valid = j < n;
+        const int e = valid ? exp_of_max(mcmax[j]) : 0;
+        double x[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int k = kb + kg * 8 + q;
+          x[q] = (valid && k < n) ? M[(size_t)k * n + j] : 0.0;
+        }
+        store_digits(x, e, b_dst, B_SLICE_BYTES, core_off(row, kg));
+      }
+      tc::fence_proxy_async();
+      __syncthreads();
+      const int ci = s % OZ_SUBS;
+      if (threadIdx.x == 0) {
+        tc::fence_after_sync();
+        issue_levels(tmem, tc::smem_u32(a_dst), tc::smem_u32(b_dst), ci == 0);
+        tc::mma_commit(&mbar[buf]);
+      }
+      pend[buf] = 1;
+      if (ci == OZ_SUBS - 1 || s == nsub - 1) {
+        bool ok = tc::mbar_wait(&mbar[buf], ph[buf]);
+        ph[buf] ^= 1u;
+        pend[buf] = 0;
+        if (pend[buf ^ 1]) {
+          ok = tc::mbar_wait(&mbar[buf ^ 1], ph[buf ^ 1]) && ok;
+          ph[buf ^ 1] ^= 1u;
+          pend[buf ^ 1] = 0;
+        }
+        if (!ok) {
+          abort_sh = 1;
+          atomicExch(err, 4);
+        }
+        __syncthreads();
+        if (abort_sh) break;
+        tc::fence_after_sync();
+        fold_levels(lane_base, H, Lo);
+        tc::fence_before_sync();
+        __syncthreads();
+      }
+    }
+    if (abort_sh) break;
+    // write the tile: consecutive lanes -> consecutive rows of one column (coalesced)
+    const int r = r0 + 32 * (warp & 3) + lane;
+    if (r < rows) {
+      const int er = exp_of_max(rmax[r]);
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        const int j = j0 + 32 * (warp >> 2) + c;
+        if (j < n) {
+          const int ee = er + exp_of_max(mcmax[j]);
+          Cout[r + (size_t)j * ldo] = ldexp((double)H[c], ee - 35) + ldexp((double)Lo[c], ee - 63);
+        }
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    __syncwarp();
+    tc::tmem_dealloc(tmem, 512);
+  }
+}
+
+bool g_attr_syrk = false, g_attr_rmul = false;
 
 }  // namespace
 
@@ -322,37 +514,38 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, doubl
   subs_per = ((subs_per + OZ_SUBS - 1) / OZ_SUBS) * OZ_SUBS;
   nsplit = (total_subs + subs_per - 1) / subs_per;
   const size_t nn = (size_t)n * n;
-  // workspace: H, Lo (int64 n*n each), E (n ints), err, scond bits
-  const size_t bytes = 2 * nn * 8 + (size_t)n * 4 + 64;
+  // workspace: H, Lo (int64 n*n each), column maxima (n), err, scond bits
+  const size_t bytes = 2 * nn * 8 + (size_t)n * 8 + 64;
   if (!ensure(c, c.sparts, bytes)) return 6;
   unsigned long long* Hacc = static_cast<unsigned long long*>(c.sparts.p);
   unsigned long long* Lacc = Hacc + nn;
-  int* E = reinterpret_cast<int*>(Lacc + nn);
-  int* err = E + n;
-  unsigned long long* bits = reinterpret_cast<unsigned long long*>(err + 2 + (n & 1));
+  unsigned long long* cmax = Lacc + nn;
+  int* err = reinterpret_cast<int*>(cmax + n);
+  unsigned long long* bits = cmax + n + 1;
   GBCP_CUDA_TRY(c, cudaMemsetAsync(Hacc, 0, bytes, c.stream));
   {
-    ProfScope ps_(c, "k_col_exp");
-    k_col_exp<<<n, 256, 0, c.stream>>>(Ar, lda, K, n, E);
+    ProfScope ps_(c, "k_col_max");
+    const int ks = std::max(1, std::min(64, (K + 4095) / 4096));
+    const int kper = (K + ks - 1) / ks;
+    k_col_max<<<dim3(n, ks), 256, 0, c.stream>>>(Ar, lda, K, n, kper, cmax);
     GBCP_LAUNCH_CHECK(c);
   }
   {
-    static bool attr_set = false;
-    if (!attr_set) {
+    if (!g_attr_syrk) {
       cudaFuncSetAttribute(k_ozaki_syrk, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM);
-      attr_set = true;
+      g_attr_syrk = true;
     }
     ProfScope ps_(c, "k_ozaki_syrk");
-    k_ozaki_syrk<<<dim3(ntiles, nsplit), OZ_THREADS, OZ_SMEM, c.stream>>>(Ar, lda, K, n, E, njb, subs_per, Hacc, Lacc,
-                                                                          err);
+    k_ozaki_syrk<<<dim3(ntiles, nsplit), OZ_THREADS, OZ_SMEM, c.stream>>>(Ar, lda, K, n, cmax, njb, subs_per, Hacc,
+                                                                          Lacc, err);
     GBCP_LAUNCH_CHECK(c);
   }
   {
     ProfScope ps_(c, "k_ozaki_syrk_finalize");
     const int fb = std::max(1, std::min(1024, (int)((nn + 255) / 256)));
     k_ozaki_syrk_finalize<<<fb, 256, 0, c.stream>>>(reinterpret_cast<const long long*>(Hacc),
-                                                    reinterpret_cast<const long long*>(Lacc), E, n, Ar, lda, c.geq0, S,
-                                                    scond_host ? bits : nullptr);
+                                                    reinterpret_cast<const long long*>(Lacc), cmax, n, Ar, lda, c.geq0,
+                                                    S, scond_host ? bits : nullptr);
     GBCP_LAUNCH_CHECK(c);
   }
   int herr = 0;
@@ -368,6 +561,45 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, doubl
     double d;
     memcpy(&d, &hb, sizeof(d));
     *scond_host = d;
+  }
+  return 0;
+}
+
+// Cout (rows x n, ldo) = A (rows x n, lda) * M (n x n row-major) on the tensor cores.
+int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout, int ldo) {
+  const size_t bytes = ((size_t)rows + n + 2) * 8 + 64;
+  if (!ensure(c, c.nl_a, bytes)) return 6;
+  unsigned long long* rmax = static_cast<unsigned long long*>(c.nl_a.p);
+  unsigned long long* mcmax = rmax + rows;
+  int* err = reinterpret_cast<int*>(mcmax + n);
+  GBCP_CUDA_TRY(c, cudaMemsetAsync(err, 0, sizeof(int), c.stream));
+  {
+    ProfScope ps_(c, "k_row_max");
+    k_row_max<<<(rows + 255) / 256, 256, 0, c.stream>>>(A, lda, rows, n, rmax);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  {
+    ProfScope ps_(c, "k_mat_col_max");
+    k_mat_col_max<<<(n + 255) / 256, 256, 0, c.stream>>>(M, n, mcmax);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  {
+    if (!g_attr_rmul) {
+      cudaFuncSetAttribute(k_ozaki_rmul, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM);
+      g_attr_rmul = true;
+    }
+    const int ntiles = ((rows + OZ_M - 1) / OZ_M) * ((n + OZ_N - 1) / OZ_N);
+    const int grid = std::max(1, std::min(ntiles, 148));
+    ProfScope ps_(c, "k_ozaki_rmul");
+    k_ozaki_rmul<<<grid, OZ_THREADS, OZ_SMEM, c.stream>>>(A, lda, rows, n, M, upper, rmax, mcmax, Cout, ldo, err);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  int herr = 0;
+  GBCP_CUDA_TRY(c, cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  if (herr) {
+    c.err = "C M (tensor cores): an mbarrier wait timed out";
+    return 4;
   }
   return 0;
 }

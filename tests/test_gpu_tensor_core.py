@@ -68,3 +68,18 @@ def test_mixed_ortho_orthonormality_gate(gpu_lib):
     s = ctx.ovlap(c)
     dev = float((s - torch.eye(cl.nstate, dtype=torch.float64, device=s.device)).abs().max())
     assert dev <= 1e-12
+
+
+@pytest.mark.parametrize("nstate,method", [(16, "gs"), (37, "gs"), (130, "gs"), (200, "gs"), (70, "lowdin")])
+def test_ortho_tensor_cores_match_oracle(gpu_lib, nstate, method):
+    """Both GEMMs of ortho (S and C M) on the tensor cores give the FP64 result."""
+    from cpmd_gb300 import Context
+    cl = make_small_cell(10.26, 32, 20.0, nstate, seed=90 + nstate)
+    c = perturbed(cl.c0, 0.03, nstate)
+    ref = O.rgs(c, cl.basis.geq0) if method == "gs" else O.lowdin(c, cl.basis.geq0)[0]
+    ctx = Context(cl.basis, "fp64")
+    ctx.set_option("gemm", 1)
+    out = c.copy(order="F")
+    ctx.ortho(out, method)
+    assert rel(out, ref) < 1e-12
+    assert np.all(out[0].imag == 0.0)
