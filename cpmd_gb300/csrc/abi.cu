@@ -15,6 +15,7 @@
 
 #include "../../include/cpmd_gb300.h"
 #include "ctx.h"
+#include "fs_plan.h"
 
 namespace gbcp {
 
@@ -260,6 +261,30 @@ static int build_fft(Ctx& c) {
     }
     c.tw64[a] = const_cast<cx<double>*>(d64);
     c.tw32[a] = const_cast<cx<float>*>(d32);
+    const int n1 = fs_n1(n);
+    if (n1 > 0) {
+      const int n2 = n / n1;
+      std::vector<cx<double>> a64(n), b64(n);
+      std::vector<cx<float>> a32(n), b32(n);
+      for (int k1 = 0; k1 < n1; ++k1)
+        for (int j = 0; j < n2; ++j) {
+          const cx<double> w = t64[(k1 * j) % n];
+          a64[k1 * n2 + j] = w;
+          b64[j * n1 + k1] = w;
+          a32[k1 * n2 + j] = mk<float>((float)w.x, (float)w.y);
+          b32[j * n1 + k1] = mk<float>((float)w.x, (float)w.y);
+        }
+      const cx<double>*pa64, *pb64;
+      const cx<float>*pa32, *pb32;
+      if (!upload(c, a64, pa64) || !upload(c, b64, pb64) || !upload(c, a32, pa32) || !upload(c, b32, pb32)) {
+        c.err = "twiddle upload failed";
+        return 6;
+      }
+      c.twA64[a] = const_cast<cx<double>*>(pa64);
+      c.twB64[a] = const_cast<cx<double>*>(pb64);
+      c.twA32[a] = const_cast<cx<float>*>(pa32);
+      c.twB32[a] = const_cast<cx<float>*>(pb32);
+    }
   }
   return 0;
 }

@@ -161,9 +161,6 @@ template <typename T> static size_t stage_smem(int n, int nl) {
   return sizeof(cx<T>) * ((size_t)n + 2 * (size_t)nl * line_stride(n));
 }
 
-template <typename KernelT> static void allow_smem(KernelT k, size_t bytes) {
-  if (bytes > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-}
 
 int band_rhoofr(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho) {
   GBCP_CUDA_TRY(c, cudaMemsetAsync(rho, 0, sizeof(double) * (size_t)c.kr[0] * c.kr[1] * c.kr[2], c.stream));

@@ -1,0 +1,386 @@
+// Four-step band-loop stage kernels (compile-time mesh sizes).
+//
+// A line of length N = N1*N2 is transformed by two groups of threads with one
+// shared-memory exchange in between:
+//   step A  thread (line, n2) holds x[n2 + N2 n1], n1 < N1, in registers:
+//           DFT of length N1, twiddle e^{S 2 pi i n2 k1 / N}, store T[k1][n2];
+//   step B  thread (line, k1) reads T[k1][*]: DFT of length N2, giving
+//           X[k1 + N1 k2], k2 < N2, in registers.
+// The forward transform that vpsi applies after V(r) starts from that
+// register layout (stride N1) without an exchange: DFT of length N2 over k2,
+// twiddle e^{-2 pi i k1 j / N}, store, DFT of length N1, output X[j + N2 j2].
+// The DFTs are the register codelets of fft_codelets.cuh.  Each stage kernel
+// maps its two thread groups so that global loads and stores are coalesced.
+//
+// Plans (N1 x N2, lines per CTA L) keep both thread groups near 256 tasks.
+#pragma once
+#include "fft_codelets.cuh"
+#include "fs_plan.h"
+
+namespace gbcp {
+namespace band {
+
+template <typename T, int N> struct FS {
+  static constexpr int N1 = fs_n1(N), N2 = N / N1, L = fs_lines(N);
+  static constexpr int LS = N + ((N % 2 == 0) ? 1 : 0);  // odd line stride in shared memory
+  static constexpr int TA = L * N2, TB = L * N1;
+  static constexpr int IA = (TA + kThreads - 1) / kThreads, IB = (TB + kThreads - 1) / kThreads;
+};
+
+template <typename T> __device__ __forceinline__ cx<T> twmul(cx<T> v, cx<T> w, bool conj) {
+  return conj ? cmulc(v, w) : cmul(v, w);
+}
+
+// step A on registers v[N1] of line position n2; writes T[k1*N2 + n2] of the line
+template <int S, typename T, int N1, int N2>
+__device__ __forceinline__ void fs_step_a(cx<T> (&v)[N1], int n2, const cx<T>* __restrict__ twA, cx<T>* line) {
+  dftn<S, N1>(v);
+#pragma unroll
+  for (int k1 = 0; k1 < N1; ++k1) {
+    cx<T> r = v[k1];
+    if (k1 > 0 && n2 > 0) r = twmul(r, twA[k1 * N2 + n2], S < 0);
+    line[k1 * N2 + n2] = r;
+  }
+}
+
+// step B: read T[k1*N2 + *] of the line, DFT of length N2
+template <int S, typename T, int N1, int N2>
+__device__ __forceinline__ void fs_step_b(const cx<T>* line, int k1, cx<T> (&w)[N2]) {
+#pragma unroll
+  for (int n2 = 0; n2 < N2; ++n2) w[n2] = line[k1 * N2 + n2];
+  dftn<S, N2>(w);
+}
+
+template <typename T>
+__device__ __forceinline__ void load_table(cx<T>* dst, const cx<T>* __restrict__ src, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+
+// ---------------------------------------------------------------- Z stage (inverse, gather)
+template <typename T, int N>
+__global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>* __restrict__ c0, int ldc, int s0,
+                                                     int nstate, cx<T>* __restrict__ zbuf,
+                                                     const cx<T>* __restrict__ twAg) {
+  using P = FS<T, N>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* twA = reinterpret_cast<cx<T>*>(smem_raw);
+  cx<T>* Ts = twA + N;
+  const int col0 = blockIdx.x * P::L, pair = blockIdx.y;
+  const int is1 = s0 + 2 * pair, is2 = is1 + 1;
+  const bool two = is2 < nstate;
+  const cx<double>* c1 = c0 + (size_t)is1 * ldc;
+  const cx<double>* c2 = c0 + (size_t)(two ? is2 : is1) * ldc;
+  load_table(twA, twAg, N);
+  __syncthreads();
+#pragma unroll
+  for (int ia = 0; ia < P::IA; ++ia) {
+    const int t = threadIdx.x + ia * kThreads;
+    if (t < P::TA) {
+      const int n2 = t / P::L, l = t - n2 * P::L, col = col0 + l;
+      cx<T> v[P::N1];
+      int st = 0, len = 0, zlo = 0;
+      if (col < g.ncol) {
+        st = g.col_start[col];
+        len = g.col_start[col + 1] - st;
+        zlo = g.col_zlo[col];
+      }
+#pragma unroll
+      for (int n1 = 0; n1 < P::N1; ++n1) {
+        const int z = n2 + P::N2 * n1;
+        const int off = freq_of(z, N) - zlo;
+        cx<T> val = mk<T>(0, 0);
+        if (off >= 0 && off < len) {
+          const int e = g.col_ent[st + off];
+          if (e != 0) {
+            const int ig = (e > 0 ? e : -e) - 1;
+            const cx<double> u = c1[ig];
+            const cx<double> w = two ? c2[ig] : mk<double>(0.0, 0.0);
+            val = (e > 0) ? mk<T>((T)(u.x - w.y), (T)(u.y + w.x)) : mk<T>((T)(u.x + w.y), (T)(w.x - u.y));
+          }
+        }
+        v[n1] = val;
+      }
+      fs_step_a<1, T, P::N1, P::N2>(v, n2, twA, Ts + l * P::LS);
+    }
+  }
+  __syncthreads();
+  cx<T>* zb = zbuf + (size_t)pair * N * g.ncol;
+#pragma unroll
+  for (int ib = 0; ib < P::IB; ++ib) {
+    const int t = threadIdx.x + ib * kThreads;
+    if (t < P::TB) {
+      const int k1 = t / P::L, l = t - k1 * P::L, col = col0 + l;
+      cx<T> w[P::N2];
+      fs_step_b<1, T, P::N1, P::N2>(Ts + l * P::LS, k1, w);
+      if (col < g.ncol) {
+#pragma unroll
+        for (int k2 = 0; k2 < P::N2; ++k2) zb[(size_t)(k1 + P::N1 * k2) * g.ncol + col] = w[k2];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- Y stage (inverse)
+template <typename T, int N>
+__global__ void __launch_bounds__(kThreads) k_yinv_fs(GeoDev g, const cx<T>* __restrict__ zbuf,
+                                                     cx<T>* __restrict__ ybuf, const cx<T>* __restrict__ twAg) {
+  using P = FS<T, N>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* twA = reinterpret_cast<cx<T>*>(smem_raw);
+  cx<T>* Ts = twA + N;
+  const int sb = blockIdx.x * P::L, z = blockIdx.y, pair = blockIdx.z;
+  const cx<T>* zrow = zbuf + ((size_t)pair * g.n3 + z) * g.ncol;
+  load_table(twA, twAg, N);
+  __syncthreads();
+#pragma unroll
+  for (int ia = 0; ia < P::IA; ++ia) {
+    const int t = threadIdx.x + ia * kThreads;
+    if (t < P::TA) {
+      const int n2 = t / P::L, l = t - n2 * P::L, s = sb + l;
+      int c0s = 0, gylo = 0, ncs = 0;
+      if (s < g.nslot) {
+        c0s = g.slot_col0[s];
+        gylo = g.slot_gylo[s];
+        ncs = g.slot_ncol[s];
+      }
+      cx<T> v[P::N1];
+#pragma unroll
+      for (int n1 = 0; n1 < P::N1; ++n1) {
+        const int off = freq_of(n2 + P::N2 * n1, N) - gylo;
+        v[n1] = (off >= 0 && off < ncs) ? zrow[c0s + off] : mk<T>(0, 0);
+      }
+      fs_step_a<1, T, P::N1, P::N2>(v, n2, twA, Ts + l * P::LS);
+    }
+  }
+  __syncthreads();
+  cx<T>* yb = ybuf + ((size_t)pair * g.n3 + z) * (size_t)N * g.nslot;
+#pragma unroll
+  for (int ib = 0; ib < P::IB; ++ib) {
+    const int t = threadIdx.x + ib * kThreads;
+    if (t < P::TB) {
+      const int k1 = t / P::L, l = t - k1 * P::L, s = sb + l;
+      cx<T> w[P::N2];
+      fs_step_b<1, T, P::N1, P::N2>(Ts + l * P::LS, k1, w);
+      if (s < g.nslot) {
+#pragma unroll
+        for (int k2 = 0; k2 < P::N2; ++k2) yb[(size_t)(k1 + P::N1 * k2) * g.nslot + s] = w[k2];
+      }
+    }
+  }
+}
+
+// step A of an x-line: gather the sphere slots of row y (l-major thread map)
+template <typename T, int N>
+__device__ __forceinline__ void xline_step_a(const GeoDev& g, const cx<T>* __restrict__ yb, int y0,
+                                             const cx<T>* twA, cx<T>* Ts) {
+  using P = FS<T, N>;
+#pragma unroll
+  for (int ia = 0; ia < P::IA; ++ia) {
+    const int t = threadIdx.x + ia * kThreads;
+    if (t < P::TA) {
+      const int l = t / P::N2, n2 = t - l * P::N2, y = y0 + l;
+      cx<T> v[P::N1];
+#pragma unroll
+      for (int n1 = 0; n1 < P::N1; ++n1) {
+        const int s = freq_of(n2 + P::N2 * n1, N) - g.gxlo;
+        v[n1] = (y < g.n2 && s >= 0 && s < g.nslot) ? yb[(size_t)y * g.nslot + s] : mk<T>(0, 0);
+      }
+      fs_step_a<1, T, P::N1, P::N2>(v, n2, twA, Ts + l * P::LS);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- X stage + density
+template <typename T, int N>
+__global__ void __launch_bounds__(kThreads) k_xrho_fs(GeoDev g, const cx<T>* __restrict__ ybuf, int npairs, int s0,
+                                                     int nstate, const double* __restrict__ f, double inv_omega,
+                                                     double* __restrict__ rho, const cx<T>* __restrict__ twAg) {
+  using P = FS<T, N>;
+  static_assert(P::IB == 1, "density tile: one step-B task per thread");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* twA = reinterpret_cast<cx<T>*>(smem_raw);
+  cx<T>* Ts = twA + N;
+  const int y0 = blockIdx.x * P::L, z = blockIdx.y;
+  load_table(twA, twAg, N);
+  // this launch's pairs accumulate in T (FP32 in the mixed mode), added to the FP64 density once
+  T acc[P::N2];
+#pragma unroll
+  for (int k2 = 0; k2 < P::N2; ++k2) acc[k2] = (T)0;
+  const int t = threadIdx.x;
+  const int lb = t / P::N1, k1 = t - lb * P::N1;
+  for (int pair = 0; pair < npairs; ++pair) {
+    const int is1 = s0 + 2 * pair, is2 = is1 + 1;
+    const T f1 = (T)(f[is1] * inv_omega);
+    const T f2 = (T)((is2 < nstate) ? f[is2] * inv_omega : 0.0);
+    const cx<T>* yb = ybuf + ((size_t)pair * g.n3 + z) * (size_t)g.n2 * g.nslot;
+    __syncthreads();  // twiddles loaded / previous pair's step B done
+    xline_step_a<T, N>(g, yb, y0, twA, Ts);
+    __syncthreads();
+    if (t < P::TB) {
+      cx<T> w[P::N2];
+      fs_step_b<1, T, P::N1, P::N2>(Ts + lb * P::LS, k1, w);
+#pragma unroll
+      for (int k2 = 0; k2 < P::N2; ++k2) acc[k2] += f1 * w[k2].x * w[k2].x + f2 * w[k2].y * w[k2].y;
+    }
+  }
+  const int y = y0 + lb;
+  if (t < P::TB && y < g.n2) {
+    double* rrow = rho + (size_t)g.k1 * (y + (size_t)g.k2 * z);
+#pragma unroll
+    for (int k2 = 0; k2 < P::N2; ++k2) rrow[k1 + P::N1 * k2] += (double)acc[k2];
+  }
+}
+
+// ---------------------------------------------------------------- X stage: inverse, x V, forward
+template <typename T, int N>
+__global__ void __launch_bounds__(kThreads) k_xvx_fs(GeoDev g, cx<T>* __restrict__ ybuf,
+                                                    const double* __restrict__ vpot, const cx<T>* __restrict__ twAg,
+                                                    const cx<T>* __restrict__ twBg) {
+  using P = FS<T, N>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* twA = reinterpret_cast<cx<T>*>(smem_raw);
+  cx<T>* twB = twA + N;
+  cx<T>* Ts = twB + N;
+  cx<T>* Ts2 = Ts + P::L * P::LS;
+  const int y0 = blockIdx.x * P::L, z = blockIdx.y, pair = blockIdx.z;
+  cx<T>* yb = ybuf + ((size_t)pair * g.n3 + z) * (size_t)g.n2 * g.nslot;
+  load_table(twA, twAg, N);
+  load_table(twB, twBg, N);
+  __syncthreads();
+  xline_step_a<T, N>(g, yb, y0, twA, Ts);
+  __syncthreads();
+#pragma unroll
+  for (int ib = 0; ib < P::IB; ++ib) {
+    const int t = threadIdx.x + ib * kThreads;
+    if (t < P::TB) {
+      const int l = t / P::N1, k1 = t - l * P::N1, y = y0 + l;
+      cx<T> w[P::N2];
+      fs_step_b<1, T, P::N1, P::N2>(Ts + l * P::LS, k1, w);
+      const double* vrow = vpot + (size_t)g.k1 * ((y < g.n2 ? y : 0) + (size_t)g.k2 * z);
+#pragma unroll
+      for (int k2 = 0; k2 < P::N2; ++k2) w[k2] = scl(w[k2], (y < g.n2) ? (T)vrow[k1 + P::N1 * k2] : (T)0);
+      // forward: DFT over k2 (stride-N1 elements), twiddle, exchange
+      dftn<-1, P::N2>(w);
+      cx<T>* line = Ts2 + l * P::LS;
+#pragma unroll
+      for (int j = 0; j < P::N2; ++j) {
+        cx<T> r = w[j];
+        if (j > 0 && k1 > 0) r = cmulc(r, twB[j * P::N1 + k1]);
+        line[j * P::N1 + k1] = r;
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int ia = 0; ia < P::IA; ++ia) {
+    const int t = threadIdx.x + ia * kThreads;
+    if (t < P::TA) {
+      const int l = t / P::N2, j = t - l * P::N2, y = y0 + l;
+      const cx<T>* line = Ts2 + l * P::LS;
+      cx<T> u[P::N1];
+#pragma unroll
+      for (int k1 = 0; k1 < P::N1; ++k1) u[k1] = line[j * P::N1 + k1];
+      dftn<-1, P::N1>(u);
+      if (y < g.n2) {
+#pragma unroll
+        for (int j2 = 0; j2 < P::N1; ++j2) {
+          const int s = freq_of(j + P::N2 * j2, N) - g.gxlo;
+          if (s >= 0 && s < g.nslot) yb[(size_t)y * g.nslot + s] = u[j2];
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- Y stage (forward)
+template <typename T, int N>
+__global__ void __launch_bounds__(kThreads) k_yfwd_fs(GeoDev g, const cx<T>* __restrict__ ybuf,
+                                                     cx<T>* __restrict__ zbuf, const cx<T>* __restrict__ twAg) {
+  using P = FS<T, N>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* twA = reinterpret_cast<cx<T>*>(smem_raw);
+  cx<T>* Ts = twA + N;
+  const int sb = blockIdx.x * P::L, z = blockIdx.y, pair = blockIdx.z;
+  const cx<T>* yb = ybuf + ((size_t)pair * g.n3 + z) * (size_t)N * g.nslot;
+  load_table(twA, twAg, N);
+  __syncthreads();
+#pragma unroll
+  for (int ia = 0; ia < P::IA; ++ia) {
+    const int t = threadIdx.x + ia * kThreads;
+    if (t < P::TA) {
+      const int n2 = t / P::L, l = t - n2 * P::L, s = sb + l;
+      cx<T> v[P::N1];
+#pragma unroll
+      for (int n1 = 0; n1 < P::N1; ++n1)
+        v[n1] = (s < g.nslot) ? yb[(size_t)(n2 + P::N2 * n1) * g.nslot + s] : mk<T>(0, 0);
+      fs_step_a<-1, T, P::N1, P::N2>(v, n2, twA, Ts + l * P::LS);
+    }
+  }
+  __syncthreads();
+  cx<T>* zrow = zbuf + ((size_t)pair * g.n3 + z) * g.ncol;
+#pragma unroll
+  for (int ib = 0; ib < P::IB; ++ib) {
+    const int t = threadIdx.x + ib * kThreads;
+    if (t < P::TB) {
+      const int k1 = t / P::L, l = t - k1 * P::L, s = sb + l;
+      cx<T> w[P::N2];
+      fs_step_b<-1, T, P::N1, P::N2>(Ts + l * P::LS, k1, w);
+      if (s < g.nslot) {
+        const int c0s = g.slot_col0[s], gylo = g.slot_gylo[s], ncs = g.slot_ncol[s];
+#pragma unroll
+        for (int k2 = 0; k2 < P::N2; ++k2) {
+          const int off = freq_of(k1 + P::N1 * k2, N) - gylo;
+          if (off >= 0 && off < ncs) zrow[c0s + off] = w[k2];
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- Z stage (forward, to sphere entries)
+template <typename T, int N>
+__global__ void __launch_bounds__(kThreads) k_zfwd_fs(GeoDev g, const cx<T>* __restrict__ zbuf, T scale,
+                                                     cx<T>* __restrict__ qbuf, const cx<T>* __restrict__ twAg) {
+  using P = FS<T, N>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* twA = reinterpret_cast<cx<T>*>(smem_raw);
+  cx<T>* Ts = twA + N;
+  const int col0 = blockIdx.x * P::L, pair = blockIdx.y;
+  const cx<T>* zb = zbuf + (size_t)pair * N * g.ncol;
+  load_table(twA, twAg, N);
+  __syncthreads();
+#pragma unroll
+  for (int ia = 0; ia < P::IA; ++ia) {
+    const int t = threadIdx.x + ia * kThreads;
+    if (t < P::TA) {
+      const int n2 = t / P::L, l = t - n2 * P::L, col = col0 + l;
+      cx<T> v[P::N1];
+#pragma unroll
+      for (int n1 = 0; n1 < P::N1; ++n1)
+        v[n1] = (col < g.ncol) ? zb[(size_t)(n2 + P::N2 * n1) * g.ncol + col] : mk<T>(0, 0);
+      fs_step_a<-1, T, P::N1, P::N2>(v, n2, twA, Ts + l * P::LS);
+    }
+  }
+  __syncthreads();
+  cx<T>* qb = qbuf + (size_t)pair * g.nent;
+#pragma unroll
+  for (int ib = 0; ib < P::IB; ++ib) {
+    const int t = threadIdx.x + ib * kThreads;
+    if (t < P::TB) {
+      const int k1 = t / P::L, l = t - k1 * P::L, col = col0 + l;
+      cx<T> w[P::N2];
+      fs_step_b<-1, T, P::N1, P::N2>(Ts + l * P::LS, k1, w);
+      if (col < g.ncol) {
+        const int st = g.col_start[col], len = g.col_start[col + 1] - st, zlo = g.col_zlo[col];
+#pragma unroll
+        for (int k2 = 0; k2 < P::N2; ++k2) {
+          const int off = freq_of(k1 + P::N1 * k2, N) - zlo;
+          if (off >= 0 && off < len) qb[st + off] = scl(w[k2], scale);
+        }
+      }
+    }
+  }
+}
+
+}  // namespace band
+}  // namespace gbcp

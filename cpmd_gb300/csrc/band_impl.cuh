@@ -19,16 +19,17 @@
 // psi(r) never reaches HBM.  The all-to-all of the reference
 // (fftutil_utils.mod.F90:292-319) becomes the layout change between stages.
 //
-// Every stage kernel is a template on the precision T and on NC, the length
-// of the axis it transforms: NC > 0 selects the compile-time plan of
-// fft_ct.cuh (all index arithmetic constant), NC = 0 the run-time plan.
+// The mesh sizes of the supported cells (2,3,5-smooth, the reference's own
+// size table gfft_utils.mod.F90:39-84) run the four-step kernels of
+// band_fs.cuh (register codelets, one shared-memory exchange per transform);
+// any other size runs the Stockham kernels below with a run-time radix plan.
 // This header is included by band64.cu and band32.cu, one per precision.
 #pragma once
 #include <algorithm>
 #include <cmath>
 
 #include "ctx.h"
-#include "fft_ct.cuh"
+#include "fft_core.cuh"
 
 namespace gbcp {
 namespace band {
@@ -38,7 +39,6 @@ constexpr int kElems = 2048;   // complex elements per CTA tile (lines * length)
 constexpr int kMaxAcc = 16;    // density accumulators per thread (run-time plan)
 
 __host__ __device__ constexpr int line_stride(int n) { return (n % 2 == 0) ? n + 1 : n; }
-__host__ __device__ constexpr int ct_lines(int n) { return (kElems / n) > 0 ? (kElems / n) : 1; }
 __device__ __forceinline__ int freq_of(int i, int n) { return (i < (n + 1) / 2) ? i : i - n; }
 __device__ __forceinline__ int idx_of(int g, int n) { return g < 0 ? g + n : g; }
 
@@ -50,18 +50,14 @@ __device__ __forceinline__ void load_tw(cx<T>* tw, const cx<T>* __restrict__ twg
 template <bool INV, typename T, int NC>
 __device__ __forceinline__ cx<T>* run_fft(cx<T>* a, cx<T>* b, int nl, int ls, const FftPlan& p,
                                           const cx<T>* tw) {
-  if constexpr (NC > 0) {
-    return fft_ct<INV, T, NC, ct_lines(NC), kThreads>(a, b, tw);
-  } else {
-    return fft_lines<INV>(a, b, nl, ls, p, tw);
-  }
+  return fft_lines<INV>(a, b, nl, ls, p, tw);
 }
 
 // stage geometry: length N, line stride LS, lines per CTA NL
 #define GBCP_STAGE(NAXIS, NLRT)                                   \
-  const int N = (NC > 0) ? NC : (NAXIS);                          \
-  const int ls = (NC > 0) ? line_stride(NC) : line_stride(N);     \
-  const int nl = (NC > 0) ? ct_lines(NC) : (NLRT);                \
+  const int N = (NAXIS);                                          \
+  const int ls = line_stride(N);                                  \
+  const int nl = (NLRT);                                          \
   extern __shared__ __align__(16) unsigned char smem_raw[];       \
   cx<T>* tw = reinterpret_cast<cx<T>*>(smem_raw);                 \
   cx<T>* a = tw + N;                                              \
@@ -154,7 +150,7 @@ __global__ void __launch_bounds__(kThreads) k_xinv_rho(GeoDev g, FftPlan p, cons
                                                       double inv_omega, double* __restrict__ rho, int nlrt,
                                                       const cx<T>* __restrict__ twg) {
   GBCP_STAGE(g.n1, nlrt)
-  constexpr int NACC = (NC > 0) ? (ct_lines(NC) * NC + kThreads - 1) / kThreads : kMaxAcc;
+  constexpr int NACC = kMaxAcc;
   const int y0 = blockIdx.x * nl, z = blockIdx.y;
   load_tw(tw, twg, N);
   // density of this launch's pairs: FP64 in the FP64 path; FP32 in the mixed path, added once
@@ -303,6 +299,14 @@ __global__ void k_decode(GeoDev g, const cx<T>* __restrict__ qbuf, const cx<doub
   }
 }
 
+}  // namespace band
+}  // namespace gbcp
+
+#include "band_fs.cuh"
+
+namespace gbcp {
+namespace band {
+
 // =========================================================================== host side
 
 inline int lines_rt(int n) { return std::max(1, std::min(64, kElems / n)); }
@@ -311,20 +315,20 @@ template <typename T> inline size_t stage_smem(int n, int nl) {
   return sizeof(cx<T>) * ((size_t)n + 2 * (size_t)nl * line_stride(n));
 }
 
-template <typename KernelT> inline void allow_smem(KernelT k, size_t bytes) {
-  if (bytes > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-}
 
 template <typename T> inline const cx<T>* tw_of(Ctx& c, int axis);
 template <> inline const cx<double>* tw_of<double>(Ctx& c, int axis) { return c.tw64[axis]; }
 template <> inline const cx<float>* tw_of<float>(Ctx& c, int axis) { return c.tw32[axis]; }
 
-// lines per CTA of a stage (compile-time plan or run-time tile)
-template <int NC> inline int stage_lines(int n) { return NC > 0 ? ct_lines(NC) : lines_rt(n); }
+template <typename T> inline const cx<T>* twA_of(Ctx& c, int axis);
+template <> inline const cx<double>* twA_of<double>(Ctx& c, int axis) { return c.twA64[axis]; }
+template <> inline const cx<float>* twA_of<float>(Ctx& c, int axis) { return c.twA32[axis]; }
+template <typename T> inline const cx<T>* twB_of(Ctx& c, int axis);
+template <> inline const cx<double>* twB_of<double>(Ctx& c, int axis) { return c.twB64[axis]; }
+template <> inline const cx<float>* twB_of<float>(Ctx& c, int axis) { return c.twB32[axis]; }
 
-#define GBCP_CT_SIZES(X) X(32) X(36) X(40) X(48) X(60) X(64) X(72) X(80) X(96) X(120) X(144) X(240)
-
-// Dispatch `launch_<name><T, NC>(args...)` on the run-time length n.
+// Dispatch `FN<T, NC>(args...)` on the run-time length n: NC > 0 runs the
+// four-step kernels of band_fs.cuh, NC = 0 the run-time planned Stockham kernels.
 #define GBCP_DISPATCH(FN, T, n, ...)                        \
   switch (n) {                                              \
     case 32: return FN<T, 32>(__VA_ARGS__);                 \
@@ -354,27 +358,48 @@ template <typename T> int ensure_band_buffers(Ctx& c, int npairs) {
   return 0;
 }
 
+template <typename T, int N> constexpr size_t fs_smem(int buffers, int tables) {
+  return sizeof(cx<T>) * ((size_t)tables * N + (size_t)buffers * FS<T, N>::L * FS<T, N>::LS);
+}
+
 template <typename T, int NC>
 int launch_zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int np) {
   const GeoDev& g = c.geo;
-  const int nl = stage_lines<NC>(g.n3);
-  const size_t sm = stage_smem<T>(g.n3, nl);
-  allow_smem(k_zinv<T, NC>, sm);
+  cx<T>* zb = static_cast<cx<T>*>(c.zbuf.p);
   ProfScope ps_(c, "k_zinv");
-  k_zinv<T, NC><<<dim3((g.ncol + nl - 1) / nl, np), kThreads, sm, c.stream>>>(
-      g, c.plan[2], c0, ldc, s0, nstate, nl, static_cast<cx<T>*>(c.zbuf.p), tw_of<T>(c, 2));
+  if constexpr (NC > 0) {
+    constexpr size_t sm = fs_smem<T, NC>(1, 1);
+    allow_smem(k_zinv_fs<T, NC>, sm);
+    k_zinv_fs<T, NC><<<dim3((g.ncol + FS<T, NC>::L - 1) / FS<T, NC>::L, np), kThreads, sm, c.stream>>>(
+        g, c0, ldc, s0, nstate, zb, twA_of<T>(c, 2));
+  } else {
+    const int nl = lines_rt(g.n3);
+    const size_t sm = stage_smem<T>(g.n3, nl);
+    allow_smem(k_zinv<T, 0>, sm);
+    k_zinv<T, 0><<<dim3((g.ncol + nl - 1) / nl, np), kThreads, sm, c.stream>>>(g, c.plan[2], c0, ldc, s0, nstate, nl,
+                                                                                zb, tw_of<T>(c, 2));
+  }
   GBCP_LAUNCH_CHECK(c);
   return 0;
 }
 
 template <typename T, int NC> int launch_yinv(Ctx& c, int np) {
   const GeoDev& g = c.geo;
-  const int nl = stage_lines<NC>(g.n2);
-  const size_t sm = stage_smem<T>(g.n2, nl);
-  allow_smem(k_yinv<T, NC>, sm);
+  const cx<T>* zb = static_cast<const cx<T>*>(c.zbuf.p);
+  cx<T>* yb = static_cast<cx<T>*>(c.ybuf.p);
   ProfScope ps_(c, "k_yinv");
-  k_yinv<T, NC><<<dim3((g.nslot + nl - 1) / nl, g.n3, np), kThreads, sm, c.stream>>>(
-      g, c.plan[1], static_cast<const cx<T>*>(c.zbuf.p), nl, static_cast<cx<T>*>(c.ybuf.p), tw_of<T>(c, 1));
+  if constexpr (NC > 0) {
+    constexpr size_t sm = fs_smem<T, NC>(1, 1);
+    allow_smem(k_yinv_fs<T, NC>, sm);
+    k_yinv_fs<T, NC><<<dim3((g.nslot + FS<T, NC>::L - 1) / FS<T, NC>::L, g.n3, np), kThreads, sm, c.stream>>>(
+        g, zb, yb, twA_of<T>(c, 1));
+  } else {
+    const int nl = lines_rt(g.n2);
+    const size_t sm = stage_smem<T>(g.n2, nl);
+    allow_smem(k_yinv<T, 0>, sm);
+    k_yinv<T, 0><<<dim3((g.nslot + nl - 1) / nl, g.n3, np), kThreads, sm, c.stream>>>(g, c.plan[1], zb, nl, yb,
+                                                                                       tw_of<T>(c, 1));
+  }
   GBCP_LAUNCH_CHECK(c);
   return 0;
 }
@@ -382,57 +407,89 @@ template <typename T, int NC> int launch_yinv(Ctx& c, int np) {
 template <typename T, int NC>
 int launch_xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho) {
   const GeoDev& g = c.geo;
-  int nl = stage_lines<NC>(g.n1);
-  if (NC == 0) {
+  const cx<T>* yb = static_cast<const cx<T>*>(c.ybuf.p);
+  if constexpr (NC > 0) {
+    constexpr size_t sm = fs_smem<T, NC>(1, 1);
+    allow_smem(k_xrho_fs<T, NC>, sm);
+    ProfScope ps_(c, "k_xinv_rho");
+    k_xrho_fs<T, NC><<<dim3((g.n2 + FS<T, NC>::L - 1) / FS<T, NC>::L, g.n3), kThreads, sm, c.stream>>>(
+        g, yb, np, s0, nstate, f, 1.0 / c.omega, rho, twA_of<T>(c, 0));
+  } else {
+    int nl = lines_rt(g.n1);
     while (nl > 1 && nl * g.n1 > kMaxAcc * kThreads) --nl;
     if (nl * g.n1 > kMaxAcc * kThreads) {
       c.err = "mesh too large for the density tile";
       return 7;
     }
+    const size_t sm = stage_smem<T>(g.n1, nl);
+    allow_smem(k_xinv_rho<T, 0>, sm);
+    ProfScope ps_(c, "k_xinv_rho");
+    k_xinv_rho<T, 0><<<dim3((g.n2 + nl - 1) / nl, g.n3), kThreads, sm, c.stream>>>(
+        g, c.plan[0], yb, np, s0, nstate, f, 1.0 / c.omega, rho, nl, tw_of<T>(c, 0));
   }
-  const size_t sm = stage_smem<T>(g.n1, nl);
-  allow_smem(k_xinv_rho<T, NC>, sm);
-  ProfScope ps_(c, "k_xinv_rho");
-  k_xinv_rho<T, NC><<<dim3((g.n2 + nl - 1) / nl, g.n3), kThreads, sm, c.stream>>>(
-      g, c.plan[0], static_cast<const cx<T>*>(c.ybuf.p), np, s0, nstate, f, 1.0 / c.omega, rho, nl, tw_of<T>(c, 0));
   GBCP_LAUNCH_CHECK(c);
   return 0;
 }
 
 template <typename T, int NC> int launch_xvx(Ctx& c, int np, const double* vpot) {
   const GeoDev& g = c.geo;
-  const int nl = stage_lines<NC>(g.n1);
-  const size_t sm = stage_smem<T>(g.n1, nl);
-  allow_smem(k_xvx<T, NC>, sm);
+  cx<T>* yb = static_cast<cx<T>*>(c.ybuf.p);
   ProfScope ps_(c, "k_xvx");
-  k_xvx<T, NC><<<dim3((g.n2 + nl - 1) / nl, g.n3, np), kThreads, sm, c.stream>>>(
-      g, c.plan[0], static_cast<cx<T>*>(c.ybuf.p), vpot, nl, tw_of<T>(c, 0));
+  if constexpr (NC > 0) {
+    constexpr size_t sm = fs_smem<T, NC>(2, 2);
+    allow_smem(k_xvx_fs<T, NC>, sm);
+    k_xvx_fs<T, NC><<<dim3((g.n2 + FS<T, NC>::L - 1) / FS<T, NC>::L, g.n3, np), kThreads, sm, c.stream>>>(
+        g, yb, vpot, twA_of<T>(c, 0), twB_of<T>(c, 0));
+  } else {
+    const int nl = lines_rt(g.n1);
+    const size_t sm = stage_smem<T>(g.n1, nl);
+    allow_smem(k_xvx<T, 0>, sm);
+    k_xvx<T, 0><<<dim3((g.n2 + nl - 1) / nl, g.n3, np), kThreads, sm, c.stream>>>(g, c.plan[0], yb, vpot, nl,
+                                                                                   tw_of<T>(c, 0));
+  }
   GBCP_LAUNCH_CHECK(c);
   return 0;
 }
 
 template <typename T, int NC> int launch_yfwd(Ctx& c, int np) {
   const GeoDev& g = c.geo;
-  const int nl = stage_lines<NC>(g.n2);
-  const size_t sm = stage_smem<T>(g.n2, nl);
-  allow_smem(k_yfwd<T, NC>, sm);
+  const cx<T>* yb = static_cast<const cx<T>*>(c.ybuf.p);
+  cx<T>* zb = static_cast<cx<T>*>(c.zbuf.p);
   ProfScope ps_(c, "k_yfwd");
-  k_yfwd<T, NC><<<dim3((g.nslot + nl - 1) / nl, g.n3, np), kThreads, sm, c.stream>>>(
-      g, c.plan[1], static_cast<const cx<T>*>(c.ybuf.p), nl, static_cast<cx<T>*>(c.zbuf.p), tw_of<T>(c, 1));
+  if constexpr (NC > 0) {
+    constexpr size_t sm = fs_smem<T, NC>(1, 1);
+    allow_smem(k_yfwd_fs<T, NC>, sm);
+    k_yfwd_fs<T, NC><<<dim3((g.nslot + FS<T, NC>::L - 1) / FS<T, NC>::L, g.n3, np), kThreads, sm, c.stream>>>(
+        g, yb, zb, twA_of<T>(c, 1));
+  } else {
+    const int nl = lines_rt(g.n2);
+    const size_t sm = stage_smem<T>(g.n2, nl);
+    allow_smem(k_yfwd<T, 0>, sm);
+    k_yfwd<T, 0><<<dim3((g.nslot + nl - 1) / nl, g.n3, np), kThreads, sm, c.stream>>>(g, c.plan[1], yb, nl, zb,
+                                                                                       tw_of<T>(c, 1));
+  }
   GBCP_LAUNCH_CHECK(c);
   return 0;
 }
 
 template <typename T, int NC> int launch_zfwd(Ctx& c, int np) {
   const GeoDev& g = c.geo;
-  const int nl = stage_lines<NC>(g.n3);
-  const size_t sm = stage_smem<T>(g.n3, nl);
+  const cx<T>* zb = static_cast<const cx<T>*>(c.zbuf.p);
+  cx<T>* qb = static_cast<cx<T>*>(c.qbuf.p);
   const T scale = (T)(1.0 / ((double)g.n1 * g.n2 * g.n3));
-  allow_smem(k_zfwd<T, NC>, sm);
   ProfScope ps_(c, "k_zfwd");
-  k_zfwd<T, NC><<<dim3((g.ncol + nl - 1) / nl, np), kThreads, sm, c.stream>>>(
-      g, c.plan[2], static_cast<const cx<T>*>(c.zbuf.p), nl, scale, static_cast<cx<T>*>(c.qbuf.p),
-      tw_of<T>(c, 2));
+  if constexpr (NC > 0) {
+    constexpr size_t sm = fs_smem<T, NC>(1, 1);
+    allow_smem(k_zfwd_fs<T, NC>, sm);
+    k_zfwd_fs<T, NC><<<dim3((g.ncol + FS<T, NC>::L - 1) / FS<T, NC>::L, np), kThreads, sm, c.stream>>>(
+        g, zb, scale, qb, twA_of<T>(c, 2));
+  } else {
+    const int nl = lines_rt(g.n3);
+    const size_t sm = stage_smem<T>(g.n3, nl);
+    allow_smem(k_zfwd<T, 0>, sm);
+    k_zfwd<T, 0><<<dim3((g.ncol + nl - 1) / nl, np), kThreads, sm, c.stream>>>(g, c.plan[2], zb, nl, scale, qb,
+                                                                               tw_of<T>(c, 2));
+  }
   GBCP_LAUNCH_CHECK(c);
   return 0;
 }

@@ -3,7 +3,9 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "common.cuh"
@@ -78,6 +80,12 @@ struct Ctx {
   FftPlan plan[3];
   cx<double>* tw64[3] = {nullptr, nullptr, nullptr};
   cx<float>* tw32[3] = {nullptr, nullptr, nullptr};
+  // four-step tables per axis (sizes with a four-step plan): twA[k1*N2+n2] =
+  // e^{2 pi i n2 k1/N}, twB[j*N1+k1] = e^{2 pi i k1 j/N}
+  cx<double>* twA64[3] = {nullptr, nullptr, nullptr};
+  cx<double>* twB64[3] = {nullptr, nullptr, nullptr};
+  cx<float>* twA32[3] = {nullptr, nullptr, nullptr};
+  cx<float>* twB32[3] = {nullptr, nullptr, nullptr};
   StageTune tune;
   // workspaces
   Scratch zbuf, ybuf, qbuf;
@@ -104,6 +112,21 @@ struct ProfScope {
 };
 void prof_fold(Ctx& c);
 
+// Raise a kernel's dynamic shared-memory limit, once per kernel and size
+// (cudaFuncSetAttribute costs host time that would otherwise be paid on
+// every launch and starve the GPU of work).
+template <typename KernelT> inline void allow_smem(KernelT k, size_t bytes) {
+  if (bytes <= 48 * 1024) return;
+  static std::mutex mu;
+  static std::unordered_map<const void*, size_t> done;
+  const void* key = reinterpret_cast<const void*>(k);
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = done.find(key);
+  if (it != done.end() && it->second >= bytes) return;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  done[key] = bytes;
+}
+
 // grow-only scratch allocation; returns false on cudaMalloc failure
 bool ensure(Ctx& c, Scratch& s, size_t bytes);
 
@@ -117,8 +140,10 @@ int rho_sum(Ctx& c, const double* rho, double* sum);
 
 // ---- linear algebra (linalg.cu) ----
 int ovlap_gamma(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S);
-int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, double* scond_host);
-int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout, int ldo);
+int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, unsigned long long* scond_bits,
+             int* status);
+int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout, int ldo,
+            int* status);
 inline bool use_tc_gemm(const Ctx& c) { return c.gemm_mode == 1 || (c.gemm_mode < 0 && c.precision == 1); }
 int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host);
 int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host);

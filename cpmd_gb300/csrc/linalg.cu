@@ -113,10 +113,12 @@ __global__ void k_syrk_fold(const double* __restrict__ part, int nsplit, int n, 
 }
 
 // Cholesky S = U^T U (upper, row-major in place) then X = U^{-1} (upper).
-// One CTA; info = k+1 at the first non-positive pivot, -1 on NaN.
+// One CTA.  *info is the ortho status word: the kernel does nothing if an
+// earlier step set it, and sets k+1 at the first non-positive pivot, -1 on NaN.
 __global__ void __launch_bounds__(1024) k_potrf_trtri(double* __restrict__ S, double* __restrict__ X, int n,
                                                       int* __restrict__ info) {
   __shared__ int bad;
+  if (*(volatile int*)info != 0) return;
   if (threadIdx.x == 0) bad = 0;
   __syncthreads();
   for (int k = 0; k < n; ++k) {
@@ -152,7 +154,6 @@ __global__ void __launch_bounds__(1024) k_potrf_trtri(double* __restrict__ S, do
       X[(size_t)i * n + j] = -s / S[(size_t)i * n + i];
     }
   }
-  if (threadIdx.x == 0) *info = 0;
 }
 
 // Same factorisation with S held in shared memory (n <= 160): the trailing
@@ -161,6 +162,7 @@ __global__ void __launch_bounds__(1024) k_potrf_trtri_smem(const double* __restr
                                                            int n, int* __restrict__ info) {
   extern __shared__ double sS[];
   __shared__ int bad;
+  if (*(volatile int*)info != 0) return;
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) sS[e] = Sg[e];
   if (threadIdx.x == 0) bad = 0;
   __syncthreads();
@@ -195,16 +197,16 @@ __global__ void __launch_bounds__(1024) k_potrf_trtri_smem(const double* __restr
       X[(size_t)i * n + j] = -s / sS[i * n + i];
     }
   }
-  if (threadIdx.x == 0) *info = 0;
 }
 
 // Cout = A * M.  A real view (rows = 2 ngw, lda), M (n x n) row-major (M[k][j]).
 // upper != 0: M is upper triangular, column block j only needs k <= j.
 __global__ void __launch_bounds__(NT) k_gemm_right(const double* __restrict__ A, int lda, int rows, int n,
                                                    const double* __restrict__ M, int upper, double* __restrict__ Cout,
-                                                   int ldo) {
+                                                   int ldo, const int* __restrict__ status) {
   __shared__ double As[BK][TS + 1];
   __shared__ double Ms[BK][TS + 1];
+  if (*(volatile const int*)status != 0) return;
   const int r0 = blockIdx.x * TS, j0 = blockIdx.y * TS;
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   double acc[4][4] = {};
@@ -245,9 +247,11 @@ __global__ void __launch_bounds__(NT) k_gemm_right(const double* __restrict__ A,
     }
 }
 
-// copy the real view back (ngw complex rows per state) and zero Im c(G=0)
+// copy the real view back (ngw complex rows per state) and zero Im c(G=0);
+// nothing is written if the status word reports a failed step (c0 untouched)
 __global__ void k_copy_back(const double* __restrict__ src, int lds, double* __restrict__ dst, int ldd, int rows,
-                            int n, int geq0) {
+                            int n, int geq0, const int* __restrict__ status) {
+  if (*(volatile const int*)status != 0) return;
   const size_t tot = (size_t)rows * n;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
     const int r = (int)(e % rows), c = (int)(e / rows);
@@ -351,8 +355,47 @@ __global__ void k_scale(double* __restrict__ X, size_t n, const double* __restri
 
 }  // namespace
 
-int ovlap_gamma_ex(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, double* scond_host) {
-  if (use_tc_gemm(c)) return ovlap_tc(c, c0, ldc, nstate, S, scond_host);
+// The ortho status word (c.d_info): int status at byte 0 (0 ok, k+1 not
+// positive definite at pivot k, -1 non-finite, -2 timed-out tensor-core wait),
+// max|S-I| as ordered bits at byte 8.  Every ortho kernel checks it, so a
+// failed step leaves c0 untouched and the host synchronises once at the end.
+static unsigned long long* scond_bits_of(Ctx& c) { return reinterpret_cast<unsigned long long*>(c.d_info + 2); }
+
+static int status_error(Ctx& c, int st) {
+  if (st > 0) {
+    c.err = "UINV: leading minor " + std::to_string(st) + " not positive definite (dpotrf)";
+    return 2;
+  }
+  if (st == -1) {
+    c.err = "UINV: non-finite overlap";
+    return 3;
+  }
+  if (st == -2) {
+    c.err = "ortho (tensor cores): an mbarrier wait timed out";
+    return 4;
+  }
+  return 0;
+}
+
+// read the status word (and scond) after one synchronisation
+static int finish_status(Ctx& c, double* scond_host) {
+  int h[4] = {0, 0, 0, 0};
+  GBCP_CUDA_TRY(c, cudaMemcpyAsync(h, c.d_info, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
+  GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  if (scond_host) {
+    unsigned long long b;
+    memcpy(&b, h + 2, sizeof(b));
+    double d;
+    memcpy(&d, &b, sizeof(d));
+    *scond_host = d;
+  }
+  return status_error(c, h[0]);
+}
+
+// S (n x n) queued on the stream; scond bits if requested.  No synchronisation.
+int ovlap_gamma_ex(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, bool want_scond) {
+  unsigned long long* bits = want_scond ? scond_bits_of(c) : nullptr;
+  if (use_tc_gemm(c)) return ovlap_tc(c, c0, ldc, nstate, S, bits, c.d_info);
   const int n = nstate;
   const int K = 2 * c.ngw;
   const int lda = 2 * ldc;
@@ -371,27 +414,20 @@ int ovlap_gamma_ex(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S,
     k_syrk_part<<<dim3(npairs, nsplit), NT, 0, c.stream>>>(Ar, lda, K, n, ntb, kchunk, part);
     GBCP_LAUNCH_CHECK(c);
   }
-  unsigned long long* bits = reinterpret_cast<unsigned long long*>(part + (size_t)nsplit * n * n);
-  if (scond_host) GBCP_CUDA_TRY(c, cudaMemsetAsync(bits, 0, sizeof(unsigned long long), c.stream));
   const int fb = std::max(1, std::min(1024, (n * n + 255) / 256));
   {
     ProfScope ps_(c, "k_syrk_fold");
-    k_syrk_fold<<<fb, 256, 0, c.stream>>>(part, nsplit, n, ntb, Ar, lda, c.geq0, S, scond_host ? bits : nullptr);
+    k_syrk_fold<<<fb, 256, 0, c.stream>>>(part, nsplit, n, ntb, Ar, lda, c.geq0, S, bits);
     GBCP_LAUNCH_CHECK(c);
-  }
-  if (scond_host) {
-    unsigned long long h = 0;
-    GBCP_CUDA_TRY(c, cudaMemcpyAsync(&h, bits, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
-    GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
-    double d;
-    memcpy(&d, &h, sizeof(d));
-    *scond_host = d;
   }
   return 0;
 }
 
 int ovlap_gamma(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S) {
-  return ovlap_gamma_ex(c, c0, ldc, nstate, S, nullptr);
+  GBCP_CUDA_TRY(c, cudaMemsetAsync(c.d_info, 0, 16, c.stream));
+  const int rc = ovlap_gamma_ex(c, c0, ldc, nstate, S, false);
+  if (rc) return rc;
+  return finish_status(c, nullptr);
 }
 
 static int apply_right(Ctx& c, cx<double>* c0, int ldc, int nstate, const double* M, int upper) {
@@ -400,17 +436,19 @@ static int apply_right(Ctx& c, cx<double>* c0, int ldc, int nstate, const double
   if (!ensure(c, c.cscr, sizeof(double) * (size_t)rows * nstate)) return 6;
   double* tmp = static_cast<double*>(c.cscr.p);
   if (use_tc_gemm(c)) {
-    const int rc = rmul_tc(c, reinterpret_cast<const double*>(c0), lda, rows, nstate, M, upper, tmp, rows);
+    const int rc = rmul_tc(c, reinterpret_cast<const double*>(c0), lda, rows, nstate, M, upper, tmp, rows, c.d_info);
     if (rc) return rc;
   } else {
     dim3 grid((rows + TS - 1) / TS, (nstate + TS - 1) / TS);
     ProfScope ps_(c, "k_gemm_right");
-    k_gemm_right<<<grid, NT, 0, c.stream>>>(reinterpret_cast<const double*>(c0), lda, rows, nstate, M, upper, tmp, rows);
+    k_gemm_right<<<grid, NT, 0, c.stream>>>(reinterpret_cast<const double*>(c0), lda, rows, nstate, M, upper, tmp, rows,
+                                            c.d_info);
     GBCP_LAUNCH_CHECK(c);
   }
   {
     ProfScope ps_(c, "k_copy_back");
-    k_copy_back<<<1024, 256, 0, c.stream>>>(tmp, rows, reinterpret_cast<double*>(c0), lda, rows, nstate, c.geq0);
+    k_copy_back<<<1024, 256, 0, c.stream>>>(tmp, rows, reinterpret_cast<double*>(c0), lda, rows, nstate, c.geq0,
+                                            c.d_info);
     GBCP_LAUNCH_CHECK(c);
   }
   return 0;
@@ -427,12 +465,12 @@ int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host) {
     return 6;
   double* S = static_cast<double*>(c.smat.p);
   double* X = static_cast<double*>(c.smat2.p);
-  int rc = ovlap_gamma_ex(c, c0, ldc, n, S, scond_host);
+  GBCP_CUDA_TRY(c, cudaMemsetAsync(c.d_info, 0, 16, c.stream));
+  int rc = ovlap_gamma_ex(c, c0, ldc, n, S, scond_host != nullptr);
   if (rc) return rc;
   if (n <= 160) {
     const size_t sm = sizeof(double) * (size_t)n * n;
-    if (sm > 48 * 1024)
-      cudaFuncSetAttribute(k_potrf_trtri_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    allow_smem(k_potrf_trtri_smem, sm);
     ProfScope ps_(c, "k_potrf_trtri");
     k_potrf_trtri_smem<<<1, 1024, sm, c.stream>>>(S, X, n, c.d_info);
     GBCP_LAUNCH_CHECK(c);
@@ -441,24 +479,9 @@ int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host) {
     k_potrf_trtri<<<1, 1024, 0, c.stream>>>(S, X, n, c.d_info);
     GBCP_LAUNCH_CHECK(c);
   }
-  // a failed factorisation leaves c0 untouched
-  int info = 0;
-  GBCP_CUDA_TRY(c, cudaMemcpyAsync(&info, c.d_info, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-  GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
-  if (info == 0) {
-    rc = apply_right(c, c0, ldc, n, X, 1);
-    if (rc) return rc;
-  }
-  GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
-  if (info > 0) {
-    c.err = "UINV: leading minor " + std::to_string(info) + " not positive definite (dpotrf)";
-    return 2;
-  }
-  if (info < 0) {
-    c.err = "UINV: non-finite overlap";
-    return 3;
-  }
-  return 0;
+  rc = apply_right(c, c0, ldc, n, X, 1);
+  if (rc) return rc;
+  return finish_status(c, scond_host);
 }
 
 int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host) {
@@ -478,8 +501,10 @@ int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host
   double* T = Z + nn;
   double* W = static_cast<double*>(c.smat3.p);
   double* scal = W + nn;  // [0] alpha, [1] residual
-  int rc = ovlap_gamma_ex(c, c0, ldc, n, S, scond_host);
+  GBCP_CUDA_TRY(c, cudaMemsetAsync(c.d_info, 0, 16, c.stream));
+  int rc = ovlap_gamma_ex(c, c0, ldc, n, S, scond_host != nullptr);
   if (rc) return rc;
+  if ((rc = finish_status(c, scond_host))) return rc;
   {
     ProfScope ps_(c, "k_ns_init");
     k_ns_init<<<1, 1024, 0, c.stream>>>(S, n, Y, Z, scal);
@@ -533,7 +558,8 @@ int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host
     k_scale<<<256, 256, 0, c.stream>>>(Z, nn, scal, -0.5);
     GBCP_LAUNCH_CHECK(c);
   }
-  return apply_right(c, c0, ldc, n, Z, 0);
+  if ((rc = apply_right(c, c0, ldc, n, Z, 0))) return rc;
+  return finish_status(c, nullptr);
 }
 
 }  // namespace gbcp

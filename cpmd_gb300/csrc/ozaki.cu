@@ -30,8 +30,9 @@
 // The digits are produced in the kernels from FP64 data with integer
 // instructions and stored straight into shared memory in the tensor core's
 // K-major core-matrix layout: no slice matrices in HBM, no FP64 arithmetic in
-// the inner loop.  Every mbarrier wait is bounded; on expiry the kernel flags
-// GBCP_ERR_TIMEOUT, frees its TMEM and returns.
+// the inner loop.  Every mbarrier wait is bounded; on expiry the kernel sets
+// the ortho status word to -2 (reported as GBCP_ERR_TIMEOUT), frees its TMEM
+// and returns.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -185,7 +186,7 @@ __global__ void k_mat_col_max(const double* __restrict__ M, int n, unsigned long
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_ozaki_syrk(const double* __restrict__ Ar, int lda, int K, int n, const unsigned long long* __restrict__ cmax,
                  int njb, int subs_per_split, unsigned long long* __restrict__ Hacc,
-                 unsigned long long* __restrict__ Lacc, int* __restrict__ err) {
+                 unsigned long long* __restrict__ Lacc, int* __restrict__ status) {
   extern __shared__ __align__(1024) uint8_t sm[];
   uint8_t* sA = sm;
   uint8_t* sB = sm + 2 * A_BUF_BYTES;
@@ -238,7 +239,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     if (pend[buf]) {
       if (!tc::mbar_wait(&mbar[buf], ph[buf])) {
         abort_sh = 1;
-        atomicExch(err, 4);
+        atomicExch(status, -2);
       }
       ph[buf] ^= 1u;
       pend[buf] = 0;
@@ -290,7 +291,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       }
       if (!ok) {
         abort_sh = 1;
-        atomicExch(err, 4);
+        atomicExch(status, -2);
       }
       __syncthreads();
       if (abort_sh) {
@@ -355,7 +356,7 @@ __global__ void k_ozaki_syrk_finalize(const long long* __restrict__ H, const lon
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_ozaki_rmul(const double* __restrict__ A, int lda, int rows, int n, const double* __restrict__ M, int upper,
                  const unsigned long long* __restrict__ rmax, const unsigned long long* __restrict__ mcmax,
-                 double* __restrict__ Cout, int ldo, int* __restrict__ err) {
+                 double* __restrict__ Cout, int ldo, int* __restrict__ status) {
   extern __shared__ __align__(1024) uint8_t sm[];
   uint8_t* sA = sm;
   uint8_t* sB = sm + 2 * A_BUF_BYTES;
@@ -366,6 +367,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   const int nrt = (rows + OZ_M - 1) / OZ_M, nct = (n + OZ_N - 1) / OZ_N;
   const int ntiles = nrt * nct;
   if ((int)blockIdx.x >= ntiles) return;
+  if (*(volatile const int*)status != 0) return;  // an earlier step of this ortho failed
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (warp == 0) {
     tc::tmem_alloc(&tmem_sh, 512);
@@ -403,7 +405,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       if (pend[buf]) {
         if (!tc::mbar_wait(&mbar[buf], ph[buf])) {
           abort_sh = 1;
-          atomicExch(err, 4);
+          atomicExch(status, -2);
         }
         ph[buf] ^= 1u;
         pend[buf] = 0;
@@ -461,7 +463,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         }
         if (!ok) {
           abort_sh = 1;
-          atomicExch(err, 4);
+          atomicExch(status, -2);
         }
         __syncthreads();
         if (abort_sh) break;
@@ -494,12 +496,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   }
 }
 
-bool g_attr_syrk = false, g_attr_rmul = false;
-
 }  // namespace
 
-// Overlap matrix on the tensor cores; scond (max|S-I|) if scond_host.
-int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, double* scond_host) {
+// Overlap matrix on the tensor cores, queued without a host synchronisation.
+// scond_bits (device, may be NULL) receives max|S-I| as ordered bits; a timed-out
+// wait sets *status = -2.
+int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, unsigned long long* scond_bits,
+             int* status) {
   const int n = nstate;
   const int K = 2 * c.ngw;
   const int lda = 2 * ldc;
@@ -514,14 +517,12 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, doubl
   subs_per = ((subs_per + OZ_SUBS - 1) / OZ_SUBS) * OZ_SUBS;
   nsplit = (total_subs + subs_per - 1) / subs_per;
   const size_t nn = (size_t)n * n;
-  // workspace: H, Lo (int64 n*n each), column maxima (n), err, scond bits
-  const size_t bytes = 2 * nn * 8 + (size_t)n * 8 + 64;
+  // workspace: H, Lo (int64 n*n each), column maxima (n)
+  const size_t bytes = 2 * nn * 8 + (size_t)n * 8;
   if (!ensure(c, c.sparts, bytes)) return 6;
   unsigned long long* Hacc = static_cast<unsigned long long*>(c.sparts.p);
   unsigned long long* Lacc = Hacc + nn;
   unsigned long long* cmax = Lacc + nn;
-  int* err = reinterpret_cast<int*>(cmax + n);
-  unsigned long long* bits = cmax + n + 1;
   GBCP_CUDA_TRY(c, cudaMemsetAsync(Hacc, 0, bytes, c.stream));
   {
     ProfScope ps_(c, "k_col_max");
@@ -531,13 +532,10 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, doubl
     GBCP_LAUNCH_CHECK(c);
   }
   {
-    if (!g_attr_syrk) {
-      cudaFuncSetAttribute(k_ozaki_syrk, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM);
-      g_attr_syrk = true;
-    }
+    allow_smem(k_ozaki_syrk, OZ_SMEM);
     ProfScope ps_(c, "k_ozaki_syrk");
     k_ozaki_syrk<<<dim3(ntiles, nsplit), OZ_THREADS, OZ_SMEM, c.stream>>>(Ar, lda, K, n, cmax, njb, subs_per, Hacc,
-                                                                          Lacc, err);
+                                                                          Lacc, status);
     GBCP_LAUNCH_CHECK(c);
   }
   {
@@ -545,34 +543,21 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, doubl
     const int fb = std::max(1, std::min(1024, (int)((nn + 255) / 256)));
     k_ozaki_syrk_finalize<<<fb, 256, 0, c.stream>>>(reinterpret_cast<const long long*>(Hacc),
                                                     reinterpret_cast<const long long*>(Lacc), cmax, n, Ar, lda, c.geq0,
-                                                    S, scond_host ? bits : nullptr);
+                                                    S, scond_bits);
     GBCP_LAUNCH_CHECK(c);
-  }
-  int herr = 0;
-  unsigned long long hb = 0;
-  GBCP_CUDA_TRY(c, cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-  if (scond_host) GBCP_CUDA_TRY(c, cudaMemcpyAsync(&hb, bits, sizeof(hb), cudaMemcpyDeviceToHost, c.stream));
-  GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
-  if (herr) {
-    c.err = "ovlap (tensor cores): an mbarrier wait timed out";
-    return 4;
-  }
-  if (scond_host) {
-    double d;
-    memcpy(&d, &hb, sizeof(d));
-    *scond_host = d;
   }
   return 0;
 }
 
-// Cout (rows x n, ldo) = A (rows x n, lda) * M (n x n row-major) on the tensor cores.
-int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout, int ldo) {
-  const size_t bytes = ((size_t)rows + n + 2) * 8 + 64;
+// Cout (rows x n, ldo) = A (rows x n, lda) * M (n x n row-major) on the tensor
+// cores, queued without a host synchronisation; skipped when *status != 0 on
+// entry, *status = -2 on a timed-out wait.
+int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout, int ldo,
+            int* status) {
+  const size_t bytes = ((size_t)rows + n) * 8;
   if (!ensure(c, c.nl_a, bytes)) return 6;
   unsigned long long* rmax = static_cast<unsigned long long*>(c.nl_a.p);
   unsigned long long* mcmax = rmax + rows;
-  int* err = reinterpret_cast<int*>(mcmax + n);
-  GBCP_CUDA_TRY(c, cudaMemsetAsync(err, 0, sizeof(int), c.stream));
   {
     ProfScope ps_(c, "k_row_max");
     k_row_max<<<(rows + 255) / 256, 256, 0, c.stream>>>(A, lda, rows, n, rmax);
@@ -584,22 +569,12 @@ int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, 
     GBCP_LAUNCH_CHECK(c);
   }
   {
-    if (!g_attr_rmul) {
-      cudaFuncSetAttribute(k_ozaki_rmul, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM);
-      g_attr_rmul = true;
-    }
+    allow_smem(k_ozaki_rmul, OZ_SMEM);
     const int ntiles = ((rows + OZ_M - 1) / OZ_M) * ((n + OZ_N - 1) / OZ_N);
     const int grid = std::max(1, std::min(ntiles, 148));
     ProfScope ps_(c, "k_ozaki_rmul");
-    k_ozaki_rmul<<<grid, OZ_THREADS, OZ_SMEM, c.stream>>>(A, lda, rows, n, M, upper, rmax, mcmax, Cout, ldo, err);
+    k_ozaki_rmul<<<grid, OZ_THREADS, OZ_SMEM, c.stream>>>(A, lda, rows, n, M, upper, rmax, mcmax, Cout, ldo, status);
     GBCP_LAUNCH_CHECK(c);
-  }
-  int herr = 0;
-  GBCP_CUDA_TRY(c, cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-  GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
-  if (herr) {
-    c.err = "C M (tensor cores): an mbarrier wait timed out";
-    return 4;
   }
   return 0;
 }

@@ -130,12 +130,14 @@ def test_vpsi_accumulates_and_odd_states(gpu_lib, nstate):
     assert rel(c2, ref) < TOL64
 
 
-@pytest.mark.parametrize("nr,ecut", [(20, 8.0), (24, 10.0), (36, 20.0), (40, 25.0), (48, 30.0), (60, 40.0),
-                                     (64, 40.0), (72, 50.0), (80, 50.0), (96, 60.0)])
+@pytest.mark.parametrize("nr,ecut,alat", [(20, 8.0, 10.26), (24, 10.0, 10.26), (36, 20.0, 10.26), (40, 25.0, 10.26),
+                                          (48, 30.0, 10.26), (60, 40.0, 10.26), (64, 40.0, 10.26),
+                                          (72, 50.0, 10.26), (80, 50.0, 10.26), (96, 60.0, 10.26),
+                                          (144, 50.0, 30.78), (240, 70.0, 41.04)])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_band_loop_all_mesh_plans(gpu_lib, nr, ecut, precision):
-    """Compile-time FFT plans (36..96) and the run-time plan (20, 24) give the oracle's rho and c2."""
-    cl = make_small_cell(10.26, nr, ecut, 5, seed=nr)
+def test_band_loop_all_mesh_plans(gpu_lib, nr, ecut, alat, precision):
+    """Four-step plans (32..240) and the run-time Stockham plan (20, 24) give the oracle's rho and c2."""
+    cl = make_small_cell(alat, nr, ecut, 5 if nr < 144 else 3, seed=nr)
     b = cl.basis
     rho_r, *_ = O.rhoofr(cl.c0, cl.f, b.mill, b.nr, b.kr, b.omega, b.hg, b.tpiba2, b.geq0)
     c2_r = O.vpsi(cl.c0, np.zeros_like(cl.c0), cl.f, cl.vpot, b.mill, b.nr, b.hg, b.tpiba2, b.geq0)
