@@ -145,6 +145,7 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, unsig
 int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout, int ldo,
             int* status);
 inline bool use_tc_gemm(const Ctx& c) { return c.gemm_mode == 1 || (c.gemm_mode < 0 && c.precision == 1); }
+int chol_inverse(Ctx& c, double* S, double* X, int n);
 int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host);
 int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host);
 

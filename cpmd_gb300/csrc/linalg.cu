@@ -10,7 +10,7 @@
 //  * S: split-K tiled FP64 GEMM over the real view (K = 2 ngw), upper block
 //    triangle only, partial tiles folded by a second kernel that also applies
 //    the G=0 correction, mirrors the lower triangle and computes max|S-I|.
-//  * U and U^{-1}: one CTA, S resident in L2/L1 (n <= 1024 states).
+//  * U and U^{-1}: blocked over many CTAs (chol.cu).
 //  * S^{-1/2}: coupled Newton-Schulz iteration on GEMMs (Y -> S^{1/2},
 //    Z -> S^{-1/2}); mathematically the same matrix as Z w^{-1/2} Z^T from the
 //    reference's dspevy, reached without an eigensolver.
@@ -109,93 +109,6 @@ __global__ void k_syrk_fold(const double* __restrict__ part, int nsplit, int n, 
     // non-negative doubles order like their bit patterns
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0) atomicMax(scond_bits, (unsigned long long)__double_as_longlong(mx));
-  }
-}
-
-// Cholesky S = U^T U (upper, row-major in place) then X = U^{-1} (upper).
-// One CTA.  *info is the ortho status word: the kernel does nothing if an
-// earlier step set it, and sets k+1 at the first non-positive pivot, -1 on NaN.
-__global__ void __launch_bounds__(1024) k_potrf_trtri(double* __restrict__ S, double* __restrict__ X, int n,
-                                                      int* __restrict__ info) {
-  __shared__ int bad;
-  if (*(volatile int*)info != 0) return;
-  if (threadIdx.x == 0) bad = 0;
-  __syncthreads();
-  for (int k = 0; k < n; ++k) {
-    if (threadIdx.x == 0) {
-      const double d = S[(size_t)k * n + k];
-      if (!(d > 0.0)) bad = (d != d) ? -1 : k + 1;
-      else S[(size_t)k * n + k] = sqrt(d);
-    }
-    __syncthreads();
-    if (bad) break;
-    const double dk = S[(size_t)k * n + k];
-    for (int j = k + 1 + threadIdx.x; j < n; j += blockDim.x) S[(size_t)k * n + j] /= dk;
-    __syncthreads();
-    const int m = n - k - 1;
-    const long long tot = (long long)m * m;
-    for (long long e = threadIdx.x; e < tot; e += blockDim.x) {
-      const int i = k + 1 + (int)(e / m), j = k + 1 + (int)(e % m);
-      if (j >= i) S[(size_t)i * n + j] -= S[(size_t)k * n + i] * S[(size_t)k * n + j];
-    }
-    __syncthreads();
-  }
-  if (bad) {
-    if (threadIdx.x == 0) *info = bad;
-    return;
-  }
-  // triangular inverse, one column per thread: X[i][j] = -(sum_{k=i+1..j} U[i][k] X[k][j]) / U[i][i]
-  for (int j = threadIdx.x; j < n; j += blockDim.x) {
-    for (int i = j + 1; i < n; ++i) X[(size_t)i * n + j] = 0.0;
-    X[(size_t)j * n + j] = 1.0 / S[(size_t)j * n + j];
-    for (int i = j - 1; i >= 0; --i) {
-      double s = 0.0;
-      for (int k = i + 1; k <= j; ++k) s = fma(S[(size_t)i * n + k], X[(size_t)k * n + j], s);
-      X[(size_t)i * n + j] = -s / S[(size_t)i * n + i];
-    }
-  }
-}
-
-// Same factorisation with S held in shared memory (n <= 160): the trailing
-// updates and the triangular inverse read shared memory instead of L2.
-__global__ void __launch_bounds__(1024) k_potrf_trtri_smem(const double* __restrict__ Sg, double* __restrict__ X,
-                                                           int n, int* __restrict__ info) {
-  extern __shared__ double sS[];
-  __shared__ int bad;
-  if (*(volatile int*)info != 0) return;
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) sS[e] = Sg[e];
-  if (threadIdx.x == 0) bad = 0;
-  __syncthreads();
-  for (int k = 0; k < n; ++k) {
-    if (threadIdx.x == 0) {
-      const double d = sS[k * n + k];
-      if (!(d > 0.0)) bad = (d != d) ? -1 : k + 1;
-      else sS[k * n + k] = sqrt(d);
-    }
-    __syncthreads();
-    if (bad) break;
-    const double dk = sS[k * n + k];
-    for (int j = k + 1 + threadIdx.x; j < n; j += blockDim.x) sS[k * n + j] /= dk;
-    __syncthreads();
-    const int m = n - k - 1;
-    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-      const int i = k + 1 + e / m, j = k + 1 + e % m;
-      if (j >= i) sS[i * n + j] -= sS[k * n + i] * sS[k * n + j];
-    }
-    __syncthreads();
-  }
-  if (bad) {
-    if (threadIdx.x == 0) *info = bad;
-    return;
-  }
-  for (int j = threadIdx.x; j < n; j += blockDim.x) {
-    for (int i = j + 1; i < n; ++i) X[(size_t)i * n + j] = 0.0;
-    X[(size_t)j * n + j] = 1.0 / sS[j * n + j];
-    for (int i = j - 1; i >= 0; --i) {
-      double s = 0.0;
-      for (int k = i + 1; k <= j; ++k) s = fma(sS[i * n + k], X[(size_t)k * n + j], s);
-      X[(size_t)i * n + j] = -s / sS[i * n + i];
-    }
   }
 }
 
@@ -468,17 +381,7 @@ int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host) {
   GBCP_CUDA_TRY(c, cudaMemsetAsync(c.d_info, 0, 16, c.stream));
   int rc = ovlap_gamma_ex(c, c0, ldc, n, S, scond_host != nullptr);
   if (rc) return rc;
-  if (n <= 160) {
-    const size_t sm = sizeof(double) * (size_t)n * n;
-    allow_smem(k_potrf_trtri_smem, sm);
-    ProfScope ps_(c, "k_potrf_trtri");
-    k_potrf_trtri_smem<<<1, 1024, sm, c.stream>>>(S, X, n, c.d_info);
-    GBCP_LAUNCH_CHECK(c);
-  } else {
-    ProfScope ps_(c, "k_potrf_trtri");
-    k_potrf_trtri<<<1, 1024, 0, c.stream>>>(S, X, n, c.d_info);
-    GBCP_LAUNCH_CHECK(c);
-  }
+  if ((rc = chol_inverse(c, S, X, n))) return rc;
   rc = apply_right(c, c0, ldc, n, X, 1);
   if (rc) return rc;
   return finish_status(c, scond_host);
