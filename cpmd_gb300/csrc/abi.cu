@@ -232,6 +232,14 @@ static int build_geometry(Ctx& c, const int32_t* inyh, const double* hg) {
     c.err = "geometry upload failed";
     return 6;
   }
+  std::vector<double> kin(ngw);
+  for (int ig = 0; ig < ngw; ++ig) kin[ig] = c.tpiba2 * hg[ig];
+  const double* dk = nullptr;
+  if (!upload(c, kin, dk)) {
+    c.err = "geometry upload failed";
+    return 6;
+  }
+  c.kin = const_cast<double*>(dk);
   return 0;
 }
 
@@ -324,7 +332,7 @@ int gbcp_ctx_create(const gbcp_grid_desc* grid, int precision, int max_batch, vo
   c.omega = grid->omega;
   c.tpiba2 = grid->tpiba2;
   c.precision = precision;
-  c.batch = max_batch > 0 ? max_batch : 8;
+  c.batch = std::min(gbcp::kMaxBatch, max_batch > 0 ? max_batch : 8);
   if (cudaStreamCreateWithFlags(&c.own, cudaStreamNonBlocking) != cudaSuccess) {
     delete h;
     return GBCP_ERR_CUDA;
@@ -348,7 +356,7 @@ int gbcp_ctx_destroy(gbcp_ctx* h) {
   if (c.stream) cudaStreamSynchronize(c.stream);
   for (void* p : c.dev_allocs) cudaFree(p);
   gbcp::Scratch* all[] = {&c.zbuf, &c.ybuf, &c.qbuf, &c.st_c0, &c.st_c2, &c.st_rho, &c.st_vpot, &c.st_f,
-                          &c.st_misc, &c.st_misc2, &c.red, &c.smat, &c.smat2, &c.smat3, &c.sparts, &c.cscr,
+                          &c.st_misc, &c.st_misc2, &c.st_vf, &c.red, &c.smat, &c.smat2, &c.smat3, &c.sparts, &c.cscr,
                           &c.nl_a, &c.nl_b, &c.nl_c, &c.nl_d};
   for (auto* s : all) gbcp::release(*s);
   if (c.d_info) cudaFree(c.d_info);
@@ -375,7 +383,7 @@ int gbcp_set_option(gbcp_ctx* h, int key, int value) {
     c.gemm_mode = value;
     return GBCP_OK;
   }
-  if (key == GBCP_OPT_BATCH && value > 0) {
+  if (key == GBCP_OPT_BATCH && value > 0 && value <= gbcp::kMaxBatch) {
     c.batch = value;
     return GBCP_OK;
   }

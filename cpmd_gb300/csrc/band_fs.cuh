@@ -95,7 +95,9 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
             const int ig = (e > 0 ? e : -e) - 1;
             const cx<double> u = c1[ig];
             const cx<double> w = two ? c2[ig] : mk<double>(0.0, 0.0);
-            val = (e > 0) ? mk<T>((T)(u.x - w.y), (T)(u.y + w.x)) : mk<T>((T)(u.x + w.y), (T)(w.x - u.y));
+            const T ux = from_double<T>(u.x), uy = from_double<T>(u.y);
+            const T wx = from_double<T>(w.x), wy = from_double<T>(w.y);
+            val = (e > 0) ? mk<T>(ux - wy, uy + wx) : mk<T>(ux + wy, wx - uy);
           }
         }
         v[n1] = val;
@@ -206,14 +208,18 @@ __global__ void __launch_bounds__(kThreads) k_xrho_fs(GeoDev g, const cx<T>* __r
   T acc[P::N2];
 #pragma unroll
   for (int k2 = 0; k2 < P::N2; ++k2) acc[k2] = (T)0;
+  // occupation weights f/omega of the launch's pairs, once per CTA (FP64 -> T)
+  __shared__ T fw[2 * kMaxBatch];
+  for (int i = threadIdx.x; i < 2 * npairs; i += kThreads) {
+    const int is = s0 + i;
+    fw[i] = from_double<T>(is < nstate ? f[is] * inv_omega : 0.0);
+  }
   const int t = threadIdx.x;
   const int lb = t / P::N1, k1 = t - lb * P::N1;
   for (int pair = 0; pair < npairs; ++pair) {
-    const int is1 = s0 + 2 * pair, is2 = is1 + 1;
-    const T f1 = (T)(f[is1] * inv_omega);
-    const T f2 = (T)((is2 < nstate) ? f[is2] * inv_omega : 0.0);
     const cx<T>* yb = ybuf + ((size_t)pair * g.n3 + z) * (size_t)g.n2 * g.nslot;
-    __syncthreads();  // twiddles loaded / previous pair's step B done
+    __syncthreads();  // twiddles and weights loaded / previous pair's step B done
+    const T f1 = fw[2 * pair], f2 = fw[2 * pair + 1];
     xline_step_a<T, N>(g, yb, y0, twA, Ts);
     __syncthreads();
     if (t < P::TB) {
@@ -227,14 +233,14 @@ __global__ void __launch_bounds__(kThreads) k_xrho_fs(GeoDev g, const cx<T>* __r
   if (t < P::TB && y < g.n2) {
     double* rrow = rho + (size_t)g.k1 * (y + (size_t)g.k2 * z);
 #pragma unroll
-    for (int k2 = 0; k2 < P::N2; ++k2) rrow[k1 + P::N1 * k2] += (double)acc[k2];
+    for (int k2 = 0; k2 < P::N2; ++k2) rrow[k1 + P::N1 * k2] += to_double<T>(acc[k2]);
   }
 }
 
 // ---------------------------------------------------------------- X stage: inverse, x V, forward
 template <typename T, int N>
 __global__ void __launch_bounds__(kThreads) k_xvx_fs(GeoDev g, cx<T>* __restrict__ ybuf,
-                                                    const double* __restrict__ vpot, const cx<T>* __restrict__ twAg,
+                                                    const T* __restrict__ vpot, const cx<T>* __restrict__ twAg,
                                                     const cx<T>* __restrict__ twBg) {
   using P = FS<T, N>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -256,9 +262,9 @@ __global__ void __launch_bounds__(kThreads) k_xvx_fs(GeoDev g, cx<T>* __restrict
       const int l = t / P::N1, k1 = t - l * P::N1, y = y0 + l;
       cx<T> w[P::N2];
       fs_step_b<1, T, P::N1, P::N2>(Ts + l * P::LS, k1, w);
-      const double* vrow = vpot + (size_t)g.k1 * ((y < g.n2 ? y : 0) + (size_t)g.k2 * z);
+      const T* vrow = vpot + (size_t)g.k1 * ((y < g.n2 ? y : 0) + (size_t)g.k2 * z);
 #pragma unroll
-      for (int k2 = 0; k2 < P::N2; ++k2) w[k2] = scl(w[k2], (y < g.n2) ? (T)vrow[k1 + P::N1 * k2] : (T)0);
+      for (int k2 = 0; k2 < P::N2; ++k2) w[k2] = scl(w[k2], (y < g.n2) ? vrow[k1 + P::N1 * k2] : (T)0);
       // forward: DFT over k2 (stride-N1 elements), twiddle, exchange
       dftn<-1, P::N2>(w);
       cx<T>* line = Ts2 + l * P::LS;

@@ -89,7 +89,9 @@ __global__ void __launch_bounds__(kThreads) k_zinv(GeoDev g, FftPlan p, const cx
           const cx<double> u = c1[ig];
           const cx<double> w = two ? c2[ig] : mk<double>(0.0, 0.0);
           // +G: c1 + i c2 ; -G: conj(c1) + i conj(c2)
-          v = (e > 0) ? mk<T>((T)(u.x - w.y), (T)(u.y + w.x)) : mk<T>((T)(u.x + w.y), (T)(w.x - u.y));
+          const T ux = from_double<T>(u.x), uy = from_double<T>(u.y);
+          const T wx = from_double<T>(w.x), wy = from_double<T>(w.y);
+          v = (e > 0) ? mk<T>(ux - wy, uy + wx) : mk<T>(ux + wy, wx - uy);
         }
       }
     }
@@ -205,7 +207,7 @@ __global__ void __launch_bounds__(kThreads) k_xvx(GeoDev g, FftPlan p, cx<T>* __
   cx<T>* o = (r == a) ? b : a;
   for (int idx = threadIdx.x; idx < nl * N; idx += kThreads) {
     const int l = idx / N, x = idx - l * N, y = y0 + l;
-    const T v = (y < g.n2) ? (T)vpot[x + (size_t)g.k1 * (y + (size_t)g.k2 * z)] : (T)0;
+    const T v = (y < g.n2) ? from_double<T>(vpot[x + (size_t)g.k1 * (y + (size_t)g.k2 * z)]) : (T)0;
     r[l * ls + x] = scl(r[l * ls + x], v);
   }
   __syncthreads();
@@ -268,34 +270,44 @@ __global__ void __launch_bounds__(kThreads) k_zfwd(GeoDev g, FftPlan p, const cx
 #undef GBCP_STAGE
 
 // ---------------------------------------------------------------- decode + kinetic (vpsi_utils.mod.F90:661-671)
+static __global__ void k_v_to_float(const double* __restrict__ v, float* __restrict__ vf, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    vf[i] = d2f_int(v[i]);
+}
+
+template <typename T> __device__ __forceinline__ double to_double(T x);
+template <> __device__ __forceinline__ double to_double<double>(double x) { return x; }
+template <> __device__ __forceinline__ double to_double<float>(float x) { return f2d_int(x); }
+
+// c2 += -f/2 (tpiba2 hg c0 + (Re fp, Im fm)) for state 1 and -f/2 (... + (Im fp, -Re fm))
+// for state 2; fp/fm in the transform precision, the update in FP64 (two FMAs per
+// component; kin = tpiba2 hg precomputed).
 template <typename T>
 __global__ void k_decode(GeoDev g, const cx<T>* __restrict__ qbuf, const cx<double>* __restrict__ c0, int ldc,
                          cx<double>* __restrict__ c2, int ldc2, const double* __restrict__ f, int s0, int nstate,
-                         double tpiba2) {
+                         const double* __restrict__ kin_g) {
   const int ig = blockIdx.x * blockDim.x + threadIdx.x;
   const int pair = blockIdx.y;
   if (ig >= g.ngw) return;
   const int is1 = s0 + 2 * pair, is2 = is1 + 1;
   const cx<T>* qb = qbuf + (size_t)pair * g.nent;
   const cx<T> qp = qb[g.pos_plus[ig]], qm = qb[g.pos_minus[ig]];
-  const double fpx = (double)qp.x + (double)qm.x, fpy = (double)qp.y + (double)qm.y;
-  const double fmx = (double)qp.x - (double)qm.x, fmy = (double)qp.y - (double)qm.y;
-  const double kin = tpiba2 * g.hg[ig];
+  const double kin = kin_g[ig];
   double fi = f[is1] * 0.5;
   if (fi == 0.0) fi = 1.0;
   {
     const cx<double> c = c0[(size_t)is1 * ldc + ig];
     cx<double>& o = c2[(size_t)is1 * ldc2 + ig];
-    o.x += -fi * (kin * c.x + fpx);
-    o.y += -fi * (kin * c.y + fmy);
+    o.x = fma(-fi, fma(kin, c.x, to_double<T>(qp.x + qm.x)), o.x);
+    o.y = fma(-fi, fma(kin, c.y, to_double<T>(qp.y - qm.y)), o.y);
   }
   if (is2 < nstate) {
     double fip1 = f[is2] * 0.5;
     if (fip1 == 0.0) fip1 = 1.0;
     const cx<double> c = c0[(size_t)is2 * ldc + ig];
     cx<double>& o = c2[(size_t)is2 * ldc2 + ig];
-    o.x += -fip1 * (kin * c.x + fpy);
-    o.y += -fip1 * (kin * c.y - fmx);
+    o.x = fma(-fip1, fma(kin, c.x, to_double<T>(qp.y + qm.y)), o.x);
+    o.y = fma(-fip1, fma(kin, c.y, to_double<T>(qm.x - qp.x)), o.y);
   }
 }
 
@@ -431,7 +443,7 @@ int launch_xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double*
   return 0;
 }
 
-template <typename T, int NC> int launch_xvx(Ctx& c, int np, const double* vpot) {
+template <typename T, int NC> int launch_xvx(Ctx& c, int np, const double* vpot, const T* vpotT) {
   const GeoDev& g = c.geo;
   cx<T>* yb = static_cast<cx<T>*>(c.ybuf.p);
   ProfScope ps_(c, "k_xvx");
@@ -439,7 +451,7 @@ template <typename T, int NC> int launch_xvx(Ctx& c, int np, const double* vpot)
     constexpr size_t sm = fs_smem<T, NC>(2, 2);
     allow_smem(k_xvx_fs<T, NC>, sm);
     k_xvx_fs<T, NC><<<dim3((g.n2 + FS<T, NC>::L - 1) / FS<T, NC>::L, g.n3, np), kThreads, sm, c.stream>>>(
-        g, yb, vpot, twA_of<T>(c, 0), twB_of<T>(c, 0));
+        g, yb, vpotT, twA_of<T>(c, 0), twB_of<T>(c, 0));
   } else {
     const int nl = lines_rt(g.n1);
     const size_t sm = stage_smem<T>(g.n1, nl);
@@ -500,7 +512,7 @@ int launch_decode(Ctx& c, int np, const cx<double>* c0, int ldc, cx<double>* c2,
   const GeoDev& g = c.geo;
   ProfScope ps_(c, "k_decode");
   k_decode<T><<<dim3((g.ngw + 255) / 256, np), 256, 0, c.stream>>>(g, static_cast<const cx<T>*>(c.qbuf.p), c0, ldc,
-                                                                     c2, ldc2, f, s0, nstate, c.tpiba2);
+                                                                     c2, ldc2, f, s0, nstate, c.kin);
   GBCP_LAUNCH_CHECK(c);
   return 0;
 }
@@ -512,8 +524,8 @@ template <typename T> int yinv(Ctx& c, int np) { GBCP_DISPATCH(launch_yinv, T, c
 template <typename T> int xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho) {
   GBCP_DISPATCH(launch_xinv_rho, T, c.nr[0], c, np, s0, nstate, f, rho)
 }
-template <typename T> int xvx(Ctx& c, int np, const double* vpot) {
-  GBCP_DISPATCH(launch_xvx, T, c.nr[0], c, np, vpot)
+template <typename T> int xvx(Ctx& c, int np, const double* vpot, const T* vpotT) {
+  GBCP_DISPATCH(launch_xvx, T, c.nr[0], c, np, vpot, vpotT)
 }
 template <typename T> int yfwd(Ctx& c, int np) { GBCP_DISPATCH(launch_yfwd, T, c.nr[1], c, np) }
 template <typename T> int zfwd(Ctx& c, int np) { GBCP_DISPATCH(launch_zfwd, T, c.nr[2], c, np) }
@@ -539,12 +551,23 @@ int vpsi_t(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, cons
   const int npairs_total = (nstate + 1) / 2;
   int rc = ensure_band_buffers<T>(c, std::min(c.batch, npairs_total));
   if (rc) return rc;
+  // V(r) in the transform precision, converted once per call
+  const T* vT = reinterpret_cast<const T*>(vpot);
+  if constexpr (sizeof(T) == 4) {
+    const size_t nnr = (size_t)c.kr[0] * c.kr[1] * c.kr[2];
+    if (!ensure(c, c.st_vf, sizeof(float) * nnr)) return 6;
+    ProfScope ps_(c, "k_v_to_float");
+    k_v_to_float<<<std::max<size_t>(1, std::min<size_t>(2048, (nnr + 255) / 256)), 256, 0, c.stream>>>(
+        vpot, static_cast<float*>(c.st_vf.p), nnr);
+    GBCP_LAUNCH_CHECK(c);
+    vT = reinterpret_cast<const T*>(c.st_vf.p);
+  }
   for (int p0 = 0; p0 < npairs_total; p0 += c.batch) {
     const int np = std::min(c.batch, npairs_total - p0);
     const int s0 = 2 * p0;
     if ((rc = zinv<T>(c, c0, ldc, s0, nstate, np))) return rc;
     if ((rc = yinv<T>(c, np))) return rc;
-    if ((rc = xvx<T>(c, np, vpot))) return rc;
+    if ((rc = xvx<T>(c, np, vpot, vT))) return rc;
     if ((rc = yfwd<T>(c, np))) return rc;
     if ((rc = zfwd<T>(c, np))) return rc;
     if ((rc = launch_decode<T>(c, np, c0, ldc, c2, ldc2, f, s0, nstate))) return rc;

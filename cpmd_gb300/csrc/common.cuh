@@ -27,6 +27,48 @@ template <int S, typename T> __device__ __forceinline__ cx<T> mul_si(cx<T> a) {
   return S > 0 ? mk<T>(-a.y, a.x) : mk<T>(a.y, -a.x);
 }
 
+// ---- precision conversions on the integer pipe --------------------------
+// On GB300 the FP64 pipe runs at 1/58 of the FP32 rate and also executes the
+// F2F/I2F conversions to and from double; in the FP32 kernels those
+// conversions alone kept the FP64 pipe a third busy.  These helpers convert
+// by IEEE-754 bit manipulation with integer instructions instead.
+
+// double -> float, round to nearest even; magnitudes below FLT_MIN flush to 0.
+__device__ __forceinline__ float d2f_int(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned int sign = (unsigned int)(b >> 63) << 31;
+  const int e = (int)((b >> 52) & 0x7FF);
+  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+  if (e == 0x7FF) return __uint_as_float(sign | 0x7F800000u | (m ? 0x400000u : 0u));
+  int ef = e - 1023 + 127;
+  if (ef <= 0) return __uint_as_float(sign);
+  unsigned int r = (unsigned int)(m >> 29);
+  const unsigned int rem = (unsigned int)(m & 0x1FFFFFFFull);
+  if (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) {
+    if (++r == 0x800000u) {
+      r = 0;
+      ++ef;
+    }
+  }
+  if (ef >= 255) return __uint_as_float(sign | 0x7F800000u);
+  return __uint_as_float(sign | ((unsigned int)ef << 23) | r);
+}
+
+// float -> double, exact; float subnormals flush to 0.
+__device__ __forceinline__ double f2d_int(float y) {
+  const unsigned int b = __float_as_uint(y);
+  const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
+  const int ef = (int)((b >> 23) & 0xFF);
+  const unsigned long long m = b & 0x7FFFFFu;
+  if (ef == 0) return __longlong_as_double((long long)sign);
+  if (ef == 255) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull | (m << 29)));
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(ef - 127 + 1023) << 52) | (m << 29)));
+}
+
+template <typename T> __device__ __forceinline__ T from_double(double x);
+template <> __device__ __forceinline__ double from_double<double>(double x) { return x; }
+template <> __device__ __forceinline__ float from_double<float>(double x) { return d2f_int(x); }
+
 // Status codes shared with the C ABI (include/cpmd_gb300.h).
 enum DevStatus : int {
   DEV_OK = 0,

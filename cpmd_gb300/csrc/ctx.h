@@ -42,6 +42,9 @@ struct GeoDev {
   const double* hg;      // ngw
 };
 
+// largest number of state pairs one band-loop launch covers
+constexpr int kMaxBatch = 64;
+
 // Launch shape of one FFT stage: lines per CTA.
 struct StageTune {
   int zl = 0, yl = 0, xl = 0;  // 0 = derive from target element count
@@ -89,11 +92,12 @@ struct Ctx {
   StageTune tune;
   // workspaces
   Scratch zbuf, ybuf, qbuf;
-  Scratch st_c0, st_c2, st_rho, st_vpot, st_f, st_misc, st_misc2;
+  Scratch st_c0, st_c2, st_rho, st_vpot, st_f, st_misc, st_misc2, st_vf;
   Scratch red;      // reductions
   Scratch smat, smat2, smat3, sparts, cscr;
   Scratch nl_a, nl_b, nl_c, nl_d;
   int* d_info = nullptr;
+  double* kin = nullptr;  // tpiba2 * hg (ngw), the kinetic factor of vpsi
   std::string err;
   // profiling
   bool prof = false;

@@ -139,6 +139,39 @@ __device__ __forceinline__ void fold_levels(uint32_t lane_base, long long (&H)[3
   }
 }
 
+// (H 2^28 + Lo) 2^(ee-63) as a correctly rounded double, with integer
+// instructions only (the FP64 pipe, 1/58 of FP32 on GB300, would otherwise
+// bound the epilogue).  Results below the normal range flush to zero.
+__device__ __forceinline__ double fold_to_double(long long H, long long Lo, int ee) {
+  __int128 v = ((__int128)H << 28) + (__int128)Lo;
+  const bool neg = v < 0;
+  unsigned __int128 m = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
+  if (m == 0) return 0.0;
+  const unsigned long long hi = (unsigned long long)(m >> 64), lo = (unsigned long long)m;
+  int top = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);  // index of the leading bit
+  unsigned long long mant;
+  const int sh = top - 52;
+  if (sh > 0) {
+    mant = (unsigned long long)(m >> sh);
+    const unsigned __int128 rem = m & (((unsigned __int128)1 << sh) - 1);
+    const unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
+    if (rem > half || (rem == half && (mant & 1ull))) {
+      if (++mant == (1ull << 53)) {
+        mant >>= 1;
+        ++top;
+      }
+    }
+  } else {
+    mant = lo << (-sh);
+  }
+  const int be = top + ee - 63 + 1023;
+  if (be <= 0) return neg ? -0.0 : 0.0;
+  if (be >= 2047) return __longlong_as_double((long long)((neg ? (1ull << 63) : 0ull) | 0x7FF0000000000000ull));
+  const unsigned long long bits =
+      (neg ? (1ull << 63) : 0ull) | ((unsigned long long)be << 52) | (mant & 0xFFFFFFFFFFFFFull);
+  return __longlong_as_double((long long)bits);
+}
+
 // ---------------------------------------------------------------- exponent pre-passes
 // column maxima |a_kj| over k (state columns of the real view): bits into cmax[j]
 __global__ void k_col_max(const double* __restrict__ Ar, int lda, int K, int n, int kper,
@@ -336,9 +369,7 @@ __global__ void k_ozaki_syrk_finalize(const long long* __restrict__ H, const lon
        e += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(e / n), j = (int)(e % n);
     if (i > j) continue;
-    const int ee = exp_of_max(cmax[i]) + exp_of_max(cmax[j]);
-    double v = ldexp((double)H[e], ee - 35) + ldexp((double)Lo[e], ee - 63);
-    v *= 2.0;
+    double v = 2.0 * fold_to_double(H[e], Lo[e], exp_of_max(cmax[i]) + exp_of_max(cmax[j]));
     if (geq0) v -= Ar[(size_t)i * lda] * Ar[(size_t)j * lda];
     S[(size_t)i * n + j] = v;
     S[(size_t)j * n + i] = v;
@@ -482,8 +513,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       for (int c = 0; c < 32; ++c) {
         const int j = j0 + 32 * (warp >> 2) + c;
         if (j < n) {
-          const int ee = er + exp_of_max(mcmax[j]);
-          Cout[r + (size_t)j * ldo] = ldexp((double)H[c], ee - 35) + ldexp((double)Lo[c], ee - 63);
+          Cout[r + (size_t)j * ldo] = fold_to_double(H[c], Lo[c], er + exp_of_max(mcmax[j]));
         }
       }
     }
