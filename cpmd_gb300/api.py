@@ -266,5 +266,71 @@ class Context:
         return c2
 
 
+    # -- energy functional and its adjoint --------------------------------------
+    def _ensure_dens_sphere(self):
+        if getattr(self, "_dens_set", False):
+            return
+        b = self.basis
+        inyh = np.ascontiguousarray(b.inyh.T.astype(np.int32))            # (nhg, 3) == Fortran (3, nhg)
+        hg = np.ascontiguousarray(b.hg, dtype=np.float64)
+        self._check("gbcp_set_dens_sphere",
+                    self.lib.gbcp_set_dens_sphere(self.h, int(b.nhg), inyh.ctypes.data_as(C.c_void_p),
+                                                  hg.ctypes.data_as(C.c_void_p)))
+        self._dens_set = True
+
+    def energy(self, c0, f, tau=None, vps=None, isp=None, vext=None, grad: bool = True, forces: bool = True):
+        """E[psi, V, R] = E_kin + E_loc + E_H + E_xc (+ E_ext) and its adjoint.
+
+        ``tau``: (nat, 3) == Fortran tau(3, nat); ``vps``: numpy (nhg,) or
+        (nhg, nsp) / torch (nhg,) or (nsp, nhg); ``isp``: host ints (nat,);
+        ``vext``: padded mesh potential or None.  Returns ``terms`` (dict) and,
+        with ``grad``, also (c2, dvloc, fion) -- see include/cpmd_gb300.h.
+        """
+        self._ensure_dens_sphere()
+        ldc, n = _ld_wfn(c0, self.ngw)
+        dev = _is_torch(c0)
+        nhg = int(self.basis.nhg)
+        nat = 0 if tau is None else int(tau.shape[0])
+        if nat:
+            if isp is None:
+                isp = np.zeros(nat, dtype=np.int32)
+            isp = np.ascontiguousarray(np.asarray(isp, dtype=np.int32))
+            nsp = int(isp.max()) + 1
+            if dev:
+                if vps.dim() == 1:
+                    vps = vps.reshape(1, nhg)
+                if tuple(vps.shape) != (nsp, nhg):
+                    raise ValueError("vps must be (nsp, nhg) on the device")
+            else:
+                vps = np.asarray(vps, dtype=np.float64).reshape(nhg, -1, order="F")
+                if vps.shape[1] != nsp:
+                    raise ValueError("vps must be (nhg, nsp)")
+                vps = np.asfortranarray(vps)
+                tau = np.ascontiguousarray(tau, dtype=np.float64)
+        else:
+            nsp, isp, vps, tau = 1, None, None, None
+        c2 = dv = fion = None
+        if grad:
+            if dev:
+                import torch
+                c2 = torch.empty((n, self.ngw), dtype=torch.complex128, device=c0.device)
+                dv = torch.empty(self.kr[::-1], dtype=torch.float64, device=c0.device)
+                fion = torch.empty((max(nat, 1), 3), dtype=torch.float64, device=c0.device) if (forces and nat) else None
+            else:
+                c2 = np.zeros((self.ngw, n), dtype=np.complex128, order="F")
+                dv = np.empty(self.kr[::-1])
+                fion = np.empty((nat, 3)) if (forces and nat) else None
+        mem = self._prep(c0, f, tau, vps, vext, c2, dv, fion)
+        e = (C.c_double * 6)()
+        isp_p = isp.ctypes.data_as(C.c_void_p) if isp is not None else None
+        self._check("gbcp_energy", self.lib.gbcp_energy(
+            self.h, _ptr(c0), ldc, n, _ptr(f), nat, nsp, isp_p, _ptr(tau), _ptr(vps), _ptr(vext), e,
+            _ptr(c2), self.ngw, _ptr(dv), _ptr(fion), mem))
+        terms = dict(etot=e[0], ekin=e[1], eloc=e[2], ehart=e[3], exc=e[4], eext=e[5])
+        if grad:
+            return terms, c2, dv, fion
+        return terms
+
+
 def kernel_launches() -> int:
     return int(_lib.load().gbcp_kernel_launches())

@@ -357,7 +357,9 @@ int gbcp_ctx_destroy(gbcp_ctx* h) {
   for (void* p : c.dev_allocs) cudaFree(p);
   gbcp::Scratch* all[] = {&c.zbuf, &c.ybuf, &c.qbuf, &c.st_c0, &c.st_c2, &c.st_rho, &c.st_vpot, &c.st_f,
                           &c.st_misc, &c.st_misc2, &c.st_vf, &c.red, &c.smat, &c.smat2, &c.smat3, &c.sparts, &c.cscr,
-                          &c.nl_a, &c.nl_b, &c.nl_c, &c.nl_d};
+                          &c.nl_a, &c.nl_b, &c.nl_c, &c.nl_d, &c.en_rho, &c.en_a, &c.en_b, &c.en_veff,
+                          &c.en_red, &c.en_ei, &c.en_fp, &c.en_idx, &c.en_in[0], &c.en_in[1], &c.en_in[2],
+                          &c.en_in[3], &c.en_in[4]};
   for (auto* s : all) gbcp::release(*s);
   if (c.d_info) cudaFree(c.d_info);
   gbcp::prof_fold(c);
@@ -714,6 +716,123 @@ int gbcp_fnonloc(gbcp_ctx* h, double* c2, int ldc2, int nstate, const double* f,
   if (!rc && mem == GBCP_MEM_HOST) rc = stage_out_cx(c, dc2, c2, ldc2, c.ngw, nstate);
   if (mem == GBCP_MEM_HOST || rc) return finish(c, rc);
   return GBCP_OK;
+}
+
+int gbcp_set_dens_sphere(gbcp_ctx* h, int nhg, const int32_t* inyh, const double* hg) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  if (nhg < c.ngw || !inyh || !hg) return set_err(h, GBCP_ERR_ARG, "set_dens_sphere: bad argument");
+  c.err.clear();
+  const int n[3] = {c.nr[0], c.nr[1], c.nr[2]};
+  std::vector<int> pos(nhg), neg(nhg);
+  std::vector<short4> mill(nhg);
+  std::vector<double> g2(nhg);
+  int dmax = 0;
+  for (int ig = 0; ig < nhg; ++ig) {
+    int m[3], p[3], q[3];
+    for (int a = 0; a < 3; ++a) {
+      m[a] = inyh[3 * (size_t)ig + a] - (n[a] / 2 + 1);
+      if (2 * std::abs(m[a]) >= n[a] || std::abs(m[a]) > 32767)
+        return set_err(h, GBCP_ERR_ARG, "set_dens_sphere: G vector outside the mesh");
+      dmax = std::max(dmax, std::abs(m[a]));
+      p[a] = ((m[a] % n[a]) + n[a]) % n[a];
+      q[a] = ((-m[a] % n[a]) + n[a]) % n[a];
+    }
+    pos[ig] = p[0] + c.kr[0] * (p[1] + c.kr[1] * p[2]);
+    neg[ig] = q[0] + c.kr[0] * (q[1] + c.kr[1] * q[2]);
+    mill[ig] = make_short4((short)m[0], (short)m[1], (short)m[2], 0);
+    g2[ig] = hg[ig] * c.tpiba2;
+  }
+  const int *dp, *dn;
+  const short4* dm;
+  const double* dg;
+  if (!gbcp::upload(c, pos, dp) || !gbcp::upload(c, neg, dn) || !gbcp::upload(c, mill, dm) ||
+      !gbcp::upload(c, g2, dg))
+    return set_err(h, GBCP_ERR_NOMEM, "set_dens_sphere: upload failed");
+  c.dpos = dp;
+  c.dneg = dn;
+  c.dmill = dm;
+  c.dg2 = dg;
+  c.dmax = dmax;
+  c.nhg = nhg;
+  return GBCP_OK;
+}
+
+int gbcp_energy(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double* f, int nat, int nsp,
+                const int32_t* isp, const double* tau, const double* vps, const double* vext, double* energies,
+                double* c2, int ldc2, double* dvloc, double* fion, int mem) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  if (bad_mem(mem) || nstate <= 0 || nat < 0 || nsp <= 0 || !c0 || !f || !energies || ldc < c.ngw ||
+      (nat > 0 && (!isp || !tau || !vps)) || (c2 && ldc2 < c.ngw))
+    return set_err(h, GBCP_ERR_ARG, "energy: bad argument");
+  if (c.nhg <= 0) return set_err(h, GBCP_ERR_ARG, "energy: call gbcp_set_dens_sphere first");
+  c.err.clear();
+  const size_t nnr1 = (size_t)c.kr[0] * c.kr[1] * c.kr[2];
+  const cx<double>* dc0 = reinterpret_cast<const cx<double>*>(c0);
+  cx<double>* dc2 = reinterpret_cast<cx<double>*>(c2);
+  const double *df = f, *dtau = tau, *dvps = vps, *dvext = vext;
+  double *ddv = dvloc, *dfi = fion;
+  int l0 = ldc, l2 = ldc2;
+  int rc = 0;
+  static const double zero3[3] = {0.0, 0.0, 0.0};
+  static const int32_t zero_sp[1] = {0};
+  const int nat_eff = nat > 0 ? nat : 1;  // no atoms: one atom of zero form factor
+  const int32_t* isp_h = nat > 0 ? isp : zero_sp;
+  if (mem == GBCP_MEM_HOST) {
+    cx<double>* t0;
+    void *tf, *tt, *tv, *te;
+    if ((rc = stage_in_cx(c, c.st_c0, c0, ldc, c.ngw, nstate, &t0))) return rc;
+    if ((rc = stage_in(c, c.st_f, f, sizeof(double) * nstate, &tf))) return rc;
+    if ((rc = stage_in(c, c.en_in[0], nat > 0 ? tau : zero3, sizeof(double) * 3 * nat_eff, &tt))) return rc;
+    dc0 = t0;
+    df = static_cast<double*>(tf);
+    dtau = static_cast<double*>(tt);
+    if (nat > 0) {
+      if ((rc = stage_in(c, c.en_in[1], vps, sizeof(double) * (size_t)c.nhg * nsp, &tv))) return rc;
+      dvps = static_cast<double*>(tv);
+    }
+    if (vext) {
+      if ((rc = stage_in(c, c.en_in[2], vext, sizeof(double) * nnr1, &te))) return rc;
+      dvext = static_cast<double*>(te);
+    }
+    if (c2) {
+      if (!gbcp::ensure(c, c.st_c2, sizeof(cx<double>) * (size_t)c.ngw * nstate)) return GBCP_ERR_NOMEM;
+      dc2 = static_cast<cx<double>*>(c.st_c2.p);
+      l2 = c.ngw;
+    }
+    if (dvloc) {
+      if (!gbcp::ensure(c, c.en_in[3], sizeof(double) * nnr1)) return GBCP_ERR_NOMEM;
+      ddv = static_cast<double*>(c.en_in[3].p);
+    }
+    if (fion) {
+      if (!gbcp::ensure(c, c.en_in[4], sizeof(double) * 3 * nat_eff)) return GBCP_ERR_NOMEM;
+      dfi = static_cast<double*>(c.en_in[4].p);
+    }
+    l0 = c.ngw;
+  }
+  if (nat == 0) {
+    // a single dummy atom at the origin with a zero form factor
+    if (mem == GBCP_MEM_DEVICE) {
+      if (!gbcp::ensure(c, c.en_in[0], sizeof(double) * 3)) return GBCP_ERR_NOMEM;
+      GBCP_CUDA_TRY(c, cudaMemsetAsync(c.en_in[0].p, 0, sizeof(double) * 3, c.stream));
+      dtau = static_cast<double*>(c.en_in[0].p);
+    }
+    if (!gbcp::ensure(c, c.en_in[1], sizeof(double) * (size_t)c.nhg)) return GBCP_ERR_NOMEM;
+    GBCP_CUDA_TRY(c, cudaMemsetAsync(c.en_in[1].p, 0, sizeof(double) * (size_t)c.nhg, c.stream));
+    dvps = static_cast<double*>(c.en_in[1].p);
+    nsp = 1;
+  }
+  double* fion_dev = (fion && nat > 0) ? dfi : nullptr;
+  rc = gbcp::energy_and_grad(c, dc0, l0, nstate, df, nat_eff, nsp, isp_h, dtau, dvps, dvext, energies, dc2, l2, ddv,
+                             fion_dev);
+  if (!rc && mem == GBCP_MEM_HOST) {
+    if (c2) rc = stage_out_cx(c, dc2, c2, ldc2, c.ngw, nstate);
+    if (!rc && dvloc) GBCP_CUDA_TRY(c, cudaMemcpyAsync(dvloc, ddv, sizeof(double) * nnr1, cudaMemcpyDeviceToHost, c.stream));
+    if (!rc && fion && nat > 0)
+      GBCP_CUDA_TRY(c, cudaMemcpyAsync(fion, dfi, sizeof(double) * 3 * nat, cudaMemcpyDeviceToHost, c.stream));
+  }
+  return finish(c, rc);
 }
 
 }  // extern "C"

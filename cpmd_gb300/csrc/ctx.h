@@ -98,6 +98,13 @@ struct Ctx {
   Scratch nl_a, nl_b, nl_c, nl_d;
   int* d_info = nullptr;
   double* kin = nullptr;  // tpiba2 * hg (ngw), the kinetic factor of vpsi
+  // density sphere of the energy functional (gbcp_set_dens_sphere)
+  int nhg = 0, dmax = 0;           // half-sphere size, largest |Miller index|
+  const int* dpos = nullptr;       // offset of +G in the (kr1, kr2, nr3) complex grid
+  const int* dneg = nullptr;       // offset of -G
+  const short4* dmill = nullptr;   // Miller indices (x, y, z, 0)
+  const double* dg2 = nullptr;     // |G|^2 in bohr^-2
+  Scratch en_rho, en_a, en_b, en_veff, en_red, en_ei, en_fp, en_idx, en_in[5];
   std::string err;
   // profiling
   bool prof = false;
@@ -152,6 +159,11 @@ inline bool use_tc_gemm(const Ctx& c) { return c.gemm_mode == 1 || (c.gemm_mode 
 int chol_inverse(Ctx& c, double* S, double* X, int n);
 int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host);
 int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host);
+
+// ---- energy functional and its adjoint (energy.cu) ----
+int energy_and_grad(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, int nat, int nsp,
+                    const int* isp_host, const double* tau, const double* vps, const double* vext,
+                    double* energies_host, cx<double>* c2, int ldc2, double* dvloc, double* fion);
 
 // ---- projectors (nonlocal.cu) ----
 int nl_rnlsm1(Ctx& c, const cx<double>* c0, int ldc, int nstate, int nat, int ngh, const int* nghtol_host,

@@ -167,6 +167,35 @@ int gbcp_fnonloc(gbcp_ctx* ctx, double* c2, int ldc2, int nstate, const double* 
                  const int32_t* nghtol, const double* twnl, const double* eigr, const double* fnl,
                  const double* wsg, int mem);
 
+/* Density sphere of the energy functional (cppt: nhg, inyh(3,nhg), hg(nhg);
+ * the first ngw entries are the wavefunction sphere of gbcp_grid_desc).
+ * Host arrays; copied once (the reference's loadpa/rggen set-up). */
+int gbcp_set_dens_sphere(gbcp_ctx* ctx, int nhg, const int32_t* inyh, const double* hg);
+
+/* Energy of the local-potential Kohn-Sham functional and its adjoint
+ * (the proposed gbcp_energy_and_grad; the reference computes the same terms
+ * in vofrhoa_utils.mod.F90:41-144, ppener_utils.mod.F90:23-108,
+ * potfor_utils.mod.F90:38-110, cp_lda_*; cubic cell):
+ *   E = E_kin + E_loc + E_H + E_xc + E_ext,
+ *   V_ion(G) = sum_a vps(G, isp[a]) e^{-iG.R_a}, E_loc = Omega sum_G conj(rho(G)) V_ion(G),
+ *   E_H = Omega sum_{G!=0,half} 4 pi |rho(G)|^2 / G^2, E_xc = LDA (Slater + Perdew-Zunger),
+ *   E_ext = Omega/N sum_r vext rho (vext may be NULL).
+ * Inputs: c0 (ngw, nstate), f (nstate), tau (3, nat) bohr, vps (nhg, nsp)
+ * form factors per unit volume, isp (nat) species 0..nsp-1 (HOST array in
+ * both memory modes), vext (kr1, kr2, kr3) or NULL.  nat = 0 means no ions.
+ * Outputs (any of c2 / dvloc / fion may be NULL):
+ *   energies[6] (host) = {E, E_kin, E_loc, E_H, E_xc, E_ext} in Ha;
+ *   c2 (ngw, nstate) overwritten with the CP force -(f/2)(G^2 c + 2 [V_eff psi](G)),
+ *     i.e. the reference's vpsi applied to V_eff = V_ion + V_H + v_xc + vext;
+ *     dE = -4 Re sum_G w_G conj(dc) c2 with w = 1/2 at G = 0, 1 elsewhere
+ *     (states with f = 0 follow vpsi's convention and are not gradients);
+ *   dvloc (kr1, kr2, kr3) = dE/dV(r) = rho(r) Omega / (nr1 nr2 nr3);
+ *   fion (3, nat) overwritten with -dE/dR.
+ * The band loop runs in the context precision; everything else is FP64. */
+int gbcp_energy(gbcp_ctx* ctx, const double* c0, int ldc, int nstate, const double* f, int nat, int nsp,
+                const int32_t* isp, const double* tau, const double* vps, const double* vext, double* energies,
+                double* c2, int ldc2, double* dvloc, double* fion, int mem);
+
 #ifdef __cplusplus
 }
 #endif

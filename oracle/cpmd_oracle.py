@@ -274,3 +274,124 @@ def fnonloc(c2, f, fnl, twnl, eigr, nghtol, wsg):
         ctm = _ci(nghtol[iv]) * (-ffi * wsg[iv])                   # (nstate,)
         out += twnl[:, iv][:, None] * (auxc * ctm[None, :])
     return out
+
+
+# ----------------------------------------------------------------------------
+# Energy functional E[psi, V_loc, R] and its adjoint
+# ----------------------------------------------------------------------------
+# E = E_kin + E_loc + E_H + E_xc (+ E_ext for an optional mesh potential):
+#   V_ion(G) = sum_a vps(G, sp_a) e^{-iG.R_a}            eicalc_utils.mod.F90:33-173,
+#                                                        phfac_utils.mod.F90:195 (eigr)
+#   rho(G)   = fwfftn(rho(r))                            vofrhoa_utils.mod.F90:90-96
+#   E_loc    = Omega sum_G conj(rho(G)) V_ion(G)         ppener_utils.mod.F90:58-99
+#              (EPSEU = 2 Re(eps) Omega, G = 0 counted once)   vofrhoa_utils.mod.F90:125
+#   E_H      = Omega sum_{G!=0, half} 4 pi |rho(G)|^2 / G^2    ppener (eh), scg = 4 pi / G^2
+#   E_xc     = Omega/N sum_r rho eps_xc(rho), Slater x (alpha = 2/3) + PZ c
+#              cp_lda_exchange_utils.mod.F90:74-97, cp_lda_correlation_utils.mod.F90:448-513
+#   forces   F_a = 2 Omega sum_{G!=0, half} Re[e^{-iG.R_a} vps conj(rho(G)) iG]
+#              potfor_utils.mod.F90:91-110 (omtp = 2 Omega tpiba)
+#   dE/dc*   the CP force C2 = vpsi(c0, 0, f, V_eff), V_eff = V_ion + V_H + v_xc + V_ext
+#   dE/dV(r) = rho(r) Omega / N  (N = nr1 nr2 nr3)
+RHO_XC_MIN = 1.0e-30   # densities at or below this carry no xc energy or potential
+
+# Perdew-Zunger 1981 parametrisation of the unpolarised correlation energy
+_PZ = dict(a=0.0311, b=-0.048, c=0.0020, d=-0.0116, gc=-0.1423, b1=1.0529, b2=0.3334)
+_SLATER_ALPHA = 2.0 / 3.0
+
+
+def xc_lda_pz(rho: np.ndarray):
+    """(rho * eps_xc, v_xc) per point; Slater exchange with alpha = 2/3 and PZ correlation."""
+    rho = np.asarray(rho, dtype=np.float64)
+    ok = rho > RHO_XC_MIN
+    r = np.where(ok, rho, 1.0)
+    # X-alpha exchange: rho eps_x = -(9/8) alpha (3/pi)^(1/3) rho^(4/3), v_x = (4/3) eps_x
+    cx = 1.5 * _SLATER_ALPHA * (3.0 / math.pi) ** (1.0 / 3.0)     # (3/pi)^(1/3) at alpha = 2/3
+    r13 = np.cbrt(r)
+    ex = -0.75 * cx * r13
+    vx = -cx * r13
+    rs = (3.0 / (4.0 * math.pi * r)) ** (1.0 / 3.0)
+    p = _PZ
+    hi = rs < 1.0
+    xln = np.log(np.where(hi, rs, 1.0))
+    ec_hi = p["a"] * xln + p["b"] + p["c"] * rs * xln + p["d"] * rs
+    vc_hi = p["a"] * xln + (p["b"] - p["a"] / 3.0) + 2.0 / 3.0 * p["c"] * rs * xln + (2.0 * p["d"] - p["c"]) / 3.0 * rs
+    x = np.sqrt(np.where(hi, 1.0, rs))
+    ox = 1.0 + p["b1"] * x + p["b2"] * rs
+    dox = 1.0 + 7.0 / 6.0 * p["b1"] * x + 4.0 / 3.0 * p["b2"] * rs
+    ec_lo = p["gc"] / ox
+    vc_lo = ec_lo * dox / ox
+    ec = np.where(hi, ec_hi, ec_lo)
+    vc = np.where(hi, vc_hi, vc_lo)
+    e = np.where(ok, rho * (ex + ec), 0.0)
+    v = np.where(ok, vx + vc, 0.0)
+    return e, v
+
+
+def structure_phase(mill, tau, tpiba):
+    """eigr(G, a) = e^{-i G.R_a}, G = mill * tpiba (cubic cell)."""
+    return np.exp(-1j * tpiba * (mill.astype(np.float64) @ np.asarray(tau, dtype=np.float64).T))
+
+
+def gaussian_vps(hg, tpiba2, omega, amp=-4.0, width2=1.0):
+    """Form factor of v(r) = amp exp(-r^2/width2): vps(G) = amp (pi w)^(3/2) e^{-w G^2/4} / Omega."""
+    g2 = np.asarray(hg) * tpiba2
+    return amp * (math.pi * width2) ** 1.5 * np.exp(-width2 * g2 / 4.0) / omega
+
+
+def energy(c0, f, basis, tau, vps, isp, vext=None, grad=True):
+    """Energy terms, C2 = -(1/2) dE/dc* in the reference's vpsi normalisation, dE/dV(r), forces.
+
+    ``basis`` carries the density half sphere (mill, hg; first ngw = wavefunction
+    sphere); ``vps`` is (nhg, nsp); ``isp`` (nat,) species of each atom;
+    ``vext`` an optional extra potential on the padded mesh (kr3, kr2, kr1).
+    """
+    nr, kr = basis.nr, basis.kr
+    n1, n2, n3 = nr
+    N = float(n1 * n2 * n3)
+    om = basis.omega
+    geq0 = basis.geq0
+    rho, ekin, _, _ = rhoofr(c0, f, basis.mill, nr, kr, om, basis.hg, basis.tpiba2, geq0)
+    r = rho[:n3, :n2, :n1]
+    rg_full = fwfftn(r.astype(np.complex128))
+    mill = np.asarray(basis.mill, dtype=np.int64)
+    ip = _grid_index(mill, nr)
+    im = _grid_index(-mill, nr)
+    rg = rg_full[ip]
+    eig = structure_phase(mill, tau, basis.tpiba)                 # (nhg, nat)
+    vps = np.asarray(vps, dtype=np.float64).reshape(len(mill), -1)
+    isp = np.asarray(isp, dtype=np.int64)
+    vion = np.einsum("ga,ga->g", eig, vps[:, isp])
+    w = np.full(len(mill), 2.0)
+    if geq0:
+        w[0] = 1.0
+    eloc = om * float(np.sum(w * (np.conj(rg) * vion).real))
+    g2 = basis.hg * basis.tpiba2
+    nz = g2 > 1e-12
+    scg = np.zeros_like(g2)
+    scg[nz] = 4.0 * math.pi / g2[nz]
+    ehart = om * float(np.sum(scg * np.abs(rg) ** 2))
+    exc_d, vxc = xc_lda_pz(r)
+    exc = om / N * float(exc_d.sum())
+    eext = 0.0
+    if vext is not None:
+        eext = om / N * float(np.sum(vext[:n3, :n2, :n1] * r))
+    terms = dict(ekin=ekin, eloc=eloc, ehart=ehart, exc=exc, eext=eext)
+    terms["etot"] = ekin + eloc + ehart + exc + eext
+    if not grad:
+        return terms
+    a = np.zeros((n3, n2, n1), dtype=np.complex128)
+    vg = vion + scg * rg
+    a[im] = np.conj(vg)
+    a[ip] = vg
+    veff = invfftn(a).real + vxc
+    if vext is not None:
+        veff = veff + vext[:n3, :n2, :n1]
+    vfull = np.zeros((kr[2], kr[1], kr[0]))
+    vfull[:n3, :n2, :n1] = veff
+    c2 = vpsi(c0, np.zeros_like(c0), f, vfull, basis.mill, nr, basis.hg, basis.tpiba2, geq0)
+    dvloc = rho * (om / N)
+    gcart = mill.astype(np.float64) * basis.tpiba
+    wf = np.where(nz, 2.0 * om, 0.0)
+    t = eig * (vps[:, isp] * np.conj(rg)[:, None])                 # (nhg, nat)
+    fion = np.einsum("g,gd,ga->ad", wf, gcart, (1j * t).real)
+    return terms, c2, dvloc, fion, veff
