@@ -96,6 +96,7 @@ struct Ctx {
   Scratch red;      // reductions
   Scratch smat, smat2, smat3, sparts, cscr;
   Scratch nl_a, nl_b, nl_c, nl_d;
+  Scratch nl_ta, nl_tb, nl_tp;  // projector GEMM slices (A, B) and split-K partials
   int* d_info = nullptr;
   double* kin = nullptr;  // tpiba2 * hg (ngw), the kinetic factor of vpsi
   // density sphere of the energy functional (gbcp_set_dens_sphere)

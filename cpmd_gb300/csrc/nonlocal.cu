@@ -7,15 +7,24 @@
 //   auxc(G,i) = sum_ia eigr(G,ia) fnl(ia,iv,i)            (dgemm 'N','N')
 //   c2(G,i) += twnl(G,iv) (-i)^l (-f_i wsg(iv)) auxc(G,i)
 //
-// GB300 form: all projectors of the species in ONE GEMM each, with the
-// (-i)^l twnl eigr operand generated tile by tile in shared memory instead of
-// being materialised (the reference builds scr per (iv) and calls dgemm per
-// projector).  rnlsm1 is a split-K reduction over G; fnonloc accumulates
-// straight into c2.
+// GB300 form: all projectors of the species in ONE GEMM each (the reference
+// builds scr per (iv) and calls dgemm per projector).
+//  * FP64 (the drop-in): SIMT FP64 GEMMs with the (-i)^l twnl eigr operand
+//    generated tile by tile in shared memory; rnlsm1 is a split-K reduction
+//    over G, fnonloc accumulates straight into c2.
+//  * mixed precision: the operands are converted to FP32 and split into three
+//    bf16 slices (x = x0 + x1 + x2) in HBM, K-major, and the product runs on the
+//    tcgen05 tensor cores through TMA (tc_gemm.cu) as the six slice pairs
+//    s + t <= 2 accumulated in FP32 -- the accuracy of an FP32 GEMM.
+//      rnlsm1:  fnl (P x n) = 2 scr^T c over K = 2 ngw real rows, split-K
+//               partials folded in FP64;
+//      fnonloc: c2 (2 ngw x n, real view) += Y Z over K = P projectors,
+//               Y = (-i)^l twnl eigr, Z = -f wsg fnl, FP64 read-modify-write.
 #include <algorithm>
 #include <vector>
 
 #include "ctx.h"
+#include "tc_gemm.h"
 
 namespace gbcp {
 
@@ -182,12 +191,207 @@ bool make_info(Ctx& c, int nat, int ngh, const int* nghtol, ProjInfo& pi) {
   return true;
 }
 
+// ---------------------------------------------------------------- mixed precision: bf16 slices
+__device__ __forceinline__ uint32_t bf16_rn(float x) {
+  const uint32_t u = __float_as_uint(x);
+  return (u + 0x7FFFu + ((u >> 16) & 1u)) >> 16;
+}
+// x = x0 + x1 + x2 (bf16 bit patterns), each the bf16 rounding of the remainder
+__device__ __forceinline__ void split3(float x, uint32_t (&h)[3]) {
+  h[0] = bf16_rn(x);
+  float r = x - __uint_as_float(h[0] << 16);
+  h[1] = bf16_rn(r);
+  r = r - __uint_as_float(h[1] << 16);
+  h[2] = bf16_rn(r);
+}
+__device__ __forceinline__ void phase_lf(int l, float& re, float& im) {
+  const float x = re, y = im;
+  switch (l & 3) {
+    case 0: break;
+    case 1: re = y; im = -x; break;
+    case 2: re = -x; im = -y; break;
+    default: re = -y; im = x; break;
+  }
+}
+
+// rnlsm1 A operand: slice s, row p = ia + nat*iv, columns (2G, 2G+1) = scr(G) with G = 0 halved
+__global__ void __launch_bounds__(256) k_nl_scr3(const double* __restrict__ twnl, const cx<double>* __restrict__ eigr,
+                                                 int ngw, ProjInfo pi, int geq0, size_t kstride,
+                                                 uint32_t* __restrict__ A) {
+  const int G = blockIdx.x * 256 + threadIdx.x, a = blockIdx.y;
+  if (G >= ngw) return;
+  const size_t P = (size_t)pi.nat * pi.ngh;
+  const cx<double> e = eigr[G + (size_t)ngw * a];
+  const float ex = d2f_int(e.x), ey = d2f_int(e.y);
+  const float half = (geq0 && G == 0) ? 0.5f : 1.0f;
+  for (int iv = 0; iv < pi.ngh; ++iv) {
+    const float tw = d2f_int(twnl[G + (size_t)ngw * iv]) * half;
+    float re = tw * ex, im = tw * ey;
+    phase_lf(pi.lmod4[iv], re, im);
+    uint32_t hr[3], hi[3];
+    split3(re, hr);
+    split3(im, hi);
+    const size_t p = (size_t)a + (size_t)pi.nat * iv;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) A[((s * P + p) * kstride) / 2 + G] = hr[s] | (hi[s] << 16);
+  }
+}
+
+// rnlsm1 B operand: slice s, row i, columns (2G, 2G+1) = c0(G, i)
+__global__ void __launch_bounds__(256) k_nl_c3(const cx<double>* __restrict__ c0, int ldc, int ngw, int nstate,
+                                               size_t kstride, uint32_t* __restrict__ B) {
+  const int G = blockIdx.x * 256 + threadIdx.x, i = blockIdx.y;
+  if (G >= ngw) return;
+  const cx<double> v = c0[G + (size_t)ldc * i];
+  uint32_t hr[3], hi[3];
+  split3(d2f_int(v.x), hr);
+  split3(d2f_int(v.y), hi);
+#pragma unroll
+  for (int s = 0; s < 3; ++s) B[(((size_t)s * nstate + i) * kstride) / 2 + G] = hr[s] | (hi[s] << 16);
+}
+
+// fnl[p + P i] = 2 sum_split part[(split n + i) P + p]
+__global__ void k_nl_fnl_fold(const float* __restrict__ part, int nsplit, size_t Pn, double* __restrict__ fnl) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < Pn; e += (size_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < nsplit; ++k) s += f2d_int(part[k * Pn + e]);
+    fnl[e] = 2.0 * s;
+  }
+}
+
+// fnonloc A operand: slice s, row 2G + c (c = re, im), column p = ia + nat*iv: Y(G, p)
+__global__ void __launch_bounds__(256) k_nl_y3(const double* __restrict__ twnl, const cx<double>* __restrict__ eigr,
+                                               int ngw, ProjInfo pi, size_t kstride, uint16_t* __restrict__ A) {
+  __shared__ float2 es[32][33];
+  __shared__ float tws[kMaxProj][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int G0 = blockIdx.x * 32, a0 = blockIdx.y * 32;
+  for (int j = ty; j < 32; j += 8) {
+    const int a = a0 + j, G = G0 + tx;
+    float2 v = make_float2(0.f, 0.f);
+    if (a < pi.nat && G < ngw) {
+      const cx<double> e = eigr[G + (size_t)ngw * a];
+      v = make_float2(d2f_int(e.x), d2f_int(e.y));
+    }
+    es[j][tx] = v;
+  }
+  for (int iv = ty; iv < pi.ngh; iv += 8) tws[iv][tx] = (G0 + tx < ngw) ? d2f_int(twnl[G0 + tx + (size_t)ngw * iv]) : 0.f;
+  __syncthreads();
+  const size_t rows = 2 * (size_t)ngw;
+  const int a = a0 + tx;
+  if (a >= pi.nat) return;
+  for (int gg = ty; gg < 32; gg += 8) {
+    const int G = G0 + gg;
+    if (G >= ngw) break;
+    const float2 e = es[tx][gg];
+    for (int iv = 0; iv < pi.ngh; ++iv) {
+      float re = tws[iv][gg] * e.x, im = tws[iv][gg] * e.y;
+      phase_lf(pi.lmod4[iv], re, im);
+      uint32_t hr[3], hi[3];
+      split3(re, hr);
+      split3(im, hi);
+      const size_t p = (size_t)a + (size_t)pi.nat * iv;
+#pragma unroll
+      for (int s = 0; s < 3; ++s) {
+        A[(s * rows + 2 * (size_t)G) * kstride + p] = (uint16_t)hr[s];
+        A[(s * rows + 2 * (size_t)G + 1) * kstride + p] = (uint16_t)hi[s];
+      }
+    }
+  }
+}
+
+// fnonloc B operand: slice s, row i, column p: Z(p, i) = -f_i wsg(iv) fnl(p, i), f < 1e-5 counted as 1
+__global__ void k_nl_z3(const double* __restrict__ fnl, const double* __restrict__ f, const double* __restrict__ wsg,
+                        int nat, size_t P, int nstate, size_t kstride, uint16_t* __restrict__ B) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < P * nstate; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t i = e / P, p = e % P;
+    const int iv = (int)(p / nat);
+    const double fi = f[i] < 1e-5 ? 1.0 : f[i];
+    uint32_t h[3];
+    split3(d2f_int(-fi * wsg[iv] * fnl[e]), h);
+#pragma unroll
+    for (int s = 0; s < 3; ++s) B[((size_t)s * nstate + i) * kstride + p] = (uint16_t)h[s];
+  }
+}
+
+constexpr int kPairS[6] = {0, 0, 1, 0, 1, 2};
+constexpr int kPairT[6] = {0, 1, 0, 2, 1, 0};
+
+size_t round8(size_t x) { return (x + 7) & ~size_t(7); }
+
+int check_status(Ctx& c) {
+  int st = 0;
+  GBCP_CUDA_TRY(c, cudaMemcpyAsync(&st, c.d_info, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  if (st == -2) {
+    c.err = "projector GEMM: tensor-core pipeline wait expired";
+    return 4;
+  }
+  return 0;
+}
+
+int rnlsm1_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, const ProjInfo& pi, const double* twnl,
+              const cx<double>* eigr, double* fnl) {
+  const int P = pi.nat * pi.ngh;
+  const int K = 2 * c.ngw;
+  const size_t ks = round8((size_t)K);
+  if (!ensure(c, c.nl_ta, 2 * 3 * ks * (size_t)P) || !ensure(c, c.nl_tb, 2 * 3 * ks * (size_t)nstate)) return 6;
+  const int ksplit = tc_gemm_splits_used(P, nstate, K, tc_gemm_ksplit(P, nstate, K));
+  if (!ensure(c, c.nl_tp, sizeof(float) * (size_t)ksplit * P * nstate)) return 6;
+  {
+    ProfScope ps_(c, "k_nl_slices");
+    k_nl_scr3<<<dim3((c.ngw + 255) / 256, pi.nat), 256, 0, c.stream>>>(twnl, eigr, c.ngw, pi, c.geq0, ks,
+                                                                      static_cast<uint32_t*>(c.nl_ta.p));
+    GBCP_LAUNCH_CHECK(c);
+    k_nl_c3<<<dim3((c.ngw + 255) / 256, nstate), 256, 0, c.stream>>>(c0, ldc, c.ngw, nstate, ks,
+                                                                    static_cast<uint32_t*>(c.nl_tb.p));
+    GBCP_LAUNCH_CHECK(c);
+  }
+  GBCP_CUDA_TRY(c, cudaMemsetAsync(c.d_info, 0, sizeof(int), c.stream));
+  int rc = tc_gemm_split3(c, static_cast<const uint16_t*>(c.nl_ta.p), P, static_cast<const uint16_t*>(c.nl_tb.p),
+                          nstate, K, (int)ks, 6, kPairS, kPairT, 0, static_cast<float*>(c.nl_tp.p), ksplit, nullptr,
+                          0, c.d_info);
+  if (rc) return rc;
+  {
+    ProfScope ps_(c, "k_nl_fnl_fold");
+    k_nl_fnl_fold<<<1024, 256, 0, c.stream>>>(static_cast<const float*>(c.nl_tp.p), ksplit, (size_t)P * nstate, fnl);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  return check_status(c);
+}
+
+int fnonloc_tc(Ctx& c, cx<double>* c2, int ldc2, int nstate, const double* f, const ProjInfo& pi,
+               const double* twnl, const cx<double>* eigr, const double* fnl, const double* wsg) {
+  const int P = pi.nat * pi.ngh;
+  const int M = 2 * c.ngw;
+  const size_t ks = round8((size_t)P);
+  if (!ensure(c, c.nl_ta, 2 * 3 * ks * (size_t)M) || !ensure(c, c.nl_tb, 2 * 3 * ks * (size_t)nstate)) return 6;
+  {
+    ProfScope ps_(c, "k_nl_slices");
+    k_nl_y3<<<dim3((c.ngw + 31) / 32, (pi.nat + 31) / 32), 256, 0, c.stream>>>(twnl, eigr, c.ngw, pi, ks,
+                                                                              static_cast<uint16_t*>(c.nl_ta.p));
+    GBCP_LAUNCH_CHECK(c);
+    k_nl_z3<<<1024, 256, 0, c.stream>>>(fnl, f, wsg, pi.nat, (size_t)P, nstate, ks, static_cast<uint16_t*>(c.nl_tb.p));
+    GBCP_LAUNCH_CHECK(c);
+  }
+  GBCP_CUDA_TRY(c, cudaMemsetAsync(c.d_info, 0, sizeof(int), c.stream));
+  int rc = tc_gemm_split3(c, static_cast<const uint16_t*>(c.nl_ta.p), M, static_cast<const uint16_t*>(c.nl_tb.p),
+                          nstate, P, (int)ks, 6, kPairS, kPairT, 1, nullptr, 1, reinterpret_cast<double*>(c2),
+                          2 * (long long)ldc2, c.d_info);
+  if (rc) return rc;
+  return check_status(c);
+}
+
+// projector GEMMs on the tensor cores: mixed precision unless the FP64 SIMT engine is forced
+bool use_tc_projectors(const Ctx& c) { return c.precision == 1 && c.gemm_mode != 0; }
+
 }  // namespace
 
 int nl_rnlsm1(Ctx& c, const cx<double>* c0, int ldc, int nstate, int nat, int ngh, const int* nghtol_host,
               const double* twnl, const cx<double>* eigr, double* fnl) {
   ProjInfo pi;
   if (!make_info(c, nat, ngh, nghtol_host, pi)) return 1;
+  if (use_tc_projectors(c)) return rnlsm1_tc(c, c0, ldc, nstate, pi, twnl, eigr, fnl);
   const int P = nat * ngh;
   const int K = 2 * c.ngw;
   const int tiles = ((P + TS - 1) / TS) * ((nstate + TS - 1) / TS);
@@ -217,6 +421,7 @@ int nl_fnonloc(Ctx& c, cx<double>* c2, int ldc2, int nstate, const double* f, in
                const double* twnl, const cx<double>* eigr, const double* fnl, const double* wsg) {
   ProjInfo pi;
   if (!make_info(c, nat, ngh, nghtol_host, pi)) return 1;
+  if (use_tc_projectors(c)) return fnonloc_tc(c, c2, ldc2, nstate, f, pi, twnl, eigr, fnl, wsg);
   const int rows = 2 * c.ngw;
   dim3 grid((rows + TS - 1) / TS, (nstate + TS - 1) / TS);
   {
