@@ -315,6 +315,11 @@ def run_gpu(args, rank, world, local):
                "sample": f"numpy/scipy restatement of rhoofr+vpsi on {args.ref_states} of {n} states scaled "
                          f"x{n // args.ref_states} + ortho on all {n} states; best of 2"}
 
+    extras = None
+    if rank == 0 and world == 1 and not args.no_extras:
+        del c0h, c2h
+        extras = run_extras(args, dev)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "state-applies/s", "n_gpus": world, "steps": args.steps,
@@ -336,10 +341,122 @@ def run_gpu(args, rank, world, local):
                     "steps": args.e2e_steps, "path": "C ABI, host (pinned) buffers, GBCP_MEM_HOST"},
             "gpu_launches": launches,
             "cpu_baseline": cpu,
+            "other_configs": extras,
         }
         print(json.dumps(line), flush=True)
     ctx_mx.close()
     ctx_64.close()
+
+
+def _timed_loop(step, steps, warmup):
+    import torch
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    s = torch.cuda.Event(enable_timing=True)
+    e = torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(steps):
+        step()
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / steps
+
+
+def run_extras(args, dev):
+    """The other cells of the hot path, one GPU, inputs resident on the device:
+    the 8-atom cell (16 states, 32^3), the energy + adjoint of the 216-atom cell
+    (432 states, 144^3) and the 512-atom projector/Loewdin cell (1024 states,
+    240^3, 4096 projectors).  Each is timed with CUDA events after warm-up."""
+    import numpy as np
+    import torch
+    from cpmd_gb300 import Context
+    from cpmd_gb300.synth import gaussian_form_factor, make_cell, make_cell_device
+
+    out = {}
+    # ---- 8 atoms, 16 states, 32^3, GS ortho
+    cl = make_cell("c0")
+    b = cl.basis
+    c0 = torch.from_numpy(np.ascontiguousarray(cl.c0.T)).to(dev)
+    f = torch.from_numpy(cl.f).to(dev)
+    v = torch.from_numpy(cl.vpot).to(dev)
+    rho = torch.empty(tuple(b.kr[::-1]), dtype=torch.float64, device=dev)
+    c2 = torch.zeros_like(c0)
+    r = {}
+    for prec in ("mixed", "fp64"):
+        ctx = Context(b, prec)
+
+        def step():
+            ctx.rhoofr(c0, f, rho, energies=False)
+            ctx.vpsi(c0, c2, f, v)
+            ctx.ortho(c0, "gs")
+        ms = _timed_loop(step, 50, 5)
+        r[prec] = {"state_applies_per_s": cl.nstate / (ms / 1e3), "ms_per_step": ms}
+        ctx.close()
+    out["cell_8atoms_16states_32cubed"] = r
+
+    # ---- 216 atoms, 432 states, 50 Ry, 144^3: energy + adjoint (dE/dpsi*, dE/dV, forces)
+    cl = make_cell_device("c2")
+    b = cl.basis
+    vps = torch.from_numpy(gaussian_form_factor(b)).to(dev)
+    tau = torch.from_numpy(cl.tau).to(dev)
+    isp = np.zeros(len(cl.tau), dtype=np.int32)
+    r = {}
+    res = {}
+    for prec in ("mixed", "fp64"):
+        ctx = Context(b, prec)
+        holder = {}
+
+        def step():
+            holder["r"] = ctx.energy(cl.c0, cl.f, tau, vps, isp)
+        ms = _timed_loop(step, 3 if prec == "mixed" else 2, 2 if prec == "mixed" else 1)
+        res[prec] = holder["r"]
+        r[prec] = {"state_applies_per_s": cl.nstate / (ms / 1e3), "ms_per_energy_and_gradient": ms}
+        ctx.close()
+    nat = len(cl.tau)
+    r["dE_Ha_per_atom_mixed_vs_fp64"] = abs(res["mixed"][0]["etot"] - res["fp64"][0]["etot"]) / nat
+    r["dF_max_Ha_per_bohr_mixed_vs_fp64"] = float((res["mixed"][3] - res["fp64"][3]).abs().max())
+    r["E_fp64_Ha"] = res["fp64"][0]["etot"]
+    r["workload"] = "E = kinetic + local + Hartree + LDA-PZ and its adjoint, 216 atoms, 432 states, 50 Ry, 144^3"
+    out["adjoint_216atoms_432states_144cubed"] = r
+    del cl, res, holder, vps, tau
+    torch.cuda.empty_cache()
+
+    # ---- 512 atoms, 1024 states, 70 Ry, 240^3, 4096 projectors, Loewdin
+    cl = make_cell_device("c4")
+    b = cl.basis
+    p = cl.proj
+    nat = len(cl.tau)
+    rho = torch.empty(tuple(b.kr[::-1]), dtype=torch.float64, device=dev)
+    fnl = torch.empty((cl.nstate, 8, nat), dtype=torch.float64, device=dev)
+    r = {}
+    energies = {}
+    dv = b.omega / (b.nr[0] * b.nr[1] * b.nr[2])
+    for prec in ("mixed", "fp64"):
+        ctx = Context(b, prec)
+        c = cl.c0.clone()
+        c2 = torch.zeros_like(c)
+
+        def step():
+            ctx.rhoofr(c, cl.f, rho, energies=False)
+            ctx.vpsi(c, c2, cl.f, cl.vpot)
+            ctx.rnlsm(c, p["twnl"], p["eigr"], p["nghtol"], fnl)
+            ctx.fnonloc(c2, cl.f, fnl, p["twnl"], p["eigr"], p["nghtol"], p["wsg"])
+            ctx.ortho(c, "lowdin")
+        ms = _timed_loop(step, 3 if prec == "mixed" else 1, 2 if prec == "mixed" else 1)
+        rh, ek, _, _ = ctx.rhoofr(c, cl.f, rho)
+        energies[prec] = ek + dv * float((rh * cl.vpot).sum())
+        scond = ctx.ortho(c, "lowdin")          # max|S - I| of the orthonormalised states
+        r[prec] = {"state_applies_per_s": cl.nstate / (ms / 1e3), "ms_per_step": ms,
+                   "orthonormality_after_ortho": scond}
+        del c, c2
+        ctx.close()
+        torch.cuda.empty_cache()
+    r["dE_Ha_per_atom_mixed_vs_fp64"] = abs(energies["mixed"] - energies["fp64"]) / nat
+    r["workload"] = ("rhoofr + vpsi + rnlsm1 + fnonloc + Loewdin ortho, 512 atoms, 1024 states, 70 Ry "
+                     f"(ngw={b.ngw}), 240^3, 4096 projectors")
+    out["projectors_512atoms_1024states_240cubed"] = r
+    return out
 
 
 def main():
@@ -353,6 +470,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--ref-states", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the 8-, 216- and 512-atom cells")
     args = ap.parse_args()
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":

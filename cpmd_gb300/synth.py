@@ -172,3 +172,100 @@ def make_small_cell(alat: float, nr: int, ecut: float, nstate: int, seed: int = 
     f = np.full(nstate, 2.0)
     proj = projectors(basis, tau, rng) if with_proj else {}
     return Cell(basis=basis, tau=tau, c0=c0, f=f, vpot=v, seed=seed, proj=proj)
+
+
+def gaussian_form_factor(basis: Basis, amp: float = -4.0, width2: float = 1.0) -> np.ndarray:
+    """vps(G) over the density half sphere for v(r) = amp exp(-r^2/width2):
+    amp (pi width2)^(3/2) exp(-width2 G^2 / 4) / Omega, so that
+    V_ion(G) = sum_a vps(G) e^{-iG.R_a} is the periodic sum of the Gaussians."""
+    g2 = basis.hg * basis.tpiba2
+    return amp * (np.pi * width2) ** 1.5 * np.exp(-width2 * g2 / 4.0) / basis.omega
+
+
+@dataclass
+class DeviceCell:
+    """The same construction as :class:`Cell`, generated on the GPU with torch
+    (torch's generator instead of numpy's, same distributions); arrays are torch
+    tensors in the device layouts of the API: c0 (nstate, ngw), vpot (kr3, kr2, kr1),
+    twnl (ngh, ngw), eigr (nat, ngw)."""
+    basis: Basis
+    tau: np.ndarray
+    c0: object
+    f: object
+    vpot: object
+    seed: int
+    proj: dict = field(default_factory=dict)
+
+    @property
+    def nstate(self) -> int:
+        return int(self.c0.shape[0])
+
+
+def make_cell_device(name: str, seed: int = 1234, nstate: int | None = None, with_proj: bool | None = None,
+                     ctx=None) -> DeviceCell:
+    """Large cells without host-side O(n^2 ngw) work: psi orthonormalised on the
+    device by the library's own FP64 Gram-Schmidt (two passes), V_loc and the
+    projectors evaluated on the device."""
+    import torch
+    from .api import Context
+    cfg = CONFIGS[name]
+    rng = np.random.default_rng(seed)
+    tau, alat = atoms(cfg["alat"], cfg["rep"], cfg["jitter"], rng)
+    basis = make_basis(alat, cfg["nr"], cfg["ecut"])
+    ns = cfg["nstate"] if nstate is None else nstate
+    dev = torch.device("cuda")
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    ngw = basis.ngw
+    g2 = torch.from_numpy(basis.hg[:ngw] * basis.tpiba2).to(dev)
+    amp = torch.exp(-g2 / 4.0)
+    re = torch.randn((ns, ngw), generator=gen, device=dev, dtype=torch.float64)
+    im = torch.randn((ns, ngw), generator=gen, device=dev, dtype=torch.float64)
+    c0 = torch.complex(re * amp, im * amp)
+    if basis.geq0:
+        c0[:, 0] = c0[:, 0].real.to(torch.complex128)
+    own = ctx is None
+    ctx = ctx or Context(basis, "fp64")
+    ctx.ortho(c0, "gs")
+    ctx.ortho(c0, "gs")
+    torch.cuda.synchronize()
+    if own:
+        ctx.close()
+    # V_loc: separable Gaussians, minimum image
+    n1, n2, n3 = basis.nr
+    k1, k2, k3 = basis.kr
+    L = basis.alat
+    v = torch.zeros((n3, n2, n1), dtype=torch.float64, device=dev)
+    ax = [torch.arange(n, dtype=torch.float64, device=dev) * (L / n) for n in (n1, n2, n3)]
+    for R in tau:
+        e = []
+        for d in range(3):
+            dd = ax[d] - float(R[d])
+            dd = dd - L * torch.round(dd / L)
+            e.append(torch.exp(-dd * dd))
+        v += -4.0 * e[2][:, None, None] * e[1][None, :, None] * e[0][None, None, :]
+    vpot = torch.zeros((k3, k2, k1), dtype=torch.float64, device=dev)
+    vpot[:n3, :n2, :n1] = v
+    f = torch.full((ns,), 2.0, dtype=torch.float64, device=dev)
+    proj = {}
+    if (with_proj is None and cfg.get("nproj")) or with_proj:
+        G = torch.from_numpy(basis.gvec_bohr(ngw)).to(dev)
+        gn = torch.sqrt((G * G).sum(dim=1))
+        twnl = torch.zeros((8, ngw), dtype=torch.float64, device=dev)
+        nghtol = np.zeros(8, dtype=np.int32)
+        ys = 1.0 / np.sqrt(4 * np.pi)
+        yp = np.sqrt(3.0 / (4 * np.pi))
+        iv = 0
+        for sg in (0.8, 1.4):
+            rad = torch.exp(-0.5 * (gn * sg) ** 2)
+            twnl[iv] = rad * ys
+            iv += 1
+            for a in range(3):
+                twnl[iv] = rad * yp * G[:, a] * sg
+                nghtol[iv] = 1
+                iv += 1
+        t = torch.from_numpy(tau).to(dev)
+        eigr = torch.exp(-1j * (t @ G.T))                     # (nat, ngw) == Fortran eigr(ngw, nat)
+        proj = dict(twnl=twnl, nghtol=nghtol, eigr=eigr,
+                    wsg=torch.from_numpy(rng.uniform(0.5, 1.5, size=8)).to(dev))
+    return DeviceCell(basis=basis, tau=tau, c0=c0, f=f, vpot=vpot, seed=seed, proj=proj)
