@@ -456,6 +456,69 @@ def run_extras(args, dev):
     r["workload"] = ("rhoofr + vpsi + rnlsm1 + fnonloc + Loewdin ortho, 512 atoms, 1024 states, 70 Ry "
                      f"(ngw={b.ngw}), 240^3, 4096 projectors")
     out["projectors_512atoms_1024states_240cubed"] = r
+    del cl, p, rho, fnl
+    torch.cuda.empty_cache()
+
+    # ---- 64 independent cells (8/16/32/64 atoms, 16-128 states, 30 Ry, 36^3-72^3), one graph launch per step
+    from cpmd_gb300 import Batch
+    from cpmd_gb300.synth import make_batch
+    cells = make_batch(64)
+    nst = sum(cc.c0.shape[1] for cc in cells)
+
+    def io_of():
+        io = []
+        for cc in cells:
+            bb = cc.basis
+            io.append(dict(c0=torch.from_numpy(np.ascontiguousarray(cc.c0.T)).to(dev), f=torch.from_numpy(cc.f).to(dev),
+                           vpot=torch.from_numpy(cc.vpot).to(dev),
+                           rhoe=torch.empty(tuple(bb.kr[::-1]), dtype=torch.float64, device=dev),
+                           c2=torch.zeros((cc.c0.shape[1], bb.ngw), dtype=torch.complex128, device=dev)))
+        return io
+
+    r = {}
+    en = {}
+    for prec in ("mixed", "fp64"):
+        io = io_of()
+        bt = Batch([cc.basis for cc in cells], prec, nstreams=16)
+        report = bt.tune(io)
+        en[prec] = bt.step(io)[0]
+        for _ in range(3):
+            bt.step(io)
+        steps = 10
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            bt.step(io)
+        ms = (time.perf_counter() - t0) / steps * 1e3
+        r[prec] = {"state_applies_per_s": nst / (ms / 1e3), "ms_per_step": ms,
+                   "kernels_per_graph_launch": bt.graph_kernels(), "autotuner": report.strip().split("\n")}
+        bt.close()
+        del io
+    # the same cells through one context each, no graph, one stream
+    io = io_of()
+    ctxs = [Context(cc.basis, "mixed") for cc in cells]
+
+    def seq():
+        for cx_, x in zip(ctxs, io):
+            cx_.rhoofr(x["c0"], x["f"], x["rhoe"], energies=False)
+            cx_.vpsi(x["c0"], x["c2"], x["f"], x["vpot"])
+            cx_.ortho(x["c0"], "gs")
+        torch.cuda.synchronize()
+    seq()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        seq()
+    ms_seq = (time.perf_counter() - t0) / 3 * 1e3
+    for cx_ in ctxs:
+        cx_.close()
+    nats = np.array([cc.tau.shape[0] for cc in cells])
+    de = np.abs(en["mixed"].sum(axis=1) - en["fp64"].sum(axis=1)) / nats
+    r["mixed_sequential_contexts"] = {"state_applies_per_s": nst / (ms_seq / 1e3), "ms_per_step": ms_seq}
+    r["dE_Ha_per_atom_mixed_vs_fp64_max"] = float(de.max())
+    r["timing"] = "host wall clock per step: one cudaGraphLaunch + stream synchronise"
+    r["workload"] = (f"64 cells, atoms uniform in {{8,16,32,64}}, {nst} states in total, 30 Ry, meshes 36^3-72^3, "
+                     "rhoofr + vpsi + GS ortho")
+    out["batch_64cells"] = r
     return out
 
 

@@ -4,5 +4,5 @@ rhoofr / vpsi (pair-packed pruned 3D FFT band loop), ortho (Cholesky
 Gram-Schmidt, Loewdin), invfftn / fwfftn, rnlsm1 / fnonloc -- hand-written
 CUDA for sm_103a behind the C ABI in include/cpmd_gb300.h.
 """
-from .api import Context, GbcpError, kernel_launches  # noqa: F401
+from .api import Batch, Context, GbcpError, kernel_launches  # noqa: F401
 from .cell import Basis, make_basis  # noqa: F401

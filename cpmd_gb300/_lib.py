@@ -62,7 +62,18 @@ SIGNATURES = {
     "gbcp_fnonloc": (_I, [_P, _P, _I, _I, _P, _I, _I, _P, _P, _P, _P, _P, _I]),
     "gbcp_set_dens_sphere": (_I, [_P, _I, _P, _P]),
     "gbcp_energy": (_I, [_P, _P, _I, _I, _P, _I, _I, _P, _P, _P, _P, _P, _P, _I, _P, _P, _I]),
+    "gbcp_batch_create": (_I, [_I, _P, _I, _I, C.POINTER(_P)]),
+    "gbcp_batch_destroy": (_I, [_P]),
+    "gbcp_batch_tune": (_I, [_P, _P, _I, _P, _I]),
+    "gbcp_batch_step": (_I, [_P, _P, _I, _P, _P]),
+    "gbcp_batch_graph_kernels": (_I, [_P, C.POINTER(C.c_int64)]),
+    "gbcp_batch_last_error": (_I, [_P, _P, _I]),
 }
+
+
+class CellIO(C.Structure):
+    _fields_ = [("c0", C.c_void_p), ("ldc", C.c_int32), ("nstate", C.c_int32), ("f", C.c_void_p),
+                ("vpot", C.c_void_p), ("rhoe", C.c_void_p), ("c2", C.c_void_p), ("ldc2", C.c_int32)]
 
 _lib = None
 

@@ -332,5 +332,117 @@ class Context:
         return terms
 
 
+STEP = {"rhoofr": 1, "vpsi": 2, "ortho": 4}
+
+
+def _grid_desc(basis):
+    """GridDesc of a basis plus the arrays it points into (keep them alive)."""
+    inyh = np.ascontiguousarray(basis.inyh[:, : basis.ngw].T.astype(np.int32))
+    hg = np.ascontiguousarray(basis.hg[: basis.ngw], dtype=np.float64)
+    g = _lib.GridDesc()
+    g.nr1, g.nr2, g.nr3 = basis.nr
+    g.kr1, g.kr2, g.kr3 = basis.kr
+    g.ngw = basis.ngw
+    g.geq0 = 1 if basis.geq0 else 0
+    g.omega = basis.omega
+    g.tpiba2 = basis.tpiba2
+    g.inyh = inyh.ctypes.data_as(C.POINTER(C.c_int32))
+    g.hg = hg.ctypes.data_as(C.POINTER(C.c_double))
+    return g, (inyh, hg)
+
+
+class Batch:
+    """Many independent cells per step, one CUDA-graph launch (gbcp_batch_*).
+
+    ``cells`` passed to :meth:`tune` / :meth:`step` is a list of dicts with
+    torch CUDA tensors ``c0`` (nstate, ngw) complex128, ``f`` (nstate,),
+    ``vpot`` and ``rhoe`` (kr3, kr2, kr1) float64 and ``c2`` like ``c0``.
+    ``flags``: an int or an iterable of "rhoofr", "vpsi", "ortho".
+    """
+
+    def __init__(self, bases, precision: str = "mixed", nstreams: int = 8):
+        self.lib = _lib.load()
+        self.bases = list(bases)
+        keep = []
+        arr = (_lib.GridDesc * len(self.bases))()
+        for i, b in enumerate(self.bases):
+            g, k = _grid_desc(b)
+            arr[i] = g
+            keep.append(k)
+        h = C.c_void_p()
+        rc = self.lib.gbcp_batch_create(len(self.bases), C.cast(arr, C.c_void_p), PREC[precision], int(nstreams),
+                                        C.byref(h))
+        if rc != 0:
+            raise GbcpError("gbcp_batch_create", rc)
+        self.h = h
+        self._keep = keep
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gbcp_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def last_error(self) -> str:
+        buf = C.create_string_buffer(512)
+        self.lib.gbcp_batch_last_error(self.h, buf, 512)
+        return buf.value.decode()
+
+    @staticmethod
+    def _flags(flags) -> int:
+        if isinstance(flags, int):
+            return flags
+        return sum(STEP[f] for f in flags)
+
+    def _io(self, cells):
+        if len(cells) != len(self.bases):
+            raise ValueError("one io entry per cell")
+        io = (_lib.CellIO * len(cells))()
+        for i, (x, b) in enumerate(zip(cells, self.bases)):
+            ldc, n = _ld_wfn(x["c0"], b.ngw)
+            io[i].c0 = _ptr(x["c0"]).value
+            io[i].ldc = ldc
+            io[i].nstate = n
+            io[i].f = _ptr(x["f"]).value
+            io[i].vpot = _ptr(x.get("vpot")).value if x.get("vpot") is not None else None
+            io[i].rhoe = _ptr(x.get("rhoe")).value if x.get("rhoe") is not None else None
+            if x.get("c2") is not None:
+                io[i].c2 = _ptr(x["c2"]).value
+                io[i].ldc2 = _ld_wfn(x["c2"], b.ngw)[0]
+        return io
+
+    def tune(self, cells, flags=("rhoofr", "vpsi", "ortho")) -> str:
+        import torch
+        torch.cuda.synchronize()
+        buf = C.create_string_buffer(8192)
+        rc = self.lib.gbcp_batch_tune(self.h, C.cast(self._io(cells), C.c_void_p), self._flags(flags), buf, 8192)
+        if rc != 0:
+            raise GbcpError("gbcp_batch_tune", rc, self.last_error())
+        return buf.value.decode()
+
+    def step(self, cells, flags=("rhoofr", "vpsi", "ortho")):
+        """Returns (energies (ncells, 2): E_kin, Omega/N sum V rho; status (ncells,))."""
+        import torch
+        torch.cuda.synchronize()
+        n = len(self.bases)
+        en = np.zeros((n, 2))
+        st = np.zeros(n, dtype=np.int32)
+        rc = self.lib.gbcp_batch_step(self.h, C.cast(self._io(cells), C.c_void_p), self._flags(flags),
+                                      en.ctypes.data_as(C.c_void_p), st.ctypes.data_as(C.c_void_p))
+        if rc != 0:
+            raise GbcpError("gbcp_batch_step", rc, self.last_error())
+        return en, st
+
+    def graph_kernels(self) -> int:
+        k = C.c_int64()
+        self.lib.gbcp_batch_graph_kernels(self.h, C.byref(k))
+        return int(k.value)
+
+
 def kernel_launches() -> int:
     return int(_lib.load().gbcp_kernel_launches())

@@ -154,6 +154,39 @@ __global__ void k_sum_partial(const double* __restrict__ x, size_t n, double* __
   }
 }
 
+// dot-product partials of two real arrays
+__global__ void k_dot_partial(const double* __restrict__ x, const double* __restrict__ y, size_t n,
+                              double* __restrict__ part) {
+  double a = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    a += x[i] * y[i];
+  __shared__ double r[kThreads];
+  r[threadIdx.x] = a;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) r[threadIdx.x] += r[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = r[0];
+    part[2 * blockIdx.x + 1] = 0.0;
+  }
+}
+
+// out = scale * sum_i part[2 i] (one CTA, deterministic order)
+__global__ void k_fold_scaled(const double* __restrict__ part, int n, double scale, double* __restrict__ out) {
+  __shared__ double r[kThreads];
+  double a = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) a += part[2 * i];
+  r[threadIdx.x] = a;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) r[threadIdx.x] += r[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = scale * r[0];
+}
+
 }  // namespace
 static int lines_for(int n, int target) { return std::max(1, std::min(64, target / n)); }
 
@@ -228,6 +261,42 @@ int kin_energy(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* 
   if (!std::isfinite(h[0]) || !std::isfinite(h[1])) {
     c.err = "non-finite kinetic energy / norm";
     return 3;
+  }
+  return 0;
+}
+
+int kin_energy_async(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* dev_out) {
+  const int gx = std::max(1, std::min(64, (c.ngw + kThreads - 1) / kThreads));
+  const int nb = gx * nstate;
+  if (!ensure(c, c.red, sizeof(double) * (2 * (size_t)nb + 2))) return 6;
+  double* part = static_cast<double*>(c.red.p);
+  {
+    ProfScope ps_(c, "k_kin_partial");
+    k_kin_partial<<<dim3(gx, nstate), kThreads, 0, c.stream>>>(c0, ldc, c.ngw, nstate, f, c.geo.hg, c.geq0, part);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  {
+    ProfScope ps_(c, "k_fold_scaled");
+    k_fold_scaled<<<1, kThreads, 0, c.stream>>>(part, nb, c.tpiba2, dev_out);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  return 0;
+}
+
+int vrho_async(Ctx& c, const double* rho, const double* vpot, double* dev_out) {
+  const size_t n = (size_t)c.kr[0] * c.kr[1] * c.kr[2];
+  const int nb = 296;
+  if (!ensure(c, c.red2, sizeof(double) * (2 * (size_t)nb + 2))) return 6;
+  double* part = static_cast<double*>(c.red2.p);
+  {
+    ProfScope ps_(c, "k_dot_partial");
+    k_dot_partial<<<nb, kThreads, 0, c.stream>>>(rho, vpot, n, part);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  {
+    ProfScope ps_(c, "k_fold_scaled");
+    k_fold_scaled<<<1, kThreads, 0, c.stream>>>(part, nb, c.omega / ((double)c.nr[0] * c.nr[1] * c.nr[2]), dev_out);
+    GBCP_LAUNCH_CHECK(c);
   }
   return 0;
 }

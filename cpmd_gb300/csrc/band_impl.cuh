@@ -518,17 +518,17 @@ int launch_decode(Ctx& c, int np, const cx<double>* c0, int ldc, cx<double>* c2,
 }
 
 template <typename T> int zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int np) {
-  GBCP_DISPATCH(launch_zinv, T, c.nr[2], c, c0, ldc, s0, nstate, np)
+  GBCP_DISPATCH(launch_zinv, T, band_len(c, c.nr[2]), c, c0, ldc, s0, nstate, np)
 }
-template <typename T> int yinv(Ctx& c, int np) { GBCP_DISPATCH(launch_yinv, T, c.nr[1], c, np) }
+template <typename T> int yinv(Ctx& c, int np) { GBCP_DISPATCH(launch_yinv, T, band_len(c, c.nr[1]), c, np) }
 template <typename T> int xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho) {
-  GBCP_DISPATCH(launch_xinv_rho, T, c.nr[0], c, np, s0, nstate, f, rho)
+  GBCP_DISPATCH(launch_xinv_rho, T, band_len(c, c.nr[0]), c, np, s0, nstate, f, rho)
 }
 template <typename T> int xvx(Ctx& c, int np, const double* vpot, const T* vpotT) {
-  GBCP_DISPATCH(launch_xvx, T, c.nr[0], c, np, vpot, vpotT)
+  GBCP_DISPATCH(launch_xvx, T, band_len(c, c.nr[0]), c, np, vpot, vpotT)
 }
-template <typename T> int yfwd(Ctx& c, int np) { GBCP_DISPATCH(launch_yfwd, T, c.nr[1], c, np) }
-template <typename T> int zfwd(Ctx& c, int np) { GBCP_DISPATCH(launch_zfwd, T, c.nr[2], c, np) }
+template <typename T> int yfwd(Ctx& c, int np) { GBCP_DISPATCH(launch_yfwd, T, band_len(c, c.nr[1]), c, np) }
+template <typename T> int zfwd(Ctx& c, int np) { GBCP_DISPATCH(launch_zfwd, T, band_len(c, c.nr[2]), c, np) }
 
 template <typename T>
 int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho) {

@@ -74,6 +74,7 @@ struct Ctx {
   int precision;
   int batch;           // pairs per batch
   int gemm_mode = -1;  // overlap GEMM: -1 by precision (mixed -> tensor cores), 0 FP64 SIMT, 1 tensor cores
+  int fft_engine = 0;  // band-loop FFTs: 0 four-step where a plan exists, else Stockham; 2 Stockham always
   cudaStream_t stream = nullptr;  // stream all work is queued on
   cudaStream_t own = nullptr;     // the context's own stream
   // geometry
@@ -93,7 +94,7 @@ struct Ctx {
   // workspaces
   Scratch zbuf, ybuf, qbuf;
   Scratch st_c0, st_c2, st_rho, st_vpot, st_f, st_misc, st_misc2, st_vf;
-  Scratch red;      // reductions
+  Scratch red, red2;  // reductions
   Scratch smat, smat2, smat3, sparts, cscr;
   Scratch nl_a, nl_b, nl_c, nl_d;
   Scratch nl_ta, nl_tb, nl_tp;  // projector GEMM slices (A, B) and split-K partials
@@ -148,6 +149,10 @@ int band_vpsi(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, c
               int nstate);
 int dense_fft(Ctx& c, cx<double>* grid, bool inv);
 int kin_energy(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* ekin, double* csumg);
+// capture-safe reductions (no host synchronisation), result in device memory:
+// kin_energy_async -> dev_out[0] = E_kin; vrho_async -> dev_out[0] = Omega/N sum_r V rho
+int kin_energy_async(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* dev_out);
+int vrho_async(Ctx& c, const double* rho, const double* vpot, double* dev_out);
 int rho_sum(Ctx& c, const double* rho, double* sum);
 
 // ---- linear algebra (linalg.cu) ----
@@ -156,9 +161,13 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, unsig
              int* status);
 int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout, int ldo,
             int* status);
+// mesh length as seen by the band-loop dispatch (-1 forces the Stockham kernels)
+inline int band_len(const Ctx& c, int n) { return c.fft_engine == 2 ? -1 : n; }
 inline bool use_tc_gemm(const Ctx& c) { return c.gemm_mode == 1 || (c.gemm_mode < 0 && c.precision == 1); }
 int chol_inverse(Ctx& c, double* S, double* X, int n);
 int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host);
+// Gram-Schmidt queued on the stream; the status word c.d_info tells the outcome (no synchronisation)
+int ortho_gs_queue(Ctx& c, cx<double>* c0, int ldc, int nstate);
 int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host);
 
 // ---- energy functional and its adjoint (energy.cu) ----
@@ -193,3 +202,8 @@ int nl_fnonloc(Ctx& c, cx<double>* c2, int ldc2, int nstate, const double* f, in
       return 5;                                                                  \
     }                                                                            \
   } while (0)
+
+// The opaque handle of the C ABI.
+struct gbcp_ctx {
+  gbcp::Ctx c;
+};

@@ -367,9 +367,7 @@ static int apply_right(Ctx& c, cx<double>* c0, int ldc, int nstate, const double
   return 0;
 }
 
-int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host) {
-  const int n = nstate;
-  if (n <= 0) return 0;
+static int ortho_gs_steps(Ctx& c, cx<double>* c0, int ldc, int n, bool want_scond) {
   if (n > 4096) {
     c.err = "ortho: nstate above 4096 not supported";
     return 7;
@@ -379,12 +377,22 @@ int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host) {
   double* S = static_cast<double*>(c.smat.p);
   double* X = static_cast<double*>(c.smat2.p);
   GBCP_CUDA_TRY(c, cudaMemsetAsync(c.d_info, 0, 16, c.stream));
-  int rc = ovlap_gamma_ex(c, c0, ldc, n, S, scond_host != nullptr);
+  int rc = ovlap_gamma_ex(c, c0, ldc, n, S, want_scond);
   if (rc) return rc;
   if ((rc = chol_inverse(c, S, X, n))) return rc;
-  rc = apply_right(c, c0, ldc, n, X, 1);
+  return apply_right(c, c0, ldc, n, X, 1);
+}
+
+int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host) {
+  if (nstate <= 0) return 0;
+  const int rc = ortho_gs_steps(c, c0, ldc, nstate, scond_host != nullptr);
   if (rc) return rc;
   return finish_status(c, scond_host);
+}
+
+int ortho_gs_queue(Ctx& c, cx<double>* c0, int ldc, int nstate) {
+  if (nstate <= 0) return 0;
+  return ortho_gs_steps(c, c0, ldc, nstate, false);
 }
 
 int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host) {

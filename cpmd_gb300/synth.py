@@ -269,3 +269,34 @@ def make_cell_device(name: str, seed: int = 1234, nstate: int | None = None, wit
         proj = dict(twnl=twnl, nghtol=nghtol, eigr=eigr,
                     wsg=torch.from_numpy(rng.uniform(0.5, 1.5, size=8)).to(dev))
     return DeviceCell(basis=basis, tau=tau, c0=c0, f=f, vpot=vpot, seed=seed, proj=proj)
+
+
+MESHES = (32, 36, 40, 48, 60, 64, 72, 80, 96, 120, 144, 240)
+
+
+def batch_cell(nat: int, seed: int, ecut: float = 30.0, alat8: float = 10.26) -> Cell:
+    """One cell of the many-cell batch: nat atoms at seeded uniform positions in a
+    cube of edge alat8 (nat/8)^(1/3) (the 8-atom cell's density), 2 nat doubly
+    occupied states, the smallest planned mesh that holds the density sphere."""
+    rng = np.random.default_rng(seed)
+    L = alat8 * (nat / 8.0) ** (1.0 / 3.0)
+    basis = None
+    for m in MESHES:
+        try:
+            basis = make_basis(L, m, ecut)
+            break
+        except ValueError:
+            continue
+    if basis is None:
+        raise ValueError("no planned mesh holds the density sphere")
+    tau = rng.uniform(0.0, L, size=(nat, 3))
+    ns = 2 * nat
+    c0 = random_states(basis, ns, rng)
+    return Cell(basis=basis, tau=tau, c0=c0, f=np.full(ns, 2.0), vpot=vloc_grid(basis, tau), seed=seed)
+
+
+def make_batch(ncells: int = 64, seed: int = 4321, atoms_choice=(8, 16, 32, 64)) -> list:
+    """ncells independent cells, atom counts drawn uniformly from atoms_choice."""
+    rng = np.random.default_rng(seed)
+    nats = rng.choice(np.asarray(atoms_choice), size=ncells)
+    return [batch_cell(int(n), seed + 1 + i) for i, n in enumerate(nats)]

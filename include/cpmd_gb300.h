@@ -85,8 +85,10 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  *   GBCP_OPT_GEMM   overlap GEMM engine: -1 = by precision (MIXED -> tensor
  *                   cores), 0 = FP64 SIMT, 1 = tcgen05 split-precision
  *                   (FP64-accurate);
- *   GBCP_OPT_BATCH  state pairs per band-loop launch (> 0). */
-enum gbcp_option { GBCP_OPT_GEMM = 1, GBCP_OPT_BATCH = 2 };
+ *   GBCP_OPT_BATCH  state pairs per band-loop launch (1..64);
+ *   GBCP_OPT_FFT    band-loop FFT kernels: 0 = four-step register codelets
+ *                   where the mesh has a plan, else Stockham; 2 = Stockham. */
+enum gbcp_option { GBCP_OPT_GEMM = 1, GBCP_OPT_BATCH = 2, GBCP_OPT_FFT = 3 };
 int gbcp_set_option(gbcp_ctx* ctx, int key, int value);
 /* Queue later work on `stream` (a cudaStream_t; NULL = the context's own
  * stream; the CUDA legacy default stream is cudaStreamLegacy).  Device-pointer calls are ordered only with respect to this stream,
@@ -195,6 +197,39 @@ int gbcp_set_dens_sphere(gbcp_ctx* ctx, int nhg, const int32_t* inyh, const doub
 int gbcp_energy(gbcp_ctx* ctx, const double* c0, int ldc, int nstate, const double* f, int nat, int nsp,
                 const int32_t* isp, const double* tau, const double* vps, const double* vext, double* energies,
                 double* c2, int ldc2, double* dvloc, double* fion, int mem);
+
+/* ---- Batches of independent cells (no counterpart in the reference, where
+ * every cell is a separate run).  A batch owns one context per cell; a step
+ * runs, for every cell, any of rhoofr (+ E_kin and int V rho in FP64),
+ * vpsi and Gram-Schmidt ortho, captured once into a CUDA graph and replayed
+ * with one graph launch per step.  All cell arrays are DEVICE pointers. */
+typedef struct gbcp_batch gbcp_batch;
+typedef struct gbcp_cell_io {
+  double* c0;          /* (ldc, nstate) complex; orthonormalised in place by GBCP_STEP_ORTHO */
+  int32_t ldc;
+  int32_t nstate;
+  const double* f;     /* (nstate) */
+  const double* vpot;  /* (kr1, kr2, kr3) */
+  double* rhoe;        /* (kr1, kr2, kr3) output of GBCP_STEP_RHOOFR */
+  double* c2;          /* (ldc2, nstate) complex, accumulated by GBCP_STEP_VPSI */
+  int32_t ldc2;
+} gbcp_cell_io;
+enum gbcp_step_flags { GBCP_STEP_RHOOFR = 1, GBCP_STEP_VPSI = 2, GBCP_STEP_ORTHO = 4 };
+/* `nstreams` worker streams run cells side by side (0 = 8). */
+int gbcp_batch_create(int ncells, const gbcp_grid_desc* grids, int precision, int nstreams, gbcp_batch** out);
+int gbcp_batch_destroy(gbcp_batch* batch);
+/* Autotuner: per size class (equal mesh, sphere and nstate) times every
+ * band-loop configuration (four-step or Stockham FFT kernels x pairs per
+ * launch) and both ortho GEMM engines on private copies of the class's first
+ * cell, and keeps the fastest.  `report` (may be NULL) gets one line per class. */
+int gbcp_batch_tune(gbcp_batch* batch, const gbcp_cell_io* io, int flags, char* report, int report_len);
+/* One step over all cells.  energies (host, may be NULL): 2 per cell, E_kin and
+ * Omega/N sum V rho of the input states; status (host, may be NULL): per-cell
+ * GBCP status of ortho.  Returns the first non-OK cell status. */
+int gbcp_batch_step(gbcp_batch* batch, const gbcp_cell_io* io, int flags, double* energies, int32_t* status);
+/* Kernels in the captured step graph (0 before the first step). */
+int gbcp_batch_graph_kernels(gbcp_batch* batch, int64_t* kernels);
+int gbcp_batch_last_error(gbcp_batch* batch, char* buf, int len);
 
 #ifdef __cplusplus
 }
