@@ -112,7 +112,8 @@ def allreduce_max(x: float, world: int) -> float:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -522,6 +523,42 @@ def run_extras(args, dev):
     return out
 
 
+def run_case_projectors(args):
+    """Mixed-precision projector contractions (rnlsm1 + fnonloc on the tensor
+    cores) on a mid-size synthetic problem: the 64-atom cell's sphere
+    (ngw = 42.7k), 128 atoms x 8 projectors, 512 states.  Small enough
+    (about 2 GB on the device) for a profiler to replay."""
+    import numpy as np
+    import torch
+    from cpmd_gb300 import Context
+    from cpmd_gb300.cell import make_basis
+
+    b = make_basis(20.52, 120, 70.0)
+    n, nat, ngh = args.case_states, args.case_atoms, 8
+    g = torch.Generator(device="cuda")
+    g.manual_seed(7)
+    c0 = torch.complex(torch.randn(n, b.ngw, generator=g, device="cuda", dtype=torch.float64),
+                       torch.randn(n, b.ngw, generator=g, device="cuda", dtype=torch.float64)) * 0.01
+    tw = torch.rand(ngh, b.ngw, generator=g, device="cuda", dtype=torch.float64)
+    eig = torch.exp(1j * 6.283185307179586 * torch.rand(nat, b.ngw, generator=g, device="cuda", dtype=torch.float64))
+    nghtol = np.array([0, 1, 1, 1, 0, 1, 1, 1], dtype=np.int32)
+    f = torch.full((n,), 2.0, dtype=torch.float64, device="cuda")
+    wsg = torch.rand(ngh, generator=g, device="cuda", dtype=torch.float64)
+    fnl = torch.empty((n, ngh, nat), dtype=torch.float64, device="cuda")
+    c2 = torch.zeros_like(c0)
+    ctx = Context(b, "mixed")
+
+    def step():
+        ctx.rnlsm(c0, tw, eig, nghtol, fnl)
+        ctx.fnonloc(c2, f, fnl, tw, eig, nghtol, wsg)
+    ms = _timed_loop(step, args.steps, args.warmup)
+    flop = 2 * 2.0 * nat * ngh * n * 2 * b.ngw      # both GEMMs, FP32-equivalent
+    print(json.dumps({"case": "projectors", "ms_per_pair_of_calls": ms, "states": n, "projectors": nat * ngh,
+                      "ngw": b.ngw, "tflops_fp32_equivalent": flop / (ms / 1e3) / 1e12,
+                      "tflops_bf16_issued": 6 * flop / (ms / 1e3) / 1e12}), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -534,7 +571,14 @@ def main():
     ap.add_argument("--ref-states", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the 8-, 216- and 512-atom cells")
+    ap.add_argument("--case", default=None, choices=["projectors"],
+                    help="run one small case of a single path instead of the benchmark (for profiling)")
+    ap.add_argument("--case-states", type=int, default=512)
+    ap.add_argument("--case-atoms", type=int, default=128)
     args = ap.parse_args()
+    if args.case == "projectors":
+        run_case_projectors(args)
+        return
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world)
