@@ -169,6 +169,12 @@ def run_reference(args, rank, world):
 
 
 # ----------------------------------------------------------------------------- GPU arm
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
+# mixed config-1 kernels, from one ncu capture of this script's own command
+# (python bench.py --steps 2 --warmup 3 --fp64-steps 1 --e2e-steps 1 --no-cpu --no-extras).
+NCU_TRAFFIC = {"k_xvx": 108.391424e6 + 44.860160e6}
+
+
 def kernel_bytes(name: str, geo: dict, np_: int, s: int) -> float:
     """Compulsory HBM bytes of one launch (s = bytes per complex of the FFT precision)."""
     n1, n2, n3 = geo["nr"]
@@ -333,7 +339,7 @@ def run_gpu(args, rank, world, local):
                      "mixed_over_fp64": value / v64},
             "accuracy": {"dE_Ha_per_atom_mixed_vs_fp64": abs(emx - e64) / nat, "E_fp64_Ha": e64},
             "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                         "frac": (achieved / hbm) if achieved else None, "traffic": NCU_TRAFFIC.get(dname),
                          "peak_source": src, "launch_ms": per_launch_ms, "bytes_per_launch": bytes_per_launch,
                          "kernel_share": dms / 2 / step_ms_prof},
             "kernels_ms_per_step": {k: round(t / 2, 4) for k, (t, _) in sorted(prof.items(), key=lambda kv: -kv[1][0])},
@@ -562,7 +568,7 @@ def run_case_projectors(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--batch", type=int, default=16)

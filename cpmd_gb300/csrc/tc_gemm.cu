@@ -205,13 +205,16 @@ __global__ void __launch_bounds__(TG_THREADS, 1)
             for (int j = 0; j < 32; ++j)
               if (col0 + j < p.N) o[(size_t)(col0 + j) * p.M] = __uint_as_float(v[j]);
           } else {
-            double* o = p.C + row;
+            // all 32 loads in flight before the first store; the FP32 -> FP64
+            // conversion runs on the integer pipe (the FP64 pipe is 1/58 of FP32)
+            double* __restrict__ o = p.C + row;
+            const int nc = min(32, p.N - col0);
+            double old[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) old[j] = (j < nc) ? o[(size_t)(col0 + j) * p.ldc] : 0.0;
 #pragma unroll
             for (int j = 0; j < 32; ++j)
-              if (col0 + j < p.N) {
-                double* q = o + (size_t)(col0 + j) * p.ldc;
-                *q = *q + (double)__uint_as_float(v[j]);
-              }
+              if (j < nc) o[(size_t)(col0 + j) * p.ldc] = old[j] + f2d_int(__uint_as_float(v[j]));
           }
         }
       }
