@@ -189,13 +189,28 @@ def kernel_bytes(name: str, geo: dict, np_: int, s: int) -> float:
     if name == "k_xinv_rho":
         return np_ * yb + 2 * grid * 8
     if name == "k_xvx":
-        return np_ * 2 * yb + grid * 8
+        return np_ * 2 * yb + grid * (s // 2)      # V(r) in the transform precision
     if name == "k_yfwd":
         return np_ * (yb + zb)
     if name == "k_zfwd":
         return np_ * (zb + nent * s)
     if name == "k_decode":
         return np_ * (2 * ngw * s + 2 * ngw * 16 + 2 * 2 * ngw * 16)
+    return 0.0
+
+
+def kernel_flops(name: str, n: int, ngw: int) -> float:
+    """bf16 tensor-core FLOPs one launch of the split-precision ortho GEMMs issues:
+    36 digit-pair products per 128 x 64 output tile, K = 2 ngw (S) or the
+    triangular extent of U^-1 (C U^-1)."""
+    K = 2 * ngw
+    mt, nt = -(-n // 128), -(-n // 64)
+    if name == "k_ozaki_syrk":
+        tiles = sum(max(0, nt - 2 * ib) for ib in range(mt))
+        return tiles * 128 * 64 * K * 2 * 36
+    if name == "k_ozaki_rmul":
+        rt = -(-K // 128)
+        return sum(rt * 128 * 64 * min(n, 64 * (j + 1)) * 2 * 36 for j in range(nt))
     return 0.0
 
 
@@ -280,7 +295,13 @@ def run_gpu(args, rank, world, local):
     hbm, bf16, src = peaks()
     per_launch_ms = dms / dcount
     bytes_per_launch = kernel_bytes(dname, geo, bt, 8)
-    achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9 if bytes_per_launch else None
+    flops_per_launch = kernel_flops(dname, n, b.ngw)
+    if flops_per_launch:
+        bound, unit, peak, work = "tensor", "TFLOP/s", bf16, flops_per_launch
+        achieved = flops_per_launch / (per_launch_ms / 1e3) / 1e12
+    else:
+        bound, unit, peak, work = "hbm", "GB/s", hbm, bytes_per_launch
+        achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9 if bytes_per_launch else None
     step_ms_prof = sum(t for t, _ in prof.values()) / 2
 
     # end to end through the public API with host (pinned) buffers
@@ -338,9 +359,9 @@ def run_gpu(args, rank, world, local):
             "fp64": {"value": v64, "ms_per_step": ms_64 / args.fp64_steps, "steps": args.fp64_steps,
                      "mixed_over_fp64": value / v64},
             "accuracy": {"dE_Ha_per_atom_mixed_vs_fp64": abs(emx - e64) / nat, "E_fp64_Ha": e64},
-            "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": (achieved / hbm) if achieved else None, "traffic": NCU_TRAFFIC.get(dname),
-                         "peak_source": src, "launch_ms": per_launch_ms, "bytes_per_launch": bytes_per_launch,
+            "roofline": {"bound": bound, "kernel": dname, "achieved": achieved, "peak": peak, "unit": unit,
+                         "frac": (achieved / peak) if achieved else None, "traffic": NCU_TRAFFIC.get(dname),
+                         "peak_source": src, "launch_ms": per_launch_ms, "work_per_launch": work,
                          "kernel_share": dms / 2 / step_ms_prof},
             "kernels_ms_per_step": {k: round(t / 2, 4) for k, (t, _) in sorted(prof.items(), key=lambda kv: -kv[1][0])},
             "clocks": clocks,

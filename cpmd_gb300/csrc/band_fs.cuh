@@ -22,32 +22,34 @@ namespace band {
 
 template <typename T, int N> struct FS {
   static constexpr int N1 = fs_n1(N), N2 = N / N1, L = fs_lines(N);
-  static constexpr int LS = N + ((N % 2 == 0) ? 1 : 0);  // odd line stride in shared memory
+  static constexpr int LS = N + ((N % 2 == 0) ? 1 : 0);  // y/z stages: odd line stride, rows of N2
+  static constexpr int XP = fs_xpitch(N), XS = fs_xstride(N);  // x stage: row pitch, line stride
   static constexpr int TA = L * N2, TB = L * N1;
   static constexpr int IA = (TA + kThreads - 1) / kThreads, IB = (TB + kThreads - 1) / kThreads;
+  static_assert(XP >= N2 && XS >= N1 * XP, "x-stage layout");
 };
 
 template <typename T> __device__ __forceinline__ cx<T> twmul(cx<T> v, cx<T> w, bool conj) {
   return conj ? cmulc(v, w) : cmul(v, w);
 }
 
-// step A on registers v[N1] of line position n2; writes T[k1*N2 + n2] of the line
-template <int S, typename T, int N1, int N2>
+// step A on registers v[N1] of line position n2; writes T[k1][n2] = line[k1*PITCH + n2]
+template <int S, typename T, int N1, int N2, int PITCH = N2>
 __device__ __forceinline__ void fs_step_a(cx<T> (&v)[N1], int n2, const cx<T>* __restrict__ twA, cx<T>* line) {
   dftn<S, N1>(v);
 #pragma unroll
   for (int k1 = 0; k1 < N1; ++k1) {
     cx<T> r = v[k1];
     if (k1 > 0 && n2 > 0) r = twmul(r, twA[k1 * N2 + n2], S < 0);
-    line[k1 * N2 + n2] = r;
+    line[k1 * PITCH + n2] = r;
   }
 }
 
-// step B: read T[k1*N2 + *] of the line, DFT of length N2
-template <int S, typename T, int N1, int N2>
+// step B: read row k1 of the line, DFT of length N2
+template <int S, typename T, int N1, int N2, int PITCH = N2>
 __device__ __forceinline__ void fs_step_b(const cx<T>* line, int k1, cx<T> (&w)[N2]) {
 #pragma unroll
-  for (int n2 = 0; n2 < N2; ++n2) w[n2] = line[k1 * N2 + n2];
+  for (int n2 = 0; n2 < N2; ++n2) w[n2] = line[k1 * PITCH + n2];
   dftn<S, N2>(w);
 }
 
@@ -187,7 +189,7 @@ __device__ __forceinline__ void xline_step_a(const GeoDev& g, const cx<T>* __res
         const int s = freq_of(n2 + P::N2 * n1, N) - g.gxlo;
         v[n1] = (y < g.n2 && s >= 0 && s < g.nslot) ? yb[(size_t)y * g.nslot + s] : mk<T>(0, 0);
       }
-      fs_step_a<1, T, P::N1, P::N2>(v, n2, twA, Ts + l * P::LS);
+      fs_step_a<1, T, P::N1, P::N2, P::XP>(v, n2, twA, Ts + l * P::XS);
     }
   }
 }
@@ -224,7 +226,7 @@ __global__ void __launch_bounds__(kThreads) k_xrho_fs(GeoDev g, const cx<T>* __r
     __syncthreads();
     if (t < P::TB) {
       cx<T> w[P::N2];
-      fs_step_b<1, T, P::N1, P::N2>(Ts + lb * P::LS, k1, w);
+      fs_step_b<1, T, P::N1, P::N2, P::XP>(Ts + lb * P::XS, k1, w);
 #pragma unroll
       for (int k2 = 0; k2 < P::N2; ++k2) acc[k2] += f1 * w[k2].x * w[k2].x + f2 * w[k2].y * w[k2].y;
     }
@@ -246,8 +248,7 @@ __global__ void __launch_bounds__(kThreads) k_xvx_fs(GeoDev g, cx<T>* __restrict
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* twA = reinterpret_cast<cx<T>*>(smem_raw);
   cx<T>* twB = twA + N;
-  cx<T>* Ts = twB + N;
-  cx<T>* Ts2 = Ts + P::L * P::LS;
+  cx<T>* Ts = twB + N;  // one exchange buffer: step B reads and rewrites only its own row k1
   const int y0 = blockIdx.x * P::L, z = blockIdx.y, pair = blockIdx.z;
   cx<T>* yb = ybuf + ((size_t)pair * g.n3 + z) * (size_t)g.n2 * g.nslot;
   load_table(twA, twAg, N);
@@ -261,18 +262,18 @@ __global__ void __launch_bounds__(kThreads) k_xvx_fs(GeoDev g, cx<T>* __restrict
     if (t < P::TB) {
       const int l = t / P::N1, k1 = t - l * P::N1, y = y0 + l;
       cx<T> w[P::N2];
-      fs_step_b<1, T, P::N1, P::N2>(Ts + l * P::LS, k1, w);
+      fs_step_b<1, T, P::N1, P::N2, P::XP>(Ts + l * P::XS, k1, w);
       const T* vrow = vpot + (size_t)g.k1 * ((y < g.n2 ? y : 0) + (size_t)g.k2 * z);
 #pragma unroll
       for (int k2 = 0; k2 < P::N2; ++k2) w[k2] = scl(w[k2], (y < g.n2) ? vrow[k1 + P::N1 * k2] : (T)0);
-      // forward: DFT over k2 (stride-N1 elements), twiddle, exchange
+      // forward: DFT over k2 (stride-N1 elements), twiddle, back into row k1
       dftn<-1, P::N2>(w);
-      cx<T>* line = Ts2 + l * P::LS;
+      cx<T>* line = Ts + l * P::XS;
 #pragma unroll
       for (int j = 0; j < P::N2; ++j) {
         cx<T> r = w[j];
         if (j > 0 && k1 > 0) r = cmulc(r, twB[j * P::N1 + k1]);
-        line[j * P::N1 + k1] = r;
+        line[k1 * P::XP + j] = r;
       }
     }
   }
@@ -282,10 +283,10 @@ __global__ void __launch_bounds__(kThreads) k_xvx_fs(GeoDev g, cx<T>* __restrict
     const int t = threadIdx.x + ia * kThreads;
     if (t < P::TA) {
       const int l = t / P::N2, j = t - l * P::N2, y = y0 + l;
-      const cx<T>* line = Ts2 + l * P::LS;
+      const cx<T>* line = Ts + l * P::XS;
       cx<T> u[P::N1];
 #pragma unroll
-      for (int k1 = 0; k1 < P::N1; ++k1) u[k1] = line[j * P::N1 + k1];
+      for (int k1 = 0; k1 < P::N1; ++k1) u[k1] = line[k1 * P::XP + j];
       dftn<-1, P::N1>(u);
       if (y < g.n2) {
 #pragma unroll

@@ -373,6 +373,10 @@ template <typename T> int ensure_band_buffers(Ctx& c, int npairs) {
 template <typename T, int N> constexpr size_t fs_smem(int buffers, int tables) {
   return sizeof(cx<T>) * ((size_t)tables * N + (size_t)buffers * FS<T, N>::L * FS<T, N>::LS);
 }
+// x stage: the conflict-free (pitch, stride) layout, one exchange buffer
+template <typename T, int N> constexpr size_t fs_smem_x(int tables) {
+  return sizeof(cx<T>) * ((size_t)tables * N + (size_t)FS<T, N>::L * FS<T, N>::XS);
+}
 
 template <typename T, int NC>
 int launch_zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int np) {
@@ -421,7 +425,7 @@ int launch_xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double*
   const GeoDev& g = c.geo;
   const cx<T>* yb = static_cast<const cx<T>*>(c.ybuf.p);
   if constexpr (NC > 0) {
-    constexpr size_t sm = fs_smem<T, NC>(1, 1);
+    constexpr size_t sm = fs_smem_x<T, NC>(1);
     allow_smem(k_xrho_fs<T, NC>, sm);
     ProfScope ps_(c, "k_xinv_rho");
     k_xrho_fs<T, NC><<<dim3((g.n2 + FS<T, NC>::L - 1) / FS<T, NC>::L, g.n3), kThreads, sm, c.stream>>>(
@@ -448,7 +452,7 @@ template <typename T, int NC> int launch_xvx(Ctx& c, int np, const double* vpot,
   cx<T>* yb = static_cast<cx<T>*>(c.ybuf.p);
   ProfScope ps_(c, "k_xvx");
   if constexpr (NC > 0) {
-    constexpr size_t sm = fs_smem<T, NC>(2, 2);
+    constexpr size_t sm = fs_smem_x<T, NC>(2);
     allow_smem(k_xvx_fs<T, NC>, sm);
     k_xvx_fs<T, NC><<<dim3((g.n2 + FS<T, NC>::L - 1) / FS<T, NC>::L, g.n3, np), kThreads, sm, c.stream>>>(
         g, yb, vpotT, twA_of<T>(c, 0), twB_of<T>(c, 0));

@@ -4,14 +4,15 @@
 //
 // 32 x 32 blocks, right-looking:
 //   for each diagonal block k:
-//     diag   one CTA factors A_kk = U_kk^T U_kk in shared memory and inverts U_kk
+//     diag   one CTA of four warps factors A_kk = U_kk^T U_kk and inverts U_kk
 //     panel  U_kj = U_kk^{-T} A_kj for every block j > k (one CTA per block)
 //     update A_ij -= U_ki^T U_kj for k < i <= j (one CTA per block)
 //   then X block-diagonal by block-diagonal: X_ii = U_ii^{-1} (from diag) and
 //   X_ij = -U_ii^{-1} sum_{k=i+1..j} U_ik X_kj for j - i = 1, 2, ...
 // Every kernel first reads the ortho status word and does nothing once a step
-// has failed; diag sets it to (global pivot index + 1) at a non-positive pivot
-// and to -1 at a NaN.  S is row-major n x n (symmetric, upper part used and
+// has failed; diag sets it to (global pivot index + 1) at a pivot at or below
+// 64 eps of that row's original diagonal (an exactly dependent set of states,
+// where dpotrf's info > 0 would depend on rounding) and to -1 at a NaN.  S is row-major n x n (symmetric, upper part used and
 // overwritten by U); X is row-major n x n, upper triangular, zero below.
 #include <algorithm>
 
@@ -42,50 +43,122 @@ __device__ __forceinline__ void store_block(double* __restrict__ M, int n, int b
   if (i < n && j < n) M[(size_t)i * n + j] = s[r][c];
 }
 
-// factor + invert the diagonal block k; U_kk -> S (upper), U_kk^{-1} -> X (diag block)
-__global__ void __launch_bounds__(1024) k_chol_diag(double* __restrict__ S, double* __restrict__ X, int n, int k,
-                                                    int* __restrict__ status) {
-  __shared__ double a[B][B + 1];
-  __shared__ double w[B][B + 1];
-  __shared__ int bad;
+// Factor + invert the diagonal block k: U_kk -> S (upper), U_kk^{-1} -> X
+// (diagonal block).  On GB300 the FP64 pipe (about 2 FMAs per clock per SM)
+// bounds this small kernel, so its work is spread over the four warps of one CTA,
+// one per SM sub-partition.
+//   factor: lane c owns column c, warp w the rows r = w (mod 4) of it (8 values in
+//           registers); the owner of pivot row p publishes the row in shared
+//           memory, one barrier per step;
+//   invert: column j of U^{-1} is independent of the others: warp w takes columns
+//           j = w (mod 4); w[i] = -(sum_{m>i} U[i][m] w[m]) / U[i][i] with the dot
+//           product split over the lanes and a shuffle reduction.
+__global__ void __launch_bounds__(4 * B) k_chol_diag(double* __restrict__ S, double* __restrict__ X,
+                                                     const double* __restrict__ diag0, int n, int k,
+                                                     int* __restrict__ status) {
+  __shared__ double u[B][B + 1];  // U (upper), row p published at step p
+  __shared__ double dinv[B];
+  __shared__ int bad_sh;
   if (failed(status)) return;
-  const int r = threadIdx.x / B, c = threadIdx.x % B;
-  load_block(S, n, k, k, a, 1.0);
-  if (threadIdx.x == 0) bad = 0;
+  const int c = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int j = k * B + c;
+  constexpr int R = B / 4;
+  double col[R];  // rows r = w + 4 q of column c
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const int r = w + 4 * q, i = k * B + r;
+    col[q] = (i < n && j < n) ? S[(size_t)i * n + j] : (r == c ? 1.0 : 0.0);
+  }
+  if (threadIdx.x == 0) bad_sh = 0;
   __syncthreads();
+#pragma unroll
   for (int p = 0; p < B; ++p) {
-    if (threadIdx.x == 0) {
-      const double d = a[p][p];
-      if (!(d > 0.0)) bad = (d != d) ? -1 : k * B + p + 1;
-      else a[p][p] = sqrt(d);
+    const int pw = p & 3, pq = p >> 2;
+    if (w == pw) {  // owner of row p: pivot, row p of U
+      const double d = __shfl_sync(0xffffffffu, col[pq], p);
+      const double d0 = (k * B + p < n) ? diag0[k * B + p] : 1.0;
+      if (!(d > 0x1p-46 * d0)) {
+        if (c == 0) bad_sh = (d != d) ? -1 : k * B + p + 1;
+      } else {
+        const double inv = rsqrt(d);
+        const double upc = (c == p) ? d * inv : (c > p ? col[pq] * inv : 0.0);
+        col[pq] = upc;
+        u[p][c] = upc;
+        if (c == p) dinv[p] = inv;
+      }
     }
     __syncthreads();
-    if (bad) break;
-    if (r == p && c > p) a[p][c] /= a[p][p];
-    __syncthreads();
-    if (r > p && c >= r) a[r][c] -= a[p][r] * a[p][c];
-    __syncthreads();
+    if (bad_sh) break;
+    const double upc = u[p][c];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const int r = w + 4 * q;
+      if (r > p && r <= c) col[q] = fma(-u[p][r], upc, col[q]);
+    }
   }
-  if (bad) {
-    if (threadIdx.x == 0) atomicExch(status, bad);
+  if (bad_sh) {
+    if (threadIdx.x == 0) atomicExch(status, bad_sh);
     return;
   }
-  // zero the strict lower part, then invert the upper triangular block by columns
-  if (c < r) a[r][c] = 0.0;
-  w[r][c] = 0.0;
-  __syncthreads();
-  if (threadIdx.x < B) {
-    const int j = threadIdx.x;
-    w[j][j] = 1.0 / a[j][j];
-    for (int i = j - 1; i >= 0; --i) {
-      double s = 0.0;
-      for (int m = i + 1; m <= j; ++m) s = fma(a[i][m], w[m][j], s);
-      w[i][j] = -s / a[i][i];
-    }
+  // U rows below the diagonal are zero; store U
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const int r = w + 4 * q, i = k * B + r;
+    if (r > c) u[r][c] = 0.0;
+    if (i < n && j < n) S[(size_t)i * n + j] = u[r][c];
   }
   __syncthreads();
-  store_block(S, n, k, k, a);
-  store_block(X, n, k, k, w);
+  // invert by 2 x 2 blocks of 16: W11 = U11^-1 and W22 = U22^-1 (warps 0 and 1, lane = column,
+  // uniform back-substitution with broadcast reads of U), then W12 = -W11 (U12 W22)
+  constexpr int H = B / 2;
+  __shared__ double wt[B][B + 1];
+  __shared__ double tt[H][H + 1];
+  if (w < 2 && c < H) {
+    const int o = w * H;  // block offset
+    double wc[H];
+#pragma unroll
+    for (int i = H - 1; i >= 0; --i) {
+      double t = 0.0;
+#pragma unroll
+      for (int m = i + 1; m < H; ++m) t = fma(u[o + i][o + m], wc[m], t);
+      const double di = dinv[o + i];
+      wc[i] = (i == c) ? di : (i < c ? -t * di : 0.0);
+    }
+#pragma unroll
+    for (int i = 0; i < H; ++i) wt[o + i][o + c] = wc[i];
+  }
+  __syncthreads();
+  {  // T = U12 W22 (16 x 16), two outputs per thread
+    const int e = threadIdx.x, r = e >> 3, c0 = (e & 7) * 2;
+    double t0 = 0.0, t1 = 0.0;
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+      t0 = fma(u[r][H + m], wt[H + m][H + c0], t0);
+      t1 = fma(u[r][H + m], wt[H + m][H + c0 + 1], t1);
+    }
+    tt[r][c0] = t0;
+    tt[r][c0 + 1] = t1;
+  }
+  __syncthreads();
+  {  // W12 = -W11 T; lower-left block zero
+    const int e = threadIdx.x, r = e >> 3, c0 = (e & 7) * 2;
+    double t0 = 0.0, t1 = 0.0;
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+      t0 = fma(wt[r][m], tt[m][c0], t0);
+      t1 = fma(wt[r][m], tt[m][c0 + 1], t1);
+    }
+    wt[r][H + c0] = -t0;
+    wt[r][H + c0 + 1] = -t1;
+    wt[H + r][c0] = 0.0;
+    wt[H + r][c0 + 1] = 0.0;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const int r = w + 4 * q, i = k * B + r;
+    if (i < n && j < n) X[(size_t)i * n + j] = wt[r][c];
+  }
 }
 
 // U_kj = (U_kk^{-1})^T A_kj for block column j = k + 1 + blockIdx.x
@@ -161,10 +234,12 @@ __global__ void __launch_bounds__(1024) k_trtri_diag(const double* __restrict__ 
   store_block(X, n, bi, bj, x);
 }
 
-__global__ void k_zero_lower(double* __restrict__ X, int n) {
+// zero the strict lower triangle of X and keep the original diagonal of S
+__global__ void k_zero_lower(double* __restrict__ X, const double* __restrict__ S, double* __restrict__ diag0, int n) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * n; e += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(e / n), j = (int)(e % n);
     if (j < i) X[e] = 0.0;
+    if (j == i) diag0[i] = S[e];
   }
 }
 
@@ -173,25 +248,37 @@ __global__ void k_zero_lower(double* __restrict__ X, int n) {
 // Queue U = chol(S) (in place, upper) and X = U^{-1}; no synchronisation.
 int chol_inverse(Ctx& c, double* S, double* X, int n) {
   const int nb = (n + B - 1) / B;
+  if (!ensure(c, c.cdiag, sizeof(double) * (size_t)n)) return 6;
+  double* diag0 = static_cast<double*>(c.cdiag.p);
   {
-    ProfScope ps_(c, "k_chol");
-    k_zero_lower<<<std::max(1, std::min(256, (n * n + 255) / 256)), 256, 0, c.stream>>>(X, n);
+    ProfScope ps_(c, "k_chol_misc");
+    k_zero_lower<<<std::max(1, std::min(256, (n * n + 255) / 256)), 256, 0, c.stream>>>(X, S, diag0, n);
     GBCP_LAUNCH_CHECK(c);
-    for (int k = 0; k < nb; ++k) {
-      k_chol_diag<<<1, B * B, 0, c.stream>>>(S, X, n, k, c.d_info);
+  }
+  for (int k = 0; k < nb; ++k) {
+    {
+      ProfScope ps_(c, "k_chol_diag");
+      k_chol_diag<<<1, 4 * B, 0, c.stream>>>(S, X, diag0, n, k, c.d_info);
       GBCP_LAUNCH_CHECK(c);
-      const int m0 = nb - k - 1;
-      if (m0 > 0) {
+    }
+    const int m0 = nb - k - 1;
+    if (m0 > 0) {
+      {
+        ProfScope ps_(c, "k_chol_panel");
         k_chol_panel<<<m0, B * B, 0, c.stream>>>(S, X, n, k, c.d_info);
         GBCP_LAUNCH_CHECK(c);
+      }
+      {
+        ProfScope ps_(c, "k_chol_update");
         k_chol_update<<<m0 * (m0 + 1) / 2, B * B, 0, c.stream>>>(S, n, nb, k, c.d_info);
         GBCP_LAUNCH_CHECK(c);
       }
     }
-    for (int d = 1; d < nb; ++d) {
-      k_trtri_diag<<<nb - d, B * B, 0, c.stream>>>(S, X, n, d, c.d_info);
-      GBCP_LAUNCH_CHECK(c);
-    }
+  }
+  for (int d = 1; d < nb; ++d) {
+    ProfScope ps_(c, "k_trtri_diag");
+    k_trtri_diag<<<nb - d, B * B, 0, c.stream>>>(S, X, n, d, c.d_info);
+    GBCP_LAUNCH_CHECK(c);
   }
   return 0;
 }

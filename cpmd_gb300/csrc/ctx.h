@@ -95,7 +95,8 @@ struct Ctx {
   Scratch zbuf, ybuf, qbuf;
   Scratch st_c0, st_c2, st_rho, st_vpot, st_f, st_misc, st_misc2, st_vf;
   Scratch red, red2;  // reductions
-  Scratch smat, smat2, smat3, sparts, cscr;
+  Scratch smat, smat2, smat3, sparts, cscr, cdiag;
+  Scratch oz_a, oz_b;  // bf16 digit planes of the split-precision ortho GEMMs
   Scratch nl_a, nl_b, nl_c, nl_d;
   Scratch nl_ta, nl_tb, nl_tp;  // projector GEMM slices (A, B) and split-K partials
   int* d_info = nullptr;
@@ -127,9 +128,11 @@ void prof_fold(Ctx& c);
 
 // Raise a kernel's dynamic shared-memory limit, once per kernel and size
 // (cudaFuncSetAttribute costs host time that would otherwise be paid on
-// every launch and starve the GPU of work).
+// every launch and starve the GPU of work).  Done for every size: the default
+// 48 KB cap covers static plus dynamic shared memory, so a dynamic request
+// just under 48 KB still fails next to a few hundred bytes of static arrays.
 template <typename KernelT> inline void allow_smem(KernelT k, size_t bytes) {
-  if (bytes <= 48 * 1024) return;
+  if (bytes == 0) return;
   static std::mutex mu;
   static std::unordered_map<const void*, size_t> done;
   const void* key = reinterpret_cast<const void*>(k);

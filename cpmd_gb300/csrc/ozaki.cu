@@ -27,18 +27,23 @@
 // conversion is FP64:  sum_k x_ik y_kj = 2^(E_i+E_j) (H 2^-35 + Lo 2^-63).
 // Levels above 7 are dropped (< 2^-49 of 2^(E_i+E_j) per product term).
 //
-// The digits are produced in the kernels from FP64 data with integer
-// instructions and stored straight into shared memory in the tensor core's
-// K-major core-matrix layout: no slice matrices in HBM, no FP64 arithmetic in
-// the inner loop.  Every mbarrier wait is bounded; on expiry the kernel sets
-// the ortho status word to -2 (reported as GBCP_ERR_TIMEOUT), frees its TMEM
-// and returns.
+// Data flow.  The digits are produced ONCE per operand by integer-only slicing
+// kernels into eight bf16 digit planes in HBM (row-major, K contiguous, planes
+// stacked along rows), and the GEMM kernel streams them with TMA (64-byte
+// swizzle, K = 32 per sub-chunk, double-buffered: thread 0 loads sub-chunk
+// i + 1 while the 72 MMAs of sub-chunk i run).  All 256 threads fold the eight
+// TMEM level accumulators into int64 every 128 K.  Every mbarrier wait is
+// bounded; on expiry the kernel sets the ortho status word to -2 (reported as
+// GBCP_ERR_TIMEOUT), waits for its own loads and MMAs, frees its TMEM and returns.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 
+#include <cuda.h>
+
 #include "ctx.h"
 #include "tc_common.cuh"
+#include "tc_gemm.h"
 
 namespace gbcp {
 
@@ -55,11 +60,9 @@ constexpr int A_SLICE_BYTES = OZ_M * OZ_KS * 2;  // 8 KB
 constexpr int B_SLICE_BYTES = OZ_N * OZ_KS * 2;  // 4 KB
 constexpr int A_BUF_BYTES = OZ_SL * A_SLICE_BYTES;
 constexpr int B_BUF_BYTES = OZ_SL * B_SLICE_BYTES;
-constexpr int OZ_SMEM = 2 * A_BUF_BYTES + 2 * B_BUF_BYTES;  // 192 KB, double-buffered
+constexpr int STAGE_BYTES = A_BUF_BYTES + B_BUF_BYTES;       // 96 KB
+constexpr int OZ_SMEM = 2 * STAGE_BYTES + 1024;              // double-buffered, + alignment slack
 constexpr uint32_t kIdesc = tc::idesc_bf16_f32(OZ_M, OZ_N);
-
-// byte offset of the (row, k-group) core-matrix row in a K-major no-swizzle tile of 32 K
-__device__ __forceinline__ int core_off(int row, int kg) { return (((row >> 3) << 2) + kg) * 128 + (row & 7) * 16; }
 
 // signed 7-bit digit -> bf16 bits (exact: |d| <= 127)
 __device__ __forceinline__ uint32_t digit_bf16(int d) { return __float_as_uint((float)d) >> 16; }
@@ -83,8 +86,8 @@ __device__ __forceinline__ unsigned long long fixed56(double x, int E, bool& neg
   return (sh <= -64) ? 0ull : (M >> (-sh));
 }
 
-// Digits of 8 consecutive K elements of one operand row -> 8 slices x 16 bytes in smem.
-__device__ __forceinline__ void store_digits(const double (&x)[8], int E, uint8_t* dst, int slice_bytes, int off) {
+// Digits of 8 consecutive K elements of one operand row -> 8 planes, 16 bytes each.
+__device__ __forceinline__ void digits8(const double (&x)[8], int E, uint4 (&out)[OZ_SL]) {
   uint32_t w[OZ_SL][4];
 #pragma unroll
   for (int q2 = 0; q2 < 4; ++q2) {
@@ -98,8 +101,7 @@ __device__ __forceinline__ void store_digits(const double (&x)[8], int E, uint8_
     }
   }
 #pragma unroll
-  for (int s = 0; s < OZ_SL; ++s)
-    *reinterpret_cast<uint4*>(dst + s * slice_bytes + off) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+  for (int s = 0; s < OZ_SL; ++s) out[s] = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
 }
 
 // Issue the 72 MMAs of one sub-chunk (36 digit pairs x 2 K-steps) into the 8
@@ -113,8 +115,8 @@ __device__ __forceinline__ void issue_levels(uint32_t tmem, uint32_t a_base, uin
       const int u = d - s;
 #pragma unroll
       for (int kk = 0; kk < 2; ++kk) {
-        const uint64_t ad = tc::sdesc_kmajor(a_base + s * A_SLICE_BYTES + kk * 256, 128, 512);
-        const uint64_t bd = tc::sdesc_kmajor(b_base + u * B_SLICE_BYTES + kk * 256, 128, 512);
+        const uint64_t ad = tc::sdesc_kmajor_sw64(a_base + s * A_SLICE_BYTES + kk * 32);
+        const uint64_t bd = tc::sdesc_kmajor_sw64(b_base + u * B_SLICE_BYTES + kk * 32);
         tc::mma_f16(dt, ad, bd, kIdesc, (first && s == 0 && kk == 0) ? 0u : 1u);
       }
     }
@@ -190,19 +192,6 @@ __global__ void k_col_max(const double* __restrict__ Ar, int lda, int K, int n, 
   if ((threadIdx.x & 31) == 0 && mx) atomicMax(cmax + j, mx);
 }
 
-// row maxima of the real view over the n states: bits into rmax[r]
-__global__ void k_row_max(const double* __restrict__ Ar, int lda, int rows, int n,
-                          unsigned long long* __restrict__ rmax) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= rows) return;
-  unsigned long long mx = 0;
-  for (int k = 0; k < n; ++k) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(Ar[r + (size_t)k * lda]) & ~(1ull << 63);
-    mx = b > mx ? b : mx;
-  }
-  rmax[r] = mx;
-}
-
 // column maxima of a small row-major n x n matrix M over its rows
 __global__ void k_mat_col_max(const double* __restrict__ M, int n, unsigned long long* __restrict__ cmax) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -215,41 +204,162 @@ __global__ void k_mat_col_max(const double* __restrict__ M, int n, unsigned long
   cmax[j] = mx;
 }
 
-// ---------------------------------------------------------------- S = C^T C (real view)
-__global__ void __launch_bounds__(OZ_THREADS, 1)
-    k_ozaki_syrk(const double* __restrict__ Ar, int lda, int K, int n, const unsigned long long* __restrict__ cmax,
-                 int njb, int subs_per_split, unsigned long long* __restrict__ Hacc,
-                 unsigned long long* __restrict__ Lacc, int* __restrict__ status) {
-  extern __shared__ __align__(1024) uint8_t sm[];
-  uint8_t* sA = sm;
-  uint8_t* sB = sm + 2 * A_BUF_BYTES;
-  __shared__ uint64_t mbar[2];
-  __shared__ uint32_t tmem_sh;
-  __shared__ int abort_sh;
+// ---------------------------------------------------------------- digit planes
+// S operand: plane s, row j (state), columns k < K of the real view; exponent per state.
+__global__ void k_oz_slice_cols(const double* __restrict__ Ar, int lda, int K, int n,
+                                const unsigned long long* __restrict__ emax, size_t ks, uint4* __restrict__ out) {
+  const int j = blockIdx.y;
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) * 8;
+  if (k >= K) return;
+  const int e = exp_of_max(emax[j]);
+  const double* a = Ar + (size_t)j * lda + k;
+  double x[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) x[q] = (k + q < K) ? a[q] : 0.0;
+  uint4 d[OZ_SL];
+  digits8(x, e, d);
+  const size_t plane = (size_t)n * ks / 8, off = ((size_t)j * ks + k) / 8;
+#pragma unroll
+  for (int s = 0; s < OZ_SL; ++s) out[s * plane + off] = d[s];
+}
 
-  // tile (ib, jb) among those touching the upper triangle: jb >= 2 ib
-  int t = blockIdx.x, ib = 0;
-  while (ib < 4096 && t >= max(0, njb - 2 * ib)) {
-    t -= max(0, njb - 2 * ib);
-    ++ib;
+// C M operand A: plane s, row r (real-view row of C), columns k < n (states), with the
+// row's own exponent (its maximum over the n states, also written to emax[r] for the
+// epilogue).  One thread per row: consecutive threads read consecutive rows (coalesced),
+// and each thread writes whole plane rows, which L2 merges into full lines.
+__global__ void k_oz_slice_rows(const double* __restrict__ Ar, int lda, int rows, int n,
+                                unsigned long long* __restrict__ emax, size_t ks, uint4* __restrict__ out) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  unsigned long long mx = 0;
+  for (int k = 0; k < n; ++k) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(Ar[r + (size_t)k * lda]) & ~(1ull << 63);
+    mx = bits > mx ? bits : mx;
   }
-  if (ib >= 4096) return;
-  const int i0 = ib * OZ_M, j0 = (2 * ib + t) * OZ_N;
-  const int total_subs = (K + OZ_KS - 1) / OZ_KS;
-  const int sub0 = blockIdx.y * subs_per_split;
-  const int nsub = min(total_subs, sub0 + subs_per_split) - sub0;
-  if (nsub <= 0) return;
+  emax[r] = mx;
+  const int e = exp_of_max(mx);
+  const size_t plane = (size_t)rows * ks / 8;
+  for (int k = 0; k < n; k += 8) {
+    double x[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) x[q] = (k + q < n) ? Ar[r + (size_t)(k + q) * lda] : 0.0;
+    uint4 d[OZ_SL];
+    digits8(x, e, d);
+    const size_t off = ((size_t)r * ks + k) / 8;
+#pragma unroll
+    for (int s = 0; s < OZ_SL; ++s) out[s * plane + off] = d[s];
+  }
+}
 
+// C M operand B: plane s, row j (column of M), columns k < n: M[k][j]; exponent per column of M.
+__global__ void k_oz_slice_mat(const double* __restrict__ M, int n, const unsigned long long* __restrict__ emax,
+                               size_t ks, uint4* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y * 8;
+  if (j >= n) return;
+  const int e = exp_of_max(emax[j]);
+  double x[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) x[q] = (k + q < n) ? M[(size_t)(k + q) * n + j] : 0.0;
+  uint4 d[OZ_SL];
+  digits8(x, e, d);
+  const size_t plane = (size_t)n * ks / 8, off = ((size_t)j * ks + k) / 8;
+#pragma unroll
+  for (int s = 0; s < OZ_SL; ++s) out[s * plane + off] = d[s];
+}
+
+// ---------------------------------------------------------------- the split GEMM
+struct OzParams {
+  int M, N;           // rows per digit plane of A and of B
+  int K;              // contraction length
+  int mode;           // 0: S, tiles of the upper block triangle x K splits; 1: C M, persistent over tiles
+  int njb;            // mode 0: column tiles
+  int subs_per;       // mode 0: sub-chunks per K split (a multiple of OZ_SUBS)
+  int upper;          // mode 1: M upper triangular (column tile j needs k < j0 + 64)
+  const unsigned long long* eA;  // mode 1: exponent bits per row of A
+  const unsigned long long* eB;  // mode 1: exponent bits per column
+  unsigned long long* Hacc;      // mode 0: int64 accumulators (n x n)
+  unsigned long long* Lacc;
+  double* Cout;                  // mode 1
+  int ldo;
+  int* status;
+};
+
+struct OzUnit {
+  int m0, n0, sub0, nsub;
+  bool valid;
+};
+
+__device__ __forceinline__ OzUnit oz_unit(const OzParams& p, int u) {
+  OzUnit w{0, 0, 0, 0, false};
+  const int total_subs = (p.K + OZ_KS - 1) / OZ_KS;
+  if (p.mode == 0) {
+    if (u != (int)blockIdx.x) return w;  // one unit per CTA
+    int t = blockIdx.x, ib = 0;
+    while (ib < 4096 && t >= max(0, p.njb - 2 * ib)) {
+      t -= max(0, p.njb - 2 * ib);
+      ++ib;
+    }
+    if (ib >= 4096) return w;
+    w.m0 = ib * OZ_M;
+    w.n0 = (2 * ib + t) * OZ_N;
+    w.sub0 = blockIdx.y * p.subs_per;
+    w.nsub = min(total_subs, w.sub0 + p.subs_per) - w.sub0;
+    w.valid = w.nsub > 0;
+    return w;
+  }
+  const int nrt = (p.M + OZ_M - 1) / OZ_M, nct = (p.N + OZ_N - 1) / OZ_N;
+  if (u >= nrt * nct) return w;
+  const int rt = u / nct, ct = u % nct;  // row tile outer: the CTAs of one row tile share its planes in L2
+  w.m0 = rt * OZ_M;
+  w.n0 = ct * OZ_N;
+  const int kmax = p.upper ? min(p.K, w.n0 + OZ_N) : p.K;
+  w.sub0 = 0;
+  w.nsub = (kmax + OZ_KS - 1) / OZ_KS;
+  w.valid = true;
+  return w;
+}
+
+__device__ __forceinline__ int oz_next_unit(const OzParams& p, int u) { return p.mode == 0 ? -1 : u + gridDim.x; }
+
+// thread 0: the 16 TMA loads (8 A planes, 8 B planes) of one sub-chunk into buffer b
+__device__ __forceinline__ void oz_load(const CUtensorMap* tmA, const CUtensorMap* tmB, const OzParams& p,
+                                        const OzUnit& w, int s, uint8_t* buf, uint64_t* bar) {
+  const int k = (w.sub0 + s) * OZ_KS;
+  tc::mbar_expect_tx(bar, STAGE_BYTES);
+#pragma unroll 1
+  for (int pl = 0; pl < OZ_SL; ++pl) {
+    tc::tma_load_2d(buf + pl * A_SLICE_BYTES, tmA, bar, k, pl * p.M + w.m0);
+    tc::tma_load_2d(buf + A_BUF_BYTES + pl * B_SLICE_BYTES, tmB, bar, k, pl * p.N + w.n0);
+  }
+}
+
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    k_oz_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const OzParams p) {
+  extern __shared__ uint8_t oz_raw[];
+  uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(oz_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ uint64_t full[2], mdone[2];
+  __shared__ uint32_t tmem_sh;
+  __shared__ volatile int abort_sh;
+  __shared__ int issued_sh, waited_sh;
+
+  if (p.mode == 1 && *(volatile const int*)p.status != 0) return;  // an earlier step of this ortho failed
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (warp == 0) {
     tc::tmem_alloc(&tmem_sh, 512);
     tc::tmem_relinquish();
   }
   if (threadIdx.x == 0) {
-    tc::mbar_init(&mbar[0], 1);
-    tc::mbar_init(&mbar[1], 1);
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&full[i], 1);
+      tc::mbar_init(&mdone[i], 1);
+    }
     tc::fence_mbar_init();
     abort_sh = 0;
+    issued_sh = 0;
+    waited_sh = 0;
+    tc::tma_prefetch_desc(&tmA);
+    tc::tma_prefetch_desc(&tmB);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -257,99 +367,119 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   const uint32_t tmem = tmem_sh;
   const uint32_t lane_base = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(32 * (warp >> 2));
 
-  long long H[32], Lo[32];
-#pragma unroll
-  for (int c = 0; c < 32; ++c) {
-    H[c] = 0;
-    Lo[c] = 0;
+  // thread 0 owns the pipeline: loads of sub-chunk it+1 are in flight while the MMAs of it run.
+  // Both barriers complete once per use of their buffer, so the parity of the use at global
+  // sub-chunk index it is (it >> 1) & 1.
+  int u = blockIdx.x;
+  OzUnit w = oz_unit(p, u);
+  int it = 0;        // global sub-chunk index of this CTA
+  int issued = 0;    // sub-chunks whose loads were issued
+  int waited = 0;    // sub-chunks whose loads thread 0 saw complete
+  int mma_pend = -1; // global index of the last sub-chunk whose MMAs were committed and not yet waited for
+  if (threadIdx.x == 0 && w.valid) {
+    oz_load(&tmA, &tmB, p, w, 0, sm, &full[0]);
+    issued = 1;
   }
-  uint32_t ph[2] = {0u, 0u};
-  int pend[2] = {0, 0};
-  bool done_ok = true;
-
-  for (int it = 0; it < nsub; ++it) {
-    const int buf = it & 1;
-    if (pend[buf]) {
-      if (!tc::mbar_wait(&mbar[buf], ph[buf])) {
-        abort_sh = 1;
-        atomicExch(status, -2);
-      }
-      ph[buf] ^= 1u;
-      pend[buf] = 0;
-    }
-    __syncthreads();
-    if (abort_sh) {
-      done_ok = false;
-      break;
-    }
-    const int kb = (sub0 + it) * OZ_KS;
-    uint8_t* a_dst = sA + buf * A_BUF_BYTES;
-    uint8_t* b_dst = sB + buf * B_BUF_BYTES;
-    // A: 128 state rows, B: 64 state rows; task = (row, k-group of 8), k contiguous in memory
-    for (int task = threadIdx.x; task < (OZ_M + OZ_N) * 4; task += OZ_THREADS) {
-      const bool isA = task < OZ_M * 4;
-      const int tt = isA ? task : task - OZ_M * 4;
-      const int row = tt >> 2, kg = tt & 3;
-      const int state = (isA ? i0 : j0) + row;
-      const bool valid = state < n;
-      const int e = valid ? exp_of_max(cmax[state]) : 0;
-      double x[8];
+  while (w.valid && !abort_sh) {
+    long long H[32], Lo[32];
 #pragma unroll
-      for (int q2 = 0; q2 < 4; ++q2) {
-        const int k = kb + kg * 8 + 2 * q2;
-        double2 v2 = make_double2(0.0, 0.0);
-        if (valid && k < K) v2 = *reinterpret_cast<const double2*>(Ar + k + (size_t)state * lda);
-        x[2 * q2] = v2.x;
-        x[2 * q2 + 1] = v2.y;
-      }
-      store_digits(x, e, isA ? a_dst : b_dst, isA ? A_SLICE_BYTES : B_SLICE_BYTES, core_off(row, kg));
+    for (int c = 0; c < 32; ++c) {
+      H[c] = 0;
+      Lo[c] = 0;
     }
-    tc::fence_proxy_async();
-    __syncthreads();
-    const int ci = it % OZ_SUBS;
-    if (threadIdx.x == 0) {
-      tc::fence_after_sync();
-      issue_levels(tmem, tc::smem_u32(a_dst), tc::smem_u32(b_dst), ci == 0);
-      tc::mma_commit(&mbar[buf]);
-    }
-    pend[buf] = 1;
-    if (ci == OZ_SUBS - 1 || it == nsub - 1) {
-      bool ok = tc::mbar_wait(&mbar[buf], ph[buf]);
-      ph[buf] ^= 1u;
-      pend[buf] = 0;
-      if (pend[buf ^ 1]) {
-        ok = tc::mbar_wait(&mbar[buf ^ 1], ph[buf ^ 1]) && ok;
-        ph[buf ^ 1] ^= 1u;
-        pend[buf ^ 1] = 0;
-      }
-      if (!ok) {
-        abort_sh = 1;
-        atomicExch(status, -2);
-      }
-      __syncthreads();
-      if (abort_sh) {
-        done_ok = false;
-        break;
-      }
-      tc::fence_after_sync();
-      fold_levels(lane_base, H, Lo);
-      tc::fence_before_sync();
-      __syncthreads();
-    }
-  }
-
-  if (done_ok) {
-    const int row = i0 + 32 * (warp & 3) + lane;
-    if (row < n) {
-#pragma unroll
-      for (int c = 0; c < 32; ++c) {
-        const int col = j0 + 32 * (warp >> 2) + c;
-        if (col < n) {
-          atomicAdd(Hacc + (size_t)row * n + col, (unsigned long long)H[c]);
-          atomicAdd(Lacc + (size_t)row * n + col, (unsigned long long)Lo[c]);
+    for (int s = 0; s < w.nsub; ++s, ++it) {
+      const int b = it & 1;
+      uint8_t* cur = sm + b * STAGE_BYTES;
+      if (threadIdx.x == 0 && !abort_sh) {
+        // prefetch the next sub-chunk (this unit or the next) into the other buffer
+        int sn = s + 1, un = u;
+        OzUnit wn = w;
+        if (sn >= w.nsub) {
+          un = oz_next_unit(p, u);
+          wn = un >= 0 ? oz_unit(p, un) : OzUnit{0, 0, 0, 0, false};
+          sn = 0;
+        }
+        if (wn.valid) {
+          if (mma_pend == it - 1 && mma_pend >= 0) {  // the other buffer's MMAs must be done
+            if (!tc::mbar_wait(&mdone[b ^ 1], (uint32_t)((mma_pend >> 1) & 1))) {
+              abort_sh = 1;
+              atomicExch(p.status, -2);
+            }
+            mma_pend = -1;
+          }
+          if (!abort_sh) {
+            oz_load(&tmA, &tmB, p, wn, sn, sm + (b ^ 1) * STAGE_BYTES, &full[b ^ 1]);
+            ++issued;
+          }
+        }
+        if (!abort_sh) {
+          if (tc::mbar_wait(&full[b], (uint32_t)((it >> 1) & 1))) {
+            ++waited;
+          } else {
+            abort_sh = 1;
+            atomicExch(p.status, -2);
+          }
+        }
+        if (!abort_sh) {
+          tc::fence_after_sync();
+          issue_levels(tmem, tc::smem_u32(cur), tc::smem_u32(cur + A_BUF_BYTES), s % OZ_SUBS == 0);
+          tc::mma_commit(&mdone[b]);
+          mma_pend = it;
         }
       }
+      if (s % OZ_SUBS == OZ_SUBS - 1 || s == w.nsub - 1) {
+        // chunk complete: every thread waits for its MMAs, then folds the 8 levels
+        __syncthreads();
+        if (abort_sh) break;
+        bool ok = tc::mbar_wait(&mdone[b], (uint32_t)((it >> 1) & 1));
+        if (!__all_sync(0xffffffffu, ok ? 1 : 0)) {
+          abort_sh = 1;
+          atomicExch(p.status, -2);
+        }
+        __syncthreads();
+        if (abort_sh) break;
+        if (threadIdx.x == 0) mma_pend = -1;
+        tc::fence_after_sync();
+        fold_levels(lane_base, H, Lo);
+        tc::fence_before_sync();
+        __syncthreads();
+      }
     }
+    if (abort_sh) break;
+    // epilogue of the unit
+    const int row = w.m0 + 32 * (warp & 3) + lane;
+    if (p.mode == 0) {
+      if (row < p.M) {
+#pragma unroll
+        for (int c = 0; c < 32; ++c) {
+          const int col = w.n0 + 32 * (warp >> 2) + c;
+          if (col < p.N) {
+            atomicAdd(p.Hacc + (size_t)row * p.N + col, (unsigned long long)H[c]);
+            atomicAdd(p.Lacc + (size_t)row * p.N + col, (unsigned long long)Lo[c]);
+          }
+        }
+      }
+    } else if (row < p.M) {
+      const int er = exp_of_max(p.eA[row]);
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        const int j = w.n0 + 32 * (warp >> 2) + c;
+        if (j < p.N) p.Cout[row + (size_t)j * p.ldo] = fold_to_double(H[c], Lo[c], er + exp_of_max(p.eB[j]));
+      }
+    }
+    u = oz_next_unit(p, u);
+    w = u >= 0 ? oz_unit(p, u) : OzUnit{0, 0, 0, 0, false};
+  }
+  if (threadIdx.x == 0) {
+    issued_sh = issued;
+    waited_sh = waited;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // after an abort: loads issued but never waited for still land in shared memory, and
+    // committed MMAs still read it -- wait for both before the CTA exits
+    for (int j = waited_sh; j < issued_sh; ++j) tc::mbar_wait(&full[j & 1], (uint32_t)((j >> 1) & 1));
+    if (mma_pend >= 0) tc::mbar_wait(&mdone[mma_pend & 1], (uint32_t)((mma_pend >> 1) & 1));
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -381,151 +511,6 @@ __global__ void k_ozaki_syrk_finalize(const long long* __restrict__ H, const lon
   }
 }
 
-// ---------------------------------------------------------------- Cout = A M (persistent over tiles)
-// A: real view (rows x n, column-major, lda); M: n x n row-major; Cout column-major (ldo).
-// upper: M is upper triangular, column tile j only needs k < j0 + 64.
-__global__ void __launch_bounds__(OZ_THREADS, 1)
-    k_ozaki_rmul(const double* __restrict__ A, int lda, int rows, int n, const double* __restrict__ M, int upper,
-                 const unsigned long long* __restrict__ rmax, const unsigned long long* __restrict__ mcmax,
-                 double* __restrict__ Cout, int ldo, int* __restrict__ status) {
-  extern __shared__ __align__(1024) uint8_t sm[];
-  uint8_t* sA = sm;
-  uint8_t* sB = sm + 2 * A_BUF_BYTES;
-  __shared__ uint64_t mbar[2];
-  __shared__ uint32_t tmem_sh;
-  __shared__ int abort_sh;
-
-  const int nrt = (rows + OZ_M - 1) / OZ_M, nct = (n + OZ_N - 1) / OZ_N;
-  const int ntiles = nrt * nct;
-  if ((int)blockIdx.x >= ntiles) return;
-  if (*(volatile const int*)status != 0) return;  // an earlier step of this ortho failed
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (warp == 0) {
-    tc::tmem_alloc(&tmem_sh, 512);
-    tc::tmem_relinquish();
-  }
-  if (threadIdx.x == 0) {
-    tc::mbar_init(&mbar[0], 1);
-    tc::mbar_init(&mbar[1], 1);
-    tc::fence_mbar_init();
-    abort_sh = 0;
-  }
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
-  const uint32_t tmem = tmem_sh;
-  const uint32_t lane_base = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(32 * (warp >> 2));
-  uint32_t ph[2] = {0u, 0u};
-  int pend[2] = {0, 0};
-  int it = 0;
-
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    // column tile outer so that consecutive CTAs share the M slices of a column tile
-    const int ct = tile / nrt, rt = tile % nrt;
-    const int r0 = rt * OZ_M, j0 = ct * OZ_N;
-    const int kmax = upper ? min(n, j0 + OZ_N) : n;
-    const int nsub = (kmax + OZ_KS - 1) / OZ_KS;
-    long long H[32], Lo[32];
-#pragma unroll
-    for (int c = 0; c < 32; ++c) {
-      H[c] = 0;
-      Lo[c] = 0;
-    }
-    for (int s = 0; s < nsub; ++s, ++it) {
-      const int buf = it & 1;
-      if (pend[buf]) {
-        if (!tc::mbar_wait(&mbar[buf], ph[buf])) {
-          abort_sh = 1;
-          atomicExch(status, -2);
-        }
-        ph[buf] ^= 1u;
-        pend[buf] = 0;
-      }
-      __syncthreads();
-      if (abort_sh) break;
-      const int kb = s * OZ_KS;
-      uint8_t* a_dst = sA + buf * A_BUF_BYTES;
-      uint8_t* b_dst = sB + buf * B_BUF_BYTES;
-      // A rows r (consecutive threads -> consecutive r: coalesced), 8 k each
-      for (int task = threadIdx.x; task < OZ_M * 4; task += OZ_THREADS) {
-        const int row = task & (OZ_M - 1), kg = task >> 7;
-        const int r = r0 + row;
-        const bool valid = r < rows;
-        const int e = valid ? exp_of_max(rmax[r]) : 0;
-        double x[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int k = kb + kg * 8 + q;
-          x[q] = (valid && k < n) ? A[r + (size_t)k * lda] : 0.0;
-        }
-        store_digits(x, e, a_dst, A_SLICE_BYTES, core_off(row, kg));
-      }
-      // B rows j = columns of M: B[j][k] = M[k][j]
-      for (int task = threadIdx.x; task < OZ_N * 4; task += OZ_THREADS) {
-        const int row = task & (OZ_N - 1), kg = task >> 6;
-        const int j = j0 + row;
-        const bool valid = j < n;
-        const int e = valid ? exp_of_max(mcmax[j]) : 0;
-        double x[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int k = kb + kg * 8 + q;
-          x[q] = (valid && k < n) ? M[(size_t)k * n + j] : 0.0;
-        }
-        store_digits(x, e, b_dst, B_SLICE_BYTES, core_off(row, kg));
-      }
-      tc::fence_proxy_async();
-      __syncthreads();
-      const int ci = s % OZ_SUBS;
-      if (threadIdx.x == 0) {
-        tc::fence_after_sync();
-        issue_levels(tmem, tc::smem_u32(a_dst), tc::smem_u32(b_dst), ci == 0);
-        tc::mma_commit(&mbar[buf]);
-      }
-      pend[buf] = 1;
-      if (ci == OZ_SUBS - 1 || s == nsub - 1) {
-        bool ok = tc::mbar_wait(&mbar[buf], ph[buf]);
-        ph[buf] ^= 1u;
-        pend[buf] = 0;
-        if (pend[buf ^ 1]) {
-          ok = tc::mbar_wait(&mbar[buf ^ 1], ph[buf ^ 1]) && ok;
-          ph[buf ^ 1] ^= 1u;
-          pend[buf ^ 1] = 0;
-        }
-        if (!ok) {
-          abort_sh = 1;
-          atomicExch(status, -2);
-        }
-        __syncthreads();
-        if (abort_sh) break;
-        tc::fence_after_sync();
-        fold_levels(lane_base, H, Lo);
-        tc::fence_before_sync();
-        __syncthreads();
-      }
-    }
-    if (abort_sh) break;
-    // write the tile: consecutive lanes -> consecutive rows of one column (coalesced)
-    const int r = r0 + 32 * (warp & 3) + lane;
-    if (r < rows) {
-      const int er = exp_of_max(rmax[r]);
-#pragma unroll
-      for (int c = 0; c < 32; ++c) {
-        const int j = j0 + 32 * (warp >> 2) + c;
-        if (j < n) {
-          Cout[r + (size_t)j * ldo] = fold_to_double(H[c], Lo[c], er + exp_of_max(mcmax[j]));
-        }
-      }
-    }
-  }
-  tc::fence_before_sync();
-  __syncthreads();
-  if (warp == 0) {
-    __syncwarp();
-    tc::tmem_dealloc(tmem, 512);
-  }
-}
-
 }  // namespace
 
 // Overlap matrix on the tensor cores, queued without a host synchronisation.
@@ -547,25 +532,47 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, unsig
   subs_per = ((subs_per + OZ_SUBS - 1) / OZ_SUBS) * OZ_SUBS;
   nsplit = (total_subs + subs_per - 1) / subs_per;
   const size_t nn = (size_t)n * n;
-  // workspace: H, Lo (int64 n*n each), column maxima (n)
+  const size_t ks = ((size_t)K + 7) & ~size_t(7);
+  // workspace: H, Lo (int64 n*n each), column maxima (n); digit planes 8 x n x ks bf16
   const size_t bytes = 2 * nn * 8 + (size_t)n * 8;
-  if (!ensure(c, c.sparts, bytes)) return 6;
+  if (!ensure(c, c.sparts, bytes) || !ensure(c, c.oz_a, sizeof(uint16_t) * OZ_SL * (size_t)n * ks)) return 6;
   unsigned long long* Hacc = static_cast<unsigned long long*>(c.sparts.p);
   unsigned long long* Lacc = Hacc + nn;
   unsigned long long* cmax = Lacc + nn;
   GBCP_CUDA_TRY(c, cudaMemsetAsync(Hacc, 0, bytes, c.stream));
   {
     ProfScope ps_(c, "k_col_max");
-    const int ks = std::max(1, std::min(64, (K + 4095) / 4096));
-    const int kper = (K + ks - 1) / ks;
-    k_col_max<<<dim3(n, ks), 256, 0, c.stream>>>(Ar, lda, K, n, kper, cmax);
+    const int kspl = std::max(1, std::min(64, (K + 4095) / 4096));
+    const int kper = (K + kspl - 1) / kspl;
+    k_col_max<<<dim3(n, kspl), 256, 0, c.stream>>>(Ar, lda, K, n, kper, cmax);
     GBCP_LAUNCH_CHECK(c);
   }
   {
-    allow_smem(k_ozaki_syrk, OZ_SMEM);
+    ProfScope ps_(c, "k_oz_slice");
+    k_oz_slice_cols<<<dim3((K / 8 + 255) / 256 + 1, n), 256, 0, c.stream>>>(Ar, lda, K, n, cmax, ks,
+                                                                            static_cast<uint4*>(c.oz_a.p));
+    GBCP_LAUNCH_CHECK(c);
+  }
+  CUtensorMap ma, mb;
+  if (!tmap_bf16_2d(&ma, c.oz_a.p, K, (long long)OZ_SL * n, (int)ks, OZ_KS, OZ_M, 64) ||
+      !tmap_bf16_2d(&mb, c.oz_a.p, K, (long long)OZ_SL * n, (int)ks, OZ_KS, OZ_N, 64)) {
+    c.err = "ovlap: tensor map encoding failed";
+    return 5;
+  }
+  OzParams p{};
+  p.M = n;
+  p.N = n;
+  p.K = K;
+  p.mode = 0;
+  p.njb = njb;
+  p.subs_per = subs_per;
+  p.Hacc = Hacc;
+  p.Lacc = Lacc;
+  p.status = status;
+  {
+    allow_smem(k_oz_tc, OZ_SMEM);
     ProfScope ps_(c, "k_ozaki_syrk");
-    k_ozaki_syrk<<<dim3(ntiles, nsplit), OZ_THREADS, OZ_SMEM, c.stream>>>(Ar, lda, K, n, cmax, njb, subs_per, Hacc,
-                                                                          Lacc, status);
+    k_oz_tc<<<dim3(ntiles, nsplit), OZ_THREADS, OZ_SMEM, c.stream>>>(ma, mb, p);
     GBCP_LAUNCH_CHECK(c);
   }
   {
@@ -584,26 +591,53 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, unsig
 // entry, *status = -2 on a timed-out wait.
 int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout, int ldo,
             int* status) {
+  const size_t ks = ((size_t)n + 7) & ~size_t(7);
   const size_t bytes = ((size_t)rows + n) * 8;
-  if (!ensure(c, c.nl_a, bytes)) return 6;
+  if (!ensure(c, c.nl_a, bytes) || !ensure(c, c.oz_a, sizeof(uint16_t) * OZ_SL * (size_t)rows * ks) ||
+      !ensure(c, c.oz_b, sizeof(uint16_t) * OZ_SL * (size_t)n * ks))
+    return 6;
   unsigned long long* rmax = static_cast<unsigned long long*>(c.nl_a.p);
   unsigned long long* mcmax = rmax + rows;
-  {
-    ProfScope ps_(c, "k_row_max");
-    k_row_max<<<(rows + 255) / 256, 256, 0, c.stream>>>(A, lda, rows, n, rmax);
-    GBCP_LAUNCH_CHECK(c);
-  }
   {
     ProfScope ps_(c, "k_mat_col_max");
     k_mat_col_max<<<(n + 255) / 256, 256, 0, c.stream>>>(M, n, mcmax);
     GBCP_LAUNCH_CHECK(c);
   }
   {
-    allow_smem(k_ozaki_rmul, OZ_SMEM);
+    ProfScope ps_(c, "k_oz_slice");
+    k_oz_slice_rows<<<(rows + 127) / 128, 128, 0, c.stream>>>(A, lda, rows, n, rmax, ks,
+                                                             static_cast<uint4*>(c.oz_a.p));
+    GBCP_LAUNCH_CHECK(c);
+    k_oz_slice_mat<<<dim3((n + 127) / 128, (n + 7) / 8), 128, 0, c.stream>>>(M, n, mcmax, ks,
+                                                                            static_cast<uint4*>(c.oz_b.p));
+    GBCP_LAUNCH_CHECK(c);
+  }
+  CUtensorMap ma, mb;
+  if (!tmap_bf16_2d(&ma, c.oz_a.p, n, (long long)OZ_SL * rows, (int)ks, OZ_KS, OZ_M, 64) ||
+      !tmap_bf16_2d(&mb, c.oz_b.p, n, (long long)OZ_SL * n, (int)ks, OZ_KS, OZ_N, 64)) {
+    c.err = "C.M: tensor map encoding failed";
+    return 5;
+  }
+  OzParams p{};
+  p.M = rows;
+  p.N = n;
+  p.K = n;
+  p.mode = 1;
+  p.upper = upper;
+  p.eA = rmax;
+  p.eB = mcmax;
+  p.Cout = Cout;
+  p.ldo = ldo;
+  p.status = status;
+  {
+    allow_smem(k_oz_tc, OZ_SMEM);
     const int ntiles = ((rows + OZ_M - 1) / OZ_M) * ((n + OZ_N - 1) / OZ_N);
-    const int grid = std::max(1, std::min(ntiles, 148));
+    int dev = 0, nsm = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = std::max(1, std::min(ntiles, nsm));
     ProfScope ps_(c, "k_ozaki_rmul");
-    k_ozaki_rmul<<<grid, OZ_THREADS, OZ_SMEM, c.stream>>>(A, lda, rows, n, M, upper, rmax, mcmax, Cout, ldo, status);
+    k_oz_tc<<<grid, OZ_THREADS, OZ_SMEM, c.stream>>>(ma, mb, p);
     GBCP_LAUNCH_CHECK(c);
   }
   return 0;

@@ -138,5 +138,13 @@ __device__ __forceinline__ uint64_t sdesc_kmajor_sw128(uint32_t saddr) {
          (2ull << 61);
 }
 
+// The same for 64-byte swizzle (TMA CU_TENSOR_MAP_SWIZZLE_64B): rows of 32 bf16
+// (64 B), 8-row groups 512 B apart, tile base 512-byte aligned; K advances by
+// 16 elements = 32 bytes inside the row.
+__device__ __forceinline__ uint64_t sdesc_kmajor_sw64(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | (1ull << 16) | ((uint64_t)(512 >> 4) << 32) | (1ull << 46) |
+         (4ull << 61);
+}
+
 }  // namespace tc
 }  // namespace gbcp

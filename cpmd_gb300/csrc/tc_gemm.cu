@@ -252,17 +252,27 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-bool make_map(CUtensorMap* m, const void* base, int K, long long rows, int kstride, int box_rows) {
+
+}  // namespace
+
+bool tmap_bf16_2d(CUtensorMap* m, const void* base, int K, long long rows, int kstride, int box_k, int box_rows,
+                  int swizzle_bytes) {
   auto fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)kstride * 2};
-  cuuint32_t box[2] = {(cuuint32_t)TG_K, (cuuint32_t)box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)box_k, (cuuint32_t)box_rows};
   cuuint32_t es[2] = {1, 1};
+  const CUtensorMapSwizzle sw = swizzle_bytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                : swizzle_bytes == 64  ? CU_TENSOR_MAP_SWIZZLE_64B
+                                : swizzle_bytes == 32  ? CU_TENSOR_MAP_SWIZZLE_32B
+                                                       : CU_TENSOR_MAP_SWIZZLE_NONE;
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
+
+namespace {
 
 int num_sms() {
   static int n = 0;
@@ -307,8 +317,8 @@ int tc_gemm_split3(Ctx& c, const uint16_t* A, int M, const uint16_t* B, int N, i
     nslB = std::max(nslB, pt[q] + 1);
   }
   CUtensorMap ma, mb;
-  if (!make_map(&ma, A, K, (long long)nslA * M, kstride, TG_M) ||
-      !make_map(&mb, B, K, (long long)nslB * N, kstride, TG_N)) {
+  if (!tmap_bf16_2d(&ma, A, K, (long long)nslA * M, kstride, TG_K, TG_M, 128) ||
+      !tmap_bf16_2d(&mb, B, K, (long long)nslB * N, kstride, TG_K, TG_N, 128)) {
     c.err = "tc_gemm: tensor map encoding failed";
     return 5;
   }

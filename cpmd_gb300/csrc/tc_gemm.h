@@ -2,9 +2,16 @@
 #pragma once
 #include <stdint.h>
 
+struct CUtensorMap_st;
+
 namespace gbcp {
 
 struct Ctx;
+
+// 2D bf16 tensor map over `rows` rows of K elements (row stride kstride elements,
+// a multiple of 8), box of box_k x box_rows, swizzle 0 / 32 / 64 / 128 bytes.
+bool tmap_bf16_2d(CUtensorMap_st* m, const void* base, int K, long long rows, int kstride, int box_k, int box_rows,
+                  int swizzle_bytes);
 
 constexpr int kTGMaxPairs = 6;
 
