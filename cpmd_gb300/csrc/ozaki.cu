@@ -105,18 +105,21 @@ __device__ __forceinline__ void digits8(const double (&x)[8], int E, uint4 (&out
 }
 
 // Issue the 72 MMAs of one sub-chunk (36 digit pairs x 2 K-steps) into the 8
-// level accumulators; `first` restarts the accumulators (chunk start).
+// level accumulators; `first` restarts the accumulators (chunk start).  Fully
+// unrolled: every descriptor is its base plus (byte offset >> 4), so the single
+// issuing thread spends two or three instructions per MMA.
 __device__ __forceinline__ void issue_levels(uint32_t tmem, uint32_t a_base, uint32_t b_base, bool first) {
-#pragma unroll 1
+  const uint64_t a0 = tc::sdesc_kmajor_sw64(a_base), b0 = tc::sdesc_kmajor_sw64(b_base);
+#pragma unroll
   for (int d = 0; d < OZ_LEV; ++d) {
     const uint32_t dt = tmem + (uint32_t)(OZ_N * d);
-#pragma unroll 1
+#pragma unroll
     for (int s = 0; s <= d; ++s) {
       const int u = d - s;
 #pragma unroll
       for (int kk = 0; kk < 2; ++kk) {
-        const uint64_t ad = tc::sdesc_kmajor_sw64(a_base + s * A_SLICE_BYTES + kk * 32);
-        const uint64_t bd = tc::sdesc_kmajor_sw64(b_base + u * B_SLICE_BYTES + kk * 32);
+        const uint64_t ad = a0 + (uint64_t)((s * A_SLICE_BYTES + kk * 32) >> 4);
+        const uint64_t bd = b0 + (uint64_t)((u * B_SLICE_BYTES + kk * 32) >> 4);
         tc::mma_f16(dt, ad, bd, kIdesc, (first && s == 0 && kk == 0) ? 0u : 1u);
       }
     }
@@ -223,31 +226,42 @@ __global__ void k_oz_slice_cols(const double* __restrict__ Ar, int lda, int K, i
   for (int s = 0; s < OZ_SL; ++s) out[s * plane + off] = d[s];
 }
 
-// C M operand A: plane s, row r (real-view row of C), columns k < n (states), with the
-// row's own exponent (its maximum over the n states, also written to emax[r] for the
-// epilogue).  One thread per row: consecutive threads read consecutive rows (coalesced),
-// and each thread writes whole plane rows, which L2 merges into full lines.
-__global__ void k_oz_slice_rows(const double* __restrict__ Ar, int lda, int rows, int n,
-                                unsigned long long* __restrict__ emax, size_t ks, uint4* __restrict__ out) {
+// row maxima of the real view over the n states: bits into rmax[r]
+__global__ void k_row_max(const double* __restrict__ Ar, int lda, int rows, int n,
+                          unsigned long long* __restrict__ rmax) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= rows) return;
   unsigned long long mx = 0;
   for (int k = 0; k < n; ++k) {
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(Ar[r + (size_t)k * lda]) & ~(1ull << 63);
-    mx = bits > mx ? bits : mx;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(Ar[r + (size_t)k * lda]) & ~(1ull << 63);
+    mx = b > mx ? b : mx;
   }
-  emax[r] = mx;
-  const int e = exp_of_max(mx);
-  const size_t plane = (size_t)rows * ks / 8;
-  for (int k = 0; k < n; k += 8) {
-    double x[8];
+  rmax[r] = mx;
+}
+
+// C M operand A: plane s, row r (real-view row of C), columns k < n (states); exponent per
+// row.  Thread = (row, 16 states): consecutive threads read consecutive rows (coalesced)
+// and each plane store is one full 32-byte sector.
+__global__ void k_oz_slice_rows(const double* __restrict__ Ar, int lda, int rows, int n,
+                                const unsigned long long* __restrict__ emax, size_t ks, uint4* __restrict__ out) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y * 16;
+  if (r >= rows) return;
+  const int e = exp_of_max(emax[r]);
+  double x0[8], x1[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) x[q] = (k + q < n) ? Ar[r + (size_t)(k + q) * lda] : 0.0;
-    uint4 d[OZ_SL];
-    digits8(x, e, d);
-    const size_t off = ((size_t)r * ks + k) / 8;
+  for (int q = 0; q < 8; ++q) {
+    x0[q] = (k + q < n) ? Ar[r + (size_t)(k + q) * lda] : 0.0;
+    x1[q] = (k + 8 + q < n) ? Ar[r + (size_t)(k + 8 + q) * lda] : 0.0;
+  }
+  uint4 d0[OZ_SL], d1[OZ_SL];
+  digits8(x0, e, d0);
+  digits8(x1, e, d1);
+  const size_t plane = (size_t)rows * ks / 8, off = ((size_t)r * ks + k) / 8;
 #pragma unroll
-    for (int s = 0; s < OZ_SL; ++s) out[s * plane + off] = d[s];
+  for (int s = 0; s < OZ_SL; ++s) {
+    out[s * plane + off] = d0[s];
+    if (k + 8 < n) out[s * plane + off + 1] = d1[s];
   }
 }
 
@@ -604,9 +618,14 @@ int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, 
     GBCP_LAUNCH_CHECK(c);
   }
   {
+    ProfScope ps_(c, "k_row_max");
+    k_row_max<<<(rows + 255) / 256, 256, 0, c.stream>>>(A, lda, rows, n, rmax);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  {
     ProfScope ps_(c, "k_oz_slice");
-    k_oz_slice_rows<<<(rows + 127) / 128, 128, 0, c.stream>>>(A, lda, rows, n, rmax, ks,
-                                                             static_cast<uint4*>(c.oz_a.p));
+    k_oz_slice_rows<<<dim3((rows + 127) / 128, (n + 15) / 16), 128, 0, c.stream>>>(A, lda, rows, n, rmax, ks,
+                                                                                  static_cast<uint4*>(c.oz_a.p));
     GBCP_LAUNCH_CHECK(c);
     k_oz_slice_mat<<<dim3((n + 127) / 128, (n + 7) / 8), 128, 0, c.stream>>>(M, n, mcmax, ks,
                                                                             static_cast<uint4*>(c.oz_b.p));
