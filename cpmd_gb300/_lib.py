@@ -60,6 +60,8 @@ SIGNATURES = {
     "gbcp_fwfftn": (_I, [_P, _P, _I]),
     "gbcp_rnlsm1": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _I]),
     "gbcp_fnonloc": (_I, [_P, _P, _I, _I, _P, _I, _I, _P, _P, _P, _P, _P, _I]),
+    "gbcp_rnlsm2": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _I]),
+    "gbcp_rnlfor": (_I, [_P, _I, _P, _I, _I, _P, _P, _P, _P, _I]),
     "gbcp_set_dens_sphere": (_I, [_P, _I, _P, _P]),
     "gbcp_energy": (_I, [_P, _P, _I, _I, _P, _I, _I, _P, _P, _P, _P, _P, _P, _I, _P, _P, _I]),
     "gbcp_batch_create": (_I, [_I, _P, _I, _I, C.POINTER(_P)]),

@@ -255,6 +255,32 @@ class Context:
                                                         _ptr(eigr), _ptr(fnl), mem))
         return fnl
 
+    def rnlsm2(self, c0, twnl, eigr, nghtol, dfnl=None):
+        """dfnl (nstate, 3, ngh, nat) == Fortran dfnl(nat, ngh, 3, nstate) = d fnl / d R."""
+        ldc, n = _ld_wfn(c0, self.ngw)
+        ngh = int(len(nghtol))
+        nat = int(eigr.shape[1] if not _is_torch(eigr) else eigr.shape[0])
+        nt = np.ascontiguousarray(np.asarray(nghtol, dtype=np.int32))
+        if dfnl is None:
+            if _is_torch(c0):
+                import torch
+                dfnl = torch.empty((n, 3, ngh, nat), dtype=torch.float64, device=c0.device)
+            else:
+                dfnl = np.empty((n, 3, ngh, nat))
+        mem = self._prep(c0, twnl, eigr, dfnl)
+        self._check("gbcp_rnlsm2", self.lib.gbcp_rnlsm2(self.h, _ptr(c0), ldc, n, nat, ngh, _ptr(nt), _ptr(twnl),
+                                                        _ptr(eigr), _ptr(dfnl), mem))
+        return dfnl
+
+    def rnlfor(self, f, fnl, dfnl, wsg, fion):
+        """fion (nat, 3) == Fortran fion(3, nat) -= the non-local forces (accumulated)."""
+        n = int(f.shape[0])
+        nat, ngh = int(fnl.shape[2]), int(fnl.shape[1])
+        mem = self._prep(f, fnl, dfnl, wsg, fion)
+        self._check("gbcp_rnlfor", self.lib.gbcp_rnlfor(self.h, n, _ptr(f), nat, ngh, _ptr(wsg), _ptr(fnl),
+                                                        _ptr(dfnl), _ptr(fion), mem))
+        return fion
+
     def fnonloc(self, c2, f, fnl, twnl, eigr, nghtol, wsg):
         ld2, n = _ld_wfn(c2, self.ngw)
         ngh = int(len(nghtol))

@@ -240,6 +240,16 @@ static int build_geometry(Ctx& c, const int32_t* inyh, const double* hg) {
     return 6;
   }
   c.kin = const_cast<double*>(dk);
+  std::vector<short4> wm(ngw);
+  for (int ig = 0; ig < ngw; ++ig)
+    wm[ig] = make_short4((short)(inyh[3 * (size_t)ig] - (n[0] / 2 + 1)), (short)(inyh[3 * (size_t)ig + 1] - (n[1] / 2 + 1)),
+                         (short)(inyh[3 * (size_t)ig + 2] - (n[2] / 2 + 1)), 0);
+  const short4* dwm = nullptr;
+  if (!upload(c, wm, dwm)) {
+    c.err = "geometry upload failed";
+    return 6;
+  }
+  c.wmill = dwm;
   return 0;
 }
 
@@ -675,6 +685,76 @@ int gbcp_rnlsm1(gbcp_ctx* h, const double* c0, int ldc, int nstate, int nat, int
   rc = gbcp::nl_rnlsm1(c, dc0, l0, nstate, nat, ngh, nghtol, dtw, de, dfnl);
   if (!rc && mem == GBCP_MEM_HOST) {
     cudaError_t e = cudaMemcpyAsync(fnl, dfnl, sizeof(double) * nfnl, cudaMemcpyDeviceToHost, c.stream);
+    if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (mem == GBCP_MEM_HOST || rc) return finish(c, rc);
+  return GBCP_OK;
+}
+
+int gbcp_rnlsm2(gbcp_ctx* h, const double* c0, int ldc, int nstate, int nat, int ngh, const int32_t* nghtol,
+                const double* twnl, const double* eigr, double* dfnl, int mem) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  if (bad_mem(mem) || nstate <= 0 || nat <= 0 || ngh <= 0 || !c0 || !nghtol || !twnl || !eigr || !dfnl ||
+      ldc < c.ngw)
+    return set_err(h, GBCP_ERR_ARG, "rnlsm2: bad argument");
+  c.err.clear();
+  const cx<double>* dc0 = reinterpret_cast<const cx<double>*>(c0);
+  const double* dtw = twnl;
+  const cx<double>* de = reinterpret_cast<const cx<double>*>(eigr);
+  double* dd = dfnl;
+  int l0 = ldc;
+  int rc = 0;
+  const size_t nd = (size_t)nat * ngh * 3 * nstate;
+  if (mem == GBCP_MEM_HOST) {
+    cx<double>* t0;
+    void *t1, *t2;
+    if ((rc = stage_in_cx(c, c.st_c0, c0, ldc, c.ngw, nstate, &t0))) return rc;
+    if ((rc = stage_in(c, c.nl_b, twnl, sizeof(double) * (size_t)c.ngw * ngh, &t1))) return rc;
+    if ((rc = stage_in(c, c.nl_c, eigr, sizeof(cx<double>) * (size_t)c.ngw * nat, &t2))) return rc;
+    if (!gbcp::ensure(c, c.nl_d, sizeof(double) * nd)) return GBCP_ERR_NOMEM;
+    dc0 = t0;
+    dtw = static_cast<double*>(t1);
+    de = static_cast<cx<double>*>(t2);
+    dd = static_cast<double*>(c.nl_d.p);
+    l0 = c.ngw;
+  }
+  rc = gbcp::nl_rnlsm2(c, dc0, l0, nstate, nat, ngh, nghtol, dtw, de, dd);
+  if (!rc && mem == GBCP_MEM_HOST) {
+    cudaError_t e = cudaMemcpyAsync(dfnl, dd, sizeof(double) * nd, cudaMemcpyDeviceToHost, c.stream);
+    if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (mem == GBCP_MEM_HOST || rc) return finish(c, rc);
+  return GBCP_OK;
+}
+
+int gbcp_rnlfor(gbcp_ctx* h, int nstate, const double* f, int nat, int ngh, const double* wsg, const double* fnl,
+                const double* dfnl, double* fion, int mem) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  if (bad_mem(mem) || nstate <= 0 || nat <= 0 || ngh <= 0 || !f || !wsg || !fnl || !dfnl || !fion)
+    return set_err(h, GBCP_ERR_ARG, "rnlfor: bad argument");
+  c.err.clear();
+  const double *df = f, *dw = wsg, *dfn = fnl, *ddf = dfnl;
+  double* dfi = fion;
+  int rc = 0;
+  const size_t P = (size_t)nat * ngh;
+  if (mem == GBCP_MEM_HOST) {
+    void *t1, *t2, *t3, *t4, *t5;
+    if ((rc = stage_in(c, c.st_f, f, sizeof(double) * nstate, &t1))) return rc;
+    if ((rc = stage_in(c, c.st_misc, wsg, sizeof(double) * ngh, &t2))) return rc;
+    if ((rc = stage_in(c, c.nl_b, fnl, sizeof(double) * P * nstate, &t3))) return rc;
+    if ((rc = stage_in(c, c.nl_d, dfnl, sizeof(double) * P * 3 * nstate, &t4))) return rc;
+    if ((rc = stage_in(c, c.st_misc2, fion, sizeof(double) * 3 * nat, &t5))) return rc;
+    df = static_cast<double*>(t1);
+    dw = static_cast<double*>(t2);
+    dfn = static_cast<double*>(t3);
+    ddf = static_cast<double*>(t4);
+    dfi = static_cast<double*>(t5);
+  }
+  rc = gbcp::nl_rnlfor(c, nstate, df, nat, ngh, dw, dfn, ddf, dfi);
+  if (!rc && mem == GBCP_MEM_HOST) {
+    cudaError_t e = cudaMemcpyAsync(fion, dfi, sizeof(double) * 3 * nat, cudaMemcpyDeviceToHost, c.stream);
     if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));
   }
   if (mem == GBCP_MEM_HOST || rc) return finish(c, rc);

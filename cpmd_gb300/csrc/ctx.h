@@ -101,6 +101,7 @@ struct Ctx {
   Scratch nl_ta, nl_tb, nl_tp;  // projector GEMM slices (A, B) and split-K partials
   int* d_info = nullptr;
   double* kin = nullptr;  // tpiba2 * hg (ngw), the kinetic factor of vpsi
+  const short4* wmill = nullptr;  // Miller indices of the wavefunction sphere (ngw)
   // density sphere of the energy functional (gbcp_set_dens_sphere)
   int nhg = 0, dmax = 0;           // half-sphere size, largest |Miller index|
   const int* dpos = nullptr;       // offset of +G in the (kr1, kr2, nr3) complex grid
@@ -181,6 +182,10 @@ int energy_and_grad(Ctx& c, const cx<double>* c0, int ldc, int nstate, const dou
 // ---- projectors (nonlocal.cu) ----
 int nl_rnlsm1(Ctx& c, const cx<double>* c0, int ldc, int nstate, int nat, int ngh, const int* nghtol_host,
               const double* twnl, const cx<double>* eigr, double* fnl);
+int nl_rnlsm2(Ctx& c, const cx<double>* c0, int ldc, int nstate, int nat, int ngh, const int* nghtol_host,
+              const double* twnl, const cx<double>* eigr, double* dfnl);
+int nl_rnlfor(Ctx& c, int nstate, const double* f, int nat, int ngh, const double* wsg, const double* fnl,
+              const double* dfnl, double* fion);
 int nl_fnonloc(Ctx& c, cx<double>* c2, int ldc2, int nstate, const double* f, int nat, int ngh,
                const int* nghtol_host, const double* twnl, const cx<double>* eigr, const double* fnl,
                const double* wsg);

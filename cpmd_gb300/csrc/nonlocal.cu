@@ -21,6 +21,7 @@
 //      fnonloc: c2 (2 ngw x n, real view) += Y Z over K = P projectors,
 //               Y = (-i)^l twnl eigr, Z = -f wsg fnl, FP64 read-modify-write.
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "ctx.h"
@@ -38,6 +39,11 @@ constexpr int kMaxProj = 64;
 struct ProjInfo {
   int nat, ngh;
   int lmod4[kMaxProj];  // angular momentum mod 4 per projector
+  // rnlsm2 (dfnl = d fnl / d R): rows p = ia + nat (iv + ngh k) for the three directions k,
+  // operand (-i)^(l+1) twnl eigr tpiba G_k (rnlsm2_utils.mod.F90:190-240)
+  int deriv;
+  const short4* gm;     // Miller indices of the sphere (deriv only)
+  double tpiba;
 };
 
 // (-i)^l * z
@@ -50,6 +56,24 @@ __device__ __forceinline__ cx<double> phase_l(int l, cx<double> z) {
   }
 }
 
+// projector operand row p at sphere index G: (-i)^l eigr times the real factor t = twnl,
+// or for rnlsm2 (-i)^(l+1) eigr times t = twnl tpiba G_k
+__device__ __forceinline__ cx<double> proj_operand(const ProjInfo& pi, const double* __restrict__ twnl,
+                                                   const cx<double>* __restrict__ eigr, int ngw, int p, int G,
+                                                   double& t) {
+  const int ia = p % pi.nat, iv = (p / pi.nat) % pi.ngh;
+  t = twnl[(size_t)iv * ngw + G];
+  int l = pi.lmod4[iv];
+  if (pi.deriv) {
+    const int kd = p / (pi.nat * pi.ngh);
+    const short4 m = pi.gm[G];
+    t *= pi.tpiba * (double)(kd == 0 ? m.x : kd == 1 ? m.y : m.z);
+    l += 1;
+  }
+  return phase_l(l, eigr[(size_t)ia * ngw + G]);
+}
+
+
 // fnl partials: part[split][p][i], p = ia + nat*iv, K over real view 2*ngw
 __global__ void __launch_bounds__(NT) k_rnlsm1_part(const double* __restrict__ c0r, int ldr, int ngw, int nstate,
                                                     ProjInfo pi, const double* __restrict__ twnl,
@@ -57,7 +81,7 @@ __global__ void __launch_bounds__(NT) k_rnlsm1_part(const double* __restrict__ c
                                                     double* __restrict__ part) {
   __shared__ double As[BK][TS + 1];
   __shared__ double Bs[BK][TS + 1];
-  const int P = pi.nat * pi.ngh;
+  const int P = pi.nat * pi.ngh * (pi.deriv ? 3 : 1);
   const int p0 = blockIdx.x * TS, i0 = blockIdx.y * TS, split = blockIdx.z;
   const int K = 2 * ngw;
   const int k0 = split * kchunk, k1 = min(K, k0 + kchunk);
@@ -71,10 +95,9 @@ __global__ void __launch_bounds__(NT) k_rnlsm1_part(const double* __restrict__ c
       double av = 0.0;
       const int p = p0 + cc;
       if (k < k1 && p < P) {
-        const int ia = p % pi.nat, iv = p / pi.nat;
         const int G = k >> 1;
-        cx<double> s = phase_l(pi.lmod4[iv], eigr[(size_t)ia * ngw + G]);
-        double t = twnl[(size_t)iv * ngw + G];
+        double t;
+        const cx<double> s = proj_operand(pi, twnl, eigr, ngw, p, G, t);
         if (geq0 && G == 0) t *= 0.5;
         av = t * ((k & 1) ? s.y : s.x);
       }
@@ -187,6 +210,9 @@ bool make_info(Ctx& c, int nat, int ngh, const int* nghtol, ProjInfo& pi) {
   }
   pi.nat = nat;
   pi.ngh = ngh;
+  pi.deriv = 0;
+  pi.gm = nullptr;
+  pi.tpiba = 0.0;
   for (int i = 0; i < ngh; ++i) pi.lmod4[i] = ((nghtol[i] % 4) + 4) % 4;
   return true;
 }
@@ -220,20 +246,32 @@ __global__ void __launch_bounds__(256) k_nl_scr3(const double* __restrict__ twnl
                                                  uint32_t* __restrict__ A) {
   const int G = blockIdx.x * 256 + threadIdx.x, a = blockIdx.y;
   if (G >= ngw) return;
-  const size_t P = (size_t)pi.nat * pi.ngh;
+  const size_t P = (size_t)pi.nat * pi.ngh * (pi.deriv ? 3 : 1);
   const cx<double> e = eigr[G + (size_t)ngw * a];
   const float ex = d2f_int(e.x), ey = d2f_int(e.y);
   const float half = (geq0 && G == 0) ? 0.5f : 1.0f;
+  float gk[3] = {1.f, 1.f, 1.f};
+  if (pi.deriv) {
+    const short4 m = pi.gm[G];
+    const float tp = d2f_int(pi.tpiba);
+    gk[0] = tp * (float)m.x;
+    gk[1] = tp * (float)m.y;
+    gk[2] = tp * (float)m.z;
+  }
+  const int nk = pi.deriv ? 3 : 1;
   for (int iv = 0; iv < pi.ngh; ++iv) {
-    const float tw = d2f_int(twnl[G + (size_t)ngw * iv]) * half;
-    float re = tw * ex, im = tw * ey;
-    phase_lf(pi.lmod4[iv], re, im);
-    uint32_t hr[3], hi[3];
-    split3(re, hr);
-    split3(im, hi);
-    const size_t p = (size_t)a + (size_t)pi.nat * iv;
+    const float tw0 = d2f_int(twnl[G + (size_t)ngw * iv]) * half;
+    for (int kd = 0; kd < nk; ++kd) {
+      const float tw = tw0 * gk[kd];
+      float re = tw * ex, im = tw * ey;
+      phase_lf(pi.lmod4[iv] + pi.deriv, re, im);
+      uint32_t hr[3], hi[3];
+      split3(re, hr);
+      split3(im, hi);
+      const size_t p = (size_t)a + (size_t)pi.nat * (iv + (size_t)pi.ngh * kd);
 #pragma unroll
-    for (int s = 0; s < 3; ++s) A[((s * P + p) * kstride) / 2 + G] = hr[s] | (hi[s] << 16);
+      for (int s = 0; s < 3; ++s) A[((s * P + p) * kstride) / 2 + G] = hr[s] | (hi[s] << 16);
+    }
   }
 }
 
@@ -332,7 +370,7 @@ int check_status(Ctx& c) {
 
 int rnlsm1_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, const ProjInfo& pi, const double* twnl,
               const cx<double>* eigr, double* fnl) {
-  const int P = pi.nat * pi.ngh;
+  const int P = pi.nat * pi.ngh * (pi.deriv ? 3 : 1);
   const int K = 2 * c.ngw;
   const size_t ks = round8((size_t)K);
   if (!ensure(c, c.nl_ta, 2 * 3 * ks * (size_t)P) || !ensure(c, c.nl_tb, 2 * 3 * ks * (size_t)nstate)) return 6;
@@ -387,12 +425,12 @@ bool use_tc_projectors(const Ctx& c) { return c.precision == 1 && c.gemm_mode !=
 
 }  // namespace
 
-int nl_rnlsm1(Ctx& c, const cx<double>* c0, int ldc, int nstate, int nat, int ngh, const int* nghtol_host,
-              const double* twnl, const cx<double>* eigr, double* fnl) {
-  ProjInfo pi;
-  if (!make_info(c, nat, ngh, nghtol_host, pi)) return 1;
-  if (use_tc_projectors(c)) return rnlsm1_tc(c, c0, ldc, nstate, pi, twnl, eigr, fnl);
-  const int P = nat * ngh;
+namespace {
+
+// fnl (or dfnl) = 2 scr^T c0 in FP64 on the SIMT units (split-K over G, folded in order)
+int rnlsm1_simt(Ctx& c, const cx<double>* c0, int ldc, int nstate, const ProjInfo& pi, const double* twnl,
+                const cx<double>* eigr, double* fnl) {
+  const int P = pi.nat * pi.ngh * (pi.deriv ? 3 : 1);
   const int K = 2 * c.ngw;
   const int tiles = ((P + TS - 1) / TS) * ((nstate + TS - 1) / TS);
   int nsplit = std::max(1, std::min(512, (4 * 152 + tiles - 1) / tiles));
@@ -414,6 +452,73 @@ int nl_rnlsm1(Ctx& c, const cx<double>* c0, int ldc, int nstate, int nat, int ng
     k_rnlsm1_fold<<<512, 256, 0, c.stream>>>(part, nsplit, n, fnl);
     GBCP_LAUNCH_CHECK(c);
   }
+  return 0;
+}
+
+}  // namespace
+
+int nl_rnlsm1(Ctx& c, const cx<double>* c0, int ldc, int nstate, int nat, int ngh, const int* nghtol_host,
+              const double* twnl, const cx<double>* eigr, double* fnl) {
+  ProjInfo pi;
+  if (!make_info(c, nat, ngh, nghtol_host, pi)) return 1;
+  if (use_tc_projectors(c)) return rnlsm1_tc(c, c0, ldc, nstate, pi, twnl, eigr, fnl);
+  return rnlsm1_simt(c, c0, ldc, nstate, pi, twnl, eigr, fnl);
+}
+
+namespace {
+
+// fion(k, ia) -= sum_i sum_iv 2 wsg(iv) f_i dfnl(ia,iv,k,i) fnl(ia,iv,i), states with |f| > 1e-12
+// (rnlfor_utils.mod.F90:283-330, KB branch); one CTA per atom, fixed-order reduction
+__global__ void __launch_bounds__(256) k_rnlfor(int nstate, const double* __restrict__ f, int nat, int ngh,
+                                                const double* __restrict__ wsg, const double* __restrict__ fnl,
+                                                const double* __restrict__ dfnl, double* __restrict__ fion) {
+  const int ia = blockIdx.x;
+  const size_t P = (size_t)nat * ngh;
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (int t = threadIdx.x; t < nstate * ngh; t += blockDim.x) {
+    const int i = t / ngh, iv = t - i * ngh;
+    const double w = f[i];
+    if (!(fabs(w) > 1e-12)) continue;
+    const size_t p = (size_t)ia + (size_t)nat * iv;
+    const double a = 2.0 * wsg[iv] * w * fnl[p + P * i];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) acc[k] = fma(a, dfnl[p + P * (k + 3 * (size_t)i)], acc[k]);
+  }
+  __shared__ double red[3][256];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) red[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) fion[3 * (size_t)ia + threadIdx.x] -= red[threadIdx.x][0];
+}
+
+}  // namespace
+
+int nl_rnlsm2(Ctx& c, const cx<double>* c0, int ldc, int nstate, int nat, int ngh, const int* nghtol_host,
+              const double* twnl, const cx<double>* eigr, double* dfnl) {
+  ProjInfo pi;
+  if (!make_info(c, nat, ngh, nghtol_host, pi)) return 1;
+  pi.deriv = 1;
+  pi.gm = c.wmill;
+  pi.tpiba = std::sqrt(c.tpiba2);
+  if (use_tc_projectors(c)) return rnlsm1_tc(c, c0, ldc, nstate, pi, twnl, eigr, dfnl);
+  return rnlsm1_simt(c, c0, ldc, nstate, pi, twnl, eigr, dfnl);
+}
+
+int nl_rnlfor(Ctx& c, int nstate, const double* f, int nat, int ngh, const double* wsg, const double* fnl,
+              const double* dfnl, double* fion) {
+  if (nat <= 0 || ngh <= 0 || nstate <= 0) {
+    c.err = "rnlfor: bad sizes";
+    return 1;
+  }
+  ProfScope ps_(c, "k_rnlfor");
+  k_rnlfor<<<nat, 256, 0, c.stream>>>(nstate, f, nat, ngh, wsg, fnl, dfnl, fion);
+  GBCP_LAUNCH_CHECK(c);
   return 0;
 }
 

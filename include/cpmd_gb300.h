@@ -162,6 +162,19 @@ int gbcp_fwfftn(gbcp_ctx* ctx, double* f, int mem);
 int gbcp_rnlsm1(gbcp_ctx* ctx, const double* c0, int ldc, int nstate, int nat, int ngh, const int32_t* nghtol,
                 const double* twnl, const double* eigr, double* fnl, int mem);
 
+/* rnlsm2(c0, nstate, ikpt, ikind)          rnlsm2_utils.mod.F90:41-299 (Γ branch l.190-240)
+ * dfnl(nat, ngh, 3, nstate) = d fnl / d R_k
+ *   = 2 tpiba Re sum_G conj((-i)^(l+1) twnl(G,iv) eigr(G,ia) G_k) c(G), G = 0 halved,
+ * G_k the Miller index along k (cubic cell).  Same operands as gbcp_rnlsm1. */
+int gbcp_rnlsm2(gbcp_ctx* ctx, const double* c0, int ldc, int nstate, int nat, int ngh, const int32_t* nghtol,
+                const double* twnl, const double* eigr, double* dfnl, int mem);
+
+/* rnlfor(fion, f, wk, nstate, nkpoint)      rnlfor_utils.mod.F90:41-368 (KB branch l.283-330)
+ * fion(3, nat) -= sum_i sum_iv 2 wsg(iv) f_i fnl(ia,iv,i) dfnl(ia,iv,k,i) for |f_i| > 1e-12
+ * (accumulated, like the reference; Γ point, one species). */
+int gbcp_rnlfor(gbcp_ctx* ctx, int nstate, const double* f, int nat, int ngh, const double* wsg, const double* fnl,
+                const double* dfnl, double* fion, int mem);
+
 /* fnonloc(c2, f, nstate, ...)               fnonloc_utils.mod.F90:306-354 (BHS/KB branch)
  * c2(G,i) += sum_iv twnl(G,iv) (-i)^l (-f_i wsg(iv)) sum_ia eigr(G,ia) fnl(ia,iv,i),
  * f_i < 1e-5 counted as 1. */

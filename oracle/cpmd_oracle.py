@@ -395,3 +395,37 @@ def energy(c0, f, basis, tau, vps, isp, vext=None, grad=True):
     t = eig * (vps[:, isp] * np.conj(rg)[:, None])                 # (nhg, nat)
     fion = np.einsum("g,gd,ga->ad", wf, gcart, (1j * t).real)
     return terms, c2, dvloc, fion, veff
+
+
+# ----------------------------------------------------------------------------
+# Non-local forces
+# ----------------------------------------------------------------------------
+def rnlsm2(c0, twnl, eigr, nghtol, mill, tpiba, geq0):
+    """dfnl(ia, iv, k, i) = 2 tpiba Re sum conj((-i)^(l+1) twnl eigr G_k) c, G = 0 halved
+    (rnlsm2_utils.mod.F90:190-240, Γ branch)."""
+    ngw, nstate = c0.shape
+    nat = eigr.shape[1]
+    ngh = twnl.shape[1]
+    g = np.asarray(mill[:ngw], dtype=np.float64)
+    dfnl = np.zeros((nat, ngh, 3, nstate))
+    for iv in range(ngh):
+        for k in range(3):
+            scr = (_ci(nghtol[iv] + 1) * twnl[:, iv] * g[:, k])[:, None] * eigr
+            if geq0:
+                scr = scr.copy()
+                scr[0] *= 0.5
+            dfnl[:, iv, k, :] = 2.0 * tpiba * (scr.real.T @ c0.real + scr.imag.T @ c0.imag)
+    return dfnl
+
+
+def rnlfor(f, fnl, dfnl, wsg):
+    """Non-local forces, KB branch (rnlfor_utils.mod.F90:283-330):
+    F(ia, k) = -sum_i sum_iv 2 wsg(iv) f_i fnl(ia,iv,i) dfnl(ia,iv,k,i), |f_i| > 1e-12."""
+    w = np.where(np.abs(f) > 1e-12, f, 0.0)
+    return -np.einsum("v,i,avi,avki->ak", 2.0 * np.asarray(wsg), w, fnl, dfnl)
+
+
+def enl(c0, f, twnl, eigr, nghtol, wsg, geq0):
+    """E_nl = sum_i f_i sum_{ia,iv} wsg(iv) fnl(ia,iv,i)^2, whose R-derivative rnlfor returns."""
+    fnl = rnlsm1(c0, twnl, eigr, nghtol, geq0)
+    return float(np.einsum("v,i,avi->", np.asarray(wsg), np.asarray(f), fnl ** 2))
