@@ -477,12 +477,23 @@ def run_extras(args, dev):
         scond = ctx.ortho(c, "lowdin")          # max|S - I| of the orthonormalised states
         r[prec] = {"state_applies_per_s": cl.nstate / (ms / 1e3), "ms_per_step": ms,
                    "orthonormality_after_ortho": scond}
+        if prec == "mixed":
+            # non-local forces of the same states: rnlsm2 (3 x 4096 derivative projectors) + rnlfor
+            dfnl = torch.empty((cl.nstate, 3, 8, nat), dtype=torch.float64, device=dev)
+            fion = torch.zeros((nat, 3), dtype=torch.float64, device=dev)
+
+            def forces():
+                ctx.rnlsm(c, p["twnl"], p["eigr"], p["nghtol"], fnl)
+                ctx.rnlsm2(c, p["twnl"], p["eigr"], p["nghtol"], dfnl)
+                ctx.rnlfor(cl.f, fnl, dfnl, p["wsg"], fion)
+            r[prec]["nl_forces_ms"] = _timed_loop(forces, 2, 1)
+            del dfnl, fion
         del c, c2
         ctx.close()
         torch.cuda.empty_cache()
     r["dE_Ha_per_atom_mixed_vs_fp64"] = abs(energies["mixed"] - energies["fp64"]) / nat
     r["workload"] = ("rhoofr + vpsi + rnlsm1 + fnonloc + Loewdin ortho, 512 atoms, 1024 states, 70 Ry "
-                     f"(ngw={b.ngw}), 240^3, 4096 projectors")
+                     f"(ngw={b.ngw}), 240^3, 4096 projectors; nl_forces_ms = rnlsm1 + rnlsm2 + rnlfor")
     out["projectors_512atoms_1024states_240cubed"] = r
     del cl, p, rho, fnl
     torch.cuda.empty_cache()
