@@ -368,6 +368,12 @@ int gbcp_ctx_destroy(gbcp_ctx* h) {
                           &c.en_red, &c.en_ei, &c.en_fp, &c.en_idx, &c.en_in[0], &c.en_in[1], &c.en_in[2],
                           &c.en_in[3], &c.en_in[4]};
   for (auto* s : all) gbcp::release(*s);
+  for (cudaStream_t* st : {&c.copy, &c.copy_out})
+    if (*st) {
+      cudaStreamSynchronize(*st);
+      cudaStreamDestroy(*st);
+    }
+  for (cudaEvent_t e : c.pipe_ev) cudaEventDestroy(e);
   if (c.d_info) cudaFree(c.d_info);
   gbcp::prof_fold(c);
   for (cudaEvent_t e : c.prof_pool) cudaEventDestroy(e);
@@ -482,6 +488,38 @@ int stage_in(Ctx& c, Scratch& s, const void* h, size_t bytes, void** d) {
   return 0;
 }
 
+// Host-memory calls of the band loop overlap their copies with the compute: the
+// states go up per band-loop batch on a second stream, and each batch waits only
+// for its own columns (and, for vpsi, sends its C2 columns back while the next
+// batch computes).  Ordered after earlier work on the context stream.
+int pipe_prepare(Ctx& c, int nbatch) {
+  if ((!c.copy && cudaStreamCreateWithFlags(&c.copy, cudaStreamNonBlocking) != cudaSuccess) ||
+      (!c.copy_out && cudaStreamCreateWithFlags(&c.copy_out, cudaStreamNonBlocking) != cudaSuccess)) {
+    c.err = "copy streams";
+    return GBCP_ERR_CUDA;
+  }
+  const size_t need = 2 * (size_t)nbatch + 2;
+  while (c.pipe_ev.size() < need) {
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      c.err = "pipeline events";
+      return GBCP_ERR_CUDA;
+    }
+    c.pipe_ev.push_back(e);
+  }
+  GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[0], c.stream));
+  GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.copy, c.pipe_ev[0], 0));
+  return 0;
+}
+
+// upload states [s0, s0 + ns) of a host (ld) array into the packed device array d (rows = ngw)
+int pipe_up(Ctx& c, cx<double>* d, const double* h, int ld, int s0, int ns) {
+  GBCP_CUDA_TRY(c, cudaMemcpy2DAsync(d + (size_t)s0 * c.ngw, sizeof(cx<double>) * c.ngw,
+                                     h + 2 * (size_t)s0 * ld, sizeof(cx<double>) * (size_t)ld,
+                                     sizeof(cx<double>) * c.ngw, ns, cudaMemcpyHostToDevice, c.copy));
+  return 0;
+}
+
 int finish(Ctx& c, int rc) {
   if (rc) {
     if (c.err.empty()) c.err = "error";
@@ -515,17 +553,27 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
   int dld = ldc;
   int rc = 0;
   if (mem == GBCP_MEM_HOST) {
-    cx<double>* t;
     void* tf;
-    if ((rc = stage_in_cx(c, c.st_c0, c0, ldc, c.ngw, nstate, &t))) return rc;
     if ((rc = stage_in(c, c.st_f, f, sizeof(double) * nstate, &tf))) return rc;
-    if (!gbcp::ensure(c, c.st_rho, sizeof(double) * nnr1)) return GBCP_ERR_NOMEM;
+    if (!gbcp::ensure(c, c.st_rho, sizeof(double) * nnr1) ||
+        !gbcp::ensure(c, c.st_c0, sizeof(cx<double>) * (size_t)c.ngw * std::max(nstate, 1)))
+      return GBCP_ERR_NOMEM;
+    cx<double>* t = static_cast<cx<double>*>(c.st_c0.p);
+    const int nb = ((nstate + 1) / 2 + c.batch - 1) / c.batch;
+    if ((rc = pipe_prepare(c, nb))) return rc;
+    for (int b = 0; b < nb; ++b) {
+      const int s0 = 2 * c.batch * b, ns = std::min(2 * c.batch, nstate - s0);
+      if ((rc = pipe_up(c, t, c0, ldc, s0, ns))) return rc;
+      GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[1 + b], c.copy));
+    }
+    c.batch_ready = c.pipe_ev.data() + 1;
     dc0 = t;
     df = static_cast<double*>(tf);
     drho = static_cast<double*>(c.st_rho.p);
     dld = c.ngw;
   }
   rc = gbcp::band_rhoofr(c, dc0, dld, nstate, df, drho);
+  c.batch_ready = nullptr;
   if (!rc && (ekin || csumg) && nstate > 0) rc = gbcp::kin_energy(c, dc0, dld, nstate, df, ekin, csumg);
   if (!rc && nstate == 0) {
     if (ekin) *ekin = 0.0;
@@ -560,14 +608,34 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
   int l0 = ldc, l2 = ldc2;
   int rc = 0;
   if (mem == GBCP_MEM_HOST) {
-    cx<double>* t0;
-    cx<double>* t2;
     void* tf;
     void* tv;
-    if ((rc = stage_in_cx(c, c.st_c0, c0, ldc, c.ngw, nstate, &t0))) return rc;
-    if ((rc = stage_in_cx(c, c.st_c2, c2, ldc2, c.ngw, nstate, &t2))) return rc;
     if ((rc = stage_in(c, c.st_f, f, sizeof(double) * nstate, &tf))) return rc;
     if ((rc = stage_in(c, c.st_vpot, vpot, sizeof(double) * nnr1, &tv))) return rc;
+    if (!gbcp::ensure(c, c.st_c0, sizeof(cx<double>) * (size_t)c.ngw * nstate) ||
+        !gbcp::ensure(c, c.st_c2, sizeof(cx<double>) * (size_t)c.ngw * nstate))
+      return GBCP_ERR_NOMEM;
+    cx<double>* t0 = static_cast<cx<double>*>(c.st_c0.p);
+    cx<double>* t2 = static_cast<cx<double>*>(c.st_c2.p);
+    const int nb = ((nstate + 1) / 2 + c.batch - 1) / c.batch;
+    if ((rc = pipe_prepare(c, nb))) return rc;
+    for (int b = 0; b < nb; ++b) {
+      const int s0 = 2 * c.batch * b, ns = std::min(2 * c.batch, nstate - s0);
+      if ((rc = pipe_up(c, t0, c0, ldc, s0, ns)) || (rc = pipe_up(c, t2, c2, ldc2, s0, ns))) return rc;
+      GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[1 + b], c.copy));
+    }
+    c.batch_ready = c.pipe_ev.data() + 1;
+    // C2 columns of batch b go back as soon as its decode is queued
+    c.batch_done = [&c, c2, ldc2, nstate, t2, nb](int b) -> int {
+      const int s0 = 2 * c.batch * b, ns = std::min(2 * c.batch, nstate - s0);
+      cudaEvent_t e = c.pipe_ev[1 + nb + b];
+      GBCP_CUDA_TRY(c, cudaEventRecord(e, c.stream));
+      GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.copy_out, e, 0));
+      GBCP_CUDA_TRY(c, cudaMemcpy2DAsync(c2 + 2 * (size_t)s0 * ldc2, sizeof(cx<double>) * (size_t)ldc2,
+                                         t2 + (size_t)s0 * c.ngw, sizeof(cx<double>) * c.ngw,
+                                         sizeof(cx<double>) * c.ngw, ns, cudaMemcpyDeviceToHost, c.copy_out));
+      return 0;
+    };
     dc0 = t0;
     dc2 = t2;
     df = static_cast<double*>(tf);
@@ -575,7 +643,14 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
     l0 = l2 = c.ngw;
   }
   rc = gbcp::band_vpsi(c, dc0, l0, dc2, l2, df, dv, nstate);
-  if (!rc && mem == GBCP_MEM_HOST) rc = stage_out_cx(c, dc2, c2, ldc2, c.ngw, nstate);
+  c.batch_ready = nullptr;
+  c.batch_done = nullptr;
+  if (mem == GBCP_MEM_HOST) {
+    // the context stream (and so finish) waits for the last C2 copies
+    cudaEvent_t e = c.pipe_ev[c.pipe_ev.size() - 1];
+    cudaEventRecord(e, c.copy_out);
+    cudaStreamWaitEvent(c.stream, e, 0);
+  }
   if (mem == GBCP_MEM_HOST || rc) return finish(c, rc);
   return GBCP_OK;
 }

@@ -542,9 +542,11 @@ int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f,
   for (int p0 = 0; p0 < npairs_total; p0 += c.batch) {
     const int np = std::min(c.batch, npairs_total - p0);
     const int s0 = 2 * p0;
+    if (c.batch_ready) GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.batch_ready[p0 / c.batch], 0));
     if ((rc = zinv<T>(c, c0, ldc, s0, nstate, np))) return rc;
     if ((rc = yinv<T>(c, np))) return rc;
     if ((rc = xinv_rho<T>(c, np, s0, nstate, f, rho))) return rc;
+    if (c.batch_done && (rc = c.batch_done(p0 / c.batch))) return rc;
   }
   return 0;
 }
@@ -569,12 +571,14 @@ int vpsi_t(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, cons
   for (int p0 = 0; p0 < npairs_total; p0 += c.batch) {
     const int np = std::min(c.batch, npairs_total - p0);
     const int s0 = 2 * p0;
+    if (c.batch_ready) GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.batch_ready[p0 / c.batch], 0));
     if ((rc = zinv<T>(c, c0, ldc, s0, nstate, np))) return rc;
     if ((rc = yinv<T>(c, np))) return rc;
     if ((rc = xvx<T>(c, np, vpot, vT))) return rc;
     if ((rc = yfwd<T>(c, np))) return rc;
     if ((rc = zfwd<T>(c, np))) return rc;
     if ((rc = launch_decode<T>(c, np, c0, ldc, c2, ldc2, f, s0, nstate))) return rc;
+    if (c.batch_done && (rc = c.batch_done(p0 / c.batch))) return rc;
   }
   return 0;
 }

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <unordered_map>
@@ -110,6 +111,12 @@ struct Ctx {
   const double* dg2 = nullptr;     // |G|^2 in bohr^-2
   Scratch en_rho, en_a, en_b, en_veff, en_red, en_ei, en_fp, en_idx, en_in[5];
   std::string err;
+  // host-staged pipelining (abi.cu): the band loop waits for batch_ready[b] before batch b
+  // and calls batch_done(b) once the kernels of batch b are queued
+  cudaStream_t copy = nullptr, copy_out = nullptr;  // uploads, downloads (separate copy engines)
+  std::vector<cudaEvent_t> pipe_ev;
+  const cudaEvent_t* batch_ready = nullptr;
+  std::function<int(int)> batch_done;
   // profiling
   bool prof = false;
   std::vector<ProfRec> prof_live;
