@@ -603,7 +603,7 @@ def main():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--fp64-steps", type=int, default=5)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--ref-states", type=int, default=16)

@@ -339,7 +339,7 @@ int gbcp_ctx_create(const gbcp_grid_desc* grid, int precision, int max_batch, vo
   c.omega = grid->omega;
   c.tpiba2 = grid->tpiba2;
   c.precision = precision;
-  c.batch = std::min(gbcp::kMaxBatch, max_batch > 0 ? max_batch : 8);
+  c.batch = std::min(gbcp::kMaxBatch, max_batch > 0 ? max_batch : gbcp::kMaxBatch);
   if (cudaStreamCreateWithFlags(&c.own, cudaStreamNonBlocking) != cudaSuccess) {
     delete h;
     return GBCP_ERR_CUDA;
@@ -520,6 +520,14 @@ int pipe_up(Ctx& c, cx<double>* d, const double* h, int ld, int s0, int ns) {
   return 0;
 }
 
+// pairs per staging chunk of a host-memory call: about four chunks, so that the whole
+// stage chain of one chunk overlaps the copies of the next; host-memory calls launch the
+// band loop chunk by chunk (their launch batch is the chunk)
+int stage_chunk(const Ctx& c, int nstate) {
+  const int npairs = (nstate + 1) / 2;
+  return std::max(1, std::min(c.batch, (npairs + 3) / 4));
+}
+
 int finish(Ctx& c, int rc) {
   if (rc) {
     if (c.err.empty()) c.err = "error";
@@ -551,7 +559,7 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
   const double* df = f;
   double* drho = rhoe;
   int dld = ldc;
-  int rc = 0;
+  int rc = 0, saved_batch = 0;
   if (mem == GBCP_MEM_HOST) {
     void* tf;
     if ((rc = stage_in(c, c.st_f, f, sizeof(double) * nstate, &tf))) return rc;
@@ -559,14 +567,18 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
         !gbcp::ensure(c, c.st_c0, sizeof(cx<double>) * (size_t)c.ngw * std::max(nstate, 1)))
       return GBCP_ERR_NOMEM;
     cx<double>* t = static_cast<cx<double>*>(c.st_c0.p);
-    const int nb = ((nstate + 1) / 2 + c.batch - 1) / c.batch;
+    const int sp = stage_chunk(c, nstate);
+    const int nb = ((nstate + 1) / 2 + sp - 1) / sp;
     if ((rc = pipe_prepare(c, nb))) return rc;
     for (int b = 0; b < nb; ++b) {
-      const int s0 = 2 * c.batch * b, ns = std::min(2 * c.batch, nstate - s0);
+      const int s0 = 2 * sp * b, ns = std::min(2 * sp, nstate - s0);
       if ((rc = pipe_up(c, t, c0, ldc, s0, ns))) return rc;
       GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[1 + b], c.copy));
     }
+    c.stage_pairs = sp;
     c.batch_ready = c.pipe_ev.data() + 1;
+    saved_batch = c.batch;
+    c.batch = sp;
     dc0 = t;
     df = static_cast<double*>(tf);
     drho = static_cast<double*>(c.st_rho.p);
@@ -574,6 +586,7 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
   }
   rc = gbcp::band_rhoofr(c, dc0, dld, nstate, df, drho);
   c.batch_ready = nullptr;
+  if (saved_batch) c.batch = saved_batch;
   if (!rc && (ekin || csumg) && nstate > 0) rc = gbcp::kin_energy(c, dc0, dld, nstate, df, ekin, csumg);
   if (!rc && nstate == 0) {
     if (ekin) *ekin = 0.0;
@@ -606,7 +619,7 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
   const double* df = f;
   const double* dv = vpot;
   int l0 = ldc, l2 = ldc2;
-  int rc = 0;
+  int rc = 0, saved_batch = 0;
   if (mem == GBCP_MEM_HOST) {
     void* tf;
     void* tv;
@@ -617,17 +630,21 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
       return GBCP_ERR_NOMEM;
     cx<double>* t0 = static_cast<cx<double>*>(c.st_c0.p);
     cx<double>* t2 = static_cast<cx<double>*>(c.st_c2.p);
-    const int nb = ((nstate + 1) / 2 + c.batch - 1) / c.batch;
+    const int sp = stage_chunk(c, nstate);
+    const int nb = ((nstate + 1) / 2 + sp - 1) / sp;
     if ((rc = pipe_prepare(c, nb))) return rc;
+    c.stage_pairs = sp;
     for (int b = 0; b < nb; ++b) {
-      const int s0 = 2 * c.batch * b, ns = std::min(2 * c.batch, nstate - s0);
+      const int s0 = 2 * sp * b, ns = std::min(2 * sp, nstate - s0);
       if ((rc = pipe_up(c, t0, c0, ldc, s0, ns)) || (rc = pipe_up(c, t2, c2, ldc2, s0, ns))) return rc;
       GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[1 + b], c.copy));
     }
     c.batch_ready = c.pipe_ev.data() + 1;
+    saved_batch = c.batch;
+    c.batch = sp;
     // C2 columns of batch b go back as soon as its decode is queued
-    c.batch_done = [&c, c2, ldc2, nstate, t2, nb](int b) -> int {
-      const int s0 = 2 * c.batch * b, ns = std::min(2 * c.batch, nstate - s0);
+    c.batch_done = [&c, c2, ldc2, nstate, t2, nb, sp](int b) -> int {
+      const int s0 = 2 * sp * b, ns = std::min(2 * sp, nstate - s0);
       cudaEvent_t e = c.pipe_ev[1 + nb + b];
       GBCP_CUDA_TRY(c, cudaEventRecord(e, c.stream));
       GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.copy_out, e, 0));
@@ -645,6 +662,7 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
   rc = gbcp::band_vpsi(c, dc0, l0, dc2, l2, df, dv, nstate);
   c.batch_ready = nullptr;
   c.batch_done = nullptr;
+  if (saved_batch) c.batch = saved_batch;
   if (mem == GBCP_MEM_HOST) {
     // the context stream (and so finish) waits for the last C2 copies
     cudaEvent_t e = c.pipe_ev[c.pipe_ev.size() - 1];

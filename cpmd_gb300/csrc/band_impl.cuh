@@ -379,9 +379,9 @@ template <typename T, int N> constexpr size_t fs_smem_x(int tables) {
 }
 
 template <typename T, int NC>
-int launch_zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int np) {
+int launch_zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int np, int poff) {
   const GeoDev& g = c.geo;
-  cx<T>* zb = static_cast<cx<T>*>(c.zbuf.p);
+  cx<T>* zb = static_cast<cx<T>*>(c.zbuf.p) + (size_t)poff * g.n3 * g.ncol;  // pair poff of the launch batch
   ProfScope ps_(c, "k_zinv");
   if constexpr (NC > 0) {
     constexpr size_t sm = fs_smem<T, NC>(1, 1);
@@ -512,17 +512,17 @@ template <typename T, int NC> int launch_zfwd(Ctx& c, int np) {
 
 template <typename T>
 int launch_decode(Ctx& c, int np, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, const double* f, int s0,
-                  int nstate) {
+                  int nstate, int poff = 0) {
   const GeoDev& g = c.geo;
   ProfScope ps_(c, "k_decode");
-  k_decode<T><<<dim3((g.ngw + 255) / 256, np), 256, 0, c.stream>>>(g, static_cast<const cx<T>*>(c.qbuf.p), c0, ldc,
-                                                                     c2, ldc2, f, s0, nstate, c.kin);
+  const cx<T>* qb = static_cast<const cx<T>*>(c.qbuf.p) + (size_t)poff * g.nent;  // pair poff of the launch batch
+  k_decode<T><<<dim3((g.ngw + 255) / 256, np), 256, 0, c.stream>>>(g, qb, c0, ldc, c2, ldc2, f, s0, nstate, c.kin);
   GBCP_LAUNCH_CHECK(c);
   return 0;
 }
 
-template <typename T> int zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int np) {
-  GBCP_DISPATCH(launch_zinv, T, band_len(c, c.nr[2]), c, c0, ldc, s0, nstate, np)
+template <typename T> int zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int np, int poff = 0) {
+  GBCP_DISPATCH(launch_zinv, T, band_len(c, c.nr[2]), c, c0, ldc, s0, nstate, np, poff)
 }
 template <typename T> int yinv(Ctx& c, int np) { GBCP_DISPATCH(launch_yinv, T, band_len(c, c.nr[1]), c, np) }
 template <typename T> int xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho) {
@@ -534,6 +534,20 @@ template <typename T> int xvx(Ctx& c, int np, const double* vpot, const T* vpotT
 template <typename T> int yfwd(Ctx& c, int np) { GBCP_DISPATCH(launch_yfwd, T, band_len(c, c.nr[1]), c, np) }
 template <typename T> int zfwd(Ctx& c, int np) { GBCP_DISPATCH(launch_zfwd, T, band_len(c, c.nr[2]), c, np) }
 
+// Z stage of pairs [p0, p0 + np): one launch, or, with host staging, one launch per
+// staging chunk after that chunk's columns have arrived
+template <typename T> int zinv_staged(Ctx& c, const cx<double>* c0, int ldc, int p0, int nstate, int np) {
+  if (!c.batch_ready) return zinv<T>(c, c0, ldc, 2 * p0, nstate, np);
+  const int sp = c.stage_pairs;
+  for (int q0 = p0; q0 < p0 + np; q0 += sp) {
+    const int nq = std::min(sp, p0 + np - q0);
+    GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.batch_ready[q0 / sp], 0));
+    const int rc = zinv<T>(c, c0, ldc, 2 * q0, nstate, nq, q0 - p0);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
 template <typename T>
 int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho) {
   const int npairs_total = (nstate + 1) / 2;
@@ -542,11 +556,9 @@ int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f,
   for (int p0 = 0; p0 < npairs_total; p0 += c.batch) {
     const int np = std::min(c.batch, npairs_total - p0);
     const int s0 = 2 * p0;
-    if (c.batch_ready) GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.batch_ready[p0 / c.batch], 0));
-    if ((rc = zinv<T>(c, c0, ldc, s0, nstate, np))) return rc;
+    if ((rc = zinv_staged<T>(c, c0, ldc, p0, nstate, np))) return rc;
     if ((rc = yinv<T>(c, np))) return rc;
     if ((rc = xinv_rho<T>(c, np, s0, nstate, f, rho))) return rc;
-    if (c.batch_done && (rc = c.batch_done(p0 / c.batch))) return rc;
   }
   return 0;
 }
@@ -571,14 +583,22 @@ int vpsi_t(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, cons
   for (int p0 = 0; p0 < npairs_total; p0 += c.batch) {
     const int np = std::min(c.batch, npairs_total - p0);
     const int s0 = 2 * p0;
-    if (c.batch_ready) GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.batch_ready[p0 / c.batch], 0));
-    if ((rc = zinv<T>(c, c0, ldc, s0, nstate, np))) return rc;
+    if ((rc = zinv_staged<T>(c, c0, ldc, p0, nstate, np))) return rc;
     if ((rc = yinv<T>(c, np))) return rc;
     if ((rc = xvx<T>(c, np, vpot, vT))) return rc;
     if ((rc = yfwd<T>(c, np))) return rc;
     if ((rc = zfwd<T>(c, np))) return rc;
-    if ((rc = launch_decode<T>(c, np, c0, ldc, c2, ldc2, f, s0, nstate))) return rc;
-    if (c.batch_done && (rc = c.batch_done(p0 / c.batch))) return rc;
+    if (!c.batch_ready) {
+      if ((rc = launch_decode<T>(c, np, c0, ldc, c2, ldc2, f, s0, nstate))) return rc;
+    } else {
+      // host staging: decode per staging chunk, each followed by its download
+      const int sp = c.stage_pairs;
+      for (int q0 = p0; q0 < p0 + np; q0 += sp) {
+        const int nq = std::min(sp, p0 + np - q0);
+        if ((rc = launch_decode<T>(c, nq, c0, ldc, c2, ldc2, f, 2 * q0, nstate, q0 - p0))) return rc;
+        if (c.batch_done && (rc = c.batch_done(q0 / sp))) return rc;
+      }
+    }
   }
   return 0;
 }

@@ -111,12 +111,13 @@ struct Ctx {
   const double* dg2 = nullptr;     // |G|^2 in bohr^-2
   Scratch en_rho, en_a, en_b, en_veff, en_red, en_ei, en_fp, en_idx, en_in[5];
   std::string err;
-  // host-staged pipelining (abi.cu): the band loop waits for batch_ready[b] before batch b
-  // and calls batch_done(b) once the kernels of batch b are queued
+  // host-staged pipelining (abi.cu): the Z stage of staging chunk q waits for batch_ready[q];
+  // vpsi calls batch_done(q) once the decode of chunk q is queued
   cudaStream_t copy = nullptr, copy_out = nullptr;  // uploads, downloads (separate copy engines)
   std::vector<cudaEvent_t> pipe_ev;
   const cudaEvent_t* batch_ready = nullptr;
   std::function<int(int)> batch_done;
+  int stage_pairs = 0;  // state pairs per staging chunk (a chunk never spans two launch batches)
   // profiling
   bool prof = false;
   std::vector<ProfRec> prof_live;
