@@ -96,7 +96,7 @@ struct Ctx {
   Scratch zbuf, ybuf, qbuf;
   Scratch st_c0, st_c2, st_rho, st_vpot, st_f, st_misc, st_misc2, st_vf;
   Scratch red, red2;  // reductions
-  Scratch smat, smat2, smat3, sparts, cscr, cdiag;
+  Scratch smat, smat2, smat3, sparts, cscr, cdiag, cwork;
   Scratch oz_a, oz_b;  // bf16 digit planes of the split-precision ortho GEMMs
   Scratch nl_a, nl_b, nl_c, nl_d;
   Scratch nl_ta, nl_tb, nl_tp;  // projector GEMM slices (A, B) and split-K partials
