@@ -195,35 +195,93 @@ __device__ __forceinline__ void xline_step_a(const GeoDev& g, const cx<T>* __res
 }
 
 // ---------------------------------------------------------------- X stage + density
+// asynchronous global -> shared copy of one complex (LDGSTS; completes without a wait loop)
+template <typename T> __device__ __forceinline__ void cp_async_cx(cx<T>* dst, const cx<T>* src) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  if constexpr (sizeof(cx<T>) == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int NPEND> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(NPEND) : "memory");
+}
+
+// slab buffers of the density x-stage: two (copy of the next pair overlaps the
+// current one) in FP32, one in FP64 (shared memory)
+template <typename T> __host__ __device__ constexpr int xrho_bufs() { return sizeof(T) == 4 ? 2 : 1; }
+
+// CTA (chunk, y-block, z): the x-lines y0 .. y0+L-1 of plane z for the pairs
+// [chunk*pchunk, ..).  Each pair's slots of those lines are one contiguous run of
+// ybuf (L rows of nslot), copied to shared memory with cp.async one pair ahead.
+// The CTA's density contribution sum_pairs f1 |Re psi|^2 + f2 |Im psi|^2 builds
+// up in registers (T).  With one chunk it is added to rho directly; with
+// several, each CTA stores its partial tile, and the last CTA of the tile to
+// finish (ticket counter) adds the partials in chunk order: the result does not
+// depend on the order the CTAs run in.
 template <typename T, int N>
 __global__ void __launch_bounds__(kThreads) k_xrho_fs(GeoDev g, const cx<T>* __restrict__ ybuf, int npairs, int s0,
                                                      int nstate, const double* __restrict__ f, double inv_omega,
-                                                     double* __restrict__ rho, const cx<T>* __restrict__ twAg) {
+                                                     double* __restrict__ rho, const cx<T>* __restrict__ twAg,
+                                                     int pchunk, T* __restrict__ part, unsigned* __restrict__ tickets) {
   using P = FS<T, N>;
+  constexpr int NBUF = xrho_bufs<T>();
   static_assert(P::IB == 1, "density tile: one step-B task per thread");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* twA = reinterpret_cast<cx<T>*>(smem_raw);
   cx<T>* Ts = twA + N;
-  const int y0 = blockIdx.x * P::L, z = blockIdx.y;
+  cx<T>* slab = Ts + P::L * P::XS;
+  const int nslot = g.nslot, slab_n = P::L * nslot;
+  const int nchunk = gridDim.x, chunk = blockIdx.x, y0 = blockIdx.y * P::L, z = blockIdx.z;
+  const int p0 = chunk * pchunk, p1 = min(npairs, p0 + pchunk);
+  const int nel = min(P::L, g.n2 - y0) * nslot;
   load_table(twA, twAg, N);
-  // this launch's pairs accumulate in T (FP32 in the mixed mode), added to the FP64 density once
   T acc[P::N2];
 #pragma unroll
   for (int k2 = 0; k2 < P::N2; ++k2) acc[k2] = (T)0;
-  // occupation weights f/omega of the launch's pairs, once per CTA (FP64 -> T)
   __shared__ T fw[2 * kMaxBatch];
-  for (int i = threadIdx.x; i < 2 * npairs; i += kThreads) {
-    const int is = s0 + i;
+  __shared__ int last_sh;
+  for (int i = threadIdx.x; i < 2 * (p1 - p0); i += kThreads) {
+    const int is = s0 + 2 * p0 + i;
     fw[i] = from_double<T>(is < nstate ? f[is] * inv_omega : 0.0);
   }
+  auto issue = [&](int pair, int buf) {
+    const cx<T>* src = ybuf + (((size_t)pair * g.n3 + z) * g.n2 + y0) * (size_t)nslot;
+    cx<T>* dst = slab + buf * slab_n;
+    for (int e = threadIdx.x; e < nel; e += kThreads) cp_async_cx(dst + e, src + e);
+    cp_async_commit();
+  };
   const int t = threadIdx.x;
   const int lb = t / P::N1, k1 = t - lb * P::N1;
-  for (int pair = 0; pair < npairs; ++pair) {
-    const cx<T>* yb = ybuf + ((size_t)pair * g.n3 + z) * (size_t)g.n2 * g.nslot;
-    __syncthreads();  // twiddles and weights loaded / previous pair's step B done
-    const T f1 = fw[2 * pair], f2 = fw[2 * pair + 1];
-    xline_step_a<T, N>(g, yb, y0, twA, Ts);
+  if (p0 < p1) issue(p0, 0);
+  for (int pair = p0; pair < p1; ++pair) {
+    const int buf = (NBUF == 2) ? ((pair - p0) & 1) : 0;
+    if (NBUF == 2 && pair + 1 < p1) {
+      issue(pair + 1, buf ^ 1);  // buffer buf^1 was last read before the previous mid-pair barrier
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();  // slab of this pair in shared memory; previous step B done with Ts
+    const cx<T>* sl = slab + buf * slab_n;
+#pragma unroll
+    for (int ia = 0; ia < P::IA; ++ia) {
+      const int ta = threadIdx.x + ia * kThreads;
+      if (ta < P::TA) {
+        const int l = ta / P::N2, n2 = ta - l * P::N2, y = y0 + l;
+        cx<T> v[P::N1];
+#pragma unroll
+        for (int n1 = 0; n1 < P::N1; ++n1) {
+          const int s = freq_of(n2 + P::N2 * n1, N) - g.gxlo;
+          v[n1] = (y < g.n2 && s >= 0 && s < nslot) ? sl[l * nslot + s] : mk<T>(0, 0);
+        }
+        fs_step_a<1, T, P::N1, P::N2, P::XP>(v, n2, twA, Ts + l * P::XS);
+      }
+    }
     __syncthreads();
+    if (NBUF == 1 && pair + 1 < p1) issue(pair + 1, 0);  // slab read by every thread; overlaps step B
+    const T f1 = fw[2 * (pair - p0)], f2 = fw[2 * (pair - p0) + 1];
     if (t < P::TB) {
       cx<T> w[P::N2];
       fs_step_b<1, T, P::N1, P::N2, P::XP>(Ts + lb * P::XS, k1, w);
@@ -232,11 +290,36 @@ __global__ void __launch_bounds__(kThreads) k_xrho_fs(GeoDev g, const cx<T>* __r
     }
   }
   const int y = y0 + lb;
-  if (t < P::TB && y < g.n2) {
-    double* rrow = rho + (size_t)g.k1 * (y + (size_t)g.k2 * z);
+  double* rrow = rho + (size_t)g.k1 * ((y < g.n2 ? y : 0) + (size_t)g.k2 * z);
+  if (nchunk == 1) {
+    if (t < P::TB && y < g.n2) {
 #pragma unroll
-    for (int k2 = 0; k2 < P::N2; ++k2) rrow[k1 + P::N1 * k2] += to_double<T>(acc[k2]);
+      for (int k2 = 0; k2 < P::N2; ++k2) rrow[k1 + P::N1 * k2] += to_double<T>(acc[k2]);
+    }
+    return;
   }
+  const int tile = blockIdx.z * gridDim.y + blockIdx.y;
+  T* mine = part + ((size_t)tile * nchunk + chunk) * (P::TB * P::N2);
+  if (t < P::TB) {
+#pragma unroll
+    for (int k2 = 0; k2 < P::N2; ++k2) mine[k2 * P::TB + t] = acc[k2];
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last_sh = (atomicAdd(&tickets[tile], 1u) == (unsigned)(nchunk - 1));
+  __syncthreads();
+  if (!last_sh) return;
+  __threadfence();
+  if (t < P::TB && y < g.n2) {
+    const T* tp = part + (size_t)tile * nchunk * (P::TB * P::N2);
+#pragma unroll
+    for (int k2 = 0; k2 < P::N2; ++k2) {
+      double sum = 0.0;
+      for (int q = 0; q < nchunk; ++q) sum += to_double<T>(__ldcg(tp + (size_t)q * (P::TB * P::N2) + k2 * P::TB + t));
+      rrow[k1 + P::N1 * k2] += sum;
+    }
+  }
+  if (threadIdx.x == 0) tickets[tile] = 0u;  // ready for the next launch
 }
 
 // ---------------------------------------------------------------- X stage: inverse, x V, forward

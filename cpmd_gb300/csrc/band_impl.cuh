@@ -420,16 +420,57 @@ template <typename T, int NC> int launch_yinv(Ctx& c, int np) {
   return 0;
 }
 
+// Pair chunks of the density x-stage: the count that minimises the busiest
+// SM's work, ceil(tiles * P / SMs) CTAs of ceil(np / P) + 1 pair-times each (the
+// +1 is the copy of the first pair and the partial-tile combine).
+constexpr int kXrhoMaxChunks = 8;
+inline int xrho_chunks(const Ctx& c, int tiles, int np) {
+  if (c.xr_chunks > 0) return std::max(1, std::min({c.xr_chunks, np, kXrhoMaxChunks}));
+  const long long nsm = c.nsm > 0 ? c.nsm : 152;
+  int best = 1;
+  long long best_cost = -1;
+  for (int p = 1; p <= std::min(np, kXrhoMaxChunks); ++p) {
+    const long long per_sm = ((long long)tiles * p + nsm - 1) / nsm;
+    const long long cost = per_sm * ((np + p - 1) / p + 1);
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best = p;
+    }
+  }
+  return best;
+}
+
 template <typename T, int NC>
 int launch_xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho) {
   const GeoDev& g = c.geo;
   const cx<T>* yb = static_cast<const cx<T>*>(c.ybuf.p);
   if constexpr (NC > 0) {
-    constexpr size_t sm = fs_smem_x<T, NC>(1);
+    using P = FS<T, NC>;
+    const int tiles_y = (g.n2 + P::L - 1) / P::L, tiles = tiles_y * g.n3;
+    const int pchunk = (np + xrho_chunks(c, tiles, np) - 1) / xrho_chunks(c, tiles, np);
+    const int nchunk = (np + pchunk - 1) / pchunk;
+    const size_t sm = fs_smem_x<T, NC>(1) + sizeof(cx<T>) * (size_t)xrho_bufs<T>() * P::L * g.nslot;
+    if (sm > (size_t)227 * 1024) {
+      c.err = "density x-stage: shared-memory tile too large for this sphere";
+      return 7;
+    }
+    T* part = nullptr;
+    unsigned* tickets = nullptr;
+    if (nchunk > 1) {
+      // sized for the largest chunk count once, so that later launches never reallocate
+      if (!ensure(c, c.xr_part, sizeof(T) * (size_t)tiles * kXrhoMaxChunks * P::TB * P::N2)) return 6;
+      const size_t tb = sizeof(unsigned) * (size_t)tiles;
+      if (!c.xr_tk.p || c.xr_tk.cap < tb) {
+        if (!ensure(c, c.xr_tk, tb)) return 6;
+        GBCP_CUDA_TRY(c, cudaMemsetAsync(c.xr_tk.p, 0, c.xr_tk.cap, c.stream));
+      }
+      part = static_cast<T*>(c.xr_part.p);
+      tickets = static_cast<unsigned*>(c.xr_tk.p);
+    }
     allow_smem(k_xrho_fs<T, NC>, sm);
     ProfScope ps_(c, "k_xinv_rho");
-    k_xrho_fs<T, NC><<<dim3((g.n2 + FS<T, NC>::L - 1) / FS<T, NC>::L, g.n3), kThreads, sm, c.stream>>>(
-        g, yb, np, s0, nstate, f, 1.0 / c.omega, rho, twA_of<T>(c, 0));
+    k_xrho_fs<T, NC><<<dim3(nchunk, tiles_y, g.n3), kThreads, sm, c.stream>>>(
+        g, yb, np, s0, nstate, f, 1.0 / c.omega, rho, twA_of<T>(c, 0), pchunk, part, tickets);
   } else {
     int nl = lines_rt(g.n1);
     while (nl > 1 && nl * g.n1 > kMaxAcc * kThreads) --nl;

@@ -75,6 +75,8 @@ struct Ctx {
   int precision;
   int batch;           // pairs per batch
   int gemm_mode = -1;  // overlap GEMM: -1 by precision (mixed -> tensor cores), 0 FP64 SIMT, 1 tensor cores
+  int nsm = 0;         // SMs of the device
+  int xr_chunks = 0;   // density x-stage pair chunks: 0 = chosen per launch
   int fft_engine = 0;  // band-loop FFTs: 0 four-step where a plan exists, else Stockham; 2 Stockham always
   cudaStream_t stream = nullptr;  // stream all work is queued on
   cudaStream_t own = nullptr;     // the context's own stream
@@ -97,6 +99,7 @@ struct Ctx {
   Scratch st_c0, st_c2, st_rho, st_vpot, st_f, st_misc, st_misc2, st_vf;
   Scratch red, red2;  // reductions
   Scratch smat, smat2, smat3, sparts, cscr, cdiag, cwork;
+  Scratch xr_part, xr_tk;  // density x-stage: partial tiles and ticket counters of the pair chunks
   Scratch oz_a, oz_b;  // bf16 digit planes of the split-precision ortho GEMMs
   Scratch nl_a, nl_b, nl_c, nl_d;
   Scratch nl_ta, nl_tb, nl_tp;  // projector GEMM slices (A, B) and split-K partials

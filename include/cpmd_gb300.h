@@ -87,8 +87,10 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  *                   (FP64-accurate);
  *   GBCP_OPT_BATCH  state pairs per band-loop launch (1..64);
  *   GBCP_OPT_FFT    band-loop FFT kernels: 0 = four-step register codelets
- *                   where the mesh has a plan, else Stockham; 2 = Stockham. */
-enum gbcp_option { GBCP_OPT_GEMM = 1, GBCP_OPT_BATCH = 2, GBCP_OPT_FFT = 3 };
+ *                   where the mesh has a plan, else Stockham; 2 = Stockham;
+ *   GBCP_OPT_XCHUNKS pair chunks of the density x-stage (four-step kernels):
+ *                   0 = chosen per launch from the SM count, 1..8 = fixed. */
+enum gbcp_option { GBCP_OPT_GEMM = 1, GBCP_OPT_BATCH = 2, GBCP_OPT_FFT = 3, GBCP_OPT_XCHUNKS = 4 };
 int gbcp_set_option(gbcp_ctx* ctx, int key, int value);
 /* Queue later work on `stream` (a cudaStream_t; NULL = the context's own
  * stream; the CUDA legacy default stream is cudaStreamLegacy).  Device-pointer calls are ordered only with respect to this stream,

@@ -95,6 +95,21 @@ def test_rhoofr_leading_dimension(gpu_lib):
     assert np.array_equal(rho1, rho2)
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL64), ("mixed", TOL32)])
+def test_rhoofr_pair_chunks_deterministic(gpu_lib, c0cell, c0ref, precision, tol):
+    """The density x-stage splits a launch's pairs into chunks whose partial tiles
+    the last CTA of each tile adds in chunk order: every chunk count matches the
+    oracle, and repeated calls are bit-identical."""
+    b = c0cell.basis
+    for chunks in (1, 3, 8, 0):
+        ctx = ctx_for(b, precision=precision)
+        ctx.set_option("xchunks", chunks)
+        rho1, *_ = ctx.rhoofr(c0cell.c0, c0cell.f)
+        rho2, *_ = ctx.rhoofr(c0cell.c0, c0cell.f)
+        assert np.array_equal(rho1, rho2), chunks
+        assert rel(rho1, c0ref["rho"]) < tol, chunks
+
+
 def test_rhoofr_zero_states(gpu_lib, c0cell):
     ctx = ctx_for(c0cell.basis)
     rho, ekin, csumg, csumr = ctx.rhoofr(np.zeros((c0cell.basis.ngw, 0), complex, order="F"), np.zeros(0))
