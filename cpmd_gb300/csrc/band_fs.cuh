@@ -88,10 +88,9 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
       }
 #pragma unroll
       for (int n1 = 0; n1 < P::N1; ++n1) {
-        const int z = n2 + P::N2 * n1;
-        const int off = freq_of(z, N) - zlo;
+        const int off = freq_split<N, P::N2>(n2, n1) - zlo;
         cx<T> val = mk<T>(0, 0);
-        if (off >= 0 && off < len) {
+        if (in_range(off, len)) {
           const int e = g.col_ent[st + off];
           if (e != 0) {
             const int ig = (e > 0 ? e : -e) - 1;
@@ -150,8 +149,8 @@ __global__ void __launch_bounds__(kThreads) k_yinv_fs(GeoDev g, const cx<T>* __r
       cx<T> v[P::N1];
 #pragma unroll
       for (int n1 = 0; n1 < P::N1; ++n1) {
-        const int off = freq_of(n2 + P::N2 * n1, N) - gylo;
-        v[n1] = (off >= 0 && off < ncs) ? zrow[c0s + off] : mk<T>(0, 0);
+        const int off = freq_split<N, P::N2>(n2, n1) - gylo;
+        v[n1] = in_range(off, ncs) ? zrow[c0s + off] : mk<T>(0, 0);
       }
       fs_step_a<1, T, P::N1, P::N2>(v, n2, twA, Ts + l * P::LS);
     }
@@ -186,8 +185,8 @@ __device__ __forceinline__ void xline_step_a(const GeoDev& g, const cx<T>* __res
       cx<T> v[P::N1];
 #pragma unroll
       for (int n1 = 0; n1 < P::N1; ++n1) {
-        const int s = freq_of(n2 + P::N2 * n1, N) - g.gxlo;
-        v[n1] = (y < g.n2 && s >= 0 && s < g.nslot) ? yb[(size_t)y * g.nslot + s] : mk<T>(0, 0);
+        const int s = freq_split<N, P::N2>(n2, n1) - g.gxlo;
+        v[n1] = (y < g.n2 && in_range(s, g.nslot)) ? yb[(size_t)y * g.nslot + s] : mk<T>(0, 0);
       }
       fs_step_a<1, T, P::N1, P::N2, P::XP>(v, n2, twA, Ts + l * P::XS);
     }
@@ -273,8 +272,8 @@ __global__ void __launch_bounds__(kThreads) k_xrho_fs(GeoDev g, const cx<T>* __r
         cx<T> v[P::N1];
 #pragma unroll
         for (int n1 = 0; n1 < P::N1; ++n1) {
-          const int s = freq_of(n2 + P::N2 * n1, N) - g.gxlo;
-          v[n1] = (y < g.n2 && s >= 0 && s < nslot) ? sl[l * nslot + s] : mk<T>(0, 0);
+          const int s = freq_split<N, P::N2>(n2, n1) - g.gxlo;
+          v[n1] = (y < g.n2 && in_range(s, nslot)) ? sl[l * nslot + s] : mk<T>(0, 0);
         }
         fs_step_a<1, T, P::N1, P::N2, P::XP>(v, n2, twA, Ts + l * P::XS);
       }
@@ -374,8 +373,8 @@ __global__ void __launch_bounds__(kThreads) k_xvx_fs(GeoDev g, cx<T>* __restrict
       if (y < g.n2) {
 #pragma unroll
         for (int j2 = 0; j2 < P::N1; ++j2) {
-          const int s = freq_of(j + P::N2 * j2, N) - g.gxlo;
-          if (s >= 0 && s < g.nslot) yb[(size_t)y * g.nslot + s] = u[j2];
+          const int s = freq_split<N, P::N2>(j, j2) - g.gxlo;
+          if (in_range(s, g.nslot)) yb[(size_t)y * g.nslot + s] = u[j2];
         }
       }
     }
@@ -419,8 +418,8 @@ __global__ void __launch_bounds__(kThreads) k_yfwd_fs(GeoDev g, const cx<T>* __r
         const int c0s = g.slot_col0[s], gylo = g.slot_gylo[s], ncs = g.slot_ncol[s];
 #pragma unroll
         for (int k2 = 0; k2 < P::N2; ++k2) {
-          const int off = freq_of(k1 + P::N1 * k2, N) - gylo;
-          if (off >= 0 && off < ncs) zrow[c0s + off] = w[k2];
+          const int off = freq_split<N, P::N1>(k1, k2) - gylo;
+          if (in_range(off, ncs)) zrow[c0s + off] = w[k2];
         }
       }
     }
@@ -464,8 +463,8 @@ __global__ void __launch_bounds__(kThreads) k_zfwd_fs(GeoDev g, const cx<T>* __r
         const int st = g.col_start[col], len = g.col_start[col + 1] - st, zlo = g.col_zlo[col];
 #pragma unroll
         for (int k2 = 0; k2 < P::N2; ++k2) {
-          const int off = freq_of(k1 + P::N1 * k2, N) - zlo;
-          if (off >= 0 && off < len) qb[st + off] = scl(w[k2], scale);
+          const int off = freq_split<N, P::N1>(k1, k2) - zlo;
+          if (in_range(off, len)) qb[st + off] = scl(w[k2], scale);
         }
       }
     }

@@ -40,6 +40,18 @@ constexpr int kMaxAcc = 16;    // density accumulators per thread (run-time plan
 
 __host__ __device__ constexpr int line_stride(int n) { return (n % 2 == 0) ? n + 1 : n; }
 __device__ __forceinline__ int freq_of(int i, int n) { return (i < (n + 1) / 2) ? i : i - n; }
+// frequency of index a + W b of a length-N transform, 0 <= a < W, b an unrolled
+// loop index: the branch folds at compile time except for the one row of W that
+// holds the Nyquist boundary
+template <int N, int W> __device__ __forceinline__ int freq_split(int a, int b) {
+  constexpr int h = (N + 1) / 2;
+  const int i = a + W * b;
+  if (W * b + W - 1 < h) return i;
+  if (W * b >= h) return i - N;
+  return i < h ? i : i - N;
+}
+// 0 <= v < n in one unsigned compare
+__device__ __forceinline__ bool in_range(int v, int n) { return (unsigned)v < (unsigned)n; }
 __device__ __forceinline__ int idx_of(int g, int n) { return g < 0 ? g + n : g; }
 
 template <typename T>

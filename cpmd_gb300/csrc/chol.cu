@@ -16,8 +16,8 @@
 //     update  A_ij -= U_ki^T U_kj for k < i <= j                  -> S
 //   then V_ik = X_ii U_ik for every i < k (into S, no longer needed), and X
 //   block-diagonal by block-diagonal: X_ij = -sum_{k=i+1..j} V_ik X_kj, j - i = 1, 2, ...
-// Every kernel first reads the ortho status word and does nothing once a step
-// has failed; diag sets it to (global pivot index + 1) at a pivot at or below
+// Every kernel reads the ortho status word before it writes and writes nothing
+// once a step has failed; diag sets it to (global pivot index + 1) at a pivot at or below
 // 2^-46 of that row's original diagonal (an exactly dependent set of states,
 // where dpotrf's info > 0 would depend on rounding) and to -1 at a NaN.  S is
 // row-major n x n (symmetric, upper part used; scratch on return); X is row-major
@@ -65,20 +65,23 @@ __global__ void __launch_bounds__(4 * B) k_chol_diag(const double* __restrict__ 
   __shared__ double z[B][B + 1];
   __shared__ double udiag[B];
   __shared__ int bad_sh;
-  if (failed(status)) return;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int base = k * B;
-  for (int e = threadIdx.x; e < B * B; e += 4 * B) {
-    const int r = e / B, cc = e - r * B, i = base + r, j = base + cc;
-    double v = 0.0;
-    if (cc >= r) v = (i < n && j < n) ? S[(size_t)i * n + j] : (r == cc ? 1.0 : 0.0);
-    z[r][cc] = v;
+  // all global loads in flight together (rows r = w + 4 t, lane = column)
+  double v[B / 4];
+#pragma unroll
+  for (int t = 0; t < B / 4; ++t) {
+    const int r = w + 4 * t, i = base + r, j = base + lane;
+    v[t] = (lane >= r && i < n && j < n) ? S[(size_t)i * n + j] : 0.0;
   }
-  double thr = 0.0;  // warp 0, lane r: pivot threshold of row r
-  if (w == 0) {
-    const int i = base + lane;
-    thr = 0x1p-46 * ((i < n) ? diag0[i] : 1.0);
+  const double d0 = (w == 0 && base + lane < n) ? diag0[base + lane] : 1.0;
+  if (failed(status)) return;
+#pragma unroll
+  for (int t = 0; t < B / 4; ++t) {
+    const int r = w + 4 * t, i = base + r, j = base + lane;
+    z[r][lane] = (i < n && j < n) ? v[t] : (r == lane ? 1.0 : 0.0);
   }
+  const double thr = 0x1p-46 * d0;  // warp 0, lane r: pivot threshold of row r
   if (threadIdx.x == 0) bad_sh = 0;
   __syncthreads();
   for (int q = 0; q < B; ++q) {
@@ -97,9 +100,22 @@ __global__ void __launch_bounds__(4 * B) k_chol_diag(const double* __restrict__ 
         if (lane == q) udiag[q] = o;
       }
     } else if (q > 0) {
-      for (int i = q + w; i < B; i += 3) {  // rows q+1 .. 31
-        const double coef = z[q - 1][i];
-        if (lane >= i || lane < q) z[i][lane] = fma(-coef, z[q - 1][lane], z[i][lane]);
+      // rows i = q + w + 3 t (q+1 .. 31, at most 10 per warp): loads first, then the FMAs
+      constexpr int T = (B - 2 + 2) / 3;
+      const double rv = z[q - 1][lane];
+      double cf[T], zv[T];
+#pragma unroll
+      for (int t = 0; t < T; ++t) {
+        const int i = q + w + 3 * t;
+        if (i < B) {
+          cf[t] = z[q - 1][i];
+          zv[t] = z[i][lane];
+        }
+      }
+#pragma unroll
+      for (int t = 0; t < T; ++t) {
+        const int i = q + w + 3 * t;
+        if (i < B && (lane >= i || lane < q)) z[i][lane] = fma(-cf[t], rv, zv[t]);
       }
     }
     __syncthreads();
@@ -118,13 +134,23 @@ __global__ void __launch_bounds__(4 * B) k_chol_diag(const double* __restrict__ 
   }
 }
 
-// rows [r0, r0 + nrow) of block (bi, bj) of a row-major n x n matrix, into s[m][c]
-// (m = row - r0); out of range -> 0
-__device__ __forceinline__ void load_rows(const double* __restrict__ M, int n, int bi, int bj, int r0, int nrow,
-                                          double (*s)[B + 1]) {
-  for (int e = threadIdx.x; e < nrow * B; e += RG * B) {
-    const int m = e / B, cc = e - m * B, i = bi * B + r0 + m, j = bj * B + cc;
-    s[m][cc] = (i < n && j < n) ? M[(size_t)i * n + j] : 0.0;
+// rows [r0, r0 + NROW) of block (bi, bj) of a row-major n x n matrix, into s[m][c]
+// (m = row - r0); rows m >= nvalid and out-of-range entries -> 0.  All loads of a
+// thread are issued before its shared-memory stores.
+template <int NROW>
+__device__ __forceinline__ void load_rows(const double* __restrict__ M, int n, int bi, int bj, int r0,
+                                          double (*s)[B + 1], int nvalid = NROW) {
+  constexpr int PER = (NROW * B + RG * B - 1) / (RG * B);
+  double v[PER];
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int e = threadIdx.x + p * RG * B, m = e / B, cc = e - m * B, i = bi * B + r0 + m, j = bj * B + cc;
+    v[p] = (e < NROW * B && m < nvalid && i < n && j < n) ? M[(size_t)i * n + j] : 0.0;
+  }
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int e = threadIdx.x + p * RG * B, m = e / B, cc = e - m * B;
+    if (e < NROW * B) s[m][cc] = v[p];
   }
 }
 
@@ -143,15 +169,15 @@ __global__ void __launch_bounds__(RG * B) k_chol_panel(const double* __restrict_
                                                        const int* __restrict__ status) {
   __shared__ double a[B][B + 1];
   __shared__ double xt[RG][B + 1];
-  if (failed(status)) return;
   const int j = k + 1 + blockIdx.x, r0 = blockIdx.y * RG;
-  load_rows(S, n, k, j, 0, r0 + RG, a);
+  load_rows<B>(S, n, k, j, 0, a, r0 + RG);
   load_cols_t(X, n, k, k, r0, xt);
   __syncthreads();
   const int rl = threadIdx.x / B, c = threadIdx.x % B, r = r0 + rl;
   double s = 0.0;
   for (int m = 0; m <= r; ++m) s = fma(xt[rl][m], a[m][c], s);
   const int i = k * B + r, jj = j * B + c;
+  if (failed(status)) return;  // read late: its latency overlaps the loads
   if (i < n && jj < n) Uw[(size_t)i * n + jj] = s;
 }
 
@@ -161,7 +187,6 @@ __global__ void __launch_bounds__(RG * B) k_chol_update(double* __restrict__ S, 
                                                         int nb, int k, const int* __restrict__ status) {
   __shared__ double uj[B][B + 1];
   __shared__ double ui[RG][B + 1];
-  if (failed(status)) return;
   const int m0 = nb - k - 1;  // trailing block count
   int t = blockIdx.x, ii = 0;
   while (ii < m0 && t >= m0 - ii) {
@@ -169,7 +194,7 @@ __global__ void __launch_bounds__(RG * B) k_chol_update(double* __restrict__ S, 
     ++ii;
   }
   const int bi = k + 1 + ii, bj = bi + t, r0 = blockIdx.y * RG;
-  load_rows(Uw, n, k, bj, 0, B, uj);
+  load_rows<B>(Uw, n, k, bj, 0, uj);
   load_cols_t(Uw, n, k, bi, r0, ui);
   __syncthreads();
   const int rl = threadIdx.x / B, c = threadIdx.x % B, r = r0 + rl;
@@ -177,6 +202,7 @@ __global__ void __launch_bounds__(RG * B) k_chol_update(double* __restrict__ S, 
 #pragma unroll 8
   for (int m = 0; m < B; ++m) s = fma(ui[rl][m], uj[m][c], s);
   const int i = bi * B + r, jj = bj * B + c;
+  if (failed(status)) return;
   if (i < n && jj < n && (bi < bj || c >= r)) S[(size_t)i * n + jj] -= s;
 }
 
@@ -187,20 +213,20 @@ __global__ void __launch_bounds__(RG * B) k_trtri_v(double* __restrict__ S, cons
                                                     const int* __restrict__ status) {
   __shared__ double u[B][B + 1];
   __shared__ double xi[RG][B + 1];
-  if (failed(status)) return;
   int t = blockIdx.x, bi = 0;
   while (bi < nb - 1 && t >= nb - 1 - bi) {
     t -= nb - 1 - bi;
     ++bi;
   }
   const int bk = bi + 1 + t, r0 = blockIdx.y * RG;
-  load_rows(Uw, n, bi, bk, 0, B, u);
-  load_rows(X, n, bi, bi, r0, RG, xi);
+  load_rows<B>(Uw, n, bi, bk, 0, u);
+  load_rows<RG>(X, n, bi, bi, r0, xi);
   __syncthreads();
   const int rl = threadIdx.x / B, c = threadIdx.x % B, r = r0 + rl;
   double s = 0.0;
   for (int m = r; m < B; ++m) s = fma(xi[rl][m], u[m][c], s);
   const int i = bi * B + r, jj = bk * B + c;
+  if (failed(status)) return;
   if (i < n && jj < n) S[(size_t)i * n + jj] = s;
 }
 
@@ -210,19 +236,19 @@ __global__ void __launch_bounds__(RG * B) k_trtri_diag(const double* __restrict_
                                                        int d, const int* __restrict__ status) {
   __shared__ double xk[B][B + 1];
   __shared__ double v[RG][B + 1];
-  if (failed(status)) return;
   const int bi = blockIdx.x, bj = bi + d, r0 = blockIdx.y * RG;
   const int rl = threadIdx.x / B, c = threadIdx.x % B, r = r0 + rl;
   double acc = 0.0;
   for (int bk = bi + 1; bk <= bj; ++bk) {
-    load_rows(X, n, bk, bj, 0, B, xk);
-    load_rows(S, n, bi, bk, r0, RG, v);
+    load_rows<B>(X, n, bk, bj, 0, xk);
+    load_rows<RG>(S, n, bi, bk, r0, v);
     __syncthreads();
 #pragma unroll 8
     for (int m = 0; m < B; ++m) acc = fma(v[rl][m], xk[m][c], acc);
     __syncthreads();
   }
   const int i = bi * B + r, jj = bj * B + c;
+  if (failed(status)) return;
   if (i < n && jj < n) X[(size_t)i * n + jj] = -acc;
 }
 

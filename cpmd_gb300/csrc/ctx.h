@@ -174,8 +174,10 @@ int rho_sum(Ctx& c, const double* rho, double* sum);
 int ovlap_gamma(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S);
 int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, unsigned long long* scond_bits,
              int* status);
+// Cout may be A itself: A is sliced into digit planes before the GEMM reads them.
+// zero_row1: row 1 of the result (Im c(G=0) of the real view) is written as 0.
 int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout, int ldo,
-            int* status);
+            int zero_row1, int* status);
 // mesh length as seen by the band-loop dispatch (-1 forces the Stockham kernels)
 inline int band_len(const Ctx& c, int n) { return c.fft_engine == 2 ? -1 : n; }
 inline bool use_tc_gemm(const Ctx& c) { return c.gemm_mode == 1 || (c.gemm_mode < 0 && c.precision == 1); }

@@ -346,12 +346,15 @@ int ovlap_gamma(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S) {
 static int apply_right(Ctx& c, cx<double>* c0, int ldc, int nstate, const double* M, int upper) {
   const int rows = 2 * c.ngw;
   const int lda = 2 * ldc;
+  if (use_tc_gemm(c)) {
+    // in place: the split GEMM reads the digit planes of C, sliced before it starts, and
+    // writes nothing once the status word reports a failed step
+    return rmul_tc(c, reinterpret_cast<const double*>(c0), lda, rows, nstate, M, upper,
+                   reinterpret_cast<double*>(c0), lda, c.geq0, c.d_info);
+  }
   if (!ensure(c, c.cscr, sizeof(double) * (size_t)rows * nstate)) return 6;
   double* tmp = static_cast<double*>(c.cscr.p);
-  if (use_tc_gemm(c)) {
-    const int rc = rmul_tc(c, reinterpret_cast<const double*>(c0), lda, rows, nstate, M, upper, tmp, rows, c.d_info);
-    if (rc) return rc;
-  } else {
+  {
     dim3 grid((rows + TS - 1) / TS, (nstate + TS - 1) / TS);
     ProfScope ps_(c, "k_gemm_right");
     k_gemm_right<<<grid, NT, 0, c.stream>>>(reinterpret_cast<const double*>(c0), lda, rows, nstate, M, upper, tmp, rows,

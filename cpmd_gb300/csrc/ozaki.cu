@@ -265,6 +265,49 @@ __global__ void k_oz_slice_rows(const double* __restrict__ Ar, int lda, int rows
   }
 }
 
+// The same slicing with the row exponents found in the same pass (n <= 256): block
+// (32 rows, ceil(n/16) column groups), thread (row, 16 states); the row maximum is
+// reduced over the column groups in shared memory and also stored to rmax.
+__global__ void __launch_bounds__(512) k_oz_slice_rows_max(const double* __restrict__ Ar, int lda, int rows, int n,
+                                                           unsigned long long* __restrict__ rmax, size_t ks,
+                                                           uint4* __restrict__ out) {
+  __shared__ unsigned long long red[16][33];
+  const int r = blockIdx.x * 32 + threadIdx.x, k = threadIdx.y * 16;
+  double x0[8], x1[8];
+  unsigned long long mx = 0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    x0[q] = (r < rows && k + q < n) ? Ar[r + (size_t)(k + q) * lda] : 0.0;
+    x1[q] = (r < rows && k + 8 + q < n) ? Ar[r + (size_t)(k + 8 + q) * lda] : 0.0;
+    const unsigned long long b0 = (unsigned long long)__double_as_longlong(x0[q]) & ~(1ull << 63);
+    const unsigned long long b1 = (unsigned long long)__double_as_longlong(x1[q]) & ~(1ull << 63);
+    mx = b0 > mx ? b0 : mx;
+    mx = b1 > mx ? b1 : mx;
+  }
+  red[threadIdx.y][threadIdx.x] = mx;
+  __syncthreads();
+  if (threadIdx.y == 0) {
+    for (int j = 1; j < (int)blockDim.y; ++j) {
+      const unsigned long long o = red[j][threadIdx.x];
+      mx = o > mx ? o : mx;
+    }
+    red[0][threadIdx.x] = mx;
+    if (r < rows) rmax[r] = mx;
+  }
+  __syncthreads();
+  if (r >= rows) return;
+  const int e = exp_of_max(red[0][threadIdx.x]);
+  uint4 d0[OZ_SL], d1[OZ_SL];
+  digits8(x0, e, d0);
+  digits8(x1, e, d1);
+  const size_t plane = (size_t)rows * ks / 8, off = ((size_t)r * ks + k) / 8;
+#pragma unroll
+  for (int s = 0; s < OZ_SL; ++s) {
+    out[s * plane + off] = d0[s];
+    if (k + 8 < n) out[s * plane + off + 1] = d1[s];
+  }
+}
+
 // C M operand B: plane s, row j (column of M), columns k < n: M[k][j]; exponent per column of M.
 __global__ void k_oz_slice_mat(const double* __restrict__ M, int n, const unsigned long long* __restrict__ emax,
                                size_t ks, uint4* __restrict__ out) {
@@ -296,6 +339,7 @@ struct OzParams {
   unsigned long long* Lacc;
   double* Cout;                  // mode 1
   int ldo;
+  int zero_row1;                 // mode 1: write 0 to row 1 (Im c(G=0) of the real view)
   int* status;
 };
 
@@ -478,7 +522,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 #pragma unroll
       for (int c = 0; c < 32; ++c) {
         const int j = w.n0 + 32 * (warp >> 2) + c;
-        if (j < p.N) p.Cout[row + (size_t)j * p.ldo] = fold_to_double(H[c], Lo[c], er + exp_of_max(p.eB[j]));
+        if (j < p.N)
+          p.Cout[row + (size_t)j * p.ldo] =
+              (p.zero_row1 && row == 1) ? 0.0 : fold_to_double(H[c], Lo[c], er + exp_of_max(p.eB[j]));
       }
     }
     u = oz_next_unit(p, u);
@@ -604,7 +650,7 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, unsig
 // cores, queued without a host synchronisation; skipped when *status != 0 on
 // entry, *status = -2 on a timed-out wait.
 int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout, int ldo,
-            int* status) {
+            int zero_row1, int* status) {
   const size_t ks = ((size_t)n + 7) & ~size_t(7);
   const size_t bytes = ((size_t)rows + n) * 8;
   if (!ensure(c, c.nl_a, bytes) || !ensure(c, c.oz_a, sizeof(uint16_t) * OZ_SL * (size_t)rows * ks) ||
@@ -617,16 +663,24 @@ int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, 
     k_mat_col_max<<<(n + 255) / 256, 256, 0, c.stream>>>(M, n, mcmax);
     GBCP_LAUNCH_CHECK(c);
   }
-  {
-    ProfScope ps_(c, "k_row_max");
-    k_row_max<<<(rows + 255) / 256, 256, 0, c.stream>>>(A, lda, rows, n, rmax);
+  if (n <= 256) {
+    ProfScope ps_(c, "k_oz_slice");
+    k_oz_slice_rows_max<<<(rows + 31) / 32, dim3(32, (n + 15) / 16), 0, c.stream>>>(A, lda, rows, n, rmax, ks,
+                                                                                   static_cast<uint4*>(c.oz_a.p));
     GBCP_LAUNCH_CHECK(c);
-  }
-  {
+  } else {
+    {
+      ProfScope ps_(c, "k_row_max");
+      k_row_max<<<(rows + 255) / 256, 256, 0, c.stream>>>(A, lda, rows, n, rmax);
+      GBCP_LAUNCH_CHECK(c);
+    }
     ProfScope ps_(c, "k_oz_slice");
     k_oz_slice_rows<<<dim3((rows + 127) / 128, (n + 15) / 16), 128, 0, c.stream>>>(A, lda, rows, n, rmax, ks,
                                                                                   static_cast<uint4*>(c.oz_a.p));
     GBCP_LAUNCH_CHECK(c);
+  }
+  {
+    ProfScope ps_(c, "k_oz_slice");
     k_oz_slice_mat<<<dim3((n + 127) / 128, (n + 7) / 8), 128, 0, c.stream>>>(M, n, mcmax, ks,
                                                                             static_cast<uint4*>(c.oz_b.p));
     GBCP_LAUNCH_CHECK(c);
@@ -647,6 +701,7 @@ int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, 
   p.eB = mcmax;
   p.Cout = Cout;
   p.ldo = ldo;
+  p.zero_row1 = zero_row1;
   p.status = status;
   {
     allow_smem(k_oz_tc, OZ_SMEM);
