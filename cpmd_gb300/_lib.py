@@ -55,6 +55,7 @@ SIGNATURES = {
     "gbcp_vpsi": (_I, [_P, _P, _I, _P, _I, _P, _P, _I, _I]),
     "gbcp_ortho": (_I, [_P, _P, _I, _I, _I, _DP, _I]),
     "gbcp_ovlap": (_I, [_P, _P, _I, _I, _P, _I]),
+    "gbcp_rortog": (_I, [_P, _P, _I, _P, _I, _I, _I, _D, _I, _P, _P, _I]),
     "gbcp_ovlap_noalloc": (_I, [_P, _I, _I, _I, _I, _P, _P]),
     "gbcp_invfftn": (_I, [_P, _P, _I]),
     "gbcp_fwfftn": (_I, [_P, _P, _I]),

@@ -231,6 +231,24 @@ class Context:
         self._check("gbcp_ovlap", self.lib.gbcp_ovlap(self.h, _ptr(c0), ldc, n, _ptr(smat), self._prep(c0, smat)))
         return smat
 
+    def rortog(self, c0, cm, tnon: bool = False, epsog: float = 1e-6, maxit: int = 30):
+        """CP-dynamics orthonormality constraint (rortog -> rortho): updates cm in place
+        to cm + c0 gam and returns (gam, iterations); gam is symmetric (nstate x nstate)."""
+        ldc0, n = _ld_wfn(c0, self.ngw)
+        ldcm, n2 = _ld_wfn(cm, self.ngw)
+        if n2 != n:
+            raise ValueError("c0 and cm hold different numbers of states")
+        if _is_torch(cm):
+            import torch
+            gam = torch.empty((n, n), dtype=torch.float64, device=cm.device)
+        else:
+            gam = np.empty((n, n))
+        it = C.c_int(0)
+        self._check("gbcp_rortog", self.lib.gbcp_rortog(self.h, _ptr(c0), ldc0, _ptr(cm), ldcm, n, int(bool(tnon)),
+                                                       float(epsog), int(maxit), _ptr(gam), C.byref(it),
+                                                       self._prep(c0, cm, gam)))
+        return gam, it.value
+
     def invfftn(self, grid):
         """In-place inverse 3D FFT of a complex grid shaped (nr3, kr2, kr1)."""
         self._check("gbcp_invfftn", self.lib.gbcp_invfftn(self.h, _ptr(grid), self._prep(grid)))

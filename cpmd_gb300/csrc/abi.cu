@@ -368,7 +368,7 @@ int gbcp_ctx_destroy(gbcp_ctx* h) {
   if (c.stream) cudaStreamSynchronize(c.stream);
   for (void* p : c.dev_allocs) cudaFree(p);
   gbcp::Scratch* all[] = {&c.zbuf, &c.ybuf, &c.qbuf, &c.st_c0, &c.st_c2, &c.st_rho, &c.st_vpot, &c.st_f,
-                          &c.st_misc, &c.st_misc2, &c.st_vf, &c.red, &c.red2, &c.smat, &c.smat2, &c.smat3, &c.sparts, &c.cscr, &c.cdiag, &c.cwork, &c.xr_part, &c.xr_tk, &c.oz_a, &c.oz_b,
+                          &c.st_misc, &c.st_misc2, &c.st_vf, &c.red, &c.red2, &c.smat, &c.smat2, &c.smat3, &c.sparts, &c.cscr, &c.cdiag, &c.cwork, &c.xr_part, &c.xr_tk, &c.rt_mats, &c.oz_a, &c.oz_b,
                           &c.nl_a, &c.nl_b, &c.nl_c, &c.nl_d, &c.nl_ta, &c.nl_tb, &c.nl_tp, &c.en_rho, &c.en_a, &c.en_b, &c.en_veff,
                           &c.en_red, &c.en_ei, &c.en_fp, &c.en_idx, &c.en_in[0], &c.en_in[1], &c.en_in[2],
                           &c.en_in[3], &c.en_in[4]};
@@ -700,6 +700,44 @@ int gbcp_ortho(gbcp_ctx* h, double* c0, int ldc, int nstate, int method, double*
   rc = method == GBCP_ORTHO_GS ? gbcp::ortho_gs(c, dc0, l0, nstate, scond)
                                : gbcp::ortho_lowdin(c, dc0, l0, nstate, scond);
   if (!rc && mem == GBCP_MEM_HOST) rc = stage_out_cx(c, dc0, c0, ldc, c.ngw, nstate);
+  return finish(c, rc);
+}
+
+int gbcp_rortog(gbcp_ctx* h, const double* c0, int ldc0, double* cm, int ldcm, int nstate, int tnon, double epsog,
+                int maxit, double* gam, int* iters, int mem) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  if (iters) *iters = 0;
+  if (bad_mem(mem) || nstate < 0 || maxit < 0 || !(epsog >= 0.0) ||
+      (nstate > 0 && (!c0 || !cm || ldc0 < c.ngw || ldcm < c.ngw || (const double*)cm == c0)))
+    return set_err(h, GBCP_ERR_ARG, "rortog: bad argument");
+  c.err.clear();
+  if (nstate == 0) return GBCP_OK;
+  const cx<double>* d0 = reinterpret_cast<const cx<double>*>(c0);
+  cx<double>* dm = reinterpret_cast<cx<double>*>(cm);
+  int l0 = ldc0, lm = ldcm;
+  double* dg = gam;
+  int rc = 0;
+  if (mem == GBCP_MEM_HOST) {
+    cx<double>* t;
+    if ((rc = stage_in_cx(c, c.st_c0, c0, ldc0, c.ngw, nstate, &t))) return rc;
+    d0 = t;
+    if ((rc = stage_in_cx(c, c.st_c2, cm, ldcm, c.ngw, nstate, &dm))) return rc;
+    l0 = lm = c.ngw;
+    if (gam) {
+      if (!gbcp::ensure(c, c.st_misc, sizeof(double) * (size_t)nstate * nstate)) return GBCP_ERR_NOMEM;
+      dg = static_cast<double*>(c.st_misc.p);
+    }
+  }
+  rc = gbcp::rortho(c, d0, l0, dm, lm, nstate, tnon, epsog, maxit, dg, iters);
+  if (!rc && mem == GBCP_MEM_HOST) {
+    rc = stage_out_cx(c, dm, cm, ldcm, c.ngw, nstate);
+    if (!rc && gam) {
+      cudaError_t e =
+          cudaMemcpyAsync(gam, dg, sizeof(double) * (size_t)nstate * nstate, cudaMemcpyDeviceToHost, c.stream);
+      if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));
+    }
+  }
   return finish(c, rc);
 }
 

@@ -100,6 +100,7 @@ struct Ctx {
   Scratch red, red2;  // reductions
   Scratch smat, smat2, smat3, sparts, cscr, cdiag, cwork;
   Scratch xr_part, xr_tk;  // density x-stage: partial tiles and ticket counters of the pair chunks
+  Scratch rt_mats;         // rortho: the n x n matrices of the constraint iteration
   Scratch oz_a, oz_b;  // bf16 digit planes of the split-precision ortho GEMMs
   Scratch nl_a, nl_b, nl_c, nl_d;
   Scratch nl_ta, nl_tb, nl_tp;  // projector GEMM slices (A, B) and split-K partials
@@ -176,8 +177,20 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, unsig
              int* status);
 // Cout may be A itself: A is sliced into digit planes before the GEMM reads them.
 // zero_row1: row 1 of the result (Im c(G=0) of the real view) is written as 0.
+// accumulate: Cout += A M (Cout must not alias A then).
 int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout, int ldo,
-            int zero_row1, int* status);
+            int zero_row1, int* status, int accumulate = 0);
+// A (row-major n x n) = <X_i | Y_j> in the Γ metric, 2 Re(X^H Y) - Re X(0) Re Y(0)^T, over the
+// real views X, Y (K = 2 ngw rows, leading dimensions ldx, ldy), FP64-accurate on the
+// tensor cores; queued without a host synchronisation.
+int xovlap_tc(Ctx& c, const double* X, int ldx, const double* Y, int ldy, int n, double* A, int* status);
+// ---- CP-dynamics constraint (rortho.cu) ----
+// A (row-major n x n) = <X_i|Y_j>; tensor cores in the mixed mode, FP64 SIMT otherwise.
+int xovlap(Ctx& c, const cx<double>* X, int ldx, const cx<double>* Y, int ldy, int n, double* A);
+// Lagrange multipliers of the orthonormality constraint and cm += c0 gam; gam_out
+// (device, n x n, may be NULL); returns 8 (not converged) past maxit with cm unchanged.
+int rortho(Ctx& c, const cx<double>* c0, int ldc0, cx<double>* cm, int ldcm, int n, int tnon, double epsog, int maxit,
+           double* gam_out, int* iters);
 // mesh length as seen by the band-loop dispatch (-1 forces the Stockham kernels)
 inline int band_len(const Ctx& c, int n) { return c.fft_engine == 2 ? -1 : n; }
 inline bool use_tc_gemm(const Ctx& c) { return c.gemm_mode == 1 || (c.gemm_mode < 0 && c.precision == 1); }

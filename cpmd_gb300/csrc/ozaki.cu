@@ -330,6 +330,7 @@ struct OzParams {
   int M, N;           // rows per digit plane of A and of B
   int K;              // contraction length
   int mode;           // 0: S, tiles of the upper block triangle x K splits; 1: C M, persistent over tiles
+  int full;           // mode 0: every tile of the nib x njb grid (two different operands)
   int njb;            // mode 0: column tiles
   int subs_per;       // mode 0: sub-chunks per K split (a multiple of OZ_SUBS)
   int upper;          // mode 1: M upper triangular (column tile j needs k < j0 + 64)
@@ -340,6 +341,7 @@ struct OzParams {
   double* Cout;                  // mode 1
   int ldo;
   int zero_row1;                 // mode 1: write 0 to row 1 (Im c(G=0) of the real view)
+  int accumulate;                // mode 1: Cout += A M instead of Cout = A M
   int* status;
 };
 
@@ -353,14 +355,19 @@ __device__ __forceinline__ OzUnit oz_unit(const OzParams& p, int u) {
   const int total_subs = (p.K + OZ_KS - 1) / OZ_KS;
   if (p.mode == 0) {
     if (u != (int)blockIdx.x) return w;  // one unit per CTA
-    int t = blockIdx.x, ib = 0;
-    while (ib < 4096 && t >= max(0, p.njb - 2 * ib)) {
-      t -= max(0, p.njb - 2 * ib);
-      ++ib;
+    if (p.full) {
+      w.m0 = (blockIdx.x / p.njb) * OZ_M;
+      w.n0 = (blockIdx.x % p.njb) * OZ_N;
+    } else {
+      int t = blockIdx.x, ib = 0;
+      while (ib < 4096 && t >= max(0, p.njb - 2 * ib)) {
+        t -= max(0, p.njb - 2 * ib);
+        ++ib;
+      }
+      if (ib >= 4096) return w;
+      w.m0 = ib * OZ_M;
+      w.n0 = (2 * ib + t) * OZ_N;
     }
-    if (ib >= 4096) return w;
-    w.m0 = ib * OZ_M;
-    w.n0 = (2 * ib + t) * OZ_N;
     w.sub0 = blockIdx.y * p.subs_per;
     w.nsub = min(total_subs, w.sub0 + p.subs_per) - w.sub0;
     w.valid = w.nsub > 0;
@@ -378,7 +385,7 @@ __device__ __forceinline__ OzUnit oz_unit(const OzParams& p, int u) {
   return w;
 }
 
-__device__ __forceinline__ int oz_next_unit(const OzParams& p, int u) { return p.mode == 0 ? -1 : u + gridDim.x; }
+__device__ __forceinline__ int oz_next_unit(const OzParams& p, int u) { return p.mode == 0 ? -1 : u + (int)gridDim.x; }
 
 // thread 0: the 16 TMA loads (8 A planes, 8 B planes) of one sub-chunk into buffer b
 __device__ __forceinline__ void oz_load(const CUtensorMap* tmA, const CUtensorMap* tmB, const OzParams& p,
@@ -522,9 +529,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 #pragma unroll
       for (int c = 0; c < 32; ++c) {
         const int j = w.n0 + 32 * (warp >> 2) + c;
-        if (j < p.N)
-          p.Cout[row + (size_t)j * p.ldo] =
-              (p.zero_row1 && row == 1) ? 0.0 : fold_to_double(H[c], Lo[c], er + exp_of_max(p.eB[j]));
+        if (j < p.N) {
+          double* o = p.Cout + row + (size_t)j * p.ldo;
+          double v = (p.zero_row1 && row == 1) ? 0.0 : fold_to_double(H[c], Lo[c], er + exp_of_max(p.eB[j]));
+          if (p.accumulate) v += *o;
+          *o = v;
+        }
       }
     }
     u = oz_next_unit(p, u);
@@ -568,6 +578,20 @@ __global__ void k_ozaki_syrk_finalize(const long long* __restrict__ H, const lon
   if (scond_bits) {
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
     if ((threadIdx.x & 31) == 0) atomicMax(scond_bits, (unsigned long long)__double_as_longlong(mx));
+  }
+}
+
+// A[i][j] = 2 <x_i|y_j> - Re x_i(0) Re y_j(0) from the int64 level sums of the full grid
+__global__ void k_ozaki_xov_finalize(const long long* __restrict__ H, const long long* __restrict__ Lo,
+                                     const unsigned long long* __restrict__ xmax,
+                                     const unsigned long long* __restrict__ ymax, int n, const double* __restrict__ X,
+                                     int ldx, const double* __restrict__ Y, int ldy, int geq0, double* __restrict__ A) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    double v = 2.0 * fold_to_double(H[e], Lo[e], exp_of_max(xmax[i]) + exp_of_max(ymax[j]));
+    if (geq0) v -= X[(size_t)i * ldx] * Y[(size_t)j * ldy];
+    A[e] = v;
   }
 }
 
@@ -646,11 +670,86 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, unsig
   return 0;
 }
 
+// Cross overlap <X_i|Y_j> of two different sets of n states on the tensor cores:
+// both operands sliced into digit planes with their own column exponents, every
+// tile of the n x n grid (mode 0, full), then the Γ-metric finalize.
+int xovlap_tc(Ctx& c, const double* X, int ldx, const double* Y, int ldy, int n, double* A, int* status) {
+  const int K = 2 * c.ngw;
+  const int nib = (n + OZ_M - 1) / OZ_M, njb = (n + OZ_N - 1) / OZ_N;
+  const int ntiles = nib * njb;
+  const int total_subs = (K + OZ_KS - 1) / OZ_KS;
+  int nsplit = std::max(1, std::min((total_subs + OZ_SUBS - 1) / OZ_SUBS, 148 / std::max(1, ntiles)));
+  int subs_per = (total_subs + nsplit - 1) / nsplit;
+  subs_per = ((subs_per + OZ_SUBS - 1) / OZ_SUBS) * OZ_SUBS;
+  nsplit = (total_subs + subs_per - 1) / subs_per;
+  const size_t nn = (size_t)n * n;
+  const size_t ks = ((size_t)K + 7) & ~size_t(7);
+  const size_t bytes = 2 * nn * 8 + 2 * (size_t)n * 8;
+  if (!ensure(c, c.sparts, bytes) || !ensure(c, c.oz_a, sizeof(uint16_t) * OZ_SL * (size_t)n * ks) ||
+      !ensure(c, c.oz_b, sizeof(uint16_t) * OZ_SL * (size_t)n * ks))
+    return 6;
+  unsigned long long* Hacc = static_cast<unsigned long long*>(c.sparts.p);
+  unsigned long long* Lacc = Hacc + nn;
+  unsigned long long* xmax = Lacc + nn;
+  unsigned long long* ymax = xmax + n;
+  GBCP_CUDA_TRY(c, cudaMemsetAsync(Hacc, 0, bytes, c.stream));
+  {
+    ProfScope ps_(c, "k_col_max");
+    const int kspl = std::max(1, std::min(64, (K + 4095) / 4096));
+    const int kper = (K + kspl - 1) / kspl;
+    k_col_max<<<dim3(n, kspl), 256, 0, c.stream>>>(X, ldx, K, n, kper, xmax);
+    GBCP_LAUNCH_CHECK(c);
+    k_col_max<<<dim3(n, kspl), 256, 0, c.stream>>>(Y, ldy, K, n, kper, ymax);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  {
+    ProfScope ps_(c, "k_oz_slice");
+    k_oz_slice_cols<<<dim3((K / 8 + 255) / 256 + 1, n), 256, 0, c.stream>>>(X, ldx, K, n, xmax, ks,
+                                                                            static_cast<uint4*>(c.oz_a.p));
+    GBCP_LAUNCH_CHECK(c);
+    k_oz_slice_cols<<<dim3((K / 8 + 255) / 256 + 1, n), 256, 0, c.stream>>>(Y, ldy, K, n, ymax, ks,
+                                                                            static_cast<uint4*>(c.oz_b.p));
+    GBCP_LAUNCH_CHECK(c);
+  }
+  CUtensorMap ma, mb;
+  if (!tmap_bf16_2d(&ma, c.oz_a.p, K, (long long)OZ_SL * n, (int)ks, OZ_KS, OZ_M, 64) ||
+      !tmap_bf16_2d(&mb, c.oz_b.p, K, (long long)OZ_SL * n, (int)ks, OZ_KS, OZ_N, 64)) {
+    c.err = "cross overlap: tensor map encoding failed";
+    return 5;
+  }
+  OzParams p{};
+  p.M = n;
+  p.N = n;
+  p.K = K;
+  p.mode = 0;
+  p.full = 1;
+  p.njb = njb;
+  p.subs_per = subs_per;
+  p.Hacc = Hacc;
+  p.Lacc = Lacc;
+  p.status = status;
+  {
+    allow_smem(k_oz_tc, OZ_SMEM);
+    ProfScope ps_(c, "k_ozaki_xov");
+    k_oz_tc<<<dim3(ntiles, nsplit), OZ_THREADS, OZ_SMEM, c.stream>>>(ma, mb, p);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  {
+    ProfScope ps_(c, "k_ozaki_syrk_finalize");
+    const int fb = std::max(1, std::min(1024, (int)((nn + 255) / 256)));
+    k_ozaki_xov_finalize<<<fb, 256, 0, c.stream>>>(reinterpret_cast<const long long*>(Hacc),
+                                                   reinterpret_cast<const long long*>(Lacc), xmax, ymax, n, X, ldx, Y,
+                                                   ldy, c.geq0, A);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  return 0;
+}
+
 // Cout (rows x n, ldo) = A (rows x n, lda) * M (n x n row-major) on the tensor
 // cores, queued without a host synchronisation; skipped when *status != 0 on
 // entry, *status = -2 on a timed-out wait.
 int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout, int ldo,
-            int zero_row1, int* status) {
+            int zero_row1, int* status, int accumulate) {
   const size_t ks = ((size_t)n + 7) & ~size_t(7);
   const size_t bytes = ((size_t)rows + n) * 8;
   if (!ensure(c, c.nl_a, bytes) || !ensure(c, c.oz_a, sizeof(uint16_t) * OZ_SL * (size_t)rows * ks) ||
@@ -702,6 +801,7 @@ int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, 
   p.Cout = Cout;
   p.ldo = ldo;
   p.zero_row1 = zero_row1;
+  p.accumulate = accumulate;
   p.status = status;
   {
     allow_smem(k_oz_tc, OZ_SMEM);

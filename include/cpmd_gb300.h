@@ -42,7 +42,7 @@ enum gbcp_status {
   GBCP_ERR_CUDA = 5,       /* CUDA runtime error */
   GBCP_ERR_NOMEM = 6,      /* device allocation failed */
   GBCP_ERR_UNSUPPORTED = 7,/* mesh size / option not supported */
-  GBCP_ERR_NOT_CONVERGED = 8 /* iterative Loewdin step did not converge */
+  GBCP_ERR_NOT_CONVERGED = 8 /* iterative Loewdin step or rortog iteration did not converge */
 };
 
 enum gbcp_precision {
@@ -133,6 +133,19 @@ int gbcp_ortho(gbcp_ctx* ctx, double* c0, int ldc, int nstate, int method, doubl
 /* Overlap matrix only: S = 2 Re(C^H C) - Re c(0) Re c(0)^T, full n x n
  * column-major (ovlap_utils.mod.F90:150-165, symmetric branch). */
 int gbcp_ovlap(gbcp_ctx* ctx, const double* c0, int ldc, int nstate, double* smat, int mem);
+
+/* Orthonormality constraint of Car-Parrinello dynamics: rortog -> rortho
+ * (rortog_utils.mod.F90:43-87, 315-498) with rotate (rotate_utils.mod.F90:63-101).
+ * c0 (orthonormal) and cm (the propagated wavefunctions): ngw x nstate complex,
+ * leading dimensions ldc0, ldcm, distinct arrays.  Iterates the Lagrange
+ * multipliers until max|gam' - gam| <= epsog/2, at most maxit iterations (the
+ * reference's defaults: 1e-6 and 30), symmetrises them, writes gam
+ * (nstate x nstate, column-major; may be NULL) and updates cm += c0 gam.
+ * tnon != 0: c0 is not exactly orthonormal (the del = (I - <c0|c0>)/2 term).
+ * *iters (may be NULL): iterations done.  GBCP_ERR_NOT_CONVERGED past maxit,
+ * cm unchanged (the reference stops). */
+int gbcp_rortog(gbcp_ctx* ctx, const double* c0, int ldc0, double* cm, int ldcm, int nstate, int tnon, double epsog,
+                int maxit, double* gam, int* iters, int mem);
 
 /* Allocation-free overlap matrix.  No counterpart in the reference: it exists
  * for callers that cannot call cudaMalloc (an application whose device memory

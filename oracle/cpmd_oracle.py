@@ -429,3 +429,49 @@ def enl(c0, f, twnl, eigr, nghtol, wsg, geq0):
     """E_nl = sum_i f_i sum_{ia,iv} wsg(iv) fnl(ia,iv,i)^2, whose R-derivative rnlfor returns."""
     fnl = rnlsm1(c0, twnl, eigr, nghtol, geq0)
     return float(np.einsum("v,i,avi->", np.asarray(wsg), np.asarray(f), fnl ** 2))
+
+
+# ----------------------------------------------------------------------------
+# CP-dynamics orthonormality constraint
+# ----------------------------------------------------------------------------
+def cross_overlap(c1, c2, geq0):
+    """A(i, j) = <c1_i | c2_j> in the Γ metric: 2 Re(c1^H c2) - Re c1(0) Re c2(0)^T
+    (ovlap_utils.mod.F90:57-160, non-symmetric branch)."""
+    a = 2.0 * (c1.real.T @ c2.real + c1.imag.T @ c2.imag)
+    if geq0:
+        a -= np.outer(c1[0].real, c2[0].real)
+    return a
+
+
+def rortho(c0, cm, geq0, tnon=False, epsog=1e-6, maxit=30):
+    """Lagrange multipliers of the orthonormality constraint and the constrained
+    update (rortog_utils.mod.F90:315-498, Parrinello-Car iteration):
+      rho = I - sym <c0|cm>,  sig = I - <cm|cm>,  del = -(<c0|c0> - I)/2 (tnon),
+      gam = sig/2,  X = rho^T rho/2 + sig/2,
+      repeat  gam' = X - (rho - gam)^T (rho - gam)/2 [+ gam^T del gam]
+      until max|gam' - gam| <= epsog/2 (at most maxit iterations),
+      gam = sym gam,  cm <- cm + c0 gam.
+    Returns (gam, cm_new, iterations); raises RuntimeError past maxit."""
+    n = c0.shape[1]
+    eye = np.eye(n)
+    a = cross_overlap(c0, cm, geq0)
+    rho = eye - 0.5 * (a + a.T)
+    sig = eye - cross_overlap(cm, cm, geq0)
+    dl = -0.5 * (cross_overlap(c0, c0, geq0) - eye) if tnon else None
+    gam = 0.5 * sig
+    x = 0.5 * (rho.T @ rho) + 0.5 * sig
+    it = 0
+    while True:
+        it += 1
+        scr = rho - gam
+        gamn = x - 0.5 * (scr.T @ scr)
+        if tnon:
+            gamn = gamn + gam.T @ (dl @ gam)
+        dif = float(np.abs(gamn - gam).max())
+        gam = gamn
+        if not (dif > 0.5 * epsog and it <= maxit):
+            break
+    if it > maxit:
+        raise RuntimeError("RORTHO: maximum number of iterations exceeded")
+    gam = 0.5 * (gam + gam.T)
+    return gam, np.asfortranarray(cm + c0 @ gam), it
