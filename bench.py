@@ -423,6 +423,40 @@ def run_extras(args, dev):
         ctx.close()
     out["cell_8atoms_16states_32cubed"] = r
 
+    # ---- CP-dynamics constraint (rortog) on the 64-atom cell: 128 states, ngw 42 736
+    cl = make_cell_device("c1")
+    b = cl.basis
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(7)
+    noise = torch.complex(torch.randn(cl.c0.shape, generator=gen, device=dev, dtype=torch.float64),
+                          torch.randn(cl.c0.shape, generator=gen, device=dev, dtype=torch.float64))
+    cm0 = cl.c0 + 1e-3 * noise / float(np.sqrt(b.ngw))
+    if b.geq0:
+        cm0[:, 0] = cm0[:, 0].real.to(torch.complex128)
+    cm = torch.empty_like(cm0)
+    r = {}
+    gams = {}
+    for prec in ("mixed", "fp64"):
+        ctx = Context(b, prec)
+        holder = {}
+
+        def step():
+            cm.copy_(cm0)
+            holder["g"], holder["it"] = ctx.rortog(cl.c0, cm, epsog=1e-6, maxit=30)
+        ms = _timed_loop(step, 5 if prec == "mixed" else 2, 2)
+        gams[prec] = holder["g"].clone()
+        s = ctx.ovlap(cm)
+        r[prec] = {"ms_per_call": ms, "iterations": holder["it"],
+                   "max_abs_overlap_minus_identity_after": float((s - torch.eye(cl.nstate, device=dev,
+                                                                                dtype=torch.float64)).abs().max())}
+        ctx.close()
+    r["max_abs_gam_mixed_vs_fp64"] = float((gams["mixed"] - gams["fp64"]).abs().max())
+    r["workload"] = ("rortog (rortho iteration + cm += c0 gam), 128 states, ngw 42736, cm = c0 + 1e-3 noise, "
+                     "epsog 1e-6; each call includes an 87.5 MB device copy restoring cm")
+    out["rortog_64atoms_128states"] = r
+    del cl, cm, cm0, noise, gams
+    torch.cuda.empty_cache()
+
     # ---- 216 atoms, 432 states, 50 Ry, 144^3: energy + adjoint (dE/dpsi*, dE/dV, forces)
     cl = make_cell_device("c2")
     b = cl.basis
