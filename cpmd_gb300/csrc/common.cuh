@@ -22,6 +22,47 @@ template <typename T> __device__ __forceinline__ cx<T> cmulc(cx<T> a, cx<T> b) {
   return mk<T>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
 }
 template <typename T> __device__ __forceinline__ cx<T> scl(cx<T> a, T s) { return mk<T>(a.x * s, a.y * s); }
+// a + s b (scalar s)
+template <typename T> __device__ __forceinline__ cx<T> cfma(cx<T> a, T s, cx<T> b) {
+  return mk<T>(fma(s, b.x, a.x), fma(s, b.y, a.y));
+}
+// a + S i b (S = +1 or -1), without forming the swapped pair i b
+template <int S, typename T> __device__ __forceinline__ cx<T> add_si(cx<T> a, cx<T> b) {
+  return S > 0 ? mk<T>(a.x - b.y, a.y + b.x) : mk<T>(a.x + b.y, a.y - b.x);
+}
+
+// FP32 complex values occupy a 64-bit register pair; sm_100-family packed
+// instructions (add/sub/mul/fma .rn.f32x2) process both halves in one issue slot.
+__device__ __forceinline__ unsigned long long f2_pack(cx<float> a) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+  return r;
+}
+__device__ __forceinline__ cx<float> f2_unpack(unsigned long long r) {
+  cx<float> a;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+  return a;
+}
+template <> __device__ __forceinline__ cx<float> operator+<float>(cx<float> a, cx<float> b) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+  return f2_unpack(r);
+}
+template <> __device__ __forceinline__ cx<float> operator-<float>(cx<float> a, cx<float> b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+  return f2_unpack(r);
+}
+template <> __device__ __forceinline__ cx<float> scl<float>(cx<float> a, float s) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(mk<float>(s, s))));
+  return f2_unpack(r);
+}
+template <> __device__ __forceinline__ cx<float> cfma<float>(cx<float> a, float s, cx<float> b) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(f2_pack(b)), "l"(f2_pack(mk<float>(s, s))), "l"(f2_pack(a)));
+  return f2_unpack(r);
+}
 // multiply by +i (S=+1) or -i (S=-1)
 template <int S, typename T> __device__ __forceinline__ cx<T> mul_si(cx<T> a) {
   return S > 0 ? mk<T>(-a.y, a.x) : mk<T>(a.y, -a.x);

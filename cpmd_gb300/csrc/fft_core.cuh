@@ -44,36 +44,36 @@ template <int S, typename T> __device__ __forceinline__ void dft2(cx<T>* v) {
 }
 
 template <int S, typename T> __device__ __forceinline__ void dft4(cx<T>& v0, cx<T>& v1, cx<T>& v2, cx<T>& v3) {
-  cx<T> a0 = v0 + v2, a1 = v0 - v2, a2 = v1 + v3, a3 = mul_si<S>(v1 - v3);
+  const cx<T> a0 = v0 + v2, a1 = v0 - v2, a2 = v1 + v3, d = v1 - v3;
   v0 = a0 + a2;
   v2 = a0 - a2;
-  v1 = a1 + a3;
-  v3 = a1 - a3;
+  v1 = add_si<S>(a1, d);
+  v3 = add_si<-S>(a1, d);
 }
 
 template <int S, typename T> __device__ __forceinline__ void dft3(cx<T>* v) {
   const T hs = (T)GBCP_S3;
-  cx<T> t1 = v[1] + v[2];
-  cx<T> t2 = v[0] - scl(t1, (T)0.5);
-  cx<T> t3 = mul_si<S>(scl(v[1] - v[2], hs));
+  const cx<T> t1 = v[1] + v[2];
+  const cx<T> t2 = cfma(v[0], (T)-0.5, t1);
+  const cx<T> d = scl(v[1] - v[2], hs);
   v[0] = v[0] + t1;
-  v[1] = t2 + t3;
-  v[2] = t2 - t3;
+  v[1] = add_si<S>(t2, d);
+  v[2] = add_si<-S>(t2, d);
 }
 
 template <int S, typename T> __device__ __forceinline__ void dft5(cx<T>* v) {
   const T c1 = (T)GBCP_C5_1, c2 = (T)GBCP_C5_2, s1 = (T)GBCP_S5_1, s2 = (T)GBCP_S5_2;
-  cx<T> a = v[1] + v[4], b = v[2] + v[3], c = v[1] - v[4], d = v[2] - v[3];
-  cx<T> v0 = v[0];
-  cx<T> p1 = mk<T>(v0.x + c1 * a.x + c2 * b.x, v0.y + c1 * a.y + c2 * b.y);
-  cx<T> p2 = mk<T>(v0.x + c2 * a.x + c1 * b.x, v0.y + c2 * a.y + c1 * b.y);
-  cx<T> q1 = mul_si<S>(mk<T>(s1 * c.x + s2 * d.x, s1 * c.y + s2 * d.y));
-  cx<T> q2 = mul_si<S>(mk<T>(s2 * c.x - s1 * d.x, s2 * c.y - s1 * d.y));
-  v[0] = mk<T>(v0.x + a.x + b.x, v0.y + a.y + b.y);
-  v[1] = p1 + q1;
-  v[4] = p1 - q1;
-  v[2] = p2 + q2;
-  v[3] = p2 - q2;
+  const cx<T> a = v[1] + v[4], b = v[2] + v[3], c = v[1] - v[4], d = v[2] - v[3];
+  const cx<T> v0 = v[0];
+  const cx<T> p1 = cfma(cfma(v0, c1, a), c2, b);
+  const cx<T> p2 = cfma(cfma(v0, c2, a), c1, b);
+  const cx<T> q1 = cfma(scl(c, s1), s2, d);
+  const cx<T> q2 = cfma(scl(c, s2), -s1, d);
+  v[0] = (v0 + a) + b;
+  v[1] = add_si<S>(p1, q1);
+  v[4] = add_si<-S>(p1, q1);
+  v[2] = add_si<S>(p2, q2);
+  v[3] = add_si<-S>(p2, q2);
 }
 
 template <int S, typename T> __device__ __forceinline__ void dft8(cx<T>* v) {
@@ -82,16 +82,15 @@ template <int S, typename T> __device__ __forceinline__ void dft8(cx<T>* v) {
   dft4<S>(e0, e1, e2, e3);
   dft4<S>(o0, o1, o2, o3);
   const T r = (T)GBCP_R2;
-  // w8 = e^{S i pi/4}
-  cx<T> w1o = mk<T>(r * (o1.x - S * o1.y), r * (o1.y + S * o1.x));   // (1 + S i)/sqrt2 * o1
-  cx<T> w2o = mul_si<S>(o2);                                           // S i * o2
-  cx<T> w3o = mk<T>(r * (-o3.x - S * o3.y), r * (-o3.y + S * o3.x));  // (-1 + S i)/sqrt2 * o3
+  // w8 = e^{S i pi/4}: (1 + S i)/sqrt2 o1 and (-1 + S i)/sqrt2 o3
+  const cx<T> w1o = scl(add_si<S>(o1, o1), r);
+  const cx<T> w3o = scl(add_si<S>(mk<T>(-o3.x, -o3.y), o3), r);
   v[0] = e0 + o0;
   v[4] = e0 - o0;
   v[1] = e1 + w1o;
   v[5] = e1 - w1o;
-  v[2] = e2 + w2o;
-  v[6] = e2 - w2o;
+  v[2] = add_si<S>(e2, o2);  // e2 +- S i o2
+  v[6] = add_si<-S>(e2, o2);
   v[3] = e3 + w3o;
   v[7] = e3 - w3o;
 }
