@@ -693,6 +693,13 @@ int gbcp_ortho(gbcp_ctx* h, double* c0, int ldc, int nstate, int method, double*
   cx<double>* dc0 = reinterpret_cast<cx<double>*>(c0);
   int l0 = ldc;
   int rc = 0;
+  if (mem == GBCP_MEM_HOST && method == GBCP_ORTHO_GS) {
+    // copies overlapped with the work where the tensor-core engine runs the step
+    rc = gbcp::ortho_gs_host(c, c0, ldc, nstate, scond);
+    if (rc != 7) return finish(c, rc);
+    rc = 0;
+    c.err.clear();
+  }
   if (mem == GBCP_MEM_HOST) {
     if ((rc = stage_in_cx(c, c.st_c0, c0, ldc, c.ngw, nstate, &dc0))) return rc;
     l0 = c.ngw;

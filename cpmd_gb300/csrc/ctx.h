@@ -184,6 +184,16 @@ int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, 
 // real views X, Y (K = 2 ngw rows, leading dimensions ldx, ldy), FP64-accurate on the
 // tensor cores; queued without a host synchronisation.
 int xovlap_tc(Ctx& c, const double* X, int ldx, const double* Y, int ldy, int n, double* A, int* status);
+// Range-pipelined forms for host-memory calls (ozaki.cu): S over K ranges kb[0..R]
+// (multiples of 32 rows of the real view; range r starts once ready[r] completes) and
+// C M over row ranges rb[0..R] (multiples of 128; done[r] recorded after range r).
+int ovlap_tc_ranges(Ctx& c, const double* Ar, int lda, int n, const int* kb, int R, const cudaEvent_t* ready,
+                    double* S, unsigned long long* scond_bits, int* status);
+int rmul_tc_ranges(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout,
+                   int ldo, int zero_row1, int* status, const int* rb, int R, const cudaEvent_t* done);
+// Gram-Schmidt of host-memory c0 with the copies overlapped (tensor-core engine);
+// returns 7 when the engine or size does not allow it (the caller stages instead).
+int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host);
 // ---- CP-dynamics constraint (rortho.cu) ----
 // A (row-major n x n) = <X_i|Y_j>; tensor cores in the mixed mode, FP64 SIMT otherwise.
 int xovlap(Ctx& c, const cx<double>* X, int ldx, const cx<double>* Y, int ldy, int n, double* A);

@@ -386,6 +386,74 @@ static int ortho_gs_steps(Ctx& c, cx<double>* c0, int ldc, int n, bool want_scon
   return apply_right(c, c0, ldc, n, X, 1);
 }
 
+// Gram-Schmidt of host-memory c0 (ld ldh) with its copies overlapped: the states
+// go up in R ranges of G rows on the copy stream, and range r's column exponents,
+// digit planes and partial overlap start as soon as it has landed; after the
+// Cholesky, C U^-1 runs range by range (in place in the staging buffer) and each
+// finished range goes back on the download stream while the next is computed.
+// A failed step skips the GEMM, so the download returns the unchanged states.
+int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host) {
+  if (!use_tc_gemm(c) || n > 4096 || n <= 0) return 7;
+  const int ngw = c.ngw;
+  // G-row ranges: multiples of 64 complex rows (128 real rows: one C M row tile, four S sub-chunks)
+  const int R = std::max(1, std::min(4, ngw / 4096));
+  int gb[5];
+  for (int r = 0; r <= R; ++r) gb[r] = (r == R) ? ngw : std::min(ngw, ((int)((long long)ngw * r / R) / 64) * 64);
+  int kb[5];
+  for (int r = 0; r <= R; ++r) kb[r] = 2 * gb[r];
+  if (!ensure(c, c.st_c0, sizeof(cx<double>) * (size_t)ngw * n) ||
+      !ensure(c, c.smat, sizeof(double) * (size_t)n * n) || !ensure(c, c.smat2, sizeof(double) * (size_t)n * n))
+    return 6;
+  if ((!c.copy && cudaStreamCreateWithFlags(&c.copy, cudaStreamNonBlocking) != cudaSuccess) ||
+      (!c.copy_out && cudaStreamCreateWithFlags(&c.copy_out, cudaStreamNonBlocking) != cudaSuccess)) {
+    c.err = "copy streams";
+    return 5;
+  }
+  while (c.pipe_ev.size() < (size_t)(2 * R + 2)) {
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      c.err = "pipeline events";
+      return 5;
+    }
+    c.pipe_ev.push_back(e);
+  }
+  cudaEvent_t* up = c.pipe_ev.data() + 1;
+  cudaEvent_t* done = c.pipe_ev.data() + 1 + R;
+  cx<double>* d = static_cast<cx<double>*>(c.st_c0.p);
+  double* S = static_cast<double*>(c.smat.p);
+  double* X = static_cast<double*>(c.smat2.p);
+  // the staging buffer is free once earlier work on the context stream is done
+  GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[0], c.stream));
+  GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.copy, c.pipe_ev[0], 0));
+  for (int r = 0; r < R; ++r) {
+    const int g0 = gb[r], g = gb[r + 1] - gb[r];
+    if (g > 0)
+      GBCP_CUDA_TRY(c, cudaMemcpy2DAsync(d + g0, sizeof(cx<double>) * (size_t)ngw, h + 2 * (size_t)g0,
+                                         sizeof(cx<double>) * (size_t)ldh, sizeof(cx<double>) * (size_t)g, n,
+                                         cudaMemcpyHostToDevice, c.copy));
+    GBCP_CUDA_TRY(c, cudaEventRecord(up[r], c.copy));
+  }
+  GBCP_CUDA_TRY(c, cudaMemsetAsync(c.d_info, 0, 16, c.stream));
+  double* Ar = reinterpret_cast<double*>(d);
+  int rc = ovlap_tc_ranges(c, Ar, 2 * ngw, n, kb, R, up, S, scond_host ? scond_bits_of(c) : nullptr, c.d_info);
+  if (!rc) rc = chol_inverse(c, S, X, n);
+  if (!rc) rc = rmul_tc_ranges(c, Ar, 2 * ngw, 2 * ngw, n, X, 1, Ar, 2 * ngw, c.geq0, c.d_info, kb, R, done);
+  if (rc) {
+    cudaStreamSynchronize(c.copy);
+    return rc;
+  }
+  for (int r = 0; r < R; ++r) {
+    const int g0 = gb[r], g = gb[r + 1] - gb[r];
+    GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.copy_out, done[r], 0));
+    if (g > 0)
+      GBCP_CUDA_TRY(c, cudaMemcpy2DAsync(h + 2 * (size_t)g0, sizeof(cx<double>) * (size_t)ldh, d + g0,
+                                         sizeof(cx<double>) * (size_t)ngw, sizeof(cx<double>) * (size_t)g, n,
+                                         cudaMemcpyDeviceToHost, c.copy_out));
+  }
+  GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.copy_out));
+  return finish_status(c, scond_host);
+}
+
 int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host) {
   if (nstate <= 0) return 0;
   const int rc = ortho_gs_steps(c, c0, ldc, nstate, scond_host != nullptr);

@@ -209,19 +209,21 @@ __global__ void k_mat_col_max(const double* __restrict__ M, int n, unsigned long
 
 // ---------------------------------------------------------------- digit planes
 // S operand: plane s, row j (state), columns k < K of the real view; exponent per state.
+// k0: first row of the slab (a multiple of 8); rows k0 .. k0+K-1 of Ar go to plane columns k0 ..
 __global__ void k_oz_slice_cols(const double* __restrict__ Ar, int lda, int K, int n,
-                                const unsigned long long* __restrict__ emax, size_t ks, uint4* __restrict__ out) {
+                                const unsigned long long* __restrict__ emax, size_t ks, uint4* __restrict__ out,
+                                int k0 = 0) {
   const int j = blockIdx.y;
   const int k = (blockIdx.x * blockDim.x + threadIdx.x) * 8;
   if (k >= K) return;
   const int e = exp_of_max(emax[j]);
-  const double* a = Ar + (size_t)j * lda + k;
+  const double* a = Ar + (size_t)j * lda + k0 + k;
   double x[8];
 #pragma unroll
   for (int q = 0; q < 8; ++q) x[q] = (k + q < K) ? a[q] : 0.0;
   uint4 d[OZ_SL];
   digits8(x, e, d);
-  const size_t plane = (size_t)n * ks / 8, off = ((size_t)j * ks + k) / 8;
+  const size_t plane = (size_t)n * ks / 8, off = ((size_t)j * ks + k0 + k) / 8;
 #pragma unroll
   for (int s = 0; s < OZ_SL; ++s) out[s * plane + off] = d[s];
 }
@@ -268,17 +270,18 @@ __global__ void k_oz_slice_rows(const double* __restrict__ Ar, int lda, int rows
 // The same slicing with the row exponents found in the same pass (n <= 256): block
 // (32 rows, ceil(n/16) column groups), thread (row, 16 states); the row maximum is
 // reduced over the column groups in shared memory and also stored to rmax.
+// rows r0 .. r1-1 (r1 <= rows; rows sets the plane stride)
 __global__ void __launch_bounds__(512) k_oz_slice_rows_max(const double* __restrict__ Ar, int lda, int rows, int n,
                                                            unsigned long long* __restrict__ rmax, size_t ks,
-                                                           uint4* __restrict__ out) {
+                                                           uint4* __restrict__ out, int r0, int r1) {
   __shared__ unsigned long long red[16][33];
-  const int r = blockIdx.x * 32 + threadIdx.x, k = threadIdx.y * 16;
+  const int r = r0 + blockIdx.x * 32 + threadIdx.x, k = threadIdx.y * 16;
   double x0[8], x1[8];
   unsigned long long mx = 0;
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
-    x0[q] = (r < rows && k + q < n) ? Ar[r + (size_t)(k + q) * lda] : 0.0;
-    x1[q] = (r < rows && k + 8 + q < n) ? Ar[r + (size_t)(k + 8 + q) * lda] : 0.0;
+    x0[q] = (r < r1 && k + q < n) ? Ar[r + (size_t)(k + q) * lda] : 0.0;
+    x1[q] = (r < r1 && k + 8 + q < n) ? Ar[r + (size_t)(k + 8 + q) * lda] : 0.0;
     const unsigned long long b0 = (unsigned long long)__double_as_longlong(x0[q]) & ~(1ull << 63);
     const unsigned long long b1 = (unsigned long long)__double_as_longlong(x1[q]) & ~(1ull << 63);
     mx = b0 > mx ? b0 : mx;
@@ -292,10 +295,10 @@ __global__ void __launch_bounds__(512) k_oz_slice_rows_max(const double* __restr
       mx = o > mx ? o : mx;
     }
     red[0][threadIdx.x] = mx;
-    if (r < rows) rmax[r] = mx;
+    if (r < r1) rmax[r] = mx;
   }
   __syncthreads();
-  if (r >= rows) return;
+  if (r >= r1) return;
   const int e = exp_of_max(red[0][threadIdx.x]);
   uint4 d0[OZ_SL], d1[OZ_SL];
   digits8(x0, e, d0);
@@ -342,6 +345,8 @@ struct OzParams {
   int ldo;
   int zero_row1;                 // mode 1: write 0 to row 1 (Im c(G=0) of the real view)
   int accumulate;                // mode 1: Cout += A M instead of Cout = A M
+  int sub_base;                  // mode 0: K offset of this launch, in sub-chunks
+  int rt0, nrt;                  // mode 1: row tiles rt0 .. rt0+nrt-1 (nrt = 0: every row tile)
   int* status;
 };
 
@@ -373,9 +378,9 @@ __device__ __forceinline__ OzUnit oz_unit(const OzParams& p, int u) {
     w.valid = w.nsub > 0;
     return w;
   }
-  const int nrt = (p.M + OZ_M - 1) / OZ_M, nct = (p.N + OZ_N - 1) / OZ_N;
+  const int nrt = p.nrt > 0 ? p.nrt : (p.M + OZ_M - 1) / OZ_M, nct = (p.N + OZ_N - 1) / OZ_N;
   if (u >= nrt * nct) return w;
-  const int rt = u / nct, ct = u % nct;  // row tile outer: the CTAs of one row tile share its planes in L2
+  const int rt = p.rt0 + u / nct, ct = u % nct;  // row tile outer: the CTAs of one row tile share its planes in L2
   w.m0 = rt * OZ_M;
   w.n0 = ct * OZ_N;
   const int kmax = p.upper ? min(p.K, w.n0 + OZ_N) : p.K;
@@ -390,7 +395,7 @@ __device__ __forceinline__ int oz_next_unit(const OzParams& p, int u) { return p
 // thread 0: the 16 TMA loads (8 A planes, 8 B planes) of one sub-chunk into buffer b
 __device__ __forceinline__ void oz_load(const CUtensorMap* tmA, const CUtensorMap* tmB, const OzParams& p,
                                         const OzUnit& w, int s, uint8_t* buf, uint64_t* bar) {
-  const int k = (w.sub0 + s) * OZ_KS;
+  const int k = (p.sub_base + w.sub0 + s) * OZ_KS;
   tc::mbar_expect_tx(bar, STAGE_BYTES);
 #pragma unroll 1
   for (int pl = 0; pl < OZ_SL; ++pl) {
@@ -595,6 +600,32 @@ __global__ void k_ozaki_xov_finalize(const long long* __restrict__ H, const long
   }
 }
 
+// S[i][j] (i <= j, mirrored) = the sum over R K ranges, in range order, of
+// 2 * 2^(E_i^r + E_j^r) (H_r 2^-35 + Lo_r 2^-63), minus Re c0_i Re c0_j
+__global__ void k_ozaki_syrk_finalize_ranges(const long long* __restrict__ H, const long long* __restrict__ Lo,
+                                             const unsigned long long* __restrict__ cmax, int R, int n,
+                                             const double* __restrict__ Ar, int lda, int geq0,
+                                             double* __restrict__ S, unsigned long long* __restrict__ scond_bits) {
+  const size_t nn = (size_t)n * n;
+  double mx = 0.0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nn; e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    if (i > j) continue;
+    double v = 0.0;
+    for (int r = 0; r < R; ++r)
+      v += 2.0 * fold_to_double(H[r * nn + e], Lo[r * nn + e],
+                                exp_of_max(cmax[(size_t)r * n + i]) + exp_of_max(cmax[(size_t)r * n + j]));
+    if (geq0) v -= Ar[(size_t)i * lda] * Ar[(size_t)j * lda];
+    S[(size_t)i * n + j] = v;
+    S[(size_t)j * n + i] = v;
+    mx = fmax(mx, fabs(i == j ? v - 1.0 : v));
+  }
+  if (scond_bits) {
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(scond_bits, (unsigned long long)__double_as_longlong(mx));
+  }
+}
+
 }  // namespace
 
 // Overlap matrix on the tensor cores, queued without a host synchronisation.
@@ -765,7 +796,8 @@ int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, 
   if (n <= 256) {
     ProfScope ps_(c, "k_oz_slice");
     k_oz_slice_rows_max<<<(rows + 31) / 32, dim3(32, (n + 15) / 16), 0, c.stream>>>(A, lda, rows, n, rmax, ks,
-                                                                                   static_cast<uint4*>(c.oz_a.p));
+                                                                                   static_cast<uint4*>(c.oz_a.p), 0,
+                                                                                   rows);
     GBCP_LAUNCH_CHECK(c);
   } else {
     {
@@ -813,6 +845,153 @@ int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, 
     ProfScope ps_(c, "k_ozaki_rmul");
     k_oz_tc<<<grid, OZ_THREADS, OZ_SMEM, c.stream>>>(ma, mb, p);
     GBCP_LAUNCH_CHECK(c);
+  }
+  return 0;
+}
+
+// S over the K ranges [kb[r], kb[r+1]) of the real view (boundaries multiples of
+// OZ_KS): range r gets its own column exponents, digit planes and int64 partial
+// sums once ready[r] (may be null) has completed on the stream, so that a host
+// upload of range r+1 overlaps range r's work; the ranges are added in order in
+// the finalize.  Queued without a host synchronisation.
+int ovlap_tc_ranges(Ctx& c, const double* Ar, int lda, int n, const int* kb, int R, const cudaEvent_t* ready,
+                    double* S, unsigned long long* scond_bits, int* status) {
+  const int K = kb[R];
+  const int nib = (n + OZ_M - 1) / OZ_M;
+  const int njb = (n + OZ_N - 1) / OZ_N;
+  int ntiles = 0;
+  for (int ib = 0; ib < nib; ++ib) ntiles += std::max(0, njb - 2 * ib);
+  const size_t nn = (size_t)n * n;
+  const size_t ks = ((size_t)K + 7) & ~size_t(7);
+  const size_t bytes = (size_t)R * (2 * nn * 8 + (size_t)n * 8);
+  if (!ensure(c, c.sparts, bytes) || !ensure(c, c.oz_a, sizeof(uint16_t) * OZ_SL * (size_t)n * ks)) return 6;
+  unsigned long long* Hacc = static_cast<unsigned long long*>(c.sparts.p);
+  unsigned long long* Lacc = Hacc + (size_t)R * nn;
+  unsigned long long* cmax = Lacc + (size_t)R * nn;
+  GBCP_CUDA_TRY(c, cudaMemsetAsync(Hacc, 0, bytes, c.stream));
+  CUtensorMap ma, mb;
+  if (!tmap_bf16_2d(&ma, c.oz_a.p, K, (long long)OZ_SL * n, (int)ks, OZ_KS, OZ_M, 64) ||
+      !tmap_bf16_2d(&mb, c.oz_a.p, K, (long long)OZ_SL * n, (int)ks, OZ_KS, OZ_N, 64)) {
+    c.err = "ovlap: tensor map encoding failed";
+    return 5;
+  }
+  allow_smem(k_oz_tc, OZ_SMEM);
+  for (int r = 0; r < R; ++r) {
+    const int k0 = kb[r], Kr = kb[r + 1] - kb[r];
+    if (Kr <= 0) continue;
+    if (ready && ready[r]) GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, ready[r], 0));
+    {
+      ProfScope ps_(c, "k_col_max");
+      const int kspl = std::max(1, std::min(64, (Kr + 4095) / 4096));
+      const int kper = (Kr + kspl - 1) / kspl;
+      k_col_max<<<dim3(n, kspl), 256, 0, c.stream>>>(Ar + k0, lda, Kr, n, kper, cmax + (size_t)r * n);
+      GBCP_LAUNCH_CHECK(c);
+    }
+    {
+      ProfScope ps_(c, "k_oz_slice");
+      k_oz_slice_cols<<<dim3((Kr / 8 + 255) / 256 + 1, n), 256, 0, c.stream>>>(
+          Ar, lda, Kr, n, cmax + (size_t)r * n, ks, static_cast<uint4*>(c.oz_a.p), k0);
+      GBCP_LAUNCH_CHECK(c);
+    }
+    const int total_subs = (Kr + OZ_KS - 1) / OZ_KS;
+    int nsplit = std::max(1, std::min((total_subs + OZ_SUBS - 1) / OZ_SUBS, 148 / std::max(1, ntiles)));
+    int subs_per = (total_subs + nsplit - 1) / nsplit;
+    subs_per = ((subs_per + OZ_SUBS - 1) / OZ_SUBS) * OZ_SUBS;
+    nsplit = (total_subs + subs_per - 1) / subs_per;
+    OzParams p{};
+    p.M = n;
+    p.N = n;
+    p.K = Kr;
+    p.mode = 0;
+    p.njb = njb;
+    p.subs_per = subs_per;
+    p.sub_base = k0 / OZ_KS;
+    p.Hacc = Hacc + (size_t)r * nn;
+    p.Lacc = Lacc + (size_t)r * nn;
+    p.status = status;
+    ProfScope ps_(c, "k_ozaki_syrk");
+    k_oz_tc<<<dim3(ntiles, nsplit), OZ_THREADS, OZ_SMEM, c.stream>>>(ma, mb, p);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  {
+    ProfScope ps_(c, "k_ozaki_syrk_finalize");
+    const int fb = std::max(1, std::min(1024, (int)((nn + 255) / 256)));
+    k_ozaki_syrk_finalize_ranges<<<fb, 256, 0, c.stream>>>(reinterpret_cast<const long long*>(Hacc),
+                                                           reinterpret_cast<const long long*>(Lacc), cmax, R, n, Ar,
+                                                           lda, c.geq0, S, scond_bits);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  return 0;
+}
+
+// C M by row ranges [rb[r], rb[r+1]) (boundaries multiples of OZ_M): done[r] (may
+// be null) is recorded once range r's rows of Cout are written, so that a host
+// download of range r overlaps the later ranges.  Otherwise as rmul_tc.
+int rmul_tc_ranges(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout,
+                   int ldo, int zero_row1, int* status, const int* rb, int R, const cudaEvent_t* done) {
+  const size_t ks = ((size_t)n + 7) & ~size_t(7);
+  const size_t bytes = ((size_t)rows + n) * 8;
+  if (!ensure(c, c.nl_a, bytes) || !ensure(c, c.oz_a, sizeof(uint16_t) * OZ_SL * (size_t)rows * ks) ||
+      !ensure(c, c.oz_b, sizeof(uint16_t) * OZ_SL * (size_t)n * ks))
+    return 6;
+  unsigned long long* rmax = static_cast<unsigned long long*>(c.nl_a.p);
+  unsigned long long* mcmax = rmax + rows;
+  {
+    ProfScope ps_(c, "k_mat_col_max");
+    k_mat_col_max<<<(n + 255) / 256, 256, 0, c.stream>>>(M, n, mcmax);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  {
+    ProfScope ps_(c, "k_oz_slice");
+    if (n > 256) {  // no fused row-maximum slicer: all rows up front
+      k_row_max<<<(rows + 255) / 256, 256, 0, c.stream>>>(A, lda, rows, n, rmax);
+      GBCP_LAUNCH_CHECK(c);
+      k_oz_slice_rows<<<dim3((rows + 127) / 128, (n + 15) / 16), 128, 0, c.stream>>>(A, lda, rows, n, rmax, ks,
+                                                                                    static_cast<uint4*>(c.oz_a.p));
+      GBCP_LAUNCH_CHECK(c);
+    }
+    k_oz_slice_mat<<<dim3((n + 127) / 128, (n + 7) / 8), 128, 0, c.stream>>>(M, n, mcmax, ks,
+                                                                            static_cast<uint4*>(c.oz_b.p));
+    GBCP_LAUNCH_CHECK(c);
+  }
+  CUtensorMap ma, mb;
+  if (!tmap_bf16_2d(&ma, c.oz_a.p, n, (long long)OZ_SL * rows, (int)ks, OZ_KS, OZ_M, 64) ||
+      !tmap_bf16_2d(&mb, c.oz_b.p, n, (long long)OZ_SL * n, (int)ks, OZ_KS, OZ_N, 64)) {
+    c.err = "C.M: tensor map encoding failed";
+    return 5;
+  }
+  allow_smem(k_oz_tc, OZ_SMEM);
+  const int nsm = c.nsm > 0 ? c.nsm : 148;
+  const int nct = (n + OZ_N - 1) / OZ_N;
+  for (int r = 0; r < R; ++r) {
+    const int r0 = rb[r], r1 = rb[r + 1];
+    if (r1 > r0) {
+      if (n <= 256) {
+        ProfScope ps_(c, "k_oz_slice");
+        k_oz_slice_rows_max<<<(r1 - r0 + 31) / 32, dim3(32, (n + 15) / 16), 0, c.stream>>>(
+            A, lda, rows, n, rmax, ks, static_cast<uint4*>(c.oz_a.p), r0, r1);
+        GBCP_LAUNCH_CHECK(c);
+      }
+      OzParams p{};
+      p.M = rows;
+      p.N = n;
+      p.K = n;
+      p.mode = 1;
+      p.upper = upper;
+      p.eA = rmax;
+      p.eB = mcmax;
+      p.Cout = Cout;
+      p.ldo = ldo;
+      p.zero_row1 = zero_row1;
+      p.status = status;
+      p.rt0 = r0 / OZ_M;
+      p.nrt = (r1 - r0 + OZ_M - 1) / OZ_M;
+      const int grid = std::max(1, std::min(p.nrt * nct, nsm));
+      ProfScope ps_(c, "k_ozaki_rmul");
+      k_oz_tc<<<grid, OZ_THREADS, OZ_SMEM, c.stream>>>(ma, mb, p);
+      GBCP_LAUNCH_CHECK(c);
+    }
+    if (done && done[r]) GBCP_CUDA_TRY(c, cudaEventRecord(done[r], c.stream));
   }
   return 0;
 }
