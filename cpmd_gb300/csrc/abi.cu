@@ -631,24 +631,40 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
   int rc = 0, saved_batch = 0;
   if (mem == GBCP_MEM_HOST) {
     void* tf;
-    void* tv;
     if ((rc = stage_in(c, c.st_f, f, sizeof(double) * nstate, &tf))) return rc;
-    if ((rc = stage_in(c, c.st_vpot, vpot, sizeof(double) * nnr1, &tv))) return rc;
-    if (!gbcp::ensure(c, c.st_c0, sizeof(cx<double>) * (size_t)c.ngw * nstate) ||
+    if (!gbcp::ensure(c, c.st_vpot, sizeof(double) * nnr1) ||
+        !gbcp::ensure(c, c.st_c0, sizeof(cx<double>) * (size_t)c.ngw * nstate) ||
         !gbcp::ensure(c, c.st_c2, sizeof(cx<double>) * (size_t)c.ngw * nstate))
       return GBCP_ERR_NOMEM;
+    void* tv = c.st_vpot.p;
     cx<double>* t0 = static_cast<cx<double>*>(c.st_c0.p);
     cx<double>* t2 = static_cast<cx<double>*>(c.st_c2.p);
     const int sp = stage_chunk(c, nstate);
     const int nb = ((nstate + 1) / 2 + sp - 1) / sp;
-    if ((rc = pipe_prepare(c, nb))) return rc;
+    // events: [0] ordering, [1, nb] c0 chunks, [nb+1, 2nb] C2 downloads, [2nb+1, 3nb] C2 uploads,
+    // [3nb+1] V(r), last: the final download
+    if ((rc = pipe_prepare(c, 2 * nb + 1))) return rc;
     c.stage_pairs = sp;
-    for (int b = 0; b < nb; ++b) {
-      const int s0 = 2 * sp * b, ns = std::min(2 * sp, nstate - s0);
-      if ((rc = pipe_up(c, t0, c0, ldc, s0, ns)) || (rc = pipe_up(c, t2, c2, ldc2, s0, ns))) return rc;
-      GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[1 + b], c.copy));
+    // copy order: the states of chunk 0, V(r), then chunk b's C2 columns behind chunk b+1's
+    // states, so that the first transforms start after one chunk and each decode finds its C2
+    for (int b = 0; b <= nb; ++b) {
+      if (b < nb) {
+        const int s0 = 2 * sp * b, ns = std::min(2 * sp, nstate - s0);
+        if ((rc = pipe_up(c, t0, c0, ldc, s0, ns))) return rc;
+        GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[1 + b], c.copy));
+      }
+      if (b == 0) {
+        GBCP_CUDA_TRY(c, cudaMemcpyAsync(tv, vpot, sizeof(double) * nnr1, cudaMemcpyHostToDevice, c.copy));
+        GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[3 * nb + 1], c.copy));
+      } else {
+        const int s0 = 2 * sp * (b - 1), ns = std::min(2 * sp, nstate - s0);
+        if ((rc = pipe_up(c, t2, c2, ldc2, s0, ns))) return rc;
+        GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[2 * nb + b], c.copy));
+      }
     }
     c.batch_ready = c.pipe_ev.data() + 1;
+    c.batch_c2_ready = c.pipe_ev.data() + 2 * nb + 1;
+    c.vpot_ready = c.pipe_ev[3 * nb + 1];
     saved_batch = c.batch;
     c.batch = sp;
     // C2 columns of batch b go back as soon as its decode is queued
@@ -670,6 +686,8 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
   }
   rc = gbcp::band_vpsi(c, dc0, l0, dc2, l2, df, dv, nstate);
   c.batch_ready = nullptr;
+  c.batch_c2_ready = nullptr;
+  c.vpot_ready = nullptr;
   c.batch_done = nullptr;
   if (saved_batch) c.batch = saved_batch;
   if (mem == GBCP_MEM_HOST) {

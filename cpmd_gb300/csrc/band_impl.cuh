@@ -622,22 +622,28 @@ int vpsi_t(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, cons
   const int npairs_total = (nstate + 1) / 2;
   int rc = ensure_band_buffers<T>(c, std::min(c.batch, npairs_total));
   if (rc) return rc;
-  // V(r) in the transform precision, converted once per call
+  // V(r) in the transform precision, converted once per call before the first
+  // x-stage (with host staging V(r) arrives behind the first chunk of states)
   const T* vT = reinterpret_cast<const T*>(vpot);
-  if constexpr (sizeof(T) == 4) {
-    const size_t nnr = (size_t)c.kr[0] * c.kr[1] * c.kr[2];
-    if (!ensure(c, c.st_vf, sizeof(float) * nnr)) return 6;
-    ProfScope ps_(c, "k_v_to_float");
-    k_v_to_float<<<std::max<size_t>(1, std::min<size_t>(2048, (nnr + 255) / 256)), 256, 0, c.stream>>>(
-        vpot, static_cast<float*>(c.st_vf.p), nnr);
-    GBCP_LAUNCH_CHECK(c);
-    vT = reinterpret_cast<const T*>(c.st_vf.p);
-  }
+  auto prepare_v = [&]() -> int {
+    if (c.vpot_ready) GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.vpot_ready, 0));
+    if constexpr (sizeof(T) == 4) {
+      const size_t nnr = (size_t)c.kr[0] * c.kr[1] * c.kr[2];
+      if (!ensure(c, c.st_vf, sizeof(float) * nnr)) return 6;
+      ProfScope ps_(c, "k_v_to_float");
+      k_v_to_float<<<std::max<size_t>(1, std::min<size_t>(2048, (nnr + 255) / 256)), 256, 0, c.stream>>>(
+          vpot, static_cast<float*>(c.st_vf.p), nnr);
+      GBCP_LAUNCH_CHECK(c);
+      vT = reinterpret_cast<const T*>(c.st_vf.p);
+    }
+    return 0;
+  };
   for (int p0 = 0; p0 < npairs_total; p0 += c.batch) {
     const int np = std::min(c.batch, npairs_total - p0);
     const int s0 = 2 * p0;
     if ((rc = zinv_staged<T>(c, c0, ldc, p0, nstate, np))) return rc;
     if ((rc = yinv<T>(c, np))) return rc;
+    if (p0 == 0 && (rc = prepare_v())) return rc;
     if ((rc = xvx<T>(c, np, vpot, vT))) return rc;
     if ((rc = yfwd<T>(c, np))) return rc;
     if ((rc = zfwd<T>(c, np))) return rc;
@@ -648,6 +654,7 @@ int vpsi_t(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, cons
       const int sp = c.stage_pairs;
       for (int q0 = p0; q0 < p0 + np; q0 += sp) {
         const int nq = std::min(sp, p0 + np - q0);
+        if (c.batch_c2_ready) GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.batch_c2_ready[q0 / sp], 0));
         if ((rc = launch_decode<T>(c, nq, c0, ldc, c2, ldc2, f, 2 * q0, nstate, q0 - p0))) return rc;
         if (c.batch_done && (rc = c.batch_done(q0 / sp))) return rc;
       }

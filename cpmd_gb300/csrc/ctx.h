@@ -120,6 +120,8 @@ struct Ctx {
   cudaStream_t copy = nullptr, copy_out = nullptr;  // uploads, downloads (separate copy engines)
   std::vector<cudaEvent_t> pipe_ev;
   const cudaEvent_t* batch_ready = nullptr;
+  const cudaEvent_t* batch_c2_ready = nullptr;  // vpsi: the decode of chunk q waits for its C2 columns
+  cudaEvent_t vpot_ready = nullptr;             // vpsi: the first x-stage waits for V(r)
   std::function<int(int)> batch_done;
   int stage_pairs = 0;  // state pairs per staging chunk (a chunk never spans two launch batches)
   // profiling
