@@ -532,9 +532,28 @@ int pipe_up(Ctx& c, cx<double>* d, const double* h, int ld, int s0, int ns) {
 // pairs per staging chunk of a host-memory call: about four chunks, so that the whole
 // stage chain of one chunk overlaps the copies of the next; host-memory calls launch the
 // band loop chunk by chunk (their launch batch is the chunk)
-int stage_chunk(const Ctx& c, int nstate) {
+// Staging chunks of a host-memory band-loop call, as pair ranges: a small first
+// chunk (its upload is the only one the transforms wait for) and three equal ones,
+// none above the launch batch.  Returns the number of chunks.
+int stage_plan(Ctx& c, int nstate) {
   const int npairs = (nstate + 1) / 2;
-  return std::max(1, std::min(c.batch, (npairs + 3) / 4));
+  std::vector<int>& b = c.stage_bounds;
+  b.assign(1, 0);
+  if (npairs <= 0) return 0;
+  const int first = std::max(1, std::min(c.batch, npairs / 16));
+  b.push_back(first);
+  const int rest = npairs - first;
+  if (rest > 0) {
+    const int per = std::min(c.batch, (rest + 2) / 3);
+    for (int p = first + per; p < npairs; p += per) b.push_back(p);
+    b.push_back(npairs);
+  }
+  return (int)b.size() - 1;
+}
+int stage_max(const Ctx& c) {
+  int m = 1;
+  for (size_t q = 0; q + 1 < c.stage_bounds.size(); ++q) m = std::max(m, c.stage_bounds[q + 1] - c.stage_bounds[q]);
+  return m;
 }
 
 int finish(Ctx& c, int rc) {
@@ -576,18 +595,16 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
         !gbcp::ensure(c, c.st_c0, sizeof(cx<double>) * (size_t)c.ngw * std::max(nstate, 1)))
       return GBCP_ERR_NOMEM;
     cx<double>* t = static_cast<cx<double>*>(c.st_c0.p);
-    const int sp = stage_chunk(c, nstate);
-    const int nb = ((nstate + 1) / 2 + sp - 1) / sp;
+    const int nb = stage_plan(c, nstate);
     if ((rc = pipe_prepare(c, nb))) return rc;
     for (int b = 0; b < nb; ++b) {
-      const int s0 = 2 * sp * b, ns = std::min(2 * sp, nstate - s0);
+      const int s0 = 2 * c.stage_bounds[b], ns = std::min(2 * c.stage_bounds[b + 1], nstate) - s0;
       if ((rc = pipe_up(c, t, c0, ldc, s0, ns))) return rc;
       GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[1 + b], c.copy));
     }
-    c.stage_pairs = sp;
     c.batch_ready = c.pipe_ev.data() + 1;
     saved_batch = c.batch;
-    c.batch = sp;
+    c.batch = stage_max(c);
     dc0 = t;
     df = static_cast<double*>(tf);
     drho = static_cast<double*>(c.st_rho.p);
@@ -639,17 +656,20 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
     void* tv = c.st_vpot.p;
     cx<double>* t0 = static_cast<cx<double>*>(c.st_c0.p);
     cx<double>* t2 = static_cast<cx<double>*>(c.st_c2.p);
-    const int sp = stage_chunk(c, nstate);
-    const int nb = ((nstate + 1) / 2 + sp - 1) / sp;
+    const int nb = stage_plan(c, nstate);
+    auto chunk = [&](int b, int* s0, int* ns) {
+      *s0 = 2 * c.stage_bounds[b];
+      *ns = std::min(2 * c.stage_bounds[b + 1], nstate) - *s0;
+    };
     // events: [0] ordering, [1, nb] c0 chunks, [nb+1, 2nb] C2 downloads, [2nb+1, 3nb] C2 uploads,
     // [3nb+1] V(r), last: the final download
     if ((rc = pipe_prepare(c, 2 * nb + 1))) return rc;
-    c.stage_pairs = sp;
     // copy order: the states of chunk 0, V(r), then chunk b's C2 columns behind chunk b+1's
     // states, so that the first transforms start after one chunk and each decode finds its C2
     for (int b = 0; b <= nb; ++b) {
+      int s0, ns;
       if (b < nb) {
-        const int s0 = 2 * sp * b, ns = std::min(2 * sp, nstate - s0);
+        chunk(b, &s0, &ns);
         if ((rc = pipe_up(c, t0, c0, ldc, s0, ns))) return rc;
         GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[1 + b], c.copy));
       }
@@ -657,7 +677,7 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
         GBCP_CUDA_TRY(c, cudaMemcpyAsync(tv, vpot, sizeof(double) * nnr1, cudaMemcpyHostToDevice, c.copy));
         GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[3 * nb + 1], c.copy));
       } else {
-        const int s0 = 2 * sp * (b - 1), ns = std::min(2 * sp, nstate - s0);
+        chunk(b - 1, &s0, &ns);
         if ((rc = pipe_up(c, t2, c2, ldc2, s0, ns))) return rc;
         GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[2 * nb + b], c.copy));
       }
@@ -666,10 +686,10 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
     c.batch_c2_ready = c.pipe_ev.data() + 2 * nb + 1;
     c.vpot_ready = c.pipe_ev[3 * nb + 1];
     saved_batch = c.batch;
-    c.batch = sp;
+    c.batch = stage_max(c);
     // C2 columns of batch b go back as soon as its decode is queued
-    c.batch_done = [&c, c2, ldc2, nstate, t2, nb, sp](int b) -> int {
-      const int s0 = 2 * sp * b, ns = std::min(2 * sp, nstate - s0);
+    c.batch_done = [&c, c2, ldc2, nstate, t2, nb](int b) -> int {
+      const int s0 = 2 * c.stage_bounds[b], ns = std::min(2 * c.stage_bounds[b + 1], nstate) - s0;
       cudaEvent_t e = c.pipe_ev[1 + nb + b];
       GBCP_CUDA_TRY(c, cudaEventRecord(e, c.stream));
       GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.copy_out, e, 0));

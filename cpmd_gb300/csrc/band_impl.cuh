@@ -591,14 +591,24 @@ template <typename T> int zfwd(Ctx& c, int np) { GBCP_DISPATCH(launch_zfwd, T, b
 // staging chunk after that chunk's columns have arrived
 template <typename T> int zinv_staged(Ctx& c, const cx<double>* c0, int ldc, int p0, int nstate, int np) {
   if (!c.batch_ready) return zinv<T>(c, c0, ldc, 2 * p0, nstate, np);
-  const int sp = c.stage_pairs;
-  for (int q0 = p0; q0 < p0 + np; q0 += sp) {
-    const int nq = std::min(sp, p0 + np - q0);
-    GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.batch_ready[q0 / sp], 0));
-    const int rc = zinv<T>(c, c0, ldc, 2 * q0, nstate, nq, q0 - p0);
+  const std::vector<int>& b = c.stage_bounds;
+  for (size_t q = 0; q + 1 < b.size(); ++q) {
+    const int q0 = std::max(b[q], p0), q1 = std::min(b[q + 1], p0 + np);
+    if (q1 <= q0) continue;
+    GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.batch_ready[q], 0));
+    const int rc = zinv<T>(c, c0, ldc, 2 * q0, nstate, q1 - q0, q0 - p0);
     if (rc) return rc;
   }
   return 0;
+}
+
+// pairs of the launch batch starting at pair p0: c.batch, or with host staging the staging chunk
+inline int launch_pairs(const Ctx& c, int p0, int npairs_total) {
+  if (c.batch_ready) {
+    for (size_t q = 0; q + 1 < c.stage_bounds.size(); ++q)
+      if (c.stage_bounds[q] == p0) return c.stage_bounds[q + 1] - p0;
+  }
+  return std::min(c.batch, npairs_total - p0);
 }
 
 template <typename T>
@@ -606,8 +616,8 @@ int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f,
   const int npairs_total = (nstate + 1) / 2;
   int rc = ensure_band_buffers<T>(c, std::min(c.batch, npairs_total));
   if (rc) return rc;
-  for (int p0 = 0; p0 < npairs_total; p0 += c.batch) {
-    const int np = std::min(c.batch, npairs_total - p0);
+  for (int p0 = 0, np = 0; p0 < npairs_total; p0 += np) {
+    np = launch_pairs(c, p0, npairs_total);
     const int s0 = 2 * p0;
     if ((rc = zinv_staged<T>(c, c0, ldc, p0, nstate, np))) return rc;
     if ((rc = yinv<T>(c, np))) return rc;
@@ -638,8 +648,8 @@ int vpsi_t(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, cons
     }
     return 0;
   };
-  for (int p0 = 0; p0 < npairs_total; p0 += c.batch) {
-    const int np = std::min(c.batch, npairs_total - p0);
+  for (int p0 = 0, np = 0; p0 < npairs_total; p0 += np) {
+    np = launch_pairs(c, p0, npairs_total);
     const int s0 = 2 * p0;
     if ((rc = zinv_staged<T>(c, c0, ldc, p0, nstate, np))) return rc;
     if ((rc = yinv<T>(c, np))) return rc;
@@ -651,12 +661,13 @@ int vpsi_t(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, cons
       if ((rc = launch_decode<T>(c, np, c0, ldc, c2, ldc2, f, s0, nstate))) return rc;
     } else {
       // host staging: decode per staging chunk, each followed by its download
-      const int sp = c.stage_pairs;
-      for (int q0 = p0; q0 < p0 + np; q0 += sp) {
-        const int nq = std::min(sp, p0 + np - q0);
-        if (c.batch_c2_ready) GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.batch_c2_ready[q0 / sp], 0));
-        if ((rc = launch_decode<T>(c, nq, c0, ldc, c2, ldc2, f, 2 * q0, nstate, q0 - p0))) return rc;
-        if (c.batch_done && (rc = c.batch_done(q0 / sp))) return rc;
+      const std::vector<int>& b = c.stage_bounds;
+      for (size_t q = 0; q + 1 < b.size(); ++q) {
+        const int q0 = std::max(b[q], p0), q1 = std::min(b[q + 1], p0 + np);
+        if (q1 <= q0) continue;
+        if (c.batch_c2_ready) GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.batch_c2_ready[q], 0));
+        if ((rc = launch_decode<T>(c, q1 - q0, c0, ldc, c2, ldc2, f, 2 * q0, nstate, q0 - p0))) return rc;
+        if (c.batch_done && (rc = c.batch_done((int)q))) return rc;
       }
     }
   }

@@ -123,7 +123,7 @@ struct Ctx {
   const cudaEvent_t* batch_c2_ready = nullptr;  // vpsi: the decode of chunk q waits for its C2 columns
   cudaEvent_t vpot_ready = nullptr;             // vpsi: the first x-stage waits for V(r)
   std::function<int(int)> batch_done;
-  int stage_pairs = 0;  // state pairs per staging chunk (a chunk never spans two launch batches)
+  std::vector<int> stage_bounds;  // staging chunks as pair ranges [b[q], b[q+1]); each is one launch batch
   // profiling
   bool prof = false;
   std::vector<ProfRec> prof_live;
