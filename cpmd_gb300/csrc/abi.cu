@@ -602,9 +602,7 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
       if ((rc = pipe_up(c, t, c0, ldc, s0, ns))) return rc;
       GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[1 + b], c.copy));
     }
-    c.batch_ready = c.pipe_ev.data() + 1;
-    saved_batch = c.batch;
-    c.batch = stage_max(c);
+    c.batch_ready = c.pipe_ev.data() + 1;  // launch batches stay c.batch pairs (see rhoofr_t)
     dc0 = t;
     df = static_cast<double*>(tf);
     drho = static_cast<double*>(c.st_rho.p);

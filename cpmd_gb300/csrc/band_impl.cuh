@@ -411,10 +411,11 @@ int launch_zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int n
   return 0;
 }
 
-template <typename T, int NC> int launch_yinv(Ctx& c, int np) {
+template <typename T, int NC> int launch_yinv(Ctx& c, int np, int poff) {
   const GeoDev& g = c.geo;
-  const cx<T>* zb = static_cast<const cx<T>*>(c.zbuf.p);
-  cx<T>* yb = static_cast<cx<T>*>(c.ybuf.p);
+  // pairs poff .. poff+np-1 of the launch batch
+  const cx<T>* zb = static_cast<const cx<T>*>(c.zbuf.p) + (size_t)poff * g.n3 * g.ncol;
+  cx<T>* yb = static_cast<cx<T>*>(c.ybuf.p) + (size_t)poff * g.n3 * g.n2 * g.nslot;
   ProfScope ps_(c, "k_yinv");
   if constexpr (NC > 0) {
     constexpr size_t sm = fs_smem<T, NC>(1, 1);
@@ -577,7 +578,9 @@ int launch_decode(Ctx& c, int np, const cx<double>* c0, int ldc, cx<double>* c2,
 template <typename T> int zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int np, int poff = 0) {
   GBCP_DISPATCH(launch_zinv, T, band_len(c, c.nr[2]), c, c0, ldc, s0, nstate, np, poff)
 }
-template <typename T> int yinv(Ctx& c, int np) { GBCP_DISPATCH(launch_yinv, T, band_len(c, c.nr[1]), c, np) }
+template <typename T> int yinv(Ctx& c, int np, int poff = 0) {
+  GBCP_DISPATCH(launch_yinv, T, band_len(c, c.nr[1]), c, np, poff)
+}
 template <typename T> int xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho) {
   GBCP_DISPATCH(launch_xinv_rho, T, band_len(c, c.nr[0]), c, np, s0, nstate, f, rho)
 }
@@ -617,10 +620,23 @@ int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f,
   int rc = ensure_band_buffers<T>(c, std::min(c.batch, npairs_total));
   if (rc) return rc;
   for (int p0 = 0, np = 0; p0 < npairs_total; p0 += np) {
-    np = launch_pairs(c, p0, npairs_total);
+    np = std::min(c.batch, npairs_total - p0);
     const int s0 = 2 * p0;
-    if ((rc = zinv_staged<T>(c, c0, ldc, p0, nstate, np))) return rc;
-    if ((rc = yinv<T>(c, np))) return rc;
+    if (!c.batch_ready) {
+      if ((rc = zinv<T>(c, c0, ldc, s0, nstate, np))) return rc;
+      if ((rc = yinv<T>(c, np))) return rc;
+    } else {
+      // host staging: Z and Y stages of each staging chunk as its states land; the
+      // density x-stage (which gains most from many pairs per launch) once per batch
+      const std::vector<int>& b = c.stage_bounds;
+      for (size_t q = 0; q + 1 < b.size(); ++q) {
+        const int q0 = std::max(b[q], p0), q1 = std::min(b[q + 1], p0 + np);
+        if (q1 <= q0) continue;
+        GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.batch_ready[q], 0));
+        if ((rc = zinv<T>(c, c0, ldc, 2 * q0, nstate, q1 - q0, q0 - p0))) return rc;
+        if ((rc = yinv<T>(c, q1 - q0, q0 - p0))) return rc;
+      }
+    }
     if ((rc = xinv_rho<T>(c, np, s0, nstate, f, rho))) return rc;
   }
   return 0;
