@@ -172,7 +172,7 @@ def run_reference(args, rank, world):
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
 # mixed config-1 kernels, from one ncu capture of this script's own command
 # (python bench.py --steps 2 --warmup 3 --fp64-steps 1 --e2e-steps 1 --no-cpu --no-extras).
-NCU_TRAFFIC = {"k_xvx": 412.851968e6 + 349.319936e6}
+NCU_TRAFFIC = {"k_xvx": 412.769536e6 + 348.129792e6}
 
 
 def kernel_bytes(name: str, geo: dict, np_: int, s: int) -> float:
