@@ -50,16 +50,19 @@ __device__ __forceinline__ int pivot_bad(double d, double thr) {
 }
 
 // Factor + invert the diagonal block k: U_kk -> Uw (upper, zero below),
-// U_kk^{-1} -> X (diagonal block).  Four warps, lane = column.
+// U_kk^{-1} -> X (diagonal block).  Eight warps, lane = column.
 // Row i of the shared array z holds the forward-substitution accumulators
 // Y[i][c] of Y = U_kk^{-T} for c < i and the matrix entries A[i][c] for c >= i;
 // after step q row q is final: Y[q][c] (c < q), Y[q][q] = d^{-1/2}, U[q][c] (c > q).
 //   Step q: warp 0 applies row q-1 to row q (one FMA per lane), takes the pivot
-//   d = A[q][q] and scales the row by d^{-1/2} (one multiply per lane).  Warps 1-3
-//   meanwhile apply row q-1 to rows i = q+1..31 round-robin, one predicated FMA
-//   per row: z[i][c] -= U[q-1][i] z[q-1][c] for c >= i (matrix) and c < q (Y).
-//   One barrier per step; the pivot chain is one FMA, the rsqrt and one multiply.
-__global__ void __launch_bounds__(4 * B) k_chol_diag(const double* __restrict__ S, double* __restrict__ Uw,
+//   d = A[q][q] and scales the row by d^{-1/2} (one multiply per lane).  The six
+//   warps on the other three SM sub-partitions (warps 1-3 and 5-7; warp 4 shares
+//   warp 0's FP64 unit and stays idle) meanwhile apply row q-1 to rows
+//   i = q+1..31 round-robin, one predicated FMA per row: z[i][c] -= U[q-1][i]
+//   z[q-1][c] for c >= i (matrix) and c < q (Y).  One barrier per step; the pivot
+//   chain is one FMA, the rsqrt and one multiply, and no updater has more than
+//   five rows.
+__global__ void __launch_bounds__(8 * B) k_chol_diag(const double* __restrict__ S, double* __restrict__ Uw,
                                                      double* __restrict__ X, const double* __restrict__ diag0, int n,
                                                      int k, int* __restrict__ status) {
   __shared__ double z[B][B + 1];
@@ -67,18 +70,18 @@ __global__ void __launch_bounds__(4 * B) k_chol_diag(const double* __restrict__ 
   __shared__ int bad_sh;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int base = k * B;
-  // all global loads in flight together (rows r = w + 4 t, lane = column)
-  double v[B / 4];
+  // all global loads in flight together (rows r = w + 8 t, lane = column)
+  double v[B / 8];
 #pragma unroll
-  for (int t = 0; t < B / 4; ++t) {
-    const int r = w + 4 * t, i = base + r, j = base + lane;
+  for (int t = 0; t < B / 8; ++t) {
+    const int r = w + 8 * t, i = base + r, j = base + lane;
     v[t] = (lane >= r && i < n && j < n) ? S[(size_t)i * n + j] : 0.0;
   }
   const double d0 = (w == 0 && base + lane < n) ? diag0[base + lane] : 1.0;
   if (failed(status)) return;
 #pragma unroll
-  for (int t = 0; t < B / 4; ++t) {
-    const int r = w + 4 * t, i = base + r, j = base + lane;
+  for (int t = 0; t < B / 8; ++t) {
+    const int r = w + 8 * t, i = base + r, j = base + lane;
     z[r][lane] = (i < n && j < n) ? v[t] : (r == lane ? 1.0 : 0.0);
   }
   const double thr = 0x1p-46 * d0;  // warp 0, lane r: pivot threshold of row r
@@ -99,14 +102,16 @@ __global__ void __launch_bounds__(4 * B) k_chol_diag(const double* __restrict__ 
         z[q][lane] = (lane == q) ? inv : o;
         if (lane == q) udiag[q] = o;
       }
-    } else if (q > 0) {
-      // rows i = q + w + 3 t (q+1 .. 31, at most 10 per warp): loads first, then the FMAs
-      constexpr int T = (B - 2 + 2) / 3;
+    } else if (q > 0 && w != 4) {
+      // updater u = 0..5: rows i = q + 1 + u + 6 t (q+1 .. 31, at most 5 per warp):
+      // loads first, then the FMAs
+      const int u = (w < 4) ? w - 1 : w - 2;
+      constexpr int T = (B - 2 + 5) / 6;
       const double rv = z[q - 1][lane];
       double cf[T], zv[T];
 #pragma unroll
       for (int t = 0; t < T; ++t) {
-        const int i = q + w + 3 * t;
+        const int i = q + 1 + u + 6 * t;
         if (i < B) {
           cf[t] = z[q - 1][i];
           zv[t] = z[i][lane];
@@ -114,7 +119,7 @@ __global__ void __launch_bounds__(4 * B) k_chol_diag(const double* __restrict__ 
       }
 #pragma unroll
       for (int t = 0; t < T; ++t) {
-        const int i = q + w + 3 * t;
+        const int i = q + 1 + u + 6 * t;
         if (i < B && (lane >= i || lane < q)) z[i][lane] = fma(-cf[t], rv, zv[t]);
       }
     }
@@ -125,7 +130,7 @@ __global__ void __launch_bounds__(4 * B) k_chol_diag(const double* __restrict__ 
     if (threadIdx.x == 0) atomicExch(status, bad_sh);
     return;
   }
-  for (int e = threadIdx.x; e < B * B; e += 4 * B) {
+  for (int e = threadIdx.x; e < B * B; e += 8 * B) {
     const int r = e / B, cc = e - r * B, i = base + r, j = base + cc;
     if (i < n && j < n) {
       Uw[(size_t)i * n + j] = (cc > r) ? z[r][cc] : (cc == r ? udiag[r] : 0.0);
@@ -279,7 +284,7 @@ int chol_inverse(Ctx& c, double* S, double* X, int n) {
   for (int k = 0; k < nb; ++k) {
     {
       ProfScope ps_(c, "k_chol_diag");
-      k_chol_diag<<<1, 4 * B, 0, c.stream>>>(S, Uw, X, diag0, n, k, c.d_info);
+      k_chol_diag<<<1, 8 * B, 0, c.stream>>>(S, Uw, X, diag0, n, k, c.d_info);
       GBCP_LAUNCH_CHECK(c);
     }
     const int m0 = nb - k - 1;
