@@ -368,7 +368,7 @@ int gbcp_ctx_destroy(gbcp_ctx* h) {
   if (c.stream) cudaStreamSynchronize(c.stream);
   for (void* p : c.dev_allocs) cudaFree(p);
   gbcp::Scratch* all[] = {&c.zbuf, &c.ybuf, &c.qbuf, &c.st_c0, &c.st_c2, &c.st_rho, &c.st_vpot, &c.st_f,
-                          &c.st_misc, &c.st_misc2, &c.st_vf, &c.red, &c.red2, &c.smat, &c.smat2, &c.smat3, &c.sparts, &c.cscr, &c.cdiag, &c.cwork, &c.xr_part, &c.xr_tk, &c.rt_mats, &c.oz_a, &c.oz_b,
+                          &c.st_misc, &c.st_misc2, &c.st_vf, &c.red, &c.red2, &c.smat, &c.smat2, &c.smat3, &c.sparts, &c.cscr, &c.cdiag, &c.cwork, &c.xr_part, &c.xr_tk, &c.rt_mats, &c.en_g3, &c.oz_a, &c.oz_b,
                           &c.nl_a, &c.nl_b, &c.nl_c, &c.nl_d, &c.nl_ta, &c.nl_tb, &c.nl_tp, &c.en_rho, &c.en_a, &c.en_b, &c.en_veff,
                           &c.en_red, &c.en_ei, &c.en_fp, &c.en_idx, &c.en_in[0], &c.en_in[1], &c.en_in[2],
                           &c.en_in[3], &c.en_in[4]};
@@ -413,6 +413,10 @@ int gbcp_set_option(gbcp_ctx* h, int key, int value) {
   }
   if (key == GBCP_OPT_XCHUNKS && value >= 0 && value <= 8) {
     c.xr_chunks = value;
+    return GBCP_OK;
+  }
+  if (key == GBCP_OPT_XC && (value == 0 || value == 1)) {
+    c.xc = value;
     return GBCP_OK;
   }
   return set_err(h, GBCP_ERR_ARG, "set_option: unknown key or value");

@@ -77,6 +77,7 @@ struct Ctx {
   int gemm_mode = -1;  // overlap GEMM: -1 by precision (mixed -> tensor cores), 0 FP64 SIMT, 1 tensor cores
   int nsm = 0;         // SMs of the device
   int xr_chunks = 0;   // density x-stage pair chunks: 0 = chosen per launch
+  int xc = 0;          // energy functional: 0 LDA (Slater + Perdew-Zunger), 1 PBE
   int fft_engine = 0;  // band-loop FFTs: 0 four-step where a plan exists, else Stockham; 2 Stockham always
   cudaStream_t stream = nullptr;  // stream all work is queued on
   cudaStream_t own = nullptr;     // the context's own stream
@@ -114,6 +115,7 @@ struct Ctx {
   const short4* dmill = nullptr;   // Miller indices (x, y, z, 0)
   const double* dg2 = nullptr;     // |G|^2 in bohr^-2
   Scratch en_rho, en_a, en_b, en_veff, en_red, en_ei, en_fp, en_idx, en_in[5];
+  Scratch en_g3;  // PBE: gradient / flux grids (3 complex FFT grids)
   std::string err;
   // host-staged pipelining (abi.cu): the Z stage of staging chunk q waits for batch_ready[q];
   // vpsi calls batch_done(q) once the decode of chunk q is queued

@@ -11,7 +11,12 @@
 //   E_H      = Omega sum_{G != 0, half} 4 pi |rho(G)|^2 / G^2   (ppener: eh, scg)
 //   E_xc     = Omega/N sum_r rho eps_xc(rho): Slater exchange (alpha = 2/3,
 //              cp_lda_exchange_utils.mod.F90:74-97) + Perdew-Zunger correlation
-//              (cp_lda_correlation_utils.mod.F90:474-513)
+//              (cp_lda_correlation_utils.mod.F90:474-513); or, with the PBE option,
+//              Omega/N sum_r f(rho, |grad rho|^2) of Perdew-Burke-Ernzerhof 1996 on
+//              Perdew-Wang 1992 correlation, grad rho from rho(G) by FFT and
+//              v_xc = df/drho - div(2 df/dsigma grad rho), the divergence by FFT too
+//              (the reference's graden + gcener route, vofrhob_utils.mod.F90:80-471,
+//              gcener_utils.mod.F90:60-304)
 //   E_ext    = Omega/N sum_r V_ext(r) rho(r)  (optional mesh potential)
 //
 // Adjoint (nothing of psi(r) is stored: the band loop recomputes it):
@@ -150,6 +155,151 @@ __device__ __forceinline__ void lda_pz(double rho, double& e, double& v) {
   }
   e = rho * (ex + ec);
   v = vx + vc;
+}
+
+// PBE, unpolarised: f = rho (eps_x + eps_c), df/drho, df/dsigma (sigma = |grad rho|^2);
+// nothing below kRhoGgaMin.  Perdew, Burke, Ernzerhof, Phys. Rev. Lett. 77, 3865 (1996);
+// correlation on Perdew, Wang, Phys. Rev. B 45, 13244 (1992).
+constexpr double kRhoGgaMin = 1.0e-10;
+__device__ __forceinline__ void pbe(double rho, double sigma, double& f, double& fr, double& fs) {
+  if (!(rho > kRhoGgaMin)) {
+    f = fr = fs = 0.0;
+    return;
+  }
+  const double pi = 3.14159265358979323846;
+  // exchange
+  const double ax = -0.73855876638202234;     // -(3/4) (3/pi)^(1/3)
+  const double cs = 0.026121172985233605;     // 1 / (4 (3 pi^2)^(2/3))
+  const double kap = 0.804, mu = 0.2195149727645171;
+  const double r13 = cbrt(rho), r43 = rho * r13;
+  const double s2 = cs * sigma / (r43 * r43);
+  const double den = kap + mu * s2;
+  const double F = 1.0 + kap - kap * kap / den;
+  const double dF = kap * kap * mu / (den * den);
+  const double fx = ax * r43 * F;
+  const double fx_r = (4.0 / 3.0) * ax * r13 * F + ax * r43 * dF * (-(8.0 / 3.0) * s2 / rho);
+  const double fx_s = ax * r43 * dF * cs / (r43 * r43);
+  // correlation: PW92
+  const double A = 0.0310907, a1 = 0.21370, b1 = 7.5957, b2 = 3.5876, b3 = 1.6382, b4 = 0.49294;
+  const double rs = 0.62035049089940009 / r13;  // (3/(4 pi rho))^(1/3)
+  const double srs = sqrt(rs);
+  const double Q = b1 * srs + b2 * rs + b3 * rs * srs + b4 * rs * rs;
+  const double dQ = 0.5 * b1 / srs + b2 + 1.5 * b3 * srs + 2.0 * b4 * rs;
+  const double L = log1p(1.0 / (2.0 * A * Q));
+  const double ec = -2.0 * A * (1.0 + a1 * rs) * L;
+  const double dec_rs = -2.0 * A * a1 * L + (1.0 + a1 * rs) * dQ / (Q * Q * (1.0 + 1.0 / (2.0 * A * Q)));
+  const double dec_r = dec_rs * (-rs / (3.0 * rho));
+  // gradient correction H(rs, t)
+  const double beta = 0.06672455060314922, gam = 0.031090690869654895;  // (1 - ln 2) / pi^2
+  const double ct = pi / (16.0 * 3.0936677262801355);                   // pi / (16 (3 pi^2)^(1/3))
+  const double y = ct * sigma / (rho * rho * r13);
+  const double E = exp(-ec / gam);
+  const double Aa = (beta / gam) / (E - 1.0);
+  const double dAa = (beta / (gam * gam)) * E / ((E - 1.0) * (E - 1.0));
+  const double Nn = 1.0 + Aa * y, Dd = 1.0 + Aa * y + Aa * Aa * y * y;
+  const double Bb = (beta / gam) * y * Nn / Dd;
+  const double H = gam * log1p(Bb);
+  const double dB_y = (beta / gam) * (Nn / Dd + y * (Aa * Dd - Nn * (Aa + 2.0 * Aa * Aa * y)) / (Dd * Dd));
+  const double dB_A = (beta / gam) * y * (y * Dd - Nn * (y + 2.0 * Aa * y * y)) / (Dd * Dd);
+  const double dH_y = gam * dB_y / (1.0 + Bb), dH_A = gam * dB_A / (1.0 + Bb);
+  const double fc = rho * (ec + H);
+  const double fc_r = (ec + H) + rho * (dec_r + dH_A * dAa * dec_r + dH_y * (-(7.0 / 3.0) * y / rho));
+  const double fc_s = rho * dH_y * ct / (rho * rho * r13);
+  f = fx + fc;
+  fr = fx_r + fc_r;
+  fs = fx_s + fc_s;
+}
+
+// i tpiba m of mesh index i on an axis of length n (Nyquist of an even n -> 0)
+__device__ __forceinline__ double deriv_freq(int i, int n) {
+  if ((n & 1) == 0 && 2 * i == n) return 0.0;
+  return (double)(2 * i < n + 1 ? i : i - n);
+}
+
+// g3[d] = i tpiba m_d rho(G), d = x, y, z, on the (k1, k2, n3) FFT grid
+__global__ void k_grad_g(const cx<double>* __restrict__ rg, cx<double>* __restrict__ g3, int n1, int n2, int n3,
+                         int k1, int k2, double tpiba) {
+  const size_t ng = (size_t)k1 * k2 * n3;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ng; i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % k1), y = (int)((i / k1) % k2), z = (int)(i / ((size_t)k1 * k2));
+    const bool in = x < n1 && y < n2;
+    const cx<double> v = in ? rg[i] : mk<double>(0.0, 0.0);
+    const double m[3] = {in ? deriv_freq(x, n1) : 0.0, in ? deriv_freq(y, n2) : 0.0, in ? deriv_freq(z, n3) : 0.0};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) g3[d * ng + i] = mk<double>(-tpiba * m[d] * v.y, tpiba * m[d] * v.x);
+  }
+}
+
+// sum_d i tpiba m_d h_d(G) into g3[0]
+__global__ void k_div_g(cx<double>* __restrict__ g3, int n1, int n2, int n3, int k1, int k2, double tpiba) {
+  const size_t ng = (size_t)k1 * k2 * n3;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ng; i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % k1), y = (int)((i / k1) % k2), z = (int)(i / ((size_t)k1 * k2));
+    const bool in = x < n1 && y < n2;
+    const double m[3] = {in ? deriv_freq(x, n1) : 0.0, in ? deriv_freq(y, n2) : 0.0, in ? deriv_freq(z, n3) : 0.0};
+    double re = 0.0, im = 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const cx<double> h = g3[d * ng + i];
+      re -= tpiba * m[d] * h.y;
+      im += tpiba * m[d] * h.x;
+    }
+    g3[i] = mk<double>(re, im);
+  }
+}
+
+// PBE per mesh point: V_eff = Re(vr) + df/drho (+ V_ext), dE/dV, partial sums of f and
+// V_ext rho; g3[d] (grad rho in the real parts) is overwritten by h_d = 2 df/dsigma d_d rho
+__global__ void __launch_bounds__(kET) k_xc_pbe(const double* __restrict__ rho, const cx<double>* __restrict__ vr,
+                                                const double* __restrict__ vext, cx<double>* __restrict__ g3,
+                                                int n1, int n2, int n3, int k1, int k2, int k3, double dscale,
+                                                double* __restrict__ veff, double* __restrict__ dvloc,
+                                                double* __restrict__ part) {
+  __shared__ double sh[kET / 32];
+  const size_t n = (size_t)k1 * k2 * k3, ng = (size_t)k1 * k2 * n3;
+  double exc = 0.0, eext = 0.0;
+  for (size_t i = blockIdx.x * (size_t)kET + threadIdx.x; i < n; i += (size_t)gridDim.x * kET) {
+    const int x = (int)(i % k1);
+    const int y = (int)((i / k1) % k2);
+    const int z = (int)(i / ((size_t)k1 * k2));
+    double ve = 0.0, dv = 0.0;
+    if (x < n1 && y < n2 && z < n3) {
+      const double r = rho[i];
+      const double gx = g3[i].x, gy = g3[ng + i].x, gz = g3[2 * ng + i].x;
+      double f, fr, fs;
+      pbe(r, gx * gx + gy * gy + gz * gz, f, fr, fs);
+      exc += f;
+      ve = vr[i].x + fr;
+      if (vext) {
+        ve += vext[i];
+        eext += vext[i] * r;
+      }
+      dv = r * dscale;
+      g3[i] = mk<double>(2.0 * fs * gx, 0.0);
+      g3[ng + i] = mk<double>(2.0 * fs * gy, 0.0);
+      g3[2 * ng + i] = mk<double>(2.0 * fs * gz, 0.0);
+    } else if (i < ng) {
+      g3[i] = g3[ng + i] = g3[2 * ng + i] = mk<double>(0.0, 0.0);
+    }
+    veff[i] = ve;
+    if (dvloc) dvloc[i] = dv;
+  }
+  const double a = cta_sum(exc, sh);
+  const double b = cta_sum(eext, sh);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = b;
+  }
+}
+
+// V_eff -= div(h) on the mesh points
+__global__ void k_sub_div(const cx<double>* __restrict__ div, int n1, int n2, int n3, int k1, int k2,
+                          double* __restrict__ veff) {
+  const size_t ng = (size_t)k1 * k2 * n3;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ng; i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % k1), y = (int)((i / k1) % k2);
+    if (x < n1 && y < n2) veff[i] -= div[i].x;
+  }
 }
 
 // V_eff = Re(vr) + v_xc + V_ext and dE/dV = rho Omega/N on the padded mesh;
@@ -349,7 +499,39 @@ int energy_and_grad(Ctx& c, const cx<double>* c0, int ldc, int nstate, const dou
   // xc, V_eff, dE/dV
   if (!ensure(c, c.en_veff, sizeof(double) * nnr1)) return 6;
   double* veff = static_cast<double*>(c.en_veff.p);
-  {
+  const int nb_n = std::max(1, (int)std::min<size_t>(4096, (ngrid + kET - 1) / kET));
+  if (c.xc == 1) {
+    // PBE: grad rho by three inverse FFTs of i G rho(G); the per-point functional writes
+    // h = 2 df/dsigma grad rho over them; div h by three forward FFTs and one inverse
+    if (!ensure(c, c.en_g3, sizeof(cx<double>) * 3 * ngrid)) return 6;
+    cx<double>* g3 = static_cast<cx<double>*>(c.en_g3.p);
+    {
+      ProfScope ps_(c, "k_grad_g");
+      k_grad_g<<<nb_n, kET, 0, c.stream>>>(ga, g3, n1, n2, n3, k1, k2, tpiba);
+      GBCP_LAUNCH_CHECK(c);
+    }
+    for (int d = 0; d < 3; ++d)
+      if ((rc = dense_fft(c, g3 + d * ngrid, true))) return rc;
+    {
+      ProfScope ps_(c, "k_xc_pbe");
+      k_xc_pbe<<<nb_r, kET, 0, c.stream>>>(rho, gb, vext, g3, n1, n2, n3, k1, k2, k3, c.omega / nmesh, veff, dvloc,
+                                           part_r);
+      GBCP_LAUNCH_CHECK(c);
+    }
+    for (int d = 0; d < 3; ++d)
+      if ((rc = dense_fft(c, g3 + d * ngrid, false))) return rc;
+    {
+      ProfScope ps_(c, "k_div_g");
+      k_div_g<<<nb_n, kET, 0, c.stream>>>(g3, n1, n2, n3, k1, k2, tpiba);
+      GBCP_LAUNCH_CHECK(c);
+    }
+    if ((rc = dense_fft(c, g3, true))) return rc;
+    {
+      ProfScope ps_(c, "k_sub_div");
+      k_sub_div<<<nb_n, kET, 0, c.stream>>>(g3, n1, n2, n3, k1, k2, veff);
+      GBCP_LAUNCH_CHECK(c);
+    }
+  } else {
     ProfScope ps_(c, "k_xc");
     k_xc<<<nb_r, kET, 0, c.stream>>>(rho, gb, vext, n1, n2, n3, k1, k2, k3, c.omega / nmesh, veff, dvloc, part_r);
     GBCP_LAUNCH_CHECK(c);

@@ -89,8 +89,11 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  *   GBCP_OPT_FFT    band-loop FFT kernels: 0 = four-step register codelets
  *                   where the mesh has a plan, else Stockham; 2 = Stockham;
  *   GBCP_OPT_XCHUNKS pair chunks of the density x-stage (four-step kernels):
- *                   0 = chosen per launch from the SM count, 1..8 = fixed. */
-enum gbcp_option { GBCP_OPT_GEMM = 1, GBCP_OPT_BATCH = 2, GBCP_OPT_FFT = 3, GBCP_OPT_XCHUNKS = 4 };
+ *                   0 = chosen per launch from the SM count, 1..8 = fixed;
+ *   GBCP_OPT_XC     exchange-correlation functional of gbcp_energy: 0 = LDA
+ *                   (Slater + Perdew-Zunger, the default), 1 = PBE (gradient-
+ *                   corrected, the reference's vofrhob/gcener route). */
+enum gbcp_option { GBCP_OPT_GEMM = 1, GBCP_OPT_BATCH = 2, GBCP_OPT_FFT = 3, GBCP_OPT_XCHUNKS = 4, GBCP_OPT_XC = 5 };
 int gbcp_set_option(gbcp_ctx* ctx, int key, int value);
 /* Queue later work on `stream` (a cudaStream_t; NULL = the context's own
  * stream; the CUDA legacy default stream is cudaStreamLegacy).  Device-pointer calls are ordered only with respect to this stream,

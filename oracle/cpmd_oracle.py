@@ -327,6 +327,99 @@ def xc_lda_pz(rho: np.ndarray):
     return e, v
 
 
+# PBE (Perdew, Burke, Ernzerhof, Phys. Rev. Lett. 77, 3865 (1996)), unpolarised, on the
+# Perdew-Wang 1992 LDA correlation (Phys. Rev. B 45, 13244): the published constants.
+_PBE = dict(kappa=0.804, mu=0.2195149727645171, beta=0.06672455060314922,
+            gamma=(1.0 - math.log(2.0)) / math.pi ** 2,
+            A=0.0310907, a1=0.21370, b1=7.5957, b2=3.5876, b3=1.6382, b4=0.49294)
+RHO_GGA_MIN = 1.0e-10
+
+
+def xc_pbe(rho, sigma):
+    """(f, df/drho, df/dsigma) per point, f = rho (eps_x + eps_c) of unpolarised PBE,
+    sigma = |grad rho|^2; points with rho <= RHO_GGA_MIN contribute nothing.  The
+    reference evaluates its GGA functionals per mesh point in gcener
+    (gcener_utils.mod.F90:60-304) and adds the divergence term there."""
+    P = _PBE
+    rho = np.asarray(rho, dtype=np.float64)
+    sigma = np.asarray(sigma, dtype=np.float64)
+    ok = rho > RHO_GGA_MIN
+    r = np.where(ok, rho, 1.0)
+    sg = np.where(ok, sigma, 0.0)
+    pi = math.pi
+    # exchange
+    ax = -0.75 * (3.0 / pi) ** (1.0 / 3.0)
+    cs = 1.0 / (4.0 * (3.0 * pi * pi) ** (2.0 / 3.0))
+    r13 = np.cbrt(r)
+    r43 = r * r13
+    s2 = cs * sg / (r43 * r43)
+    kap, mu = P["kappa"], P["mu"]
+    den = kap + mu * s2
+    F = 1.0 + kap - kap * kap / den
+    dF = kap * kap * mu / (den * den)
+    fx = ax * r43 * F
+    fx_r = (4.0 / 3.0) * ax * r13 * F + ax * r43 * dF * (-(8.0 / 3.0) * s2 / r)
+    fx_s = ax * r43 * dF * cs / (r43 * r43)
+    # correlation: PW92
+    A, a1 = P["A"], P["a1"]
+    rs = (3.0 / (4.0 * pi * r)) ** (1.0 / 3.0)
+    srs = np.sqrt(rs)
+    Q = P["b1"] * srs + P["b2"] * rs + P["b3"] * rs * srs + P["b4"] * rs * rs
+    dQ = 0.5 * P["b1"] / srs + P["b2"] + 1.5 * P["b3"] * srs + 2.0 * P["b4"] * rs
+    L = np.log1p(1.0 / (2.0 * A * Q))
+    ec = -2.0 * A * (1.0 + a1 * rs) * L
+    dec_rs = -2.0 * A * a1 * L + (1.0 + a1 * rs) * dQ / (Q * Q * (1.0 + 1.0 / (2.0 * A * Q)))
+    dec_r = dec_rs * (-rs / (3.0 * r))
+    # gradient correction H(rs, t)
+    beta, gam = P["beta"], P["gamma"]
+    ct = pi / (16.0 * (3.0 * pi * pi) ** (1.0 / 3.0))
+    y = ct * sg / (r * r * r13)                       # t^2 = sigma pi / (16 k_F rho^2)
+    E = np.exp(-ec / gam)
+    Aa = (beta / gam) / (E - 1.0)
+    dAa = (beta / (gam * gam)) * E / ((E - 1.0) ** 2)  # dA/d eps_c
+    Nn = 1.0 + Aa * y
+    Dd = 1.0 + Aa * y + Aa * Aa * y * y
+    Bb = (beta / gam) * y * Nn / Dd
+    H = gam * np.log1p(Bb)
+    dB_y = (beta / gam) * (Nn / Dd + y * (Aa * Dd - Nn * (Aa + 2.0 * Aa * Aa * y)) / (Dd * Dd))
+    dB_A = (beta / gam) * y * (y * Dd - Nn * (y + 2.0 * Aa * y * y)) / (Dd * Dd)
+    dH_y = gam * dB_y / (1.0 + Bb)
+    dH_A = gam * dB_A / (1.0 + Bb)
+    fc = r * (ec + H)
+    fc_r = (ec + H) + r * (dec_r + dH_A * dAa * dec_r + dH_y * (-(7.0 / 3.0) * y / r))
+    fc_s = r * dH_y * ct / (r * r * r13)
+    f = np.where(ok, fx + fc, 0.0)
+    f_r = np.where(ok, fx_r + fc_r, 0.0)
+    f_s = np.where(ok, fx_s + fc_s, 0.0)
+    return f, f_r, f_s
+
+
+def _deriv_factors(n: int, tpiba: float) -> np.ndarray:
+    """i G_d of a periodic axis of length n (Nyquist term of an even n set to 0)."""
+    k = np.fft.fftfreq(n, d=1.0 / n)
+    if n % 2 == 0:
+        k[n // 2] = 0.0
+    return 1j * tpiba * k
+
+
+def xc_pbe_mesh(r, tpiba):
+    """E_xc density f(r) and v_xc = df/drho - div(2 df/dsigma grad rho) on the (n3, n2, n1)
+    mesh, gradients and divergence by FFT (the reference's graden/gcener route)."""
+    n3, n2, n1 = r.shape
+    rg = fwfftn(r.astype(np.complex128))
+    dz = _deriv_factors(n3, tpiba)[:, None, None]
+    dy = _deriv_factors(n2, tpiba)[None, :, None]
+    dx = _deriv_factors(n1, tpiba)[None, None, :]
+    grads = [invfftn(d * rg).real for d in (dx, dy, dz)]
+    sigma = grads[0] ** 2 + grads[1] ** 2 + grads[2] ** 2
+    f, f_r, f_s = xc_pbe(r, sigma)
+    div = np.zeros(r.shape, dtype=np.complex128)
+    for d, gcomp in zip((dx, dy, dz), grads):
+        div += d * fwfftn((2.0 * f_s * gcomp).astype(np.complex128))
+    v = f_r - invfftn(div).real
+    return f, v
+
+
 def structure_phase(mill, tau, tpiba):
     """eigr(G, a) = e^{-i G.R_a}, G = mill * tpiba (cubic cell)."""
     return np.exp(-1j * tpiba * (mill.astype(np.float64) @ np.asarray(tau, dtype=np.float64).T))
@@ -338,7 +431,7 @@ def gaussian_vps(hg, tpiba2, omega, amp=-4.0, width2=1.0):
     return amp * (math.pi * width2) ** 1.5 * np.exp(-width2 * g2 / 4.0) / omega
 
 
-def energy(c0, f, basis, tau, vps, isp, vext=None, grad=True):
+def energy(c0, f, basis, tau, vps, isp, vext=None, grad=True, xc="lda"):
     """Energy terms, C2 = -(1/2) dE/dc* in the reference's vpsi normalisation, dE/dV(r), forces.
 
     ``basis`` carries the density half sphere (mill, hg; first ngw = wavefunction
@@ -370,7 +463,10 @@ def energy(c0, f, basis, tau, vps, isp, vext=None, grad=True):
     scg = np.zeros_like(g2)
     scg[nz] = 4.0 * math.pi / g2[nz]
     ehart = om * float(np.sum(scg * np.abs(rg) ** 2))
-    exc_d, vxc = xc_lda_pz(r)
+    if xc == "pbe":
+        exc_d, vxc = xc_pbe_mesh(r, basis.tpiba)
+    else:
+        exc_d, vxc = xc_lda_pz(r)
     exc = om / N * float(exc_d.sum())
     eext = 0.0
     if vext is not None:

@@ -188,3 +188,56 @@ def test_energy_c2_mixed_gate_and_fd(gpu_lib, c2cell):
             ep = ctx64.energy(cl.c0, cl.f, tp, vps, isp, grad=False)["etot"]
             em = ctx64.energy(cl.c0, cl.f, tm, vps, isp, grad=False)["etot"]
             assert abs(-(ep - em) / (2 * h) - f64[a, d]) < 1e-6 * np.abs(f64).max()
+
+
+# ------------------------------------------------------------------ PBE (gradient-corrected xc)
+@pytest.mark.parametrize("mode", ["host", "device"])
+def test_energy_pbe_fp64_parity(gpu_lib, c0case, mode):
+    """GBCP_OPT_XC = PBE: energies, C2, dE/dV and forces vs the oracle's PBE route
+    (grad rho and the divergence term by FFT) to 1e-10 relative."""
+    cl, vps, isp, vext, _ = c0case
+    terms_ref, c2_ref, dv_ref, f_ref, _ = O.energy(cl.c0, cl.f, cl.basis, cl.tau, vps, isp, vext, xc="pbe")
+    ctx = ctx_for(cl.basis)
+    ctx.set_option("xc", 1)
+    if mode == "host":
+        terms, c2, dv, fion = ctx.energy(cl.c0, cl.f, cl.tau, vps, isp, vext)
+    else:
+        terms, c2, dv, fion = ctx.energy(dev(cl.c0), dev(cl.f), dev(cl.tau), dev(np.ascontiguousarray(vps.T)), isp,
+                                         dev(vext))
+        c2 = np.asfortranarray(c2.cpu().numpy().T)
+        dv = dv.cpu().numpy()
+        fion = fion.cpu().numpy()
+    for k in ("ekin", "eloc", "ehart", "exc", "eext", "etot"):
+        assert abs(terms[k] - terms_ref[k]) <= TOL64 * max(abs(terms_ref[k]), 1.0), k
+    assert rel(c2, c2_ref) < TOL64
+    assert rel(dv, dv_ref) < TOL64
+    assert rel(fion, f_ref) < TOL64
+    # the functional differs from LDA by a gradient correction of the expected size
+    ctx.set_option("xc", 0)
+    lda = ctx.energy(cl.c0, cl.f, cl.tau, vps, isp, vext, grad=False)
+    assert 1e-4 < abs(terms_ref["exc"] - lda["exc"]) < 0.2 * abs(lda["exc"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_energy_pbe_fd(gpu_lib, precision):
+    """dE/dc* of the PBE energy (C2 from vpsi on V_eff with the divergence term) vs
+    central differences of the GPU energy; mixed precision keeps |dE| <= 1e-6 Ha/atom."""
+    cl = make_small_cell(10.26, 24, 10.0, 6, seed=5)
+    b = cl.basis
+    vps, isp, vext = setup(cl)
+    ctx = ctx_for(b, precision)
+    ctx.set_option("xc", 1)
+    terms, c2, dv, fion = ctx.energy(cl.c0, cl.f, cl.tau, vps, isp, vext)
+    E = lambda c: ctx.energy(c, cl.f, cl.tau, vps, isp, vext, grad=False)["etot"]  # noqa: E731
+    rng = np.random.default_rng(11)
+    dc = (rng.standard_normal(cl.c0.shape) + 1j * rng.standard_normal(cl.c0.shape)) * 1e-2
+    dc[0] = dc[0].real
+    w = np.ones(b.ngw)
+    w[0] = 0.5
+    hc = 1e-3
+    fdc = (E(np.asfortranarray(cl.c0 + hc * dc)) - E(np.asfortranarray(cl.c0 - hc * dc))) / (2 * hc)
+    an = -4.0 * np.sum(w[:, None] * (np.conj(dc) * c2).real)
+    assert abs(fdc - an) < (1e-6 if precision == "fp64" else 1e-4) * abs(an)
+    if precision == "mixed":
+        ref = O.energy(cl.c0, cl.f, b, cl.tau, vps, isp, vext, grad=False, xc="pbe")
+        assert abs(terms["etot"] - ref["etot"]) / len(cl.tau) < 1e-6
