@@ -536,22 +536,26 @@ int pipe_up(Ctx& c, cx<double>* d, const double* h, int ld, int s0, int ns) {
 // pairs per staging chunk of a host-memory call: about four chunks, so that the whole
 // stage chain of one chunk overlaps the copies of the next; host-memory calls launch the
 // band loop chunk by chunk (their launch batch is the chunk)
-// Staging chunks of a host-memory band-loop call, as pair ranges: a small first
-// chunk (its upload is the only one the transforms wait for) and three equal ones,
-// none above the launch batch.  Returns the number of chunks.
+// Staging chunks of a host-memory band-loop call, as pair ranges, each at most one
+// launch batch: a small first chunk (its upload is the only one the transforms
+// wait for), two large middle ones, and a small last one (its transforms and, in
+// vpsi, its C2 download are the tail nothing overlaps).  Returns the number of chunks.
 int stage_plan(Ctx& c, int nstate) {
   const int npairs = (nstate + 1) / 2;
   std::vector<int>& b = c.stage_bounds;
   b.assign(1, 0);
   if (npairs <= 0) return 0;
   const int first = std::max(1, std::min(c.batch, npairs / 16));
-  b.push_back(first);
-  const int rest = npairs - first;
-  if (rest > 0) {
-    const int per = std::min(c.batch, (rest + 2) / 3);
-    for (int p = first + per; p < npairs; p += per) b.push_back(p);
-    b.push_back(npairs);
+  const int last = (npairs - first >= 3) ? std::max(1, std::min(c.batch, npairs / 6)) : 0;
+  int p = first;
+  b.push_back(p);
+  const int mid = npairs - first - last;
+  if (mid > 0) {
+    const int per = std::min(c.batch, std::max(1, (mid + 1) / 2));
+    for (int q = p + per; q < first + mid; q += per) b.push_back(q);
+    b.push_back(first + mid);
   }
+  if (last > 0) b.push_back(npairs);
   return (int)b.size() - 1;
 }
 int stage_max(const Ctx& c) {
