@@ -55,6 +55,7 @@ SIGNATURES = {
     "gbcp_vpsi": (_I, [_P, _P, _I, _P, _I, _P, _P, _I, _I]),
     "gbcp_ortho": (_I, [_P, _P, _I, _I, _I, _DP, _I]),
     "gbcp_ovlap": (_I, [_P, _P, _I, _I, _P, _I]),
+    "gbcp_profile_timeline": (_I, [_P, _I, C.c_char_p, _I, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "gbcp_rortog": (_I, [_P, _P, _I, _P, _I, _I, _I, _D, _I, _P, _P, _I]),
     "gbcp_ovlap_noalloc": (_I, [_P, _I, _I, _I, _I, _P, _P]),
     "gbcp_invfftn": (_I, [_P, _P, _I]),

@@ -168,6 +168,20 @@ class Context:
             i += 1
         return out
 
+    def profile_timeline(self) -> list:
+        """[(name, lane, start ms, end ms)] since the last profile(True); lane 0 is the
+        context stream, 1 host->device staging copies, 2 device->host copies."""
+        out = []
+        i = 0
+        buf = C.create_string_buffer(128)
+        lane = C.c_int()
+        t0 = C.c_double()
+        t1 = C.c_double()
+        while self.lib.gbcp_profile_timeline(self.h, i, buf, 128, C.byref(lane), C.byref(t0), C.byref(t1)) == 0:
+            out.append((buf.value.decode(), lane.value, t0.value, t1.value))
+            i += 1
+        return out
+
     def _check(self, fn: str, rc: int):
         if rc != 0:
             raise GbcpError(fn, rc, self.last_error())

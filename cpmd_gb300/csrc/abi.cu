@@ -50,26 +50,45 @@ static cudaEvent_t pool_event(Ctx& c) {
   return e;
 }
 
-ProfScope::ProfScope(Ctx& ctx, const char* name) : c(ctx), on(ctx.prof) {
+ProfScope::ProfScope(Ctx& ctx, const char* name) : c(ctx), on(ctx.prof), s(ctx.stream) {
   if (!on) return;
   r.name = name;
+  r.lane = 0;
   r.a = pool_event(c);
   r.b = pool_event(c);
-  cudaEventRecord(r.a, c.stream);
+  cudaEventRecord(r.a, s);
+}
+
+ProfScope::ProfScope(Ctx& ctx, const char* name, cudaStream_t stream, int lane)
+    : c(ctx), on(ctx.prof), s(stream) {
+  if (!on) return;
+  r.name = name;
+  r.lane = lane;
+  r.a = pool_event(c);
+  r.b = pool_event(c);
+  cudaEventRecord(r.a, s);
 }
 
 ProfScope::~ProfScope() {
   if (!on) return;
-  cudaEventRecord(r.b, c.stream);
+  cudaEventRecord(r.b, s);
   c.prof_live.push_back(r);
 }
 
 void prof_fold(Ctx& c) {
   if (c.prof_live.empty()) return;
   cudaStreamSynchronize(c.stream);
+  if (c.copy) cudaStreamSynchronize(c.copy);
+  if (c.copy_out) cudaStreamSynchronize(c.copy_out);
   for (ProfRec& r : c.prof_live) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, r.a, r.b);
+    if (c.prof_base) {
+      float t0 = 0.f, t1 = 0.f;
+      cudaEventElapsedTime(&t0, c.prof_base, r.a);
+      cudaEventElapsedTime(&t1, c.prof_base, r.b);
+      c.prof_tl.push_back({r.name, r.lane, t0, t1});
+    }
     bool found = false;
     for (auto& kv : c.prof_acc) {
       if (kv.first == r.name) {
@@ -382,6 +401,7 @@ int gbcp_ctx_destroy(gbcp_ctx* h) {
   if (c.d_info) cudaFree(c.d_info);
   gbcp::prof_fold(c);
   for (cudaEvent_t e : c.prof_pool) cudaEventDestroy(e);
+  if (c.prof_base) cudaEventDestroy(c.prof_base);
   if (c.own) {
     cudaStreamSynchronize(c.own);
     cudaStreamDestroy(c.own);
@@ -452,7 +472,25 @@ int gbcp_profile_enable(gbcp_ctx* h, int enable) {
   Ctx& c = h->c;
   gbcp::prof_fold(c);
   c.prof_acc.clear();
+  c.prof_tl.clear();
   c.prof = enable != 0;
+  if (c.prof) {
+    if (!c.prof_base && cudaEventCreate(&c.prof_base) != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, "profile event");
+    cudaEventRecord(c.prof_base, c.stream);
+  }
+  return GBCP_OK;
+}
+
+int gbcp_profile_timeline(gbcp_ctx* h, int idx, char* name, int name_len, int* lane, double* t0_ms, double* t1_ms) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  gbcp::prof_fold(c);
+  if (idx < 0 || idx >= (int)c.prof_tl.size()) return GBCP_ERR_ARG;
+  const gbcp::TimelineRec& r = c.prof_tl[(size_t)idx];
+  if (name && name_len > 0) snprintf(name, (size_t)name_len, "%s", r.name.c_str());
+  if (lane) *lane = r.lane;
+  if (t0_ms) *t0_ms = r.t0;
+  if (t1_ms) *t1_ms = r.t1;
   return GBCP_OK;
 }
 
@@ -480,6 +518,7 @@ int stage_in_cx(Ctx& c, Scratch& s, const double* h, int ld, int rows, int n, cx
   if (!gbcp::ensure(c, s, bytes)) return GBCP_ERR_NOMEM;
   *d = static_cast<cx<double>*>(s.p);
   if (n > 0) {
+    gbcp::ProfScope ps_(c, "h2d_states", c.stream, 1);
     GBCP_CUDA_TRY(c, cudaMemcpy2DAsync(s.p, sizeof(cx<double>) * rows, h, sizeof(cx<double>) * (size_t)ld,
                                        sizeof(cx<double>) * rows, n, cudaMemcpyHostToDevice, c.stream));
   }
@@ -488,6 +527,7 @@ int stage_in_cx(Ctx& c, Scratch& s, const double* h, int ld, int rows, int n, cx
 
 int stage_out_cx(Ctx& c, const cx<double>* d, double* h, int ld, int rows, int n) {
   if (n > 0) {
+    gbcp::ProfScope ps_(c, "d2h_states", c.stream, 2);
     GBCP_CUDA_TRY(c, cudaMemcpy2DAsync(h, sizeof(cx<double>) * (size_t)ld, d, sizeof(cx<double>) * rows,
                                        sizeof(cx<double>) * rows, n, cudaMemcpyDeviceToHost, c.stream));
   }
@@ -527,6 +567,7 @@ int pipe_prepare(Ctx& c, int nbatch) {
 
 // upload states [s0, s0 + ns) of a host (ld) array into the packed device array d (rows = ngw)
 int pipe_up(Ctx& c, cx<double>* d, const double* h, int ld, int s0, int ns) {
+  gbcp::ProfScope ps_(c, "h2d_states", c.copy, 1);
   GBCP_CUDA_TRY(c, cudaMemcpy2DAsync(d + (size_t)s0 * c.ngw, sizeof(cx<double>) * c.ngw,
                                      h + 2 * (size_t)s0 * ld, sizeof(cx<double>) * (size_t)ld,
                                      sizeof(cx<double>) * c.ngw, ns, cudaMemcpyHostToDevice, c.copy));
@@ -630,6 +671,7 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
     *csumr = s * c.omega / ((double)c.nr[0] * c.nr[1] * c.nr[2]);
   }
   if (!rc && mem == GBCP_MEM_HOST) {
+    gbcp::ProfScope ps_(c, "d2h_rho", c.stream, 2);
     cudaError_t e = cudaMemcpyAsync(rhoe, drho, sizeof(double) * nnr1, cudaMemcpyDeviceToHost, c.stream);
     if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));
   }
@@ -680,6 +722,7 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
         GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[1 + b], c.copy));
       }
       if (b == 0) {
+        gbcp::ProfScope ps_(c, "h2d_vpot", c.copy, 1);
         GBCP_CUDA_TRY(c, cudaMemcpyAsync(tv, vpot, sizeof(double) * nnr1, cudaMemcpyHostToDevice, c.copy));
         GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[3 * nb + 1], c.copy));
       } else {
@@ -699,6 +742,7 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
       cudaEvent_t e = c.pipe_ev[1 + nb + b];
       GBCP_CUDA_TRY(c, cudaEventRecord(e, c.stream));
       GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.copy_out, e, 0));
+      gbcp::ProfScope ps_(c, "d2h_c2", c.copy_out, 2);
       GBCP_CUDA_TRY(c, cudaMemcpy2DAsync(c2 + 2 * (size_t)s0 * ldc2, sizeof(cx<double>) * (size_t)ldc2,
                                          t2 + (size_t)s0 * c.ngw, sizeof(cx<double>) * c.ngw,
                                          sizeof(cx<double>) * c.ngw, ns, cudaMemcpyDeviceToHost, c.copy_out));

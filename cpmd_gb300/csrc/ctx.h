@@ -62,6 +62,12 @@ struct Scratch {
 struct ProfRec {
   const char* name;
   cudaEvent_t a, b;
+  int lane;  // 0 context stream, 1 upload stream, 2 download stream
+};
+struct TimelineRec {
+  std::string name;
+  int lane;
+  double t0, t1;  // ms after the profile was enabled
 };
 struct ProfAcc {
   double ms = 0.0;
@@ -128,6 +134,8 @@ struct Ctx {
   std::vector<int> stage_bounds;  // staging chunks as pair ranges [b[q], b[q+1]); each is one launch batch
   // profiling
   bool prof = false;
+  cudaEvent_t prof_base = nullptr;  // recorded on the context stream when profiling is enabled
+  std::vector<TimelineRec> prof_tl;
   std::vector<ProfRec> prof_live;
   std::vector<cudaEvent_t> prof_pool;
   std::vector<std::pair<std::string, ProfAcc>> prof_acc;
@@ -138,7 +146,10 @@ struct ProfScope {
   Ctx& c;
   ProfRec r{};
   bool on;
+  cudaStream_t s;
   ProfScope(Ctx& ctx, const char* name);
+  // work queued on another stream (the host-staging copies): lane 1 uploads, 2 downloads
+  ProfScope(Ctx& ctx, const char* name, cudaStream_t stream, int lane);
   ~ProfScope();
 };
 void prof_fold(Ctx& c);

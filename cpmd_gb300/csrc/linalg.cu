@@ -427,6 +427,7 @@ int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host) {
   GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.copy, c.pipe_ev[0], 0));
   for (int r = 0; r < R; ++r) {
     const int g0 = gb[r], g = gb[r + 1] - gb[r];
+    ProfScope ps_(c, "h2d_states", c.copy, 1);
     if (g > 0)
       GBCP_CUDA_TRY(c, cudaMemcpy2DAsync(d + g0, sizeof(cx<double>) * (size_t)ngw, h + 2 * (size_t)g0,
                                          sizeof(cx<double>) * (size_t)ldh, sizeof(cx<double>) * (size_t)g, n,
@@ -445,6 +446,7 @@ int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host) {
   for (int r = 0; r < R; ++r) {
     const int g0 = gb[r], g = gb[r + 1] - gb[r];
     GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.copy_out, done[r], 0));
+    ProfScope ps_(c, "d2h_states", c.copy_out, 2);
     if (g > 0)
       GBCP_CUDA_TRY(c, cudaMemcpy2DAsync(h + 2 * (size_t)g0, sizeof(cx<double>) * (size_t)ldh, d + g0,
                                          sizeof(cx<double>) * (size_t)ngw, sizeof(cx<double>) * (size_t)g, n,

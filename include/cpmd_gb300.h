@@ -114,6 +114,11 @@ int64_t gbcp_kernel_launches(void);
  * the last entry. */
 int gbcp_profile_enable(gbcp_ctx* ctx, int enable);
 int gbcp_profile_read(gbcp_ctx* ctx, int idx, char* name, int name_len, double* total_ms, int64_t* count);
+/* Timeline of the same records since the last enable: entry `idx` (name, lane:
+ * 0 context stream, 1 host->device staging copies, 2 device->host copies, and
+ * start / end in milliseconds after the enable), in the order they were queued;
+ * GBCP_ERR_ARG past the last entry. */
+int gbcp_profile_timeline(gbcp_ctx* ctx, int idx, char* name, int name_len, int* lane, double* t0_ms, double* t1_ms);
 
 /* rhoofr(c0, rhoe, psi, nstate)            rhoofr_utils.mod.F90:122-644
  * rhoe(kr1,kr2,kr3) = sum_i f_i/omega psi_i(r)^2 (zero in the padding);

@@ -312,3 +312,20 @@ def test_full_size_ortho_gs(gpu_lib):
     ctx.ortho(c, "gs")
     s = ctx.ovlap(c)
     assert float((s - torch.eye(cl.nstate, dtype=torch.float64, device=s.device)).abs().max()) < 1e-12
+
+
+def test_profile_timeline_host_staging(gpu_lib, c0cell):
+    """gbcp_profile_timeline: the staged copies of a host-memory call appear on their
+    lanes with the kernels, each record ends after it starts and after the enable."""
+    ctx = ctx_for(c0cell.basis, precision="mixed")
+    ctx.profile(True)
+    ctx.rhoofr(c0cell.c0, c0cell.f)
+    tl = ctx.profile_timeline()
+    names = {r[0] for r in tl}
+    assert "h2d_states" in names and "d2h_rho" in names and "k_zinv" in names
+    assert {r[1] for r in tl} >= {0, 1, 2}
+    assert all(0.0 <= r[2] <= r[3] for r in tl)
+    ups = [r for r in tl if r[0] == "h2d_states"]
+    zinv = [r for r in tl if r[0] == "k_zinv"]
+    assert min(z[2] for z in zinv) >= min(u[3] for u in ups) - 1e-3  # the first Z stage waits for its states
+    ctx.profile(False)
