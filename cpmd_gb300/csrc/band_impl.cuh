@@ -454,9 +454,10 @@ inline int xrho_chunks(const Ctx& c, int tiles, int np) {
 }
 
 template <typename T, int NC>
-int launch_xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho) {
+int launch_xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho, int poff) {
   const GeoDev& g = c.geo;
-  const cx<T>* yb = static_cast<const cx<T>*>(c.ybuf.p);
+  // pairs poff .. poff+np-1 of the launch batch (states from s0)
+  const cx<T>* yb = static_cast<const cx<T>*>(c.ybuf.p) + (size_t)poff * g.n3 * g.n2 * g.nslot;
   if constexpr (NC > 0) {
     using P = FS<T, NC>;
     const int tiles_y = (g.n2 + P::L - 1) / P::L, tiles = tiles_y * g.n3;
@@ -581,8 +582,9 @@ template <typename T> int zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, in
 template <typename T> int yinv(Ctx& c, int np, int poff = 0) {
   GBCP_DISPATCH(launch_yinv, T, band_len(c, c.nr[1]), c, np, poff)
 }
-template <typename T> int xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho) {
-  GBCP_DISPATCH(launch_xinv_rho, T, band_len(c, c.nr[0]), c, np, s0, nstate, f, rho)
+template <typename T>
+int xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho, int poff = 0) {
+  GBCP_DISPATCH(launch_xinv_rho, T, band_len(c, c.nr[0]), c, np, s0, nstate, f, rho, poff)
 }
 template <typename T> int xvx(Ctx& c, int np, const double* vpot, const T* vpotT) {
   GBCP_DISPATCH(launch_xvx, T, band_len(c, c.nr[0]), c, np, vpot, vpotT)
@@ -625,19 +627,29 @@ int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f,
     if (!c.batch_ready) {
       if ((rc = zinv<T>(c, c0, ldc, s0, nstate, np))) return rc;
       if ((rc = yinv<T>(c, np))) return rc;
+      if ((rc = xinv_rho<T>(c, np, s0, nstate, f, rho))) return rc;
     } else {
       // host staging: Z and Y stages of each staging chunk as its states land; the
-      // density x-stage (which gains most from many pairs per launch) once per batch
+      // density x-stage (which gains most from many pairs per launch) in two groups
+      // of chunks, the first overlapping the later uploads, the second the tail
       const std::vector<int>& b = c.stage_bounds;
-      for (size_t q = 0; q + 1 < b.size(); ++q) {
+      const size_t nq = b.size() - 1, split = nq > 1 ? (nq + 1) / 2 : nq;
+      int g0 = p0;  // first pair of the x-stage group not yet launched
+      for (size_t q = 0; q < nq; ++q) {
         const int q0 = std::max(b[q], p0), q1 = std::min(b[q + 1], p0 + np);
-        if (q1 <= q0) continue;
-        GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.batch_ready[q], 0));
-        if ((rc = zinv<T>(c, c0, ldc, 2 * q0, nstate, q1 - q0, q0 - p0))) return rc;
-        if ((rc = yinv<T>(c, q1 - q0, q0 - p0))) return rc;
+        if (q1 > q0) {
+          GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.batch_ready[q], 0));
+          if ((rc = zinv<T>(c, c0, ldc, 2 * q0, nstate, q1 - q0, q0 - p0))) return rc;
+          if ((rc = yinv<T>(c, q1 - q0, q0 - p0))) return rc;
+        }
+        const int gend = std::min(b[q + 1], p0 + np);
+        if ((q + 1 == split || q + 1 == nq) && gend > g0) {
+          if ((rc = xinv_rho<T>(c, gend - g0, 2 * g0, nstate, f, rho, g0 - p0))) return rc;
+          g0 = gend;
+        }
       }
+      if (g0 < p0 + np && (rc = xinv_rho<T>(c, p0 + np - g0, 2 * g0, nstate, f, rho, g0 - p0))) return rc;
     }
-    if ((rc = xinv_rho<T>(c, np, s0, nstate, f, rho))) return rc;
   }
   return 0;
 }
