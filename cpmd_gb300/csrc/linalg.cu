@@ -221,49 +221,68 @@ __global__ void __launch_bounds__(NT) k_gemm_nn(const double* __restrict__ A, co
 }
 
 // Newton-Schulz set-up: alpha = max row sum |S| (>= lambda_max), Y = S/alpha, Z = I
-__global__ void k_ns_init(const double* __restrict__ S, int n, double* __restrict__ Y, double* __restrict__ Z,
-                          double* __restrict__ alpha_out) {
-  __shared__ double red[1024];
+// max |T - I| over an n x n matrix as ordered bits (many CTAs)
+__global__ void k_dev_from_identity(const double* __restrict__ T, int n, unsigned long long* __restrict__ bits) {
   double mx = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    double s = 0.0;
-    for (int j = 0; j < n; ++j) s += fabs(S[(size_t)i * n + j]);
-    mx = fmax(mx, s);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const double d = fabs(T[e] - (((e / n) == (e % n)) ? 1.0 : 0.0));
+    mx = (d > mx || d != d) ? d : mx;
   }
-  red[threadIdx.x] = mx;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
-    __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v = __shfl_down_sync(0xffffffffu, mx, o);
+    mx = (v > mx || v != v) ? v : mx;
   }
-  const double alpha = red[0];
-  for (size_t e = threadIdx.x; e < (size_t)n * n; e += blockDim.x) {
-    Y[e] = S[e] / alpha;
-    Z[e] = ((e / n) == (e % n)) ? 1.0 : 0.0;
-  }
-  if (threadIdx.x == 0) *alpha_out = alpha;
-}
-
-// max |T - I| over an n x n matrix (one CTA)
-__global__ void k_dev_from_identity(const double* __restrict__ T, int n, double* __restrict__ out) {
-  __shared__ double red[1024];
-  double mx = 0.0;
-  for (size_t e = threadIdx.x; e < (size_t)n * n; e += blockDim.x) {
-    const double d = T[e] - (((e / n) == (e % n)) ? 1.0 : 0.0);
-    mx = fmax(mx, fabs(d));
-  }
-  red[threadIdx.x] = mx;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) *out = red[0];
+  if ((threadIdx.x & 31) == 0) atomicMax(bits, (unsigned long long)__double_as_longlong(mx));
 }
 
 __global__ void k_scale(double* __restrict__ X, size_t n, const double* __restrict__ alpha, double power) {
   const double s = pow(*alpha, power);
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) X[e] *= s;
+}
+
+// T = 3/2 I - (P + P^T)/4 (P = Z Y of the Newton-Schulz step, symmetric up to rounding,
+// symmetrised here) and max |T - I| as ordered bits
+__global__ void k_ns_t(const double* __restrict__ P, int n, double* __restrict__ T,
+                       unsigned long long* __restrict__ dev_bits) {
+  double mx = 0.0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    const double d = (i == j) ? 1.0 : 0.0;
+    const double t = 1.5 * d - 0.25 * (P[e] + P[(size_t)j * n + i]);
+    T[e] = t;
+    const double a = fabs(t - d);
+    mx = (a > mx || a != a) ? a : mx;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v = __shfl_down_sync(0xffffffffu, mx, o);
+    mx = (v > mx || v != v) ? v : mx;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(dev_bits, (unsigned long long)__double_as_longlong(mx));
+}
+
+// max over rows of sum_j |S_ij| as ordered bits (many CTAs, one warp per row)
+__global__ void k_row_abs_max(const double* __restrict__ S, int n, unsigned long long* __restrict__ bits) {
+  const int lane = threadIdx.x & 31;
+  for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += gridDim.x * (blockDim.x >> 5)) {
+    double sum = 0.0;
+    for (int j = lane; j < n; j += 32) sum += fabs(S[(size_t)i * n + j]);
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == 0) atomicMax(bits, (unsigned long long)__double_as_longlong(sum));
+  }
+}
+
+// Y = S / alpha, Z = I, alpha from its ordered bits
+__global__ void k_ns_start(const double* __restrict__ S, int n, const unsigned long long* __restrict__ abits,
+                           double* __restrict__ Y, double* __restrict__ Z, double* __restrict__ alpha_out) {
+  const double alpha = __longlong_as_double((long long)*abits);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    Y[e] = S[e] / alpha;
+    Z[e] = ((e / n) == (e % n)) ? 1.0 : 0.0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *alpha_out = alpha;
 }
 
 }  // namespace
@@ -489,15 +508,48 @@ int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host
   int rc = ovlap_gamma_ex(c, c0, ldc, n, S, scond_host != nullptr);
   if (rc) return rc;
   if ((rc = finish_status(c, scond_host))) return rc;
+  const int nbe = std::max(1, std::min(1024, (int)((nn + 255) / 256)));
+  unsigned long long* bits = reinterpret_cast<unsigned long long*>(scal + 2);  // [0] alpha, [1] max|T - I|
   {
     ProfScope ps_(c, "k_ns_init");
-    k_ns_init<<<1, 1024, 0, c.stream>>>(S, n, Y, Z, scal);
+    GBCP_CUDA_TRY(c, cudaMemsetAsync(bits, 0, 2 * sizeof(unsigned long long), c.stream));
+    k_row_abs_max<<<std::max(1, std::min(1024, (n + 7) / 8)), 256, 0, c.stream>>>(S, n, bits);
+    GBCP_LAUNCH_CHECK(c);
+    k_ns_start<<<nbe, 256, 0, c.stream>>>(S, n, bits, Y, Z, scal);
     GBCP_LAUNCH_CHECK(c);
   }
   dim3 grid((n + TS - 1) / TS, (n + TS - 1) / TS);
   double prev = 1e300, res = 1e300;
   bool ok = false;
+  const bool tc = use_tc_gemm(c);
   for (int it = 0; it < 100; ++it) {
+    if (tc) {
+      // the products on the tensor cores, FP64-accurate (split GEMM): column-major
+      // A times row-major M; all of Y, Z, T are symmetric polynomials in S and commute,
+      // so the transposed views give the same matrices
+      GBCP_CUDA_TRY(c, cudaMemsetAsync(bits + 1, 0, sizeof(unsigned long long), c.stream));
+      if ((rc = rmul_tc(c, Z, n, n, n, Y, 0, W, n, 0, c.d_info))) return rc;  // W = Z Y
+      {
+        ProfScope ps_(c, "k_ns_t");
+        k_ns_t<<<nbe, 256, 0, c.stream>>>(W, n, T, bits + 1);
+        GBCP_LAUNCH_CHECK(c);
+      }
+      if ((rc = rmul_tc(c, Y, n, n, n, T, 0, W, n, 0, c.d_info))) return rc;  // W = Y T
+      std::swap(Y, W);
+      if ((rc = rmul_tc(c, T, n, n, n, Z, 0, W, n, 0, c.d_info))) return rc;  // W = T Z
+      std::swap(Z, W);
+      unsigned long long hb = 0;
+      GBCP_CUDA_TRY(c, cudaMemcpyAsync(&hb, bits + 1, sizeof(hb), cudaMemcpyDeviceToHost, c.stream));
+      GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+      memcpy(&res, &hb, sizeof(res));
+      if (!std::isfinite(res)) break;
+      if (res < 1e-15 * std::max(1, n / 16) || (res < 1e-10 && res >= prev)) {
+        ok = true;
+        break;
+      }
+      prev = res;
+      continue;
+    }
     // T = (3 I - Z Y) / 2 ; Y <- Y T ; Z <- T Z
     {
       ProfScope ps_(c, "k_gemm_nn");
@@ -518,11 +570,16 @@ int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host
     std::swap(Z, W);
     {
       ProfScope ps_(c, "k_dev_from_identity");
-      k_dev_from_identity<<<1, 1024, 0, c.stream>>>(T, n, scal + 1);
+      GBCP_CUDA_TRY(c, cudaMemsetAsync(bits + 1, 0, sizeof(unsigned long long), c.stream));
+      k_dev_from_identity<<<nbe, 256, 0, c.stream>>>(T, n, bits + 1);
       GBCP_LAUNCH_CHECK(c);
     }
-    GBCP_CUDA_TRY(c, cudaMemcpyAsync(&res, scal + 1, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-    GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+    {
+      unsigned long long hb = 0;
+      GBCP_CUDA_TRY(c, cudaMemcpyAsync(&hb, bits + 1, sizeof(hb), cudaMemcpyDeviceToHost, c.stream));
+      GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+      memcpy(&res, &hb, sizeof(res));
+    }
     if (!std::isfinite(res)) break;
     // quadratic convergence ends at rounding level: stop when T = I to ~n eps
     // or when the deviation no longer drops

@@ -189,12 +189,16 @@ def test_ortho_gs_parity(gpu_lib, nstate):
 
 
 @pytest.mark.parametrize("nstate", [16, 70])
-def test_ortho_lowdin_parity(gpu_lib, nstate):
+@pytest.mark.parametrize("gemm", [0, 1])
+def test_ortho_lowdin_parity(gpu_lib, nstate, gemm):
+    """Both GEMM engines (FP64 SIMT; tcgen05 split GEMMs for the overlap, the
+    Newton-Schulz products and C S^-1/2) give the oracle's Loewdin states."""
     cl = make_small_cell(10.26, 32, 20.0, nstate, seed=41)
     b = cl.basis
     c = perturbed(cl, 0.03)
     ref, sc_ref = O.lowdin(c, b.geq0)
     ctx = ctx_for(b)
+    ctx.set_option("gemm", gemm)
     out = dev(c)
     sc = ctx.ortho(out, "lowdin")
     out = host_wfn(out)
