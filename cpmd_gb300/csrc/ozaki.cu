@@ -17,24 +17,28 @@
 // up to 2^(E-56).  A digit is an integer in [-127, 127] -- exact in bf16 -- and
 // a digit product is exact in FP32.
 //
-// Products.  For a 128 x 64 output tile the CTA runs, per K-chunk of 128, the
+// Products.  For a 128 x 32 output tile the CTA runs, per K-chunk of 128, the
 // 36 digit-pair products with s + t = d <= 7 ("level" d), accumulating all pairs
-// of a level in one FP32 TMEM accumulator (8 levels x 64 columns = the 512 TMEM
-// columns).  A level sum is an integer below 8 * 128 * 127^2 < 2^24, so FP32
-// holds it exactly.  After each chunk the accumulators are read back and folded
-// into two int64 registers per output (H = levels 0-3, Lo = levels 4-7, 7 bits
-// apart); int64 keeps the sum over every chunk exact and only the final
-// conversion is FP64:  sum_k x_ik y_kj = 2^(E_i+E_j) (H 2^-35 + Lo 2^-63).
-// Levels above 7 are dropped (< 2^-49 of 2^(E_i+E_j) per product term).
+// of a level in one FP32 TMEM accumulator (8 levels x 32 columns = one
+// accumulator set; two sets fill the 512 TMEM columns).  A level sum is an
+// integer below 8 * 128 * 127^2 < 2^24, so FP32 holds it exactly.  After each
+// chunk the accumulators are read back and folded into two int64 registers per
+// output (H = levels 0-3, Lo = levels 4-7, 7 bits apart); int64 keeps the sum
+// over every chunk exact and only the final conversion is rounded:
+// sum_k x_ik y_kj = 2^(E_i+E_j) (H 2^-35 + Lo 2^-63).  Levels above 7 are
+// dropped (< 2^-49 of 2^(E_i+E_j) per product term).
 //
 // Data flow.  The digits are produced ONCE per operand by integer-only slicing
 // kernels into eight bf16 digit planes in HBM (row-major, K contiguous, planes
 // stacked along rows), and the GEMM kernel streams them with TMA (64-byte
-// swizzle, K = 32 per sub-chunk, double-buffered: thread 0 loads sub-chunk
-// i + 1 while the 72 MMAs of sub-chunk i run).  All 256 threads fold the eight
-// TMEM level accumulators into int64 every 128 K.  Every mbarrier wait is
-// bounded; on expiry the kernel sets the ortho status word to -2 (reported as
-// GBCP_ERR_TIMEOUT), waits for its own loads and MMAs, frees its TMEM and returns.
+// swizzle, K = 32 per sub-chunk, two shared-memory stages).  The CTA is split by
+// role: one thread issues the TMA loads, one thread the 72 MMAs per sub-chunk,
+// and eight warps fold a finished accumulator set into int64 and write the
+// outputs while the MMAs of the next chunk fill the other set, so that the
+// integer fold and the FP64 rounding run beside the tensor core instead of
+// between its chunks.  Every mbarrier wait is bounded; on expiry the kernel sets
+// the ortho status word to -2 (reported as GBCP_ERR_TIMEOUT), waits for its own
+// loads and MMAs, frees its TMEM and returns.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -50,19 +54,24 @@ namespace gbcp {
 namespace {
 
 constexpr int OZ_M = 128;      // output rows per tile
-constexpr int OZ_N = 64;       // output columns per tile
+constexpr int OZ_N = 32;       // output columns per tile
+constexpr int OZ_NB = OZ_M / OZ_N;  // column tiles per row-tile width (upper block triangle)
 constexpr int OZ_KS = 32;      // K per sub-chunk (two MMAs of K = 16)
 constexpr int OZ_SUBS = 4;     // sub-chunks per exact accumulation chunk (K = 128)
 constexpr int OZ_SL = 8;       // digit slices
 constexpr int OZ_LEV = 8;      // levels kept (s + t <= 7)
-constexpr int OZ_THREADS = 256;
+constexpr int OZ_CONS = 8;     // fold / epilogue warps (two per TMEM lane quadrant)
+constexpr int OZ_TMA_WARP = OZ_CONS, OZ_MMA_WARP = OZ_CONS + 1;
+constexpr int OZ_THREADS = 32 * (OZ_CONS + 2);
+constexpr int OZ_TBUF = OZ_LEV * OZ_N;  // TMEM columns of one accumulator set (two sets: 512)
 constexpr int A_SLICE_BYTES = OZ_M * OZ_KS * 2;  // 8 KB
-constexpr int B_SLICE_BYTES = OZ_N * OZ_KS * 2;  // 4 KB
+constexpr int B_SLICE_BYTES = OZ_N * OZ_KS * 2;  // 2 KB
 constexpr int A_BUF_BYTES = OZ_SL * A_SLICE_BYTES;
 constexpr int B_BUF_BYTES = OZ_SL * B_SLICE_BYTES;
-constexpr int STAGE_BYTES = A_BUF_BYTES + B_BUF_BYTES;       // 96 KB
-constexpr int OZ_SMEM = 2 * STAGE_BYTES + 1024;              // double-buffered, + alignment slack
+constexpr int STAGE_BYTES = A_BUF_BYTES + B_BUF_BYTES;       // 80 KB
+constexpr int OZ_SMEM = 2 * STAGE_BYTES + 1024;              // two stages, + alignment slack
 constexpr uint32_t kIdesc = tc::idesc_bf16_f32(OZ_M, OZ_N);
+static_assert(2 * OZ_TBUF == 512, "two accumulator sets fill the TMEM columns");
 
 // signed 7-bit digit -> bf16 bits (exact: |d| <= 127)
 __device__ __forceinline__ uint32_t digit_bf16(int d) { return __float_as_uint((float)d) >> 16; }
@@ -126,20 +135,39 @@ __device__ __forceinline__ void issue_levels(uint32_t tmem, uint32_t a_base, uin
   }
 }
 
-// Fold the 8 level accumulators of this thread's TMEM lane, 32 columns, into H / Lo.
-__device__ __forceinline__ void fold_levels(uint32_t lane_base, long long (&H)[32], long long (&Lo)[32]) {
-#pragma unroll 1
-  for (int d = 0; d < OZ_LEV; ++d) {
-    uint32_t r[32];
-    tc::tmem_ld32(lane_base + (uint32_t)(OZ_N * d), r);
-    tc::tmem_ld_wait();
-    const long long m = 1ll << (7 * (3 - (d & 3)));
-    if (d < 4) {
+// Fold one chunk's 8 level accumulators (this thread's TMEM lane, 16 columns at
+// taddr) into H (levels 0-3) and Lo (levels 4-7).  Levels are read in pairs and
+// combined in 32-bit first: v_2k 2^7 + v_2k+1 stays below 2^31 because a level-d
+// sum is bounded by 128 (d + 1) 127^2 (level 7: 16 516 096; pair 6-7:
+// 1 866 318 848).  Once the last pair is in registers the warp releases the
+// accumulator set (`tempty`), so the MMAs of a later chunk may overwrite it while
+// the integer work finishes.
+__device__ __forceinline__ void fold_chunk(uint32_t taddr, long long (&H)[16], long long (&Lo)[16],
+                                           uint64_t* tempty, int lane) {
+  uint32_t ra[16], rb[16];
+  int pr[16];
 #pragma unroll
-      for (int c = 0; c < 32; ++c) H[c] += (long long)__float2int_rn(__uint_as_float(r[c])) * m;
+  for (int g = 0; g < 4; ++g) {
+    tc::tmem_ld16(taddr + (uint32_t)(OZ_N * (2 * g)), ra);
+    tc::tmem_ld16(taddr + (uint32_t)(OZ_N * (2 * g + 1)), rb);
+    tc::tmem_ld_wait();
+    if (g == 3) {
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(tempty);
+    }
+    if ((g & 1) == 0) {
+#pragma unroll
+      for (int c = 0; c < 16; ++c)
+        pr[c] = __float2int_rn(__uint_as_float(ra[c])) * 128 + __float2int_rn(__uint_as_float(rb[c]));
     } else {
 #pragma unroll
-      for (int c = 0; c < 32; ++c) Lo[c] += (long long)__float2int_rn(__uint_as_float(r[c])) * m;
+      for (int c = 0; c < 16; ++c) {
+        const int lo = __float2int_rn(__uint_as_float(ra[c])) * 128 + __float2int_rn(__uint_as_float(rb[c]));
+        const long long v = (long long)pr[c] * 16384 + (long long)lo;
+        if (g == 1) H[c] += v;
+        else Lo[c] += v;
+      }
     }
   }
 }
@@ -365,13 +393,13 @@ __device__ __forceinline__ OzUnit oz_unit(const OzParams& p, int u) {
       w.n0 = (blockIdx.x % p.njb) * OZ_N;
     } else {
       int t = blockIdx.x, ib = 0;
-      while (ib < 4096 && t >= max(0, p.njb - 2 * ib)) {
-        t -= max(0, p.njb - 2 * ib);
+      while (ib < 4096 && t >= max(0, p.njb - OZ_NB * ib)) {
+        t -= max(0, p.njb - OZ_NB * ib);
         ++ib;
       }
       if (ib >= 4096) return w;
       w.m0 = ib * OZ_M;
-      w.n0 = (2 * ib + t) * OZ_N;
+      w.n0 = (OZ_NB * ib + t) * OZ_N;
     }
     w.sub0 = blockIdx.y * p.subs_per;
     w.nsub = min(total_subs, w.sub0 + p.subs_per) - w.sub0;
@@ -379,8 +407,13 @@ __device__ __forceinline__ OzUnit oz_unit(const OzParams& p, int u) {
     return w;
   }
   const int nrt = p.nrt > 0 ? p.nrt : (p.M + OZ_M - 1) / OZ_M, nct = (p.N + OZ_N - 1) / OZ_N;
-  if (u >= nrt * nct) return w;
-  const int rt = p.rt0 + u / nct, ct = u % nct;  // row tile outer: the CTAs of one row tile share its planes in L2
+  // Round k of the persistent loop covers units [k G, k G + G) (G = grid size);
+  // odd rounds run the CTAs in reverse order, so that with an upper triangular M
+  // (column tile ct costs ct + 1 sub-chunks) each CTA alternates cheap and
+  // dear column tiles instead of keeping one for every round.
+  const int G = (int)gridDim.x, k = u / G, v = (k & 1) ? k * G + (G - 1 - u % G) : u;
+  if (v >= nrt * nct) return w;
+  const int rt = p.rt0 + v / nct, ct = v % nct;  // row tile outer: the CTAs of one row tile share its planes in L2
   w.m0 = rt * OZ_M;
   w.n0 = ct * OZ_N;
   const int kmax = p.upper ? min(p.K, w.n0 + OZ_N) : p.K;
@@ -404,30 +437,49 @@ __device__ __forceinline__ void oz_load(const CUtensorMap* tmA, const CUtensorMa
   }
 }
 
+// Warp roles: warp OZ_TMA_WARP (one thread) streams the digit planes into two
+// shared-memory stages; warp OZ_MMA_WARP (one thread) issues each chunk's MMAs
+// into one of two TMEM accumulator sets; the OZ_CONS fold warps read a finished
+// set, fold it into int64 and, at the end of a unit, write the unit's outputs,
+// while the MMAs of the next chunk run in the other set.
+//   full[s]  : stage s loaded (TMA transaction bytes)     empty[s]  : stage s read by its MMAs (commit)
+//   tfull[b] : accumulator set b complete (commit)        tempty[b] : set b read by every fold warp
+// Every barrier completes once per use; use j of a two-slot resource is slot
+// j & 1, phase j >> 1, so a consumer waits for parity (j >> 1) & 1 and the
+// producer of use j waits for the release of use j - 2, parity ((j >> 1) & 1) ^ 1
+// (a fresh barrier reports that parity as complete).
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_oz_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const OzParams p) {
   extern __shared__ uint8_t oz_raw[];
   uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(oz_raw) + 1023) & ~uintptr_t(1023));
-  __shared__ uint64_t full[2], mdone[2];
+  __shared__ uint64_t full[2], empty[2], tfull[2], tempty[2], drain;
   __shared__ uint32_t tmem_sh;
   __shared__ volatile int abort_sh;
-  __shared__ int issued_sh, waited_sh;
+  __shared__ int skip_sh, issued_sh, consumed_sh;
 
-  if (p.mode == 1 && *(volatile const int*)p.status != 0) return;  // an earlier step of this ortho failed
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    // an earlier step of this ortho failed: every thread leaves before any setup
+    skip_sh = (p.mode == 1 && *(volatile const int*)p.status != 0) ? 1 : 0;
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&full[i], 1);
+      tc::mbar_init(&empty[i], 1);
+      tc::mbar_init(&tfull[i], 1);
+      tc::mbar_init(&tempty[i], OZ_CONS);
+    }
+    tc::mbar_init(&drain, 1);
+    tc::fence_mbar_init();
+    abort_sh = 0;
+    issued_sh = 0;
+    consumed_sh = 0;
+  }
+  __syncthreads();
+  if (skip_sh) return;
   if (warp == 0) {
     tc::tmem_alloc(&tmem_sh, 512);
     tc::tmem_relinquish();
   }
-  if (threadIdx.x == 0) {
-    for (int i = 0; i < 2; ++i) {
-      tc::mbar_init(&full[i], 1);
-      tc::mbar_init(&mdone[i], 1);
-    }
-    tc::fence_mbar_init();
-    abort_sh = 0;
-    issued_sh = 0;
-    waited_sh = 0;
+  if (warp == OZ_TMA_WARP && lane == 0) {
     tc::tma_prefetch_desc(&tmA);
     tc::tma_prefetch_desc(&tmB);
   }
@@ -435,131 +487,130 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_sh;
-  const uint32_t lane_base = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(32 * (warp >> 2));
 
-  // thread 0 owns the pipeline: loads of sub-chunk it+1 are in flight while the MMAs of it run.
-  // Both barriers complete once per use of their buffer, so the parity of the use at global
-  // sub-chunk index it is (it >> 1) & 1.
-  int u = blockIdx.x;
-  OzUnit w = oz_unit(p, u);
-  int it = 0;        // global sub-chunk index of this CTA
-  int issued = 0;    // sub-chunks whose loads were issued
-  int waited = 0;    // sub-chunks whose loads thread 0 saw complete
-  int mma_pend = -1; // global index of the last sub-chunk whose MMAs were committed and not yet waited for
-  if (threadIdx.x == 0 && w.valid) {
-    oz_load(&tmA, &tmB, p, w, 0, sm, &full[0]);
-    issued = 1;
-  }
-  while (w.valid && !abort_sh) {
-    long long H[32], Lo[32];
-#pragma unroll
-    for (int c = 0; c < 32; ++c) {
-      H[c] = 0;
-      Lo[c] = 0;
-    }
-    for (int s = 0; s < w.nsub; ++s, ++it) {
-      const int b = it & 1;
-      uint8_t* cur = sm + b * STAGE_BYTES;
-      if (threadIdx.x == 0 && !abort_sh) {
-        // prefetch the next sub-chunk (this unit or the next) into the other buffer
-        int sn = s + 1, un = u;
-        OzUnit wn = w;
-        if (sn >= w.nsub) {
-          un = oz_next_unit(p, u);
-          wn = un >= 0 ? oz_unit(p, un) : OzUnit{0, 0, 0, 0, false};
-          sn = 0;
-        }
-        if (wn.valid) {
-          if (mma_pend == it - 1 && mma_pend >= 0) {  // the other buffer's MMAs must be done
-            if (!tc::mbar_wait(&mdone[b ^ 1], (uint32_t)((mma_pend >> 1) & 1))) {
-              abort_sh = 1;
-              atomicExch(p.status, -2);
-            }
-            mma_pend = -1;
-          }
-          if (!abort_sh) {
-            oz_load(&tmA, &tmB, p, wn, sn, sm + (b ^ 1) * STAGE_BYTES, &full[b ^ 1]);
-            ++issued;
-          }
-        }
-        if (!abort_sh) {
-          if (tc::mbar_wait(&full[b], (uint32_t)((it >> 1) & 1))) {
-            ++waited;
-          } else {
+  if (warp == OZ_TMA_WARP) {
+    if (lane == 0) {
+      int it = 0;  // sub-chunks loaded by this CTA
+      for (int u = blockIdx.x; u >= 0 && !abort_sh; u = oz_next_unit(p, u)) {
+        const OzUnit w = oz_unit(p, u);
+        if (!w.valid) break;
+        for (int s = 0; s < w.nsub && !abort_sh; ++s, ++it) {
+          const int slot = it & 1;
+          if (!tc::mbar_wait(&empty[slot], (uint32_t)(((it >> 1) & 1) ^ 1))) {
             abort_sh = 1;
             atomicExch(p.status, -2);
+            break;
           }
+          oz_load(&tmA, &tmB, p, w, s, sm + slot * STAGE_BYTES, &full[slot]);
         }
-        if (!abort_sh) {
+      }
+      issued_sh = it;
+    }
+  } else if (warp == OZ_MMA_WARP) {
+    if (lane == 0) {
+      int it = 0, ch = 0;  // sub-chunks consumed, chunks issued
+      bool stop = false;
+      for (int u = blockIdx.x; u >= 0 && !stop; u = oz_next_unit(p, u)) {
+        const OzUnit w = oz_unit(p, u);
+        if (!w.valid) break;
+        for (int c0 = 0; c0 < w.nsub && !stop; c0 += OZ_SUBS, ++ch) {
+          const int b = ch & 1;
+          if (abort_sh || !tc::mbar_wait(&tempty[b], (uint32_t)(((ch >> 1) & 1) ^ 1))) {
+            stop = true;
+            break;
+          }
           tc::fence_after_sync();
-          issue_levels(tmem, tc::smem_u32(cur), tc::smem_u32(cur + A_BUF_BYTES), s % OZ_SUBS == 0);
-          tc::mma_commit(&mdone[b]);
-          mma_pend = it;
+          const int c1 = min(w.nsub, c0 + OZ_SUBS);
+          for (int s = c0; s < c1; ++s, ++it) {
+            const int slot = it & 1;
+            if (abort_sh || !tc::mbar_wait(&full[slot], (uint32_t)((it >> 1) & 1))) {
+              stop = true;
+              break;
+            }
+            tc::fence_after_sync();
+            uint8_t* cur = sm + slot * STAGE_BYTES;
+            issue_levels(tmem + (uint32_t)(b * OZ_TBUF), tc::smem_u32(cur), tc::smem_u32(cur + A_BUF_BYTES), s == c0);
+            tc::mma_commit(&empty[slot]);
+          }
+          if (stop) break;
+          tc::mma_commit(&tfull[b]);
         }
       }
-      if (s % OZ_SUBS == OZ_SUBS - 1 || s == w.nsub - 1) {
-        // chunk complete: every thread waits for its MMAs, then folds the 8 levels
-        __syncthreads();
-        if (abort_sh) break;
-        bool ok = tc::mbar_wait(&mdone[b], (uint32_t)((it >> 1) & 1));
-        if (!__all_sync(0xffffffffu, ok ? 1 : 0)) {
-          abort_sh = 1;
-          atomicExch(p.status, -2);
-        }
-        __syncthreads();
-        if (abort_sh) break;
-        if (threadIdx.x == 0) mma_pend = -1;
-        tc::fence_after_sync();
-        fold_levels(lane_base, H, Lo);
-        tc::fence_before_sync();
-        __syncthreads();
+      if (stop && !abort_sh) {
+        abort_sh = 1;
+        atomicExch(p.status, -2);
       }
+      consumed_sh = it;
+      // every MMA this thread issued has finished once this commit arrives
+      tc::mma_commit(&drain);
+      if (!tc::mbar_wait(&drain, 0)) atomicExch(p.status, -2);
     }
-    if (abort_sh) break;
-    // epilogue of the unit
-    const int row = w.m0 + 32 * (warp & 3) + lane;
-    if (p.mode == 0) {
-      if (row < p.M) {
+  } else {
+    const int q = warp & 3, h = warp >> 2;  // TMEM lane quadrant, column half
+    const uint32_t tl = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(16 * h);
+    int ch = 0;
+    bool stop = false;
+    for (int u = blockIdx.x; u >= 0 && !stop; u = oz_next_unit(p, u)) {
+      const OzUnit w = oz_unit(p, u);
+      if (!w.valid) break;
+      long long H[16], Lo[16];
 #pragma unroll
-        for (int c = 0; c < 32; ++c) {
-          const int col = w.n0 + 32 * (warp >> 2) + c;
-          if (col < p.N) {
-            atomicAdd(p.Hacc + (size_t)row * p.N + col, (unsigned long long)H[c]);
-            atomicAdd(p.Lacc + (size_t)row * p.N + col, (unsigned long long)Lo[c]);
+      for (int c = 0; c < 16; ++c) {
+        H[c] = 0;
+        Lo[c] = 0;
+      }
+      for (int c0 = 0; c0 < w.nsub; c0 += OZ_SUBS, ++ch) {
+        const int b = ch & 1;
+        const bool ok = !abort_sh && tc::mbar_wait(&tfull[b], (uint32_t)((ch >> 1) & 1));
+        if (!__all_sync(0xffffffffu, ok ? 1 : 0)) {
+          stop = true;
+          break;
+        }
+        tc::fence_after_sync();
+        fold_chunk(tl + (uint32_t)(b * OZ_TBUF), H, Lo, &tempty[b], lane);
+      }
+      if (stop) break;
+      const int row = w.m0 + 32 * q + lane;
+      if (p.mode == 0) {
+        if (row < p.M) {
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const int col = w.n0 + 16 * h + c;
+            if (col < p.N) {
+              atomicAdd(p.Hacc + (size_t)row * p.N + col, (unsigned long long)H[c]);
+              atomicAdd(p.Lacc + (size_t)row * p.N + col, (unsigned long long)Lo[c]);
+            }
+          }
+        }
+      } else if (row < p.M) {
+        const int er = exp_of_max(p.eA[row]);
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          const int j = w.n0 + 16 * h + c;
+          if (j < p.N) {
+            double* o = p.Cout + row + (size_t)j * p.ldo;
+            double v = (p.zero_row1 && row == 1) ? 0.0 : fold_to_double(H[c], Lo[c], er + exp_of_max(p.eB[j]));
+            if (p.accumulate) v += *o;
+            *o = v;
           }
         }
       }
-    } else if (row < p.M) {
-      const int er = exp_of_max(p.eA[row]);
-#pragma unroll
-      for (int c = 0; c < 32; ++c) {
-        const int j = w.n0 + 32 * (warp >> 2) + c;
-        if (j < p.N) {
-          double* o = p.Cout + row + (size_t)j * p.ldo;
-          double v = (p.zero_row1 && row == 1) ? 0.0 : fold_to_double(H[c], Lo[c], er + exp_of_max(p.eB[j]));
-          if (p.accumulate) v += *o;
-          *o = v;
-        }
-      }
     }
-    u = oz_next_unit(p, u);
-    w = u >= 0 ? oz_unit(p, u) : OzUnit{0, 0, 0, 0, false};
-  }
-  if (threadIdx.x == 0) {
-    issued_sh = issued;
-    waited_sh = waited;
+    if (stop && lane == 0 && !abort_sh) {
+      abort_sh = 1;
+      atomicExch(p.status, -2);
+    }
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    // after an abort: loads issued but never waited for still land in shared memory, and
-    // committed MMAs still read it -- wait for both before the CTA exits
-    for (int j = waited_sh; j < issued_sh; ++j) tc::mbar_wait(&full[j & 1], (uint32_t)((j >> 1) & 1));
-    if (mma_pend >= 0) tc::mbar_wait(&mdone[mma_pend & 1], (uint32_t)((mma_pend >> 1) & 1));
+  if (warp == OZ_TMA_WARP && lane == 0) {
+    // loads issued but never consumed (after an abort) still land in shared
+    // memory: wait for them before the CTA exits (at most one per stage)
+    for (int j = consumed_sh; j < issued_sh; ++j) tc::mbar_wait(&full[j & 1], (uint32_t)((j >> 1) & 1));
   }
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) {
-    __syncwarp();
+    tc::fence_after_sync();
     tc::tmem_dealloc(tmem, 512);
   }
 }
@@ -640,9 +691,9 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, unsig
   const int nib = (n + OZ_M - 1) / OZ_M;
   const int njb = (n + OZ_N - 1) / OZ_N;
   int ntiles = 0;
-  for (int ib = 0; ib < nib; ++ib) ntiles += std::max(0, njb - 2 * ib);
+  for (int ib = 0; ib < nib; ++ib) ntiles += std::max(0, njb - OZ_NB * ib);
   const int total_subs = (K + OZ_KS - 1) / OZ_KS;
-  int nsplit = std::max(1, std::min((total_subs + OZ_SUBS - 1) / OZ_SUBS, 148 / std::max(1, ntiles)));
+  int nsplit = std::max(1, std::min((total_subs + OZ_SUBS - 1) / OZ_SUBS, (c.nsm > 0 ? c.nsm : 148) / std::max(1, ntiles)));
   int subs_per = (total_subs + nsplit - 1) / nsplit;
   subs_per = ((subs_per + OZ_SUBS - 1) / OZ_SUBS) * OZ_SUBS;
   nsplit = (total_subs + subs_per - 1) / subs_per;
@@ -709,7 +760,7 @@ int xovlap_tc(Ctx& c, const double* X, int ldx, const double* Y, int ldy, int n,
   const int nib = (n + OZ_M - 1) / OZ_M, njb = (n + OZ_N - 1) / OZ_N;
   const int ntiles = nib * njb;
   const int total_subs = (K + OZ_KS - 1) / OZ_KS;
-  int nsplit = std::max(1, std::min((total_subs + OZ_SUBS - 1) / OZ_SUBS, 148 / std::max(1, ntiles)));
+  int nsplit = std::max(1, std::min((total_subs + OZ_SUBS - 1) / OZ_SUBS, (c.nsm > 0 ? c.nsm : 148) / std::max(1, ntiles)));
   int subs_per = (total_subs + nsplit - 1) / nsplit;
   subs_per = ((subs_per + OZ_SUBS - 1) / OZ_SUBS) * OZ_SUBS;
   nsplit = (total_subs + subs_per - 1) / subs_per;
@@ -860,7 +911,7 @@ int ovlap_tc_ranges(Ctx& c, const double* Ar, int lda, int n, const int* kb, int
   const int nib = (n + OZ_M - 1) / OZ_M;
   const int njb = (n + OZ_N - 1) / OZ_N;
   int ntiles = 0;
-  for (int ib = 0; ib < nib; ++ib) ntiles += std::max(0, njb - 2 * ib);
+  for (int ib = 0; ib < nib; ++ib) ntiles += std::max(0, njb - OZ_NB * ib);
   const size_t nn = (size_t)n * n;
   const size_t ks = ((size_t)K + 7) & ~size_t(7);
   const size_t bytes = (size_t)R * (2 * nn * 8 + (size_t)n * 8);
@@ -894,7 +945,7 @@ int ovlap_tc_ranges(Ctx& c, const double* Ar, int lda, int n, const int* kb, int
       GBCP_LAUNCH_CHECK(c);
     }
     const int total_subs = (Kr + OZ_KS - 1) / OZ_KS;
-    int nsplit = std::max(1, std::min((total_subs + OZ_SUBS - 1) / OZ_SUBS, 148 / std::max(1, ntiles)));
+    int nsplit = std::max(1, std::min((total_subs + OZ_SUBS - 1) / OZ_SUBS, (c.nsm > 0 ? c.nsm : 148) / std::max(1, ntiles)));
     int subs_per = (total_subs + nsplit - 1) / nsplit;
     subs_per = ((subs_per + OZ_SUBS - 1) / OZ_SUBS) * OZ_SUBS;
     nsplit = (total_subs + subs_per - 1) / subs_per;
