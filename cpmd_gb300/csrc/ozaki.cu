@@ -32,7 +32,7 @@
 // kernels into eight bf16 digit planes in HBM (row-major, K contiguous, planes
 // stacked along rows), and the GEMM kernel streams them with TMA (64-byte
 // swizzle, K = 32 per sub-chunk, two shared-memory stages).  The CTA is split by
-// role: one thread issues the TMA loads, one thread the 72 MMAs per sub-chunk,
+// role: one thread issues the TMA loads, one thread the 16 MMAs per sub-chunk,
 // and eight warps fold a finished accumulator set into int64 and write the
 // outputs while the MMAs of the next chunk fill the other set, so that the
 // integer fold and the FP64 rounding run beside the tensor core instead of
@@ -70,8 +70,8 @@ constexpr int A_BUF_BYTES = OZ_SL * A_SLICE_BYTES;
 constexpr int B_BUF_BYTES = OZ_SL * B_SLICE_BYTES;
 constexpr int STAGE_BYTES = A_BUF_BYTES + B_BUF_BYTES;       // 80 KB
 constexpr int OZ_SMEM = 2 * STAGE_BYTES + 1024;              // two stages, + alignment slack
-constexpr uint32_t kIdesc = tc::idesc_bf16_f32(OZ_M, OZ_N);
 static_assert(2 * OZ_TBUF == 512, "two accumulator sets fill the TMEM columns");
+static_assert(OZ_N * OZ_LEV <= 256 && OZ_SL == OZ_LEV, "one MMA covers the levels s..7 of A plane s");
 
 // signed 7-bit digit -> bf16 bits (exact: |d| <= 127)
 __device__ __forceinline__ uint32_t digit_bf16(int d) { return __float_as_uint((float)d) >> 16; }
@@ -113,24 +113,23 @@ __device__ __forceinline__ void digits8(const double (&x)[8], int E, uint4 (&out
   for (int s = 0; s < OZ_SL; ++s) out[s] = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
 }
 
-// Issue the 72 MMAs of one sub-chunk (36 digit pairs x 2 K-steps) into the 8
-// level accumulators; `first` restarts the accumulators (chunk start).  Fully
-// unrolled: every descriptor is its base plus (byte offset >> 4), so the single
-// issuing thread spends two or three instructions per MMA.
+// Issue the MMAs of one sub-chunk (all 36 digit pairs, 2 K-steps) into the 8
+// level accumulators at tmem (level d at column OZ_N d); `first` restarts them
+// (chunk start).  The B planes t = 0..7 of a stage lie back to back, each a
+// K-major 64-byte-swizzle tile of OZ_N rows, so planes t = 0..7-s read as one
+// B operand of OZ_N (8 - s) rows; with D at level s, its column block t lands in
+// level s + t.  One MMA per A plane and K-step (8 x 2 instead of 36 x 2) reads
+// each A plane from shared memory once per K-step, not once per pair.
 __device__ __forceinline__ void issue_levels(uint32_t tmem, uint32_t a_base, uint32_t b_base, bool first) {
   const uint64_t a0 = tc::sdesc_kmajor_sw64(a_base), b0 = tc::sdesc_kmajor_sw64(b_base);
 #pragma unroll
-  for (int d = 0; d < OZ_LEV; ++d) {
-    const uint32_t dt = tmem + (uint32_t)(OZ_N * d);
+  for (int kk = 0; kk < 2; ++kk) {
 #pragma unroll
-    for (int s = 0; s <= d; ++s) {
-      const int u = d - s;
-#pragma unroll
-      for (int kk = 0; kk < 2; ++kk) {
-        const uint64_t ad = a0 + (uint64_t)((s * A_SLICE_BYTES + kk * 32) >> 4);
-        const uint64_t bd = b0 + (uint64_t)((u * B_SLICE_BYTES + kk * 32) >> 4);
-        tc::mma_f16(dt, ad, bd, kIdesc, (first && s == 0 && kk == 0) ? 0u : 1u);
-      }
+    for (int s = 0; s < OZ_SL; ++s) {
+      const uint64_t ad = a0 + (uint64_t)((s * A_SLICE_BYTES + kk * 32) >> 4);
+      const uint64_t bd = b0 + (uint64_t)((kk * 32) >> 4);
+      tc::mma_f16(tmem + (uint32_t)(OZ_N * s), ad, bd, tc::idesc_bf16_f32(OZ_M, OZ_N * (OZ_LEV - s)),
+                  (first && kk == 0 && s == 0) ? 0u : 1u);
     }
   }
 }
@@ -172,30 +171,33 @@ __device__ __forceinline__ void fold_chunk(uint32_t taddr, long long (&H)[16], l
   }
 }
 
-// (H 2^28 + Lo) 2^(ee-63) as a correctly rounded double, with integer
-// instructions only (the FP64 pipe, 1/58 of FP32 on GB300, would otherwise
-// bound the epilogue).  Results below the normal range flush to zero.
+// (H 2^28 + Lo) 2^(ee-63) as a correctly rounded double (nearest, ties to even),
+// with 64-bit integer instructions only and no data-dependent branch but the
+// zero test (the FP64 pipe, 1/58 of FP32 on GB300, would otherwise bound the
+// epilogue).  Valid for |H| < 2^62.  The value is rewritten as T 2^28 + r with
+// T = H + floor(Lo / 2^28) and 0 <= r < 2^28; its magnitude |T'| 2^28 + r' is
+// cut to a 64-bit window W (the bits below it only matter as a sticky bit) and
+// W is rounded to 53 bits.  Results below the normal range flush to zero.
 __device__ __forceinline__ double fold_to_double(long long H, long long Lo, int ee) {
-  __int128 v = ((__int128)H << 28) + (__int128)Lo;
-  const bool neg = v < 0;
-  unsigned __int128 m = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
-  if (m == 0) return 0.0;
-  const unsigned long long hi = (unsigned long long)(m >> 64), lo = (unsigned long long)m;
-  int top = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);  // index of the leading bit
-  unsigned long long mant;
-  const int sh = top - 52;
-  if (sh > 0) {
-    mant = (unsigned long long)(m >> sh);
-    const unsigned __int128 rem = m & (((unsigned __int128)1 << sh) - 1);
-    const unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
-    if (rem > half || (rem == half && (mant & 1ull))) {
-      if (++mant == (1ull << 53)) {
-        mant >>= 1;
-        ++top;
-      }
-    }
-  } else {
-    mant = lo << (-sh);
+  const long long T = H + (Lo >> 28);
+  const unsigned long long r = (unsigned long long)Lo & 0xFFFFFFFull;
+  const bool neg = T < 0;
+  const unsigned long long Tm = neg ? (unsigned long long)(-T) - (r != 0 ? 1ull : 0ull) : (unsigned long long)T;
+  const unsigned long long rm = neg ? ((0x10000000ull - r) & 0xFFFFFFFull) : r;
+  if ((Tm | rm) == 0) return 0.0;
+  const int msbT = 63 - __clzll((long long)Tm);  // -1 when Tm == 0
+  const int sh0 = msbT > 35 ? msbT - 35 : 0;     // bits of rm below the window
+  const unsigned long long W = (Tm << (28 - sh0)) | (rm >> sh0);
+  const bool sticky = (rm & ((1ull << sh0) - 1)) != 0;
+  const int lz = __clzll((long long)W);
+  const unsigned long long Wn = W << lz;
+  int top = 63 - lz + sh0;  // index of the leading bit of the magnitude
+  unsigned long long mant = Wn >> 11;
+  const unsigned long long low = Wn & 0x7FFull;
+  mant += (low > 0x400ull || (low == 0x400ull && (sticky || (mant & 1ull)))) ? 1ull : 0ull;
+  if (mant >> 53) {
+    mant >>= 1;
+    ++top;
   }
   const int be = top + ee - 63 + 1023;
   if (be <= 0) return neg ? -0.0 : 0.0;
