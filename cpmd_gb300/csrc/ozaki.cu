@@ -207,6 +207,35 @@ __device__ __forceinline__ double fold_to_double(long long H, long long Lo, int 
   return __longlong_as_double((long long)bits);
 }
 
+// The C M epilogue's conversion: (H 2^28 + Lo) 2^(ee-63) to within
+// 2^(s+ee-63) + half an ulp, about a third of the integer instructions of
+// fold_to_double (whose 64-bit chain bounded that epilogue).  The low s bits of
+// Lo are dropped, so x = H 2^(28-s) + floor(Lo 2^-s) fits in 64 bits (a K-chunk's
+// level sums give |H| < 2^42.03 and |Lo| < 2^44.4; with m chunks, s = 9 +
+// ceil(log2 m) keeps |x| < 2^62), and x is rounded to nearest even.  The dropped
+// part, below 2^(s-63) = 2^-54 of the scale 2^(E_i+E_j) for one chunk, lies
+// under the truncation of the split itself (levels s + t > 7, 2^-49 of the
+// scale per product term).
+__device__ __forceinline__ double fold_to_double_fast(long long H, long long Lo, int ee, int s) {
+  const long long x = (long long)((unsigned long long)H << (28 - s)) + (Lo >> s);
+  const unsigned long long sg = (unsigned long long)x & (1ull << 63);
+  const unsigned long long a = x < 0 ? (unsigned long long)(-x) : (unsigned long long)x;
+  const int lz = __clzll((long long)a);        // 64 when a == 0
+  const unsigned long long m = a << (lz & 63);  // leading bit at 63 (0 when a == 0)
+  const unsigned long long q = m >> 11;         // 53 bits
+  const unsigned long long low = m & 0x7FFull;
+  const unsigned long long r = q + ((low > 0x400ull || (low == 0x400ull && (q & 1ull))) ? 1ull : 0ull);
+  const int be = (63 - lz) + s + ee - 63 + 1023;  // biased exponent of the leading bit
+  // r in [2^52, 2^53]: its leading bit (and a rounding carry) lands in the exponent field
+  unsigned long long bits = sg | (((unsigned long long)(be - 1) << 52) + r);
+  // selects, no branch, so that the compiler can interleave the conversions of
+  // a thread's 16 outputs: zero and results below the normal range give signed
+  // zero, results above it infinity (the scales of real operands are far inside)
+  bits = (a == 0 || be <= 0) ? sg : bits;
+  bits = be >= 2046 ? (sg | 0x7FF0000000000000ull) : bits;
+  return __longlong_as_double((long long)bits);
+}
+
 // ---------------------------------------------------------------- exponent pre-passes
 // column maxima |a_kj| over k (state columns of the real view): bits into cmax[j]
 __global__ void k_col_max(const double* __restrict__ Ar, int lda, int K, int n, int kper,
@@ -555,6 +584,18 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     for (int u = blockIdx.x; u >= 0 && !stop; u = oz_next_unit(p, u)) {
       const OzUnit w = oz_unit(p, u);
       if (!w.valid) break;
+      const int row = w.m0 + 32 * q + lane;
+      // mode 1: the scale exponents of this thread's outputs, read before the
+      // fold so that their latency hides behind it (loaded between the output
+      // stores they would be serialised with them: the compiler cannot tell
+      // that the exponent arrays and the output do not overlap)
+      int eo[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const int j = w.n0 + 16 * h + c;
+        eo[c] = (p.mode == 1 && j < p.N) ? exp_of_max(__ldg(p.eB + j)) : 0;
+      }
+      const int er = (p.mode == 1 && row < p.M) ? exp_of_max(__ldg(p.eA + row)) : 0;
       long long H[16], Lo[16];
 #pragma unroll
       for (int c = 0; c < 16; ++c) {
@@ -572,7 +613,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         fold_chunk(tl + (uint32_t)(b * OZ_TBUF), H, Lo, &tempty[b], lane);
       }
       if (stop) break;
-      const int row = w.m0 + 32 * q + lane;
       if (p.mode == 0) {
         if (row < p.M) {
 #pragma unroll
@@ -585,15 +625,24 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           }
         }
       } else if (row < p.M) {
-        const int er = exp_of_max(p.eA[row]);
+        double* o = p.Cout + row + (size_t)(w.n0 + 16 * h) * p.ldo;
+        const int ncol = min(16, p.N - (w.n0 + 16 * h));
+        int sdrop = 9;  // 9 + ceil(log2(chunks))
+        for (int m = 1; m < (w.nsub + OZ_SUBS - 1) / OZ_SUBS; m *= 2) ++sdrop;
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
-          const int j = w.n0 + 16 * h + c;
-          if (j < p.N) {
-            double* o = p.Cout + row + (size_t)j * p.ldo;
-            double v = (p.zero_row1 && row == 1) ? 0.0 : fold_to_double(H[c], Lo[c], er + exp_of_max(p.eB[j]));
-            if (p.accumulate) v += *o;
-            *o = v;
+        for (int g = 0; g < 16; g += 8) {
+          double prev[8];
+          if (p.accumulate) {  // the group's reads before its stores
+#pragma unroll
+            for (int c = 0; c < 8; ++c) prev[c] = g + c < ncol ? o[(size_t)(g + c) * p.ldo] : 0.0;
+          }
+#pragma unroll
+          for (int c = 0; c < 8; ++c) {
+            if (g + c < ncol) {
+              double v = (p.zero_row1 && row == 1) ? 0.0 : fold_to_double_fast(H[g + c], Lo[g + c], er + eo[g + c], sdrop);
+              if (p.accumulate) v += prev[c];
+              o[(size_t)(g + c) * p.ldo] = v;
+            }
           }
         }
       }
