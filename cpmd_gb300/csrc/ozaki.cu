@@ -33,7 +33,7 @@
 // stacked along rows), and the GEMM kernel streams them with TMA (64-byte
 // swizzle, K = 32 per sub-chunk, two shared-memory stages).  The CTA is split by
 // role: one thread issues the TMA loads, one thread the 16 MMAs per sub-chunk,
-// and eight warps fold a finished accumulator set into int64 and write the
+// and sixteen warps fold a finished accumulator set into int64 and write the
 // outputs while the MMAs of the next chunk fill the other set, so that the
 // integer fold and the FP64 rounding run beside the tensor core instead of
 // between its chunks.  Every mbarrier wait is bounded; on expiry the kernel sets
@@ -60,7 +60,8 @@ constexpr int OZ_KS = 32;      // K per sub-chunk (two MMAs of K = 16)
 constexpr int OZ_SUBS = 4;     // sub-chunks per exact accumulation chunk (K = 128)
 constexpr int OZ_SL = 8;       // digit slices
 constexpr int OZ_LEV = 8;      // levels kept (s + t <= 7)
-constexpr int OZ_CONS = 8;     // fold / epilogue warps (two per TMEM lane quadrant)
+constexpr int OZ_CONS = 16;    // fold / epilogue warps (four per TMEM lane quadrant)
+constexpr int OZ_CW = OZ_N / (OZ_CONS / 4);  // output columns per fold warp
 constexpr int OZ_TMA_WARP = OZ_CONS, OZ_MMA_WARP = OZ_CONS + 1;
 constexpr int OZ_THREADS = 32 * (OZ_CONS + 2);
 constexpr int OZ_TBUF = OZ_LEV * OZ_N;  // TMEM columns of one accumulator set (two sets: 512)
@@ -72,6 +73,7 @@ constexpr int STAGE_BYTES = A_BUF_BYTES + B_BUF_BYTES;       // 80 KB
 constexpr int OZ_SMEM = 2 * STAGE_BYTES + 1024;              // two stages, + alignment slack
 static_assert(2 * OZ_TBUF == 512, "two accumulator sets fill the TMEM columns");
 static_assert(OZ_N * OZ_LEV <= 256 && OZ_SL == OZ_LEV, "one MMA covers the levels s..7 of A plane s");
+static_assert(OZ_CW % 8 == 0, "fold warps read TMEM 8 columns at a time");
 
 // signed 7-bit digit -> bf16 bits (exact: |d| <= 127)
 __device__ __forceinline__ uint32_t digit_bf16(int d) { return __float_as_uint((float)d) >> 16; }
@@ -134,21 +136,21 @@ __device__ __forceinline__ void issue_levels(uint32_t tmem, uint32_t a_base, uin
   }
 }
 
-// Fold one chunk's 8 level accumulators (this thread's TMEM lane, 16 columns at
+// Fold one chunk's 8 level accumulators (this thread's TMEM lane, OZ_CW columns at
 // taddr) into H (levels 0-3) and Lo (levels 4-7).  Levels are read in pairs and
 // combined in 32-bit first: v_2k 2^7 + v_2k+1 stays below 2^31 because a level-d
 // sum is bounded by 128 (d + 1) 127^2 (level 7: 16 516 096; pair 6-7:
 // 1 866 318 848).  Once the last pair is in registers the warp releases the
 // accumulator set (`tempty`), so the MMAs of a later chunk may overwrite it while
 // the integer work finishes.
-__device__ __forceinline__ void fold_chunk(uint32_t taddr, long long (&H)[16], long long (&Lo)[16],
+__device__ __forceinline__ void fold_chunk(uint32_t taddr, long long (&H)[OZ_CW], long long (&Lo)[OZ_CW],
                                            uint64_t* tempty, int lane) {
-  uint32_t ra[16], rb[16];
-  int pr[16];
+  uint32_t ra[OZ_CW], rb[OZ_CW];
+  int pr[OZ_CW];
 #pragma unroll
   for (int g = 0; g < 4; ++g) {
-    tc::tmem_ld16(taddr + (uint32_t)(OZ_N * (2 * g)), ra);
-    tc::tmem_ld16(taddr + (uint32_t)(OZ_N * (2 * g + 1)), rb);
+    tc::tmem_ld8(taddr + (uint32_t)(OZ_N * (2 * g)), ra);
+    tc::tmem_ld8(taddr + (uint32_t)(OZ_N * (2 * g + 1)), rb);
     tc::tmem_ld_wait();
     if (g == 3) {
       tc::fence_before_sync();
@@ -157,11 +159,11 @@ __device__ __forceinline__ void fold_chunk(uint32_t taddr, long long (&H)[16], l
     }
     if ((g & 1) == 0) {
 #pragma unroll
-      for (int c = 0; c < 16; ++c)
+      for (int c = 0; c < OZ_CW; ++c)
         pr[c] = __float2int_rn(__uint_as_float(ra[c])) * 128 + __float2int_rn(__uint_as_float(rb[c]));
     } else {
 #pragma unroll
-      for (int c = 0; c < 16; ++c) {
+      for (int c = 0; c < OZ_CW; ++c) {
         const int lo = __float2int_rn(__uint_as_float(ra[c])) * 128 + __float2int_rn(__uint_as_float(rb[c]));
         const long long v = (long long)pr[c] * 16384 + (long long)lo;
         if (g == 1) H[c] += v;
@@ -229,7 +231,7 @@ __device__ __forceinline__ double fold_to_double_fast(long long H, long long Lo,
   // r in [2^52, 2^53]: its leading bit (and a rounding carry) lands in the exponent field
   unsigned long long bits = sg | (((unsigned long long)(be - 1) << 52) + r);
   // selects, no branch, so that the compiler can interleave the conversions of
-  // a thread's 16 outputs: zero and results below the normal range give signed
+  // a thread's outputs: zero and results below the normal range give signed
   // zero, results above it infinity (the scales of real operands are far inside)
   bits = (a == 0 || be <= 0) ? sg : bits;
   bits = be >= 2046 ? (sg | 0x7FF0000000000000ull) : bits;
@@ -577,8 +579,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       if (!tc::mbar_wait(&drain, 0)) atomicExch(p.status, -2);
     }
   } else {
-    const int q = warp & 3, h = warp >> 2;  // TMEM lane quadrant, column half
-    const uint32_t tl = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(16 * h);
+    const int q = warp & 3, h = warp >> 2;  // TMEM lane quadrant, column group
+    const uint32_t tl = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(OZ_CW * h);
     int ch = 0;
     bool stop = false;
     for (int u = blockIdx.x; u >= 0 && !stop; u = oz_next_unit(p, u)) {
@@ -589,16 +591,16 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       // fold so that their latency hides behind it (loaded between the output
       // stores they would be serialised with them: the compiler cannot tell
       // that the exponent arrays and the output do not overlap)
-      int eo[16];
+      int eo[OZ_CW];
 #pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        const int j = w.n0 + 16 * h + c;
+      for (int c = 0; c < OZ_CW; ++c) {
+        const int j = w.n0 + OZ_CW * h + c;
         eo[c] = (p.mode == 1 && j < p.N) ? exp_of_max(__ldg(p.eB + j)) : 0;
       }
       const int er = (p.mode == 1 && row < p.M) ? exp_of_max(__ldg(p.eA + row)) : 0;
-      long long H[16], Lo[16];
+      long long H[OZ_CW], Lo[OZ_CW];
 #pragma unroll
-      for (int c = 0; c < 16; ++c) {
+      for (int c = 0; c < OZ_CW; ++c) {
         H[c] = 0;
         Lo[c] = 0;
       }
@@ -616,8 +618,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       if (p.mode == 0) {
         if (row < p.M) {
 #pragma unroll
-          for (int c = 0; c < 16; ++c) {
-            const int col = w.n0 + 16 * h + c;
+          for (int c = 0; c < OZ_CW; ++c) {
+            const int col = w.n0 + OZ_CW * h + c;
             if (col < p.N) {
               atomicAdd(p.Hacc + (size_t)row * p.N + col, (unsigned long long)H[c]);
               atomicAdd(p.Lacc + (size_t)row * p.N + col, (unsigned long long)Lo[c]);
@@ -625,12 +627,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           }
         }
       } else if (row < p.M) {
-        double* o = p.Cout + row + (size_t)(w.n0 + 16 * h) * p.ldo;
-        const int ncol = min(16, p.N - (w.n0 + 16 * h));
+        double* o = p.Cout + row + (size_t)(w.n0 + OZ_CW * h) * p.ldo;
+        const int ncol = min(OZ_CW, p.N - (w.n0 + OZ_CW * h));
         int sdrop = 9;  // 9 + ceil(log2(chunks))
         for (int m = 1; m < (w.nsub + OZ_SUBS - 1) / OZ_SUBS; m *= 2) ++sdrop;
 #pragma unroll
-        for (int g = 0; g < 16; g += 8) {
+        for (int g = 0; g < OZ_CW; g += 8) {
           double prev[8];
           if (p.accumulate) {  // the group's reads before its stores
 #pragma unroll
