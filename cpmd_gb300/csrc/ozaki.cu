@@ -239,15 +239,24 @@ __device__ __forceinline__ double fold_to_double_fast(long long H, long long Lo,
 }
 
 // ---------------------------------------------------------------- exponent pre-passes
-// column maxima |a_kj| over k (state columns of the real view): bits into cmax[j]
+// column maxima |a_kj| over k (state columns of the real view): bits into cmax[j].
+// Eight independent loads per thread and pass keep enough reads in flight for
+// the HBM bandwidth (one dependent load per pass left the kernel latency-bound).
 __global__ void k_col_max(const double* __restrict__ Ar, int lda, int K, int n, int kper,
                           unsigned long long* __restrict__ cmax) {
   const int j = blockIdx.x;
   const int k0 = blockIdx.y * kper, k1 = min(K, k0 + kper);
+  const unsigned long long* a = reinterpret_cast<const unsigned long long*>(Ar) + (size_t)j * lda;
   unsigned long long mx = 0;
-  for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(Ar[k + (size_t)j * lda]) & ~(1ull << 63);
-    mx = b > mx ? b : mx;
+  for (int kb = k0 + threadIdx.x; kb < k1; kb += 8 * blockDim.x) {
+    unsigned long long b[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int k = kb + u * blockDim.x;
+      b[u] = k < k1 ? (__ldg(a + k) & ~(1ull << 63)) : 0ull;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) mx = b[u] > mx ? b[u] : mx;
   }
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long v = __shfl_down_sync(0xffffffffu, mx, o);
@@ -256,16 +265,26 @@ __global__ void k_col_max(const double* __restrict__ Ar, int lda, int K, int n, 
   if ((threadIdx.x & 31) == 0 && mx) atomicMax(cmax + j, mx);
 }
 
-// column maxima of a small row-major n x n matrix M over its rows
-__global__ void k_mat_col_max(const double* __restrict__ M, int n, unsigned long long* __restrict__ cmax) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
+// column maxima of a small row-major n x n matrix M over its rows: block = 32
+// columns x 8 row groups, reduced in shared memory
+__global__ void __launch_bounds__(256) k_mat_col_max(const double* __restrict__ M, int n,
+                                                     unsigned long long* __restrict__ cmax) {
+  __shared__ unsigned long long red[8][33];
+  const int j = blockIdx.x * 32 + threadIdx.x, g = threadIdx.y;
   unsigned long long mx = 0;
-  for (int k = 0; k < n; ++k) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(M[(size_t)k * n + j]) & ~(1ull << 63);
-    mx = b > mx ? b : mx;
+  if (j < n) {
+    for (int k = g; k < n; k += 8) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong(__ldg(M + (size_t)k * n + j)) & ~(1ull << 63);
+      mx = b > mx ? b : mx;
+    }
   }
-  cmax[j] = mx;
+  red[g][threadIdx.x] = mx;
+  __syncthreads();
+  if (g == 0 && j < n) {
+#pragma unroll
+    for (int q = 1; q < 8; ++q) mx = red[q][threadIdx.x] > mx ? red[q][threadIdx.x] : mx;
+    cmax[j] = mx;
+  }
 }
 
 // ---------------------------------------------------------------- digit planes
@@ -894,7 +913,7 @@ int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, 
   unsigned long long* mcmax = rmax + rows;
   {
     ProfScope ps_(c, "k_mat_col_max");
-    k_mat_col_max<<<(n + 255) / 256, 256, 0, c.stream>>>(M, n, mcmax);
+    k_mat_col_max<<<(n + 31) / 32, dim3(32, 8), 0, c.stream>>>(M, n, mcmax);
     GBCP_LAUNCH_CHECK(c);
   }
   if (n <= 256) {
@@ -1042,7 +1061,7 @@ int rmul_tc_ranges(Ctx& c, const double* A, int lda, int rows, int n, const doub
   unsigned long long* mcmax = rmax + rows;
   {
     ProfScope ps_(c, "k_mat_col_max");
-    k_mat_col_max<<<(n + 255) / 256, 256, 0, c.stream>>>(M, n, mcmax);
+    k_mat_col_max<<<(n + 31) / 32, dim3(32, 8), 0, c.stream>>>(M, n, mcmax);
     GBCP_LAUNCH_CHECK(c);
   }
   {
