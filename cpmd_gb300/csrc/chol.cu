@@ -65,6 +65,7 @@ __device__ __forceinline__ int pivot_bad(double d, double thr) {
 __global__ void __launch_bounds__(8 * B) k_chol_diag(const double* __restrict__ S, double* __restrict__ Uw,
                                                      double* __restrict__ X, const double* __restrict__ diag0, int n,
                                                      int k, int* __restrict__ status) {
+  pdl_entry();
   __shared__ double z[B][B + 1];
   __shared__ double udiag[B];
   __shared__ int bad_sh;
@@ -172,6 +173,7 @@ __device__ __forceinline__ void load_cols_t(const double* __restrict__ M, int n,
 __global__ void __launch_bounds__(RG * B) k_chol_panel(const double* __restrict__ S, const double* __restrict__ X,
                                                        double* __restrict__ Uw, int n, int k,
                                                        const int* __restrict__ status) {
+  pdl_entry();
   __shared__ double a[B][B + 1];
   __shared__ double xt[RG][B + 1];
   const int j = k + 1 + blockIdx.x, r0 = blockIdx.y * RG;
@@ -190,6 +192,7 @@ __global__ void __launch_bounds__(RG * B) k_chol_panel(const double* __restrict_
 // triangle, blockIdx.y the row group of block row i
 __global__ void __launch_bounds__(RG * B) k_chol_update(double* __restrict__ S, const double* __restrict__ Uw, int n,
                                                         int nb, int k, const int* __restrict__ status) {
+  pdl_entry();
   __shared__ double uj[B][B + 1];
   __shared__ double ui[RG][B + 1];
   const int m0 = nb - k - 1;  // trailing block count
@@ -216,6 +219,7 @@ __global__ void __launch_bounds__(RG * B) k_chol_update(double* __restrict__ S, 
 __global__ void __launch_bounds__(RG * B) k_trtri_v(double* __restrict__ S, const double* __restrict__ Uw,
                                                     const double* __restrict__ X, int n, int nb,
                                                     const int* __restrict__ status) {
+  pdl_entry();
   __shared__ double u[B][B + 1];
   __shared__ double xi[RG][B + 1];
   int t = blockIdx.x, bi = 0;
@@ -239,6 +243,7 @@ __global__ void __launch_bounds__(RG * B) k_trtri_v(double* __restrict__ S, cons
 // blockIdx.x = i, blockIdx.y the row group
 __global__ void __launch_bounds__(RG * B) k_trtri_diag(const double* __restrict__ S, double* __restrict__ X, int n,
                                                        int d, const int* __restrict__ status) {
+  pdl_entry();
   __shared__ double xk[B][B + 1];
   __shared__ double v[RG][B + 1];
   const int bi = blockIdx.x, bj = bi + d, r0 = blockIdx.y * RG;
@@ -259,6 +264,7 @@ __global__ void __launch_bounds__(RG * B) k_trtri_diag(const double* __restrict_
 
 // zero the strict lower triangle of X and keep the original diagonal of S
 __global__ void k_zero_lower(double* __restrict__ X, const double* __restrict__ S, double* __restrict__ diag0, int n) {
+  pdl_entry();
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * n; e += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(e / n), j = (int)(e % n);
     if (j < i) X[e] = 0.0;
@@ -278,38 +284,37 @@ int chol_inverse(Ctx& c, double* S, double* X, int n) {
   const dim3 blk(RG * B);
   {
     ProfScope ps_(c, "k_chol_misc");
-    k_zero_lower<<<std::max(1, std::min(256, (n * n + 255) / 256)), 256, 0, c.stream>>>(X, S, diag0, n);
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_zero_lower, dim3(std::max(1, std::min(256, (n * n + 255) / 256))), dim3(256), 0, X,
+                    (const double*)S, diag0, n);
   }
   for (int k = 0; k < nb; ++k) {
     {
       ProfScope ps_(c, "k_chol_diag");
-      k_chol_diag<<<1, 8 * B, 0, c.stream>>>(S, Uw, X, diag0, n, k, c.d_info);
-      GBCP_LAUNCH_CHECK(c);
+      GBCP_LAUNCH_PDL(c, k_chol_diag, dim3(1), dim3(8 * B), 0, (const double*)S, Uw, X, (const double*)diag0, n, k,
+                      c.d_info);
     }
     const int m0 = nb - k - 1;
     if (m0 > 0) {
       {
         ProfScope ps_(c, "k_chol_panel");
-        k_chol_panel<<<dim3(m0, B / RG), blk, 0, c.stream>>>(S, X, Uw, n, k, c.d_info);
-        GBCP_LAUNCH_CHECK(c);
+        GBCP_LAUNCH_PDL(c, k_chol_panel, dim3(m0, B / RG), blk, 0, (const double*)S, (const double*)X, Uw, n, k,
+                        (const int*)c.d_info);
       }
       {
         ProfScope ps_(c, "k_chol_update");
-        k_chol_update<<<dim3(m0 * (m0 + 1) / 2, B / RG), blk, 0, c.stream>>>(S, Uw, n, nb, k, c.d_info);
-        GBCP_LAUNCH_CHECK(c);
+        GBCP_LAUNCH_PDL(c, k_chol_update, dim3(m0 * (m0 + 1) / 2, B / RG), blk, 0, S, (const double*)Uw, n, nb, k,
+                        (const int*)c.d_info);
       }
     }
   }
   if (nb > 1) {
     ProfScope ps_(c, "k_trtri_v");
-    k_trtri_v<<<dim3(nb * (nb - 1) / 2, B / RG), blk, 0, c.stream>>>(S, Uw, X, n, nb, c.d_info);
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_trtri_v, dim3(nb * (nb - 1) / 2, B / RG), blk, 0, S, (const double*)Uw, (const double*)X, n,
+                    nb, (const int*)c.d_info);
   }
   for (int d = 1; d < nb; ++d) {
     ProfScope ps_(c, "k_trtri_diag");
-    k_trtri_diag<<<dim3(nb - d, B / RG), blk, 0, c.stream>>>(S, X, n, d, c.d_info);
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_trtri_diag, dim3(nb - d, B / RG), blk, 0, (const double*)S, X, n, d, (const int*)c.d_info);
   }
   return 0;
 }

@@ -11,6 +11,14 @@ template <typename T> struct alignas(2 * sizeof(T)) cx {
   T x, y;
 };
 
+// First statement of a kernel launched with launch_pdl: let the next kernel on
+// the stream be scheduled, then wait until the previous one has finished and
+// its writes are visible.  Harmless in a kernel launched the ordinary way.
+__device__ __forceinline__ void pdl_entry() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 template <typename T> __host__ __device__ __forceinline__ cx<T> mk(T a, T b) { cx<T> r; r.x = a; r.y = b; return r; }
 template <typename T> __device__ __forceinline__ cx<T> operator+(cx<T> a, cx<T> b) { return mk<T>(a.x + b.x, a.y + b.y); }
 template <typename T> __device__ __forceinline__ cx<T> operator-(cx<T> a, cx<T> b) { return mk<T>(a.x - b.x, a.y - b.y); }

@@ -7,12 +7,35 @@
 #include <mutex>
 #include <string>
 #include <unordered_map>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
 #include "fft_core.cuh"
 
 namespace gbcp {
+
+// Programmatic dependent launch for chains of small dependent kernels: the
+// kernel may be scheduled while its predecessor on the stream still runs and
+// must call pdl_entry() before its first global-memory access (that waits for
+// the predecessor grid to finish and its writes to be visible), so only the
+// launch latency overlaps.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
+
 
 extern std::atomic<long long> g_launches;
 inline void count_launch(int n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
@@ -256,6 +279,18 @@ int nl_fnonloc(Ctx& c, cx<double>* c2, int ldc2, int nstate, const double* f, in
   do {                                                                           \
     ::gbcp::count_launch();                                                      \
     cudaError_t e_ = cudaGetLastError();                                         \
+    if (e_ != cudaSuccess) {                                                     \
+      (ctx).err = std::string("launch: ") + cudaGetErrorString(e_) + " at " + __FILE__ + ":" + std::to_string(__LINE__); \
+      return 5;                                                                  \
+    }                                                                            \
+  } while (0)
+
+// GBCP_LAUNCH_PDL: launch_pdl with the error handling of GBCP_LAUNCH_CHECK.
+#define GBCP_LAUNCH_PDL(ctx, kernel, grid, block, smem, ...)                      \
+  do {                                                                           \
+    ::gbcp::count_launch();                                                      \
+    cudaError_t e_ = ::gbcp::launch_pdl(kernel, grid, block, smem, (ctx).stream, __VA_ARGS__); \
+    if (e_ == cudaSuccess) e_ = cudaGetLastError();                              \
     if (e_ != cudaSuccess) {                                                     \
       (ctx).err = std::string("launch: ") + cudaGetErrorString(e_) + " at " + __FILE__ + ":" + std::to_string(__LINE__); \
       return 5;                                                                  \
