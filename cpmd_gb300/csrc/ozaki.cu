@@ -244,6 +244,7 @@ __device__ __forceinline__ double fold_to_double_fast(long long H, long long Lo,
 // the HBM bandwidth (one dependent load per pass left the kernel latency-bound).
 __global__ void k_col_max(const double* __restrict__ Ar, int lda, int K, int n, int kper,
                           unsigned long long* __restrict__ cmax) {
+  pdl_entry();
   const int j = blockIdx.x;
   const int k0 = blockIdx.y * kper, k1 = min(K, k0 + kper);
   const unsigned long long* a = reinterpret_cast<const unsigned long long*>(Ar) + (size_t)j * lda;
@@ -269,6 +270,7 @@ __global__ void k_col_max(const double* __restrict__ Ar, int lda, int K, int n, 
 // columns x 8 row groups, reduced in shared memory
 __global__ void __launch_bounds__(256) k_mat_col_max(const double* __restrict__ M, int n,
                                                      unsigned long long* __restrict__ cmax) {
+  pdl_entry();
   __shared__ unsigned long long red[8][33];
   const int j = blockIdx.x * 32 + threadIdx.x, g = threadIdx.y;
   unsigned long long mx = 0;
@@ -292,7 +294,8 @@ __global__ void __launch_bounds__(256) k_mat_col_max(const double* __restrict__ 
 // k0: first row of the slab (a multiple of 8); rows k0 .. k0+K-1 of Ar go to plane columns k0 ..
 __global__ void k_oz_slice_cols(const double* __restrict__ Ar, int lda, int K, int n,
                                 const unsigned long long* __restrict__ emax, size_t ks, uint4* __restrict__ out,
-                                int k0 = 0) {
+                                int k0) {
+  pdl_entry();
   const int j = blockIdx.y;
   const int k = (blockIdx.x * blockDim.x + threadIdx.x) * 8;
   if (k >= K) return;
@@ -311,6 +314,7 @@ __global__ void k_oz_slice_cols(const double* __restrict__ Ar, int lda, int K, i
 // row maxima of the real view over the n states: bits into rmax[r]
 __global__ void k_row_max(const double* __restrict__ Ar, int lda, int rows, int n,
                           unsigned long long* __restrict__ rmax) {
+  pdl_entry();
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= rows) return;
   unsigned long long mx = 0;
@@ -326,6 +330,7 @@ __global__ void k_row_max(const double* __restrict__ Ar, int lda, int rows, int 
 // and each plane store is one full 32-byte sector.
 __global__ void k_oz_slice_rows(const double* __restrict__ Ar, int lda, int rows, int n,
                                 const unsigned long long* __restrict__ emax, size_t ks, uint4* __restrict__ out) {
+  pdl_entry();
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   const int k = blockIdx.y * 16;
   if (r >= rows) return;
@@ -354,6 +359,7 @@ __global__ void k_oz_slice_rows(const double* __restrict__ Ar, int lda, int rows
 __global__ void __launch_bounds__(512) k_oz_slice_rows_max(const double* __restrict__ Ar, int lda, int rows, int n,
                                                            unsigned long long* __restrict__ rmax, size_t ks,
                                                            uint4* __restrict__ out, int r0, int r1) {
+  pdl_entry();
   __shared__ unsigned long long red[16][33];
   const int r = r0 + blockIdx.x * 32 + threadIdx.x, k = threadIdx.y * 16;
   double x0[8], x1[8];
@@ -394,6 +400,7 @@ __global__ void __launch_bounds__(512) k_oz_slice_rows_max(const double* __restr
 // C M operand B: plane s, row j (column of M), columns k < n: M[k][j]; exponent per column of M.
 __global__ void k_oz_slice_mat(const double* __restrict__ M, int n, const unsigned long long* __restrict__ emax,
                                size_t ks, uint4* __restrict__ out) {
+  pdl_entry();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int k = blockIdx.y * 8;
   if (j >= n) return;
@@ -502,6 +509,7 @@ __device__ __forceinline__ void oz_load(const CUtensorMap* tmA, const CUtensorMa
 // (a fresh barrier reports that parity as complete).
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_oz_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const OzParams p) {
+  pdl_entry();
   extern __shared__ uint8_t oz_raw[];
   uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(oz_raw) + 1023) & ~uintptr_t(1023));
   __shared__ uint64_t full[2], empty[2], tfull[2], tempty[2], drain;
@@ -692,6 +700,7 @@ __global__ void k_ozaki_syrk_finalize(const long long* __restrict__ H, const lon
                                       const unsigned long long* __restrict__ cmax, int n,
                                       const double* __restrict__ Ar, int lda, int geq0, double* __restrict__ S,
                                       unsigned long long* __restrict__ scond_bits) {
+  pdl_entry();
   double mx = 0.0;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * n;
        e += (size_t)gridDim.x * blockDim.x) {
@@ -714,6 +723,7 @@ __global__ void k_ozaki_xov_finalize(const long long* __restrict__ H, const long
                                      const unsigned long long* __restrict__ xmax,
                                      const unsigned long long* __restrict__ ymax, int n, const double* __restrict__ X,
                                      int ldx, const double* __restrict__ Y, int ldy, int geq0, double* __restrict__ A) {
+  pdl_entry();
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)n * n;
        e += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(e / n), j = (int)(e % n);
@@ -729,6 +739,7 @@ __global__ void k_ozaki_syrk_finalize_ranges(const long long* __restrict__ H, co
                                              const unsigned long long* __restrict__ cmax, int R, int n,
                                              const double* __restrict__ Ar, int lda, int geq0,
                                              double* __restrict__ S, unsigned long long* __restrict__ scond_bits) {
+  pdl_entry();
   const size_t nn = (size_t)n * n;
   double mx = 0.0;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nn; e += (size_t)gridDim.x * blockDim.x) {
@@ -782,14 +793,12 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, unsig
     ProfScope ps_(c, "k_col_max");
     const int kspl = std::max(1, std::min(64, (K + 4095) / 4096));
     const int kper = (K + kspl - 1) / kspl;
-    k_col_max<<<dim3(n, kspl), 256, 0, c.stream>>>(Ar, lda, K, n, kper, cmax);
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_col_max, dim3(n, kspl), dim3(256), 0, Ar, lda, K, n, kper, cmax);
   }
   {
     ProfScope ps_(c, "k_oz_slice");
-    k_oz_slice_cols<<<dim3((K / 8 + 255) / 256 + 1, n), 256, 0, c.stream>>>(Ar, lda, K, n, cmax, ks,
-                                                                            static_cast<uint4*>(c.oz_a.p));
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_oz_slice_cols, dim3((K / 8 + 255) / 256 + 1, n), dim3(256), 0, Ar, lda, K, n, cmax, ks,
+        static_cast<uint4*>(c.oz_a.p), 0);
   }
   CUtensorMap ma, mb;
   if (!tmap_bf16_2d(&ma, c.oz_a.p, K, (long long)OZ_SL * n, (int)ks, OZ_KS, OZ_M, 64) ||
@@ -810,16 +819,13 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, unsig
   {
     allow_smem(k_oz_tc, OZ_SMEM);
     ProfScope ps_(c, "k_ozaki_syrk");
-    k_oz_tc<<<dim3(ntiles, nsplit), OZ_THREADS, OZ_SMEM, c.stream>>>(ma, mb, p);
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_oz_tc, dim3(ntiles, nsplit), dim3(OZ_THREADS), OZ_SMEM, ma, mb, p);
   }
   {
     ProfScope ps_(c, "k_ozaki_syrk_finalize");
     const int fb = std::max(1, std::min(1024, (int)((nn + 255) / 256)));
-    k_ozaki_syrk_finalize<<<fb, 256, 0, c.stream>>>(reinterpret_cast<const long long*>(Hacc),
-                                                    reinterpret_cast<const long long*>(Lacc), cmax, n, Ar, lda, c.geq0,
-                                                    S, scond_bits);
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_ozaki_syrk_finalize, dim3(fb), dim3(256), 0, reinterpret_cast<const long long*>(Hacc),
+        reinterpret_cast<const long long*>(Lacc), cmax, n, Ar, lda, c.geq0, S, scond_bits);
   }
   return 0;
 }
@@ -851,19 +857,15 @@ int xovlap_tc(Ctx& c, const double* X, int ldx, const double* Y, int ldy, int n,
     ProfScope ps_(c, "k_col_max");
     const int kspl = std::max(1, std::min(64, (K + 4095) / 4096));
     const int kper = (K + kspl - 1) / kspl;
-    k_col_max<<<dim3(n, kspl), 256, 0, c.stream>>>(X, ldx, K, n, kper, xmax);
-    GBCP_LAUNCH_CHECK(c);
-    k_col_max<<<dim3(n, kspl), 256, 0, c.stream>>>(Y, ldy, K, n, kper, ymax);
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_col_max, dim3(n, kspl), dim3(256), 0, X, ldx, K, n, kper, xmax);
+    GBCP_LAUNCH_PDL(c, k_col_max, dim3(n, kspl), dim3(256), 0, Y, ldy, K, n, kper, ymax);
   }
   {
     ProfScope ps_(c, "k_oz_slice");
-    k_oz_slice_cols<<<dim3((K / 8 + 255) / 256 + 1, n), 256, 0, c.stream>>>(X, ldx, K, n, xmax, ks,
-                                                                            static_cast<uint4*>(c.oz_a.p));
-    GBCP_LAUNCH_CHECK(c);
-    k_oz_slice_cols<<<dim3((K / 8 + 255) / 256 + 1, n), 256, 0, c.stream>>>(Y, ldy, K, n, ymax, ks,
-                                                                            static_cast<uint4*>(c.oz_b.p));
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_oz_slice_cols, dim3((K / 8 + 255) / 256 + 1, n), dim3(256), 0, X, ldx, K, n, xmax, ks,
+        static_cast<uint4*>(c.oz_a.p), 0);
+    GBCP_LAUNCH_PDL(c, k_oz_slice_cols, dim3((K / 8 + 255) / 256 + 1, n), dim3(256), 0, Y, ldy, K, n, ymax, ks,
+        static_cast<uint4*>(c.oz_b.p), 0);
   }
   CUtensorMap ma, mb;
   if (!tmap_bf16_2d(&ma, c.oz_a.p, K, (long long)OZ_SL * n, (int)ks, OZ_KS, OZ_M, 64) ||
@@ -885,16 +887,13 @@ int xovlap_tc(Ctx& c, const double* X, int ldx, const double* Y, int ldy, int n,
   {
     allow_smem(k_oz_tc, OZ_SMEM);
     ProfScope ps_(c, "k_ozaki_xov");
-    k_oz_tc<<<dim3(ntiles, nsplit), OZ_THREADS, OZ_SMEM, c.stream>>>(ma, mb, p);
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_oz_tc, dim3(ntiles, nsplit), dim3(OZ_THREADS), OZ_SMEM, ma, mb, p);
   }
   {
     ProfScope ps_(c, "k_ozaki_syrk_finalize");
     const int fb = std::max(1, std::min(1024, (int)((nn + 255) / 256)));
-    k_ozaki_xov_finalize<<<fb, 256, 0, c.stream>>>(reinterpret_cast<const long long*>(Hacc),
-                                                   reinterpret_cast<const long long*>(Lacc), xmax, ymax, n, X, ldx, Y,
-                                                   ldy, c.geq0, A);
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_ozaki_xov_finalize, dim3(fb), dim3(256), 0, reinterpret_cast<const long long*>(Hacc),
+        reinterpret_cast<const long long*>(Lacc), xmax, ymax, n, X, ldx, Y, ldy, c.geq0, A);
   }
   return 0;
 }
@@ -913,31 +912,25 @@ int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, 
   unsigned long long* mcmax = rmax + rows;
   {
     ProfScope ps_(c, "k_mat_col_max");
-    k_mat_col_max<<<(n + 31) / 32, dim3(32, 8), 0, c.stream>>>(M, n, mcmax);
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_mat_col_max, dim3((n + 31) / 32), dim3(32, 8), 0, M, n, mcmax);
   }
   if (n <= 256) {
     ProfScope ps_(c, "k_oz_slice");
-    k_oz_slice_rows_max<<<(rows + 31) / 32, dim3(32, (n + 15) / 16), 0, c.stream>>>(A, lda, rows, n, rmax, ks,
-                                                                                   static_cast<uint4*>(c.oz_a.p), 0,
-                                                                                   rows);
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_oz_slice_rows_max, dim3((rows + 31) / 32), dim3(32, (n + 15) / 16), 0, A, lda, rows, n, rmax,
+        ks, static_cast<uint4*>(c.oz_a.p), 0, rows);
   } else {
     {
       ProfScope ps_(c, "k_row_max");
-      k_row_max<<<(rows + 255) / 256, 256, 0, c.stream>>>(A, lda, rows, n, rmax);
-      GBCP_LAUNCH_CHECK(c);
+      GBCP_LAUNCH_PDL(c, k_row_max, dim3((rows + 255) / 256), dim3(256), 0, A, lda, rows, n, rmax);
     }
     ProfScope ps_(c, "k_oz_slice");
-    k_oz_slice_rows<<<dim3((rows + 127) / 128, (n + 15) / 16), 128, 0, c.stream>>>(A, lda, rows, n, rmax, ks,
-                                                                                  static_cast<uint4*>(c.oz_a.p));
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_oz_slice_rows, dim3((rows + 127) / 128, (n + 15) / 16), dim3(128), 0, A, lda, rows, n, rmax,
+        ks, static_cast<uint4*>(c.oz_a.p));
   }
   {
     ProfScope ps_(c, "k_oz_slice");
-    k_oz_slice_mat<<<dim3((n + 127) / 128, (n + 7) / 8), 128, 0, c.stream>>>(M, n, mcmax, ks,
-                                                                            static_cast<uint4*>(c.oz_b.p));
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_oz_slice_mat, dim3((n + 127) / 128, (n + 7) / 8), dim3(128), 0, M, n, mcmax, ks,
+        static_cast<uint4*>(c.oz_b.p));
   }
   CUtensorMap ma, mb;
   if (!tmap_bf16_2d(&ma, c.oz_a.p, n, (long long)OZ_SL * rows, (int)ks, OZ_KS, OZ_M, 64) ||
@@ -966,8 +959,7 @@ int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, 
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int grid = std::max(1, std::min(ntiles, nsm));
     ProfScope ps_(c, "k_ozaki_rmul");
-    k_oz_tc<<<grid, OZ_THREADS, OZ_SMEM, c.stream>>>(ma, mb, p);
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_oz_tc, dim3(grid), dim3(OZ_THREADS), OZ_SMEM, ma, mb, p);
   }
   return 0;
 }
@@ -1007,14 +999,12 @@ int ovlap_tc_ranges(Ctx& c, const double* Ar, int lda, int n, const int* kb, int
       ProfScope ps_(c, "k_col_max");
       const int kspl = std::max(1, std::min(64, (Kr + 4095) / 4096));
       const int kper = (Kr + kspl - 1) / kspl;
-      k_col_max<<<dim3(n, kspl), 256, 0, c.stream>>>(Ar + k0, lda, Kr, n, kper, cmax + (size_t)r * n);
-      GBCP_LAUNCH_CHECK(c);
+      GBCP_LAUNCH_PDL(c, k_col_max, dim3(n, kspl), dim3(256), 0, Ar + k0, lda, Kr, n, kper, cmax + (size_t)r * n);
     }
     {
       ProfScope ps_(c, "k_oz_slice");
-      k_oz_slice_cols<<<dim3((Kr / 8 + 255) / 256 + 1, n), 256, 0, c.stream>>>(
-          Ar, lda, Kr, n, cmax + (size_t)r * n, ks, static_cast<uint4*>(c.oz_a.p), k0);
-      GBCP_LAUNCH_CHECK(c);
+      GBCP_LAUNCH_PDL(c, k_oz_slice_cols, dim3((Kr / 8 + 255) / 256 + 1, n), dim3(256), 0, Ar, lda, Kr, n,
+          cmax + (size_t)r * n, ks, static_cast<uint4*>(c.oz_a.p), k0);
     }
     const int total_subs = (Kr + OZ_KS - 1) / OZ_KS;
     int nsplit = std::max(1, std::min((total_subs + OZ_SUBS - 1) / OZ_SUBS, (c.nsm > 0 ? c.nsm : 148) / std::max(1, ntiles)));
@@ -1033,16 +1023,13 @@ int ovlap_tc_ranges(Ctx& c, const double* Ar, int lda, int n, const int* kb, int
     p.Lacc = Lacc + (size_t)r * nn;
     p.status = status;
     ProfScope ps_(c, "k_ozaki_syrk");
-    k_oz_tc<<<dim3(ntiles, nsplit), OZ_THREADS, OZ_SMEM, c.stream>>>(ma, mb, p);
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_oz_tc, dim3(ntiles, nsplit), dim3(OZ_THREADS), OZ_SMEM, ma, mb, p);
   }
   {
     ProfScope ps_(c, "k_ozaki_syrk_finalize");
     const int fb = std::max(1, std::min(1024, (int)((nn + 255) / 256)));
-    k_ozaki_syrk_finalize_ranges<<<fb, 256, 0, c.stream>>>(reinterpret_cast<const long long*>(Hacc),
-                                                           reinterpret_cast<const long long*>(Lacc), cmax, R, n, Ar,
-                                                           lda, c.geq0, S, scond_bits);
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_ozaki_syrk_finalize_ranges, dim3(fb), dim3(256), 0, reinterpret_cast<const long long*>(Hacc),
+        reinterpret_cast<const long long*>(Lacc), cmax, R, n, Ar, lda, c.geq0, S, scond_bits);
   }
   return 0;
 }
@@ -1061,21 +1048,17 @@ int rmul_tc_ranges(Ctx& c, const double* A, int lda, int rows, int n, const doub
   unsigned long long* mcmax = rmax + rows;
   {
     ProfScope ps_(c, "k_mat_col_max");
-    k_mat_col_max<<<(n + 31) / 32, dim3(32, 8), 0, c.stream>>>(M, n, mcmax);
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_mat_col_max, dim3((n + 31) / 32), dim3(32, 8), 0, M, n, mcmax);
   }
   {
     ProfScope ps_(c, "k_oz_slice");
     if (n > 256) {  // no fused row-maximum slicer: all rows up front
-      k_row_max<<<(rows + 255) / 256, 256, 0, c.stream>>>(A, lda, rows, n, rmax);
-      GBCP_LAUNCH_CHECK(c);
-      k_oz_slice_rows<<<dim3((rows + 127) / 128, (n + 15) / 16), 128, 0, c.stream>>>(A, lda, rows, n, rmax, ks,
-                                                                                    static_cast<uint4*>(c.oz_a.p));
-      GBCP_LAUNCH_CHECK(c);
+      GBCP_LAUNCH_PDL(c, k_row_max, dim3((rows + 255) / 256), dim3(256), 0, A, lda, rows, n, rmax);
+      GBCP_LAUNCH_PDL(c, k_oz_slice_rows, dim3((rows + 127) / 128, (n + 15) / 16), dim3(128), 0, A, lda, rows, n,
+          rmax, ks, static_cast<uint4*>(c.oz_a.p));
     }
-    k_oz_slice_mat<<<dim3((n + 127) / 128, (n + 7) / 8), 128, 0, c.stream>>>(M, n, mcmax, ks,
-                                                                            static_cast<uint4*>(c.oz_b.p));
-    GBCP_LAUNCH_CHECK(c);
+    GBCP_LAUNCH_PDL(c, k_oz_slice_mat, dim3((n + 127) / 128, (n + 7) / 8), dim3(128), 0, M, n, mcmax, ks,
+        static_cast<uint4*>(c.oz_b.p));
   }
   CUtensorMap ma, mb;
   if (!tmap_bf16_2d(&ma, c.oz_a.p, n, (long long)OZ_SL * rows, (int)ks, OZ_KS, OZ_M, 64) ||
@@ -1091,9 +1074,8 @@ int rmul_tc_ranges(Ctx& c, const double* A, int lda, int rows, int n, const doub
     if (r1 > r0) {
       if (n <= 256) {
         ProfScope ps_(c, "k_oz_slice");
-        k_oz_slice_rows_max<<<(r1 - r0 + 31) / 32, dim3(32, (n + 15) / 16), 0, c.stream>>>(
-            A, lda, rows, n, rmax, ks, static_cast<uint4*>(c.oz_a.p), r0, r1);
-        GBCP_LAUNCH_CHECK(c);
+        GBCP_LAUNCH_PDL(c, k_oz_slice_rows_max, dim3((r1 - r0 + 31) / 32), dim3(32, (n + 15) / 16), 0, A, lda, rows,
+            n, rmax, ks, static_cast<uint4*>(c.oz_a.p), r0, r1);
       }
       OzParams p{};
       p.M = rows;
@@ -1111,8 +1093,7 @@ int rmul_tc_ranges(Ctx& c, const double* A, int lda, int rows, int n, const doub
       p.nrt = (r1 - r0 + OZ_M - 1) / OZ_M;
       const int grid = std::max(1, std::min(p.nrt * nct, nsm));
       ProfScope ps_(c, "k_ozaki_rmul");
-      k_oz_tc<<<grid, OZ_THREADS, OZ_SMEM, c.stream>>>(ma, mb, p);
-      GBCP_LAUNCH_CHECK(c);
+      GBCP_LAUNCH_PDL(c, k_oz_tc, dim3(grid), dim3(OZ_THREADS), OZ_SMEM, ma, mb, p);
     }
     if (done && done[r]) GBCP_CUDA_TRY(c, cudaEventRecord(done[r], c.stream));
   }
