@@ -46,6 +46,7 @@
 #include <cuda.h>
 
 #include "ctx.h"
+#include "fold_round.h"
 #include "tc_common.cuh"
 #include "tc_gemm.h"
 
@@ -173,69 +174,15 @@ __device__ __forceinline__ void fold_chunk(uint32_t taddr, long long (&H)[OZ_CW]
   }
 }
 
-// (H 2^28 + Lo) 2^(ee-63) as a correctly rounded double (nearest, ties to even),
-// with 64-bit integer instructions only and no data-dependent branch but the
-// zero test (the FP64 pipe, 1/58 of FP32 on GB300, would otherwise bound the
-// epilogue).  Valid for |H| < 2^62.  The value is rewritten as T 2^28 + r with
-// T = H + floor(Lo / 2^28) and 0 <= r < 2^28; its magnitude |T'| 2^28 + r' is
-// cut to a 64-bit window W (the bits below it only matter as a sticky bit) and
-// W is rounded to 53 bits.  Results below the normal range flush to zero.
+// Conversions of the int64 level sums: fold_round.h (the S finalizers round
+// exactly; the C M epilogue uses the 62-bit window, whose dropped part, below
+// 2^-54 of the scale 2^(E_i+E_j) for one chunk, lies under the truncation of the
+// split itself: levels s + t > 7, 2^-49 of the scale per product term).
 __device__ __forceinline__ double fold_to_double(long long H, long long Lo, int ee) {
-  const long long T = H + (Lo >> 28);
-  const unsigned long long r = (unsigned long long)Lo & 0xFFFFFFFull;
-  const bool neg = T < 0;
-  const unsigned long long Tm = neg ? (unsigned long long)(-T) - (r != 0 ? 1ull : 0ull) : (unsigned long long)T;
-  const unsigned long long rm = neg ? ((0x10000000ull - r) & 0xFFFFFFFull) : r;
-  if ((Tm | rm) == 0) return 0.0;
-  const int msbT = 63 - __clzll((long long)Tm);  // -1 when Tm == 0
-  const int sh0 = msbT > 35 ? msbT - 35 : 0;     // bits of rm below the window
-  const unsigned long long W = (Tm << (28 - sh0)) | (rm >> sh0);
-  const bool sticky = (rm & ((1ull << sh0) - 1)) != 0;
-  const int lz = __clzll((long long)W);
-  const unsigned long long Wn = W << lz;
-  int top = 63 - lz + sh0;  // index of the leading bit of the magnitude
-  unsigned long long mant = Wn >> 11;
-  const unsigned long long low = Wn & 0x7FFull;
-  mant += (low > 0x400ull || (low == 0x400ull && (sticky || (mant & 1ull)))) ? 1ull : 0ull;
-  if (mant >> 53) {
-    mant >>= 1;
-    ++top;
-  }
-  const int be = top + ee - 63 + 1023;
-  if (be <= 0) return neg ? -0.0 : 0.0;
-  if (be >= 2047) return __longlong_as_double((long long)((neg ? (1ull << 63) : 0ull) | 0x7FF0000000000000ull));
-  const unsigned long long bits =
-      (neg ? (1ull << 63) : 0ull) | ((unsigned long long)be << 52) | (mant & 0xFFFFFFFFFFFFFull);
-  return __longlong_as_double((long long)bits);
+  return fold::to_double_exact(H, Lo, ee);
 }
-
-// The C M epilogue's conversion: (H 2^28 + Lo) 2^(ee-63) to within
-// 2^(s+ee-63) + half an ulp, about a third of the integer instructions of
-// fold_to_double (whose 64-bit chain bounded that epilogue).  The low s bits of
-// Lo are dropped, so x = H 2^(28-s) + floor(Lo 2^-s) fits in 64 bits (a K-chunk's
-// level sums give |H| < 2^42.03 and |Lo| < 2^44.4; with m chunks, s = 9 +
-// ceil(log2 m) keeps |x| < 2^62), and x is rounded to nearest even.  The dropped
-// part, below 2^(s-63) = 2^-54 of the scale 2^(E_i+E_j) for one chunk, lies
-// under the truncation of the split itself (levels s + t > 7, 2^-49 of the
-// scale per product term).
 __device__ __forceinline__ double fold_to_double_fast(long long H, long long Lo, int ee, int s) {
-  const long long x = (long long)((unsigned long long)H << (28 - s)) + (Lo >> s);
-  const unsigned long long sg = (unsigned long long)x & (1ull << 63);
-  const unsigned long long a = x < 0 ? (unsigned long long)(-x) : (unsigned long long)x;
-  const int lz = __clzll((long long)a);        // 64 when a == 0
-  const unsigned long long m = a << (lz & 63);  // leading bit at 63 (0 when a == 0)
-  const unsigned long long q = m >> 11;         // 53 bits
-  const unsigned long long low = m & 0x7FFull;
-  const unsigned long long r = q + ((low > 0x400ull || (low == 0x400ull && (q & 1ull))) ? 1ull : 0ull);
-  const int be = (63 - lz) + s + ee - 63 + 1023;  // biased exponent of the leading bit
-  // r in [2^52, 2^53]: its leading bit (and a rounding carry) lands in the exponent field
-  unsigned long long bits = sg | (((unsigned long long)(be - 1) << 52) + r);
-  // selects, no branch, so that the compiler can interleave the conversions of
-  // a thread's outputs: zero and results below the normal range give signed
-  // zero, results above it infinity (the scales of real operands are far inside)
-  bits = (a == 0 || be <= 0) ? sg : bits;
-  bits = be >= 2046 ? (sg | 0x7FF0000000000000ull) : bits;
-  return __longlong_as_double((long long)bits);
+  return fold::to_double_window(H, Lo, ee, s);
 }
 
 // ---------------------------------------------------------------- exponent pre-passes
@@ -656,8 +603,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       } else if (row < p.M) {
         double* o = p.Cout + row + (size_t)(w.n0 + OZ_CW * h) * p.ldo;
         const int ncol = min(OZ_CW, p.N - (w.n0 + OZ_CW * h));
-        int sdrop = 9;  // 9 + ceil(log2(chunks))
-        for (int m = 1; m < (w.nsub + OZ_SUBS - 1) / OZ_SUBS; m *= 2) ++sdrop;
+        const int sdrop = fold::window_drop_bits((w.nsub + OZ_SUBS - 1) / OZ_SUBS);
 #pragma unroll
         for (int g = 0; g < OZ_CW; g += 8) {
           double prev[8];
