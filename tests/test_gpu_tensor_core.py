@@ -70,9 +70,13 @@ def test_mixed_ortho_orthonormality_gate(gpu_lib):
     assert dev <= 1e-12
 
 
-@pytest.mark.parametrize("nstate,method", [(16, "gs"), (37, "gs"), (130, "gs"), (200, "gs"), (70, "lowdin")])
+@pytest.mark.parametrize("nstate,method", [(16, "gs"), (37, "gs"), (130, "gs"), (200, "gs"), (300, "gs"),
+                                           (70, "lowdin"), (300, "lowdin")])
 def test_ortho_tensor_cores_match_oracle(gpu_lib, nstate, method):
-    """Both GEMMs of ortho (S and C M) on the tensor cores give the FP64 result."""
+    """Both GEMMs of ortho (S and C M) on the tensor cores give the FP64 result.
+    300 states: C M slices its rows with the separate row-maximum pass, runs
+    three K-chunks (11 low bits dropped in the epilogue's window conversion) and
+    ends on a 12-column tile."""
     from cpmd_gb300 import Context
     cl = make_small_cell(10.26, 32, 20.0, nstate, seed=90 + nstate)
     c = perturbed(cl.c0, 0.03, nstate)
