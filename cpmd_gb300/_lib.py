@@ -11,7 +11,7 @@ LIB_PATH = _PKG / "libcpmd_gb300.so"
 GBCP_OK = 0
 STATUS = {
     0: "OK", 1: "ERR_ARG", 2: "ERR_NOT_SPD", 3: "ERR_NONFINITE", 4: "ERR_TIMEOUT",
-    5: "ERR_CUDA", 6: "ERR_NOMEM", 7: "ERR_UNSUPPORTED", 8: "ERR_NOT_CONVERGED",
+    5: "ERR_CUDA", 6: "ERR_NOMEM", 7: "ERR_UNSUPPORTED", 8: "ERR_NOT_CONVERGED", 9: "ERR_IO",
 }
 PREC = {"fp64": 0, "mixed": 1}
 MEM_HOST, MEM_DEVICE = 0, 1
@@ -72,12 +72,30 @@ SIGNATURES = {
     "gbcp_batch_step": (_I, [_P, _P, _I, _P, _P]),
     "gbcp_batch_graph_kernels": (_I, [_P, C.POINTER(C.c_int64)]),
     "gbcp_batch_last_error": (_I, [_P, _P, _I]),
+    "gbcp_restart_write": (_I, [C.c_char_p, _P]),
+    "gbcp_restart_read": (_I, [C.c_char_p, _P]),
 }
 
 
 class CellIO(C.Structure):
     _fields_ = [("c0", C.c_void_p), ("ldc", C.c_int32), ("nstate", C.c_int32), ("f", C.c_void_p),
                 ("vpot", C.c_void_p), ("rhoe", C.c_void_p), ("c2", C.c_void_p), ("ldc2", C.c_int32)]
+
+
+
+class Restart(C.Structure):
+    """gbcp_restart of include/cpmd_gb300.h."""
+    _fields_ = [("ibrav", C.c_int32), ("indpg", C.c_int32), ("celldm", C.c_double * 6),
+                ("nsp", C.c_int32), ("nat", C.c_int32), ("na", C.c_void_p),
+                ("tau0", C.c_void_p), ("taum", C.c_void_p), ("taui", C.c_void_p),
+                ("ecut", C.c_double), ("cdual", C.c_double), ("dual", C.c_int32), ("nel", C.c_int32),
+                ("nr1s", C.c_int32), ("nr2s", C.c_int32), ("nr3s", C.c_int32),
+                ("nstate", C.c_int32), ("nkpts", C.c_int32),
+                ("ngwks", C.c_int32), ("ngwls", C.c_int32), ("nhgs", C.c_int32), ("nhgls", C.c_int32),
+                ("c0", C.c_void_p), ("ldc", C.c_int32), ("ngw", C.c_int32), ("nstate_cap", C.c_int32),
+                ("icompr", C.c_int32), ("scale", C.c_double),
+                ("nstate_read", C.c_int32), ("nstate_file", C.c_int32), ("sections", C.c_int32)]
+
 
 _lib = None
 

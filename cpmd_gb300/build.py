@@ -17,7 +17,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libcpmd_gb300.so"
-SOURCES = ["band.cu", "band64.cu", "band32.cu", "linalg.cu", "chol.cu", "ozaki.cu", "nonlocal.cu", "tc_gemm.cu", "energy.cu", "batch.cu", "rortho.cu", "abi.cu"]
+SOURCES = ["band.cu", "band64.cu", "band32.cu", "linalg.cu", "chol.cu", "ozaki.cu", "nonlocal.cu", "tc_gemm.cu", "energy.cu", "batch.cu", "rortho.cu", "abi.cu", "restart.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -42,7 +42,8 @@ enum gbcp_status {
   GBCP_ERR_CUDA = 5,       /* CUDA runtime error */
   GBCP_ERR_NOMEM = 6,      /* device allocation failed */
   GBCP_ERR_UNSUPPORTED = 7,/* mesh size / option not supported */
-  GBCP_ERR_NOT_CONVERGED = 8 /* iterative Loewdin step or rortog iteration did not converge */
+  GBCP_ERR_NOT_CONVERGED = 8, /* iterative Loewdin step or rortog iteration did not converge */
+  GBCP_ERR_IO = 9          /* RESTART file cannot be opened, written, or is malformed */
 };
 
 enum gbcp_precision {
@@ -266,6 +267,52 @@ int gbcp_batch_step(gbcp_batch* batch, const gbcp_cell_io* io, int flags, double
 /* Kernels in the captured step graph (0 before the first step). */
 int gbcp_batch_graph_kernels(gbcp_batch* batch, int64_t* kernels);
 int gbcp_batch_last_error(gbcp_batch* batch, char* buf, int len);
+
+/* ---- RESTART wavefunction file (Gamma point) --------------------------------
+ * The reference's restart file (zhwwf/wv30, wv30_utils.mod.F90:99-233,235-1300;
+ * zhrwf/rv30, rv30_utils.mod.F90:104-2242): Fortran unformatted records with
+ * 4-byte length markers, sections 1..99 each opened by a record (irecord, fpos)
+ * giving the number of records that follow.  Written: 1 header, 2 cell,
+ * 3 species counts, 4 tau0, 5 taum, 6 taui (5 and 6 only when given), 7 cutoff /
+ * electrons / mesh, 8 states and plane-wave counts, 9 the states C0 in the
+ * w_wfnio layout (wfnio_utils.mod.F90:52-233: type 1, then per state the
+ * coefficients in the global G order, compress.F90: icompr 1 = FP64 as is,
+ * 2 = 32-bit fixed point on the scale max|c|), 10..99 empty.  Read: sections
+ * 1..9 of a sequential or STREAM file (icompr 1, 2, 4 or 8; the C0 format with a
+ * negative section-9 record count); the rest of the file is not read.
+ * The coefficient order is the reference's global G order, which is the order
+ * of the basis (inyh/hg) a context is created with. */
+typedef struct gbcp_restart {
+  int32_t ibrav, indpg;   /* section 2 (parm%ibrav, symmi%indpg) */
+  double celldm[6];       /* section 2 (cell_com%celldm) */
+  int32_t nsp, nat;       /* section 3: species and atoms */
+  int32_t* na;            /* (nsp) atoms per species */
+  double* tau0;           /* (3, nat) section 4, species-major like tau0(:,ia,is) */
+  double* taum;           /* (3, nat) section 5 (velocities); write: NULL = empty section */
+  double* taui;           /* (3, nat) section 6 (initial positions); write: NULL = empty */
+  double ecut, cdual;     /* section 7: cutoff (Ry), dual */
+  int32_t dual, nel;      /* section 7: dual flag, number of electrons */
+  int32_t nr1s, nr2s, nr3s;
+  int32_t nstate, nkpts;  /* section 8: crge%n, k points (0 = Gamma) */
+  int32_t ngwks, ngwls, nhgs, nhgls;
+  double* c0;             /* (ldc, nstate) complex; read: (ldc, nstate_cap), rows beyond the
+                             file's plane waves zeroed, states beyond nstate_read untouched */
+  int32_t ldc;            /* leading dimension of c0 (complex elements) */
+  int32_t ngw;            /* write: rows of c0 stored (the file's plane waves); read: rows of c0 filled */
+  int32_t nstate_cap;     /* read: states c0 can hold */
+  int32_t icompr;         /* write: 1 or 2; read: the file's */
+  double scale;           /* read: the file's compression scale */
+  int32_t nstate_read;    /* read: states stored into c0 */
+  int32_t nstate_file;    /* read: states in the file's section 9 */
+  int32_t sections;       /* read: bit (k-1) set when section k (1..9) held data */
+} gbcp_restart;
+/* Write `path` (overwritten). */
+int gbcp_restart_write(const char* path, const gbcp_restart* r);
+/* Read `path`: every scalar field of sections 2, 3, 7, 8 and 9 is filled; array
+ * fields that are NULL are skipped (call once with NULL arrays to learn nsp,
+ * nat, nstate, ngwks, then allocate).  Inputs: the array pointers, ldc, ngw and
+ * nstate_cap; min(nstate_cap, states in the file) states are stored. */
+int gbcp_restart_read(const char* path, gbcp_restart* r);
 
 #ifdef __cplusplus
 }
