@@ -80,6 +80,7 @@ void prof_fold(Ctx& c) {
   cudaStreamSynchronize(c.stream);
   if (c.copy) cudaStreamSynchronize(c.copy);
   if (c.copy_out) cudaStreamSynchronize(c.copy_out);
+  if (c.side) cudaStreamSynchronize(c.side);
   for (ProfRec& r : c.prof_live) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, r.a, r.b);
@@ -390,14 +391,15 @@ int gbcp_ctx_destroy(gbcp_ctx* h) {
                           &c.st_misc, &c.st_misc2, &c.st_vf, &c.red, &c.red2, &c.smat, &c.smat2, &c.smat3, &c.sparts, &c.cscr, &c.cdiag, &c.cwork, &c.xr_part, &c.xr_tk, &c.rt_mats, &c.en_g3, &c.oz_a, &c.oz_b,
                           &c.nl_a, &c.nl_b, &c.nl_c, &c.nl_d, &c.nl_ta, &c.nl_tb, &c.nl_tp, &c.en_rho, &c.en_a, &c.en_b, &c.en_veff,
                           &c.en_red, &c.en_ei, &c.en_fp, &c.en_idx, &c.en_in[0], &c.en_in[1], &c.en_in[2],
-                          &c.en_in[3], &c.en_in[4]};
+                          &c.en_in[3], &c.en_in[4], &c.oz_c, &c.oz_rmax};
   for (auto* s : all) gbcp::release(*s);
-  for (cudaStream_t* st : {&c.copy, &c.copy_out})
+  for (cudaStream_t* st : {&c.copy, &c.copy_out, &c.side})
     if (*st) {
       cudaStreamSynchronize(*st);
       cudaStreamDestroy(*st);
     }
   for (cudaEvent_t e : c.pipe_ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : c.side_ev) cudaEventDestroy(e);
   if (c.d_info) cudaFree(c.d_info);
   gbcp::prof_fold(c);
   for (cudaEvent_t e : c.prof_pool) cudaEventDestroy(e);

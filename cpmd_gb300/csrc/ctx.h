@@ -132,6 +132,7 @@ struct Ctx {
   Scratch xr_part, xr_tk;  // density x-stage: partial tiles and ticket counters of the pair chunks
   Scratch rt_mats;         // rortho: the n x n matrices of the constraint iteration
   Scratch oz_a, oz_b;  // bf16 digit planes of the split-precision ortho GEMMs
+  Scratch oz_c, oz_rmax;  // C M: planes and row maxima of C, sliced on the side stream while S and the Cholesky run
   Scratch nl_a, nl_b, nl_c, nl_d;
   Scratch nl_ta, nl_tb, nl_tp;  // projector GEMM slices (A, B) and split-K partials
   int* d_info = nullptr;
@@ -149,6 +150,8 @@ struct Ctx {
   // host-staged pipelining (abi.cu): the Z stage of staging chunk q waits for batch_ready[q];
   // vpsi calls batch_done(q) once the decode of chunk q is queued
   cudaStream_t copy = nullptr, copy_out = nullptr;  // uploads, downloads (separate copy engines)
+  cudaStream_t side = nullptr;                      // ortho: C M row slicing beside S and the Cholesky
+  std::vector<cudaEvent_t> side_ev;
   std::vector<cudaEvent_t> pipe_ev;
   const cudaEvent_t* batch_ready = nullptr;
   const cudaEvent_t* batch_c2_ready = nullptr;  // vpsi: the decode of chunk q waits for its C2 columns
@@ -228,7 +231,15 @@ int xovlap_tc(Ctx& c, const double* X, int ldx, const double* Y, int ldy, int n,
 int ovlap_tc_ranges(Ctx& c, const double* Ar, int lda, int n, const int* kb, int R, const cudaEvent_t* ready,
                     double* S, unsigned long long* scond_bits, int* status);
 int rmul_tc_ranges(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout,
-                   int ldo, int zero_row1, int* status, const int* rb, int R, const cudaEvent_t* done);
+                   int ldo, int zero_row1, int* status, const int* rb, int R, const cudaEvent_t* done,
+                   const cudaEvent_t* sliced = nullptr);
+// The digit planes and row maxima C M needs from A (rows x n, n <= 256), range by
+// range on the side stream into oz_c / oz_rmax: range r starts once ready[r] (or, with
+// ready null, the work queued so far on the context stream) is done, and sliced[r]
+// (R events, from side_ev) is recorded when its planes are written.  rmul_tc_ranges
+// with these events skips its own slicing.  Returns 7 when n > 256.
+int slice_rows_side(Ctx& c, const double* A, int lda, int rows, int n, const int* rb, int R,
+                    const cudaEvent_t* ready, const cudaEvent_t** sliced);
 // Gram-Schmidt of host-memory c0 with the copies overlapped (tensor-core engine);
 // returns 7 when the engine or size does not allow it (the caller stages instead).
 int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host);

@@ -399,9 +399,29 @@ static int ortho_gs_steps(Ctx& c, cx<double>* c0, int ldc, int n, bool want_scon
   double* S = static_cast<double*>(c.smat.p);
   double* X = static_cast<double*>(c.smat2.p);
   GBCP_CUDA_TRY(c, cudaMemsetAsync(c.d_info, 0, 16, c.stream));
+  // tensor-core engine: the digit planes of C for C U^-1 depend on C only, so they
+  // are cut on the side stream while the Cholesky (a few SMs) runs -- queued after S,
+  // whose own HBM-bound passes it would otherwise slow; not inside a stream capture
+  // (the batch graph keeps the single-stream order)
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  GBCP_CUDA_TRY(c, cudaStreamIsCapturing(c.stream, &cap));
+  const cudaEvent_t* sliced = nullptr;
+  const int rows = 2 * c.ngw, lda = 2 * ldc;
+  int rb[2] = {0, rows};
+  double* Ar = reinterpret_cast<double*>(c0);
   int rc = ovlap_gamma_ex(c, c0, ldc, n, S, want_scond);
   if (rc) return rc;
-  if ((rc = chol_inverse(c, S, X, n))) return rc;
+  if (use_tc_gemm(c) && n <= 256 && cap == cudaStreamCaptureStatusNone) {
+    rc = slice_rows_side(c, Ar, lda, rows, n, rb, 1, nullptr, &sliced);
+    if (rc) return rc;
+  }
+  rc = chol_inverse(c, S, X, n);
+  if (!rc && sliced) rc = rmul_tc_ranges(c, Ar, lda, rows, n, X, 1, Ar, lda, c.geq0, c.d_info, rb, 1, nullptr, sliced);
+  if (rc || sliced) {
+    // the side stream still reads C: the context stream waits for it before returning
+    if (rc && sliced) cudaStreamWaitEvent(c.stream, sliced[0], 0);
+    return rc;
+  }
   return apply_right(c, c0, ldc, n, X, 1);
 }
 
@@ -455,11 +475,16 @@ int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host) {
   }
   GBCP_CUDA_TRY(c, cudaMemsetAsync(c.d_info, 0, 16, c.stream));
   double* Ar = reinterpret_cast<double*>(d);
-  int rc = ovlap_tc_ranges(c, Ar, 2 * ngw, n, kb, R, up, S, scond_host ? scond_bits_of(c) : nullptr, c.d_info);
+  // C U^-1's digit planes of range r are cut on the side stream once range r has
+  // landed, beside the overlap ranges and the Cholesky
+  const cudaEvent_t* sliced = nullptr;
+  int rc = n <= 256 ? slice_rows_side(c, Ar, 2 * ngw, 2 * ngw, n, kb, R, up, &sliced) : 0;
+  if (!rc) rc = ovlap_tc_ranges(c, Ar, 2 * ngw, n, kb, R, up, S, scond_host ? scond_bits_of(c) : nullptr, c.d_info);
   if (!rc) rc = chol_inverse(c, S, X, n);
-  if (!rc) rc = rmul_tc_ranges(c, Ar, 2 * ngw, 2 * ngw, n, X, 1, Ar, 2 * ngw, c.geq0, c.d_info, kb, R, done);
+  if (!rc) rc = rmul_tc_ranges(c, Ar, 2 * ngw, 2 * ngw, n, X, 1, Ar, 2 * ngw, c.geq0, c.d_info, kb, R, done, sliced);
   if (rc) {
     cudaStreamSynchronize(c.copy);
+    if (c.side) cudaStreamSynchronize(c.side);
     return rc;
   }
   for (int r = 0; r < R; ++r) {

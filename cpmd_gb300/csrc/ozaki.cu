@@ -983,15 +983,58 @@ int ovlap_tc_ranges(Ctx& c, const double* Ar, int lda, int n, const int* kb, int
 // C M by row ranges [rb[r], rb[r+1]) (boundaries multiples of OZ_M): done[r] (may
 // be null) is recorded once range r's rows of Cout are written, so that a host
 // download of range r overlaps the later ranges.  Otherwise as rmul_tc.
+int slice_rows_side(Ctx& c, const double* A, int lda, int rows, int n, const int* rb, int R,
+                    const cudaEvent_t* ready, const cudaEvent_t** sliced) {
+  if (n > 256 || n <= 0 || R <= 0) return 7;
+  const size_t ks = ((size_t)n + 7) & ~size_t(7);
+  if (!ensure(c, c.oz_c, sizeof(uint16_t) * OZ_SL * (size_t)rows * ks) ||
+      !ensure(c, c.oz_rmax, sizeof(unsigned long long) * (size_t)rows))
+    return 6;
+  if (!c.side && cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking) != cudaSuccess) {
+    c.err = "side stream";
+    return 5;
+  }
+  while (c.side_ev.size() < (size_t)(R + 1)) {
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      c.err = "side stream events";
+      return 5;
+    }
+    c.side_ev.push_back(e);
+  }
+  if (!ready) {  // A as queued so far on the context stream
+    GBCP_CUDA_TRY(c, cudaEventRecord(c.side_ev[R], c.stream));
+    GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.side, c.side_ev[R], 0));
+  }
+  unsigned long long* rmax = static_cast<unsigned long long*>(c.oz_rmax.p);
+  for (int r = 0; r < R; ++r) {
+    const int r0 = rb[r], r1 = rb[r + 1];
+    if (ready && ready[r]) GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.side, ready[r], 0));
+    if (r1 > r0) {
+      ProfScope ps_(c, "k_oz_slice", c.side, 0);
+      k_oz_slice_rows_max<<<(r1 - r0 + 31) / 32, dim3(32, (n + 15) / 16), 0, c.side>>>(
+          A, lda, rows, n, rmax, ks, static_cast<uint4*>(c.oz_c.p), r0, r1);
+      GBCP_LAUNCH_CHECK(c);
+    }
+    GBCP_CUDA_TRY(c, cudaEventRecord(c.side_ev[r], c.side));
+  }
+  *sliced = c.side_ev.data();
+  return 0;
+}
+
 int rmul_tc_ranges(Ctx& c, const double* A, int lda, int rows, int n, const double* M, int upper, double* Cout,
-                   int ldo, int zero_row1, int* status, const int* rb, int R, const cudaEvent_t* done) {
+                   int ldo, int zero_row1, int* status, const int* rb, int R, const cudaEvent_t* done,
+                   const cudaEvent_t* sliced) {
   const size_t ks = ((size_t)n + 7) & ~size_t(7);
   const size_t bytes = ((size_t)rows + n) * 8;
-  if (!ensure(c, c.nl_a, bytes) || !ensure(c, c.oz_a, sizeof(uint16_t) * OZ_SL * (size_t)rows * ks) ||
+  if (!ensure(c, c.nl_a, bytes) || (!sliced && !ensure(c, c.oz_a, sizeof(uint16_t) * OZ_SL * (size_t)rows * ks)) ||
       !ensure(c, c.oz_b, sizeof(uint16_t) * OZ_SL * (size_t)n * ks))
     return 6;
-  unsigned long long* rmax = static_cast<unsigned long long*>(c.nl_a.p);
-  unsigned long long* mcmax = rmax + rows;
+  if (sliced && (n > 256 || !c.oz_c.p || !c.oz_rmax.p)) return 7;
+  unsigned long long* rmax =
+      sliced ? static_cast<unsigned long long*>(c.oz_rmax.p) : static_cast<unsigned long long*>(c.nl_a.p);
+  unsigned long long* mcmax = static_cast<unsigned long long*>(c.nl_a.p) + rows;
+  void* planes = sliced ? c.oz_c.p : c.oz_a.p;
   {
     ProfScope ps_(c, "k_mat_col_max");
     GBCP_LAUNCH_PDL(c, k_mat_col_max, dim3((n + 31) / 32), dim3(32, 8), 0, M, n, mcmax);
@@ -1007,7 +1050,7 @@ int rmul_tc_ranges(Ctx& c, const double* A, int lda, int rows, int n, const doub
         static_cast<uint4*>(c.oz_b.p));
   }
   CUtensorMap ma, mb;
-  if (!tmap_bf16_2d(&ma, c.oz_a.p, n, (long long)OZ_SL * rows, (int)ks, OZ_KS, OZ_M, 64) ||
+  if (!tmap_bf16_2d(&ma, planes, n, (long long)OZ_SL * rows, (int)ks, OZ_KS, OZ_M, 64) ||
       !tmap_bf16_2d(&mb, c.oz_b.p, n, (long long)OZ_SL * n, (int)ks, OZ_KS, OZ_N, 64)) {
     c.err = "C.M: tensor map encoding failed";
     return 5;
@@ -1018,7 +1061,9 @@ int rmul_tc_ranges(Ctx& c, const double* A, int lda, int rows, int n, const doub
   for (int r = 0; r < R; ++r) {
     const int r0 = rb[r], r1 = rb[r + 1];
     if (r1 > r0) {
-      if (n <= 256) {
+      if (sliced) {  // planes of this range written on the side stream
+        GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, sliced[r], 0));
+      } else if (n <= 256) {
         ProfScope ps_(c, "k_oz_slice");
         GBCP_LAUNCH_PDL(c, k_oz_slice_rows_max, dim3((r1 - r0 + 31) / 32), dim3(32, (n + 15) / 16), 0, A, lda, rows,
             n, rmax, ks, static_cast<uint4*>(c.oz_a.p), r0, r1);
