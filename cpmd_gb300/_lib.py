@@ -94,7 +94,8 @@ class Restart(C.Structure):
                 ("ngwks", C.c_int32), ("ngwls", C.c_int32), ("nhgs", C.c_int32), ("nhgls", C.c_int32),
                 ("c0", C.c_void_p), ("ldc", C.c_int32), ("ngw", C.c_int32), ("nstate_cap", C.c_int32),
                 ("icompr", C.c_int32), ("scale", C.c_double),
-                ("nstate_read", C.c_int32), ("nstate_file", C.c_int32), ("sections", C.c_int32)]
+                ("nstate_read", C.c_int32), ("nstate_file", C.c_int32), ("sections", C.c_int32),
+                ("f", C.c_void_p), ("eigv", C.c_void_p), ("amu", C.c_double)]
 
 
 _lib = None

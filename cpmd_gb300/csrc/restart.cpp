@@ -8,7 +8,8 @@
 // position of the section end instead).  Section 1 is one 80-character record
 // (" STUTTGART VERSION 3.0").  Sections 2..99 each start with a record
 // (irecord int32, fpos int64) and are followed by irecord records (0: section
-// empty); section 9, the states, uses a negative count -(2 n + 3) for the
+// empty; the count is what lets a reader skip a section it does not parse);
+// section 9, the states, uses a negative count -(2 n + 3) for the
 // w_wfnio format: (iwfntype), (n, ngwks, icompr, scale), (tlsd, nsup, nsdown),
 // then per state (nx) and the 2 nx 32-bit words of the compressed coefficients
 // in the global G order.
@@ -169,8 +170,25 @@ int write_restart(const char* path, const gbcp_restart* r) {
   } else {
     w.section(0);
   }
-  // sections 10 .. 99: empty
-  for (int sec = 10; sec <= 99; ++sec) w.section(0);
+  // sections 10 .. 22: empty
+  for (int sec = 10; sec <= 22; ++sec) w.section(0);
+  // section 23: occupation numbers (one k point)
+  if (r->f && r->nstate > 0) {
+    w.section(1);
+    w.rec({{r->f, 8 * (size_t)r->nstate}});
+  } else {
+    w.section(0);
+  }
+  // section 24: Fermi energy, eigenvalues
+  if (r->eigv && r->nstate > 0) {
+    w.section(2);
+    w.rec({{&r->amu, 8}});
+    w.rec({{r->eigv, 8 * (size_t)r->nstate}});
+  } else {
+    w.section(0);
+  }
+  // sections 25 .. 99: empty
+  for (int sec = 25; sec <= 99; ++sec) w.section(0);
   return w.close() ? GBCP_OK : GBCP_ERR_IO;
 }
 
@@ -391,7 +409,36 @@ int read_restart(const char* path, gbcp_restart* r) {
       for (int64_t i = 2 * (int64_t)m; i < 2 * (int64_t)r->ngw; ++i) c[i] = 0.0;
       r->nstate_read = s + 1;
     }
+    // the states not stored: two records each (nx, words)
+    if (rd.stream) {
+      if (!rd.skip(irecord, fpos, buf)) return GBCP_ERR_IO;
+    } else {
+      for (int s = nread; s < n0; ++s)
+        if (!rd.next(buf, 0) || !rd.next(buf, 0)) return GBCP_ERR_IO;
+    }
     r->sections |= 1 << 8;
+  }
+  // sections 10 .. 22: skipped by their record counts; the file may end here
+  for (int sec = 10; sec <= 24; ++sec) {
+    if (std::feof(rd.f) || std::fgetc(rd.f) == EOF) break;
+    std::fseek(rd.f, -1, SEEK_CUR);
+    if (!rd.section(irecord, fpos, buf)) return GBCP_ERR_IO;
+    if (sec == 23 && irecord >= 1 && r->nstate > 0) {  // occupations of the first k point
+      if (!rd.next(buf, 8 * (size_t)r->nstate) || buf.size() < 8 * (size_t)r->nstate) return GBCP_ERR_IO;
+      if (r->f) std::memcpy(r->f, buf.data(), 8 * (size_t)r->nstate);
+      r->sections |= 1 << 22;
+      if (!rd.stream && irecord > 1 && !rd.skip(irecord - 1, 0, buf)) return GBCP_ERR_IO;
+      if (rd.stream && irecord > 1 && !rd.skip(irecord, fpos, buf)) return GBCP_ERR_IO;
+    } else if (sec == 24 && irecord >= 2 && r->nstate > 0) {  // amu, then eigenvalues of the first k point
+      if (!rd.read(&r->amu, 8, buf)) return GBCP_ERR_IO;
+      if (!rd.next(buf, 8 * (size_t)r->nstate) || buf.size() < 8 * (size_t)r->nstate) return GBCP_ERR_IO;
+      if (r->eigv) std::memcpy(r->eigv, buf.data(), 8 * (size_t)r->nstate);
+      r->sections |= 1 << 23;
+      if (!rd.stream && irecord > 2 && !rd.skip(irecord - 2, 0, buf)) return GBCP_ERR_IO;
+      if (rd.stream && irecord > 2 && !rd.skip(irecord, fpos, buf)) return GBCP_ERR_IO;
+    } else if (irecord != 0 && !rd.skip(irecord, fpos, buf)) {
+      return GBCP_ERR_IO;
+    }
   }
   return GBCP_OK;
 }

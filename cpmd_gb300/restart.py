@@ -5,8 +5,9 @@
 235-1300) and ``read_restart`` its zhrwf/rv30 (rv30_utils.mod.F90:104-2242) for
 the records the wavefunction path needs: sections 1-8 (header, cell, species,
 coordinates, velocities, initial coordinates, cutoff/electrons/mesh, state and
-plane-wave counts) and section 9, the states C0 in the w_wfnio layout
-(wfnio_utils.mod.F90:52-233; compress.F90 for icompr 1 = FP64 and 2 = 32-bit).
+plane-wave counts), section 9, the states C0 in the w_wfnio layout
+(wfnio_utils.mod.F90:52-233; compress.F90 for icompr 1 = FP64 and 2 = 32-bit),
+and sections 23-24, the occupation numbers, Fermi energy and eigenvalues.
 The coefficients are stored in the reference's global G order, which is the
 order ``cell.make_basis`` generates, so a state column maps row for row onto a
 context's basis.
@@ -24,7 +25,7 @@ from . import _lib as L
 
 @dataclass
 class RestartData:
-    """The contents of sections 1-9 of a RESTART file."""
+    """The contents of sections 1-9, 23 and 24 of a RESTART file."""
     c0: np.ndarray | None                 # (ngw, nstate_read) complex128, column-major
     na: np.ndarray                        # atoms per species
     tau0: np.ndarray | None               # (nat, 3), species-major
@@ -47,6 +48,9 @@ class RestartData:
     scale: float = 0.0
     nstate_file: int = 0
     sections: int = 0
+    f: np.ndarray | None = None           # (nstate) occupation numbers (section 23)
+    eigv: np.ndarray | None = None        # (nstate) eigenvalues (section 24)
+    amu: float = 0.0                      # Fermi energy (section 24)
 
     def has_section(self, k: int) -> bool:
         return bool(self.sections >> (k - 1) & 1)
@@ -63,11 +67,13 @@ def _check(fn, rc):
 
 def write_restart(path: str | os.PathLike, c0, *, na, tau0, ecut: float, nel: int, nr, alat: float,
                   taum=None, taui=None, ibrav: int = 1, indpg: int = 0, celldm=None, cdual: float = 4.0,
-                  dual: bool = False, ngwls: int = 0, nhgs: int = 0, nhgls: int = 0, icompr: int = 1) -> None:
+                  dual: bool = False, ngwls: int = 0, nhgs: int = 0, nhgls: int = 0, icompr: int = 1,
+                  f=None, eigv=None, amu: float = 0.0) -> None:
     """Write a RESTART file: c0 (ngw, nstate) complex, na per species, tau0 (nat, 3)
     species-major, ecut in Ry, nel electrons, nr the mesh, alat the cubic cell edge
     (celldm(1), unless celldm is given).  icompr 1 stores FP64 as is, 2 as 32-bit
-    fixed point on the largest coefficient's modulus."""
+    fixed point on the largest coefficient's modulus.  f (occupations) and eigv
+    (eigenvalues, with the Fermi energy amu) fill sections 23 and 24 when given."""
     lib = L.load()
     c = np.asfortranarray(np.asarray(c0, dtype=np.complex128))
     ngw, nstate = c.shape
@@ -92,11 +98,17 @@ def write_restart(path: str | os.PathLike, c0, *, na, tau0, ecut: float, nel: in
     r.nstate, r.nkpts = nstate, 0
     r.ngwks, r.ngwls, r.nhgs, r.nhgls = ngw, int(ngwls), int(nhgs), int(nhgls)
     r.c0, r.ldc, r.ngw, r.icompr = _ptr(c), ngw, ngw, int(icompr)
+    f_ = None if f is None else np.ascontiguousarray(np.asarray(f, dtype=np.float64))
+    e_ = None if eigv is None else np.ascontiguousarray(np.asarray(eigv, dtype=np.float64))
+    for a in (f_, e_):
+        if a is not None and a.size != nstate:
+            raise ValueError("f and eigv need one entry per state")
+    r.f, r.eigv, r.amu = _ptr(f_), _ptr(e_), float(amu)
     _check("gbcp_restart_write", lib.gbcp_restart_write(os.fsencode(os.fspath(path)), C.byref(r)))
 
 
 def read_restart(path: str | os.PathLike, ngw: int | None = None, nstate: int | None = None) -> RestartData:
-    """Read sections 1-9.  ngw: rows of the returned states (default: the file's
+    """Read sections 1-9, 23 and 24.  ngw: rows of the returned states (default: the file's
     plane waves; more rows are zero, fewer truncate); nstate: states to read
     (default: all of the file's)."""
     lib = L.load()
@@ -110,8 +122,11 @@ def read_restart(path: str | os.PathLike, ngw: int | None = None, nstate: int | 
     ng = int(r.ngwks if ngw is None else ngw)
     ns = int(r.nstate_file if nstate is None else min(nstate, r.nstate_file))
     c0 = np.zeros((max(ng, 1), max(ns, 1)), dtype=np.complex128, order="F")
+    occ = np.zeros(max(r.nstate, 1))
+    eig = np.zeros(max(r.nstate, 1))
     r2 = L.Restart()
     r2.na, r2.tau0, r2.taum, r2.taui = _ptr(na), _ptr(tau0), _ptr(taum), _ptr(taui)
+    r2.f, r2.eigv = _ptr(occ), _ptr(eig)
     if ng > 0 and ns > 0:
         r2.c0, r2.ldc, r2.ngw, r2.nstate_cap = _ptr(c0), c0.shape[0], ng, ns
     _check("gbcp_restart_read", lib.gbcp_restart_read(p, C.byref(r2)))
@@ -125,4 +140,6 @@ def read_restart(path: str | os.PathLike, ngw: int | None = None, nstate: int | 
         ibrav=r2.ibrav, indpg=r2.indpg, celldm=np.array(list(r2.celldm)), ecut=r2.ecut, cdual=r2.cdual,
         dual=bool(r2.dual), nel=r2.nel, nr=(r2.nr1s, r2.nr2s, r2.nr3s), nstate=r2.nstate, ngwks=r2.ngwks,
         ngwls=r2.ngwls, nhgs=r2.nhgs, nhgls=r2.nhgls, icompr=r2.icompr, scale=r2.scale,
-        nstate_file=r2.nstate_file, sections=sec)
+        nstate_file=r2.nstate_file, sections=sec,
+        f=occ[:r2.nstate].copy() if sec >> 22 & 1 else None,
+        eigv=eig[:r2.nstate].copy() if sec >> 23 & 1 else None, amu=r2.amu)

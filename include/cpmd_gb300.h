@@ -277,9 +277,11 @@ int gbcp_batch_last_error(gbcp_batch* batch, char* buf, int len);
  * electrons / mesh, 8 states and plane-wave counts, 9 the states C0 in the
  * w_wfnio layout (wfnio_utils.mod.F90:52-233: type 1, then per state the
  * coefficients in the global G order, compress.F90: icompr 1 = FP64 as is,
- * 2 = 32-bit fixed point on the scale max|c|), 10..99 empty.  Read: sections
- * 1..9 of a sequential or STREAM file (icompr 1, 2, 4 or 8; the C0 format with a
- * negative section-9 record count); the rest of the file is not read.
+ * 2 = 32-bit fixed point on the scale max|c|), 23 occupation numbers and 24 the
+ * Fermi energy and eigenvalues when given, the others empty.  Read: sections
+ * 1..9, 23 and 24 of a sequential or STREAM file (icompr 1, 2, 4 or 8; the C0
+ * format with a negative section-9 record count), skipping 10..22 by their
+ * record counts; the file may end after section 9.
  * The coefficient order is the reference's global G order, which is the order
  * of the basis (inyh/hg) a context is created with. */
 typedef struct gbcp_restart {
@@ -304,11 +306,14 @@ typedef struct gbcp_restart {
   double scale;           /* read: the file's compression scale */
   int32_t nstate_read;    /* read: states stored into c0 */
   int32_t nstate_file;    /* read: states in the file's section 9 */
-  int32_t sections;       /* read: bit (k-1) set when section k (1..9) held data */
+  int32_t sections;       /* read: bit (k-1) set when section k (1..24) held data */
+  double* f;              /* (nstate) section 23 occupation numbers (crge%f); write: NULL = empty */
+  double* eigv;           /* (nstate) section 24 eigenvalues; write: NULL = empty */
+  double amu;             /* section 24 Fermi energy (ener_com%amu) */
 } gbcp_restart;
 /* Write `path` (overwritten). */
 int gbcp_restart_write(const char* path, const gbcp_restart* r);
-/* Read `path`: every scalar field of sections 2, 3, 7, 8 and 9 is filled; array
+/* Read `path`: every scalar field of sections 2, 3, 7, 8, 9 and 24 is filled; array
  * fields that are NULL are skipped (call once with NULL arrays to learn nsp,
  * nat, nstate, ngwks, then allocate).  Inputs: the array pointers, ldc, ngw and
  * nstate_cap; min(nstate_cap, states in the file) states are stored. */

@@ -19,6 +19,8 @@ so the layout is restated from its source only:
 * compress.F90:1-130, 336-430 ......... icompr 1: FP64 as is; icompr 2, 4, 8:
   nb = 64/icompr bits, NINT(x fx) + 2^(nb-1), fx = (2^(nb-1)-1)/scale, packed
   high part first; the reader decodes (nx-1) icompr values.
+* wv30_utils.mod.F90:856-895 ......... section 23: nkpts records of the
+  occupations; section 24: amu, then nkpts records of eigenvalues.
 * wfnio_utils.mod.F90:130-135 ........ scale = |c| of the element with the
   largest |Re| + |Im| (izamax).
 * rv30_utils.mod.F90:290-640 ......... the reader: sections taken in order,
@@ -91,7 +93,9 @@ def pack_state(a: np.ndarray, icompr: int, scale: float) -> tuple[int, np.ndarra
 
 
 def write(path, c0, *, na, tau0, ecut, nel, nr, celldm, taum=None, taui=None, ibrav=1, indpg=0, cdual=4.0,
-          dual=False, ngwls=0, nhgs=0, nhgls=0, icompr=1, stream=False):
+          dual=False, ngwls=0, nhgs=0, nhgls=0, icompr=1, stream=False, f=None, eigv=None, amu=0.0,
+          fill=None):
+    """fill: {section: [record bytes, ...]} for sections 10-22 (a reader must skip them)."""
     c = np.asfortranarray(np.asarray(c0, dtype=np.complex128))
     ngw, nstate = c.shape
     na = np.asarray(na, dtype=np.int32)
@@ -122,7 +126,15 @@ def write(path, c0, *, na, tau0, ecut, nel, nr, celldm, taum=None, taui=None, ib
         w.rec(struct.pack("<iq", -(2 * nstate + 3), -1))
         for b in body:
             w.rec(b)
-    for _ in range(10, 100):
+    for sec in range(10, 23):
+        body = (fill or {}).get(sec, [])
+        w.section(len(body), body)
+    w.section(1, [np.asarray(f, "<f8").tobytes()]) if f is not None else w.section(0)
+    if eigv is not None:
+        w.section(2, [struct.pack("<d", amu), np.asarray(eigv, "<f8").tobytes()])
+    else:
+        w.section(0)
+    for _ in range(25, 100):
         w.section(0)
     with open(path, "wb") as f:
         f.write(w.bytes())
@@ -233,4 +245,18 @@ def read(path) -> dict:
             a[:len(v)] = v
             c[:, s] = a[0::2] + 1j * a[1::2]
         out.update(iwfntype=iwfntype, icompr=icompr, scale=scale, c0=c)
+    if r.p >= len(r.d):
+        return out
+    for _ in range(10, 23):
+        irec, fpos = r.section()
+        r.skip(irec, fpos)
+    n = out.get("nstate", 0)
+    irec, fpos = r.section()
+    if irec >= 1:
+        out["f"] = np.frombuffer(r.rec(8 * n)[:8 * n], "<f8").copy()
+        r.skip(irec - 1, fpos) if not r.stream else None
+    irec, fpos = r.section()
+    if irec >= 2:
+        (out["amu"],) = struct.unpack("<d", r.rec(8)[:8])
+        out["eigv"] = np.frombuffer(r.rec(8 * n)[:8 * n], "<f8").copy()
     return out

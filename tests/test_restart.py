@@ -1,8 +1,9 @@
 """RESTART wavefunction files (gbcp_restart_write / gbcp_restart_read, host code
 of the C ABI) against the layout restated in oracle/restart_oracle.py: files
 written by the library are read by the oracle and the reverse, sequential and
-STREAM files, every compression type, plane-wave and state-count changes, and
-malformed files.  No GPU is involved."""
+STREAM files, every compression type, plane-wave and state-count changes, the
+occupation and eigenvalue sections behind skipped ones, and malformed files.
+No GPU is involved."""
 import struct
 
 import numpy as np
@@ -191,3 +192,48 @@ def test_write_rejects_bad_arguments(lib, tmp_path):
     assert e.value.code == 1
     with pytest.raises(ValueError):
         write_restart(tmp_path / "y", states(16, 2, 1), na=[9], tau0=tau0, ecut=1.0, nel=2, nr=16, alat=5.0)
+
+
+@pytest.mark.parametrize("stream", [False, True])
+def test_occupations_and_eigenvalues(lib, tmp_path, stream):
+    """Sections 23-24 after sections 10-22 that hold records the reader must skip,
+    with only part of section 9's states read."""
+    from cpmd_gb300.restart import read_restart, write_restart
+    na, tau0 = cell(9)
+    c = states(96, 7, 9)
+    occ = np.array([2.0, 2.0, 2.0, 1.5, 1.0, 0.5, 0.0])
+    eig = np.linspace(-0.8, 0.3, 7)
+    p = tmp_path / "RESTART.occ"
+    write_restart(p, c, na=na, tau0=tau0, ecut=20.0, nel=9, nr=32, alat=10.0, f=occ, eigv=eig, amu=0.125)
+    ref = RO.read(p)
+    assert np.array_equal(ref["f"], occ) and np.array_equal(ref["eigv"], eig) and ref["amu"] == 0.125
+    d = read_restart(p, nstate=3)
+    assert d.c0.shape == (96, 3) and np.array_equal(d.c0, c[:, :3])
+    assert np.array_equal(d.f, occ) and np.array_equal(d.eigv, eig) and d.amu == 0.125
+    assert d.has_section(23) and d.has_section(24)
+    # the reference's own sections in between: velocities (10), potential (18), density (22)
+    q = tmp_path / "RESTART.fill"
+    fill = {10: [b"v" * 20, b"w" * 40, b"x" * 8], 18: [b"p" * 160], 22: [b"r" * 72, b"s" * 8]}
+    RO.write(q, c, na=na, tau0=tau0, ecut=20.0, nel=9, nr=32, celldm=[10, 1, 1, 0, 0, 0], f=occ, eigv=eig,
+             amu=-0.25, fill=fill, stream=stream, icompr=2)
+    d = read_restart(q, nstate=2)
+    assert d.c0.shape == (96, 2)
+    assert np.array_equal(d.c0, RO.read(q)["c0"][:, :2])
+    assert np.array_equal(d.f, occ) and np.array_equal(d.eigv, eig) and d.amu == -0.25
+
+
+def test_file_may_end_after_the_states(lib, tmp_path):
+    from cpmd_gb300.restart import read_restart
+    na, tau0 = cell()
+    c = states(64, 3, 11)
+    p = tmp_path / "RESTART.full"
+    RO.write(p, c, na=na, tau0=tau0, ecut=20.0, nel=6, nr=32, celldm=[10, 1, 1, 0, 0, 0])
+    raw = p.read_bytes()
+    # cut right after section 9: the first empty section header (record of 12 bytes) follows it
+    hdr10 = struct.pack("<i", 12) + struct.pack("<iq", 0, 0) + struct.pack("<i", 12)
+    cut = len(raw) - 90 * len(hdr10)  # sections 10..99, all empty
+    assert raw[cut:cut + len(hdr10)] == hdr10
+    q = tmp_path / "RESTART.cut"
+    q.write_bytes(raw[:cut])
+    d = read_restart(q)
+    assert np.array_equal(d.c0, c) and d.f is None and d.eigv is None
