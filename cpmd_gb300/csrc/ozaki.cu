@@ -370,7 +370,7 @@ struct OzParams {
   int full;           // mode 0: every tile of the nib x njb grid (two different operands)
   int njb;            // mode 0: column tiles
   int subs_per;       // mode 0: sub-chunks per K split (a multiple of OZ_SUBS)
-  int upper;          // mode 1: M upper triangular (column tile j needs k < j0 + 64)
+  int upper;          // mode 1: M upper triangular (column tile j needs k < j0 + OZ_N)
   const unsigned long long* eA;  // mode 1: exponent bits per row of A
   const unsigned long long* eB;  // mode 1: exponent bits per column
   unsigned long long* Hacc;      // mode 0: int64 accumulators (n x n)
@@ -431,7 +431,7 @@ __device__ __forceinline__ OzUnit oz_unit(const OzParams& p, int u) {
 
 __device__ __forceinline__ int oz_next_unit(const OzParams& p, int u) { return p.mode == 0 ? -1 : u + (int)gridDim.x; }
 
-// thread 0: the 16 TMA loads (8 A planes, 8 B planes) of one sub-chunk into buffer b
+// the TMA thread: the 16 loads (8 A planes, 8 B planes) of one sub-chunk into stage buf
 __device__ __forceinline__ void oz_load(const CUtensorMap* tmA, const CUtensorMap* tmB, const OzParams& p,
                                         const OzUnit& w, int s, uint8_t* buf, uint64_t* bar) {
   const int k = (p.sub_base + w.sub0 + s) * OZ_KS;
