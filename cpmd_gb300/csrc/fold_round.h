@@ -1,5 +1,6 @@
-// Rounding of the split GEMM's int64 level sums to FP64, shared by the device
-// code and a host test (the file compiles as plain C++ too).
+// The integer arithmetic of the split GEMM shared by the device code and host
+// tests (the file compiles as plain C++ too): splitting an FP64 value into
+// signed 7-bit digits, and rounding the int64 level sums back to FP64.
 //
 // A split GEMM output is v 2^(ee-63) with v = H 2^28 + Lo: H holds levels 0-3
 // and Lo levels 4-7 of the digit-pair sums (7 bits apart), ee = E_i + E_j the sum
@@ -35,6 +36,43 @@ GBCP_FOLD_FN double from_bits(unsigned long long b) {
   memcpy(&d, &b, sizeof d);
   return d;
 #endif
+}
+
+GBCP_FOLD_FN unsigned long long to_bits(double x) {
+#if defined(__CUDA_ARCH__)
+  return (unsigned long long)__double_as_longlong(x);
+#else
+  unsigned long long b;
+  memcpy(&b, &x, sizeof b);
+  return b;
+#endif
+}
+
+// exponent E with |x| < 2^E from the bit pattern of max |x| (-1021 for zero and subnormals)
+GBCP_FOLD_FN int exp_of_max(unsigned long long bits) {
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  return (ex == 0) ? -1021 : ex - 1022;
+}
+
+// Fixed-point magnitude trunc(|x| 2^(56-E)) (< 2^56) and the sign, integer ops
+// only; zero and subnormal values give 0.  x = 2^E sum_s d_s 2^(-7(s+1)) up to
+// 2^(E-56), with the digits d_s of digit().
+GBCP_FOLD_FN unsigned long long fixed56(double x, int E, bool& neg) {
+  const unsigned long long b = to_bits(x);
+  neg = (b >> 63) != 0;
+  const int ex = (int)((b >> 52) & 0x7FF);
+  if (ex == 0) return 0ull;
+  const unsigned long long M = (b & ((1ull << 52) - 1)) | (1ull << 52);
+  int sh = ex - 1019 - E;  // = (ex - 1023) + 4 - E
+  if (sh > 3) sh = 3;      // cannot happen when |x| < 2^E; keeps v < 2^56
+  if (sh >= 0) return M << sh;
+  return (sh <= -64) ? 0ull : (M >> (-sh));
+}
+
+// signed digit s (0 = most significant, s < 8) of a fixed56 magnitude: |d| <= 127
+GBCP_FOLD_FN int digit(unsigned long long f, bool neg, int s) {
+  const int d = (int)((f >> (7 * (7 - s))) & 127ull);
+  return neg ? -d : d;
 }
 
 // v 2^(ee-63) correctly rounded (nearest, ties to even), valid for |H| < 2^62.

@@ -79,24 +79,11 @@ static_assert(OZ_CW % 8 == 0, "fold warps read TMEM 8 columns at a time");
 // signed 7-bit digit -> bf16 bits (exact: |d| <= 127)
 __device__ __forceinline__ uint32_t digit_bf16(int d) { return __float_as_uint((float)d) >> 16; }
 
-// exponent E with |x| < 2^E from the bit pattern of max |x|
-__device__ __forceinline__ int exp_of_max(unsigned long long bits) {
-  const int ex = (int)((bits >> 52) & 0x7FF);
-  return (ex == 0) ? -1021 : ex - 1022;
-}
+// exponent E with |x| < 2^E from the bit pattern of max |x| (fold_round.h)
+__device__ __forceinline__ int exp_of_max(unsigned long long bits) { return fold::exp_of_max(bits); }
 
-// Fixed-point magnitude trunc(|x| 2^(56-E)) (< 2^56) and the sign, integer ops only.
-__device__ __forceinline__ unsigned long long fixed56(double x, int E, bool& neg) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  neg = (b >> 63) != 0;
-  const int ex = (int)((b >> 52) & 0x7FF);
-  if (ex == 0) return 0ull;  // zero or subnormal
-  const unsigned long long M = (b & ((1ull << 52) - 1)) | (1ull << 52);
-  int sh = ex - 1019 - E;  // = (ex - 1023) + 4 - E
-  if (sh > 3) sh = 3;      // cannot happen when |x| < 2^E; keeps v < 2^56
-  if (sh >= 0) return M << sh;
-  return (sh <= -64) ? 0ull : (M >> (-sh));
-}
+// Fixed-point magnitude trunc(|x| 2^(56-E)) (< 2^56) and the sign (fold_round.h)
+__device__ __forceinline__ unsigned long long fixed56(double x, int E, bool& neg) { return fold::fixed56(x, E, neg); }
 
 // Digits of 8 consecutive K elements of one operand row -> 8 planes, 16 bytes each.
 __device__ __forceinline__ void digits8(const double (&x)[8], int E, uint4 (&out)[OZ_SL]) {
@@ -107,9 +94,7 @@ __device__ __forceinline__ void digits8(const double (&x)[8], int E, uint4 (&out
     const unsigned long long f0 = fixed56(x[2 * q2], E, n0), f1 = fixed56(x[2 * q2 + 1], E, n1);
 #pragma unroll
     for (int s = 0; s < OZ_SL; ++s) {
-      const int sh = 7 * (OZ_SL - 1 - s);
-      const int d0 = (int)((f0 >> sh) & 127ull), d1 = (int)((f1 >> sh) & 127ull);
-      w[s][q2] = digit_bf16(n0 ? -d0 : d0) | (digit_bf16(n1 ? -d1 : d1) << 16);
+      w[s][q2] = digit_bf16(fold::digit(f0, n0, s)) | (digit_bf16(fold::digit(f1, n1, s)) << 16);
     }
   }
 #pragma unroll
