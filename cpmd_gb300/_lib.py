@@ -95,7 +95,8 @@ class Restart(C.Structure):
                 ("c0", C.c_void_p), ("ldc", C.c_int32), ("ngw", C.c_int32), ("nstate_cap", C.c_int32),
                 ("icompr", C.c_int32), ("scale", C.c_double),
                 ("nstate_read", C.c_int32), ("nstate_file", C.c_int32), ("sections", C.c_int32),
-                ("f", C.c_void_p), ("eigv", C.c_void_p), ("amu", C.c_double)]
+                ("f", C.c_void_p), ("eigv", C.c_void_p), ("amu", C.c_double),
+                ("cm", C.c_void_p), ("ncm_read", C.c_int32), ("pad_", C.c_int32)]
 
 
 _lib = None

@@ -111,6 +111,14 @@ double izamax_scale(const double* c0, int ldc, int ngw, int nstate) {
   return std::hypot(re, im);
 }
 
+// the largest |component| of the real view (idamax, wr30wfn_utils.mod.F90:636-637)
+double idamax_scale(const double* c, int ldc, int ngw, int nstate) {
+  double best = 0.0;
+  for (int s = 0; s < nstate; ++s)
+    for (int i = 0; i < 2 * ngw; ++i) best = std::max(best, std::fabs(c[2 * (size_t)s * ldc + i]));
+  return best;
+}
+
 int write_restart(const char* path, const gbcp_restart* r) {
   if (!path || !r || r->nsp < 0 || r->nat < 0 || r->nstate < 0) return GBCP_ERR_ARG;
   if ((r->nsp > 0 && !r->na) || (r->nat > 0 && !r->tau0)) return GBCP_ERR_ARG;
@@ -170,8 +178,23 @@ int write_restart(const char* path, const gbcp_restart* r) {
   } else {
     w.section(0);
   }
-  // sections 10 .. 22: empty
-  for (int sec = 10; sec <= 22; ++sec) w.section(0);
+  // section 10: wavefunction velocities (wr30wfn 'NIL')
+  if (r->cm && states) {
+    const int32_t icompr = r->icompr;
+    const double scale = idamax_scale(r->cm, r->ldc, r->ngw, r->nstate);
+    w.section(2 * r->nstate + 1);
+    w.rec({{&r->nstate, 4}, {&ngwks, 4}, {&icompr, 4}, {&scale, 8}});
+    std::vector<uint32_t> words;
+    for (int s = 0; s < r->nstate && w.ok; ++s) {
+      const int32_t nx = compress_state(r->cm + 2 * (size_t)s * r->ldc, 2 * (int64_t)ngwks, icompr, scale, words);
+      w.rec({{&nx, 4}});
+      w.rec({{words.data(), 8 * (size_t)nx}});
+    }
+  } else {
+    w.section(0);
+  }
+  // sections 11 .. 22: empty
+  for (int sec = 11; sec <= 22; ++sec) w.section(0);
   // section 23: occupation numbers (one k point)
   if (r->f && r->nstate > 0) {
     w.section(1);
@@ -266,6 +289,62 @@ int64_t decompress_state(const uint32_t* w, int32_t nx, int icompr, double scale
     a[i] = (double)u * fx;
   }
   return n;
+}
+
+// The per-state records (nx), (2 nx words) of n0 states: the first min(n0, cap)
+// decoded into dst (ngw rows of leading dimension ld; rows beyond the file's
+// ngwks0 zeroed, as rdwfn does), the rest skipped (STREAM: to the section end).
+int read_states(RecReader& rd, std::vector<uint8_t>& buf, int n0, int ngwks0, int icompr, double scale,
+                double* dst, int ld, int ngw, int cap, int64_t fpos, int32_t* nread) {
+  const int nr = dst ? (n0 < cap ? n0 : cap) : 0;
+  std::vector<double> ca(2 * (size_t)ngwks0 + 16);
+  *nread = 0;
+  for (int s = 0; s < nr; ++s) {
+    int32_t nx = 0;
+    if (!rd.read(&nx, 4, buf) || nx < 0) return GBCP_ERR_IO;
+    if (!rd.next(buf, 8 * (size_t)nx) || buf.size() < 8 * (size_t)nx) return GBCP_ERR_IO;
+    std::fill(ca.begin(), ca.end(), 0.0);
+    if (decompress_state(reinterpret_cast<const uint32_t*>(buf.data()), nx, icompr, scale, ca.data(),
+                         2 * (int64_t)ngwks0) < 0)
+      return GBCP_ERR_IO;
+    double* c = dst + 2 * (size_t)s * ld;
+    const int m = ngwks0 < ngw ? ngwks0 : ngw;
+    for (int64_t i = 0; i < 2 * (int64_t)m; ++i) {
+      if (!std::isfinite(ca[(size_t)i])) return GBCP_ERR_NONFINITE;  // rdwfn stops on non-finite values
+      c[i] = ca[(size_t)i];
+    }
+    for (int64_t i = 2 * (int64_t)m; i < 2 * (int64_t)ngw; ++i) c[i] = 0.0;
+    *nread = s + 1;
+  }
+  if (rd.stream) {
+    if (nr < n0 && !rd.skip(0, fpos, buf)) return GBCP_ERR_IO;
+  } else {
+    for (int s = nr; s < n0; ++s)
+      if (!rd.next(buf, 0) || !rd.next(buf, 0)) return GBCP_ERR_IO;
+  }
+  return GBCP_OK;
+}
+
+// w_wfnio type-1 records after a negative section count: (iwfntype),
+// (n, ngwks, icompr, scale), (tlsd, nsup, nsdown), then the states
+int read_wfnio(RecReader& rd, std::vector<uint8_t>& buf, double* dst, int ld, int ngw, int cap, int64_t fpos,
+               int32_t* n0_out, int32_t* icompr_out, double* scale_out, int32_t* nread) {
+  int32_t iwfntype = 0;
+  if (!rd.read(&iwfntype, 4, buf)) return GBCP_ERR_IO;
+  if (iwfntype != 1) return GBCP_ERR_UNSUPPORTED;  // 9: broken-symmetry pair of wavefunctions
+  if (!rd.next(buf, 20) || buf.size() < 20) return GBCP_ERR_IO;
+  int32_t n0, ngwks0, icompr;
+  double scale;
+  std::memcpy(&n0, buf.data(), 4);
+  std::memcpy(&ngwks0, buf.data() + 4, 4);
+  std::memcpy(&icompr, buf.data() + 8, 4);
+  std::memcpy(&scale, buf.data() + 12, 8);
+  if (n0 < 0 || ngwks0 < 0 || (icompr != 1 && icompr != 2 && icompr != 4 && icompr != 8)) return GBCP_ERR_IO;
+  if (!rd.next(buf, 12) || buf.size() < 12) return GBCP_ERR_IO;  // tlsd, nsup, nsdown
+  *n0_out = n0;
+  *icompr_out = icompr;
+  *scale_out = scale;
+  return read_states(rd, buf, n0, ngwks0, icompr, scale, dst, ld, ngw, cap, fpos, nread);
 }
 
 int read_restart(const char* path, gbcp_restart* r) {
@@ -377,53 +456,39 @@ int read_restart(const char* path, gbcp_restart* r) {
   if (!rd.section(irecord, fpos, buf)) return GBCP_ERR_IO;
   if (irecord > 0) return GBCP_ERR_UNSUPPORTED;  // the older wr30wfn layout
   if (irecord < 0) {
-    int32_t iwfntype = 0;
-    if (!rd.read(&iwfntype, 4, buf)) return GBCP_ERR_IO;
-    if (iwfntype != 1) return GBCP_ERR_UNSUPPORTED;  // 9: broken-symmetry pair of wavefunctions
-    if (!rd.next(buf, 20) || buf.size() < 20) return GBCP_ERR_IO;
-    int32_t n0, ngwks0, icompr;
-    std::memcpy(&n0, buf.data(), 4);
-    std::memcpy(&ngwks0, buf.data() + 4, 4);
-    std::memcpy(&icompr, buf.data() + 8, 4);
-    std::memcpy(&r->scale, buf.data() + 12, 8);
-    if (n0 < 0 || ngwks0 < 0 || (icompr != 1 && icompr != 2 && icompr != 4 && icompr != 8)) return GBCP_ERR_IO;
-    if (!rd.next(buf, 12) || buf.size() < 12) return GBCP_ERR_IO;  // tlsd, nsup, nsdown
-    r->icompr = icompr;
-    r->nstate_file = n0;
-    const int nread = r->c0 ? (n0 < r->nstate_cap ? n0 : r->nstate_cap) : 0;
-    std::vector<double> ca(2 * (size_t)ngwks0 + 16);
-    for (int s = 0; s < nread; ++s) {
-      int32_t nx = 0;
-      if (!rd.read(&nx, 4, buf) || nx < 0) return GBCP_ERR_IO;
-      if (!rd.next(buf, 8 * (size_t)nx) || buf.size() < 8 * (size_t)nx) return GBCP_ERR_IO;
-      std::fill(ca.begin(), ca.end(), 0.0);
-      if (decompress_state(reinterpret_cast<const uint32_t*>(buf.data()), nx, icompr, r->scale, ca.data(),
-                           2 * (int64_t)ngwks0) < 0)
-        return GBCP_ERR_IO;
-      double* c = r->c0 + 2 * (size_t)s * r->ldc;
-      const int m = ngwks0 < r->ngw ? ngwks0 : r->ngw;
-      for (int64_t i = 0; i < 2 * (int64_t)m; ++i) {
-        if (!std::isfinite(ca[(size_t)i])) return GBCP_ERR_NONFINITE;  // rdwfn stops on non-finite values
-        c[i] = ca[(size_t)i];
-      }
-      for (int64_t i = 2 * (int64_t)m; i < 2 * (int64_t)r->ngw; ++i) c[i] = 0.0;
-      r->nstate_read = s + 1;
-    }
-    // the states not stored: two records each (nx, words)
-    if (rd.stream) {
-      if (!rd.skip(irecord, fpos, buf)) return GBCP_ERR_IO;
-    } else {
-      for (int s = nread; s < n0; ++s)
-        if (!rd.next(buf, 0) || !rd.next(buf, 0)) return GBCP_ERR_IO;
-    }
+    const int rc = read_wfnio(rd, buf, r->c0, r->ldc, r->ngw, r->nstate_cap, fpos, &r->nstate_file, &r->icompr,
+                              &r->scale, &r->nstate_read);
+    if (rc) return rc;
     r->sections |= 1 << 8;
   }
-  // sections 10 .. 22: skipped by their record counts; the file may end here
+  // section 10 (velocities), 11 .. 22 skipped by their record counts, 23, 24; the file may end after 9
+  r->ncm_read = 0;
   for (int sec = 10; sec <= 24; ++sec) {
     if (std::feof(rd.f) || std::fgetc(rd.f) == EOF) break;
     std::fseek(rd.f, -1, SEEK_CUR);
     if (!rd.section(irecord, fpos, buf)) return GBCP_ERR_IO;
-    if (sec == 23 && irecord >= 1 && r->nstate > 0) {  // occupations of the first k point
+    if (sec == 10 && irecord > 0) {  // wr30wfn: (n, ngwks, icompr, scale), then the states
+      if (!rd.next(buf, 20) || buf.size() < 20) return GBCP_ERR_IO;
+      int32_t n0, ngwks0, icompr;
+      double scale;
+      std::memcpy(&n0, buf.data(), 4);
+      std::memcpy(&ngwks0, buf.data() + 4, 4);
+      std::memcpy(&icompr, buf.data() + 8, 4);
+      std::memcpy(&scale, buf.data() + 12, 8);
+      if (n0 < 0 || ngwks0 < 0 || irecord != 2 * n0 + 1 || (icompr != 1 && icompr != 2 && icompr != 4 && icompr != 8))
+        return GBCP_ERR_IO;
+      const int rc = read_states(rd, buf, n0, ngwks0, icompr, scale, r->cm, r->ldc, r->ngw, r->nstate_cap, fpos,
+                                 &r->ncm_read);
+      if (rc) return rc;
+      r->sections |= 1 << 9;
+    } else if (sec == 10 && irecord < 0) {  // the w_wfnio layout
+      int32_t n0, icompr;
+      double scale;
+      const int rc = read_wfnio(rd, buf, r->cm, r->ldc, r->ngw, r->nstate_cap, fpos, &n0, &icompr, &scale,
+                                &r->ncm_read);
+      if (rc) return rc;
+      r->sections |= 1 << 9;
+    } else if (sec == 23 && irecord >= 1 && r->nstate > 0) {  // occupations of the first k point
       if (!rd.next(buf, 8 * (size_t)r->nstate) || buf.size() < 8 * (size_t)r->nstate) return GBCP_ERR_IO;
       if (r->f) std::memcpy(r->f, buf.data(), 8 * (size_t)r->nstate);
       r->sections |= 1 << 22;

@@ -7,7 +7,8 @@ the records the wavefunction path needs: sections 1-8 (header, cell, species,
 coordinates, velocities, initial coordinates, cutoff/electrons/mesh, state and
 plane-wave counts), section 9, the states C0 in the w_wfnio layout
 (wfnio_utils.mod.F90:52-233; compress.F90 for icompr 1 = FP64 and 2 = 32-bit),
-and sections 23-24, the occupation numbers, Fermi energy and eigenvalues.
+section 10, the wavefunction velocities cm of CP dynamics (wr30wfn_utils.mod.F90:
+569-693), and sections 23-24, the occupation numbers, Fermi energy and eigenvalues.
 The coefficients are stored in the reference's global G order, which is the
 order ``cell.make_basis`` generates, so a state column maps row for row onto a
 context's basis.
@@ -25,7 +26,7 @@ from . import _lib as L
 
 @dataclass
 class RestartData:
-    """The contents of sections 1-9, 23 and 24 of a RESTART file."""
+    """The contents of sections 1-10, 23 and 24 of a RESTART file."""
     c0: np.ndarray | None                 # (ngw, nstate_read) complex128, column-major
     na: np.ndarray                        # atoms per species
     tau0: np.ndarray | None               # (nat, 3), species-major
@@ -51,6 +52,7 @@ class RestartData:
     f: np.ndarray | None = None           # (nstate) occupation numbers (section 23)
     eigv: np.ndarray | None = None        # (nstate) eigenvalues (section 24)
     amu: float = 0.0                      # Fermi energy (section 24)
+    cm: np.ndarray | None = None          # (ngw, n) wavefunction velocities (section 10)
 
     def has_section(self, k: int) -> bool:
         return bool(self.sections >> (k - 1) & 1)
@@ -68,12 +70,13 @@ def _check(fn, rc):
 def write_restart(path: str | os.PathLike, c0, *, na, tau0, ecut: float, nel: int, nr, alat: float,
                   taum=None, taui=None, ibrav: int = 1, indpg: int = 0, celldm=None, cdual: float = 4.0,
                   dual: bool = False, ngwls: int = 0, nhgs: int = 0, nhgls: int = 0, icompr: int = 1,
-                  f=None, eigv=None, amu: float = 0.0) -> None:
+                  f=None, eigv=None, amu: float = 0.0, cm=None) -> None:
     """Write a RESTART file: c0 (ngw, nstate) complex, na per species, tau0 (nat, 3)
     species-major, ecut in Ry, nel electrons, nr the mesh, alat the cubic cell edge
     (celldm(1), unless celldm is given).  icompr 1 stores FP64 as is, 2 as 32-bit
     fixed point on the largest coefficient's modulus.  f (occupations) and eigv
-    (eigenvalues, with the Fermi energy amu) fill sections 23 and 24 when given."""
+    (eigenvalues, with the Fermi energy amu) fill sections 23 and 24 when given,
+    cm (ngw, nstate) the velocities of section 10."""
     lib = L.load()
     c = np.asfortranarray(np.asarray(c0, dtype=np.complex128))
     ngw, nstate = c.shape
@@ -104,11 +107,15 @@ def write_restart(path: str | os.PathLike, c0, *, na, tau0, ecut: float, nel: in
         if a is not None and a.size != nstate:
             raise ValueError("f and eigv need one entry per state")
     r.f, r.eigv, r.amu = _ptr(f_), _ptr(e_), float(amu)
+    cm_ = None if cm is None else np.asfortranarray(np.asarray(cm, dtype=np.complex128))
+    if cm_ is not None and cm_.shape != c.shape:
+        raise ValueError("cm must have the shape of c0")
+    r.cm = _ptr(cm_)
     _check("gbcp_restart_write", lib.gbcp_restart_write(os.fsencode(os.fspath(path)), C.byref(r)))
 
 
 def read_restart(path: str | os.PathLike, ngw: int | None = None, nstate: int | None = None) -> RestartData:
-    """Read sections 1-9, 23 and 24.  ngw: rows of the returned states (default: the file's
+    """Read sections 1-10, 23 and 24.  ngw: rows of the returned states (default: the file's
     plane waves; more rows are zero, fewer truncate); nstate: states to read
     (default: all of the file's)."""
     lib = L.load()
@@ -127,8 +134,10 @@ def read_restart(path: str | os.PathLike, ngw: int | None = None, nstate: int | 
     r2 = L.Restart()
     r2.na, r2.tau0, r2.taum, r2.taui = _ptr(na), _ptr(tau0), _ptr(taum), _ptr(taui)
     r2.f, r2.eigv = _ptr(occ), _ptr(eig)
+    cmv = np.zeros_like(c0)
     if ng > 0 and ns > 0:
         r2.c0, r2.ldc, r2.ngw, r2.nstate_cap = _ptr(c0), c0.shape[0], ng, ns
+        r2.cm = _ptr(cmv)
     _check("gbcp_restart_read", lib.gbcp_restart_read(p, C.byref(r2)))
     sec = r2.sections
     nat = r2.nat
@@ -142,4 +151,5 @@ def read_restart(path: str | os.PathLike, ngw: int | None = None, nstate: int | 
         ngwls=r2.ngwls, nhgs=r2.nhgs, nhgls=r2.nhgls, icompr=r2.icompr, scale=r2.scale,
         nstate_file=r2.nstate_file, sections=sec,
         f=occ[:r2.nstate].copy() if sec >> 22 & 1 else None,
-        eigv=eig[:r2.nstate].copy() if sec >> 23 & 1 else None, amu=r2.amu)
+        eigv=eig[:r2.nstate].copy() if sec >> 23 & 1 else None, amu=r2.amu,
+        cm=cmv[:ng, :r2.ncm_read] if r2.ncm_read else None)

@@ -277,11 +277,13 @@ int gbcp_batch_last_error(gbcp_batch* batch, char* buf, int len);
  * electrons / mesh, 8 states and plane-wave counts, 9 the states C0 in the
  * w_wfnio layout (wfnio_utils.mod.F90:52-233: type 1, then per state the
  * coefficients in the global G order, compress.F90: icompr 1 = FP64 as is,
- * 2 = 32-bit fixed point on the scale max|c|), 23 occupation numbers and 24 the
- * Fermi energy and eigenvalues when given, the others empty.  Read: sections
- * 1..9, 23 and 24 of a sequential or STREAM file (icompr 1, 2, 4 or 8; the C0
- * format with a negative section-9 record count), skipping 10..22 by their
- * record counts; the file may end after section 9.
+ * 2 = 32-bit fixed point on the scale max|c|), 10 the velocities cm when given
+ * (wr30wfn_utils.mod.F90:569-693, 'NIL': scale max|component|), 23 occupation
+ * numbers and 24 the Fermi energy and eigenvalues when given, the others empty.
+ * Read: sections 1..10, 23 and 24 of a sequential or STREAM file (icompr 1, 2, 4
+ * or 8; the C0 format with a negative section-9 record count, either format of
+ * section 10), skipping 11..22 by their record counts; the file may end after
+ * section 9.
  * The coefficient order is the reference's global G order, which is the order
  * of the basis (inyh/hg) a context is created with. */
 typedef struct gbcp_restart {
@@ -310,10 +312,14 @@ typedef struct gbcp_restart {
   double* f;              /* (nstate) section 23 occupation numbers (crge%f); write: NULL = empty */
   double* eigv;           /* (nstate) section 24 eigenvalues; write: NULL = empty */
   double amu;             /* section 24 Fermi energy (ener_com%amu) */
+  double* cm;             /* (ldc, nstate) section 10 wavefunction velocities, laid out like c0;
+                             write: NULL = empty section; read: NULL = skipped */
+  int32_t ncm_read;       /* read: velocity states stored into cm */
+  int32_t pad_;
 } gbcp_restart;
 /* Write `path` (overwritten). */
 int gbcp_restart_write(const char* path, const gbcp_restart* r);
-/* Read `path`: every scalar field of sections 2, 3, 7, 8, 9 and 24 is filled; array
+/* Read `path`: every scalar field of sections 2, 3, 7, 8, 9, 10 and 24 is filled; array
  * fields that are NULL are skipped (call once with NULL arrays to learn nsp,
  * nat, nstate, ngwks, then allocate).  Inputs: the array pointers, ldc, ngw and
  * nstate_cap; min(nstate_cap, states in the file) states are stored. */

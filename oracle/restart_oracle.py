@@ -19,6 +19,8 @@ so the layout is restated from its source only:
 * compress.F90:1-130, 336-430 ......... icompr 1: FP64 as is; icompr 2, 4, 8:
   nb = 64/icompr bits, NINT(x fx) + 2^(nb-1), fx = (2^(nb-1)-1)/scale, packed
   high part first; the reader decodes (nx-1) icompr values.
+* wr30wfn_utils.mod.F90:569-693 ...... section 10 ('NIL'): irecord = 2n+1,
+  (n, ngwks, icompr, scale = max |component|), then the per-state records.
 * wv30_utils.mod.F90:856-895 ......... section 23: nkpts records of the
   occupations; section 24: amu, then nkpts records of eigenvalues.
 * wfnio_utils.mod.F90:130-135 ........ scale = |c| of the element with the
@@ -94,7 +96,7 @@ def pack_state(a: np.ndarray, icompr: int, scale: float) -> tuple[int, np.ndarra
 
 def write(path, c0, *, na, tau0, ecut, nel, nr, celldm, taum=None, taui=None, ibrav=1, indpg=0, cdual=4.0,
           dual=False, ngwls=0, nhgs=0, nhgls=0, icompr=1, stream=False, f=None, eigv=None, amu=0.0,
-          fill=None):
+          fill=None, cm=None):
     """fill: {section: [record bytes, ...]} for sections 10-22 (a reader must skip them)."""
     c = np.asfortranarray(np.asarray(c0, dtype=np.complex128))
     ngw, nstate = c.shape
@@ -126,7 +128,20 @@ def write(path, c0, *, na, tau0, ecut, nel, nr, celldm, taum=None, taui=None, ib
         w.rec(struct.pack("<iq", -(2 * nstate + 3), -1))
         for b in body:
             w.rec(b)
-    for sec in range(10, 23):
+    if cm is not None:
+        cmf = np.asfortranarray(np.asarray(cm, dtype=np.complex128))
+        sc = float(np.abs(np.concatenate([cmf.real.ravel(), cmf.imag.ravel()])).max())
+        body = [struct.pack("<iiid", nstate, ngw, icompr, sc)]
+        for s_ in range(nstate):
+            real = np.empty(2 * ngw)
+            real[0::2], real[1::2] = cmf[:, s_].real, cmf[:, s_].imag
+            nx, words = pack_state(real, icompr, sc)
+            body += [struct.pack("<i", nx), words.tobytes()]
+        w.section(2 * nstate + 1, body)
+    else:
+        body = (fill or {}).get(10, [])
+        w.section(len(body), body)
+    for sec in range(11, 23):
         body = (fill or {}).get(sec, [])
         w.section(len(body), body)
     w.section(1, [np.asarray(f, "<f8").tobytes()]) if f is not None else w.section(0)
@@ -247,7 +262,21 @@ def read(path) -> dict:
         out.update(iwfntype=iwfntype, icompr=icompr, scale=scale, c0=c)
     if r.p >= len(r.d):
         return out
-    for _ in range(10, 23):
+    irec, fpos = r.section()
+    if irec > 0:
+        n0, ngwks0, icompr, scale = struct.unpack("<iiid", r.rec(20)[:20])
+        cmv = np.zeros((ngwks0, n0), dtype=np.complex128, order="F")
+        for s in range(n0):
+            (nx,) = struct.unpack("<i", r.rec(4)[:4])
+            words = np.frombuffer(r.rec(8 * nx)[:8 * nx], "<u4")
+            a = np.zeros(2 * ngwks0)
+            v = unpack_state(words, nx, icompr, scale)
+            a[:len(v)] = v
+            cmv[:, s] = a[0::2] + 1j * a[1::2]
+        out.update(cm=cmv, cm_scale=scale)
+    else:
+        r.skip(irec, fpos)
+    for _ in range(11, 23):
         irec, fpos = r.section()
         r.skip(irec, fpos)
     n = out.get("nstate", 0)

@@ -2,7 +2,8 @@
 of the C ABI) against the layout restated in oracle/restart_oracle.py: files
 written by the library are read by the oracle and the reverse, sequential and
 STREAM files, every compression type, plane-wave and state-count changes, the
-occupation and eigenvalue sections behind skipped ones, and malformed files.
+wavefunction velocities, the occupation and eigenvalue sections behind skipped
+ones, and malformed files.
 No GPU is involved."""
 import struct
 
@@ -211,9 +212,9 @@ def test_occupations_and_eigenvalues(lib, tmp_path, stream):
     assert d.c0.shape == (96, 3) and np.array_equal(d.c0, c[:, :3])
     assert np.array_equal(d.f, occ) and np.array_equal(d.eigv, eig) and d.amu == 0.125
     assert d.has_section(23) and d.has_section(24)
-    # the reference's own sections in between: velocities (10), potential (18), density (22)
+    # the reference's own sections in between: accumulators (11), potential (18), density (22)
     q = tmp_path / "RESTART.fill"
-    fill = {10: [b"v" * 20, b"w" * 40, b"x" * 8], 18: [b"p" * 160], 22: [b"r" * 72, b"s" * 8]}
+    fill = {11: [b"v" * 20, b"w" * 40, b"x" * 8], 18: [b"p" * 160], 22: [b"r" * 72, b"s" * 8]}
     RO.write(q, c, na=na, tau0=tau0, ecut=20.0, nel=9, nr=32, celldm=[10, 1, 1, 0, 0, 0], f=occ, eigv=eig,
              amu=-0.25, fill=fill, stream=stream, icompr=2)
     d = read_restart(q, nstate=2)
@@ -237,3 +238,36 @@ def test_file_may_end_after_the_states(lib, tmp_path):
     q.write_bytes(raw[:cut])
     d = read_restart(q)
     assert np.array_equal(d.c0, c) and d.f is None and d.eigv is None
+
+
+@pytest.mark.parametrize("icompr", [1, 2])
+@pytest.mark.parametrize("stream", [False, True])
+def test_wavefunction_velocities(lib, tmp_path, icompr, stream):
+    """Section 10 (wr30wfn 'NIL', scale = largest |component|) both ways, ahead of
+    sections 23-24, with fewer states read than stored."""
+    from cpmd_gb300.restart import read_restart, write_restart
+    na, tau0 = cell(13)
+    c = states(80, 5, 13)
+    cm = states(80, 5, 14) * 1e-3
+    occ = np.full(5, 2.0)
+    p = tmp_path / "RESTART.cm"
+    if not stream:
+        write_restart(p, c, na=na, tau0=tau0, ecut=20.0, nel=10, nr=32, alat=10.0, cm=cm, f=occ, icompr=icompr)
+        ref = RO.read(p)
+        assert ref["cm_scale"] == np.abs(np.concatenate([cm.real.ravel(), cm.imag.ravel()])).max()
+        if icompr == 1:
+            assert np.array_equal(ref["cm"], cm)
+    else:
+        RO.write(p, c, na=na, tau0=tau0, ecut=20.0, nel=10, nr=32, celldm=[10, 1, 1, 0, 0, 0], cm=cm, f=occ,
+                 icompr=icompr, stream=True)
+        ref = RO.read(p)
+    d = read_restart(p, nstate=3)
+    assert d.has_section(10) and d.cm.shape == (80, 3)
+    assert np.array_equal(d.cm, ref["cm"][:, :3])
+    if icompr == 1:
+        assert np.array_equal(d.cm, cm[:, :3])
+    else:
+        assert np.abs(d.cm[:-1] - cm[:-1, :3]).max() <= ref["cm_scale"] / (2 ** 31 - 1)
+    assert np.array_equal(d.f, occ)
+    full = read_restart(p)
+    assert full.cm.shape == (80, 5) and np.array_equal(full.cm, ref["cm"])
