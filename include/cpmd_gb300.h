@@ -85,7 +85,9 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  * become per-context settings):
  *   GBCP_OPT_GEMM   overlap GEMM engine: -1 = by precision (MIXED -> tensor
  *                   cores), 0 = FP64 SIMT, 1 = tcgen05 split-precision
- *                   (FP64-accurate);
+ *                   (FP64-level: per product term below 2^-52 of the scale
+ *                   of its row and column maxima, the overlap rounded once,
+ *                   C M within 2^-54 of that scale more);
  *   GBCP_OPT_BATCH  state pairs per band-loop launch (1..64);
  *   GBCP_OPT_FFT    band-loop FFT kernels: 0 = four-step register codelets
  *                   where the mesh has a plan, else Stockham; 2 = Stockham;
