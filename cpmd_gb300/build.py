@@ -29,7 +29,7 @@ def nvcc() -> str:
 
 
 def _flags(extra=()):
-    return ["-O3", "-std=c++17", "-lineinfo", "--use_fast_math" if False else "-Xptxas=-O3",
+    return ["-O3", "-std=c++17", "-lineinfo", "-Xptxas=-O3",
             "-Xcompiler", "-fPIC", *ARCH, *extra]
 
 

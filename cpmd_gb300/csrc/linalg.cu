@@ -22,6 +22,8 @@
 #include <mutex>
 #include <vector>
 
+#include <cuda.h>
+
 #include "ctx.h"
 
 namespace gbcp {
@@ -652,23 +654,73 @@ static __device__ __align__(256) double g_noalloc_scratch[size_t(1) << 20];
 
 namespace {
 constexpr size_t kNoAllocDoubles = size_t(1) << 20;
-constexpr int kNoAllocMaxDevices = 64;
-double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
-std::mutex g_noalloc_mu;
+constexpr int kNoAllocSlots = 64;
 
-// Device address of the scratch array for the current device.  The host-side
-// name g_noalloc_scratch is only a stand-in for the symbol, not a device
-// address, so it is resolved once per device with cudaGetSymbolAddress.
-int noalloc_scratch(double** out) {
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return 5;
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return 5;
-    g_noalloc_ptr[dev] = static_cast<double*>(p);
+// The array's device address belongs to the module as loaded into one CUDA
+// context: a cudaDeviceReset, or a caller's own driver-API context on the same
+// device, loads the module again at another address.  So the address is looked
+// up once per context and remembered under the context's process-unique id
+// (cuCtxGetId, reached through the runtime's driver entry points so that no
+// driver library is linked), never under the device ordinal.
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+struct NoAllocSlot {
+  unsigned long long ctx_id = 0;
+  double* ptr = nullptr;
+};
+NoAllocSlot g_noalloc_slots[kNoAllocSlots];
+int g_noalloc_next = 0;
+std::mutex g_noalloc_mu;
+PfnCtxGetCurrent g_ctx_current = nullptr;
+PfnCtxGetId g_ctx_id = nullptr;
+bool g_entry_looked_up = false;
+
+// id of the current context; false when it cannot be told (then the address
+// is looked up on every call, which is always correct)
+bool current_ctx_id(unsigned long long* id) {
+  if (!g_entry_looked_up) {
+    g_entry_looked_up = true;
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+        q1 == cudaDriverEntryPointSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+        q2 == cudaDriverEntryPointSuccess) {
+      g_ctx_current = reinterpret_cast<PfnCtxGetCurrent>(f1);
+      g_ctx_id = reinterpret_cast<PfnCtxGetId>(f2);
+    }
   }
-  *out = g_noalloc_ptr[dev];
+  if (!g_ctx_current || !g_ctx_id) return false;
+  CUcontext cx = nullptr;
+  if (g_ctx_current(&cx) != CUDA_SUCCESS || cx == nullptr) return false;
+  return g_ctx_id(cx, id) == CUDA_SUCCESS && *id != 0;
+}
+
+// Device address of the scratch array in the current context.  The host-side
+// name g_noalloc_scratch is only a stand-in for the symbol, not a device
+// address, so it is resolved with cudaGetSymbolAddress (which allocates
+// nothing; on a context's first use it loads the module, which is why the
+// first call in a context should come before any stream capture).
+int noalloc_scratch(double** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  unsigned long long id = 0;
+  const bool known = current_ctx_id(&id);
+  if (known) {
+    for (const NoAllocSlot& s : g_noalloc_slots)
+      if (s.ctx_id == id) {
+        *out = s.ptr;
+        return 0;
+      }
+  }
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return 5;
+  *out = static_cast<double*>(p);
+  // the lookup may have made the primary context current just now
+  if (known || current_ctx_id(&id)) {
+    g_noalloc_slots[g_noalloc_next] = {id, *out};
+    g_noalloc_next = (g_noalloc_next + 1) % kNoAllocSlots;
+  }
   return 0;
 }
 }  // namespace
@@ -682,6 +734,9 @@ extern "C" int gbcp_ovlap_noalloc(const double* c0, int ldc, int ngw, int nstate
   const int n = nstate;
   const size_t nn = (size_t)n * n;
   if (nn > kNoAllocDoubles) return 1;  // nstate above 1024
+  // an error the caller left pending is theirs: report it without launching,
+  // so that the launch checks below see only this call's own errors
+  if (cudaPeekAtLastError() != cudaSuccess) return 5;
   double* scratch = nullptr;
   if (noalloc_scratch(&scratch)) return 5;
   const int K = 2 * ngw, lda = 2 * ldc;

@@ -220,7 +220,17 @@ struct RecReader {
   FILE* f = nullptr;
   bool stream = false;  // STREAM file: no record frames
   bool ok = true;
-  explicit RecReader(const char* path) : f(std::fopen(path, "rb")) { ok = f != nullptr; }
+  int64_t size = 0;      // file length: no record or state may claim more than what is left
+  explicit RecReader(const char* path) : f(std::fopen(path, "rb")) {
+    ok = f != nullptr;
+    if (ok && std::fseek(f, 0, SEEK_END) == 0) {
+      size = (int64_t)std::ftell(f);
+      ok = size >= 0 && std::fseek(f, 0, SEEK_SET) == 0;
+    } else {
+      ok = false;
+    }
+  }
+  int64_t left() const { return f ? size - (int64_t)std::ftell(f) : 0; }
   ~RecReader() {
     if (f) std::fclose(f);
   }
@@ -232,11 +242,13 @@ struct RecReader {
   bool next(std::vector<uint8_t>& buf, size_t want) {
     if (!ok) return false;
     if (stream) {
+      if ((int64_t)want > left()) return ok = false;
       buf.resize(want);
       return raw(buf.data(), want);
     }
     int32_t m = 0, t = 0;
     if (!raw(&m, 4) || m < 0) return ok = false;  // negative: a split record, not written by the reference here
+    if ((int64_t)m + 4 > left()) return ok = false;  // longer than the rest of the file: corrupt
     buf.resize((size_t)m);
     if (!raw(buf.data(), (size_t)m) || !raw(&t, 4) || t != m) return ok = false;
     return true;
@@ -297,7 +309,10 @@ int64_t decompress_state(const uint32_t* w, int32_t nx, int icompr, double scale
 int read_states(RecReader& rd, std::vector<uint8_t>& buf, int n0, int ngwks0, int icompr, double scale,
                 double* dst, int ld, int ngw, int cap, int64_t fpos, int32_t* nread) {
   const int nr = dst ? (n0 < cap ? n0 : cap) : 0;
-  std::vector<double> ca(2 * (size_t)ngwks0 + 16);
+  // a state of ngwks0 coefficients takes at least 2 ngwks0 bytes (icompr 8), so a
+  // count beyond what is left of the file is corrupt (and must not size a buffer)
+  if (nr > 0 && 2 * (int64_t)ngwks0 > rd.left()) return GBCP_ERR_IO;
+  std::vector<double> ca(nr > 0 ? 2 * (size_t)ngwks0 + 16 : 0);
   *nread = 0;
   for (int s = 0; s < nr; ++s) {
     int32_t nx = 0;
@@ -510,5 +525,19 @@ int read_restart(const char* path, gbcp_restart* r) {
 
 }  // namespace
 
-extern "C" int gbcp_restart_write(const char* path, const gbcp_restart* r) { return write_restart(path, r); }
-extern "C" int gbcp_restart_read(const char* path, gbcp_restart* r) { return read_restart(path, r); }
+// No C++ exception may cross the C ABI into a Fortran or C caller: a failed
+// allocation (or any other exception) becomes GBCP_ERR_IO.
+extern "C" int gbcp_restart_write(const char* path, const gbcp_restart* r) {
+  try {
+    return write_restart(path, r);
+  } catch (...) {
+    return GBCP_ERR_IO;
+  }
+}
+extern "C" int gbcp_restart_read(const char* path, gbcp_restart* r) {
+  try {
+    return read_restart(path, r);
+  } catch (...) {
+    return GBCP_ERR_IO;
+  }
+}

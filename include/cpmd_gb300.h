@@ -167,10 +167,14 @@ int gbcp_rortog(gbcp_ctx* ctx, const double* c0, int ldc0, double* cm, int ldcm,
  * It calls no cudaMalloc/cudaFree: its split-K partial sums live in a fixed
  * 8 MiB device array inside the library (held by every GPU that loads the
  * library until the process exits), so nstate <= 1024 (GBCP_ERR_ARG above).
- * The first call on each device, with that device current, looks up the
- * array's device address (cudaGetSymbolAddress); make that first call before
- * any stream capture.  All calls share the array: calls whose work overlaps on
- * the GPU race.  c0: device, complex, leading dimension ldc >= ngw;
+ * The first call in each CUDA context (normally: once per device, with that
+ * device current) looks up the array's device address in that context
+ * (cudaGetSymbolAddress) and remembers it under the context's unique id, so a
+ * new context after cudaDeviceReset, or a caller's own driver-API context, gets
+ * its own lookup; make that first call before any stream capture.  An error
+ * already pending in the calling thread is returned as GBCP_ERR_CUDA without
+ * launching.  All calls share the array: calls whose work overlaps on the GPU
+ * race.  c0: device, complex, leading dimension ldc >= ngw;
  * smat: device, nstate x nstate. */
 int gbcp_ovlap_noalloc(const double* c0, int ldc, int ngw, int nstate, int geq0, double* smat, void* stream);
 

@@ -162,6 +162,33 @@ def test_malformed_files_are_reported(lib, tmp_path):
     assert _status(lib, tmp_path / "text") == 9
 
 
+def test_oversized_counts_are_reported_not_allocated(lib, tmp_path):
+    """Lengths and counts read from a corrupt file are bounded by what is left
+    of the file: a 2 GiB record marker or a 2^30-coefficient state count is
+    reported as GBCP_ERR_IO before any buffer is sized from it."""
+    na, tau0 = cell()
+    c = states(64, 3, 5)
+    good = tmp_path / "RESTART.good"
+    RO.write(good, c, na=na, tau0=tau0, ecut=20.0, nel=6, nr=32, celldm=[10, 1, 1, 0, 0, 0])
+    data = good.read_bytes()
+    bad = bytearray(data)
+    bad[0:4] = struct.pack("<i", 2 ** 31 - 1)  # leading frame of the first record
+    (tmp_path / "huge_record").write_bytes(bytes(bad))
+    assert _status(lib, tmp_path / "huge_record") == 9
+    # the w_wfnio header (n, ngwks, icompr, scale): n = 3 states of ngwks = 64 coefficients
+    key = struct.pack("<ii", 3, 64)
+    at = data.find(key)
+    assert at > 0
+    bad = bytearray(data)
+    bad[at + 4:at + 8] = struct.pack("<i", 2 ** 30)
+    (tmp_path / "huge_states").write_bytes(bytes(bad))
+    from cpmd_gb300 import GbcpError
+    from cpmd_gb300.restart import read_restart
+    with pytest.raises(GbcpError) as e:
+        read_restart(tmp_path / "huge_states")
+    assert e.value.code == 9
+
+
 def test_unsupported_layouts_are_reported(lib, tmp_path):
     na, tau0 = cell()
     c = states(64, 3, 6)
