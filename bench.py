@@ -1,8 +1,9 @@
 #!/usr/bin/env python
 """Benchmark: state-applies/s of the Γ-point wavefunction step (H psi + rho + ortho).
 
-One step = rhoofr + vpsi + ortho(Gram-Schmidt) over all states of the cell,
-i.e. the three hot-path routines a CPMD wavefunction-optimisation step calls
+One step = rhoofr (density, kinetic energy and the reference's charge check)
++ vpsi + ortho(Gram-Schmidt) over all states of the cell, i.e. the three
+hot-path routines a CPMD wavefunction-optimisation step calls
 (forces_driver.mod.F90:165-224, updwf_utils.mod.F90:150).
 state-applies/s = nstate * steps / time.
 
@@ -13,9 +14,9 @@ V*psi, FP64 accumulation, reductions and ortho); the plain FP64 drop-in is
 measured in the same run (`fp64`).  Inputs (c0, c2: 87.5 MB each) are larger
 than the 129 MB L2 together, so no L2 flush is needed between steps.
 
---impl reference times the reference's CPU path restated in numpy/scipy (the
-reference itself, Fortran + FFTW + BLAS, cannot be built here) on a bounded
-sample of the same step, on all host cores.
+--impl reference times the reference's CPU path restated in C++/OpenMP FP64
+(oracle/cpmd_port.cpp; the reference itself, Fortran + FFTW + BLAS, cannot be
+built here): full 128-state steps on all host cores of rank 0.
 
 Multi-GPU (torchrun): every rank runs an independent replica (the step does
 not shard across GPUs in this build); value = total over ranks, time = max.
@@ -118,51 +119,64 @@ def allreduce_max(x: float, world: int) -> float:
     return float(t.item())
 
 
-# ----------------------------------------------------------------------------- CPU reference (oracle port)
-def cpu_reference_sample(cell, n_band: int = 16):
-    """Time the restated reference path on a bounded sample: rhoofr + vpsi on
-    the first n_band states, ortho (Cholesky GS) on all states.  Returns the
-    extrapolated full-step time and a description."""
+# ----------------------------------------------------------------------------- CPU reference (C++ port)
+def bench_config(world: int) -> dict:
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": WORKLOAD, "global_batch": 128 * world, "seq_len": 120 ** 3,
+            "parallelism": "replicas" if world > 1 else "none",
+            "l2": "inputs larger than L2 (c0+c2 = 175 MB)"}
+
+
+def cpu_port_steps(cell, steps: int, warmup: int = 0, threads: int = 0, n_band=None):
+    """Time the C++/OpenMP FP64 restatement of the step (rhoofr + vpsi + Gram-Schmidt)
+    on the host cores.  n_band: time rhoofr + vpsi on the first n_band states only (a
+    bounded sample of a large cell; then ortho is not timed).  Returns (seconds per step,
+    threads, states the timed step covered)."""
     import numpy as np
-    from oracle import cpmd_oracle as O
-    b = cell.basis
-    sub = np.asfortranarray(cell.c0[:, :n_band])
-    f = cell.f[:n_band]
+    from oracle import cpmd_port as CP
+    port = CP.Port(cell.basis, threads)
+    c0 = np.asfortranarray(cell.c0 if n_band is None else cell.c0[:, :n_band])
+    f = np.ascontiguousarray(cell.f[: c0.shape[1]])
+    c2 = np.zeros_like(c0)
+    work = c0.copy(order="F")
+
+    def step():
+        _, ek, cg, cr = port.rhoofr(work, f)
+        if abs(cr - cg) > 1e-6:  # the reference's charge check (rhoofr_utils.mod.F90:625)
+            raise RuntimeError("port: total density sums are not equal")
+        port.vpsi(work, c2, f, cell.vpot)
+        if n_band is None:
+            port.rgs(work)
+
+    for _ in range(warmup):
+        step()
     t0 = time.perf_counter()
-    O.rhoofr(sub, f, b.mill, b.nr, b.kr, b.omega, b.hg, b.tpiba2, b.geq0)
-    O.vpsi(sub, np.zeros_like(sub), f, cell.vpot, b.mill, b.nr, b.hg, b.tpiba2, b.geq0)
-    t1 = time.perf_counter()
-    O.rgs(cell.c0, b.geq0)
-    t2 = time.perf_counter()
-    n = cell.nstate
-    t_step = (t1 - t0) * (n / n_band) + (t2 - t1)
-    return t_step, (t1 - t0), (t2 - t1)
+    for _ in range(steps):
+        step()
+    t = (time.perf_counter() - t0) / max(1, steps)
+    th = port.threads
+    port.close()
+    return t, th, c0.shape[1]
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the C++/OpenMP FP64 restatement of rhoofr + vpsi + rgs
+    (the reference's own Fortran/FFTW/BLAS build is not possible here), full
+    128-state steps of the 64-atom cell on all host cores of rank 0."""
     if rank != 0:
         return
     from cpmd_gb300.synth import make_cell
     cell = make_cell("c1")
-    cores = os.cpu_count() or 1
-    for _ in range(args.warmup):
-        cpu_reference_sample(cell, args.ref_states)
-    ts = []
-    for _ in range(args.steps):
-        t_step, tb, to = cpu_reference_sample(cell, args.ref_states)
-        ts.append(t_step)
-    t = sum(ts) / len(ts)
+    t, th, _ = cpu_port_steps(cell, args.steps, args.warmup)
     value = cell.nstate / t
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "state-applies/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "global_batch": cell.nstate, "seq_len": 120 ** 3, "parallelism": "none",
-                   "l2": "inputs larger than L2"},
-        "cpu_baseline": {"value": value, "unit": "state-applies/s", "cores": cores, "kind": "port",
-                         "sample": f"numpy/scipy restatement (scipy.fft workers=-1, OpenBLAS): rhoofr+vpsi on "
-                                   f"{args.ref_states} of {cell.nstate} states scaled x{cell.nstate // args.ref_states}"
-                                   f", ortho on all {cell.nstate} states, per step"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded psi, V_loc)",
+        "config": bench_config(world),
+        "cpu_baseline": {"value": value, "unit": "state-applies/s", "cores": th, "kind": "port",
+                         "sample": f"C++/OpenMP FP64 restatement of rhoofr + vpsi + Gram-Schmidt ortho "
+                                   f"(oracle/cpmd_port.cpp), full {cell.nstate}-state steps, {th} threads"},
         "e2e": {"value": value, "unit": "state-applies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -232,8 +246,10 @@ def run_gpu(args, rank, world, local):
     c2 = torch.zeros_like(c0)
 
     def make_step(ctx):
+        # the reference's full rhoofr: density, kinetic energy and the charge check
+        # (the library returns an error when |csumr - csumg| fails it)
         def step():
-            ctx.rhoofr(c0, f, rho, energies=False)
+            ctx.rhoofr(c0, f, rho, energies=True)
             ctx.vpsi(c0, c2, f, v)
             ctx.ortho(c0, "gs")
         return step
@@ -318,55 +334,72 @@ def run_gpu(args, rank, world, local):
     vh[:] = cell.vpot
     rhoh = pin(tuple(b.kr[::-1]), torch.float64)
 
-    def e2e_step():
-        ctx_mx.rhoofr(c0h, fh, rhoh, energies=False)
-        ctx_mx.vpsi(c0h, c2h, fh, vh)
-        ctx_mx.ortho(c0h, "gs")
+    def e2e_run(ctx, steps):
+        def e2e_step():
+            ctx.rhoofr(c0h, fh, rhoh, energies=True)
+            ctx.vpsi(c0h, c2h, fh, vh)
+            ctx.ortho(c0h, "gs")
+        for _ in range(2):
+            e2e_step()
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            e2e_step()
+        return allreduce_max(time.perf_counter() - t0, world)
 
-    for _ in range(2):
-        e2e_step()
-    barrier(world)
-    t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
-        e2e_step()
-    t_e2e = allreduce_max(time.perf_counter() - t0, world)
+    t_e2e = e2e_run(ctx_mx, args.e2e_steps)
+    c0h[:] = cell.c0
+    t_e2e64 = e2e_run(ctx_64, 2)
     wfn = b.ngw * n * 16
     grid = b.nnr1 * 8
     h2d = 3 * wfn + wfn + 2 * n * 8 + grid
     d2h = grid + wfn + wfn
     e2e = world * n * args.e2e_steps / t_e2e
+    e2e64 = world * n * 2 / t_e2e64
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        ts = [cpu_reference_sample(cell, args.ref_states)[0] for _ in range(2)]
-        cpu = {"value": n / min(ts), "unit": "state-applies/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"numpy/scipy restatement of rhoofr+vpsi on {args.ref_states} of {n} states scaled "
-                         f"x{n // args.ref_states} + ortho on all {n} states; best of 2"}
+        t_cpu, th, _ = cpu_port_steps(cell, 2, 1)
+        cpu = {"value": n / t_cpu, "unit": "state-applies/s", "cores": th, "kind": "port",
+               "sample": f"C++/OpenMP FP64 restatement (oracle/cpmd_port.cpp) of rhoofr + vpsi + Gram-Schmidt, "
+                         f"2 full {n}-state steps after 1 warm-up, {th} threads"}
 
     extras = None
     if rank == 0 and world == 1 and not args.no_extras:
         del c0h, c2h
         extras = run_extras(args, dev)
 
+    # every band-loop stage against the HBM roof (algorithmic bytes per launch / mean launch time)
+    stages = {}
+    for k, (t_ms, cnt) in prof.items():
+        by = kernel_bytes(k, geo, bt, 8)
+        if by and cnt:
+            gbs = by / (t_ms / cnt / 1e3) / 1e9
+            stages[k] = {"ms_per_step": round(t_ms / 2, 4), "GB_s": round(gbs, 1), "frac": round(gbs / hbm, 3)}
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "state-applies/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_mx / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32-fft/f64-accum", "data": "synthetic (seeded psi, V_loc)",
-            "config": {"workload": WORKLOAD, "global_batch": n * world, "seq_len": 120 ** 3,
-                       "parallelism": "replicas" if world > 1 else "none", "precision": "mixed",
-                       "pairs_per_batch": bt, "l2": "inputs larger than L2 (c0+c2 = 175 MB)"},
+            "config": bench_config(world),
+            "run": {"precision": "mixed", "pairs_per_batch": bt, "step": "rhoofr (with E_kin and the charge check) "
+                    "+ vpsi + Gram-Schmidt ortho over all 128 states"},
             "fp64": {"value": v64, "ms_per_step": ms_64 / args.fp64_steps, "steps": args.fp64_steps,
                      "mixed_over_fp64": value / v64},
             "accuracy": {"dE_Ha_per_atom_mixed_vs_fp64": abs(emx - e64) / nat, "E_fp64_Ha": e64},
             "roofline": {"bound": bound, "kernel": dname, "achieved": achieved, "peak": peak, "unit": unit,
                          "frac": (achieved / peak) if achieved else None, "traffic": NCU_TRAFFIC.get(dname),
                          "peak_source": src, "launch_ms": per_launch_ms, "work_per_launch": work,
-                         "kernel_share": dms / 2 / step_ms_prof},
+                         "kernel_share": dms / 2 / step_ms_prof, "stages": stages},
             "kernels_ms_per_step": {k: round(t / 2, 4) for k, (t, _) in sorted(prof.items(), key=lambda kv: -kv[1][0])},
             "clocks": clocks,
             "e2e": {"value": e2e, "unit": "state-applies/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "steps": args.e2e_steps, "path": "C ABI, host (pinned) buffers, GBCP_MEM_HOST"},
+                    "steps": args.e2e_steps, "path": "C ABI, host (pinned) buffers, GBCP_MEM_HOST",
+                    "fp64_drop_in": {"value": v64, "e2e_value": e2e64, "ms_per_step": ms_64 / args.fp64_steps,
+                                     "mixed_over_fp64": value / v64,
+                                     "note": "the plain FP64 drop-in on the same cell, device-resident "
+                                             "(value) and through host buffers (e2e_value)"}},
             "gpu_launches": launches,
             "cpu_baseline": cpu,
             "other_configs": extras,
@@ -374,6 +407,22 @@ def run_gpu(args, rank, world, local):
         print(json.dumps(line), flush=True)
     ctx_mx.close()
     ctx_64.close()
+
+
+def cpu_band_sample(cl, n_band: int) -> dict:
+    """CPU baseline of a large device-resident cell: the C++/OpenMP FP64
+    restatement's rhoofr + vpsi on its first n_band states (copied to the host),
+    one timed call after one warm-up; the rate is per state of the band loop
+    only (the rest of the cell's step is not in the sample)."""
+    import types
+    import numpy as np
+    c0 = np.asfortranarray(cl.c0[:n_band].cpu().numpy().T)
+    host = types.SimpleNamespace(basis=cl.basis, c0=c0, f=cl.f[:n_band].cpu().numpy(),
+                                 vpot=np.ascontiguousarray(cl.vpot.cpu().numpy()))
+    t, th, ns = cpu_port_steps(host, 1, 1, n_band=n_band)
+    return {"value": ns / t, "unit": "state-applies/s (band loop only)", "cores": th, "kind": "port",
+            "sample": f"C++/OpenMP FP64 restatement: rhoofr + vpsi on {ns} of {cl.nstate} states, one call after "
+                      f"one warm-up, {th} threads; ortho, projectors and the energy terms not timed"}
 
 
 def _timed_loop(step, steps, warmup):
@@ -415,12 +464,15 @@ def run_extras(args, dev):
         ctx = Context(b, prec)
 
         def step():
-            ctx.rhoofr(c0, f, rho, energies=False)
+            ctx.rhoofr(c0, f, rho, energies=True)
             ctx.vpsi(c0, c2, f, v)
             ctx.ortho(c0, "gs")
         ms = _timed_loop(step, 50, 5)
         r[prec] = {"state_applies_per_s": cl.nstate / (ms / 1e3), "ms_per_step": ms}
         ctx.close()
+    t_cpu, th, _ = cpu_port_steps(cl, 20, 2)
+    r["cpu_baseline"] = {"value": cl.nstate / t_cpu, "unit": "state-applies/s", "cores": th, "kind": "port",
+                         "sample": "C++/OpenMP FP64 restatement, 20 full 16-state steps (rhoofr + vpsi + rgs)"}
     out["cell_8atoms_16states_32cubed"] = r
 
     # ---- CP-dynamics constraint (rortog) on the 64-atom cell: 128 states, ngw 42 736
@@ -498,6 +550,7 @@ def run_extras(args, dev):
                 "dE_Ha_per_atom_mixed_vs_fp64": abs(pbe["mixed"]["E_Ha"] - pbe["fp64"]["E_Ha"]) / nat,
                 "dF_max_Ha_per_bohr_mixed_vs_fp64": float((pbe["mixed"]["F"] - pbe["fp64"]["F"]).abs().max()),
                 "E_fp64_Ha": pbe["fp64"]["E_Ha"]}
+    r["cpu_baseline"] = cpu_band_sample(cl, 16)
     out["adjoint_216atoms_432states_144cubed"] = r
     del cl, res, holder, vps, tau
     torch.cuda.empty_cache()
@@ -518,7 +571,7 @@ def run_extras(args, dev):
         c2 = torch.zeros_like(c)
 
         def step():
-            ctx.rhoofr(c, cl.f, rho, energies=False)
+            ctx.rhoofr(c, cl.f, rho, energies=True)
             ctx.vpsi(c, c2, cl.f, cl.vpot)
             ctx.rnlsm(c, p["twnl"], p["eigr"], p["nghtol"], fnl)
             ctx.fnonloc(c2, cl.f, fnl, p["twnl"], p["eigr"], p["nghtol"], p["wsg"])
@@ -546,6 +599,7 @@ def run_extras(args, dev):
     r["dE_Ha_per_atom_mixed_vs_fp64"] = abs(energies["mixed"] - energies["fp64"]) / nat
     r["workload"] = ("rhoofr + vpsi + rnlsm1 + fnonloc + Loewdin ortho, 512 atoms, 1024 states, 70 Ry "
                      f"(ngw={b.ngw}), 240^3, 4096 projectors; nl_forces_ms = rnlsm1 + rnlsm2 + rnlfor")
+    r["cpu_baseline"] = cpu_band_sample(cl, 16)
     out["projectors_512atoms_1024states_240cubed"] = r
     del cl, p, rho, fnl
     torch.cuda.empty_cache()
@@ -591,7 +645,7 @@ def run_extras(args, dev):
 
     def seq():
         for cx_, x in zip(ctxs, io):
-            cx_.rhoofr(x["c0"], x["f"], x["rhoe"], energies=False)
+            cx_.rhoofr(x["c0"], x["f"], x["rhoe"], energies=True)
             cx_.vpsi(x["c0"], x["c2"], x["f"], x["vpot"])
             cx_.ortho(x["c0"], "gs")
         torch.cuda.synchronize()
@@ -606,6 +660,18 @@ def run_extras(args, dev):
     de = np.abs(en["mixed"].sum(axis=1) - en["fp64"].sum(axis=1)) / nats
     r["mixed_sequential_contexts"] = {"state_applies_per_s": nst / (ms_seq / 1e3), "ms_per_step": ms_seq}
     r["dE_Ha_per_atom_mixed_vs_fp64_max"] = float(de.max())
+    # CPU baseline: the C++/OpenMP restatement on one cell of each size class (full steps),
+    # weighted by the number of cells in the class
+    classes = {}
+    for cc in cells:
+        classes.setdefault((tuple(cc.basis.nr), cc.basis.ngw, cc.c0.shape[1]), []).append(cc)
+    t_all, th = 0.0, 1
+    for members in classes.values():
+        t, th, _ = cpu_port_steps(members[0], 2, 1)
+        t_all += t * len(members)
+    r["cpu_baseline"] = {"value": nst / t_all, "unit": "state-applies/s", "cores": th, "kind": "port",
+                         "sample": f"C++/OpenMP FP64 restatement, 2 full steps of one cell per size class "
+                                   f"({len(classes)} classes) scaled by the class counts, {th} threads"}
     r["timing"] = "host wall clock per step: one cudaGraphLaunch + stream synchronise"
     r["workload"] = (f"64 cells, atoms uniform in {{8,16,32,64}}, {nst} states in total, 30 Ry, meshes 36^3-72^3, "
                      "rhoofr + vpsi + GS ortho")
@@ -658,7 +724,6 @@ def main():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--fp64-steps", type=int, default=5)
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--ref-states", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the 8-, 216- and 512-atom cells")
     ap.add_argument("--case", default=None, choices=["projectors"],

@@ -12,6 +12,7 @@ GBCP_OK = 0
 STATUS = {
     0: "OK", 1: "ERR_ARG", 2: "ERR_NOT_SPD", 3: "ERR_NONFINITE", 4: "ERR_TIMEOUT",
     5: "ERR_CUDA", 6: "ERR_NOMEM", 7: "ERR_UNSUPPORTED", 8: "ERR_NOT_CONVERGED", 9: "ERR_IO",
+    10: "ERR_CHARGE",
 }
 PREC = {"fp64": 0, "mixed": 1}
 MEM_HOST, MEM_DEVICE = 0, 1

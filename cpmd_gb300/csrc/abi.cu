@@ -233,7 +233,9 @@ static int build_geometry(Ctx& c, const int32_t* inyh, const double* hg) {
   for (int ig = 0; ig < ngw; ++ig)
     if (pos_minus[ig] < 0) pos_minus[ig] = pos_plus[ig];  // G = 0 is its own mirror
   std::vector<double> hgv(hg, hg + ngw);
+  std::vector<float> hg32v(hg, hg + ngw);
   GeoDev& g = c.geo;
+  g.geq0 = c.geq0;
   g.n1 = n[0];
   g.n2 = n[1];
   g.n3 = n[2];
@@ -248,7 +250,7 @@ static int build_geometry(Ctx& c, const int32_t* inyh, const double* hg) {
       !upload(c, col_slot, g.col_slot) || !upload(c, col_gy, g.col_gy) || !upload(c, ent_col, g.ent_col) ||
       !upload(c, slot_col0, g.slot_col0) || !upload(c, slot_gylo, g.slot_gylo) ||
       !upload(c, slot_ncol, g.slot_ncol) || !upload(c, pos_plus, g.pos_plus) || !upload(c, pos_minus, g.pos_minus) ||
-      !upload(c, hgv, g.hg)) {
+      !upload(c, hgv, g.hg) || !upload(c, hg32v, g.hg32)) {
     c.err = "geometry upload failed";
     return 6;
   }
@@ -626,6 +628,13 @@ bool bad_mem(int mem) { return mem != GBCP_MEM_HOST && mem != GBCP_MEM_DEVICE; }
 
 extern "C" {
 
+// |csumr - csumg| allowed by rhoofr's charge check: the reference's delta = 1e-6
+// (rhoofr_utils.mod.F90:625) in FP64; in the mixed mode, where rho comes from
+// FP32 transforms, 1e-6 of the charge (the FP32 density agrees to ~1e-7 of it).
+static double charge_tolerance(const gbcp::Ctx& c, double csumg) {
+  return c.precision == GBCP_PREC_FP64 ? 1e-6 : 1e-6 * std::max(1.0, std::fabs(csumg));
+}
+
 int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double* f, double* rhoe, double* ekin,
                 double* csumg, double* csumr, int mem) {
   if (!h) return GBCP_ERR_ARG;
@@ -659,23 +668,40 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
     drho = static_cast<double*>(c.st_rho.p);
     dld = c.ngw;
   }
-  rc = gbcp::band_rhoofr(c, dc0, dld, nstate, df, drho);
+  // E_kin and csumg are summed inside the band loop's gather, csumr from the
+  // density, all on the device; the host reads the three at the end
+  const bool scalars = ekin || csumg || csumr;
+  double* dsc = nullptr;
+  if (scalars) {
+    if (!gbcp::ensure(c, c.rho_sc, 4 * sizeof(double))) return GBCP_ERR_NOMEM;
+    dsc = static_cast<double*>(c.rho_sc.p);
+  }
+  rc = gbcp::band_rhoofr(c, dc0, dld, nstate, df, drho, dsc);
   c.batch_ready = nullptr;
   if (saved_batch) c.batch = saved_batch;
-  if (!rc && (ekin || csumg) && nstate > 0) rc = gbcp::kin_energy(c, dc0, dld, nstate, df, ekin, csumg);
-  if (!rc && nstate == 0) {
-    if (ekin) *ekin = 0.0;
-    if (csumg) *csumg = 0.0;
-  }
-  if (!rc && csumr) {
-    double s = 0.0;
-    rc = gbcp::rho_sum(c, drho, &s);
-    *csumr = s * c.omega / ((double)c.nr[0] * c.nr[1] * c.nr[2]);
-  }
   if (!rc && mem == GBCP_MEM_HOST) {
     gbcp::ProfScope ps_(c, "d2h_rho", c.stream, 2);
     cudaError_t e = cudaMemcpyAsync(rhoe, drho, sizeof(double) * nnr1, cudaMemcpyDeviceToHost, c.stream);
     if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (!rc && scalars) {
+    double hs[3] = {0.0, 0.0, 0.0};
+    GBCP_CUDA_TRY(c, cudaMemcpyAsync(hs, dsc, sizeof(hs), cudaMemcpyDeviceToHost, c.stream));
+    GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+    if (ekin) *ekin = hs[0];
+    if (csumg) *csumg = hs[1];
+    if (csumr) *csumr = hs[2];
+    if (!std::isfinite(hs[0]) || !std::isfinite(hs[1]) || !std::isfinite(hs[2])) {
+      c.err = "rhoofr: non-finite kinetic energy, norm or density";
+      rc = GBCP_ERR_NONFINITE;
+    } else if (std::fabs(hs[2] - hs[1]) > charge_tolerance(c, hs[1])) {
+      // the reference stops here: 'TOTAL DENSITY SUMS ARE NOT EQUAL' (rhoofr_utils.mod.F90:625-635)
+      char msg[160];
+      snprintf(msg, sizeof(msg), "rhoofr: total density sums are not equal (Fourier space %.12f, real space %.12f)",
+               hs[1], hs[2]);
+      c.err = msg;
+      rc = GBCP_ERR_CHARGE;
+    }
   }
   if (mem == GBCP_MEM_HOST || rc) return finish(c, rc);
   return GBCP_OK;

@@ -10,10 +10,14 @@
 
 namespace gbcp {
 
-int band_rhoofr_fp64(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho);
+int band_rhoofr_fp64(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho,
+                     double* kpart);
 int band_vpsi_fp64(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, const double* f,
                    const double* vpot, int nstate);
-int band_rhoofr_fp32(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho);
+int band_rhoofr_fp32(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho,
+                     double* kpart);
+int band_zinv_blocks_fp64(const Ctx& c);
+int band_zinv_blocks_fp32(const Ctx& c);
 int band_vpsi_fp32(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, const double* f,
                    const double* vpot, int nstate);
 
@@ -187,6 +191,62 @@ __global__ void k_fold_scaled(const double* __restrict__ part, int n, double sca
   if (threadIdx.x == 0) *out = scale * r[0];
 }
 
+// First fold level of rhoofr's scalars: CTA b sums the 2-component partials
+// [b*chunk, (b+1)*chunk) in index order into out[2b], out[2b+1].
+__global__ void k_fold2_ranges(const double* __restrict__ part, int n, int chunk, double* __restrict__ out) {
+  __shared__ double r0[kThreads], r1[kThreads];
+  const int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
+  double a = 0.0, b = 0.0;
+  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    a += part[2 * i];
+    b += part[2 * i + 1];
+  }
+  r0[threadIdx.x] = a;
+  r1[threadIdx.x] = b;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      r0[threadIdx.x] += r0[threadIdx.x + s];
+      r1[threadIdx.x] += r1[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[2 * blockIdx.x] = r0[0];
+    out[2 * blockIdx.x + 1] = r1[0];
+  }
+}
+
+// Last level: out = {tpiba2 * sum kin, sum norm, rscale * sum rho} from nk
+// 2-component kinetic/norm partials and nr density partials (k_sum_partial).
+__global__ void k_rho_scalars(const double* __restrict__ kp, int nk, const double* __restrict__ rp, int nr,
+                              double tpiba2, double rscale, double* __restrict__ out) {
+  __shared__ double r0[kThreads], r1[kThreads], r2[kThreads];
+  double a = 0.0, b = 0.0, d = 0.0;
+  for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+    a += kp[2 * i];
+    b += kp[2 * i + 1];
+  }
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) d += rp[2 * i];
+  r0[threadIdx.x] = a;
+  r1[threadIdx.x] = b;
+  r2[threadIdx.x] = d;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      r0[threadIdx.x] += r0[threadIdx.x + s];
+      r1[threadIdx.x] += r1[threadIdx.x + s];
+      r2[threadIdx.x] += r2[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = tpiba2 * r0[0];
+    out[1] = r1[0];
+    out[2] = rscale * r2[0];
+  }
+}
+
 }  // namespace
 static int lines_for(int n, int target) { return std::max(1, std::min(64, target / n)); }
 
@@ -195,10 +255,46 @@ template <typename T> static size_t stage_smem(int n, int nl) {
 }
 
 
-int band_rhoofr(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho) {
-  GBCP_CUDA_TRY(c, cudaMemsetAsync(rho, 0, sizeof(double) * (size_t)c.kr[0] * c.kr[1] * c.kr[2], c.stream));
-  if (nstate <= 0) return 0;
-  return c.precision == 0 ? band_rhoofr_fp64(c, c0, ldc, nstate, f, rho) : band_rhoofr_fp32(c, c0, ldc, nstate, f, rho);
+int band_rhoofr(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho,
+                double* scalars) {
+  const size_t nnr = (size_t)c.kr[0] * c.kr[1] * c.kr[2];
+  GBCP_CUDA_TRY(c, cudaMemsetAsync(rho, 0, sizeof(double) * nnr, c.stream));
+  if (nstate <= 0) {
+    if (scalars) GBCP_CUDA_TRY(c, cudaMemsetAsync(scalars, 0, 3 * sizeof(double), c.stream));
+    return 0;
+  }
+  // partials of E_kin / norm: one pair of doubles per Z-stage CTA of every pair,
+  // then one per first-level fold CTA, then the density sum's partials
+  const int npairs = (nstate + 1) / 2;
+  const int nkb = npairs * (c.precision == 0 ? band_zinv_blocks_fp64(c) : band_zinv_blocks_fp32(c));
+  const int kchunk = 4096, nk1 = (nkb + kchunk - 1) / kchunk, nrp = 296;
+  double* kpart = nullptr;
+  if (scalars) {
+    if (!ensure(c, c.red, sizeof(double) * 2 * ((size_t)nkb + nk1 + nrp))) return 6;
+    kpart = static_cast<double*>(c.red.p);
+  }
+  const int rc = c.precision == 0 ? band_rhoofr_fp64(c, c0, ldc, nstate, f, rho, kpart)
+                                  : band_rhoofr_fp32(c, c0, ldc, nstate, f, rho, kpart);
+  if (rc || !scalars) return rc;
+  double* k1 = kpart + 2 * (size_t)nkb;
+  double* rp = k1 + 2 * (size_t)nk1;
+  {
+    ProfScope ps_(c, "k_fold2_ranges");
+    k_fold2_ranges<<<nk1, kThreads, 0, c.stream>>>(kpart, nkb, kchunk, k1);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  {
+    ProfScope ps_(c, "k_sum_partial");
+    k_sum_partial<<<nrp, kThreads, 0, c.stream>>>(rho, nnr, rp);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  {
+    ProfScope ps_(c, "k_rho_scalars");
+    k_rho_scalars<<<1, kThreads, 0, c.stream>>>(k1, nk1, rp, nrp, c.tpiba2,
+                                                c.omega / ((double)c.nr[0] * c.nr[1] * c.nr[2]), scalars);
+    GBCP_LAUNCH_CHECK(c);
+  }
+  return 0;
 }
 
 int band_vpsi(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, const double* f, const double* vpot,

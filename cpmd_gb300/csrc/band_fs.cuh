@@ -62,7 +62,8 @@ __device__ __forceinline__ void load_table(cx<T>* dst, const cx<T>* __restrict__
 template <typename T, int N>
 __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>* __restrict__ c0, int ldc, int s0,
                                                      int nstate, cx<T>* __restrict__ zbuf,
-                                                     const cx<T>* __restrict__ twAg) {
+                                                     const cx<T>* __restrict__ twAg, const double* __restrict__ f,
+                                                     double* __restrict__ kpart) {
   using P = FS<T, N>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* twA = reinterpret_cast<cx<T>*>(smem_raw);
@@ -72,6 +73,7 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
   const bool two = is2 < nstate;
   const cx<double>* c1 = c0 + (size_t)is1 * ldc;
   const cx<double>* c2 = c0 + (size_t)(two ? is2 : is1) * ldc;
+  KinAcc<T> kacc;
   load_table(twA, twAg, N);
   __syncthreads();
 #pragma unroll
@@ -99,6 +101,7 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
             const T ux = from_double<T>(u.x), uy = from_double<T>(u.y);
             const T wx = from_double<T>(w.x), wy = from_double<T>(w.y);
             val = (e > 0) ? mk<T>(ux - wy, uy + wx) : mk<T>(ux + wy, wx - uy);
+            if (kpart && e > 0) kin_entry(kacc, g, ig, ux, uy, wx, wy);
           }
         }
         v[n1] = val;
@@ -121,6 +124,9 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
       }
     }
   }
+  if (kpart)
+    kin_flush(kacc, f[is1], two ? f[is2] : 0.0,
+              kpart + 2 * ((size_t)(s0 / 2 + pair) * gridDim.x + blockIdx.x));
 }
 
 // ---------------------------------------------------------------- Y stage (inverse)

@@ -75,11 +75,109 @@ __device__ __forceinline__ cx<T>* run_fft(cx<T>* a, cx<T>* b, int nl, int ls, co
   cx<T>* a = tw + N;                                              \
   cx<T>* b = a + nl * ls;
 
+// ---------------------------------------------------------------- rhoofr scalars in the Z-stage gather
+// The gather of rhoofr's Z stage holds every coefficient of the pair once as a
+// +G entry, so the kinetic energy E_kin = tpiba2 sum_i f_i sum_G hg |c_i(G)|^2
+// (kin_energy_utils.mod.F90:93-108; the 1/2 and the x2 of the half sphere
+// cancel) and the Γ norm csumg = sum_i f_i <c_i|c_i> (2|c|^2, Re c^2 at G = 0;
+// dotp_utils.mod.F90:45-52, rhoofr_utils.mod.F90:607-635) are summed there, with
+// no second read of c0.  Each CTA writes its two occupation-weighted totals to
+// kpart[2 b], kpart[2 b + 1], b = global pair * (column blocks) + column block.
+// FP64 kernels sum in FP64.  FP32 kernels square the FP32-rounded coefficients
+// (relative rounding 2^-24 per coefficient, unbiased) and accumulate in
+// double-float (Knuth's TwoSum), so no summation error builds up and the FP64
+// pipe, 1/58 of the FP32 rate on GB300, is used only once per warp.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float bh, float bl) {
+  const float s = hi + bh;
+  const float v = s - hi;
+  float e = (hi - (s - v)) + (bh - v);
+  e += lo + bl;
+  hi = s + e;
+  lo = e - (hi - s);
+}
+
+template <typename T> struct KinAcc;
+template <> struct KinAcc<double> {
+  double k1 = 0.0, n1 = 0.0, k2 = 0.0, n2 = 0.0;
+  __device__ __forceinline__ void add(double hg, double, bool g0, double ux, double uy, double wx, double wy) {
+    const double a1 = fma(ux, ux, uy * uy), a2 = fma(wx, wx, wy * wy);
+    k1 = fma(hg, a1, k1);
+    k2 = fma(hg, a2, k2);
+    n1 += g0 ? ux * ux : 2.0 * a1;
+    n2 += g0 ? wx * wx : 2.0 * a2;
+  }
+  // warp totals, FP64
+  __device__ __forceinline__ void warp_totals(double (&o)[4]) {
+    o[0] = k1; o[1] = n1; o[2] = k2; o[3] = n2;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) o[q] += __shfl_down_sync(0xffffffffu, o[q], d);
+  }
+};
+template <> struct KinAcc<float> {
+  float kh[2] = {0.f, 0.f}, kl[2] = {0.f, 0.f}, nh[2] = {0.f, 0.f}, nl[2] = {0.f, 0.f};
+  __device__ __forceinline__ void add(double, float hg, bool g0, float ux, float uy, float wx, float wy) {
+    const float a1 = fmaf(ux, ux, uy * uy), a2 = fmaf(wx, wx, wy * wy);
+    df_add(kh[0], kl[0], hg * a1, 0.f);
+    df_add(kh[1], kl[1], hg * a2, 0.f);
+    df_add(nh[0], nl[0], g0 ? ux * ux : 2.f * a1, 0.f);
+    df_add(nh[1], nl[1], g0 ? wx * wx : 2.f * a2, 0.f);
+  }
+  __device__ __forceinline__ void warp_totals(double (&o)[4]) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        df_add(kh[q], kl[q], __shfl_down_sync(0xffffffffu, kh[q], d), __shfl_down_sync(0xffffffffu, kl[q], d));
+        df_add(nh[q], nl[q], __shfl_down_sync(0xffffffffu, nh[q], d), __shfl_down_sync(0xffffffffu, nl[q], d));
+      }
+    }
+    o[0] = f2d_int(kh[0]) + f2d_int(kl[0]);
+    o[1] = f2d_int(nh[0]) + f2d_int(nl[0]);
+    o[2] = f2d_int(kh[1]) + f2d_int(kl[1]);
+    o[3] = f2d_int(nh[1]) + f2d_int(nl[1]);
+  }
+};
+
+// One +G entry (e > 0) of the gather: u, w the two states' coefficients as the
+// kernel holds them (FP64, or FP32-rounded).
+__device__ __forceinline__ void kin_entry(KinAcc<double>& acc, const GeoDev& g, int ig, double ux, double uy,
+                                          double wx, double wy) {
+  acc.add(g.hg[ig], 0.0, g.geq0 && ig == 0, ux, uy, wx, wy);
+}
+__device__ __forceinline__ void kin_entry(KinAcc<float>& acc, const GeoDev& g, int ig, float ux, float uy, float wx,
+                                          float wy) {
+  acc.add(0.0, g.hg32[ig], g.geq0 && ig == 0, ux, uy, wx, wy);
+}
+
+// CTA totals weighted by f1, f2 into out[0..1].  Every thread of the CTA calls it.
+template <typename T>
+__device__ __forceinline__ void kin_flush(KinAcc<T>& acc, double f1, double f2, double* __restrict__ out) {
+  __shared__ double wsum[kThreads / 32][4];
+  double o[4];
+  acc.warp_totals(o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) wsum[warp][q] = o[q];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) t[q] += wsum[w][q];
+    out[0] = f1 * t[0] + f2 * t[2];
+    out[1] = f1 * t[1] + f2 * t[3];
+  }
+}
+
 // ---------------------------------------------------------------- Z stage (inverse, gather)
 template <typename T, int NC>
 __global__ void __launch_bounds__(kThreads) k_zinv(GeoDev g, FftPlan p, const cx<double>* __restrict__ c0, int ldc,
                                                   int s0, int nstate, int nlrt, cx<T>* __restrict__ zbuf,
-                                                  const cx<T>* __restrict__ twg) {
+                                                  const cx<T>* __restrict__ twg, const double* __restrict__ f,
+                                                  double* __restrict__ kpart) {
   GBCP_STAGE(g.n3, nlrt)
   const int pair = blockIdx.y;
   const int col0 = blockIdx.x * nl;
@@ -87,6 +185,7 @@ __global__ void __launch_bounds__(kThreads) k_zinv(GeoDev g, FftPlan p, const cx
   const bool two = is2 < nstate;
   const cx<double>* c1 = c0 + (size_t)is1 * ldc;
   const cx<double>* c2 = c0 + (size_t)(two ? is2 : is1) * ldc;
+  KinAcc<T> kacc;
   load_tw(tw, twg, N);
   for (int idx = threadIdx.x; idx < nl * N; idx += kThreads) {
     const int l = idx / N, z = idx - l * N, col = col0 + l;
@@ -104,6 +203,7 @@ __global__ void __launch_bounds__(kThreads) k_zinv(GeoDev g, FftPlan p, const cx
           const T ux = from_double<T>(u.x), uy = from_double<T>(u.y);
           const T wx = from_double<T>(w.x), wy = from_double<T>(w.y);
           v = (e > 0) ? mk<T>(ux - wy, uy + wx) : mk<T>(ux + wy, wx - uy);
+          if (kpart && e > 0) kin_entry(kacc, g, ig, ux, uy, wx, wy);
         }
       }
     }
@@ -116,6 +216,9 @@ __global__ void __launch_bounds__(kThreads) k_zinv(GeoDev g, FftPlan p, const cx
     const int z = idx / nl, l = idx - z * nl, col = col0 + l;
     if (col < g.ncol) zb[(size_t)z * g.ncol + col] = r[l * ls + z];
   }
+  if (kpart)
+    kin_flush(kacc, f[is1], two ? f[is2] : 0.0,
+              kpart + 2 * ((size_t)(s0 / 2 + pair) * gridDim.x + blockIdx.x));
 }
 
 // ---------------------------------------------------------------- Y stage (inverse)
@@ -390,22 +493,31 @@ template <typename T, int N> constexpr size_t fs_smem_x(int tables) {
   return sizeof(cx<T>) * ((size_t)tables * N + (size_t)FS<T, N>::L * FS<T, N>::XS);
 }
 
+// Column blocks of the Z stage (the grid's x extent), for the size of the
+// per-CTA partials of rhoofr's scalars.
+template <typename T, int NC> int zinv_blocks_n(const Ctx& c) {
+  if constexpr (NC > 0) return (c.geo.ncol + FS<T, NC>::L - 1) / FS<T, NC>::L;
+  else return (c.geo.ncol + lines_rt(c.geo.n3) - 1) / lines_rt(c.geo.n3);
+}
+
+// kpart (may be null): per-CTA partials of E_kin and the norm (rhoofr only)
 template <typename T, int NC>
-int launch_zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int np, int poff) {
+int launch_zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int np, int poff, const double* f,
+                double* kpart) {
   const GeoDev& g = c.geo;
   cx<T>* zb = static_cast<cx<T>*>(c.zbuf.p) + (size_t)poff * g.n3 * g.ncol;  // pair poff of the launch batch
   ProfScope ps_(c, "k_zinv");
   if constexpr (NC > 0) {
     constexpr size_t sm = fs_smem<T, NC>(1, 1);
     allow_smem(k_zinv_fs<T, NC>, sm);
-    k_zinv_fs<T, NC><<<dim3((g.ncol + FS<T, NC>::L - 1) / FS<T, NC>::L, np), kThreads, sm, c.stream>>>(
-        g, c0, ldc, s0, nstate, zb, twA_of<T>(c, 2));
+    k_zinv_fs<T, NC><<<dim3(zinv_blocks_n<T, NC>(c), np), kThreads, sm, c.stream>>>(g, c0, ldc, s0, nstate, zb,
+                                                                                    twA_of<T>(c, 2), f, kpart);
   } else {
     const int nl = lines_rt(g.n3);
     const size_t sm = stage_smem<T>(g.n3, nl);
     allow_smem(k_zinv<T, 0>, sm);
-    k_zinv<T, 0><<<dim3((g.ncol + nl - 1) / nl, np), kThreads, sm, c.stream>>>(g, c.plan[2], c0, ldc, s0, nstate, nl,
-                                                                                zb, tw_of<T>(c, 2));
+    k_zinv<T, 0><<<dim3(zinv_blocks_n<T, 0>(c), np), kThreads, sm, c.stream>>>(g, c.plan[2], c0, ldc, s0, nstate, nl,
+                                                                               zb, tw_of<T>(c, 2), f, kpart);
   }
   GBCP_LAUNCH_CHECK(c);
   return 0;
@@ -576,9 +688,12 @@ int launch_decode(Ctx& c, int np, const cx<double>* c0, int ldc, cx<double>* c2,
   return 0;
 }
 
-template <typename T> int zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int np, int poff = 0) {
-  GBCP_DISPATCH(launch_zinv, T, band_len(c, c.nr[2]), c, c0, ldc, s0, nstate, np, poff)
+template <typename T>
+int zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int np, int poff = 0, const double* f = nullptr,
+         double* kpart = nullptr) {
+  GBCP_DISPATCH(launch_zinv, T, band_len(c, c.nr[2]), c, c0, ldc, s0, nstate, np, poff, f, kpart)
 }
+template <typename T> int zinv_blocks(const Ctx& c) { GBCP_DISPATCH(zinv_blocks_n, T, band_len(c, c.nr[2]), c) }
 template <typename T> int yinv(Ctx& c, int np, int poff = 0) {
   GBCP_DISPATCH(launch_yinv, T, band_len(c, c.nr[1]), c, np, poff)
 }
@@ -616,8 +731,9 @@ inline int launch_pairs(const Ctx& c, int p0, int npairs_total) {
   return std::min(c.batch, npairs_total - p0);
 }
 
+// kpart (may be null): E_kin / norm partials, 2 * npairs * zinv_blocks<T>(c) doubles
 template <typename T>
-int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho) {
+int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho, double* kpart) {
   const int npairs_total = (nstate + 1) / 2;
   int rc = ensure_band_buffers<T>(c, std::min(c.batch, npairs_total));
   if (rc) return rc;
@@ -625,7 +741,7 @@ int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f,
     np = std::min(c.batch, npairs_total - p0);
     const int s0 = 2 * p0;
     if (!c.batch_ready) {
-      if ((rc = zinv<T>(c, c0, ldc, s0, nstate, np))) return rc;
+      if ((rc = zinv<T>(c, c0, ldc, s0, nstate, np, 0, f, kpart))) return rc;
       if ((rc = yinv<T>(c, np))) return rc;
       if ((rc = xinv_rho<T>(c, np, s0, nstate, f, rho))) return rc;
     } else {
@@ -639,7 +755,7 @@ int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f,
         const int q0 = std::max(b[q], p0), q1 = std::min(b[q + 1], p0 + np);
         if (q1 > q0) {
           GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.batch_ready[q], 0));
-          if ((rc = zinv<T>(c, c0, ldc, 2 * q0, nstate, q1 - q0, q0 - p0))) return rc;
+          if ((rc = zinv<T>(c, c0, ldc, 2 * q0, nstate, q1 - q0, q0 - p0, f, kpart))) return rc;
           if ((rc = yinv<T>(c, q1 - q0, q0 - p0))) return rc;
         }
         const int gend = std::min(b[q + 1], p0 + np);

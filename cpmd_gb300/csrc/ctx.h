@@ -64,6 +64,8 @@ struct GeoDev {
   const int* pos_plus;   // ngw: entry position of +G
   const int* pos_minus;  // ngw: entry position of -G
   const double* hg;      // ngw
+  const float* hg32;     // ngw, hg rounded to FP32 (the FP32 kernels' kinetic sums)
+  int geq0;              // entry 0 is G = 0
 };
 
 // largest number of state pairs one band-loop launch covers
@@ -128,6 +130,7 @@ struct Ctx {
   Scratch zbuf, ybuf, qbuf;
   Scratch st_c0, st_c2, st_rho, st_vpot, st_f, st_misc, st_misc2, st_vf;
   Scratch red, red2;  // reductions
+  Scratch rho_sc;     // rhoofr's {E_kin, csumg, csumr} on the device
   Scratch smat, smat2, smat3, sparts, cscr, cdiag, cwork;
   Scratch xr_part, xr_tk;  // density x-stage: partial tiles and ticket counters of the pair chunks
   Scratch rt_mats;         // rortho: the n x n matrices of the constraint iteration
@@ -201,7 +204,10 @@ template <typename KernelT> inline void allow_smem(KernelT k, size_t bytes) {
 bool ensure(Ctx& c, Scratch& s, size_t bytes);
 
 // ---- band loop (band.cu) ----
-int band_rhoofr(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho);
+// scalars (device, may be null): {E_kin, csumg, csumr} of rhoofr (kin_energy_utils.mod.F90:93-108,
+// rhoofr_utils.mod.F90:607-635), queued on the stream without a host synchronisation
+int band_rhoofr(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho,
+                double* scalars = nullptr);
 int band_vpsi(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, const double* f, const double* vpot,
               int nstate);
 int dense_fft(Ctx& c, cx<double>* grid, bool inv);

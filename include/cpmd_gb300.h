@@ -43,7 +43,9 @@ enum gbcp_status {
   GBCP_ERR_NOMEM = 6,      /* device allocation failed */
   GBCP_ERR_UNSUPPORTED = 7,/* mesh size / option not supported */
   GBCP_ERR_NOT_CONVERGED = 8, /* iterative Loewdin step or rortog iteration did not converge */
-  GBCP_ERR_IO = 9          /* RESTART file cannot be opened, written, or is malformed */
+  GBCP_ERR_IO = 9,         /* RESTART file cannot be opened, written, or is malformed */
+  GBCP_ERR_CHARGE = 10     /* rhoofr: density sums in real and Fourier space differ
+                              (rhoofr_utils.mod.F90:625-635, where the reference stops) */
 };
 
 enum gbcp_precision {
@@ -127,7 +129,12 @@ int gbcp_profile_timeline(gbcp_ctx* ctx, int idx, char* name, int name_len, int*
  * rhoe(kr1,kr2,kr3) = sum_i f_i/omega psi_i(r)^2 (zero in the padding);
  * ekin = tpiba2 sum_i f_i sum_G hg |c|^2 (kin_energy_utils.mod.F90:93-108);
  * csumg = sum_i f_i <c_i|c_i>; csumr = sum_r rhoe * omega / (nr1 nr2 nr3)
- * (rhoofr_utils.mod.F90:607-635).  Scalar outputs may be NULL. */
+ * (rhoofr_utils.mod.F90:607-635).  Scalar outputs (host) may be NULL; when
+ * any is given the call synchronises once and applies the reference's charge
+ * check: |csumr - csumg| above 1e-6 (FP64) or 1e-6 csumg (mixed) returns
+ * GBCP_ERR_CHARGE with all outputs written.  In the mixed mode E_kin and csumg
+ * square the FP32-rounded coefficients (relative error 2^-24 per term,
+ * unbiased) and sum them in double-float. */
 int gbcp_rhoofr(gbcp_ctx* ctx, const double* c0, int ldc, int nstate, const double* f, double* rhoe,
                 double* ekin, double* csumg, double* csumr, int mem);
 

@@ -276,6 +276,38 @@ def fnonloc(c2, f, fnl, twnl, eigr, nghtol, wsg):
     return out
 
 
+def rnlsm1_factored(c0, twnl, eigr, nghtol, geq0):
+    """rnlsm1 for large cells: the same fnl with the G sum reordered as one
+    complex GEMM, fnl(ia, iv, i) = 2 Re[conj((-i)^l) sum_G conj(eigr(G, ia))
+    twnl(G, iv) c(G, i)], G = 0 halved (rnlsm1_utils.mod.F90:83-167).  The
+    loop form above builds scr(ngw, nat) per projector, which is memory-bound
+    at the 512-atom cell; both forms are checked against each other."""
+    ngw, n = c0.shape
+    nat = eigr.shape[1]
+    ngh = twnl.shape[1]
+    w = np.array(twnl, dtype=np.float64, copy=True)
+    if geq0:
+        w[0] *= 0.5
+    x = (w[:, :, None] * c0[:, None, :]).reshape(ngw, ngh * n)
+    y = (np.conj(eigr).T @ x).reshape(nat, ngh, n)
+    ph = np.array([np.conj(_ci(l)) for l in nghtol])
+    return 2.0 * (ph[None, :, None] * y).real
+
+
+def fnonloc_factored(c2, f, fnl, twnl, eigr, nghtol, wsg):
+    """fnonloc for large cells: the sum over atoms of every projector as one
+    complex GEMM, c2 += sum_iv twnl (-i)^l (-f wsg) (eigr fnl)(G, iv, i)
+    (fnonloc_utils.mod.F90:306-354, f < 1e-5 counted as 1)."""
+    ngw = c2.shape[0]
+    nat, ngh, n = fnl.shape
+    ffi = np.where(f < 1e-5, 1.0, f)
+    y = (eigr @ fnl.reshape(nat, ngh * n)).reshape(ngw, ngh, n)
+    ctm = np.array([_ci(l) for l in nghtol])[:, None] * (-ffi[None, :] * np.asarray(wsg)[:, None])   # (ngh, n)
+    out = np.array(c2, dtype=np.complex128, copy=True, order="F")
+    out += np.einsum("gv,gvi,vi->gi", twnl, y, ctm)
+    return out
+
+
 # ----------------------------------------------------------------------------
 # Energy functional E[psi, V_loc, R] and its adjoint
 # ----------------------------------------------------------------------------

@@ -298,7 +298,8 @@ def test_full_size_rhoofr_vpsi_consistency(gpu_lib, precision, tol):
     # the reference aborts above 1e-6 absolute (rhoofr_utils.mod.F90:625); the
     # FP32 FFT of the mixed mode holds the charge to 1e-7 relative instead
     assert abs(csumr - csumg) <= (1e-6 if precision == "fp64" else 1e-7 * csumg)
-    assert abs(csumg - 2.0 * cl.nstate) < 1e-8
+    # the mixed mode sums the norm of the FP32-rounded coefficients (the ones its band loop transforms)
+    assert abs(csumg - 2.0 * cl.nstate) < (1e-8 if precision == "fp64" else 1e-7 * csumg)
     c2 = torch.zeros_like(c0)
     ctx.vpsi(c0, c2, f, v)
     n1, n2, n3 = b.nr

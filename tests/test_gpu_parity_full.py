@@ -1,0 +1,264 @@
+"""Element-wise parity with the FP64 oracle at the benchmark sizes.
+
+The small-cell parity tests (test_gpu_parity.py) cover the edge cases; these
+compare the CUDA path with ``oracle/cpmd_oracle.py`` on the benchmark cells
+themselves, through the C ABI with device memory:
+
+* the 64-atom cell (120^3 mesh, 128 states, ngw 42 736): rho, E_kin, csumg,
+  csumr, C2 of vpsi, Gram-Schmidt and Loewdin ortho on both overlap engines;
+* the 216-atom cell (144^3, 50 Ry, ngw ~87k): energy terms, C2, dE/dV and
+  forces of the functional, on 48 states;
+* the 512-atom cell (240^3, 70 Ry, ngw 341 843): rho and C2 on 6 states, and
+  rnlsm1 / fnonloc with all 4096 projectors at the full ngw on 32 states;
+* the dense invfftn / fwfftn at 120^3, 144^3 and 240^3.
+
+FP64 drop-in: 1e-10 relative (max-norm of the difference over the max-norm of
+the oracle; 1e-12 for the dense FFTs).  Mixed mode, against the oracle:
+|dE| <= 1e-6 Ha/atom (E = E_kin + int V rho, or the functional), forces
+<= 1e-5 Ha/bohr, ||S - I|| <= 1e-12 after ortho, projector GEMMs within the
+FP32-class bound 2e-6 |A||B|.
+"""
+import numpy as np
+import pytest
+
+from cpmd_gb300.synth import make_cell, random_states, vloc_grid, atoms, projectors
+from oracle import cpmd_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-10
+
+
+def rel(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300))
+
+
+def dev(x):
+    import torch
+    if x.dtype == np.complex128 and x.ndim == 2:
+        return torch.from_numpy(np.ascontiguousarray(x.T)).cuda()
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def host_wfn(t):
+    return np.asfortranarray(t.cpu().numpy().T)
+
+
+def ctx_for(basis, precision="fp64", gemm=None):
+    from cpmd_gb300 import Context
+    ctx = Context(basis, precision=precision)
+    if gemm is not None:
+        ctx.set_option("gemm", gemm)
+    return ctx
+
+
+def perturbed(c0, scale, seed):
+    rng = np.random.default_rng(seed)
+    c = c0 + scale * (rng.standard_normal(c0.shape) + 1j * rng.standard_normal(c0.shape)) * np.abs(c0).max()
+    c[0] = c[0].real
+    return np.asfortranarray(c)
+
+
+# ====================================================================== 64 atoms, 120^3, 128 states
+@pytest.fixture(scope="module")
+def c1():
+    cl = make_cell("c1")
+    b = cl.basis
+    rho, ekin, csumg, csumr = O.rhoofr(cl.c0, cl.f, b.mill, b.nr, b.kr, b.omega, b.hg, b.tpiba2, b.geq0)
+    c2 = O.vpsi(cl.c0, np.zeros_like(cl.c0), cl.f, cl.vpot, b.mill, b.nr, b.hg, b.tpiba2, b.geq0)
+    dv = b.omega / float(np.prod(b.nr))
+    e = ekin + dv * float((rho * cl.vpot).sum())
+    return cl, dict(rho=rho, ekin=ekin, csumg=csumg, csumr=csumr, c2=c2, e=e)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_c1_rhoofr_vpsi_vs_oracle(gpu_lib, c1, precision):
+    import torch
+    cl, ref = c1
+    b = cl.basis
+    ctx = ctx_for(b, precision)
+    c0 = dev(cl.c0)
+    rho, ekin, csumg, csumr = ctx.rhoofr(c0, dev(cl.f))
+    c2 = torch.zeros_like(c0)
+    ctx.vpsi(c0, c2, dev(cl.f), dev(cl.vpot))
+    rho = rho.cpu().numpy()
+    c2 = host_wfn(c2)
+    if precision == "fp64":
+        assert rel(rho, ref["rho"]) < TOL64
+        assert rel(c2, ref["c2"]) < TOL64
+        for got, want in ((ekin, ref["ekin"]), (csumg, ref["csumg"]), (csumr, ref["csumr"])):
+            assert abs(got - want) <= TOL64 * abs(want)
+    else:
+        assert rel(rho, ref["rho"]) < 2e-5
+        assert rel(c2, ref["c2"]) < 2e-5
+        # E_kin of the FP32-rounded coefficients, summed in double-float
+        assert abs(ekin - ref["ekin"]) <= 1e-7 * abs(ref["ekin"])
+        dv = b.omega / float(np.prod(b.nr))
+        e = ekin + dv * float((rho * cl.vpot).sum())
+        assert abs(e - ref["e"]) / cl.tau.shape[0] <= 1e-6
+
+
+@pytest.mark.parametrize("precision,gemm", [("fp64", 0), ("fp64", 1), ("mixed", None)])
+@pytest.mark.parametrize("method", ["gs", "lowdin"])
+def test_c1_ortho_vs_oracle(gpu_lib, c1, precision, gemm, method):
+    import torch
+    cl, _ = c1
+    b = cl.basis
+    cp = perturbed(cl.c0, 0.02, seed=5)
+    if method == "gs":
+        ref = O.rgs(cp, b.geq0)
+    else:
+        ref, _ = O.lowdin(cp, b.geq0)
+    ctx = ctx_for(b, precision, gemm)
+    c = dev(cp)
+    ctx.ortho(c, method)
+    got = host_wfn(c)
+    assert rel(got, ref) < TOL64
+    assert np.all(got[0].imag == 0.0)  # zclean
+    s = ctx.ovlap(c)
+    assert float((s - torch.eye(cl.nstate, dtype=torch.float64, device=s.device)).abs().max()) < 1e-12
+
+
+def test_c1_charge_check_reports_unequal_sums(gpu_lib, c1):
+    """rhoofr applies the reference's charge check (rhoofr_utils.mod.F90:625-635):
+    an imaginary G = 0 coefficient, which the Γ norm ignores but the density does
+    not, makes csumr and csumg differ and the call returns GBCP_ERR_CHARGE with
+    the density still written."""
+    from cpmd_gb300 import GbcpError
+    cl, ref = c1
+    c = cl.c0.copy(order="F")
+    c[0, 3] += 0.3j
+    ctx = ctx_for(cl.basis)
+    rho = dev(np.zeros(tuple(cl.basis.kr[::-1])))
+    with pytest.raises(GbcpError) as e:
+        ctx.rhoofr(dev(c), dev(cl.f), rho)
+    assert e.value.code == 10
+    assert float(rho.abs().max()) > 0.0
+    # a clean call on the same context afterwards
+    _, _, csumg, csumr = ctx.rhoofr(dev(cl.c0), dev(cl.f))
+    assert abs(csumr - csumg) < 1e-6
+
+
+# ====================================================================== 216 atoms, 144^3, the functional
+@pytest.fixture(scope="module")
+def c2case():
+    cl = make_cell("c2", nstate=48)
+    b = cl.basis
+    vps = O.gaussian_vps(b.hg, b.tpiba2, b.omega)[:, None]
+    isp = np.zeros(len(cl.tau), dtype=np.int32)
+    ref = O.energy(cl.c0, cl.f, b, cl.tau, vps, isp)
+    return cl, vps, isp, ref
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_c2_energy_vs_oracle(gpu_lib, c2case, precision):
+    cl, vps, isp, ref = c2case
+    terms_ref, c2_ref, dv_ref, f_ref, _ = ref
+    ctx = ctx_for(cl.basis, precision)
+    terms, c2, dv, fion = ctx.energy(dev(cl.c0), dev(cl.f), dev(cl.tau), dev(np.ascontiguousarray(vps.T)), isp)
+    c2 = host_wfn(c2)
+    dv = dv.cpu().numpy()
+    fion = fion.cpu().numpy()
+    nat = cl.tau.shape[0]
+    if precision == "fp64":
+        for k in ("ekin", "eloc", "ehart", "exc", "etot"):
+            assert abs(terms[k] - terms_ref[k]) <= TOL64 * max(abs(terms_ref[k]), 1.0), k
+        assert rel(c2, c2_ref) < TOL64
+        assert rel(dv, dv_ref) < TOL64
+        assert rel(fion, f_ref) < TOL64
+    else:
+        assert abs(terms["etot"] - terms_ref["etot"]) / nat <= 1e-6
+        assert float(np.abs(fion - f_ref).max()) <= 1e-5
+        assert rel(c2, c2_ref) < 2e-5
+
+
+# ====================================================================== 512 atoms, 240^3
+@pytest.fixture(scope="module")
+def c4basis():
+    from cpmd_gb300.cell import make_basis
+    rng = np.random.default_rng(4)
+    tau, alat = atoms(10.26, 4, 0.05, rng)
+    return make_basis(alat, 240, 70.0), tau, rng
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_c4_band_loop_vs_oracle(gpu_lib, c4basis, precision):
+    import torch
+    b, tau, _ = c4basis
+    rng = np.random.default_rng(40)
+    c0 = random_states(b, 6, rng)
+    f = np.full(6, 2.0)
+    vpot = vloc_grid(b, tau[::64])                 # 8 of the 512 atoms: the potential's form does not matter here
+    rho_ref, ek_ref, _, _ = O.rhoofr(c0, f, b.mill, b.nr, b.kr, b.omega, b.hg, b.tpiba2, b.geq0)
+    c2_ref = O.vpsi(c0, np.zeros_like(c0), f, vpot, b.mill, b.nr, b.hg, b.tpiba2, b.geq0)
+    ctx = ctx_for(b, precision)
+    c = dev(c0)
+    rho, ekin, csumg, csumr = ctx.rhoofr(c, dev(f))
+    c2 = torch.zeros_like(c)
+    ctx.vpsi(c, c2, dev(f), dev(vpot))
+    tol = TOL64 if precision == "fp64" else 2e-5
+    assert rel(rho.cpu().numpy(), rho_ref) < tol
+    assert rel(host_wfn(c2), c2_ref) < tol
+    assert abs(ekin - ek_ref) <= (TOL64 if precision == "fp64" else 1e-7) * abs(ek_ref)
+
+
+@pytest.fixture(scope="module")
+def c4proj(c4basis):
+    b, tau, rng = c4basis
+    p = projectors(b, tau, rng)                    # 8 projectors x 512 atoms, eigr (ngw, 512)
+    c0 = random_states(b, 32, np.random.default_rng(41))
+    fnl_ref = O.rnlsm1_factored(c0, p["twnl"], p["eigr"], p["nghtol"], b.geq0)
+    return b, p, c0, fnl_ref
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_c4_projectors_full_ngw_vs_oracle(gpu_lib, c4proj, precision):
+    b, p, c0, fnl_ref = c4proj
+    assert b.ngw == 341843 and p["eigr"].shape[1] * p["twnl"].shape[1] == 4096
+    ctx = ctx_for(b, precision)
+    tw, eig = dev(np.ascontiguousarray(p["twnl"].T)), dev(p["eigr"])
+    fnl = ctx.rnlsm(dev(c0), tw, eig, p["nghtol"])                   # (n, ngh, nat)
+    fnl = np.transpose(fnl.cpu().numpy(), (2, 1, 0))
+    n = c0.shape[1]
+    f = np.full(n, 2.0)
+    f[3] = 0.0                                                       # counted as 1 by fnonloc
+    c2in = perturbed(c0, 0.5, seed=42)
+    ref = O.fnonloc_factored(c2in, f, fnl_ref, p["twnl"], p["eigr"], p["nghtol"], p["wsg"])
+    c2 = dev(c2in)
+    ctx.fnonloc(c2, dev(f), dev(np.ascontiguousarray(np.transpose(fnl_ref, (2, 1, 0)))), tw, eig, p["nghtol"],
+                dev(p["wsg"]))
+    got = host_wfn(c2)
+    if precision == "fp64":
+        assert rel(fnl, fnl_ref) < TOL64
+        assert rel(got - c2in, ref - c2in) < TOL64
+        return
+    # FP32-class bound of the split-bf16 tensor-core GEMMs, elementwise against
+    # the sum of absolute terms |A||B| (|eigr| = 1)
+    aw = np.abs(p["twnl"]).copy()
+    aw[0] *= 0.5
+    bf = 2.0 * (aw.T @ np.abs(c0))                                   # (ngh, n), every atom alike
+    ffi = np.where(f < 1e-5, 1.0, f)
+    z = (np.abs(fnl_ref) * (ffi[None, None, :] * np.abs(p["wsg"])[None, :, None])).sum(axis=0)   # (ngh, n)
+    bc = np.abs(p["twnl"]) @ z                                       # (ngw, n)
+    assert float((np.abs(fnl - fnl_ref) / bf[None, :, :]).max()) < 1e-5
+    assert float((np.abs(got - ref) / bc).max()) < 1e-5
+
+
+# ====================================================================== dense FFTs
+@pytest.mark.parametrize("nr", [120, 144, 240])
+def test_dense_fft_full_size(gpu_lib, nr):
+    from cpmd_gb300.cell import make_basis
+    b = make_basis(10.26 * nr / 30, nr, 8.0)
+    k1, k2, _ = b.kr
+    rng = np.random.default_rng(nr)
+    g = np.zeros((nr, k2, k1), complex)
+    g[:, :nr, :nr] = rng.standard_normal((nr, nr, nr)) + 1j * rng.standard_normal((nr, nr, nr))
+    import torch
+    ctx = ctx_for(b)
+    a = torch.from_numpy(g).cuda()
+    ctx.invfftn(a)
+    inv = a.cpu().numpy()
+    assert rel(inv[:, :nr, :nr], O.invfftn(g[:, :nr, :nr])) < 1e-12
+    ctx.fwfftn(a)
+    back = a.cpu().numpy()
+    assert rel(back[:, :nr, :nr], g[:, :nr, :nr]) < 1e-12

@@ -222,3 +222,22 @@ def test_golden_fixture_regression():
     assert np.abs(c2 - fx["c2"]).max() <= 1e-12 * np.abs(fx["c2"]).max()
     o = O.rgs(np.asfortranarray(fx["c_pert"]), b.geq0)
     assert np.abs(o - fx["c_gs"]).max() < 1e-11
+
+
+def test_factored_projector_forms_match_loop_forms():
+    """The GEMM-ordered rnlsm1 / fnonloc used at the 512-atom size against the
+    per-projector loop forms (same sums, reordered)."""
+    from cpmd_gb300.synth import make_small_cell
+    cl = make_small_cell(10.26, 32, 20.0, 9, seed=61, nat_rep=1, with_proj=True)
+    p = cl.proj
+    nghtol = np.array([0, 1, 2, 3, 0, 1, 2, 3], dtype=np.int32)
+    a = O.rnlsm1(cl.c0, p["twnl"], p["eigr"], nghtol, cl.basis.geq0)
+    b = O.rnlsm1_factored(cl.c0, p["twnl"], p["eigr"], nghtol, cl.basis.geq0)
+    assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max()
+    f = cl.f.copy()
+    f[2] = 0.0
+    rng = np.random.default_rng(5)
+    c2 = np.asfortranarray(rng.standard_normal(cl.c0.shape) + 1j * rng.standard_normal(cl.c0.shape))
+    x = O.fnonloc(c2, f, a, p["twnl"], p["eigr"], nghtol, p["wsg"])
+    y = O.fnonloc_factored(c2, f, a, p["twnl"], p["eigr"], nghtol, p["wsg"])
+    assert np.abs(x - y).max() <= 1e-13 * np.abs(x - c2).max()
