@@ -59,12 +59,14 @@ SIGNATURES = {
     "gbcp_profile_timeline": (_I, [_P, _I, C.c_char_p, _I, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "gbcp_rortog": (_I, [_P, _P, _I, _P, _I, _I, _I, _D, _I, _P, _P, _I]),
     "gbcp_ovlap_noalloc": (_I, [_P, _I, _I, _I, _I, _P, _P]),
+    "gbcp_ovlap2": (_I, [_P, _P, _I, _P, _I, _I, _P, _I]),
+    "gbcp_vofrho": (_I, [_P, _P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _I]),
     "gbcp_invfftn": (_I, [_P, _P, _I]),
     "gbcp_fwfftn": (_I, [_P, _P, _I]),
-    "gbcp_rnlsm1": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _I]),
-    "gbcp_fnonloc": (_I, [_P, _P, _I, _I, _P, _I, _I, _P, _P, _P, _P, _P, _I]),
-    "gbcp_rnlsm2": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _I]),
-    "gbcp_rnlfor": (_I, [_P, _I, _P, _I, _I, _P, _P, _P, _P, _I]),
+    "gbcp_rnlsm1": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _I, _I, _I]),
+    "gbcp_fnonloc": (_I, [_P, _P, _I, _I, _P, _I, _I, _P, _P, _P, _P, _I, _I, _P, _I]),
+    "gbcp_rnlsm2": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _I, _I, _I]),
+    "gbcp_rnlfor": (_I, [_P, _I, _P, _I, _I, _P, _P, _P, _I, _I, _P, _I]),
     "gbcp_set_dens_sphere": (_I, [_P, _I, _P, _P]),
     "gbcp_energy": (_I, [_P, _P, _I, _I, _P, _I, _I, _P, _P, _P, _P, _P, _P, _I, _P, _P, _I]),
     "gbcp_batch_create": (_I, [_I, _P, _I, _I, C.POINTER(_P)]),

@@ -141,7 +141,7 @@ class Context:
         """key 'gemm' (-1 by precision, 0 FP64 SIMT, 1 tensor cores), 'batch' (pairs per
         launch), 'fft' (0 four-step, 2 Stockham), 'xchunks' (density x-stage pair chunks,
         0 = automatic) or 'xc' (energy functional: 0 LDA-PZ, 1 PBE)."""
-        k = {"gemm": 1, "batch": 2, "fft": 3, "xchunks": 4, "xc": 5}[key]
+        k = {"gemm": 1, "batch": 2, "fft": 3, "xchunks": 4, "xc": 5, "test_timeout": 90}[key]
         self._check("gbcp_set_option", self.lib.gbcp_set_option(self.h, k, int(value)))
 
     def synchronize(self):
@@ -245,6 +245,24 @@ class Context:
         self._check("gbcp_ovlap", self.lib.gbcp_ovlap(self.h, _ptr(c0), ldc, n, _ptr(smat), self._prep(c0, smat)))
         return smat
 
+    def ovlap2(self, c1, c2, amat=None):
+        """a(i, j) = <c1_i|c2_j> in the Γ metric (the reference's ovlap with c1 != c2),
+        returned column-major like a(nstate, nstate): a torch tensor / numpy array whose
+        element [j, i] is a(i, j)."""
+        ld1, n = _ld_wfn(c1, self.ngw)
+        ld2, n2 = _ld_wfn(c2, self.ngw)
+        if n2 != n:
+            raise ValueError("c1 and c2 hold different numbers of states")
+        if amat is None:
+            if _is_torch(c1):
+                import torch
+                amat = torch.empty((n, n), dtype=torch.float64, device=c1.device)
+            else:
+                amat = np.empty((n, n))
+        self._check("gbcp_ovlap2", self.lib.gbcp_ovlap2(self.h, _ptr(c1), ld1, _ptr(c2), ld2, n, _ptr(amat),
+                                                        self._prep(c1, c2, amat)))
+        return amat
+
     def rortog(self, c0, cm, tnon: bool = False, epsog: float = 1e-6, maxit: int = 30):
         """CP-dynamics orthonormality constraint (rortog -> rortho): updates cm in place
         to cm + c0 gam and returns (gam, iterations); gam is symmetric (nstate x nstate)."""
@@ -272,8 +290,20 @@ class Context:
         self._check("gbcp_fwfftn", self.lib.gbcp_fwfftn(self.h, _ptr(grid), self._prep(grid)))
         return grid
 
-    def rnlsm(self, c0, twnl, eigr, nghtol, fnl=None):
-        """fnl (nstate, ngh, nat) == Fortran fnl(nat, ngh, nstate)."""
+    @staticmethod
+    def _fnl_block(arr, isa0):
+        """(pointer, ld_atoms, ld_proj) of a species block: the whole dense array when
+        isa0 is None, else the block at atom isa0 of a global array shaped like the
+        reference's fnl(nat_total, nhxs, nstate) -> (nstate, nhxs, nat_total) (dfnl:
+        (nstate, 3, nhxs, nat_total)), written or read in place."""
+        if isa0 is None:
+            return _ptr(arr), 0, 0
+        base = _ptr(arr)
+        return C.c_void_p(base.value + 8 * int(isa0)), int(arr.shape[-1]), int(arr.shape[-2])
+
+    def rnlsm(self, c0, twnl, eigr, nghtol, fnl=None, isa0=None):
+        """fnl (nstate, ngh, nat) == Fortran fnl(nat, ngh, nstate); with ``isa0`` the
+        species block of a global (nstate, nhxs, nat_total) array at atom isa0."""
         ldc, n = _ld_wfn(c0, self.ngw)
         ngh = int(len(nghtol))
         nat = int(eigr.shape[1] if not _is_torch(eigr) else eigr.shape[0])
@@ -285,12 +315,14 @@ class Context:
             else:
                 fnl = np.empty((n, ngh, nat))
         mem = self._prep(c0, twnl, eigr, fnl)
+        fp, la, lp = self._fnl_block(fnl, isa0)
         self._check("gbcp_rnlsm1", self.lib.gbcp_rnlsm1(self.h, _ptr(c0), ldc, n, nat, ngh, _ptr(nt), _ptr(twnl),
-                                                        _ptr(eigr), _ptr(fnl), mem))
+                                                        _ptr(eigr), fp, la, lp, mem))
         return fnl
 
-    def rnlsm2(self, c0, twnl, eigr, nghtol, dfnl=None):
-        """dfnl (nstate, 3, ngh, nat) == Fortran dfnl(nat, ngh, 3, nstate) = d fnl / d R."""
+    def rnlsm2(self, c0, twnl, eigr, nghtol, dfnl=None, isa0=None):
+        """dfnl (nstate, 3, ngh, nat) == Fortran dfnl(nat, ngh, 3, nstate) = d fnl / d R; with
+        ``isa0`` the species block of a global (nstate, 3, nhxs, nat_total) array."""
         ldc, n = _ld_wfn(c0, self.ngw)
         ngh = int(len(nghtol))
         nat = int(eigr.shape[1] if not _is_torch(eigr) else eigr.shape[0])
@@ -302,27 +334,35 @@ class Context:
             else:
                 dfnl = np.empty((n, 3, ngh, nat))
         mem = self._prep(c0, twnl, eigr, dfnl)
+        fp, la, lp = self._fnl_block(dfnl, isa0)
         self._check("gbcp_rnlsm2", self.lib.gbcp_rnlsm2(self.h, _ptr(c0), ldc, n, nat, ngh, _ptr(nt), _ptr(twnl),
-                                                        _ptr(eigr), _ptr(dfnl), mem))
+                                                        _ptr(eigr), fp, la, lp, mem))
         return dfnl
 
-    def rnlfor(self, f, fnl, dfnl, wsg, fion):
-        """fion (nat, 3) == Fortran fion(3, nat) -= the non-local forces (accumulated)."""
+    def rnlfor(self, f, fnl, dfnl, wsg, fion, nat=None, ngh=None, isa0=None):
+        """fion (nat, 3) == Fortran fion(3, nat) -= the non-local forces (accumulated).  With
+        ``isa0``, fnl / dfnl are the global arrays and nat, ngh the species block's sizes."""
         n = int(f.shape[0])
-        nat, ngh = int(fnl.shape[2]), int(fnl.shape[1])
+        if isa0 is None:
+            nat, ngh = int(fnl.shape[2]), int(fnl.shape[1])
         mem = self._prep(f, fnl, dfnl, wsg, fion)
-        self._check("gbcp_rnlfor", self.lib.gbcp_rnlfor(self.h, n, _ptr(f), nat, ngh, _ptr(wsg), _ptr(fnl),
-                                                        _ptr(dfnl), _ptr(fion), mem))
+        fp, la, lp = self._fnl_block(fnl, isa0)
+        dp, _, _ = self._fnl_block(dfnl, isa0)
+        self._check("gbcp_rnlfor", self.lib.gbcp_rnlfor(self.h, n, _ptr(f), nat, ngh, _ptr(wsg), fp, dp, la, lp,
+                                                        _ptr(fion), mem))
         return fion
 
-    def fnonloc(self, c2, f, fnl, twnl, eigr, nghtol, wsg):
+    def fnonloc(self, c2, f, fnl, twnl, eigr, nghtol, wsg, isa0=None):
+        """c2 += the non-local term of one species; fnl dense (nstate, ngh, nat) or, with
+        ``isa0``, the global (nstate, nhxs, nat_total) array read at atom isa0."""
         ld2, n = _ld_wfn(c2, self.ngw)
         ngh = int(len(nghtol))
         nat = int(eigr.shape[1] if not _is_torch(eigr) else eigr.shape[0])
         nt = np.ascontiguousarray(np.asarray(nghtol, dtype=np.int32))
         mem = self._prep(c2, f, fnl, twnl, eigr, wsg)
+        fp, la, lp = self._fnl_block(fnl, isa0)
         self._check("gbcp_fnonloc", self.lib.gbcp_fnonloc(self.h, _ptr(c2), ld2, n, _ptr(f), nat, ngh, _ptr(nt),
-                                                          _ptr(twnl), _ptr(eigr), _ptr(fnl), _ptr(wsg), mem))
+                                                          _ptr(twnl), _ptr(eigr), fp, la, lp, _ptr(wsg), mem))
         return c2
 
 
@@ -337,6 +377,49 @@ class Context:
                     self.lib.gbcp_set_dens_sphere(self.h, int(b.nhg), inyh.ctypes.data_as(C.c_void_p),
                                                   hg.ctypes.data_as(C.c_void_p)))
         self._dens_set = True
+
+    def _species_args(self, tau, vps, isp, dev):
+        nhg = int(self.basis.nhg)
+        nat = 0 if tau is None else int(tau.shape[0])
+        if nat:
+            if isp is None:
+                isp = np.zeros(nat, dtype=np.int32)
+            isp = np.ascontiguousarray(np.asarray(isp, dtype=np.int32))
+            nsp = int(isp.max()) + 1
+            if dev:
+                if vps.dim() == 1:
+                    vps = vps.reshape(1, nhg)
+                if tuple(vps.shape) != (nsp, nhg):
+                    raise ValueError("vps must be (nsp, nhg) on the device")
+            else:
+                vps = np.asarray(vps, dtype=np.float64).reshape(nhg, -1, order="F")
+                if vps.shape[1] != nsp:
+                    raise ValueError("vps must be (nhg, nsp)")
+                vps = np.asfortranarray(vps)
+                tau = np.ascontiguousarray(tau, dtype=np.float64)
+            return nat, nsp, isp, vps, tau
+        return 0, 1, None, None, None
+
+    def vofrho(self, rhoe, tau=None, vps=None, isp=None, vext=None, forces: bool = True):
+        """Density -> potential (vofrho): returns (veff, terms, fion) with veff on the
+        padded mesh, terms = {eloc, ehart, exc, eext} and the local-potential forces
+        (nat, 3) (None without atoms or with forces=False).  Arguments as in energy()."""
+        self._ensure_dens_sphere()
+        dev = _is_torch(rhoe)
+        nat, nsp, isp, vps, tau = self._species_args(tau, vps, isp, dev)
+        if dev:
+            import torch
+            veff = torch.empty(self.kr[::-1], dtype=torch.float64, device=rhoe.device)
+            fion = torch.empty((nat, 3), dtype=torch.float64, device=rhoe.device) if (forces and nat) else None
+        else:
+            veff = np.empty(self.kr[::-1])
+            fion = np.empty((nat, 3)) if (forces and nat) else None
+        mem = self._prep(rhoe, tau, vps, vext, veff, fion)
+        e = (C.c_double * 4)()
+        isp_p = isp.ctypes.data_as(C.c_void_p) if isp is not None else None
+        self._check("gbcp_vofrho", self.lib.gbcp_vofrho(self.h, _ptr(rhoe), nat, nsp, isp_p, _ptr(tau), _ptr(vps),
+                                                        _ptr(vext), _ptr(veff), e, _ptr(fion), mem))
+        return veff, dict(eloc=e[0], ehart=e[1], exc=e[2], eext=e[3]), fion
 
     def energy(self, c0, f, tau=None, vps=None, isp=None, vext=None, grad: bool = True, forces: bool = True):
         """E[psi, V, R] = E_kin + E_loc + E_H + E_xc (+ E_ext) and its adjoint.

@@ -443,6 +443,10 @@ int gbcp_set_option(gbcp_ctx* h, int key, int value) {
     c.xc = value;
     return GBCP_OK;
   }
+  if (key == GBCP_OPT_TEST_TIMEOUT && (value == 0 || value == 1)) {
+    c.test_stall = value;
+    return GBCP_OK;
+  }
   return set_err(h, GBCP_ERR_ARG, "set_option: unknown key or value");
 }
 
@@ -916,13 +920,25 @@ static int fft_entry(gbcp_ctx* h, double* f, int mem, bool inv) {
 int gbcp_invfftn(gbcp_ctx* h, double* f, int mem) { return fft_entry(h, f, mem, true); }
 int gbcp_fwfftn(gbcp_ctx* h, double* f, int mem) { return fft_entry(h, f, mem, false); }
 
+// Elements of the caller's fnl (kdim 1) or dfnl (kdim 3) a species block spans from
+// its base: fnl(ia, iv, i) at ia + lda (iv + ldp i), dfnl(ia, iv, k, i) at
+// ia + lda (iv + ldp (k + 3 i)); lda = 0 / ldp = 0 stand for nat / ngh.
+static size_t fnl_span(int nat, int ngh, int nstate, int& lda, int& ldp, int kdim) {
+  lda = lda > 0 ? lda : nat;
+  ldp = ldp > 0 ? ldp : ngh;
+  if (lda < nat || ldp < ngh) return 0;
+  return (size_t)(nat - 1) + (size_t)lda * ((size_t)(ngh - 1) + (size_t)ldp * ((size_t)kdim * nstate - 1)) + 1;
+}
+
 int gbcp_rnlsm1(gbcp_ctx* h, const double* c0, int ldc, int nstate, int nat, int ngh, const int32_t* nghtol,
-                const double* twnl, const double* eigr, double* fnl, int mem) {
+                const double* twnl, const double* eigr, double* fnl, int ld_atoms, int ld_proj, int mem) {
   if (!h) return GBCP_ERR_ARG;
   Ctx& c = h->c;
   if (bad_mem(mem) || nstate <= 0 || nat <= 0 || ngh <= 0 || !c0 || !nghtol || !twnl || !eigr || !fnl ||
       ldc < c.ngw)
     return set_err(h, GBCP_ERR_ARG, "rnlsm1: bad argument");
+  const size_t nfnl = fnl_span(nat, ngh, nstate, ld_atoms, ld_proj, 1);
+  if (!nfnl) return set_err(h, GBCP_ERR_ARG, "rnlsm1: fnl leading dimensions below nat / ngh");
   c.err.clear();
   const cx<double>* dc0 = reinterpret_cast<const cx<double>*>(c0);
   const double* dtw = twnl;
@@ -930,22 +946,21 @@ int gbcp_rnlsm1(gbcp_ctx* h, const double* c0, int ldc, int nstate, int nat, int
   double* dfnl = fnl;
   int l0 = ldc;
   int rc = 0;
-  const size_t nfnl = (size_t)nat * ngh * nstate;
   if (mem == GBCP_MEM_HOST) {
     cx<double>* t0;
-    void* t1;
-    void* t2;
+    void *t1, *t2, *t3;
     if ((rc = stage_in_cx(c, c.st_c0, c0, ldc, c.ngw, nstate, &t0))) return rc;
     if ((rc = stage_in(c, c.nl_b, twnl, sizeof(double) * (size_t)c.ngw * ngh, &t1))) return rc;
     if ((rc = stage_in(c, c.nl_c, eigr, sizeof(cx<double>) * (size_t)c.ngw * nat, &t2))) return rc;
-    if (!gbcp::ensure(c, c.nl_d, sizeof(double) * nfnl)) return GBCP_ERR_NOMEM;
+    // the span holds other species' entries too: staged in and out whole, so they come back unchanged
+    if ((rc = stage_in(c, c.nl_d, fnl, sizeof(double) * nfnl, &t3))) return rc;
     dc0 = t0;
     dtw = static_cast<double*>(t1);
     de = static_cast<cx<double>*>(t2);
-    dfnl = static_cast<double*>(c.nl_d.p);
+    dfnl = static_cast<double*>(t3);
     l0 = c.ngw;
   }
-  rc = gbcp::nl_rnlsm1(c, dc0, l0, nstate, nat, ngh, nghtol, dtw, de, dfnl);
+  rc = gbcp::nl_rnlsm1(c, dc0, l0, nstate, nat, ngh, nghtol, dtw, de, dfnl, ld_atoms, ld_proj);
   if (!rc && mem == GBCP_MEM_HOST) {
     cudaError_t e = cudaMemcpyAsync(fnl, dfnl, sizeof(double) * nfnl, cudaMemcpyDeviceToHost, c.stream);
     if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));
@@ -955,12 +970,14 @@ int gbcp_rnlsm1(gbcp_ctx* h, const double* c0, int ldc, int nstate, int nat, int
 }
 
 int gbcp_rnlsm2(gbcp_ctx* h, const double* c0, int ldc, int nstate, int nat, int ngh, const int32_t* nghtol,
-                const double* twnl, const double* eigr, double* dfnl, int mem) {
+                const double* twnl, const double* eigr, double* dfnl, int ld_atoms, int ld_proj, int mem) {
   if (!h) return GBCP_ERR_ARG;
   Ctx& c = h->c;
   if (bad_mem(mem) || nstate <= 0 || nat <= 0 || ngh <= 0 || !c0 || !nghtol || !twnl || !eigr || !dfnl ||
       ldc < c.ngw)
     return set_err(h, GBCP_ERR_ARG, "rnlsm2: bad argument");
+  const size_t nd = fnl_span(nat, ngh, nstate, ld_atoms, ld_proj, 3);
+  if (!nd) return set_err(h, GBCP_ERR_ARG, "rnlsm2: dfnl leading dimensions below nat / ngh");
   c.err.clear();
   const cx<double>* dc0 = reinterpret_cast<const cx<double>*>(c0);
   const double* dtw = twnl;
@@ -968,21 +985,20 @@ int gbcp_rnlsm2(gbcp_ctx* h, const double* c0, int ldc, int nstate, int nat, int
   double* dd = dfnl;
   int l0 = ldc;
   int rc = 0;
-  const size_t nd = (size_t)nat * ngh * 3 * nstate;
   if (mem == GBCP_MEM_HOST) {
     cx<double>* t0;
-    void *t1, *t2;
+    void *t1, *t2, *t3;
     if ((rc = stage_in_cx(c, c.st_c0, c0, ldc, c.ngw, nstate, &t0))) return rc;
     if ((rc = stage_in(c, c.nl_b, twnl, sizeof(double) * (size_t)c.ngw * ngh, &t1))) return rc;
     if ((rc = stage_in(c, c.nl_c, eigr, sizeof(cx<double>) * (size_t)c.ngw * nat, &t2))) return rc;
-    if (!gbcp::ensure(c, c.nl_d, sizeof(double) * nd)) return GBCP_ERR_NOMEM;
+    if ((rc = stage_in(c, c.nl_d, dfnl, sizeof(double) * nd, &t3))) return rc;
     dc0 = t0;
     dtw = static_cast<double*>(t1);
     de = static_cast<cx<double>*>(t2);
-    dd = static_cast<double*>(c.nl_d.p);
+    dd = static_cast<double*>(t3);
     l0 = c.ngw;
   }
-  rc = gbcp::nl_rnlsm2(c, dc0, l0, nstate, nat, ngh, nghtol, dtw, de, dd);
+  rc = gbcp::nl_rnlsm2(c, dc0, l0, nstate, nat, ngh, nghtol, dtw, de, dd, ld_atoms, ld_proj);
   if (!rc && mem == GBCP_MEM_HOST) {
     cudaError_t e = cudaMemcpyAsync(dfnl, dd, sizeof(double) * nd, cudaMemcpyDeviceToHost, c.stream);
     if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));
@@ -992,22 +1008,24 @@ int gbcp_rnlsm2(gbcp_ctx* h, const double* c0, int ldc, int nstate, int nat, int
 }
 
 int gbcp_rnlfor(gbcp_ctx* h, int nstate, const double* f, int nat, int ngh, const double* wsg, const double* fnl,
-                const double* dfnl, double* fion, int mem) {
+                const double* dfnl, int ld_atoms, int ld_proj, double* fion, int mem) {
   if (!h) return GBCP_ERR_ARG;
   Ctx& c = h->c;
   if (bad_mem(mem) || nstate <= 0 || nat <= 0 || ngh <= 0 || !f || !wsg || !fnl || !dfnl || !fion)
     return set_err(h, GBCP_ERR_ARG, "rnlfor: bad argument");
+  const size_t nf = fnl_span(nat, ngh, nstate, ld_atoms, ld_proj, 1);
+  const size_t nd = fnl_span(nat, ngh, nstate, ld_atoms, ld_proj, 3);
+  if (!nf || !nd) return set_err(h, GBCP_ERR_ARG, "rnlfor: fnl leading dimensions below nat / ngh");
   c.err.clear();
   const double *df = f, *dw = wsg, *dfn = fnl, *ddf = dfnl;
   double* dfi = fion;
   int rc = 0;
-  const size_t P = (size_t)nat * ngh;
   if (mem == GBCP_MEM_HOST) {
     void *t1, *t2, *t3, *t4, *t5;
     if ((rc = stage_in(c, c.st_f, f, sizeof(double) * nstate, &t1))) return rc;
     if ((rc = stage_in(c, c.st_misc, wsg, sizeof(double) * ngh, &t2))) return rc;
-    if ((rc = stage_in(c, c.nl_b, fnl, sizeof(double) * P * nstate, &t3))) return rc;
-    if ((rc = stage_in(c, c.nl_d, dfnl, sizeof(double) * P * 3 * nstate, &t4))) return rc;
+    if ((rc = stage_in(c, c.nl_b, fnl, sizeof(double) * nf, &t3))) return rc;
+    if ((rc = stage_in(c, c.nl_d, dfnl, sizeof(double) * nd, &t4))) return rc;
     if ((rc = stage_in(c, c.st_misc2, fion, sizeof(double) * 3 * nat, &t5))) return rc;
     df = static_cast<double*>(t1);
     dw = static_cast<double*>(t2);
@@ -1015,7 +1033,7 @@ int gbcp_rnlfor(gbcp_ctx* h, int nstate, const double* f, int nat, int ngh, cons
     ddf = static_cast<double*>(t4);
     dfi = static_cast<double*>(t5);
   }
-  rc = gbcp::nl_rnlfor(c, nstate, df, nat, ngh, dw, dfn, ddf, dfi);
+  rc = gbcp::nl_rnlfor(c, nstate, df, nat, ngh, dw, dfn, ddf, dfi, ld_atoms, ld_proj);
   if (!rc && mem == GBCP_MEM_HOST) {
     cudaError_t e = cudaMemcpyAsync(fion, dfi, sizeof(double) * 3 * nat, cudaMemcpyDeviceToHost, c.stream);
     if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));
@@ -1025,13 +1043,15 @@ int gbcp_rnlfor(gbcp_ctx* h, int nstate, const double* f, int nat, int ngh, cons
 }
 
 int gbcp_fnonloc(gbcp_ctx* h, double* c2, int ldc2, int nstate, const double* f, int nat, int ngh,
-                 const int32_t* nghtol, const double* twnl, const double* eigr, const double* fnl, const double* wsg,
-                 int mem) {
+                 const int32_t* nghtol, const double* twnl, const double* eigr, const double* fnl, int ld_atoms,
+                 int ld_proj, const double* wsg, int mem) {
   if (!h) return GBCP_ERR_ARG;
   Ctx& c = h->c;
   if (bad_mem(mem) || nstate <= 0 || nat <= 0 || ngh <= 0 || !c2 || !f || !nghtol || !twnl || !eigr || !fnl ||
       !wsg || ldc2 < c.ngw)
     return set_err(h, GBCP_ERR_ARG, "fnonloc: bad argument");
+  const size_t nf = fnl_span(nat, ngh, nstate, ld_atoms, ld_proj, 1);
+  if (!nf) return set_err(h, GBCP_ERR_ARG, "fnonloc: fnl leading dimensions below nat / ngh");
   c.err.clear();
   cx<double>* dc2 = reinterpret_cast<cx<double>*>(c2);
   const double* df = f;
@@ -1047,7 +1067,7 @@ int gbcp_fnonloc(gbcp_ctx* h, double* c2, int ldc2, int nstate, const double* f,
     if ((rc = stage_in(c, c.st_f, f, sizeof(double) * nstate, &t1))) return rc;
     if ((rc = stage_in(c, c.nl_b, twnl, sizeof(double) * (size_t)c.ngw * ngh, &t2))) return rc;
     if ((rc = stage_in(c, c.nl_c, eigr, sizeof(cx<double>) * (size_t)c.ngw * nat, &t3))) return rc;
-    if ((rc = stage_in(c, c.nl_d, fnl, sizeof(double) * (size_t)nat * ngh * nstate, &t4))) return rc;
+    if ((rc = stage_in(c, c.nl_d, fnl, sizeof(double) * nf, &t4))) return rc;
     if ((rc = stage_in(c, c.st_misc, wsg, sizeof(double) * ngh, &t5))) return rc;
     df = static_cast<double*>(t1);
     dtw = static_cast<double*>(t2);
@@ -1056,7 +1076,7 @@ int gbcp_fnonloc(gbcp_ctx* h, double* c2, int ldc2, int nstate, const double* f,
     dw = static_cast<double*>(t5);
     l2 = c.ngw;
   }
-  rc = gbcp::nl_fnonloc(c, dc2, l2, nstate, df, nat, ngh, nghtol, dtw, de, dfnl, dw);
+  rc = gbcp::nl_fnonloc(c, dc2, l2, nstate, df, nat, ngh, nghtol, dtw, de, dfnl, dw, ld_atoms, ld_proj);
   if (!rc && mem == GBCP_MEM_HOST) rc = stage_out_cx(c, dc2, c2, ldc2, c.ngw, nstate);
   if (mem == GBCP_MEM_HOST || rc) return finish(c, rc);
   return GBCP_OK;
@@ -1099,6 +1119,105 @@ int gbcp_set_dens_sphere(gbcp_ctx* h, int nhg, const int32_t* inyh, const double
   c.dg2 = dg;
   c.dmax = dmax;
   c.nhg = nhg;
+  return GBCP_OK;
+}
+
+int gbcp_vofrho(gbcp_ctx* h, const double* rhoe, int nat, int nsp, const int32_t* isp, const double* tau,
+                const double* vps, const double* vext, double* veff, double* energies, double* fion, int mem) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  if (bad_mem(mem) || nat < 0 || nsp <= 0 || !rhoe || !veff || !energies || (nat > 0 && (!isp || !tau || !vps)))
+    return set_err(h, GBCP_ERR_ARG, "vofrho: bad argument");
+  if (c.nhg <= 0) return set_err(h, GBCP_ERR_ARG, "vofrho: call gbcp_set_dens_sphere first");
+  c.err.clear();
+  const size_t nnr1 = (size_t)c.kr[0] * c.kr[1] * c.kr[2];
+  const double *drho = rhoe, *dtau = tau, *dvps = vps, *dvext = vext;
+  double *dve = veff, *dfi = fion;
+  int rc = 0;
+  static const double zero3[3] = {0.0, 0.0, 0.0};
+  static const int32_t zero_sp[1] = {0};
+  const int nat_eff = nat > 0 ? nat : 1;  // no atoms: one atom of zero form factor
+  const int32_t* isp_h = nat > 0 ? isp : zero_sp;
+  if (mem == GBCP_MEM_HOST) {
+    void *tr, *tt, *tv, *te;
+    if ((rc = stage_in(c, c.en_in[2], rhoe, sizeof(double) * nnr1, &tr))) return rc;
+    if ((rc = stage_in(c, c.en_in[0], nat > 0 ? tau : zero3, sizeof(double) * 3 * nat_eff, &tt))) return rc;
+    drho = static_cast<double*>(tr);
+    dtau = static_cast<double*>(tt);
+    if (nat > 0) {
+      if ((rc = stage_in(c, c.en_in[1], vps, sizeof(double) * (size_t)c.nhg * nsp, &tv))) return rc;
+      dvps = static_cast<double*>(tv);
+    }
+    if (vext) {
+      if ((rc = stage_in(c, c.en_in[3], vext, sizeof(double) * nnr1, &te))) return rc;
+      dvext = static_cast<double*>(te);
+    }
+    if (!gbcp::ensure(c, c.st_vpot, sizeof(double) * nnr1)) return GBCP_ERR_NOMEM;
+    dve = static_cast<double*>(c.st_vpot.p);
+    if (fion) {
+      if (!gbcp::ensure(c, c.en_in[4], sizeof(double) * 3 * nat_eff)) return GBCP_ERR_NOMEM;
+      dfi = static_cast<double*>(c.en_in[4].p);
+    }
+  }
+  if (nat == 0) {
+    if (mem == GBCP_MEM_DEVICE) {
+      if (!gbcp::ensure(c, c.en_in[0], sizeof(double) * 3)) return GBCP_ERR_NOMEM;
+      GBCP_CUDA_TRY(c, cudaMemsetAsync(c.en_in[0].p, 0, sizeof(double) * 3, c.stream));
+      dtau = static_cast<double*>(c.en_in[0].p);
+    }
+    if (!gbcp::ensure(c, c.en_in[1], sizeof(double) * (size_t)c.nhg)) return GBCP_ERR_NOMEM;
+    GBCP_CUDA_TRY(c, cudaMemsetAsync(c.en_in[1].p, 0, sizeof(double) * (size_t)c.nhg, c.stream));
+    dvps = static_cast<double*>(c.en_in[1].p);
+    nsp = 1;
+  }
+  double* fion_dev = (fion && nat > 0) ? dfi : nullptr;
+  rc = gbcp::vofrho_host_energies(c, nat_eff, nsp, isp_h, drho, dtau, dvps, dvext, dve, energies, fion_dev);
+  if (!rc && mem == GBCP_MEM_HOST) {
+    GBCP_CUDA_TRY(c, cudaMemcpyAsync(veff, dve, sizeof(double) * nnr1, cudaMemcpyDeviceToHost, c.stream));
+    if (fion && nat > 0)
+      GBCP_CUDA_TRY(c, cudaMemcpyAsync(fion, dfi, sizeof(double) * 3 * nat, cudaMemcpyDeviceToHost, c.stream));
+  }
+  return finish(c, rc);
+}
+
+int gbcp_ovlap2(gbcp_ctx* h, const double* c1, int ldc1, const double* c2, int ldc2, int nstate, double* amat,
+                int mem) {
+  if (!h) return GBCP_ERR_ARG;
+  Ctx& c = h->c;
+  if (bad_mem(mem) || nstate <= 0 || !c1 || !c2 || !amat || ldc1 < c.ngw || ldc2 < c.ngw)
+    return set_err(h, GBCP_ERR_ARG, "ovlap2: bad argument");
+  c.err.clear();
+  const cx<double>* d1 = reinterpret_cast<const cx<double>*>(c1);
+  const cx<double>* d2 = reinterpret_cast<const cx<double>*>(c2);
+  int l1 = ldc1, l2 = ldc2;
+  double* dA = amat;
+  int rc = 0;
+  if (mem == GBCP_MEM_HOST) {
+    cx<double>*t1, *t2;
+    if ((rc = stage_in_cx(c, c.st_c0, c1, ldc1, c.ngw, nstate, &t1))) return rc;
+    if ((rc = stage_in_cx(c, c.st_c2, c2, ldc2, c.ngw, nstate, &t2))) return rc;
+    d1 = t1;
+    d2 = t2;
+    l1 = l2 = c.ngw;
+    if (!gbcp::ensure(c, c.st_misc, sizeof(double) * (size_t)nstate * nstate)) return GBCP_ERR_NOMEM;
+    dA = static_cast<double*>(c.st_misc.p);
+  }
+  GBCP_CUDA_TRY(c, cudaMemsetAsync(c.d_info, 0, 16, c.stream));
+  // xovlap writes row-major A[i][j] = <X_i|Y_j>; with X = c2, Y = c1 that is the
+  // column-major a(i, j) = <c1_i|c2_j> of the reference
+  rc = gbcp::xovlap(c, d2, l2, d1, l1, nstate, dA);
+  if (!rc && gbcp::use_tc_gemm(c)) {
+    int st = 0;
+    GBCP_CUDA_TRY(c, cudaMemcpyAsync(&st, c.d_info, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+    if (st == -2) rc = set_err(h, GBCP_ERR_TIMEOUT, "ovlap2: tensor-core pipeline wait expired");
+  }
+  if (!rc && mem == GBCP_MEM_HOST) {
+    cudaError_t e =
+        cudaMemcpyAsync(amat, dA, sizeof(double) * (size_t)nstate * nstate, cudaMemcpyDeviceToHost, c.stream);
+    if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (mem == GBCP_MEM_HOST || rc) return finish(c, rc);
   return GBCP_OK;
 }
 

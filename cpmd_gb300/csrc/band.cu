@@ -1,5 +1,6 @@
 // Band-loop dispatch (precision) plus the dense 3D FFT (invfftn/fwfftn) and
-// the FP64 reductions of rhoofr (kinetic energy, charge sums).
+// the FP64 folds of rhoofr's scalars (kinetic energy and norm partials of the
+// Z-stage gather, the density sum).
 //
 // The pruned band-loop kernels themselves live in band_impl.cuh, instantiated
 // once per precision in band64.cu and band32.cu.
@@ -86,78 +87,6 @@ __global__ void __launch_bounds__(kThreads) k_axis_fft(cx<double>* __restrict__ 
 
 // ---------------------------------------------------------------- reductions
 // Per-block partial sums, then one block folds them (deterministic order).
-__global__ void k_kin_partial(const cx<double>* __restrict__ c0, int ldc, int ngw, int nstate,
-                              const double* __restrict__ f, const double* __restrict__ hg, int geq0,
-                              double* __restrict__ part) {
-  // grid.x = blocks over G, grid.y = state
-  const int i = blockIdx.y;
-  double sk = 0.0, sn = 0.0;
-  const double fi = f[i];
-  if (fi != 0.0) {
-    for (int ig = blockIdx.x * blockDim.x + threadIdx.x; ig < ngw; ig += gridDim.x * blockDim.x) {
-      const cx<double> c = c0[(size_t)i * ldc + ig];
-      const double a2 = c.x * c.x + c.y * c.y;
-      sk += hg[ig] * a2;
-      sn += (geq0 && ig == 0) ? c.x * c.x : 2.0 * a2;  // dotp_utils.mod.F90:45-52
-    }
-  }
-  __shared__ double rk[kThreads], rn[kThreads];
-  rk[threadIdx.x] = fi * sk;
-  rn[threadIdx.x] = fi * sn;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      rk[threadIdx.x] += rk[threadIdx.x + s];
-      rn[threadIdx.x] += rn[threadIdx.x + s];
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    const int b = blockIdx.y * gridDim.x + blockIdx.x;
-    part[2 * b] = rk[0];
-    part[2 * b + 1] = rn[0];
-  }
-}
-
-__global__ void k_fold2(const double* __restrict__ part, int n, double* __restrict__ out) {
-  __shared__ double r0[kThreads], r1[kThreads];
-  double a = 0.0, b = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    a += part[2 * i];
-    b += part[2 * i + 1];
-  }
-  r0[threadIdx.x] = a;
-  r1[threadIdx.x] = b;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      r0[threadIdx.x] += r0[threadIdx.x + s];
-      r1[threadIdx.x] += r1[threadIdx.x + s];
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    out[0] = r0[0];
-    out[1] = r1[0];
-  }
-}
-
-__global__ void k_sum_partial(const double* __restrict__ x, size_t n, double* __restrict__ part) {
-  double a = 0.0;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) a += x[i];
-  __shared__ double r[kThreads];
-  r[threadIdx.x] = a;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) r[threadIdx.x] += r[threadIdx.x + s];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    part[2 * blockIdx.x] = r[0];
-    part[2 * blockIdx.x + 1] = 0.0;
-  }
-}
-
 // dot-product partials of two real arrays
 __global__ void k_dot_partial(const double* __restrict__ x, const double* __restrict__ y, size_t n,
                               double* __restrict__ part) {
@@ -191,59 +120,62 @@ __global__ void k_fold_scaled(const double* __restrict__ part, int n, double sca
   if (threadIdx.x == 0) *out = scale * r[0];
 }
 
-// First fold level of rhoofr's scalars: CTA b sums the 2-component partials
-// [b*chunk, (b+1)*chunk) in index order into out[2b], out[2b+1].
-__global__ void k_fold2_ranges(const double* __restrict__ part, int n, int chunk, double* __restrict__ out) {
-  __shared__ double r0[kThreads], r1[kThreads];
-  const int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
-  double a = 0.0, b = 0.0;
-  for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-    a += part[2 * i];
-    b += part[2 * i + 1];
-  }
-  r0[threadIdx.x] = a;
-  r1[threadIdx.x] = b;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      r0[threadIdx.x] += r0[threadIdx.x + s];
-      r1[threadIdx.x] += r1[threadIdx.x + s];
+// rhoofr's scalars in one launch.  CTA b adds, in index order, the kinetic and
+// norm partials [b kc, (b+1) kc) of the Z stage and the density elements
+// [b rc, (b+1) rc), writes its three totals, and the last CTA to finish (ticket
+// counter) adds the CTA totals in CTA order and writes out = {tpiba2 sum kin,
+// sum norm, rscale sum rho}; the result does not depend on the scheduling.
+__global__ void __launch_bounds__(kThreads) k_rho_scalars(const double* __restrict__ kp, int nk, int kc,
+                                                         const double* __restrict__ rho, long long nr, long long rc,
+                                                         double* __restrict__ part, unsigned* __restrict__ ticket,
+                                                         double tpiba2, double rscale, double* __restrict__ out) {
+  __shared__ double red[3][kThreads / 32];
+  __shared__ bool last;
+  double v[3] = {0.0, 0.0, 0.0};
+  {
+    const int lo = blockIdx.x * kc, hi = min(nk, lo + kc);
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+      v[0] += kp[2 * (size_t)i];
+      v[1] += kp[2 * (size_t)i + 1];
     }
-    __syncthreads();
+    const long long rlo = blockIdx.x * rc, rhi = min(nr, rlo + rc);
+    for (long long i = rlo + threadIdx.x; i < rhi; i += blockDim.x) v[2] += rho[i];
   }
-  if (threadIdx.x == 0) {
-    out[2 * blockIdx.x] = r0[0];
-    out[2 * blockIdx.x + 1] = r1[0];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    for (int d = 16; d > 0; d >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], d);
+    if (lane == 0) red[q][warp] = v[q];
   }
-}
-
-// Last level: out = {tpiba2 * sum kin, sum norm, rscale * sum rho} from nk
-// 2-component kinetic/norm partials and nr density partials (k_sum_partial).
-__global__ void k_rho_scalars(const double* __restrict__ kp, int nk, const double* __restrict__ rp, int nr,
-                              double tpiba2, double rscale, double* __restrict__ out) {
-  __shared__ double r0[kThreads], r1[kThreads], r2[kThreads];
-  double a = 0.0, b = 0.0, d = 0.0;
-  for (int i = threadIdx.x; i < nk; i += blockDim.x) {
-    a += kp[2 * i];
-    b += kp[2 * i + 1];
-  }
-  for (int i = threadIdx.x; i < nr; i += blockDim.x) d += rp[2 * i];
-  r0[threadIdx.x] = a;
-  r1[threadIdx.x] = b;
-  r2[threadIdx.x] = d;
   __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      r0[threadIdx.x] += r0[threadIdx.x + s];
-      r1[threadIdx.x] += r1[threadIdx.x + s];
-      r2[threadIdx.x] += r2[threadIdx.x + s];
-    }
-    __syncthreads();
-  }
   if (threadIdx.x == 0) {
-    out[0] = tpiba2 * r0[0];
-    out[1] = r1[0];
-    out[2] = rscale * r2[0];
+    double t[3] = {0.0, 0.0, 0.0};
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+      for (int q = 0; q < 3; ++q) t[q] += red[q][w];
+    for (int q = 0; q < 3; ++q) part[3 * (size_t)blockIdx.x + q] = t[q];
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double w[3] = {0.0, 0.0, 0.0};
+  for (int bI = threadIdx.x; bI < (int)gridDim.x; bI += blockDim.x)
+    for (int q = 0; q < 3; ++q) w[q] += part[3 * (size_t)bI + q];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    for (int d = 16; d > 0; d >>= 1) w[q] += __shfl_down_sync(0xffffffffu, w[q], d);
+    if (lane == 0) red[q][warp] = w[q];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t[3] = {0.0, 0.0, 0.0};
+    for (int ww = 0; ww < (int)(blockDim.x >> 5); ++ww)
+      for (int q = 0; q < 3; ++q) t[q] += red[q][ww];
+    out[0] = tpiba2 * t[0];
+    out[1] = t[1];
+    out[2] = rscale * t[2];
+    *ticket = 0u;  // ready for the next call
   }
 }
 
@@ -264,44 +196,32 @@ int band_rhoofr(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double*
     return 0;
   }
   // partials of E_kin / norm: one pair of doubles per Z-stage CTA of every pair,
-  // then one per first-level fold CTA, then the density sum's partials
+  // then three per CTA of the fold
   const int npairs = (nstate + 1) / 2;
   const int nkb = npairs * (c.precision == 0 ? band_zinv_blocks_fp64(c) : band_zinv_blocks_fp32(c));
-  const int kchunk = 4096, nk1 = (nkb + kchunk - 1) / kchunk, nrp = 296;
+  const int nfold = std::max(1, std::min(2 * (c.nsm > 0 ? c.nsm : 152), (int)((nnr + 4095) / 4096)));
   double* kpart = nullptr;
   if (scalars) {
-    if (!ensure(c, c.red, sizeof(double) * 2 * ((size_t)nkb + nk1 + nrp))) return 6;
+    if (!ensure(c, c.red, sizeof(double) * (2 * (size_t)nkb + 3 * (size_t)nfold))) return 6;
     kpart = static_cast<double*>(c.red.p);
+    if (!c.rho_tk.p) {
+      if (!ensure(c, c.rho_tk, sizeof(unsigned))) return 6;
+      GBCP_CUDA_TRY(c, cudaMemsetAsync(c.rho_tk.p, 0, sizeof(unsigned), c.stream));
+    }
   }
   const int rc = c.precision == 0 ? band_rhoofr_fp64(c, c0, ldc, nstate, f, rho, kpart)
                                   : band_rhoofr_fp32(c, c0, ldc, nstate, f, rho, kpart);
   if (rc || !scalars) return rc;
-  double* k1 = kpart + 2 * (size_t)nkb;
-  double* rp = k1 + 2 * (size_t)nk1;
-  {
-    ProfScope ps_(c, "k_fold2_ranges");
-    k_fold2_ranges<<<nk1, kThreads, 0, c.stream>>>(kpart, nkb, kchunk, k1);
-    GBCP_LAUNCH_CHECK(c);
-  }
-  {
-    ProfScope ps_(c, "k_sum_partial");
-    k_sum_partial<<<nrp, kThreads, 0, c.stream>>>(rho, nnr, rp);
-    GBCP_LAUNCH_CHECK(c);
-  }
   {
     ProfScope ps_(c, "k_rho_scalars");
-    k_rho_scalars<<<1, kThreads, 0, c.stream>>>(k1, nk1, rp, nrp, c.tpiba2,
-                                                c.omega / ((double)c.nr[0] * c.nr[1] * c.nr[2]), scalars);
+    const int kc = (nkb + nfold - 1) / nfold;
+    const long long rcnt = ((long long)nnr + nfold - 1) / nfold;
+    k_rho_scalars<<<nfold, kThreads, 0, c.stream>>>(kpart, nkb, kc, rho, (long long)nnr, rcnt, kpart + 2 * (size_t)nkb,
+                                                    static_cast<unsigned*>(c.rho_tk.p), c.tpiba2,
+                                                    c.omega / ((double)c.nr[0] * c.nr[1] * c.nr[2]), scalars);
     GBCP_LAUNCH_CHECK(c);
   }
   return 0;
-}
-
-int band_vpsi(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, const double* f, const double* vpot,
-              int nstate) {
-  if (nstate <= 0) return 0;
-  return c.precision == 0 ? band_vpsi_fp64(c, c0, ldc, c2, ldc2, f, vpot, nstate)
-                          : band_vpsi_fp32(c, c0, ldc, c2, ldc2, f, vpot, nstate);
 }
 
 int dense_fft(Ctx& c, cx<double>* grid, bool inv) {
@@ -334,51 +254,6 @@ int dense_fft(Ctx& c, cx<double>* grid, bool inv) {
   return 0;
 }
 
-int kin_energy(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* ekin, double* csumg) {
-  const int gx = std::max(1, std::min(64, (c.ngw + kThreads - 1) / kThreads));
-  const int nb = gx * nstate;
-  if (!ensure(c, c.red, sizeof(double) * (2 * (size_t)nb + 2))) return 6;
-  double* part = static_cast<double*>(c.red.p);
-  {
-    ProfScope ps_(c, "k_kin_partial");
-    k_kin_partial<<<dim3(gx, nstate), kThreads, 0, c.stream>>>(c0, ldc, c.ngw, nstate, f, c.geo.hg, c.geq0, part);
-    GBCP_LAUNCH_CHECK(c);
-  }
-  {
-    ProfScope ps_(c, "k_fold2");
-    k_fold2<<<1, kThreads, 0, c.stream>>>(part, nb, part + 2 * nb);
-    GBCP_LAUNCH_CHECK(c);
-  }
-  double h[2];
-  GBCP_CUDA_TRY(c, cudaMemcpyAsync(h, part + 2 * nb, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
-  GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
-  if (ekin) *ekin = h[0] * c.tpiba2;
-  if (csumg) *csumg = h[1];
-  if (!std::isfinite(h[0]) || !std::isfinite(h[1])) {
-    c.err = "non-finite kinetic energy / norm";
-    return 3;
-  }
-  return 0;
-}
-
-int kin_energy_async(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* dev_out) {
-  const int gx = std::max(1, std::min(64, (c.ngw + kThreads - 1) / kThreads));
-  const int nb = gx * nstate;
-  if (!ensure(c, c.red, sizeof(double) * (2 * (size_t)nb + 2))) return 6;
-  double* part = static_cast<double*>(c.red.p);
-  {
-    ProfScope ps_(c, "k_kin_partial");
-    k_kin_partial<<<dim3(gx, nstate), kThreads, 0, c.stream>>>(c0, ldc, c.ngw, nstate, f, c.geo.hg, c.geq0, part);
-    GBCP_LAUNCH_CHECK(c);
-  }
-  {
-    ProfScope ps_(c, "k_fold_scaled");
-    k_fold_scaled<<<1, kThreads, 0, c.stream>>>(part, nb, c.tpiba2, dev_out);
-    GBCP_LAUNCH_CHECK(c);
-  }
-  return 0;
-}
-
 int vrho_async(Ctx& c, const double* rho, const double* vpot, double* dev_out) {
   const size_t n = (size_t)c.kr[0] * c.kr[1] * c.kr[2];
   const int nb = 296;
@@ -393,32 +268,6 @@ int vrho_async(Ctx& c, const double* rho, const double* vpot, double* dev_out) {
     ProfScope ps_(c, "k_fold_scaled");
     k_fold_scaled<<<1, kThreads, 0, c.stream>>>(part, nb, c.omega / ((double)c.nr[0] * c.nr[1] * c.nr[2]), dev_out);
     GBCP_LAUNCH_CHECK(c);
-  }
-  return 0;
-}
-
-int rho_sum(Ctx& c, const double* rho, double* sum) {
-  const size_t n = (size_t)c.kr[0] * c.kr[1] * c.kr[2];
-  const int nb = 296;
-  if (!ensure(c, c.red, sizeof(double) * (2 * (size_t)nb + 2))) return 6;
-  double* part = static_cast<double*>(c.red.p);
-  {
-    ProfScope ps_(c, "k_sum_partial");
-    k_sum_partial<<<nb, kThreads, 0, c.stream>>>(rho, n, part);
-    GBCP_LAUNCH_CHECK(c);
-  }
-  {
-    ProfScope ps_(c, "k_fold2");
-    k_fold2<<<1, kThreads, 0, c.stream>>>(part, nb, part + 2 * nb);
-    GBCP_LAUNCH_CHECK(c);
-  }
-  double h[2];
-  GBCP_CUDA_TRY(c, cudaMemcpyAsync(h, part + 2 * nb, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
-  GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
-  *sum = h[0];
-  if (!std::isfinite(h[0])) {
-    c.err = "non-finite density";
-    return 3;
   }
   return 0;
 }

@@ -84,9 +84,11 @@ __device__ __forceinline__ cx<T>* run_fft(cx<T>* a, cx<T>* b, int nl, int ls, co
 // no second read of c0.  Each CTA writes its two occupation-weighted totals to
 // kpart[2 b], kpart[2 b + 1], b = global pair * (column blocks) + column block.
 // FP64 kernels sum in FP64.  FP32 kernels square the FP32-rounded coefficients
-// (relative rounding 2^-24 per coefficient, unbiased) and accumulate in
-// double-float (Knuth's TwoSum), so no summation error builds up and the FP64
-// pipe, 1/58 of the FP32 rate on GB300, is used only once per warp.
+// (relative rounding 2^-24 per coefficient, unbiased), add a thread's few terms
+// (at most N1 per line it owns) in FP32 and combine the threads of a warp in
+// double-float (Knuth's TwoSum), so the summation error stays far below the
+// coefficient rounding and the FP64 pipe, 1/58 of the FP32 rate on GB300, is
+// used once per warp.
 __device__ __forceinline__ void df_add(float& hi, float& lo, float bh, float bl) {
   const float s = hi + bh;
   const float v = s - hi;
@@ -116,27 +118,23 @@ template <> struct KinAcc<double> {
   }
 };
 template <> struct KinAcc<float> {
-  float kh[2] = {0.f, 0.f}, kl[2] = {0.f, 0.f}, nh[2] = {0.f, 0.f}, nl[2] = {0.f, 0.f};
+  float k1 = 0.f, n1 = 0.f, k2 = 0.f, n2 = 0.f;
   __device__ __forceinline__ void add(double, float hg, bool g0, float ux, float uy, float wx, float wy) {
     const float a1 = fmaf(ux, ux, uy * uy), a2 = fmaf(wx, wx, wy * wy);
-    df_add(kh[0], kl[0], hg * a1, 0.f);
-    df_add(kh[1], kl[1], hg * a2, 0.f);
-    df_add(nh[0], nl[0], g0 ? ux * ux : 2.f * a1, 0.f);
-    df_add(nh[1], nl[1], g0 ? wx * wx : 2.f * a2, 0.f);
+    k1 = fmaf(hg, a1, k1);
+    k2 = fmaf(hg, a2, k2);
+    n1 += g0 ? ux * ux : 2.f * a1;
+    n2 += g0 ? wx * wx : 2.f * a2;
   }
   __device__ __forceinline__ void warp_totals(double (&o)[4]) {
+    float h[4] = {k1, n1, k2, n2}, l[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
+    for (int d = 16; d > 0; d >>= 1)
 #pragma unroll
-      for (int q = 0; q < 2; ++q) {
-        df_add(kh[q], kl[q], __shfl_down_sync(0xffffffffu, kh[q], d), __shfl_down_sync(0xffffffffu, kl[q], d));
-        df_add(nh[q], nl[q], __shfl_down_sync(0xffffffffu, nh[q], d), __shfl_down_sync(0xffffffffu, nl[q], d));
-      }
-    }
-    o[0] = f2d_int(kh[0]) + f2d_int(kl[0]);
-    o[1] = f2d_int(nh[0]) + f2d_int(nl[0]);
-    o[2] = f2d_int(kh[1]) + f2d_int(kl[1]);
-    o[3] = f2d_int(nh[1]) + f2d_int(nl[1]);
+      for (int q = 0; q < 4; ++q)
+        df_add(h[q], l[q], __shfl_down_sync(0xffffffffu, h[q], d), __shfl_down_sync(0xffffffffu, l[q], d));
+#pragma unroll
+    for (int q = 0; q < 4; ++q) o[q] = f2d_int(h[q]) + f2d_int(l[q]);
   }
 };
 

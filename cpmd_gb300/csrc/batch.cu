@@ -73,8 +73,11 @@ int queue_cell(Ctx& c, const gbcp_cell_io& io, int flags, double* dout, int* dst
   cx<double>* c0 = reinterpret_cast<cx<double>*>(io.c0);
   int rc = 0;
   if (flags & GBCP_STEP_RHOOFR) {
-    if ((rc = gbcp::band_rhoofr(c, c0, io.ldc, io.nstate, io.f, io.rhoe))) return rc;
-    if ((rc = gbcp::kin_energy_async(c, c0, io.ldc, io.nstate, io.f, dout))) return rc;
+    // E_kin summed in the band loop's gather, as in gbcp_rhoofr (the scalars stay on the device)
+    if (!gbcp::ensure(c, c.rho_sc, 4 * sizeof(double))) return 6;
+    double* sc = static_cast<double*>(c.rho_sc.p);
+    if ((rc = gbcp::band_rhoofr(c, c0, io.ldc, io.nstate, io.f, io.rhoe, sc))) return rc;
+    GBCP_CUDA_TRY(c, cudaMemcpyAsync(dout, sc, sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
     if ((rc = gbcp::vrho_async(c, io.rhoe, io.vpot, dout + 1))) return rc;
   }
   if (flags & GBCP_STEP_VPSI) {

@@ -110,6 +110,7 @@ struct Ctx {
   int xr_chunks = 0;   // density x-stage pair chunks: 0 = chosen per launch
   int xc = 0;          // energy functional: 0 LDA (Slater + Perdew-Zunger), 1 PBE
   int fft_engine = 0;  // band-loop FFTs: 0 four-step where a plan exists, else Stockham; 2 Stockham always
+  int test_stall = 0;  // test hook: the next tensor-core overlap issues no loads and times out (one call)
   cudaStream_t stream = nullptr;  // stream all work is queued on
   cudaStream_t own = nullptr;     // the context's own stream
   // geometry
@@ -131,6 +132,7 @@ struct Ctx {
   Scratch st_c0, st_c2, st_rho, st_vpot, st_f, st_misc, st_misc2, st_vf;
   Scratch red, red2;  // reductions
   Scratch rho_sc;     // rhoofr's {E_kin, csumg, csumr} on the device
+  Scratch rho_tk;     // ticket counter of the last-CTA fold of those scalars
   Scratch smat, smat2, smat3, sparts, cscr, cdiag, cwork;
   Scratch xr_part, xr_tk;  // density x-stage: partial tiles and ticket counters of the pair chunks
   Scratch rt_mats;         // rortho: the n x n matrices of the constraint iteration
@@ -211,12 +213,9 @@ int band_rhoofr(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double*
 int band_vpsi(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, const double* f, const double* vpot,
               int nstate);
 int dense_fft(Ctx& c, cx<double>* grid, bool inv);
-int kin_energy(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* ekin, double* csumg);
 // capture-safe reductions (no host synchronisation), result in device memory:
-// kin_energy_async -> dev_out[0] = E_kin; vrho_async -> dev_out[0] = Omega/N sum_r V rho
-int kin_energy_async(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* dev_out);
+// vrho_async -> dev_out[0] = Omega/N sum_r V rho
 int vrho_async(Ctx& c, const double* rho, const double* vpot, double* dev_out);
-int rho_sum(Ctx& c, const double* rho, double* sum);
 
 // ---- linear algebra (linalg.cu) ----
 int ovlap_gamma(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S);
@@ -266,20 +265,26 @@ int ortho_gs_queue(Ctx& c, cx<double>* c0, int ldc, int nstate);
 int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host);
 
 // ---- energy functional and its adjoint (energy.cu) ----
+// density -> potential (vofrho): V_eff (padded layout, device), energies4 (host) = {E_loc, E_H,
+// E_xc, E_ext}, the local-potential forces fion (device, may be null, overwritten)
+int vofrho_host_energies(Ctx& c, int nat, int nsp, const int* isp_host, const double* rho, const double* tau,
+                         const double* vps, const double* vext, double* veff, double* energies4, double* fion);
 int energy_and_grad(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, int nat, int nsp,
                     const int* isp_host, const double* tau, const double* vps, const double* vext,
                     double* energies_host, cx<double>* c2, int ldc2, double* dvloc, double* fion);
 
 // ---- projectors (nonlocal.cu) ----
+// fnl(ia, iv, i) at ia + lda (iv + ldp i), dfnl(ia, iv, k, i) at ia + lda (iv + ldp (k + 3 i));
+// lda = 0 / ldp = 0 mean nat / ngh (a dense species block)
 int nl_rnlsm1(Ctx& c, const cx<double>* c0, int ldc, int nstate, int nat, int ngh, const int* nghtol_host,
-              const double* twnl, const cx<double>* eigr, double* fnl);
+              const double* twnl, const cx<double>* eigr, double* fnl, int lda = 0, int ldp = 0);
 int nl_rnlsm2(Ctx& c, const cx<double>* c0, int ldc, int nstate, int nat, int ngh, const int* nghtol_host,
-              const double* twnl, const cx<double>* eigr, double* dfnl);
+              const double* twnl, const cx<double>* eigr, double* dfnl, int lda = 0, int ldp = 0);
 int nl_rnlfor(Ctx& c, int nstate, const double* f, int nat, int ngh, const double* wsg, const double* fnl,
-              const double* dfnl, double* fion);
+              const double* dfnl, double* fion, int lda = 0, int ldp = 0);
 int nl_fnonloc(Ctx& c, cx<double>* c2, int ldc2, int nstate, const double* f, int nat, int ngh,
                const int* nghtol_host, const double* twnl, const cx<double>* eigr, const double* fnl,
-               const double* wsg);
+               const double* wsg, int lda = 0, int ldp = 0);
 
 }  // namespace gbcp
 

@@ -407,9 +407,13 @@ __global__ void __launch_bounds__(kET) k_fold_pairs(const double* __restrict__ p
 
 }  // namespace
 
-int energy_and_grad(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, int nat, int nsp,
-                    const int* isp_host, const double* tau, const double* vps, const double* vext,
-                    double* energies_host, cx<double>* c2, int ldc2, double* dvloc, double* fion) {
+// Density -> potential (the reference's vofrho: vofrhoa_utils.mod.F90:41-144 with the
+// vofrhob xc step): from rho(r) (padded layout, device) to V_eff(r) = V_ion + V_H + v_xc
+// (+ vext), dE/dV = rho Omega / N (dvloc, may be null), the local-potential forces
+// (fion, may be null) and the energy partial sums, left on the device in sums[0..3]
+// = {E_loc / Omega, E_H / Omega, sum eps_xc rho, sum vext rho} (no host synchronisation).
+int vofrho(Ctx& c, const double* rho, int nat, int nsp, const int* isp_host, const double* tau, const double* vps,
+           const double* vext, double* veff, double* dvloc, double* fion, double** sums_out) {
   if (c.nhg <= 0) {
     c.err = "energy: no density sphere (gbcp_set_dens_sphere)";
     return 1;
@@ -450,13 +454,6 @@ int energy_and_grad(Ctx& c, const cx<double>* c0, int ldc, int nstate, const dou
   const int* d_jsp = d_idx + nat;
   const int* d_spstart = d_idx + 2 * nat;
 
-  // density and kinetic energy (band loop in the context precision)
-  if (!ensure(c, c.en_rho, sizeof(double) * nnr1)) return 6;
-  double* rho = static_cast<double*>(c.en_rho.p);
-  if ((rc = band_rhoofr(c, c0, ldc, nstate, f, rho))) return rc;
-  double ekin = 0.0;
-  if ((rc = kin_energy(c, c0, ldc, nstate, f, &ekin, nullptr))) return rc;
-
   // rho(G)
   if (!ensure(c, c.en_a, sizeof(cx<double>) * ngrid) || !ensure(c, c.en_b, sizeof(cx<double>) * ngrid)) return 6;
   cx<double>* ga = static_cast<cx<double>*>(c.en_a.p);
@@ -470,9 +467,9 @@ int energy_and_grad(Ctx& c, const cx<double>* c0, int ldc, int nstate, const dou
 
   // structure-factor tables
   const int w = 2 * c.dmax + 1;
-  if (!ensure(c, c.en_ei, sizeof(cx<double>) * (size_t)nat * 3 * w)) return 6;
+  if (!ensure(c, c.en_ei, sizeof(cx<double>) * (size_t)std::max(nat, 1) * 3 * w)) return 6;
   cx<double>* ei = static_cast<cx<double>*>(c.en_ei.p);
-  {
+  if (nat > 0) {
     ProfScope ps_(c, "k_ei_table");
     const size_t tot = (size_t)nat * 3 * w;
     k_ei_table<<<std::max<size_t>(1, std::min<size_t>(1024, (tot + kET - 1) / kET)), kET, 0, c.stream>>>(
@@ -497,8 +494,6 @@ int energy_and_grad(Ctx& c, const cx<double>* c0, int ldc, int nstate, const dou
   if ((rc = dense_fft(c, gb, true))) return rc;
 
   // xc, V_eff, dE/dV
-  if (!ensure(c, c.en_veff, sizeof(double) * nnr1)) return 6;
-  double* veff = static_cast<double*>(c.en_veff.p);
   const int nb_n = std::max(1, (int)std::min<size_t>(4096, (ngrid + kET - 1) / kET));
   if (c.xc == 1) {
     // PBE: grad rho by three inverse FFTs of i G rho(G); the per-point functional writes
@@ -545,7 +540,7 @@ int energy_and_grad(Ctx& c, const cx<double>* c0, int ldc, int nstate, const dou
   }
 
   // forces
-  if (fion) {
+  if (fion && nat > 0) {
     const int ntile = (nat + kAT - 1) / kAT;
     const int nchunk = std::max(1, std::min((c.nhg + kET - 1) / kET, (4 * 152 + ntile - 1) / ntile));
     if (!ensure(c, c.en_fp, sizeof(double) * (size_t)nchunk * 3 * nat)) return 6;
@@ -558,6 +553,56 @@ int energy_and_grad(Ctx& c, const cx<double>* c0, int ldc, int nstate, const dou
                                                                 fion);
     GBCP_LAUNCH_CHECK(c);
   }
+  *sums_out = sums;
+  return 0;
+}
+
+// host read of the four partial sums of vofrho: {E_loc, E_H, E_xc, E_ext} in Ha
+static int vofrho_energies(Ctx& c, const double* sums, const double* dscal, double* e4, double* ekin) {
+  double h[8];
+  GBCP_CUDA_TRY(c, cudaMemcpyAsync(h, sums, 4 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  if (dscal) GBCP_CUDA_TRY(c, cudaMemcpyAsync(h + 4, dscal, 3 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  const double nmesh = (double)c.nr[0] * c.nr[1] * c.nr[2];
+  e4[0] = c.omega * h[0];
+  e4[1] = c.omega * h[1];
+  e4[2] = c.omega / nmesh * h[2];
+  e4[3] = c.omega / nmesh * h[3];
+  if (ekin) *ekin = h[4];
+  for (int k = 0; k < 4; ++k)
+    if (!std::isfinite(e4[k])) {
+      c.err = "energy: non-finite result";
+      return 3;
+    }
+  if (ekin && !std::isfinite(*ekin)) {
+    c.err = "energy: non-finite kinetic energy";
+    return 3;
+  }
+  return 0;
+}
+
+int vofrho_host_energies(Ctx& c, int nat, int nsp, const int* isp_host, const double* rho, const double* tau,
+                         const double* vps, const double* vext, double* veff, double* energies4, double* fion) {
+  double* sums = nullptr;
+  int rc = vofrho(c, rho, nat, nsp, isp_host, tau, vps, vext, veff, nullptr, fion, &sums);
+  if (rc) return rc;
+  return vofrho_energies(c, sums, nullptr, energies4, nullptr);
+}
+
+int energy_and_grad(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, int nat, int nsp,
+                    const int* isp_host, const double* tau, const double* vps, const double* vext,
+                    double* energies_host, cx<double>* c2, int ldc2, double* dvloc, double* fion) {
+  const size_t nnr1 = (size_t)c.kr[0] * c.kr[1] * c.kr[2];
+  int rc;
+  // density and E_kin (band loop in the context precision; E_kin summed in its gather)
+  if (!ensure(c, c.en_rho, sizeof(double) * nnr1) || !ensure(c, c.rho_sc, 4 * sizeof(double))) return 6;
+  double* rho = static_cast<double*>(c.en_rho.p);
+  double* dscal = static_cast<double*>(c.rho_sc.p);
+  if ((rc = band_rhoofr(c, c0, ldc, nstate, f, rho, dscal))) return rc;
+  if (!ensure(c, c.en_veff, sizeof(double) * nnr1)) return 6;
+  double* veff = static_cast<double*>(c.en_veff.p);
+  double* sums = nullptr;
+  if ((rc = vofrho(c, rho, nat, nsp, isp_host, tau, vps, vext, veff, dvloc, fion, &sums))) return rc;
 
   // C2 = vpsi(c0, 0, f, V_eff)
   if (c2) {
@@ -566,22 +611,11 @@ int energy_and_grad(Ctx& c, const cx<double>* c0, int ldc, int nstate, const dou
     if ((rc = band_vpsi(c, c0, ldc, c2, ldc2, f, veff, nstate))) return rc;
   }
 
-  double h[4];
-  GBCP_CUDA_TRY(c, cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
-  GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
-  const double eloc = c.omega * h[0], ehart = c.omega * h[1];
-  const double exc = c.omega / nmesh * h[2], eext = c.omega / nmesh * h[3];
-  energies_host[0] = ekin + eloc + ehart + exc + eext;
+  double e4[4], ekin = 0.0;
+  if ((rc = vofrho_energies(c, sums, dscal, e4, &ekin))) return rc;
+  energies_host[0] = ekin + e4[0] + e4[1] + e4[2] + e4[3];
   energies_host[1] = ekin;
-  energies_host[2] = eloc;
-  energies_host[3] = ehart;
-  energies_host[4] = exc;
-  energies_host[5] = eext;
-  for (int k = 0; k < 6; ++k)
-    if (!std::isfinite(energies_host[k])) {
-      c.err = "energy: non-finite result";
-      return 3;
-    }
+  for (int k = 0; k < 4; ++k) energies_host[2 + k] = e4[k];
   return 0;
 }
 

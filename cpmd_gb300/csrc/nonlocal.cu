@@ -38,6 +38,10 @@ constexpr int kMaxProj = 64;
 
 struct ProjInfo {
   int nat, ngh;
+  // the caller's fnl / dfnl layout: fnl(ia, iv, i) at ia + lda (iv + ldp i), dfnl(ia, iv, k, i)
+  // at ia + lda (iv + ldp (k + 3 i)) -- the reference's global fnl(imagp, ions1%nat, nhxs, n)
+  // seen from a species block fnl(1, isa0+1, 1, 1) (rnlsm1_utils.mod.F90:156-165)
+  int lda, ldp;
   int lmod4[kMaxProj];  // angular momentum mod 4 per projector
   // rnlsm2 (dfnl = d fnl / d R): rows p = ia + nat (iv + ngh k) for the three directions k,
   // operand (-i)^(l+1) twnl eigr tpiba G_k (rnlsm2_utils.mod.F90:190-240)
@@ -45,6 +49,13 @@ struct ProjInfo {
   const short4* gm;     // Miller indices of the sphere (deriv only)
   double tpiba;
 };
+
+// offset of row p = ia + nat (iv + ngh k) of state i in the caller's fnl (kdim 1) or dfnl (kdim 3)
+__device__ __forceinline__ size_t fnl_at(const ProjInfo& pi, size_t p, size_t i, int kdim) {
+  const size_t ia = p % pi.nat, q = p / pi.nat;
+  const size_t iv = q % pi.ngh, k = q / pi.ngh;
+  return ia + (size_t)pi.lda * (iv + (size_t)pi.ldp * (k + (size_t)kdim * i));
+}
 
 // (-i)^l * z
 __device__ __forceinline__ cx<double> phase_l(int l, cx<double> z) {
@@ -131,11 +142,13 @@ __global__ void __launch_bounds__(NT) k_rnlsm1_part(const double* __restrict__ c
     }
 }
 
-__global__ void k_rnlsm1_fold(const double* __restrict__ part, int nsplit, size_t n, double* __restrict__ fnl) {
+// partials part[split][p + P i] folded in split order into the caller's layout
+__global__ void k_rnlsm1_fold(const double* __restrict__ part, int nsplit, size_t P, size_t n, ProjInfo pi, int kdim,
+                              double* __restrict__ fnl) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
     double s = 0.0;
     for (int p = 0; p < nsplit; ++p) s += part[(size_t)p * n + e];
-    fnl[e] = 2.0 * s;
+    fnl[fnl_at(pi, e % P, e / P, kdim)] = 2.0 * s;
   }
 }
 
@@ -174,7 +187,7 @@ __global__ void __launch_bounds__(NT) k_fnonloc(double* __restrict__ c2r, int ld
         const int iv = p2 / pi.nat;
         double ffi = f[i];
         if (ffi < 1e-5) ffi = 1.0;
-        bv = fnl[p2 + (size_t)P * i] * (-ffi * wsg[iv]);
+        bv = fnl[fnl_at(pi, p2, i, 1)] * (-ffi * wsg[iv]);
       }
       Bs[kp][cc] = bv;
     }
@@ -203,13 +216,19 @@ __global__ void __launch_bounds__(NT) k_fnonloc(double* __restrict__ c2r, int ld
     }
 }
 
-bool make_info(Ctx& c, int nat, int ngh, const int* nghtol, ProjInfo& pi) {
+bool make_info(Ctx& c, int nat, int ngh, const int* nghtol, int lda, int ldp, ProjInfo& pi) {
   if (nat <= 0 || ngh <= 0 || ngh > kMaxProj) {
     c.err = "projectors: need 0 < ngh <= 64 and nat > 0";
     return false;
   }
   pi.nat = nat;
   pi.ngh = ngh;
+  pi.lda = lda > 0 ? lda : nat;
+  pi.ldp = ldp > 0 ? ldp : ngh;
+  if (pi.lda < nat || pi.ldp < ngh) {
+    c.err = "projectors: fnl leading dimensions below nat / ngh";
+    return false;
+  }
   pi.deriv = 0;
   pi.gm = nullptr;
   pi.tpiba = 0.0;
@@ -288,12 +307,13 @@ __global__ void __launch_bounds__(256) k_nl_c3(const cx<double>* __restrict__ c0
   for (int s = 0; s < 3; ++s) B[(((size_t)s * nstate + i) * kstride) / 2 + G] = hr[s] | (hi[s] << 16);
 }
 
-// fnl[p + P i] = 2 sum_split part[(split n + i) P + p]
-__global__ void k_nl_fnl_fold(const float* __restrict__ part, int nsplit, size_t Pn, double* __restrict__ fnl) {
+// fnl(p, i) = 2 sum_split part[(split n + i) P + p], written in the caller's layout
+__global__ void k_nl_fnl_fold(const float* __restrict__ part, int nsplit, size_t P, size_t Pn, ProjInfo pi, int kdim,
+                              double* __restrict__ fnl) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < Pn; e += (size_t)gridDim.x * blockDim.x) {
     double s = 0.0;
     for (int k = 0; k < nsplit; ++k) s += f2d_int(part[k * Pn + e]);
-    fnl[e] = 2.0 * s;
+    fnl[fnl_at(pi, e % P, e / P, kdim)] = 2.0 * s;
   }
 }
 
@@ -340,13 +360,13 @@ __global__ void __launch_bounds__(256) k_nl_y3(const double* __restrict__ twnl, 
 
 // fnonloc B operand: slice s, row i, column p: Z(p, i) = -f_i wsg(iv) fnl(p, i), f < 1e-5 counted as 1
 __global__ void k_nl_z3(const double* __restrict__ fnl, const double* __restrict__ f, const double* __restrict__ wsg,
-                        int nat, size_t P, int nstate, size_t kstride, uint16_t* __restrict__ B) {
+                        ProjInfo pi, size_t P, int nstate, size_t kstride, uint16_t* __restrict__ B) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < P * nstate; e += (size_t)gridDim.x * blockDim.x) {
     const size_t i = e / P, p = e % P;
-    const int iv = (int)(p / nat);
+    const int iv = (int)(p / pi.nat);
     const double fi = f[i] < 1e-5 ? 1.0 : f[i];
     uint32_t h[3];
-    split3(d2f_int(-fi * wsg[iv] * fnl[e]), h);
+    split3(d2f_int(-fi * wsg[iv] * fnl[fnl_at(pi, p, i, 1)]), h);
 #pragma unroll
     for (int s = 0; s < 3; ++s) B[((size_t)s * nstate + i) * kstride + p] = (uint16_t)h[s];
   }
@@ -392,7 +412,8 @@ int rnlsm1_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, const ProjInfo&
   if (rc) return rc;
   {
     ProfScope ps_(c, "k_nl_fnl_fold");
-    k_nl_fnl_fold<<<1024, 256, 0, c.stream>>>(static_cast<const float*>(c.nl_tp.p), ksplit, (size_t)P * nstate, fnl);
+    k_nl_fnl_fold<<<1024, 256, 0, c.stream>>>(static_cast<const float*>(c.nl_tp.p), ksplit, (size_t)P,
+                                              (size_t)P * nstate, pi, pi.deriv ? 3 : 1, fnl);
     GBCP_LAUNCH_CHECK(c);
   }
   return check_status(c);
@@ -409,7 +430,7 @@ int fnonloc_tc(Ctx& c, cx<double>* c2, int ldc2, int nstate, const double* f, co
     k_nl_y3<<<dim3((c.ngw + 31) / 32, (pi.nat + 31) / 32), 256, 0, c.stream>>>(twnl, eigr, c.ngw, pi, ks,
                                                                               static_cast<uint16_t*>(c.nl_ta.p));
     GBCP_LAUNCH_CHECK(c);
-    k_nl_z3<<<1024, 256, 0, c.stream>>>(fnl, f, wsg, pi.nat, (size_t)P, nstate, ks, static_cast<uint16_t*>(c.nl_tb.p));
+    k_nl_z3<<<1024, 256, 0, c.stream>>>(fnl, f, wsg, pi, (size_t)P, nstate, ks, static_cast<uint16_t*>(c.nl_tb.p));
     GBCP_LAUNCH_CHECK(c);
   }
   GBCP_CUDA_TRY(c, cudaMemsetAsync(c.d_info, 0, sizeof(int), c.stream));
@@ -449,7 +470,7 @@ int rnlsm1_simt(Ctx& c, const cx<double>* c0, int ldc, int nstate, const ProjInf
   }
   {
     ProfScope ps_(c, "k_rnlsm1_fold");
-    k_rnlsm1_fold<<<512, 256, 0, c.stream>>>(part, nsplit, n, fnl);
+    k_rnlsm1_fold<<<512, 256, 0, c.stream>>>(part, nsplit, (size_t)P, n, pi, pi.deriv ? 3 : 1, fnl);
     GBCP_LAUNCH_CHECK(c);
   }
   return 0;
@@ -458,9 +479,9 @@ int rnlsm1_simt(Ctx& c, const cx<double>* c0, int ldc, int nstate, const ProjInf
 }  // namespace
 
 int nl_rnlsm1(Ctx& c, const cx<double>* c0, int ldc, int nstate, int nat, int ngh, const int* nghtol_host,
-              const double* twnl, const cx<double>* eigr, double* fnl) {
+              const double* twnl, const cx<double>* eigr, double* fnl, int lda, int ldp) {
   ProjInfo pi;
-  if (!make_info(c, nat, ngh, nghtol_host, pi)) return 1;
+  if (!make_info(c, nat, ngh, nghtol_host, lda, ldp, pi)) return 1;
   if (use_tc_projectors(c)) return rnlsm1_tc(c, c0, ldc, nstate, pi, twnl, eigr, fnl);
   return rnlsm1_simt(c, c0, ldc, nstate, pi, twnl, eigr, fnl);
 }
@@ -470,19 +491,19 @@ namespace {
 // fion(k, ia) -= sum_i sum_iv 2 wsg(iv) f_i dfnl(ia,iv,k,i) fnl(ia,iv,i), states with |f| > 1e-12
 // (rnlfor_utils.mod.F90:283-330, KB branch); one CTA per atom, fixed-order reduction
 __global__ void __launch_bounds__(256) k_rnlfor(int nstate, const double* __restrict__ f, int nat, int ngh,
-                                                const double* __restrict__ wsg, const double* __restrict__ fnl,
-                                                const double* __restrict__ dfnl, double* __restrict__ fion) {
+                                                int lda, int ldp, const double* __restrict__ wsg,
+                                                const double* __restrict__ fnl, const double* __restrict__ dfnl,
+                                                double* __restrict__ fion) {
   const int ia = blockIdx.x;
-  const size_t P = (size_t)nat * ngh;
   double acc[3] = {0.0, 0.0, 0.0};
   for (int t = threadIdx.x; t < nstate * ngh; t += blockDim.x) {
     const int i = t / ngh, iv = t - i * ngh;
     const double w = f[i];
     if (!(fabs(w) > 1e-12)) continue;
-    const size_t p = (size_t)ia + (size_t)nat * iv;
-    const double a = 2.0 * wsg[iv] * w * fnl[p + P * i];
+    const double a = 2.0 * wsg[iv] * w * fnl[(size_t)ia + (size_t)lda * (iv + (size_t)ldp * i)];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) acc[k] = fma(a, dfnl[p + P * (k + 3 * (size_t)i)], acc[k]);
+    for (int k = 0; k < 3; ++k)
+      acc[k] = fma(a, dfnl[(size_t)ia + (size_t)lda * (iv + (size_t)ldp * (k + 3 * (size_t)i))], acc[k]);
   }
   __shared__ double red[3][256];
 #pragma unroll
@@ -500,9 +521,9 @@ __global__ void __launch_bounds__(256) k_rnlfor(int nstate, const double* __rest
 }  // namespace
 
 int nl_rnlsm2(Ctx& c, const cx<double>* c0, int ldc, int nstate, int nat, int ngh, const int* nghtol_host,
-              const double* twnl, const cx<double>* eigr, double* dfnl) {
+              const double* twnl, const cx<double>* eigr, double* dfnl, int lda, int ldp) {
   ProjInfo pi;
-  if (!make_info(c, nat, ngh, nghtol_host, pi)) return 1;
+  if (!make_info(c, nat, ngh, nghtol_host, lda, ldp, pi)) return 1;
   pi.deriv = 1;
   pi.gm = c.wmill;
   pi.tpiba = std::sqrt(c.tpiba2);
@@ -511,21 +532,23 @@ int nl_rnlsm2(Ctx& c, const cx<double>* c0, int ldc, int nstate, int nat, int ng
 }
 
 int nl_rnlfor(Ctx& c, int nstate, const double* f, int nat, int ngh, const double* wsg, const double* fnl,
-              const double* dfnl, double* fion) {
-  if (nat <= 0 || ngh <= 0 || nstate <= 0) {
-    c.err = "rnlfor: bad sizes";
+              const double* dfnl, double* fion, int lda, int ldp) {
+  lda = lda > 0 ? lda : nat;
+  ldp = ldp > 0 ? ldp : ngh;
+  if (nat <= 0 || ngh <= 0 || nstate <= 0 || lda < nat || ldp < ngh) {
+    c.err = "rnlfor: bad sizes or fnl leading dimensions";
     return 1;
   }
   ProfScope ps_(c, "k_rnlfor");
-  k_rnlfor<<<nat, 256, 0, c.stream>>>(nstate, f, nat, ngh, wsg, fnl, dfnl, fion);
+  k_rnlfor<<<nat, 256, 0, c.stream>>>(nstate, f, nat, ngh, lda, ldp, wsg, fnl, dfnl, fion);
   GBCP_LAUNCH_CHECK(c);
   return 0;
 }
 
 int nl_fnonloc(Ctx& c, cx<double>* c2, int ldc2, int nstate, const double* f, int nat, int ngh, const int* nghtol_host,
-               const double* twnl, const cx<double>* eigr, const double* fnl, const double* wsg) {
+               const double* twnl, const cx<double>* eigr, const double* fnl, const double* wsg, int lda, int ldp) {
   ProjInfo pi;
-  if (!make_info(c, nat, ngh, nghtol_host, pi)) return 1;
+  if (!make_info(c, nat, ngh, nghtol_host, lda, ldp, pi)) return 1;
   if (use_tc_projectors(c)) return fnonloc_tc(c, c2, ldc2, nstate, f, pi, twnl, eigr, fnl, wsg);
   const int rows = 2 * c.ngw;
   dim3 grid((rows + TS - 1) / TS, (nstate + TS - 1) / TS);

@@ -81,6 +81,9 @@ __device__ __forceinline__ uint32_t digit_bf16(int d) { return __float_as_uint((
 
 // exponent E with |x| < 2^E from the bit pattern of max |x| (fold_round.h)
 __device__ __forceinline__ int exp_of_max(unsigned long long bits) { return fold::exp_of_max(bits); }
+// a column maximum that is NaN or infinite: its column held a non-finite value, and every
+// overlap entry of that column is reported as NaN (the digit split of it is meaningless)
+__device__ __forceinline__ bool max_nonfinite(unsigned long long bits) { return ((bits >> 52) & 0x7FF) == 0x7FF; }
 
 // Fixed-point magnitude trunc(|x| 2^(56-E)) (< 2^56) and the sign (fold_round.h)
 __device__ __forceinline__ unsigned long long fixed56(double x, int E, bool& neg) { return fold::fixed56(x, E, neg); }
@@ -367,6 +370,11 @@ struct OzParams {
   int sub_base;                  // mode 0: K offset of this launch, in sub-chunks
   int rt0, nrt;                  // mode 1: row tiles rt0 .. rt0+nrt-1 (nrt = 0: every row tile)
   int* status;
+  // test of the timeout path: stall != 0 makes the TMA thread issue no loads, so the
+  // MMA thread's first wait on a stage (no copy in flight towards it) runs out after
+  // wait_limit cycles (0 = the default limit of about a second)
+  int stall;
+  long long wait_limit;
 };
 
 struct OzUnit {
@@ -479,16 +487,17 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_sh;
+  const long long lim = p.wait_limit > 0 ? p.wait_limit : 2000000000LL;
 
   if (warp == OZ_TMA_WARP) {
     if (lane == 0) {
       int it = 0;  // sub-chunks loaded by this CTA
-      for (int u = blockIdx.x; u >= 0 && !abort_sh; u = oz_next_unit(p, u)) {
+      for (int u = blockIdx.x; u >= 0 && !abort_sh && !p.stall; u = oz_next_unit(p, u)) {
         const OzUnit w = oz_unit(p, u);
         if (!w.valid) break;
         for (int s = 0; s < w.nsub && !abort_sh; ++s, ++it) {
           const int slot = it & 1;
-          if (!tc::mbar_wait(&empty[slot], (uint32_t)(((it >> 1) & 1) ^ 1))) {
+          if (!tc::mbar_wait(&empty[slot], (uint32_t)(((it >> 1) & 1) ^ 1), lim)) {
             abort_sh = 1;
             atomicExch(p.status, -2);
             break;
@@ -507,7 +516,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         if (!w.valid) break;
         for (int c0 = 0; c0 < w.nsub && !stop; c0 += OZ_SUBS, ++ch) {
           const int b = ch & 1;
-          if (abort_sh || !tc::mbar_wait(&tempty[b], (uint32_t)(((ch >> 1) & 1) ^ 1))) {
+          if (abort_sh || !tc::mbar_wait(&tempty[b], (uint32_t)(((ch >> 1) & 1) ^ 1), lim)) {
             stop = true;
             break;
           }
@@ -515,7 +524,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           const int c1 = min(w.nsub, c0 + OZ_SUBS);
           for (int s = c0; s < c1; ++s, ++it) {
             const int slot = it & 1;
-            if (abort_sh || !tc::mbar_wait(&full[slot], (uint32_t)((it >> 1) & 1))) {
+            if (abort_sh || !tc::mbar_wait(&full[slot], (uint32_t)((it >> 1) & 1), lim)) {
               stop = true;
               break;
             }
@@ -535,7 +544,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       consumed_sh = it;
       // every MMA this thread issued has finished once this commit arrives
       tc::mma_commit(&drain);
-      if (!tc::mbar_wait(&drain, 0)) atomicExch(p.status, -2);
+      if (!tc::mbar_wait(&drain, 0, lim)) atomicExch(p.status, -2);
     }
   } else {
     const int q = warp & 3, h = warp >> 2;  // TMEM lane quadrant, column group
@@ -565,7 +574,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       }
       for (int c0 = 0; c0 < w.nsub; c0 += OZ_SUBS, ++ch) {
         const int b = ch & 1;
-        const bool ok = !abort_sh && tc::mbar_wait(&tfull[b], (uint32_t)((ch >> 1) & 1));
+        const bool ok = !abort_sh && tc::mbar_wait(&tfull[b], (uint32_t)((ch >> 1) & 1), lim);
         if (!__all_sync(0xffffffffu, ok ? 1 : 0)) {
           stop = true;
           break;
@@ -616,7 +625,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   if (warp == OZ_TMA_WARP && lane == 0) {
     // loads issued but never consumed (after an abort) still land in shared
     // memory: wait for them before the CTA exits (at most one per stage)
-    for (int j = consumed_sh; j < issued_sh; ++j) tc::mbar_wait(&full[j & 1], (uint32_t)((j >> 1) & 1));
+    for (int j = consumed_sh; j < issued_sh; ++j) tc::mbar_wait(&full[j & 1], (uint32_t)((j >> 1) & 1), lim);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -639,6 +648,7 @@ __global__ void k_ozaki_syrk_finalize(const long long* __restrict__ H, const lon
     if (i > j) continue;
     double v = 2.0 * fold_to_double(H[e], Lo[e], exp_of_max(cmax[i]) + exp_of_max(cmax[j]));
     if (geq0) v -= Ar[(size_t)i * lda] * Ar[(size_t)j * lda];
+    if (max_nonfinite(cmax[i]) || max_nonfinite(cmax[j])) v = __longlong_as_double(0x7FF8000000000000LL);
     S[(size_t)i * n + j] = v;
     S[(size_t)j * n + i] = v;
     mx = fmax(mx, fabs(i == j ? v - 1.0 : v));
@@ -660,6 +670,7 @@ __global__ void k_ozaki_xov_finalize(const long long* __restrict__ H, const long
     const int i = (int)(e / n), j = (int)(e % n);
     double v = 2.0 * fold_to_double(H[e], Lo[e], exp_of_max(xmax[i]) + exp_of_max(ymax[j]));
     if (geq0) v -= X[(size_t)i * ldx] * Y[(size_t)j * ldy];
+    if (max_nonfinite(xmax[i]) || max_nonfinite(ymax[j])) v = __longlong_as_double(0x7FF8000000000000LL);
     A[e] = v;
   }
 }
@@ -677,9 +688,12 @@ __global__ void k_ozaki_syrk_finalize_ranges(const long long* __restrict__ H, co
     const int i = (int)(e / n), j = (int)(e % n);
     if (i > j) continue;
     double v = 0.0;
-    for (int r = 0; r < R; ++r)
+    for (int r = 0; r < R; ++r) {
       v += 2.0 * fold_to_double(H[r * nn + e], Lo[r * nn + e],
                                 exp_of_max(cmax[(size_t)r * n + i]) + exp_of_max(cmax[(size_t)r * n + j]));
+      if (max_nonfinite(cmax[(size_t)r * n + i]) || max_nonfinite(cmax[(size_t)r * n + j]))
+        v = __longlong_as_double(0x7FF8000000000000LL);
+    }
     if (geq0) v -= Ar[(size_t)i * lda] * Ar[(size_t)j * lda];
     S[(size_t)i * n + j] = v;
     S[(size_t)j * n + i] = v;
@@ -747,6 +761,11 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, unsig
   p.Hacc = Hacc;
   p.Lacc = Lacc;
   p.status = status;
+  if (c.test_stall) {  // one call only: the test of the timeout path
+    p.stall = 1;
+    p.wait_limit = 2000000;  // about a millisecond
+    c.test_stall = 0;
+  }
   {
     allow_smem(k_oz_tc, OZ_SMEM);
     ProfScope ps_(c, "k_ozaki_syrk");
@@ -953,9 +972,14 @@ int ovlap_tc_ranges(Ctx& c, const double* Ar, int lda, int n, const int* kb, int
     p.Hacc = Hacc + (size_t)r * nn;
     p.Lacc = Lacc + (size_t)r * nn;
     p.status = status;
+    if (c.test_stall && r == 0) {  // the test of the timeout path, first range of one call
+      p.stall = 1;
+      p.wait_limit = 2000000;
+    }
     ProfScope ps_(c, "k_ozaki_syrk");
     GBCP_LAUNCH_PDL(c, k_oz_tc, dim3(ntiles, nsplit), dim3(OZ_THREADS), OZ_SMEM, ma, mb, p);
   }
+  c.test_stall = 0;
   {
     ProfScope ps_(c, "k_ozaki_syrk_finalize");
     const int fb = std::max(1, std::min(1024, (int)((nn + 255) / 256)));

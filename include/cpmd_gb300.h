@@ -97,8 +97,14 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  *                   0 = chosen per launch from the SM count, 1..8 = fixed;
  *   GBCP_OPT_XC     exchange-correlation functional of gbcp_energy: 0 = LDA
  *                   (Slater + Perdew-Zunger, the default), 1 = PBE (gradient-
- *                   corrected, the reference's vofrhob/gcener route). */
-enum gbcp_option { GBCP_OPT_GEMM = 1, GBCP_OPT_BATCH = 2, GBCP_OPT_FFT = 3, GBCP_OPT_XCHUNKS = 4, GBCP_OPT_XC = 5 };
+ *                   corrected, the reference's vofrhob/gcener route);
+ *   GBCP_OPT_TEST_TIMEOUT  test hook of the failure path: 1 = the next overlap
+ *                   on the tensor cores issues no operand loads, so its first
+ *                   bounded wait (no copy in flight towards it) runs out after
+ *                   about a millisecond; the call returns GBCP_ERR_TIMEOUT with
+ *                   c0 untouched and the hook clears itself. */
+enum gbcp_option { GBCP_OPT_GEMM = 1, GBCP_OPT_BATCH = 2, GBCP_OPT_FFT = 3, GBCP_OPT_XCHUNKS = 4, GBCP_OPT_XC = 5,
+                   GBCP_OPT_TEST_TIMEOUT = 90 };
 int gbcp_set_option(gbcp_ctx* ctx, int key, int value);
 /* Queue later work on `stream` (a cudaStream_t; NULL = the context's own
  * stream; the CUDA legacy default stream is cudaStreamLegacy).  Device-pointer calls are ordered only with respect to this stream,
@@ -194,30 +200,41 @@ int gbcp_fwfftn(gbcp_ctx* ctx, double* f, int mem);
 
 /* rnlsm(c0, nstate, ...) -> rnlsm1         rnlsm1_utils.mod.F90:42-193
  * One species of nat atoms with ngh projectors of angular momentum nghtol[iv]:
- * fnl(nat, ngh, nstate) = 2 Re sum_G conj((-i)^l twnl(G,iv) eigr(G,ia)) c(G),
- * with the G = 0 term halved.  twnl(ngw, ngh) real, eigr(ngw, nat) complex. */
+ * fnl(ia, iv, i) = 2 Re sum_G conj((-i)^l twnl(G,iv) eigr(G,ia)) c(G),
+ * with the G = 0 term halved.  twnl(ngw, ngh) real, eigr(ngw, nat) complex.
+ * fnl layout: element (ia, iv, i) at fnl[ia + ld_atoms (iv + ld_proj i)], so a
+ * species block of the reference's global fnl(imagp, ions1%nat, maxsys%nhxs,
+ * nstate) is written in place with fnl = C_LOC(fnl(1, isa0+1, 1, 1)),
+ * ld_atoms = ions1%nat, ld_proj = maxsys%nhxs (rnlsm1_utils.mod.F90:156-165);
+ * only the block's own entries are written.  ld_atoms = 0 / ld_proj = 0 mean
+ * nat / ngh (a dense (nat, ngh, nstate) array). */
 int gbcp_rnlsm1(gbcp_ctx* ctx, const double* c0, int ldc, int nstate, int nat, int ngh, const int32_t* nghtol,
-                const double* twnl, const double* eigr, double* fnl, int mem);
+                const double* twnl, const double* eigr, double* fnl, int ld_atoms, int ld_proj, int mem);
 
 /* rnlsm2(c0, nstate, ikpt, ikind)          rnlsm2_utils.mod.F90:41-299 (Γ branch l.190-240)
- * dfnl(nat, ngh, 3, nstate) = d fnl / d R_k
+ * dfnl(ia, iv, k, i) = d fnl / d R_k
  *   = 2 tpiba Re sum_G conj((-i)^(l+1) twnl(G,iv) eigr(G,ia) G_k) c(G), G = 0 halved,
- * G_k the Miller index along k (cubic cell).  Same operands as gbcp_rnlsm1. */
+ * G_k the Miller index along k (cubic cell).  Same operands as gbcp_rnlsm1;
+ * dfnl layout: element (ia, iv, k, i) at dfnl[ia + ld_atoms (iv + ld_proj (k + 3 i))],
+ * the reference's dfnl(imagp, ions1%nat, maxsys%nhxs, 3, nstate) seen from
+ * dfnl(1, isa0+1, 1, 1, 1); 0 / 0 mean a dense (nat, ngh, 3, nstate) array. */
 int gbcp_rnlsm2(gbcp_ctx* ctx, const double* c0, int ldc, int nstate, int nat, int ngh, const int32_t* nghtol,
-                const double* twnl, const double* eigr, double* dfnl, int mem);
+                const double* twnl, const double* eigr, double* dfnl, int ld_atoms, int ld_proj, int mem);
 
 /* rnlfor(fion, f, wk, nstate, nkpoint)      rnlfor_utils.mod.F90:41-368 (KB branch l.283-330)
  * fion(3, nat) -= sum_i sum_iv 2 wsg(iv) f_i fnl(ia,iv,i) dfnl(ia,iv,k,i) for |f_i| > 1e-12
- * (accumulated, like the reference; Γ point, one species). */
+ * (accumulated, like the reference; Γ point, one species); fnl and dfnl in the
+ * layouts of gbcp_rnlsm1 / gbcp_rnlsm2 with the same ld_atoms, ld_proj. */
 int gbcp_rnlfor(gbcp_ctx* ctx, int nstate, const double* f, int nat, int ngh, const double* wsg, const double* fnl,
-                const double* dfnl, double* fion, int mem);
+                const double* dfnl, int ld_atoms, int ld_proj, double* fion, int mem);
 
 /* fnonloc(c2, f, nstate, ...)               fnonloc_utils.mod.F90:306-354 (BHS/KB branch)
  * c2(G,i) += sum_iv twnl(G,iv) (-i)^l (-f_i wsg(iv)) sum_ia eigr(G,ia) fnl(ia,iv,i),
- * f_i < 1e-5 counted as 1. */
+ * f_i < 1e-5 counted as 1; fnl in the layout of gbcp_rnlsm1 (the reference reads
+ * fnl(1, isa0+1, iv, i), fnonloc_utils.mod.F90:322-324). */
 int gbcp_fnonloc(gbcp_ctx* ctx, double* c2, int ldc2, int nstate, const double* f, int nat, int ngh,
-                 const int32_t* nghtol, const double* twnl, const double* eigr, const double* fnl,
-                 const double* wsg, int mem);
+                 const int32_t* nghtol, const double* twnl, const double* eigr, const double* fnl, int ld_atoms,
+                 int ld_proj, const double* wsg, int mem);
 
 /* Density sphere of the energy functional (cppt: nhg, inyh(3,nhg), hg(nhg);
  * the first ngw entries are the wavefunction sphere of gbcp_grid_desc).
@@ -247,6 +264,26 @@ int gbcp_set_dens_sphere(gbcp_ctx* ctx, int nhg, const int32_t* inyh, const doub
 int gbcp_energy(gbcp_ctx* ctx, const double* c0, int ldc, int nstate, const double* f, int nat, int nsp,
                 const int32_t* isp, const double* tau, const double* vps, const double* vext, double* energies,
                 double* c2, int ldc2, double* dvloc, double* fion, int mem);
+
+/* Density -> potential, the reference's vofrho for a local pseudopotential
+ * (rscpot_utils.mod.F90:132 -> vofrhoa_utils.mod.F90:41-144 with the xc step of
+ * vofrhob_utils.mod.F90:80-471; cubic cell): from rhoe (kr1, kr2, kr3) to
+ *   veff (kr1, kr2, kr3) = V_ion + V_H + v_xc (+ vext), the V(r) that vpsi and the
+ *   caller's own fnonloc / force sequence then use (forces_driver.mod.F90:224);
+ *   energies[4] (host) = {E_loc, E_H, E_xc, E_ext} in Ha, as in gbcp_energy;
+ *   fion (3, nat) overwritten with the local-potential forces (may be NULL).
+ * The other arguments are those of gbcp_energy; GBCP_OPT_XC selects LDA or PBE. */
+int gbcp_vofrho(gbcp_ctx* ctx, const double* rhoe, int nat, int nsp, const int32_t* isp, const double* tau,
+                const double* vps, const double* vext, double* veff, double* energies, double* fion, int mem);
+
+/* General overlap, the reference's ovlap with c1 != c2 (ovlap_utils.mod.F90:157-166,
+ * dgemm('T','N') over the real views plus the dger G = 0 correction):
+ *   a(i, j) = <c1_i|c2_j> = 2 Re sum_G conj(c1_i) c2_j - Re c1_i(0) Re c2_j(0),
+ * a (nstate x nstate) column-major; used for the Lagrange multipliers of CP
+ * dynamics (forces_driver.mod.F90:262).  FP64 SIMT, or the FP64-accurate split
+ * GEMM on the tensor cores when GBCP_OPT_GEMM selects it. */
+int gbcp_ovlap2(gbcp_ctx* ctx, const double* c1, int ldc1, const double* c2, int ldc2, int nstate, double* amat,
+                int mem);
 
 /* ---- Batches of independent cells (no counterpart in the reference, where
  * every cell is a separate run).  A batch owns one context per cell; a step

@@ -65,7 +65,7 @@ def test_create_rejects_bad_arguments_without_gpu(lib):
     assert lib.gbcp_vpsi(None, None, 0, None, 0, None, None, 0, 0) == 1
     assert lib.gbcp_ortho(None, None, 0, 0, 0, None, 0) == 1
     assert lib.gbcp_invfftn(None, None, 0) == 1
-    assert lib.gbcp_rnlsm1(None, None, 0, 0, 0, 0, None, None, None, None, 0) == 1
+    assert lib.gbcp_rnlsm1(None, None, 0, 0, 0, 0, None, None, None, None, 0, 0, 0) == 1
     assert lib.gbcp_kernel_launches() >= 0
 
 

@@ -240,7 +240,10 @@ def test_c4_projectors_full_ngw_vs_oracle(gpu_lib, c4proj, precision):
     ffi = np.where(f < 1e-5, 1.0, f)
     z = (np.abs(fnl_ref) * (ffi[None, None, :] * np.abs(p["wsg"])[None, :, None])).sum(axis=0)   # (ngh, n)
     bc = np.abs(p["twnl"]) @ z                                       # (ngw, n)
-    assert float((np.abs(fnl - fnl_ref) / bf[None, :, :]).max()) < 1e-5
+    # FP32 accumulation over K = 2 ngw = 683 686 terms (split-K partials folded in FP64):
+    # the bound of the 64-atom tests (1e-5 at K = 85 472) grown like sqrt(K)
+    tol_k = 1e-5 * np.sqrt(2 * b.ngw / 85472.0)
+    assert float((np.abs(fnl - fnl_ref) / bf[None, :, :]).max()) < tol_k
     assert float((np.abs(got - ref) / bc).max()) < 1e-5
 
 
