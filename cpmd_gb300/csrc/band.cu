@@ -224,6 +224,13 @@ int band_rhoofr(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double*
   return 0;
 }
 
+int band_vpsi(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, const double* f, const double* vpot,
+              int nstate) {
+  if (nstate <= 0) return 0;
+  return c.precision == 0 ? band_vpsi_fp64(c, c0, ldc, c2, ldc2, f, vpot, nstate)
+                          : band_vpsi_fp32(c, c0, ldc, c2, ldc2, f, vpot, nstate);
+}
+
 int dense_fft(Ctx& c, cx<double>* grid, bool inv) {
   const int n1 = c.nr[0], n2 = c.nr[1], n3 = c.nr[2], k1 = c.kr[0], k2 = c.kr[1];
   const double scale_last = inv ? 1.0 : 1.0 / ((double)n1 * n2 * n3);
