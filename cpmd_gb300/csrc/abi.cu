@@ -23,6 +23,7 @@ std::atomic<long long> g_launches{0};
 
 bool ensure(Ctx& c, Scratch& s, size_t bytes) {
   if (bytes <= s.cap && s.p) return true;
+  if (&s == &c.st_c0) c.wfn.valid = false;  // a new buffer holds no cached wavefunction
   if (s.p) {
     cudaStreamSynchronize(c.stream);
     cudaFree(s.p);
@@ -393,7 +394,7 @@ int gbcp_ctx_destroy(gbcp_ctx* h) {
                           &c.st_misc, &c.st_misc2, &c.st_vf, &c.red, &c.red2, &c.smat, &c.smat2, &c.smat3, &c.sparts, &c.cscr, &c.cdiag, &c.cwork, &c.xr_part, &c.xr_tk, &c.rt_mats, &c.en_g3, &c.oz_a, &c.oz_b,
                           &c.nl_a, &c.nl_b, &c.nl_c, &c.nl_d, &c.nl_ta, &c.nl_tb, &c.nl_tp, &c.en_rho, &c.en_a, &c.en_b, &c.en_veff,
                           &c.en_red, &c.en_ei, &c.en_fp, &c.en_idx, &c.en_in[0], &c.en_in[1], &c.en_in[2],
-                          &c.en_in[3], &c.en_in[4], &c.oz_c, &c.oz_rmax};
+                          &c.en_in[3], &c.en_in[4], &c.oz_c, &c.oz_rmax, &c.rho_sc, &c.rho_tk};
   for (auto* s : all) gbcp::release(*s);
   for (cudaStream_t* st : {&c.copy, &c.copy_out, &c.side})
     if (*st) {
@@ -441,6 +442,11 @@ int gbcp_set_option(gbcp_ctx* h, int key, int value) {
   }
   if (key == GBCP_OPT_XC && (value == 0 || value == 1)) {
     c.xc = value;
+    return GBCP_OK;
+  }
+  if (key == GBCP_OPT_WFN_CACHE && (value == 0 || value == 1)) {
+    c.wfn.on = value == 1;
+    c.wfn.valid = false;  // setting the option always drops a kept copy
     return GBCP_OK;
   }
   if (key == GBCP_OPT_TEST_TIMEOUT && (value == 0 || value == 1)) {
@@ -521,7 +527,31 @@ namespace {
 using gbcp::Scratch;
 
 // Stage a host (ngw x n, leading dim ld) complex array into packed device memory.
+// ---- the wavefunction cache (see WfnCache) ----
+// the reference's key, SUM(ABS(c0(:,1))) (rhoofr_utils.mod.F90:244)
+double wfn_key(const double* h, int rows) {
+  double s = 0.0;
+  for (int i = 0; i < rows; ++i) s += std::hypot(h[2 * (size_t)i], h[2 * (size_t)i + 1]);
+  return s;
+}
+bool wfn_hit(Ctx& c, const double* h, int ld, int n) {
+  const gbcp::WfnCache& w = c.wfn;
+  return w.on && w.valid && w.host == h && w.ldc == ld && w.n == n && w.dev == c.st_c0.p &&
+         wfn_key(h, c.ngw) == w.key;
+}
+void wfn_put(Ctx& c, const double* h, int ld, int n) {
+  gbcp::WfnCache& w = c.wfn;
+  if (!w.on) return;
+  w.valid = true;
+  w.host = h;
+  w.dev = c.st_c0.p;
+  w.ldc = ld;
+  w.n = n;
+  w.key = wfn_key(h, c.ngw);
+}
+
 int stage_in_cx(Ctx& c, Scratch& s, const double* h, int ld, int rows, int n, cx<double>** d) {
+  if (&s == &c.st_c0) c.wfn.valid = false;  // the cached copy is overwritten
   const size_t bytes = sizeof(cx<double>) * (size_t)rows * n;
   if (!gbcp::ensure(c, s, bytes)) return GBCP_ERR_NOMEM;
   *d = static_cast<cx<double>*>(s.p);
@@ -661,11 +691,13 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
     cx<double>* t = static_cast<cx<double>*>(c.st_c0.p);
     const int nb = stage_plan(c, nstate);
     if ((rc = pipe_prepare(c, nb))) return rc;
+    const bool resident = wfn_hit(c, c0, ldc, nstate);
     for (int b = 0; b < nb; ++b) {
       const int s0 = 2 * c.stage_bounds[b], ns = std::min(2 * c.stage_bounds[b + 1], nstate) - s0;
-      if ((rc = pipe_up(c, t, c0, ldc, s0, ns))) return rc;
+      if (!resident && (rc = pipe_up(c, t, c0, ldc, s0, ns))) return rc;
       GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[1 + b], c.copy));
     }
+    wfn_put(c, c0, ldc, nstate);
     c.batch_ready = c.pipe_ev.data() + 1;  // launch batches stay c.batch pairs (see rhoofr_t)
     dc0 = t;
     df = static_cast<double*>(tf);
@@ -744,13 +776,14 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
     // events: [0] ordering, [1, nb] c0 chunks, [nb+1, 2nb] C2 downloads, [2nb+1, 3nb] C2 uploads,
     // [3nb+1] V(r), last: the final download
     if ((rc = pipe_prepare(c, 2 * nb + 1))) return rc;
+    const bool resident = wfn_hit(c, c0, ldc, nstate);  // c0 still on the device from rhoofr
     // copy order: the states of chunk 0, V(r), then chunk b's C2 columns behind chunk b+1's
     // states, so that the first transforms start after one chunk and each decode finds its C2
     for (int b = 0; b <= nb; ++b) {
       int s0, ns;
       if (b < nb) {
         chunk(b, &s0, &ns);
-        if ((rc = pipe_up(c, t0, c0, ldc, s0, ns))) return rc;
+        if (!resident && (rc = pipe_up(c, t0, c0, ldc, s0, ns))) return rc;
         GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[1 + b], c.copy));
       }
       if (b == 0) {
@@ -814,8 +847,11 @@ int gbcp_ortho(gbcp_ctx* h, double* c0, int ldc, int nstate, int method, double*
   int l0 = ldc;
   int rc = 0;
   if (mem == GBCP_MEM_HOST && method == GBCP_ORTHO_GS) {
-    // copies overlapped with the work where the tensor-core engine runs the step
-    rc = gbcp::ortho_gs_host(c, c0, ldc, nstate, scond);
+    // copies overlapped with the work where the tensor-core engine runs the step; c0 is
+    // rewritten in st_c0 and on the host, so the cached copy ends here
+    const bool resident = wfn_hit(c, c0, ldc, nstate);
+    c.wfn.valid = false;
+    rc = gbcp::ortho_gs_host(c, c0, ldc, nstate, scond, resident ? 1 : 0);
     if (rc != 7) return finish(c, rc);
     rc = 0;
     c.err.clear();

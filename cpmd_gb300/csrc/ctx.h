@@ -99,6 +99,20 @@ struct ProfAcc {
   long long n = 0;
 };
 
+// Device copy of a host wavefunction array kept between host-memory calls (the
+// reference's cp_cuwfn_put / cp_cuwfn_get cache, rhoofr_utils.mod.F90:240-245,
+// vpsi_utils.mod.F90:278-281): rhoofr's upload of c0 into st_c0 is reused by the
+// following vpsi and ortho calls on the same array, recognised by its address,
+// leading dimension, state count and SUM(ABS(c0(:,1))), the reference's key.
+struct WfnCache {
+  bool on = false;       // GBCP_OPT_WFN_CACHE
+  bool valid = false;    // st_c0 holds the array below
+  const void* host = nullptr;
+  const void* dev = nullptr;  // st_c0.p when it was filled (a reallocation drops the copy)
+  int ldc = 0, n = 0;
+  double key = 0.0;
+};
+
 struct Ctx {
   // grid
   int nr[3], kr[3], ngw, geq0;
@@ -111,6 +125,7 @@ struct Ctx {
   int xc = 0;          // energy functional: 0 LDA (Slater + Perdew-Zunger), 1 PBE
   int fft_engine = 0;  // band-loop FFTs: 0 four-step where a plan exists, else Stockham; 2 Stockham always
   int test_stall = 0;  // test hook: the next tensor-core overlap issues no loads and times out (one call)
+  WfnCache wfn;        // host wavefunction kept on the device between host-memory calls
   cudaStream_t stream = nullptr;  // stream all work is queued on
   cudaStream_t own = nullptr;     // the context's own stream
   // geometry
@@ -247,7 +262,8 @@ int slice_rows_side(Ctx& c, const double* A, int lda, int rows, int n, const int
                     const cudaEvent_t* ready, const cudaEvent_t** sliced);
 // Gram-Schmidt of host-memory c0 with the copies overlapped (tensor-core engine);
 // returns 7 when the engine or size does not allow it (the caller stages instead).
-int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host);
+// resident != 0: st_c0 already holds h (the wavefunction cache), no uploads
+int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host, int resident = 0);
 // ---- CP-dynamics constraint (rortho.cu) ----
 // A (row-major n x n) = <X_i|Y_j>; tensor cores in the mixed mode, FP64 SIMT otherwise.
 int xovlap(Ctx& c, const cx<double>* X, int ldx, const cx<double>* Y, int ldy, int n, double* A);

@@ -433,7 +433,7 @@ static int ortho_gs_steps(Ctx& c, cx<double>* c0, int ldc, int n, bool want_scon
 // Cholesky, C U^-1 runs range by range (in place in the staging buffer) and each
 // finished range goes back on the download stream while the next is computed.
 // A failed step skips the GEMM, so the download returns the unchanged states.
-int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host) {
+int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host, int resident) {
   if (!use_tc_gemm(c) || n > 4096 || n <= 0) return 7;
   const int ngw = c.ngw;
   // G-row ranges: multiples of 64 complex rows (128 real rows: one C M row tile, four S sub-chunks)
@@ -468,11 +468,12 @@ int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host) {
   GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.copy, c.pipe_ev[0], 0));
   for (int r = 0; r < R; ++r) {
     const int g0 = gb[r], g = gb[r + 1] - gb[r];
-    ProfScope ps_(c, "h2d_states", c.copy, 1);
-    if (g > 0)
+    if (g > 0 && !resident) {
+      ProfScope ps_(c, "h2d_states", c.copy, 1);
       GBCP_CUDA_TRY(c, cudaMemcpy2DAsync(d + g0, sizeof(cx<double>) * (size_t)ngw, h + 2 * (size_t)g0,
                                          sizeof(cx<double>) * (size_t)ldh, sizeof(cx<double>) * (size_t)g, n,
                                          cudaMemcpyHostToDevice, c.copy));
+    }
     GBCP_CUDA_TRY(c, cudaEventRecord(up[r], c.copy));
   }
   GBCP_CUDA_TRY(c, cudaMemsetAsync(c.d_info, 0, 16, c.stream));

@@ -98,13 +98,23 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  *   GBCP_OPT_XC     exchange-correlation functional of gbcp_energy: 0 = LDA
  *                   (Slater + Perdew-Zunger, the default), 1 = PBE (gradient-
  *                   corrected, the reference's vofrhob/gcener route);
+ *   GBCP_OPT_WFN_CACHE  1 = keep the device copy of a host-memory c0 that
+ *                   gbcp_rhoofr uploads, and let the following gbcp_vpsi and
+ *                   gbcp_ortho (Gram-Schmidt) on the same array use it instead
+ *                   of uploading again -- the reference's cp_cuwfn cache
+ *                   (rhoofr_utils.mod.F90:240-245, vpsi_utils.mod.F90:278-281),
+ *                   recognised like there by the array (address, leading
+ *                   dimension, states) and SUM(ABS(c0(:,1))); gbcp_ortho ends
+ *                   it (it rewrites c0).  A caller that changes c0 on the host
+ *                   in a way that keeps that key must drop the copy by setting
+ *                   the option again (any value).  0 (the default) = off;
  *   GBCP_OPT_TEST_TIMEOUT  test hook of the failure path: 1 = the next overlap
  *                   on the tensor cores issues no operand loads, so its first
  *                   bounded wait (no copy in flight towards it) runs out after
  *                   about a millisecond; the call returns GBCP_ERR_TIMEOUT with
  *                   c0 untouched and the hook clears itself. */
 enum gbcp_option { GBCP_OPT_GEMM = 1, GBCP_OPT_BATCH = 2, GBCP_OPT_FFT = 3, GBCP_OPT_XCHUNKS = 4, GBCP_OPT_XC = 5,
-                   GBCP_OPT_TEST_TIMEOUT = 90 };
+                   GBCP_OPT_WFN_CACHE = 6, GBCP_OPT_TEST_TIMEOUT = 90 };
 int gbcp_set_option(gbcp_ctx* ctx, int key, int value);
 /* Queue later work on `stream` (a cudaStream_t; NULL = the context's own
  * stream; the CUDA legacy default stream is cudaStreamLegacy).  Device-pointer calls are ordered only with respect to this stream,

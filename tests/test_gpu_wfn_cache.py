@@ -1,0 +1,73 @@
+"""The wavefunction cache across host-memory calls (GBCP_OPT_WFN_CACHE).
+
+The reference keeps c0 on the device between rhoofr and vpsi, keyed by
+SUM(ABS(c0(:,1))) (cp_cuwfn_put / cp_cuwfn_get, rhoofr_utils.mod.F90:240-245,
+vpsi_utils.mod.F90:278-281).  Here rhoofr's upload is reused by vpsi and by the
+Gram-Schmidt ortho on the same host array: the results equal those of the
+uncached calls bit for bit, the reused calls upload no states (profiler
+timeline), a change of c0's first column is noticed, and setting the option
+again drops the copy.
+"""
+import numpy as np
+import pytest
+
+from cpmd_gb300.synth import make_cell
+
+pytestmark = pytest.mark.gpu
+
+
+def run_step(ctx, c0, f, vpot):
+    rho, ek, cg, cr = ctx.rhoofr(c0, f)
+    c2 = np.zeros_like(c0)
+    ctx.vpsi(c0, c2, f, vpot)
+    ctx.ortho(c0, "gs")
+    return rho, ek, c2, c0
+
+
+def test_cached_step_equals_uncached_and_skips_uploads(gpu_lib):
+    from cpmd_gb300 import Context
+    cl = make_cell("c1", nstate=64)
+    plain = Context(cl.basis, "mixed")
+    cached = Context(cl.basis, "mixed")
+    cached.set_option("wfn_cache", 1)
+    a = run_step(plain, cl.c0.copy(order="F"), cl.f, cl.vpot)
+    cached.profile(True)
+    b = run_step(cached, cl.c0.copy(order="F"), cl.f, cl.vpot)
+    tl = cached.profile_timeline()
+    cached.profile(False)
+    for x, y in zip(a, b):
+        assert np.array_equal(np.asarray(x), np.asarray(y))
+    # only rhoofr's state uploads: vpsi's c2 and ortho's states are not in 'h2d_states' of c0
+    ups = [r for r in tl if r[0] == "h2d_states"]
+    ups_plain = None
+    plain.profile(True)
+    run_step(plain, cl.c0.copy(order="F"), cl.f, cl.vpot)
+    ups_plain = [r for r in plain.profile_timeline() if r[0] == "h2d_states"]
+    plain.profile(False)
+    assert 0 < len(ups) < len(ups_plain)
+
+
+def test_changed_first_column_is_noticed_and_option_drops_copy(gpu_lib):
+    from cpmd_gb300 import Context
+    cl = make_cell("c1", nstate=32)
+    ctx = Context(cl.basis, "fp64")
+    ctx.set_option("wfn_cache", 1)
+    ref = Context(cl.basis, "fp64")
+    c0 = cl.c0.copy(order="F")
+    ctx.rhoofr(c0, cl.f)
+    # the caller changes the first column: the key changes, vpsi uploads again
+    c0[:, 0] *= 1.5
+    c2 = np.zeros_like(c0)
+    ctx.vpsi(c0, c2, cl.f, cl.vpot)
+    c2r = np.zeros_like(c0)
+    ref.vpsi(c0, c2r, cl.f, cl.vpot)
+    assert np.array_equal(c2, c2r)
+    # a change elsewhere keeps the key: the documented remedy is to set the option again
+    ctx.rhoofr(c0, cl.f)
+    c0[:, 5] *= -1.0
+    ctx.set_option("wfn_cache", 1)
+    c2[:] = 0
+    ctx.vpsi(c0, c2, cl.f, cl.vpot)
+    c2r[:] = 0
+    ref.vpsi(c0, c2r, cl.f, cl.vpot)
+    assert np.array_equal(c2, c2r)
