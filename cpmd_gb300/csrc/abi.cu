@@ -444,6 +444,10 @@ int gbcp_set_option(gbcp_ctx* h, int key, int value) {
     c.xc = value;
     return GBCP_OK;
   }
+  if (key == GBCP_OPT_PLANE && (value == 0 || value == 1)) {
+    c.plane = value;
+    return GBCP_OK;
+  }
   if (key == GBCP_OPT_WFN_CACHE && (value == 0 || value == 1)) {
     c.wfn.on = value == 1;
     c.wfn.valid = false;  // setting the option always drops a kept copy

@@ -428,6 +428,7 @@ __global__ void k_decode(GeoDev g, const cx<T>* __restrict__ qbuf, const cx<doub
 }  // namespace gbcp
 
 #include "band_fs.cuh"
+#include "band_plane.cuh"
 
 namespace gbcp {
 namespace band {
@@ -471,10 +472,11 @@ template <> inline const cx<float>* twB_of<float>(Ctx& c, int axis) { return c.t
     default: return FN<T, 0>(__VA_ARGS__);                  \
   }
 
-template <typename T> int ensure_band_buffers(Ctx& c, int npairs) {
+// no_ybuf: the plane kernels run the y and x stages, ybuf is not needed
+template <typename T> int ensure_band_buffers(Ctx& c, int npairs, bool no_ybuf = false) {
   const GeoDev& g = c.geo;
   const size_t zb = sizeof(cx<T>) * (size_t)npairs * g.n3 * g.ncol;
-  const size_t yb = sizeof(cx<T>) * (size_t)npairs * g.n3 * g.n2 * g.nslot;
+  const size_t yb = no_ybuf ? 16 : sizeof(cx<T>) * (size_t)npairs * g.n3 * g.n2 * g.nslot;
   const size_t qb = sizeof(cx<T>) * (size_t)npairs * g.nent;
   if (!ensure(c, c.zbuf, zb) || !ensure(c, c.ybuf, yb) || !ensure(c, c.qbuf, qb)) {
     c.err = "band workspace allocation failed";
@@ -675,6 +677,103 @@ template <typename T, int NC> int launch_zfwd(Ctx& c, int np) {
   return 0;
 }
 
+// ---- plane-fused Y and X stages (FP32, band_plane.cuh) ----
+constexpr size_t kSmemMax = 227 * 1024;
+// largest mesh length with plane kernels: a 240-point plane of a sphere that fills
+// it does not fit in shared memory (and its density tile would spill registers)
+constexpr int kPlaneMaxN = 144;
+// whether the plane kernels run this context's band loop: FP32, four-step plan,
+// equal x and y lengths, the plane fits in shared memory (GBCP_OPT_PLANE on)
+template <typename T, int NC> bool plane_fits_n(const Ctx& c) {
+  if constexpr (sizeof(T) == 4 && NC > 0 && NC <= kPlaneMaxN) {
+    return c.plane && c.nr[0] == c.nr[1] && PlaneLayout<NC>::bytes(3, c.geo.nslot) <= kSmemMax;
+  } else {
+    return false;
+  }
+}
+template <typename T> bool plane_fits(const Ctx& c) {
+  if (c.fft_engine == 2 || c.nr[0] != c.nr[1]) return false;
+  GBCP_DISPATCH(plane_fits_n, T, c.nr[0], c)
+}
+
+template <typename T, int NC> int launch_plane_vx(Ctx& c, int np, int poff, const T* vpotT) {
+  if constexpr (sizeof(T) == 4 && NC > 0 && NC <= kPlaneMaxN) {
+    const GeoDev& g = c.geo;
+    cx<float>* zb = static_cast<cx<float>*>(c.zbuf.p) + (size_t)poff * g.n3 * g.ncol;
+    const size_t sm = PlaneLayout<NC>::bytes(3, g.nslot);
+    allow_smem(k_plane_vx_fs<NC>, sm);
+    ProfScope ps_(c, "k_plane_vx");
+    k_plane_vx_fs<NC><<<dim3(g.n3, np), kThreads, sm, c.stream>>>(g, zb, reinterpret_cast<const float*>(vpotT),
+                                                                  twA_of<float>(c, 1), twA_of<float>(c, 0),
+                                                                  twB_of<float>(c, 0));
+    GBCP_LAUNCH_CHECK(c);
+    return 0;
+  } else {
+    c.err = "plane kernels: FP32 four-step meshes only";
+    return 7;
+  }
+}
+
+// CTAs of the plane density kernel resident on one SM (measured once per mesh)
+template <int NC> int plane_rho_ctas_per_sm(size_t sm) {
+  static int n = 0;
+  if (!n) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_plane_rho_fs<NC>, kThreads, sm) != cudaSuccess || n < 1) {
+      cudaGetLastError();
+      n = 1;
+    }
+  }
+  return n;
+}
+
+template <typename T, int NC>
+int launch_plane_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho, int poff) {
+  if constexpr (sizeof(T) == 4 && NC > 0 && NC <= kPlaneMaxN) {
+    const GeoDev& g = c.geo;
+    using PL = PlaneLayout<NC>;
+    const cx<float>* zb = static_cast<const cx<float>*>(c.zbuf.p) + (size_t)poff * g.n3 * g.ncol;
+    const size_t sm = PL::bytes(2, g.nslot);
+    allow_smem(k_plane_rho_fs<NC>, sm);
+    // pair chunks: the count that minimises the busiest SM's work, as for the x-stage
+    const int per_sm = plane_rho_ctas_per_sm<NC>(sm);
+    const long long slots = (long long)(c.nsm > 0 ? c.nsm : 152) * per_sm;
+    int nchunk = 1;
+    long long best = -1;
+    for (int q = 1; q <= std::min(np, kXrhoMaxChunks); ++q) {
+      const long long cost = (((long long)g.n3 * q + slots - 1) / slots) * ((np + q - 1) / q + 1);
+      if (best < 0 || cost < best) {
+        best = cost;
+        nchunk = q;
+      }
+    }
+    if (c.xr_chunks > 0) nchunk = std::max(1, std::min({c.xr_chunks, np, kXrhoMaxChunks}));
+    const int pchunk = (np + nchunk - 1) / nchunk;
+    nchunk = (np + pchunk - 1) / pchunk;
+    float* part = nullptr;
+    unsigned* tickets = nullptr;
+    if (nchunk > 1) {
+      constexpr size_t tile = (size_t)PL::NB * FS<float, NC>::TB * FS<float, NC>::N2;
+      if (!ensure(c, c.xr_part, sizeof(float) * tile * (size_t)g.n3 * kXrhoMaxChunks)) return 6;
+      const size_t tb = sizeof(unsigned) * (size_t)std::max(g.n3, 1);
+      if (!c.xr_tk.p || c.xr_tk.cap < tb) {
+        if (!ensure(c, c.xr_tk, tb)) return 6;
+        GBCP_CUDA_TRY(c, cudaMemsetAsync(c.xr_tk.p, 0, c.xr_tk.cap, c.stream));
+      }
+      part = static_cast<float*>(c.xr_part.p);
+      tickets = static_cast<unsigned*>(c.xr_tk.p);
+    }
+    ProfScope ps_(c, "k_plane_rho");
+    k_plane_rho_fs<NC><<<dim3(nchunk, g.n3), kThreads, sm, c.stream>>>(g, zb, np, s0, nstate, f, 1.0 / c.omega, rho,
+                                                                       twA_of<float>(c, 1), twA_of<float>(c, 0),
+                                                                       pchunk, part, tickets);
+    GBCP_LAUNCH_CHECK(c);
+    return 0;
+  } else {
+    c.err = "plane kernels: FP32 four-step meshes only";
+    return 7;
+  }
+}
+
 template <typename T>
 int launch_decode(Ctx& c, int np, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, const double* f, int s0,
                   int nstate, int poff = 0) {
@@ -703,6 +802,13 @@ template <typename T> int xvx(Ctx& c, int np, const double* vpot, const T* vpotT
   GBCP_DISPATCH(launch_xvx, T, band_len(c, c.nr[0]), c, np, vpot, vpotT)
 }
 template <typename T> int yfwd(Ctx& c, int np) { GBCP_DISPATCH(launch_yfwd, T, band_len(c, c.nr[1]), c, np) }
+template <typename T> int plane_vx(Ctx& c, int np, const T* vpotT) {
+  GBCP_DISPATCH(launch_plane_vx, T, c.nr[0], c, np, 0, vpotT)
+}
+template <typename T>
+int plane_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho, int poff = 0) {
+  GBCP_DISPATCH(launch_plane_rho, T, c.nr[0], c, np, s0, nstate, f, rho, poff)
+}
 template <typename T> int zfwd(Ctx& c, int np) { GBCP_DISPATCH(launch_zfwd, T, band_len(c, c.nr[2]), c, np) }
 
 // Z stage of pairs [p0, p0 + np): one launch, or, with host staging, one launch per
@@ -733,15 +839,21 @@ inline int launch_pairs(const Ctx& c, int p0, int npairs_total) {
 template <typename T>
 int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho, double* kpart) {
   const int npairs_total = (nstate + 1) / 2;
-  int rc = ensure_band_buffers<T>(c, std::min(c.batch, npairs_total));
+  const bool plane = plane_fits<T>(c);  // y and x stages fused per z-plane, no ybuf
+  int rc = ensure_band_buffers<T>(c, std::min(c.batch, npairs_total), plane);
   if (rc) return rc;
+  // the density x-stage of the pairs [g0, g1) of the launch batch starting at p0
+  auto density = [&](int g0, int g1, int p0b) -> int {
+    return plane ? plane_rho<T>(c, g1 - g0, 2 * g0, nstate, f, rho, g0 - p0b)
+                 : xinv_rho<T>(c, g1 - g0, 2 * g0, nstate, f, rho, g0 - p0b);
+  };
   for (int p0 = 0, np = 0; p0 < npairs_total; p0 += np) {
     np = std::min(c.batch, npairs_total - p0);
     const int s0 = 2 * p0;
     if (!c.batch_ready) {
       if ((rc = zinv<T>(c, c0, ldc, s0, nstate, np, 0, f, kpart))) return rc;
-      if ((rc = yinv<T>(c, np))) return rc;
-      if ((rc = xinv_rho<T>(c, np, s0, nstate, f, rho))) return rc;
+      if (!plane && (rc = yinv<T>(c, np))) return rc;
+      if ((rc = density(p0, p0 + np, p0))) return rc;
     } else {
       // host staging: Z and Y stages of each staging chunk as its states land; the
       // density x-stage (which gains most from many pairs per launch) in two groups
@@ -754,15 +866,15 @@ int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f,
         if (q1 > q0) {
           GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.batch_ready[q], 0));
           if ((rc = zinv<T>(c, c0, ldc, 2 * q0, nstate, q1 - q0, q0 - p0, f, kpart))) return rc;
-          if ((rc = yinv<T>(c, q1 - q0, q0 - p0))) return rc;
+          if (!plane && (rc = yinv<T>(c, q1 - q0, q0 - p0))) return rc;
         }
         const int gend = std::min(b[q + 1], p0 + np);
         if ((q + 1 == split || q + 1 == nq) && gend > g0) {
-          if ((rc = xinv_rho<T>(c, gend - g0, 2 * g0, nstate, f, rho, g0 - p0))) return rc;
+          if ((rc = density(g0, gend, p0))) return rc;
           g0 = gend;
         }
       }
-      if (g0 < p0 + np && (rc = xinv_rho<T>(c, p0 + np - g0, 2 * g0, nstate, f, rho, g0 - p0))) return rc;
+      if (g0 < p0 + np && (rc = density(g0, p0 + np, p0))) return rc;
     }
   }
   return 0;
@@ -772,7 +884,8 @@ template <typename T>
 int vpsi_t(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, const double* f, const double* vpot,
            int nstate) {
   const int npairs_total = (nstate + 1) / 2;
-  int rc = ensure_band_buffers<T>(c, std::min(c.batch, npairs_total));
+  const bool plane = plane_fits<T>(c);  // y and x stages fused per z-plane, no ybuf
+  int rc = ensure_band_buffers<T>(c, std::min(c.batch, npairs_total), plane);
   if (rc) return rc;
   // V(r) in the transform precision, converted once per call before the first
   // x-stage (with host staging V(r) arrives behind the first chunk of states)
@@ -794,10 +907,15 @@ int vpsi_t(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, cons
     np = launch_pairs(c, p0, npairs_total);
     const int s0 = 2 * p0;
     if ((rc = zinv_staged<T>(c, c0, ldc, p0, nstate, np))) return rc;
-    if ((rc = yinv<T>(c, np))) return rc;
-    if (p0 == 0 && (rc = prepare_v())) return rc;
-    if ((rc = xvx<T>(c, np, vpot, vT))) return rc;
-    if ((rc = yfwd<T>(c, np))) return rc;
+    if (plane) {
+      if (p0 == 0 && (rc = prepare_v())) return rc;
+      if ((rc = plane_vx<T>(c, np, vT))) return rc;
+    } else {
+      if ((rc = yinv<T>(c, np))) return rc;
+      if (p0 == 0 && (rc = prepare_v())) return rc;
+      if ((rc = xvx<T>(c, np, vpot, vT))) return rc;
+      if ((rc = yfwd<T>(c, np))) return rc;
+    }
     if ((rc = zfwd<T>(c, np))) return rc;
     if (!c.batch_ready) {
       if ((rc = launch_decode<T>(c, np, c0, ldc, c2, ldc2, f, s0, nstate))) return rc;

@@ -124,6 +124,7 @@ struct Ctx {
   int xr_chunks = 0;   // density x-stage pair chunks: 0 = chosen per launch
   int xc = 0;          // energy functional: 0 LDA (Slater + Perdew-Zunger), 1 PBE
   int fft_engine = 0;  // band-loop FFTs: 0 four-step where a plan exists, else Stockham; 2 Stockham always
+  int plane = 1;       // FP32 band loop: y and x stages fused per z-plane where the plane fits in shared memory
   int test_stall = 0;  // test hook: the next tensor-core overlap issues no loads and times out (one call)
   WfnCache wfn;        // host wavefunction kept on the device between host-memory calls
   cudaStream_t stream = nullptr;  // stream all work is queued on

@@ -98,6 +98,10 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  *   GBCP_OPT_XC     exchange-correlation functional of gbcp_energy: 0 = LDA
  *                   (Slater + Perdew-Zunger, the default), 1 = PBE (gradient-
  *                   corrected, the reference's vofrhob/gcener route);
+ *   GBCP_OPT_PLANE  FP32 band loop: 1 (the default) = the y and x stages of
+ *                   each z-plane in one kernel, the plane held in shared memory
+ *                   (no y-stage buffer in HBM), where the x and y lengths are
+ *                   equal and the plane fits; 0 = the three-stage kernels;
  *   GBCP_OPT_WFN_CACHE  1 = keep the device copy of a host-memory c0 that
  *                   gbcp_rhoofr uploads, and let the following gbcp_vpsi and
  *                   gbcp_ortho (Gram-Schmidt) on the same array use it instead
@@ -114,7 +118,7 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  *                   about a millisecond; the call returns GBCP_ERR_TIMEOUT with
  *                   c0 untouched and the hook clears itself. */
 enum gbcp_option { GBCP_OPT_GEMM = 1, GBCP_OPT_BATCH = 2, GBCP_OPT_FFT = 3, GBCP_OPT_XCHUNKS = 4, GBCP_OPT_XC = 5,
-                   GBCP_OPT_WFN_CACHE = 6, GBCP_OPT_TEST_TIMEOUT = 90 };
+                   GBCP_OPT_WFN_CACHE = 6, GBCP_OPT_PLANE = 7, GBCP_OPT_TEST_TIMEOUT = 90 };
 int gbcp_set_option(gbcp_ctx* ctx, int key, int value);
 /* Queue later work on `stream` (a cudaStream_t; NULL = the context's own
  * stream; the CUDA legacy default stream is cudaStreamLegacy).  Device-pointer calls are ordered only with respect to this stream,

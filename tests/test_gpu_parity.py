@@ -149,14 +149,16 @@ def test_vpsi_accumulates_and_odd_states(gpu_lib, nstate):
                                           (48, 30.0, 10.26), (60, 40.0, 10.26), (64, 40.0, 10.26),
                                           (72, 50.0, 10.26), (80, 50.0, 10.26), (96, 60.0, 10.26),
                                           (144, 50.0, 30.78), (240, 70.0, 41.04)])
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_band_loop_all_mesh_plans(gpu_lib, nr, ecut, alat, precision):
-    """Four-step plans (32..240) and the run-time Stockham plan (20, 24) give the oracle's rho and c2."""
+@pytest.mark.parametrize("precision,plane", [("fp64", 0), ("mixed", 0), ("mixed", 1)])
+def test_band_loop_all_mesh_plans(gpu_lib, nr, ecut, alat, precision, plane):
+    """Four-step plans (32..240) and the run-time Stockham plan (20, 24) give the oracle's rho and c2;
+    in FP32 both with the three-stage kernels and with the plane-fused y/x stages (where they apply)."""
     cl = make_small_cell(alat, nr, ecut, 5 if nr < 144 else 3, seed=nr)
     b = cl.basis
     rho_r, *_ = O.rhoofr(cl.c0, cl.f, b.mill, b.nr, b.kr, b.omega, b.hg, b.tpiba2, b.geq0)
     c2_r = O.vpsi(cl.c0, np.zeros_like(cl.c0), cl.f, cl.vpot, b.mill, b.nr, b.hg, b.tpiba2, b.geq0)
     ctx = ctx_for(b, precision)
+    ctx.set_option("plane", plane)
     rho, *_ = ctx.rhoofr(cl.c0, cl.f)
     c2 = np.zeros_like(cl.c0)
     ctx.vpsi(cl.c0, c2, cl.f, cl.vpot)
