@@ -686,7 +686,8 @@ constexpr int kPlaneMaxN = 144;
 // equal x and y lengths, the plane fits in shared memory (GBCP_OPT_PLANE on)
 template <typename T, int NC> bool plane_fits_n(const Ctx& c) {
   if constexpr (sizeof(T) == 4 && NC > 0 && NC <= kPlaneMaxN) {
-    return c.plane && c.nr[0] == c.nr[1] && PlaneLayout<NC>::bytes(3, c.geo.nslot) <= kSmemMax;
+    return c.plane && c.nr[0] == c.nr[1] && PlaneLayout<NC>::bytes(3, c.geo.nslot) <= kSmemMax &&
+           PlaneLayout<NC>::bytes(2, c.geo.nslot, 2) <= kSmemMax;
   } else {
     return false;
   }
@@ -718,7 +719,8 @@ template <typename T, int NC> int launch_plane_vx(Ctx& c, int np, int poff, cons
 template <int NC> int plane_rho_ctas_per_sm(size_t sm) {
   static int n = 0;
   if (!n) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_plane_rho_fs<NC>, kThreads, sm) != cudaSuccess || n < 1) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_plane_rho_fs<NC>, kPlaneRhoThreads, sm) != cudaSuccess ||
+        n < 1) {
       cudaGetLastError();
       n = 1;
     }
@@ -732,7 +734,7 @@ int launch_plane_rho(Ctx& c, int np, int s0, int nstate, const double* f, double
     const GeoDev& g = c.geo;
     using PL = PlaneLayout<NC>;
     const cx<float>* zb = static_cast<const cx<float>*>(c.zbuf.p) + (size_t)poff * g.n3 * g.ncol;
-    const size_t sm = PL::bytes(2, g.nslot);
+    const size_t sm = PL::bytes(2, g.nslot, 2);
     allow_smem(k_plane_rho_fs<NC>, sm);
     // pair chunks: the count that minimises the busiest SM's work, as for the x-stage
     const int per_sm = plane_rho_ctas_per_sm<NC>(sm);
@@ -752,7 +754,7 @@ int launch_plane_rho(Ctx& c, int np, int s0, int nstate, const double* f, double
     float* part = nullptr;
     unsigned* tickets = nullptr;
     if (nchunk > 1) {
-      constexpr size_t tile = (size_t)PL::NB * FS<float, NC>::TB * FS<float, NC>::N2;
+      constexpr size_t tile = (size_t)2 * ((PL::NB + 1) / 2) * FS<float, NC>::TB * FS<float, NC>::N2;
       if (!ensure(c, c.xr_part, sizeof(float) * tile * (size_t)g.n3 * kXrhoMaxChunks)) return 6;
       const size_t tb = sizeof(unsigned) * (size_t)std::max(g.n3, 1);
       if (!c.xr_tk.p || c.xr_tk.cap < tb) {
@@ -763,7 +765,8 @@ int launch_plane_rho(Ctx& c, int np, int s0, int nstate, const double* f, double
       tickets = static_cast<unsigned*>(c.xr_tk.p);
     }
     ProfScope ps_(c, "k_plane_rho");
-    k_plane_rho_fs<NC><<<dim3(nchunk, g.n3), kThreads, sm, c.stream>>>(g, zb, np, s0, nstate, f, 1.0 / c.omega, rho,
+    k_plane_rho_fs<NC><<<dim3(nchunk, g.n3), kPlaneRhoThreads, sm, c.stream>>>(g, zb, np, s0, nstate, f, 1.0 / c.omega,
+                                                                               rho,
                                                                        twA_of<float>(c, 1), twA_of<float>(c, 0),
                                                                        pchunk, part, tickets);
     GBCP_LAUNCH_CHECK(c);

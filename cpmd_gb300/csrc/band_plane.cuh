@@ -22,21 +22,27 @@ template <int N> struct PlaneLayout {
   using P = FS<float, N>;
   static constexpr int XEL = (P::L * P::LS > P::L * P::XS) ? P::L * P::LS : P::L * P::XS;
   static constexpr int NB = (N + P::L - 1) / P::L;  // x-row blocks of a plane
-  __host__ __device__ static constexpr size_t bytes(int tables, int nslot) {
-    return sizeof(cx<float>) * ((size_t)tables * N + (size_t)XEL + (size_t)nslot * P::LS);
+  // `tiles` exchange tiles (one per group of kThreads threads)
+  __host__ __device__ static constexpr size_t bytes(int tables, int nslot, int tiles = 1) {
+    return sizeof(cx<float>) * ((size_t)tables * N + (size_t)tiles * XEL + (size_t)nslot * P::LS);
   }
 };
 
 // inverse y-transforms of the slot lines of one z-plane: zrow (sphere columns of
-// the plane) -> Pl[s * LS + y]; ends with a barrier
+// the plane) -> Pl[s * LS + y]; ends with a barrier.  The CTA is nh groups of
+// kThreads threads (tt = thread within the group, h = group); group h transforms
+// the slot-line blocks h, h + nh, ... in its own exchange tile X, every group
+// running the same number of barriers.
 template <int N>
 __device__ __forceinline__ void plane_yinv(const GeoDev& g, const cx<float>* __restrict__ zrow, const cx<float>* twy,
-                                           cx<float>* Pl, cx<float>* X) {
+                                           cx<float>* Pl, cx<float>* X, int tt = threadIdx.x, int h = 0, int nh = 1) {
   using P = FS<float, N>;
-  for (int sb = 0; sb < g.nslot; sb += P::L) {
+  const int nblk = (g.nslot + P::L - 1) / P::L;
+  for (int it = 0; it < (nblk + nh - 1) / nh; ++it) {
+    const int sb = (it * nh + h) * P::L;  // past the last block: every s >= nslot, nothing is written
 #pragma unroll
     for (int ia = 0; ia < P::IA; ++ia) {
-      const int t = threadIdx.x + ia * kThreads;
+      const int t = tt + ia * kThreads;
       if (t < P::TA) {
         const int n2 = t / P::L, l = t - n2 * P::L, s = sb + l;
         int c0s = 0, gylo = 0, ncs = 0;
@@ -57,7 +63,7 @@ __device__ __forceinline__ void plane_yinv(const GeoDev& g, const cx<float>* __r
     __syncthreads();
 #pragma unroll
     for (int ib = 0; ib < P::IB; ++ib) {
-      const int t = threadIdx.x + ib * kThreads;
+      const int t = tt + ib * kThreads;
       if (t < P::TB) {
         const int k1 = t / P::L, l = t - k1 * P::L, s = sb + l;
         cx<float> w[P::N2];
@@ -76,11 +82,11 @@ __device__ __forceinline__ void plane_yinv(const GeoDev& g, const cx<float>* __r
 // step A of the inverse x-transform of rows y0 .. y0+L-1: the slots of row y from Pl
 template <int N>
 __device__ __forceinline__ void plane_xrow_a(const GeoDev& g, const cx<float>* Pl, int y0, const cx<float>* twx,
-                                             cx<float>* X) {
+                                             cx<float>* X, int tt = threadIdx.x) {
   using P = FS<float, N>;
 #pragma unroll
   for (int ia = 0; ia < P::IA; ++ia) {
-    const int t = threadIdx.x + ia * kThreads;
+    const int t = tt + ia * kThreads;
     if (t < P::TA) {
       const int l = t / P::N2, n2 = t - l * P::N2, y = y0 + l;
       cx<float> v[P::N1];
@@ -199,83 +205,92 @@ __global__ void __launch_bounds__(kThreads, 2) k_plane_vx_fs(GeoDev g, cx<float>
 }
 
 // CTA (chunk, z): rhoofr's y-inverse and x-inverse of plane z for the pairs
-// [chunk*pchunk, ..), the density of the plane in registers (NB x N2 per
-// thread, the x-stage map of k_xrho_fs per row block).  One chunk: added to rho
+// [chunk*pchunk, ..).  Two groups of kThreads threads share the plane, each with
+// its own exchange tile: the slot-line blocks and the x-row blocks alternate
+// between them, so every barrier covers two blocks' work and twice the warps are
+// resident.  The density of the plane builds up in registers (the x-stage map of
+// k_xrho_fs; row blocks b = h, h + 2, ... of group h).  One chunk: added to rho
 // directly; several: partial planes, and the last CTA of the plane to finish
-// (ticket counter) adds them in chunk order, so rho does not depend on the
-// order the CTAs run in.
+// (ticket counter) adds them in chunk order, so rho does not depend on the order
+// the CTAs run in.
+constexpr int kPlaneRhoThreads = 2 * kThreads;
 template <int N>
-__global__ void __launch_bounds__(kThreads, 1) k_plane_rho_fs(GeoDev g, const cx<float>* __restrict__ zbuf,
-                                                             int npairs, int s0, int nstate,
-                                                             const double* __restrict__ f, double inv_omega,
-                                                             double* __restrict__ rho,
-                                                             const cx<float>* __restrict__ twAyg,
-                                                             const cx<float>* __restrict__ twAxg, int pchunk,
-                                                             float* __restrict__ part, unsigned* __restrict__ tickets) {
+__global__ void __launch_bounds__(kPlaneRhoThreads, 1) k_plane_rho_fs(GeoDev g, const cx<float>* __restrict__ zbuf,
+                                                                     int npairs, int s0, int nstate,
+                                                                     const double* __restrict__ f, double inv_omega,
+                                                                     double* __restrict__ rho,
+                                                                     const cx<float>* __restrict__ twAyg,
+                                                                     const cx<float>* __restrict__ twAxg, int pchunk,
+                                                                     float* __restrict__ part,
+                                                                     unsigned* __restrict__ tickets) {
   using P = FS<float, N>;
   using PL = PlaneLayout<N>;
   constexpr int NB = PL::NB;
+  constexpr int NBH = (NB + 1) / 2;  // row blocks of one group
   static_assert(P::IB == 1, "density rows: one step-B task per thread");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<float>* twy = reinterpret_cast<cx<float>*>(smem_raw);
   cx<float>* twx = twy + N;
-  cx<float>* X = twx + N;
-  cx<float>* Pl = X + PL::XEL;
+  const int h = threadIdx.x / kThreads, tt = threadIdx.x - h * kThreads;
+  cx<float>* X = twx + N + h * PL::XEL;
+  cx<float>* Pl = twx + N + 2 * PL::XEL;
   __shared__ float fw[2 * kMaxBatch];
   __shared__ int last_sh;
   const int nchunk = gridDim.x, chunk = blockIdx.x, z = blockIdx.y;
   const int p0 = chunk * pchunk, p1 = min(npairs, p0 + pchunk);
-  load_table(twy, twAyg, N);
-  load_table(twx, twAxg, N);
-  for (int i = threadIdx.x; i < 2 * (p1 - p0); i += kThreads) {
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    twy[i] = twAyg[i];
+    twx[i] = twAxg[i];
+  }
+  for (int i = threadIdx.x; i < 2 * (p1 - p0); i += blockDim.x) {
     const int is = s0 + 2 * p0 + i;
     fw[i] = d2f_int(is < nstate ? f[is] * inv_omega : 0.0);
   }
   __syncthreads();
-  const int t = threadIdx.x;
-  const int lb = t / P::N1, k1 = t - lb * P::N1;
-  float acc[NB][P::N2];
+  const int lb = tt / P::N1, k1 = tt - lb * P::N1;
+  float acc[NBH][P::N2];
 #pragma unroll
-  for (int b = 0; b < NB; ++b)
+  for (int b = 0; b < NBH; ++b)
 #pragma unroll
     for (int k2 = 0; k2 < P::N2; ++k2) acc[b][k2] = 0.f;
   for (int pair = p0; pair < p1; ++pair) {
-    plane_yinv<N>(g, zbuf + ((size_t)pair * g.n3 + z) * g.ncol, twy, Pl, X);
+    plane_yinv<N>(g, zbuf + ((size_t)pair * g.n3 + z) * g.ncol, twy, Pl, X, tt, h, 2);
     const float f1 = fw[2 * (pair - p0)], f2 = fw[2 * (pair - p0) + 1];
 #pragma unroll
-    for (int b = 0; b < NB; ++b) {
-      plane_xrow_a<N>(g, Pl, b * P::L, twx, X);
+    for (int bh = 0; bh < NBH; ++bh) {
+      const int b = 2 * bh + h;  // this group's row block (past the last one: rows >= N, zeros)
+      plane_xrow_a<N>(g, Pl, b * P::L, twx, X, tt);
       __syncthreads();
-      if (t < P::TB) {
+      if (tt < P::TB) {
         cx<float> w[P::N2];
         fs_step_b<1, float, P::N1, P::N2, P::XP>(X + lb * P::XS, k1, w);
 #pragma unroll
-        for (int k2 = 0; k2 < P::N2; ++k2) acc[b][k2] += f1 * w[k2].x * w[k2].x + f2 * w[k2].y * w[k2].y;
+        for (int k2 = 0; k2 < P::N2; ++k2) acc[bh][k2] += f1 * w[k2].x * w[k2].x + f2 * w[k2].y * w[k2].y;
       }
       __syncthreads();
     }
   }
   if (nchunk == 1) {
-    if (t < P::TB) {
+    if (tt < P::TB) {
 #pragma unroll
-      for (int b = 0; b < NB; ++b) {
-        const int y = b * P::L + lb;
+      for (int bh = 0; bh < NBH; ++bh) {
+        const int y = (2 * bh + h) * P::L + lb;
         if (y < N) {
           double* rrow = rho + (size_t)g.k1 * (y + (size_t)g.k2 * z);
 #pragma unroll
-          for (int k2 = 0; k2 < P::N2; ++k2) rrow[k1 + P::N1 * k2] += f2d_int(acc[b][k2]);
+          for (int k2 = 0; k2 < P::N2; ++k2) rrow[k1 + P::N1 * k2] += f2d_int(acc[bh][k2]);
         }
       }
     }
     return;
   }
-  constexpr int TILE = NB * P::TB * P::N2;
+  constexpr int TILE = 2 * NBH * P::TB * P::N2;
   float* mine = part + ((size_t)z * nchunk + chunk) * TILE;
-  if (t < P::TB) {
+  if (tt < P::TB) {
 #pragma unroll
-    for (int b = 0; b < NB; ++b)
+    for (int bh = 0; bh < NBH; ++bh)
 #pragma unroll
-      for (int k2 = 0; k2 < P::N2; ++k2) mine[(b * P::N2 + k2) * P::TB + t] = acc[b][k2];
+      for (int k2 = 0; k2 < P::N2; ++k2) mine[((h * NBH + bh) * P::N2 + k2) * P::TB + tt] = acc[bh][k2];
   }
   __threadfence();
   __syncthreads();
@@ -283,17 +298,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_plane_rho_fs(GeoDev g, const cx
   __syncthreads();
   if (!last_sh) return;
   __threadfence();
-  if (t < P::TB) {
+  if (tt < P::TB) {
     const float* tp = part + (size_t)z * nchunk * TILE;
 #pragma unroll
-    for (int b = 0; b < NB; ++b) {
-      const int y = b * P::L + lb;
+    for (int bh = 0; bh < NBH; ++bh) {
+      const int y = (2 * bh + h) * P::L + lb;
       if (y >= N) continue;
       double* rrow = rho + (size_t)g.k1 * (y + (size_t)g.k2 * z);
 #pragma unroll
       for (int k2 = 0; k2 < P::N2; ++k2) {
         double sum = 0.0;
-        for (int q = 0; q < nchunk; ++q) sum += f2d_int(__ldcg(tp + (size_t)q * TILE + (b * P::N2 + k2) * P::TB + t));
+        for (int q = 0; q < nchunk; ++q)
+          sum += f2d_int(__ldcg(tp + (size_t)q * TILE + ((h * NBH + bh) * P::N2 + k2) * P::TB + tt));
         rrow[k1 + P::N1 * k2] += sum;
       }
     }
