@@ -444,7 +444,7 @@ int gbcp_set_option(gbcp_ctx* h, int key, int value) {
     c.xc = value;
     return GBCP_OK;
   }
-  if (key == GBCP_OPT_PLANE && (value == 0 || value == 1)) {
+  if (key == GBCP_OPT_PLANE && value >= 0 && value <= 3) {
     c.plane = value;
     return GBCP_OK;
   }

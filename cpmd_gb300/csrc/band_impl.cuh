@@ -686,7 +686,7 @@ constexpr int kPlaneMaxN = 144;
 // equal x and y lengths, the plane fits in shared memory (GBCP_OPT_PLANE on)
 template <typename T, int NC> bool plane_fits_n(const Ctx& c) {
   if constexpr (sizeof(T) == 4 && NC > 0 && NC <= kPlaneMaxN) {
-    return c.plane && c.nr[0] == c.nr[1] && PlaneLayout<NC>::bytes(3, c.geo.nslot) <= kSmemMax &&
+    return c.nr[0] == c.nr[1] && PlaneLayout<NC>::bytes(3, c.geo.nslot) <= kSmemMax &&
            PlaneLayout<NC>::bytes(2, c.geo.nslot, 2) <= kSmemMax;
   } else {
     return false;
@@ -842,7 +842,7 @@ inline int launch_pairs(const Ctx& c, int p0, int npairs_total) {
 template <typename T>
 int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f, double* rho, double* kpart) {
   const int npairs_total = (nstate + 1) / 2;
-  const bool plane = plane_fits<T>(c);  // y and x stages fused per z-plane, no ybuf
+  const bool plane = (c.plane & 2) && plane_fits<T>(c);  // y and x stages fused per z-plane, no ybuf
   int rc = ensure_band_buffers<T>(c, std::min(c.batch, npairs_total), plane);
   if (rc) return rc;
   // the density x-stage of the pairs [g0, g1) of the launch batch starting at p0
@@ -887,7 +887,7 @@ template <typename T>
 int vpsi_t(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, const double* f, const double* vpot,
            int nstate) {
   const int npairs_total = (nstate + 1) / 2;
-  const bool plane = plane_fits<T>(c);  // y and x stages fused per z-plane, no ybuf
+  const bool plane = (c.plane & 1) && plane_fits<T>(c);  // y and x stages fused per z-plane, no ybuf
   int rc = ensure_band_buffers<T>(c, std::min(c.batch, npairs_total), plane);
   if (rc) return rc;
   // V(r) in the transform precision, converted once per call before the first

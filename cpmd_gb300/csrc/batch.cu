@@ -310,53 +310,87 @@ int gbcp_batch_tune(gbcp_batch* b, const gbcp_cell_io* io, int flags, char* repo
       if (bt < npairs && bt <= gbcp::kMaxBatch) batches.push_back(bt);
     if (npairs <= gbcp::kMaxBatch) batches.push_back(npairs);
     float best = 1e30f, t = 0.f;
-    int best_e = c.fft_engine, best_b = c.batch, best_g = c.gemm_mode;
+    int best_e = c.fft_engine, best_b = c.batch, best_g = c.gemm_mode, best_p = c.plane;
+    int best_ks = c.oz_ksplit, best_rg = c.oz_rgrid;
     const int band_flags = flags & (GBCP_STEP_RHOOFR | GBCP_STEP_VPSI);
-    char line[256];
+    // plane-fused y/x stages (FP32, four-step meshes whose plane fits): none, vpsi,
+    // rhoofr or both
+    std::vector<int> planes{0};
+    if (c.precision == GBCP_PREC_MIXED) planes = {0, 1, 2, 3};
+    char line[320];
     if (band_flags) {
       for (int e : engines)
-        for (int bt : batches) {
-          c.fft_engine = e;
-          c.batch = bt;
-          if ((rc = time_cell(b, c, xt, band_flags, b->d_out + 2 * i0, b->d_status + i0, &t))) break;
-          if (t < best) {
-            best = t;
-            best_e = e;
-            best_b = bt;
+        for (int bt : batches)
+          for (int pl : planes) {
+            if (e != 0 && pl != 0) continue;  // the plane kernels are four-step kernels
+            c.fft_engine = e;
+            c.batch = bt;
+            c.plane = pl;
+            if ((rc = time_cell(b, c, xt, band_flags, b->d_out + 2 * i0, b->d_status + i0, &t))) break;
+            if (t < best) {
+              best = t;
+              best_e = e;
+              best_b = bt;
+              best_p = pl;
+            }
           }
-        }
       c.fft_engine = best_e;
       c.batch = best_b;
+      c.plane = best_p;
     }
     float best_o = 0.f;
     if (!rc && (flags & GBCP_STEP_ORTHO)) {
       best_o = 1e30f;
-      for (int g : {0, 1}) {
-        c.gemm_mode = g;
+      // GEMM engine, and for the split GEMM its partition: K splits of the overlap
+      // tiles and persistent CTAs of C U^-1 (many cells share the SMs in a batch)
+      struct Part {
+        int g, ks, rg;
+      };
+      std::vector<Part> parts{{0, 0, 0}};
+      for (int ks : {0, 1, 2, 4, 8})
+        for (int rg : {0, 16, 38, 76}) parts.push_back({1, ks, rg});
+      for (const Part& q : parts) {
+        c.gemm_mode = q.g;
+        c.oz_ksplit = q.ks;
+        c.oz_rgrid = q.rg;
         if ((rc = time_cell(b, c, xt, GBCP_STEP_ORTHO, b->d_out + 2 * i0, b->d_status + i0, &t))) break;
         if (t < best_o) {
           best_o = t;
-          best_g = g;
+          best_g = q.g;
+          best_ks = q.ks;
+          best_rg = q.rg;
         }
       }
       c.gemm_mode = best_g;
+      c.oz_ksplit = best_ks;
+      c.oz_rgrid = best_rg;
     }
     cudaStreamSynchronize(b->s0);
     cudaFree(t0);
     if (t2) cudaFree(t2);
     if (rc) return fail(b, rc, "batch tune: " + c.err);
-    std::snprintf(line, sizeof(line), "mesh %dx%dx%d ngw %d nstate %d (%d cells): fft %s, %d pairs/launch, ortho %s; "
+    static const char* plane_name[4] = {"three-stage", "plane vpsi", "plane rhoofr", "plane rhoofr+vpsi"};
+    char gemm[64];
+    if (best_g == 1)
+      std::snprintf(gemm, sizeof(gemm), "tcgen05 (K splits %s%d, C M CTAs %s%d)", best_ks ? "" : "auto ",
+                    best_ks, best_rg ? "" : "auto ", best_rg);
+    else
+      std::snprintf(gemm, sizeof(gemm), "fp64-simt");
+    std::snprintf(line, sizeof(line), "mesh %dx%dx%d ngw %d nstate %d (%d cells): fft %s %s, %d pairs/launch, ortho %s; "
                                       "band %.3f ms, ortho %.3f ms\n",
                   c.nr[0], c.nr[1], c.nr[2], c.ngw, x.nstate,
                   (int)std::count(b->klass.begin(), b->klass.end(), (int)k), best_e == 0 ? "four-step" : "stockham",
-                  best_b, best_g == 1 ? "tcgen05" : "fp64-simt", band_flags ? best : 0.f, best_o);
+                  plane_name[best_p & 3], best_b, gemm, band_flags ? best : 0.f, best_o);
     b->report += line;
     for (int i = 0; i < n; ++i)
       if (b->klass[i] == (int)k) {
         Ctx& ci = b->cells[i]->c;
         ci.fft_engine = best_e;
         ci.batch = best_b;
+        ci.plane = best_p;
         ci.gemm_mode = best_g;
+        ci.oz_ksplit = best_ks;
+        ci.oz_rgrid = best_rg;
       }
   }
   if (report && report_len > 0) {

@@ -124,8 +124,10 @@ struct Ctx {
   int xr_chunks = 0;   // density x-stage pair chunks: 0 = chosen per launch
   int xc = 0;          // energy functional: 0 LDA (Slater + Perdew-Zunger), 1 PBE
   int fft_engine = 0;  // band-loop FFTs: 0 four-step where a plan exists, else Stockham; 2 Stockham always
-  int plane = 1;       // FP32 band loop: y and x stages fused per z-plane where the plane fits in shared memory
+  int plane = 1;       // FP32 band loop, y and x stages fused per z-plane where the plane fits: bit 0 vpsi, bit 1 rhoofr
   int test_stall = 0;  // test hook: the next tensor-core overlap issues no loads and times out (one call)
+  int oz_ksplit = 0;   // split GEMM partition: K splits per overlap tile (0 = fill the SMs)
+  int oz_rgrid = 0;    // split GEMM partition: persistent CTAs of C M (0 = one per SM)
   WfnCache wfn;        // host wavefunction kept on the device between host-memory calls
   cudaStream_t stream = nullptr;  // stream all work is queued on
   cudaStream_t own = nullptr;     // the context's own stream

@@ -721,7 +721,9 @@ int ovlap_tc(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S, unsig
   int ntiles = 0;
   for (int ib = 0; ib < nib; ++ib) ntiles += std::max(0, njb - OZ_NB * ib);
   const int total_subs = (K + OZ_KS - 1) / OZ_KS;
-  int nsplit = std::max(1, std::min((total_subs + OZ_SUBS - 1) / OZ_SUBS, (c.nsm > 0 ? c.nsm : 148) / std::max(1, ntiles)));
+  // K splits per output tile: enough CTAs to fill the SMs, or the tuned count (c.oz_ksplit)
+  const int want = c.oz_ksplit > 0 ? c.oz_ksplit : (c.nsm > 0 ? c.nsm : 148) / std::max(1, ntiles);
+  int nsplit = std::max(1, std::min((total_subs + OZ_SUBS - 1) / OZ_SUBS, want));
   int subs_per = (total_subs + nsplit - 1) / nsplit;
   subs_per = ((subs_per + OZ_SUBS - 1) / OZ_SUBS) * OZ_SUBS;
   nsplit = (total_subs + subs_per - 1) / subs_per;
@@ -904,10 +906,9 @@ int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, 
   {
     allow_smem(k_oz_tc, OZ_SMEM);
     const int ntiles = ((rows + OZ_M - 1) / OZ_M) * ((n + OZ_N - 1) / OZ_N);
-    int dev = 0, nsm = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int grid = std::max(1, std::min(ntiles, nsm));
+    const int nsm = c.nsm > 0 ? c.nsm : 148;
+    // persistent CTAs: one per SM, or the tuned count (c.oz_rgrid)
+    const int grid = std::max(1, std::min(ntiles, c.oz_rgrid > 0 ? c.oz_rgrid : nsm));
     ProfScope ps_(c, "k_ozaki_rmul");
     GBCP_LAUNCH_PDL(c, k_oz_tc, dim3(grid), dim3(OZ_THREADS), OZ_SMEM, ma, mb, p);
   }

@@ -98,10 +98,11 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  *   GBCP_OPT_XC     exchange-correlation functional of gbcp_energy: 0 = LDA
  *                   (Slater + Perdew-Zunger, the default), 1 = PBE (gradient-
  *                   corrected, the reference's vofrhob/gcener route);
- *   GBCP_OPT_PLANE  FP32 band loop: 1 (the default) = the y and x stages of
- *                   each z-plane in one kernel, the plane held in shared memory
- *                   (no y-stage buffer in HBM), where the x and y lengths are
- *                   equal and the plane fits; 0 = the three-stage kernels;
+ *   GBCP_OPT_PLANE  FP32 band loop: the y and x stages of each z-plane in one
+ *                   kernel, the plane held in shared memory (no y-stage buffer
+ *                   in HBM), where the x and y lengths are equal and the plane
+ *                   fits; bit 0 for vpsi, bit 1 for rhoofr (default 1: vpsi only,
+ *                   the faster split on the 120^3 cell); 0 = three-stage kernels;
  *   GBCP_OPT_WFN_CACHE  1 = keep the device copy of a host-memory c0 that
  *                   gbcp_rhoofr uploads, and let the following gbcp_vpsi and
  *                   gbcp_ortho (Gram-Schmidt) on the same array use it instead

@@ -149,7 +149,7 @@ def test_vpsi_accumulates_and_odd_states(gpu_lib, nstate):
                                           (48, 30.0, 10.26), (60, 40.0, 10.26), (64, 40.0, 10.26),
                                           (72, 50.0, 10.26), (80, 50.0, 10.26), (96, 60.0, 10.26),
                                           (144, 50.0, 30.78), (240, 70.0, 41.04)])
-@pytest.mark.parametrize("precision,plane", [("fp64", 0), ("mixed", 0), ("mixed", 1)])
+@pytest.mark.parametrize("precision,plane", [("fp64", 0), ("mixed", 0), ("mixed", 3)])
 def test_band_loop_all_mesh_plans(gpu_lib, nr, ecut, alat, precision, plane):
     """Four-step plans (32..240) and the run-time Stockham plan (20, 24) give the oracle's rho and c2;
     in FP32 both with the three-stage kernels and with the plane-fused y/x stages (where they apply)."""

@@ -274,7 +274,7 @@ def test_c1_plane_kernels_match_three_stage(gpu_lib, c1, mode):
     import torch
     cl, _ = c1
     out = {}
-    for plane in (0, 1):
+    for plane in (0, 3):                   # three-stage kernels; plane kernels in rhoofr and vpsi
         ctx = ctx_for(cl.basis, "mixed")
         ctx.set_option("plane", plane)
         if mode == "device":
@@ -288,6 +288,6 @@ def test_c1_plane_kernels_match_three_stage(gpu_lib, c1, mode):
             c2 = np.zeros_like(cl.c0)
             ctx.vpsi(cl.c0, c2, cl.f, cl.vpot)
             out[plane] = (rho, c2, ek)
-    assert rel(out[1][0], out[0][0]) < 1e-6
-    assert rel(out[1][1], out[0][1]) < 1e-6
-    assert out[1][2] == out[0][2]          # E_kin comes from the Z stage, the same in both
+    assert rel(out[3][0], out[0][0]) < 1e-6
+    assert rel(out[3][1], out[0][1]) < 1e-6
+    assert out[3][2] == out[0][2]          # E_kin comes from the Z stage, the same in both
