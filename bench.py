@@ -621,12 +621,38 @@ def run_extras(args, dev):
             ctx.fnonloc(c2, cl.f, fnl, p["twnl"], p["eigr"], p["nghtol"], p["wsg"])
             ctx.ortho(c, "lowdin")
         ms = _timed_loop(step, 3 if prec == "mixed" else 1, 2 if prec == "mixed" else 1)
+        if prec == "mixed":
+            # per-kernel CUDA-event times of one step; the tensor-core GEMMs against the sustained peak
+            ctx.profile(True)
+            step()
+            kp = ctx.profile_read()
+            ctx.profile(False)
         rh, ek, _, _ = ctx.rhoofr(c, cl.f, rho)
         energies[prec] = ek + dv * float((rh * cl.vpot).sum())
         scond = ctx.ortho(c, "lowdin")          # max|S - I| of the orthonormalised states
         r[prec] = {"state_applies_per_s": cl.nstate / (ms / 1e3), "ms_per_step": ms,
                    "orthonormality_after_ortho": scond}
         if prec == "mixed":
+            r[prec]["kernels_ms_per_step"] = {k: round(t, 3) for k, (t, _) in
+                                              sorted(kp.items(), key=lambda kv: -kv[1][0])[:14]}
+            P = 8 * nat
+            K = 2 * b.ngw
+            # rnlsm1 + fnonloc: 2 x (2 P n K) FLOPs of the FP32-class product, 6 bf16 slice pairs each
+            proj = 2 * 2.0 * P * cl.nstate * K
+            if "k_tc_gemm" in kp:
+                t_tc = kp["k_tc_gemm"][0] / 1e3
+                r[prec]["projector_gemms"] = {
+                    "ms": kp["k_tc_gemm"][0], "fp32_class_tflops": proj / t_tc / 1e12,
+                    "bf16_issued_tflops": 6 * proj / t_tc / 1e12,
+                    "frac_of_sustained_bf16": 6 * proj / t_tc / 1e12 / float(json.loads(
+                        (ROOT / "MEASURED_PEAKS.json").read_text()).get("bf16_tflops_sustained", 1714.6))
+                    if (ROOT / "MEASURED_PEAKS.json").exists() else None}
+            if "k_ozaki_ns" in kp:
+                tns, cnt = kp["k_ozaki_ns"]
+                # each n x n x n split product issues 36 digit-pair bf16 MMAs per 128 x 32 output tile and K step
+                ns_flops = cnt * 2.0 * cl.nstate ** 3 * 36
+                r[prec]["loewdin_ns_gemms"] = {"ms": tns, "products": cnt,
+                                               "bf16_issued_tflops": ns_flops / (tns / 1e3) / 1e12}
             # non-local forces of the same states: rnlsm2 (3 x 4096 derivative projectors) + rnlfor
             dfnl = torch.empty((cl.nstate, 3, 8, nat), dtype=torch.float64, device=dev)
             fion = torch.zeros((nat, 3), dtype=torch.float64, device=dev)

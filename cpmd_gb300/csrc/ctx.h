@@ -128,6 +128,7 @@ struct Ctx {
   int test_stall = 0;  // test hook: the next tensor-core overlap issues no loads and times out (one call)
   int oz_ksplit = 0;   // split GEMM partition: K splits per overlap tile (0 = fill the SMs)
   int oz_rgrid = 0;    // split GEMM partition: persistent CTAs of C M (0 = one per SM)
+  const char* rmul_name = nullptr;  // profiler name of the next split C M products (Loewdin's n x n ones)
   WfnCache wfn;        // host wavefunction kept on the device between host-memory calls
   cudaStream_t stream = nullptr;  // stream all work is queued on
   cudaStream_t own = nullptr;     // the context's own stream

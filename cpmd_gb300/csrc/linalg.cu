@@ -556,16 +556,24 @@ int ortho_lowdin(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host
       // A times row-major M; all of Y, Z, T are symmetric polynomials in S and commute,
       // so the transposed views give the same matrices
       GBCP_CUDA_TRY(c, cudaMemsetAsync(bits + 1, 0, sizeof(unsigned long long), c.stream));
-      if ((rc = rmul_tc(c, Z, n, n, n, Y, 0, W, n, 0, c.d_info))) return rc;  // W = Z Y
+      c.rmul_name = "k_ozaki_ns";  // the n x n x n products of the iteration, timed apart from C A
+      rc = rmul_tc(c, Z, n, n, n, Y, 0, W, n, 0, c.d_info);  // W = Z Y
+      c.rmul_name = nullptr;
+      if (rc) return rc;
       {
         ProfScope ps_(c, "k_ns_t");
         k_ns_t<<<nbe, 256, 0, c.stream>>>(W, n, T, bits + 1);
         GBCP_LAUNCH_CHECK(c);
       }
-      if ((rc = rmul_tc(c, Y, n, n, n, T, 0, W, n, 0, c.d_info))) return rc;  // W = Y T
-      std::swap(Y, W);
-      if ((rc = rmul_tc(c, T, n, n, n, Z, 0, W, n, 0, c.d_info))) return rc;  // W = T Z
-      std::swap(Z, W);
+      c.rmul_name = "k_ozaki_ns";
+      rc = rmul_tc(c, Y, n, n, n, T, 0, W, n, 0, c.d_info);  // W = Y T
+      if (!rc) {
+        std::swap(Y, W);
+        rc = rmul_tc(c, T, n, n, n, Z, 0, W, n, 0, c.d_info);  // W = T Z
+        std::swap(Z, W);
+      }
+      c.rmul_name = nullptr;
+      if (rc) return rc;
       unsigned long long hb = 0;
       GBCP_CUDA_TRY(c, cudaMemcpyAsync(&hb, bits + 1, sizeof(hb), cudaMemcpyDeviceToHost, c.stream));
       GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));

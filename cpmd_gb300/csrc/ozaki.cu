@@ -909,7 +909,7 @@ int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, 
     const int nsm = c.nsm > 0 ? c.nsm : 148;
     // persistent CTAs: one per SM, or the tuned count (c.oz_rgrid)
     const int grid = std::max(1, std::min(ntiles, c.oz_rgrid > 0 ? c.oz_rgrid : nsm));
-    ProfScope ps_(c, "k_ozaki_rmul");
+    ProfScope ps_(c, c.rmul_name ? c.rmul_name : "k_ozaki_rmul");
     GBCP_LAUNCH_PDL(c, k_oz_tc, dim3(grid), dim3(OZ_THREADS), OZ_SMEM, ma, mb, p);
   }
   return 0;
