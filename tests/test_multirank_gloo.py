@@ -1,5 +1,7 @@
-"""World-size-2 host logic on CPU (gloo): the benchmark's replica timing
-(barrier, max over ranks) and the state-block density reduction."""
+"""World-size-2 host logic (gloo): the benchmark's replica timing (barrier,
+max over ranks), the state-block density and C2 reductions on CPU with the
+oracle as each rank's band loop, and (-m gpu) the same with the CUDA context
+as the band loop plus the G-split overlap reduction, both ranks on cuda:0."""
 import os
 import socket
 
@@ -87,3 +89,81 @@ def test_sharded_density_gloo():
     for _, r, e in out:
         assert np.abs(r - rho).max() <= 1e-12 * np.abs(rho).max()
         assert abs(e - ekin) <= 1e-12 * ekin
+
+
+def _vpsi_worker(rank, world, port, q):
+    dist = _init(rank, world, port)
+    from cpmd_gb300.shard import vpsi_sharded
+    from cpmd_gb300.synth import make_small_cell
+    from oracle import cpmd_oracle as O
+    cl = make_small_cell(10.26, 16, 6.0, 7, seed=22)
+    b = cl.basis
+
+    def local(c, c2, f, v):
+        c2[:] = O.vpsi(c, c2, f, v, b.mill, b.nr, b.hg, b.tpiba2, b.geq0)
+    c2 = np.zeros_like(cl.c0)
+    vpsi_sharded(local, cl.c0, c2, cl.f, cl.vpot, rank, world)
+    q.put((rank, c2))
+    dist.destroy_process_group()
+
+
+def test_sharded_vpsi_gloo():
+    """Each rank applies vpsi to its state block; one sum over the group gives every
+    rank all of C2 (the reference's cp_grp_redist of C2)."""
+    from cpmd_gb300.synth import make_small_cell
+    from oracle import cpmd_oracle as O
+    out = _run(_vpsi_worker)
+    cl = make_small_cell(10.26, 16, 6.0, 7, seed=22)
+    b = cl.basis
+    ref = O.vpsi(cl.c0, np.zeros_like(cl.c0), cl.f, cl.vpot, b.mill, b.nr, b.hg, b.tpiba2, b.geq0)
+    for _, c2 in out:
+        assert np.abs(c2 - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def _cuda_worker(rank, world, port, q):
+    """Both ranks on cuda:0 (separate processes, separate contexts, no kernel waits on
+    the other rank): the CUDA Context as each rank's local band loop, and the G-split
+    overlap through the allocation-free kernel."""
+    dist = _init(rank, world, port)
+    import torch
+    from cpmd_gb300 import Context
+    from cpmd_gb300.shard import overlap_sharded, rhoofr_sharded, vpsi_sharded
+    from cpmd_gb300.synth import make_small_cell
+    torch.cuda.set_device(0)
+    cl = make_small_cell(10.26, 32, 20.0, 13, seed=23)
+    b = cl.basis
+    ctx = Context(b, "fp64")
+    c0 = torch.from_numpy(np.ascontiguousarray(cl.c0.T)).cuda()
+    f = torch.from_numpy(cl.f).cuda()
+    v = torch.from_numpy(cl.vpot).cuda()
+
+    def local_rho(c, ff):
+        return ctx.rhoofr(c, ff)
+
+    def local_vpsi(c, c2, ff, vv):
+        ctx.vpsi(c, c2, ff, vv)
+    rho, ekin = rhoofr_sharded(local_rho, c0, f, rank, world)
+    c2 = torch.zeros_like(c0)
+    vpsi_sharded(local_vpsi, c0, c2, f, v, rank, world)
+    s = overlap_sharded(c0, b.ngw, rank, world, b.geq0)
+    torch.cuda.synchronize()
+    q.put((rank, rho.cpu().numpy(), ekin, np.asfortranarray(c2.cpu().numpy().T), s.cpu().numpy()))
+    ctx.close()
+    dist.destroy_process_group()
+
+
+@pytest.mark.gpu
+def test_sharded_band_loop_and_overlap_on_cuda_gloo():
+    from cpmd_gb300.synth import make_small_cell
+    from oracle import cpmd_oracle as O
+    out = _run(_cuda_worker)
+    cl = make_small_cell(10.26, 32, 20.0, 13, seed=23)
+    b = cl.basis
+    rho, ekin, _, _ = O.rhoofr(cl.c0, cl.f, b.mill, b.nr, b.kr, b.omega, b.hg, b.tpiba2, b.geq0)
+    c2 = O.vpsi(cl.c0, np.zeros_like(cl.c0), cl.f, cl.vpot, b.mill, b.nr, b.hg, b.tpiba2, b.geq0)
+    s = O.overlap(cl.c0, b.geq0)
+    for _, r, e, c, sm in out:
+        assert np.abs(r - rho).max() <= 1e-10 * np.abs(rho).max()
+        assert abs(e - ekin) <= 1e-10 * ekin
+        assert np.abs(c - c2).max() <= 1e-10 * np.abs(c2).max()
+        assert np.abs(sm - s).max() <= 1e-12 * np.abs(s).max()
