@@ -368,22 +368,32 @@ def run_gpu(args, rank, world, local):
     vh[:] = cell.vpot
     rhoh = pin(tuple(b.kr[::-1]), torch.float64)
 
-    def e2e_run(ctx, steps):
+    calls = {"rhoofr": 0.0, "vpsi": 0.0, "ortho": 0.0}
+
+    def e2e_run(ctx, steps, split=None):
         def e2e_step():
+            t = time.perf_counter()
             ctx.rhoofr(c0h, fh, rhoh, energies=True)
+            t1 = time.perf_counter()
             ctx.vpsi(c0h, c2h, fh, vh)
+            t2 = time.perf_counter()
             ctx.ortho(c0h, "gs")
+            t3 = time.perf_counter()
+            return t1 - t, t2 - t1, t3 - t2
         for _ in range(2):
             e2e_step()
         barrier(world)
         t0 = time.perf_counter()
         for _ in range(steps):
-            e2e_step()
+            r = e2e_step()
+            if split is not None:
+                for k, v in zip(("rhoofr", "vpsi", "ortho"), r):
+                    split[k] += v / steps
         return allreduce_max(time.perf_counter() - t0, world)
 
     # rhoofr's upload of c0 serves vpsi and ortho as well (the reference's cp_cuwfn cache)
     ctx_mx.set_option("wfn_cache", 1)
-    t_e2e = e2e_run(ctx_mx, args.e2e_steps)
+    t_e2e = e2e_run(ctx_mx, args.e2e_steps, calls)
     c0h[:] = cell.c0
     t_e2e64 = e2e_run(ctx_64, 2)
     wfn = b.ngw * n * 16
@@ -437,7 +447,8 @@ def run_gpu(args, rank, world, local):
             "kernels_ms_per_step": {k: round(t / 2, 4) for k, (t, _) in sorted(prof.items(), key=lambda kv: -kv[1][0])},
             "clocks": clocks,
             "e2e": {"value": e2e, "unit": "state-applies/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "steps": args.e2e_steps, "path": "C ABI, host (pinned) buffers, GBCP_MEM_HOST; c0 uploaded once "
+                    "steps": args.e2e_steps,
+                    "ms_per_call": {k: round(v * 1e3, 4) for k, v in calls.items()}, "path": "C ABI, host (pinned) buffers, GBCP_MEM_HOST; c0 uploaded once "
                                                       "per step by rhoofr and reused by vpsi and ortho "
                                                       "(GBCP_OPT_WFN_CACHE)",
                     "fp64_drop_in": {"value": v64, "e2e_value": e2e64, "ms_per_step": ms_64 / args.fp64_steps,

@@ -141,7 +141,8 @@ class Context:
         """key 'gemm' (-1 by precision, 0 FP64 SIMT, 1 tensor cores), 'batch' (pairs per
         launch), 'fft' (0 four-step, 2 Stockham), 'xchunks' (density x-stage pair chunks,
         0 = automatic) or 'xc' (energy functional: 0 LDA-PZ, 1 PBE)."""
-        k = {"gemm": 1, "batch": 2, "fft": 3, "xchunks": 4, "xc": 5, "wfn_cache": 6, "plane": 7, "test_timeout": 90}[key]
+        k = {"gemm": 1, "batch": 2, "fft": 3, "xchunks": 4, "xc": 5, "wfn_cache": 6, "plane": 7, "chol": 8,
+             "test_timeout": 90}[key]
         self._check("gbcp_set_option", self.lib.gbcp_set_option(self.h, k, int(value)))
 
     def synchronize(self):

@@ -272,10 +272,339 @@ __global__ void k_zero_lower(double* __restrict__ X, const double* __restrict__ 
   }
 }
 
+// ---- one-CTA Cholesky and inverse in double-float arithmetic (n <= 128) ----
+//
+// The blocked chain above spends most of its time in the FP64 pivot chain of
+// k_chol_diag (GB300 issues FP64 at 1/64 of the FP32 rate).  For the overlap
+// matrices of up to 128 states one CTA does the whole job instead, in
+// double-float arithmetic: a value is the unevaluated sum hi + lo of two FP32
+// numbers, kept by the error-free transformations TwoSum (Knuth) and
+// TwoProduct by FMA (Dekker 1971) to about 2^-46 relative per operation; two
+// slots go through each packed f32x2 instruction.  Against the FP64 chain the
+// orthonormality of C U^-1 goes from a few 1e-16 to a few 1e-14 at n = 128.
+//
+// Scaling.  D = diag(2^k_i), k_i = -floor(e_i / 2) from the binary exponent e_i
+// of S_ii, puts the diagonal of A = D S D in [1, 4) and (S being SPD) every
+// entry below 4 in magnitude, inside FP32's range whatever the scale of S.
+// A = L L^T gives U = L^T D^-1 and X = U^-1 = D L^-T.  Splitting S_ij into
+// hi + lo, the scaling and the conversion back are integer operations on the
+// bit patterns (the FP64 pipe also runs the F2F conversions).
+//
+// Elimination.  Slot (i, q), q <= i, lives in a register of warp i mod PR, lane
+// q mod 32.  It holds A_iq (the Schur complement) up to step q and Z_iq after
+// it, Z the inverse of the unit lower factor of A.  Step j, with d = A_jj and
+// w_i = A_ij / d for the rows i > j:
+//     A_iq -= w_i A_qj  (j < q <= i),   Z_ij = -w_i,   Z_iq -= w_i Z_jq  (q < j),
+// so every slot of row i subtracts w_i times entry q of one vector, row j of Z
+// followed by column j of A, which the owners of those slots publish in shared
+// memory at the end of step j - 1 (double-buffered: one barrier per step).
+// Then L^-1 = diag(d)^-1/2 Z: X_qi = 2^k_q d_i^-1/2 Z_iq (q < i), X_ii =
+// 2^k_i d_i^-1/2.  A pivot at or below 2^-40 of its row's scaled original
+// diagonal stops the factorisation with status (index + 1), a NaN pivot with
+// -1: the rounding an exactly dependent set of states leaves in its pivot (a
+// few 2^-46 of the diagonal) stays well inside that threshold.
+
+typedef unsigned long long u64;
+
+struct Dfl {
+  float h, l;
+};
+
+__device__ __forceinline__ u64 p2(float a, float b) {
+  u64 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float p2lo(u64 r) {
+  float a, b;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+  return a;
+}
+__device__ __forceinline__ float p2hi(u64 r) {
+  float a, b;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+  return b;
+}
+__device__ __forceinline__ u64 padd(u64 a, u64 b) {
+  u64 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ u64 psub(u64 a, u64 b) {
+  u64 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ u64 pmul(u64 a, u64 b) {
+  u64 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ u64 pfma(u64 a, u64 b, u64 c) {
+  u64 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
+// TwoSum: s + e = a + b exactly
+__device__ __forceinline__ Dfl df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+// Fast2Sum (|a| >= |b|)
+__device__ __forceinline__ Dfl df_fast(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ Dfl df_mul(Dfl a, Dfl b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return df_fast(p, e);
+}
+// 1 / d: the correctly rounded FP32 reciprocal r and one Newton step,
+// r + r (1 - d r) with the residual taken in double-float
+__device__ __forceinline__ Dfl df_rcp(Dfl d) {
+  const float r = __frcp_rn(d.h);
+  float e = __fmaf_rn(-d.h, r, 1.0f);
+  e = __fmaf_rn(-d.l, r, e);
+  return df_fast(r, __fmul_rn(r, e));
+}
+// d^-1/2: an FP32 estimate, one Newton step y (3 - d y^2) / 2 in FP32 and one
+// y + y (1 - d y^2) / 2 with d y^2 in double-float (1 - d y^2 is exact there)
+__device__ __forceinline__ Dfl df_rsqrt(Dfl d) {
+  float y = rsqrtf(d.h);
+  y = __fmul_rn(y, __fmaf_rn(__fmul_rn(-0.5f * d.h, y), y, 1.5f));
+  const float p = __fmul_rn(y, y), pe = __fmaf_rn(y, y, -p);
+  const float t = __fmul_rn(d.h, p);
+  float te = __fmaf_rn(d.h, p, -t);
+  te = __fmaf_rn(d.h, pe, te);
+  te = __fmaf_rn(d.l, p, te);
+  const float e = __fsub_rn(__fsub_rn(1.0f, t), te);
+  return df_fast(y, __fmul_rn(__fmul_rn(0.5f, y), e));
+}
+
+// x 2^s as hi + lo: hi the leading 24 significand bits, lo the other 29 rounded
+// to 24; magnitudes below FP32's normal range give 0, NaN and infinity NaN
+__device__ __forceinline__ Dfl df_of_double(double x, int s) {
+  const u64 b = (u64)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int E = (int)((b >> 52) & 0x7FF);
+  if (E == 0x7FF) return {__uint_as_float(0x7FC00000u), 0.0f};
+  const int e = E - 1023 + s;
+  if (E == 0 || e < -126) return {__uint_as_float(sign), 0.0f};
+  if (e > 127) return {__uint_as_float(sign | 0x7F800000u), 0.0f};
+  const u64 m = b & 0xFFFFFFFFFFFFFull;
+  const float hi = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | (unsigned)(m >> 29));
+  float lo = 0.0f;
+  if (e >= -74)
+    lo = __fmul_rn(__uint2float_rn((unsigned)(m & 0x1FFFFFFFull)), __uint_as_float((unsigned)(e - 52 + 127) << 23));
+  return {hi, __uint_as_float(__float_as_uint(lo) | sign)};
+}
+
+// (h + l) 2^s as a double.  After TwoSum the two significands lie 24 or more
+// binades apart, so their sum fits the 53 bits of a double but for bits of l
+// below 2^-52 of h; FP32 subnormal parts count as 0.
+__device__ __forceinline__ double df_to_double(Dfl v, int s) {
+  const Dfl t = df_two_sum(v.h, v.l);
+  const unsigned bh = __float_as_uint(t.h), bl = __float_as_uint(t.l);
+  const int eh = (int)((bh >> 23) & 0xFF), el = (int)((bl >> 23) & 0xFF);
+  if (eh == 0xFF) return __longlong_as_double(0x7FF8000000000000LL);
+  if (eh == 0) return 0.0;
+  long long T = (long long)((u64)(0x800000u | (bh & 0x7FFFFFu)) << 29);  // units of 2^(eh - 127 - 52)
+  if (el != 0) {
+    const int sh = eh - el;
+    const u64 ml = (u64)(0x800000u | (bl & 0x7FFFFFu));
+    const long long lv = sh <= 29 ? (long long)(ml << (29 - sh)) : (sh < 53 ? (long long)(ml >> (sh - 29)) : 0LL);
+    T += ((bh ^ bl) & 0x80000000u) ? -lv : lv;
+  }
+  int e = eh - 127 + s;
+  if (T >= (1LL << 53)) {
+    T >>= 1;
+    ++e;
+  } else if (T < (1LL << 52)) {
+    T <<= 1;
+    --e;
+  }
+  const u64 sign = (u64)(bh & 0x80000000u) << 32;
+  if (e + 1023 <= 0) return __longlong_as_double((long long)sign);
+  if (e + 1023 >= 2047) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
+  return __longlong_as_double((long long)(sign | ((u64)(e + 1023) << 52) | ((u64)T & 0xFFFFFFFFFFFFFull)));
+}
+
+// S row-major n x n (upper part used), X = U^-1 row-major, zero below the
+// diagonal; NMAX / PR rows per warp, lanes over columns in pairs of 32-column
+// blocks (q, q + 32) packed into one f32x2 register pair (hi parts, lo parts).
+// The loops over the slots carry explicit unroll counts: without them the
+// 128-state instance kept the slot arrays in local memory.
+template <int NMAX, int PR>
+__global__ void __launch_bounds__(32 * PR) k_chol_df(const double* __restrict__ S, double* __restrict__ X, int n,
+                                                     int* __restrict__ status) {
+  constexpr int RA = NMAX / PR, NP = NMAX / 64;
+  static_assert(NMAX % 64 == 0 && NMAX % PR == 0, "layout");
+  pdl_entry();
+  __shared__ float2 buf[2][NMAX];  // the broadcast vector of the step (double-buffered)
+  __shared__ float2 piv[NMAX];     // the pivots d_j
+  __shared__ float thr[NMAX];      // 2^-40 of the scaled original diagonal
+  __shared__ int kx[NMAX];         // k_i
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (failed(status)) return;
+  for (int t = threadIdx.x; t < NMAX; t += 32 * PR) {
+    int k = 0;
+    if (t < n) {
+      const int E = (int)((__double_as_longlong(S[(size_t)t * n + t]) >> 52) & 0x7FF);
+      if (E != 0 && E != 0x7FF) k = -((E - 1023) >> 1);
+    }
+    kx[t] = k;
+    buf[0][t] = buf[1][t] = make_float2(0.0f, 0.0f);
+    thr[t] = 0.0f;
+  }
+  __syncthreads();
+  u64 H[RA][NP], L[RA][NP];  // slots (i, q) and (i, q + 32): i = w + PR a, q = lane + 64 p
+#pragma unroll 16
+  for (int a = 0; a < RA; ++a) {
+    const int i = w + PR * a;
+#pragma unroll 16
+    for (int p = 0; p < NP; ++p) {
+      const int q0 = lane + 64 * p, q1 = q0 + 32;
+      Dfl v0 = {0.0f, 0.0f}, v1 = {0.0f, 0.0f};
+      if (i < n && q0 <= i) v0 = df_of_double(S[(size_t)q0 * n + i], kx[i] + kx[q0]);
+      if (i < n && q1 <= i) v1 = df_of_double(S[(size_t)q1 * n + i], kx[i] + kx[q1]);
+      H[a][p] = p2(v0.h, v1.h);
+      L[a][p] = p2(v0.l, v1.l);
+      if (i < n) {
+        if (q0 == i) thr[i] = 0x1p-40f * v0.h;
+        if (q1 == i) thr[i] = 0x1p-40f * v1.h;
+        if (q0 == 0) buf[0][i] = make_float2(v0.h, v0.l);  // column 0, the first pivot included
+      }
+    }
+  }
+  for (int j = 0; j < n; ++j) {
+    __syncthreads();
+    const float2* b = buf[j & 1];
+    float2* bn = buf[(j + 1) & 1];
+    const float2 dv = b[j];
+    if (!(dv.x > thr[j])) {  // every thread reads the same pivot: a uniform exit
+      if (threadIdx.x == 0) atomicExch(status, dv.x != dv.x ? -1 : j + 1);
+      return;
+    }
+    if (threadIdx.x == 0) piv[j] = dv;
+    const Dfl rd = df_rcp({dv.x, dv.y});
+    u64 vh[NP], vl[NP];
+#pragma unroll 16
+    for (int p = 0; p < NP; ++p) {
+      const float2 x0 = b[lane + 64 * p], x1 = b[lane + 64 * p + 32];
+      vh[p] = p2(x0.x, x1.x);
+      vl[p] = p2(x0.y, x1.y);
+    }
+    const int j1 = j + 1;
+#pragma unroll 16
+    for (int a = 0; a < RA; ++a) {
+      const int i = w + PR * a;
+      if (i > j && i < n) {  // warp-uniform
+      const float2 bi = b[i];
+      const Dfl wi = df_mul({bi.x, bi.y}, rd);
+      const u64 wh = p2(wi.h, wi.h), wl = p2(wi.l, wi.l), nwh = p2(-wi.h, -wi.h);
+#pragma unroll 16
+      for (int p = 0; p < NP; ++p) {
+        if (64 * p <= i) {  // some slot of this pair on the row (warp-uniform)
+        // (H, L) -= w v: TwoProduct of the hi parts, TwoSum into H, the rest into L
+        const u64 np = pmul(nwh, vh[p]);
+        u64 pe = pfma(wh, vh[p], np);
+        pe = pfma(wh, vl[p], pe);
+        pe = pfma(wl, vh[p], pe);
+        const u64 s = padd(H[a][p], np);
+        const u64 bb = psub(s, H[a][p]);
+        const u64 e = padd(psub(H[a][p], psub(s, bb)), psub(np, bb));
+        H[a][p] = s;
+        L[a][p] = padd(e, psub(L[a][p], pe));
+        if (j & 1) {  // renormalise every second step: the lo parts' own rounding stays at 2^-48 of hi
+          const u64 s2 = padd(H[a][p], L[a][p]);
+          const u64 b2 = psub(s2, H[a][p]);
+          L[a][p] = padd(psub(H[a][p], psub(s2, b2)), psub(L[a][p], b2));
+          H[a][p] = s2;
+        }
+        if ((j >> 6) == p && lane == (j & 31)) {  // slot (i, j): Z_ij = -w_i
+          float h0 = p2lo(H[a][p]), h1 = p2hi(H[a][p]), l0 = p2lo(L[a][p]), l1 = p2hi(L[a][p]);
+          if (j & 32) {
+            h1 = -wi.h;
+            l1 = -wi.l;
+          } else {
+            h0 = -wi.h;
+            l0 = -wi.l;
+          }
+          H[a][p] = p2(h0, h1);
+          L[a][p] = p2(l0, l1);
+        }
+        }
+      }
+      // the vector of step j + 1: row j + 1 (Z part and pivot), then column j + 1
+      if (i == j1) {
+#pragma unroll 16
+        for (int p = 0; p < NP; ++p) {
+          const int q0 = lane + 64 * p;
+          if (q0 <= i) {
+            const Dfl t = df_two_sum(p2lo(H[a][p]), p2lo(L[a][p]));
+            bn[q0] = make_float2(t.h, t.l);
+          }
+          if (q0 + 32 <= i) {
+            const Dfl t = df_two_sum(p2hi(H[a][p]), p2hi(L[a][p]));
+            bn[q0 + 32] = make_float2(t.h, t.l);
+          }
+        }
+      } else if (lane == (j1 & 31)) {
+#pragma unroll 16
+        for (int p = 0; p < NP; ++p) {
+          if ((j1 >> 6) == p) {
+            const bool up = (j1 & 32) != 0;
+            const Dfl t = df_two_sum(up ? p2hi(H[a][p]) : p2lo(H[a][p]), up ? p2hi(L[a][p]) : p2lo(L[a][p]));
+            bn[i] = make_float2(t.h, t.l);
+          }
+        }
+      }
+      }
+    }
+  }
+  __syncthreads();
+  // X_qi = 2^k_q d_i^-1/2 Z_iq (q < i), X_ii = 2^k_i d_i^-1/2, zero below the diagonal
+#pragma unroll 16
+  for (int a = 0; a < RA; ++a) {
+    const int i = w + PR * a;
+    if (i < n) {
+      const float2 pv = piv[i];
+      const Dfl ri = df_rsqrt({pv.x, pv.y});
+#pragma unroll 16
+      for (int p = 0; p < NP; ++p) {
+#pragma unroll 16
+        for (int hf = 0; hf < 2; ++hf) {
+          const int q = lane + 64 * p + 32 * hf;
+          if (q == i) {
+            X[(size_t)i * n + i] = df_to_double(ri, kx[i]);
+          } else if (q < i) {
+            const Dfl z = df_two_sum(hf ? p2hi(H[a][p]) : p2lo(H[a][p]), hf ? p2hi(L[a][p]) : p2lo(L[a][p]));
+            X[(size_t)q * n + i] = df_to_double(df_mul(z, ri), kx[q]);
+            X[(size_t)i * n + q] = 0.0;
+          }
+        }
+      }
+    }
+  }
+}
+
 }  // namespace
 
-// Queue U = chol(S) and X = U^{-1}; no synchronisation.  S is overwritten.
+// Queue U = chol(S) and X = U^{-1}; no synchronisation.  S is overwritten (the
+// blocked FP64 chain) or left as it was (the one-CTA double-float kernel).
 int chol_inverse(Ctx& c, double* S, double* X, int n) {
+  if (n <= 128 && (c.chol_df == 2 || (c.chol_df == 1 && c.precision == 1))) {
+    ProfScope ps_(c, "k_chol_df");
+    if (n <= 64)
+      GBCP_LAUNCH_PDL(c, (k_chol_df<64, 8>), dim3(1), dim3(256), 0, (const double*)S, X, n, c.d_info);
+    else
+      GBCP_LAUNCH_PDL(c, (k_chol_df<128, 16>), dim3(1), dim3(512), 0, (const double*)S, X, n, c.d_info);
+    return 0;
+  }
   const int nb = (n + B - 1) / B;
   if (!ensure(c, c.cdiag, sizeof(double) * (size_t)n)) return 6;
   if (!ensure(c, c.cwork, sizeof(double) * (size_t)n * n)) return 6;

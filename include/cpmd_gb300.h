@@ -113,13 +113,21 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  *                   it (it rewrites c0).  A caller that changes c0 on the host
  *                   in a way that keeps that key must drop the copy by setting
  *                   the option again (any value).  0 (the default) = off;
+ *   GBCP_OPT_CHOL   Cholesky factor and inverse of the ortho overlap matrix:
+ *                   0 = blocked FP64 over many CTAs at every size; 1 (the
+ *                   default) = for nstate <= 128 in the MIXED precision, one
+ *                   CTA in double-float arithmetic (about 2^-46 relative per
+ *                   operation; a pivot at or below 2^-40 of its row's original
+ *                   diagonal reports GBCP_ERR_NOT_SPD, where the FP64 chain
+ *                   uses 2^-46); 2 = that kernel in both precisions;
  *   GBCP_OPT_TEST_TIMEOUT  test hook of the failure path: 1 = the next overlap
  *                   on the tensor cores issues no operand loads, so its first
  *                   bounded wait (no copy in flight towards it) runs out after
  *                   about a millisecond; the call returns GBCP_ERR_TIMEOUT with
  *                   c0 untouched and the hook clears itself. */
 enum gbcp_option { GBCP_OPT_GEMM = 1, GBCP_OPT_BATCH = 2, GBCP_OPT_FFT = 3, GBCP_OPT_XCHUNKS = 4, GBCP_OPT_XC = 5,
-                   GBCP_OPT_WFN_CACHE = 6, GBCP_OPT_PLANE = 7, GBCP_OPT_TEST_TIMEOUT = 90 };
+                   GBCP_OPT_WFN_CACHE = 6, GBCP_OPT_PLANE = 7, GBCP_OPT_CHOL = 8,
+                   GBCP_OPT_TEST_TIMEOUT = 90 };
 int gbcp_set_option(gbcp_ctx* ctx, int key, int value);
 /* Queue later work on `stream` (a cudaStream_t; NULL = the context's own
  * stream; the CUDA legacy default stream is cudaStreamLegacy).  Device-pointer calls are ordered only with respect to this stream,
