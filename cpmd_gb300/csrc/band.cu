@@ -125,7 +125,7 @@ __global__ void k_fold_scaled(const double* __restrict__ part, int n, double sca
 // [b rc, (b+1) rc), writes its three totals, and the last CTA to finish (ticket
 // counter) adds the CTA totals in CTA order and writes out = {tpiba2 sum kin,
 // sum norm, rscale sum rho}; the result does not depend on the scheduling.
-__global__ void __launch_bounds__(kThreads) k_rho_scalars(const double* __restrict__ kp, int nk, int kc,
+__global__ void __launch_bounds__(kThreads) k_rho_scalars(const double* __restrict__ kp, int kp_df, int nk, int kc,
                                                          const double* __restrict__ rho, long long nr, long long rc,
                                                          double* __restrict__ part, unsigned* __restrict__ ticket,
                                                          double tpiba2, double rscale, double* __restrict__ out) {
@@ -135,8 +135,14 @@ __global__ void __launch_bounds__(kThreads) k_rho_scalars(const double* __restri
   {
     const int lo = blockIdx.x * kc, hi = min(nk, lo + kc);
     for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-      v[0] += kp[2 * (size_t)i];
-      v[1] += kp[2 * (size_t)i + 1];
+      if (kp_df) {  // (kin hi, kin lo, norm hi, norm lo) floats of the FP32 gather
+        const float4 q = reinterpret_cast<const float4*>(kp)[i];
+        v[0] += f2d_int(q.x) + f2d_int(q.y);
+        v[1] += f2d_int(q.z) + f2d_int(q.w);
+      } else {
+        v[0] += kp[2 * (size_t)i];
+        v[1] += kp[2 * (size_t)i + 1];
+      }
     }
     const long long rlo = blockIdx.x * rc, rhi = min(nr, rlo + rc);
     for (long long i = rlo + threadIdx.x; i < rhi; i += blockDim.x) v[2] += rho[i];
@@ -195,8 +201,8 @@ int band_rhoofr(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double*
     if (scalars) GBCP_CUDA_TRY(c, cudaMemsetAsync(scalars, 0, 3 * sizeof(double), c.stream));
     return 0;
   }
-  // partials of E_kin / norm: one pair of doubles per Z-stage CTA of every pair,
-  // then three per CTA of the fold
+  // partials of E_kin / norm: one pair of doubles (FP32 gather: four floats, two
+  // double-float pairs) per Z-stage CTA of every pair, then three per CTA of the fold
   const int npairs = (nstate + 1) / 2;
   const int nkb = npairs * (c.precision == 0 ? band_zinv_blocks_fp64(c) : band_zinv_blocks_fp32(c));
   const int nfold = std::max(1, std::min(2 * (c.nsm > 0 ? c.nsm : 152), (int)((nnr + 4095) / 4096)));
@@ -216,7 +222,7 @@ int band_rhoofr(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double*
     ProfScope ps_(c, "k_rho_scalars");
     const int kc = (nkb + nfold - 1) / nfold;
     const long long rcnt = ((long long)nnr + nfold - 1) / nfold;
-    k_rho_scalars<<<nfold, kThreads, 0, c.stream>>>(kpart, nkb, kc, rho, (long long)nnr, rcnt, kpart + 2 * (size_t)nkb,
+    k_rho_scalars<<<nfold, kThreads, 0, c.stream>>>(kpart, c.precision != 0, nkb, kc, rho, (long long)nnr, rcnt, kpart + 2 * (size_t)nkb,
                                                     static_cast<unsigned*>(c.rho_tk.p), c.tpiba2,
                                                     c.omega / ((double)c.nr[0] * c.nr[1] * c.nr[2]), scalars);
     GBCP_LAUNCH_CHECK(c);

@@ -126,15 +126,16 @@ template <> struct KinAcc<float> {
     n1 += g0 ? ux * ux : 2.f * a1;
     n2 += g0 ? wx * wx : 2.f * a2;
   }
-  __device__ __forceinline__ void warp_totals(double (&o)[4]) {
-    float h[4] = {k1, n1, k2, n2}, l[4] = {0.f, 0.f, 0.f, 0.f};
+  // warp totals as double-float pairs (h + l)
+  __device__ __forceinline__ void warp_totals(float (&h)[4], float (&l)[4]) {
+    h[0] = k1; h[1] = n1; h[2] = k2; h[3] = n2;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) l[q] = 0.f;
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1)
 #pragma unroll
       for (int q = 0; q < 4; ++q)
         df_add(h[q], l[q], __shfl_down_sync(0xffffffffu, h[q], d), __shfl_down_sync(0xffffffffu, l[q], d));
-#pragma unroll
-    for (int q = 0; q < 4; ++q) o[q] = f2d_int(h[q]) + f2d_int(l[q]);
   }
 };
 
@@ -150,8 +151,7 @@ __device__ __forceinline__ void kin_entry(KinAcc<float>& acc, const GeoDev& g, i
 }
 
 // CTA totals weighted by f1, f2 into out[0..1].  Every thread of the CTA calls it.
-template <typename T>
-__device__ __forceinline__ void kin_flush(KinAcc<T>& acc, double f1, double f2, double* __restrict__ out) {
+__device__ __forceinline__ void kin_flush(KinAcc<double>& acc, double f1, double f2, double* __restrict__ out) {
   __shared__ double wsum[kThreads / 32][4];
   double o[4];
   acc.warp_totals(o);
@@ -167,6 +167,39 @@ __device__ __forceinline__ void kin_flush(KinAcc<T>& acc, double f1, double f2, 
       for (int q = 0; q < 4; ++q) t[q] += wsum[w][q];
     out[0] = f1 * t[0] + f2 * t[2];
     out[1] = f1 * t[1] + f2 * t[3];
+  }
+}
+// FP32 kernels: the warp and CTA sums stay double-float and out[0..1] receives
+// (kin hi, kin lo, norm hi, norm lo) as four floats, converted by the fold
+// (k_rho_scalars), so that the gather kernel issues almost no FP64 instruction
+// (each holds an SM sub-partition for ~64 clocks on GB300)
+__device__ __forceinline__ void df_mul_add(float& h, float& l, float ah, float al, float bh, float bl) {
+  const float p = ah * bh;
+  const float e = fmaf(al, bh, fmaf(ah, bl, fmaf(ah, bh, -p)));
+  df_add(h, l, p, e);
+}
+__device__ __forceinline__ void kin_flush(KinAcc<float>& acc, double f1, double f2, double* __restrict__ out) {
+  __shared__ float2 wsum[kThreads / 32][4];
+  float h[4], l[4];
+  acc.warp_totals(h, l);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) wsum[warp][q] = make_float2(h[q], l[q]);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float th[4] = {0.f, 0.f, 0.f, 0.f}, tl[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) df_add(th[q], tl[q], wsum[w][q].x, wsum[w][q].y);
+    const float f1h = d2f_int(f1), f1l = d2f_int(f1 - f2d_int(f1h));
+    const float f2h = d2f_int(f2), f2l = d2f_int(f2 - f2d_int(f2h));
+    float kh = 0.f, kl = 0.f, nh = 0.f, nl = 0.f;
+    df_mul_add(kh, kl, f1h, f1l, th[0], tl[0]);
+    df_mul_add(kh, kl, f2h, f2l, th[2], tl[2]);
+    df_mul_add(nh, nl, f1h, f1l, th[1], tl[1]);
+    df_mul_add(nh, nl, f2h, f2l, th[3], tl[3]);
+    *reinterpret_cast<float4*>(out) = make_float4(kh, kl, nh, nl);
   }
 }
 
