@@ -49,21 +49,58 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """Clocks and throttle reasons sampled during the timed region: read through
+    NVML (the driver's libnvidia-ml, read-only queries) every 2 ms, or nvidia-smi
+    every 0.2 s where NVML cannot be loaded."""
 
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
+    # NVML clocks-event reason bits: hw_slowdown, hw_thermal_slowdown, sw_thermal_slowdown, sw_power_cap
+    BITS = (0x8, 0x40, 0x20, 0x4)
 
     def __init__(self, index: int):
         self.index = index
         self.samples = []
         self.stop_ev = threading.Event()
+        self.nvml = self._nvml()
         self.th = threading.Thread(target=self.run, daemon=True)
+
+    def _nvml(self):
+        import ctypes as C
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+            for fn in ("nvmlDeviceGetClockInfo", "nvmlDeviceGetMaxClockInfo", "nvmlDeviceGetCurrentClocksEventReasons"):
+                getattr(lib, fn)
+            if lib.nvmlInit_v2() != 0:
+                return None
+            dev = C.c_void_p()
+            if lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.index), C.byref(dev)) != 0:
+                return None
+            return lib, dev
+        except Exception:
+            return None
+
+    def _nvml_sample(self):
+        import ctypes as C
+        lib, dev = self.nvml
+        sm, mx, reasons = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        if lib.nvmlDeviceGetClockInfo(dev, 1, C.byref(sm)) != 0 or lib.nvmlDeviceGetMaxClockInfo(dev, 1, C.byref(mx)) != 0:
+            return None
+        if lib.nvmlDeviceGetCurrentClocksEventReasons(dev, C.byref(reasons)) != 0:
+            return None
+        r = reasons.value
+        return [str(sm.value), str(mx.value), ""] + ["Active" if r & bit else "Not Active" for bit in self.BITS]
 
     def run(self):
         while not self.stop_ev.is_set():
             try:
+                if self.nvml:
+                    vals = self._nvml_sample()
+                    if vals:
+                        self.samples.append(vals)
+                    self.stop_ev.wait(0.002)
+                    continue
                 out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
                                       "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
                 vals = [v.strip() for v in out.stdout.strip().split(",")]
@@ -89,7 +126,7 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower().startswith("active")})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(self.samples), "source": "nvml" if self.nvml else "nvidia-smi"}
 
 
 def dist_setup(n_gpus: int):

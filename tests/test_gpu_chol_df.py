@@ -39,6 +39,7 @@ def test_gs_double_float_matches_oracle(gpu_lib, nstate):
     c = perturbed(cl.c0, 0.03, nstate)
     ref = O.rgs(c, cl.basis.geq0)
     ctx = Context(cl.basis, "mixed")
+    ctx.set_option("chol", 1)
     out = c.copy(order="F")
     ctx.ortho(out, "gs")
     assert rel(out, ref) < 1e-12
@@ -48,7 +49,7 @@ def test_gs_double_float_matches_oracle(gpu_lib, nstate):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_chol_option_engines_agree(gpu_lib, precision):
-    """Option 0 (blocked FP64), 1 (double-float in the mixed precision) and 2
+    """Option 0 (blocked FP64, the default), 1 (double-float in the mixed precision) and 2
     (double-float in both) give the same orthonormal set to 1e-12."""
     from cpmd_gb300 import Context
     cl = make_small_cell(10.26, 32, 20.0, 100, seed=411)
@@ -91,6 +92,7 @@ def test_gs_double_float_dependent_states_not_spd(gpu_lib, nstate, dup):
     c[:, dup[1]] = c[:, dup[0]]
     keep = c.copy(order="F")
     ctx = Context(cl.basis, "mixed")
+    ctx.set_option("chol", 1)
     with pytest.raises(GbcpError) as e:
         ctx.ortho(c, "gs")
     assert e.value.code == 2
