@@ -30,7 +30,7 @@ def nvcc() -> str:
 
 def _flags(extra=()):
     return ["-O3", "-std=c++17", "-lineinfo", "-Xptxas=-O3",
-            "-Xcompiler", "-fPIC", *ARCH, *extra]
+            "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-math-errno", *ARCH, *extra]
 
 
 def _stale(obj: Path, src: Path) -> bool:

@@ -792,9 +792,16 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
     // events: [0] ordering, [1, nb] c0 chunks, [nb+1, 2nb] C2 downloads, [2nb+1, 3nb] C2 uploads,
     // [3nb+1] V(r), last: the final download
     if ((rc = pipe_prepare(c, 2 * nb + 1))) return rc;
+    // V(r) goes first, queued before the host reads the cache key, so the copy engine
+    // is busy meanwhile; then chunk 0's states, and chunk b's C2 columns behind chunk
+    // b+1's states, so that the first transforms start after one chunk and each
+    // decode finds its C2
+    {
+      gbcp::ProfScope ps_(c, "h2d_vpot", c.copy, 1);
+      GBCP_CUDA_TRY(c, cudaMemcpyAsync(tv, vpot, sizeof(double) * nnr1, cudaMemcpyHostToDevice, c.copy));
+      GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[3 * nb + 1], c.copy));
+    }
     const bool resident = wfn_hit(c, c0, ldc, nstate);  // c0 still on the device from rhoofr
-    // copy order: the states of chunk 0, V(r), then chunk b's C2 columns behind chunk b+1's
-    // states, so that the first transforms start after one chunk and each decode finds its C2
     for (int b = 0; b <= nb; ++b) {
       int s0, ns;
       if (b < nb) {
@@ -802,11 +809,7 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
         if (!resident && (rc = pipe_up(c, t0, c0, ldc, s0, ns))) return rc;
         GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[1 + b], c.copy));
       }
-      if (b == 0) {
-        gbcp::ProfScope ps_(c, "h2d_vpot", c.copy, 1);
-        GBCP_CUDA_TRY(c, cudaMemcpyAsync(tv, vpot, sizeof(double) * nnr1, cudaMemcpyHostToDevice, c.copy));
-        GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[3 * nb + 1], c.copy));
-      } else {
+      if (b > 0) {
         chunk(b - 1, &s0, &ns);
         if ((rc = pipe_up(c, t2, c2, ldc2, s0, ns))) return rc;
         GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[2 * nb + b], c.copy));

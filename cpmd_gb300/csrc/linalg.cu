@@ -479,10 +479,19 @@ int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host, int res
   GBCP_CUDA_TRY(c, cudaMemsetAsync(c.d_info, 0, 16, c.stream));
   double* Ar = reinterpret_cast<double*>(d);
   // C U^-1's digit planes of range r are cut on the side stream once range r has
-  // landed, beside the overlap ranges and the Cholesky
+  // landed, beside the overlap ranges and the Cholesky.  States already on the
+  // device (the wavefunction cache): S in one pass as in the device-memory call,
+  // the planes cut beside the Cholesky only
   const cudaEvent_t* sliced = nullptr;
-  int rc = n <= 256 ? slice_rows_side(c, Ar, 2 * ngw, 2 * ngw, n, kb, R, up, &sliced) : 0;
-  if (!rc) rc = ovlap_tc_ranges(c, Ar, 2 * ngw, n, kb, R, up, S, scond_host ? scond_bits_of(c) : nullptr, c.d_info);
+  unsigned long long* sbits = scond_host ? scond_bits_of(c) : nullptr;
+  int rc = 0;
+  if (resident) {
+    rc = ovlap_tc(c, d, ngw, n, S, sbits, c.d_info);
+    if (!rc && n <= 256) rc = slice_rows_side(c, Ar, 2 * ngw, 2 * ngw, n, kb, R, nullptr, &sliced);
+  } else {
+    rc = n <= 256 ? slice_rows_side(c, Ar, 2 * ngw, 2 * ngw, n, kb, R, up, &sliced) : 0;
+    if (!rc) rc = ovlap_tc_ranges(c, Ar, 2 * ngw, n, kb, R, up, S, sbits, c.d_info);
+  }
   if (!rc) rc = chol_inverse(c, S, X, n);
   if (!rc) rc = rmul_tc_ranges(c, Ar, 2 * ngw, 2 * ngw, n, X, 1, Ar, 2 * ngw, c.geq0, c.d_info, kb, R, done, sliced);
   if (rc) {
