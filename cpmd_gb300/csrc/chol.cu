@@ -592,17 +592,116 @@ __global__ void __launch_bounds__(32 * PR) k_chol_df(const double* __restrict__ 
   }
 }
 
+// The diagonal block k of the blocked chain in double-float (the elimination of
+// k_chol_df on a 32 x 32 block, scalar pairs): X_kk = U_kk^-1 of the block's
+// current Schur complement, without the FP64 pivot chain of k_chol_diag.
+// Scaled by the block's own diagonal; a pivot at or below 2^-40 of the row's
+// original diagonal (diag0) stops with status (global index + 1), a NaN one with
+// -1.  Writes the diagonal block of X (zero below its diagonal) and leaves Uw's
+// diagonal block alone (the panel, update and inverse kernels read only X_kk
+// and Uw's off-diagonal blocks).
+__device__ __forceinline__ Dfl df_sub_mul(Dfl m, Dfl w, Dfl v) {
+  const float np = __fmul_rn(-w.h, v.h);
+  float pe = __fmaf_rn(w.h, v.h, np);
+  pe = __fmaf_rn(w.h, v.l, pe);
+  pe = __fmaf_rn(w.l, v.h, pe);
+  const Dfl s = df_two_sum(m.h, np);
+  return df_two_sum(s.h, __fadd_rn(s.l, __fsub_rn(m.l, pe)));
+}
+
+__global__ void __launch_bounds__(8 * B) k_chol_diag_df(const double* __restrict__ S, double* __restrict__ X,
+                                                        const double* __restrict__ diag0, int n, int k,
+                                                        int* __restrict__ status) {
+  pdl_entry();
+  __shared__ float2 buf[2][B];
+  __shared__ float2 piv[B];
+  __shared__ float thr[B];
+  __shared__ int kx[B];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int base = k * B, m = min(B, n - base);
+  if (failed(status)) return;
+  if (threadIdx.x < B) {
+    const int t = threadIdx.x;
+    int kk = 0;
+    float th = 0.0f;
+    if (t < m) {
+      const int E = (int)((__double_as_longlong(S[(size_t)(base + t) * n + base + t]) >> 52) & 0x7FF);
+      if (E != 0 && E != 0x7FF) kk = -((E - 1023) >> 1);
+      th = 0x1p-40f * df_of_double(diag0[base + t], 2 * kk).h;
+    }
+    kx[t] = kk;
+    thr[t] = th;
+    buf[0][t] = buf[1][t] = make_float2(0.0f, 0.0f);
+  }
+  __syncthreads();
+  Dfl M[B / 8];  // slots (i, lane), i = w + 8 a
+#pragma unroll
+  for (int a = 0; a < B / 8; ++a) {
+    const int i = w + 8 * a;
+    M[a] = {0.0f, 0.0f};
+    if (i < m && lane <= i) M[a] = df_of_double(S[(size_t)(base + lane) * n + base + i], kx[i] + kx[lane]);
+    if (i < m && lane == 0) buf[0][i] = make_float2(M[a].h, M[a].l);
+  }
+  for (int j = 0; j < m; ++j) {
+    __syncthreads();
+    const float2* b = buf[j & 1];
+    float2* bn = buf[(j + 1) & 1];
+    const float2 dv = b[j];
+    if (!(dv.x > thr[j])) {  // the same pivot in every thread: a uniform exit
+      if (threadIdx.x == 0) atomicExch(status, dv.x != dv.x ? -1 : base + j + 1);
+      return;
+    }
+    if (threadIdx.x == 0) piv[j] = dv;
+    const Dfl rd = df_rcp({dv.x, dv.y});
+    const float2 vq = b[lane];
+#pragma unroll
+    for (int a = 0; a < B / 8; ++a) {
+      const int i = w + 8 * a;
+      if (i > j && i < m) {  // warp-uniform
+        const float2 bi = b[i];
+        const Dfl wi = df_mul({bi.x, bi.y}, rd);
+        if (lane <= i) M[a] = (lane == j) ? Dfl{-wi.h, -wi.l} : df_sub_mul(M[a], wi, {vq.x, vq.y});
+        if (i == j + 1) {
+          if (lane <= i) bn[lane] = make_float2(M[a].h, M[a].l);
+        } else if (lane == j + 1) {
+          bn[i] = make_float2(M[a].h, M[a].l);
+        }
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int a = 0; a < B / 8; ++a) {
+    const int i = w + 8 * a;
+    if (i < m && lane < m) {
+      double* xb = X + (size_t)base * n + base;
+      if (lane < i) {
+        const Dfl ri = df_rsqrt({piv[i].x, piv[i].y});
+        xb[(size_t)lane * n + i] = df_to_double(df_mul(M[a], ri), kx[lane]);
+        xb[(size_t)i * n + lane] = 0.0;
+      } else if (lane == i) {
+        xb[(size_t)i * n + i] = df_to_double(df_rsqrt({piv[i].x, piv[i].y}), kx[i]);
+      }
+    }
+  }
+}
+
 }  // namespace
 
 // Queue U = chol(S) and X = U^{-1}; no synchronisation.  S is overwritten (the
 // blocked FP64 chain) or left as it was (the one-CTA double-float kernel).
 int chol_inverse(Ctx& c, double* S, double* X, int n) {
-  if (n <= 128 && (c.chol_df == 2 || (c.chol_df == 1 && c.precision == 1))) {
+  // double-float: the whole job in one CTA up to 64 states, the diagonal blocks of
+  // the blocked chain above (one CTA for all 128 states is slower than the chain)
+  const bool df = c.chol_df == 2 || (c.chol_df == 1 && c.precision == 1);
+  if (df && n <= 64) {
     ProfScope ps_(c, "k_chol_df");
-    if (n <= 64)
-      GBCP_LAUNCH_PDL(c, (k_chol_df<64, 8>), dim3(1), dim3(256), 0, (const double*)S, X, n, c.d_info);
-    else
-      GBCP_LAUNCH_PDL(c, (k_chol_df<128, 16>), dim3(1), dim3(512), 0, (const double*)S, X, n, c.d_info);
+    GBCP_LAUNCH_PDL(c, (k_chol_df<64, 8>), dim3(1), dim3(256), 0, (const double*)S, X, n, c.d_info);
+    return 0;
+  }
+  if (c.chol_df == 3 && n <= 128) {
+    ProfScope ps_(c, "k_chol_df");
+    GBCP_LAUNCH_PDL(c, (k_chol_df<128, 16>), dim3(1), dim3(512), 0, (const double*)S, X, n, c.d_info);
     return 0;
   }
   const int nb = (n + B - 1) / B;
@@ -617,7 +716,11 @@ int chol_inverse(Ctx& c, double* S, double* X, int n) {
                     (const double*)S, diag0, n);
   }
   for (int k = 0; k < nb; ++k) {
-    {
+    if (df) {
+      ProfScope ps_(c, "k_chol_diag");
+      GBCP_LAUNCH_PDL(c, k_chol_diag_df, dim3(1), dim3(8 * B), 0, (const double*)S, X, (const double*)diag0, n, k,
+                      c.d_info);
+    } else {
       ProfScope ps_(c, "k_chol_diag");
       GBCP_LAUNCH_PDL(c, k_chol_diag, dim3(1), dim3(8 * B), 0, (const double*)S, Uw, X, (const double*)diag0, n, k,
                       c.d_info);

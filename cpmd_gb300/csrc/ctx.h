@@ -126,7 +126,7 @@ struct Ctx {
   int fft_engine = 0;  // band-loop FFTs: 0 four-step where a plan exists, else Stockham; 2 Stockham always
   int plane = 1;       // FP32 band loop, y and x stages fused per z-plane where the plane fits: bit 0 vpsi, bit 1 rhoofr
   int test_stall = 0;  // test hook: the next tensor-core overlap issues no loads and times out (one call)
-  int chol_df = 0;     // U^-1 for n <= 128 in one CTA in double-float: 0 never, 1 mixed precision, 2 both precisions
+  int chol_df = 1;     // double-float Cholesky (one CTA to 64 states, diagonal blocks above): 0 never, 1 mixed, 2 both, 3 one CTA to 128
   int oz_ksplit = 0;   // split GEMM partition: K splits per overlap tile (0 = fill the SMs)
   int oz_rgrid = 0;    // split GEMM partition: persistent CTAs of C M (0 = one per SM)
   const char* rmul_name = nullptr;  // profiler name of the next split C M products (Loewdin's n x n ones)

@@ -114,13 +114,15 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  *                   in a way that keeps that key must drop the copy by setting
  *                   the option again (any value).  0 (the default) = off;
  *   GBCP_OPT_CHOL   Cholesky factor and inverse of the ortho overlap matrix:
- *                   0 (the default) = blocked FP64 over many CTAs; 1 = for
- *                   nstate <= 128 in the MIXED precision, one CTA in
- *                   double-float arithmetic (about 2^-46 relative per
- *                   operation; a pivot at or below 2^-40 of its row's original
- *                   diagonal reports GBCP_ERR_NOT_SPD, where the FP64 chain
- *                   uses 2^-46; at 128 states it takes longer than the FP64
- *                   chain on GB300); 2 = that kernel in both precisions;
+ *                   0 = blocked FP64 over many CTAs; 1 (the default) = in the
+ *                   MIXED precision, double-float arithmetic (FP32 pairs, about
+ *                   2^-46 relative per operation) for the whole job in one CTA
+ *                   up to 64 states and for the 32 x 32 diagonal blocks of the
+ *                   blocked chain above, where FP64 pivot chains are slow on
+ *                   GB300; a pivot at or below 2^-40 of its row's original
+ *                   diagonal then reports GBCP_ERR_NOT_SPD (the FP64 chain:
+ *                   2^-46); 2 = that in both precisions; 3 = as 2, with the
+ *                   one-CTA kernel up to 128 states;
  *   GBCP_OPT_TEST_TIMEOUT  test hook of the failure path: 1 = the next overlap
  *                   on the tensor cores issues no operand loads, so its first
  *                   bounded wait (no copy in flight towards it) runs out after

@@ -1,8 +1,11 @@
-"""The one-CTA double-float Cholesky factor and inverse of ortho (GBCP_OPT_CHOL).
+"""The double-float Cholesky factor and inverse of ortho (GBCP_OPT_CHOL): one CTA
+up to 64 states (128 with option 3), double-float diagonal blocks of the
+blocked chain above.
 
-Gram-Schmidt through it must match the oracle's rgs (dpotrf + dtrtri + dtrmm,
+Gram-Schmidt through them must match the oracle's rgs (dpotrf + dtrtri + dtrmm,
 rgs_utils.mod.F90:63-74, 95-162) and keep ||C^H C - I|| <= 1e-12 at every size
-it takes (1..128 states: both instances, partial column pairs), be invariant to
+(1..200 states: both one-CTA instances, partial column pairs, partial diagonal
+blocks), be invariant to
 positive scaling of the states (the power-of-two scaling of the overlap matrix
 keeps any magnitude inside FP32's range) and report an exactly dependent set as
 not positive definite, like the FP64 chain.
@@ -32,14 +35,15 @@ def orthonormality(c, geq0=True):
     return float(np.abs(s - np.eye(s.shape[0])).max())
 
 
-@pytest.mark.parametrize("nstate", [1, 5, 33, 64, 65, 97, 128])
-def test_gs_double_float_matches_oracle(gpu_lib, nstate):
+@pytest.mark.parametrize("nstate,opt", [(1, 1), (5, 1), (33, 1), (64, 1), (65, 1), (97, 1), (128, 1), (200, 1),
+                                       (65, 3), (128, 3)])
+def test_gs_double_float_matches_oracle(gpu_lib, nstate, opt):
     from cpmd_gb300 import Context
     cl = make_small_cell(10.26, 32, 20.0, nstate, seed=300 + nstate)
     c = perturbed(cl.c0, 0.03, nstate)
     ref = O.rgs(c, cl.basis.geq0)
     ctx = Context(cl.basis, "mixed")
-    ctx.set_option("chol", 1)
+    ctx.set_option("chol", opt)
     out = c.copy(order="F")
     ctx.ortho(out, "gs")
     assert rel(out, ref) < 1e-12
@@ -49,34 +53,36 @@ def test_gs_double_float_matches_oracle(gpu_lib, nstate):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_chol_option_engines_agree(gpu_lib, precision):
-    """Option 0 (blocked FP64, the default), 1 (double-float in the mixed precision) and 2
-    (double-float in both) give the same orthonormal set to 1e-12."""
+    """Options 0 (blocked FP64), 1 (double-float in the mixed precision, the
+    default), 2 (double-float in both) and 3 (one CTA to 128 states) give the same
+    orthonormal set to 1e-12."""
     from cpmd_gb300 import Context
     cl = make_small_cell(10.26, 32, 20.0, 100, seed=411)
     c = perturbed(cl.c0, 0.05, 7)
     ctx = Context(cl.basis, precision)
     outs = []
-    for opt in (0, 1, 2):
+    for opt in (0, 1, 2, 3):
         ctx.set_option("chol", opt)
         out = c.copy(order="F")
         ctx.ortho(out, "gs")
         outs.append(out)
-    assert rel(outs[1], outs[0]) < 1e-12
-    assert rel(outs[2], outs[0]) < 1e-12
-    assert orthonormality(outs[2], cl.basis.geq0) <= 1e-12
+    for o in outs[1:]:
+        assert rel(o, outs[0]) < 1e-12
+        assert orthonormality(o, cl.basis.geq0) <= 1e-12
 
 
-def test_gs_double_float_scale_invariant(gpu_lib):
+@pytest.mark.parametrize("nstate", [48, 100])
+def test_gs_double_float_scale_invariant(gpu_lib, nstate):
     """Gram-Schmidt of states scaled by 2^-40 .. 2^40 (overlap entries 2^-80 ..
     2^80, far outside FP32's range unscaled) is the Gram-Schmidt of the states.
     FP64 GEMMs around the double-float kernel (option 2): the tensor-core C M
     bounds its error by the row maxima of C, which such a spread of state
     norms defeats whatever the Cholesky does."""
     from cpmd_gb300 import Context
-    cl = make_small_cell(10.26, 32, 20.0, 48, seed=412)
+    cl = make_small_cell(10.26, 32, 20.0, nstate, seed=412)
     c = perturbed(cl.c0, 0.02, 8)
     ref = O.rgs(c, cl.basis.geq0)
-    scales = 2.0 ** np.linspace(-40, 40, 48).round()
+    scales = 2.0 ** np.linspace(-40, 40, nstate).round()
     cs = np.asfortranarray(c * scales[None, :])
     ctx = Context(cl.basis, "fp64")
     ctx.set_option("chol", 2)
