@@ -448,7 +448,7 @@ int gbcp_set_option(gbcp_ctx* h, int key, int value) {
     c.plane = value;
     return GBCP_OK;
   }
-  if (key == GBCP_OPT_CHOL && value >= 0 && value <= 2) {
+  if (key == GBCP_OPT_CHOL && value >= 0 && value <= 3) {
     c.chol_df = value;
     return GBCP_OK;
   }
