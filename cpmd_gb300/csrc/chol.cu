@@ -363,13 +363,20 @@ __device__ __forceinline__ Dfl df_mul(Dfl a, Dfl b) {
   e = __fmaf_rn(a.l, b.h, e);
   return df_fast(p, e);
 }
-// 1 / d: the correctly rounded FP32 reciprocal r and one Newton step,
-// r + r (1 - d r) with the residual taken in double-float
+// 1 / d: the hardware reciprocal estimate, one Newton step r + r (1 - d r) in
+// FP32 and one with the residual taken in double-float (no branch, no slow path)
 __device__ __forceinline__ Dfl df_rcp(Dfl d) {
-  const float r = __frcp_rn(d.h);
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d.h));
+  r = __fmaf_rn(r, __fmaf_rn(-d.h, r, 1.0f), r);
   float e = __fmaf_rn(-d.h, r, 1.0f);
   e = __fmaf_rn(-d.l, r, e);
   return df_fast(r, __fmul_rn(r, e));
+}
+// d + 1
+__device__ __forceinline__ Dfl df_add1(Dfl d) {
+  const Dfl s = df_two_sum(d.h, 1.0f);
+  return df_fast(s.h, __fadd_rn(s.l, d.l));
 }
 // d^-1/2: an FP32 estimate, one Newton step y (3 - d y^2) / 2 in FP32 and one
 // y + y (1 - d y^2) / 2 with d y^2 in double-float (1 - d y^2 is exact there)
@@ -491,78 +498,99 @@ __global__ void __launch_bounds__(32 * PR) k_chol_df(const double* __restrict__ 
     }
     if (threadIdx.x == 0) piv[j] = dv;
     const Dfl rd = df_rcp({dv.x, dv.y});
+    // entry j of the vector is d + 1: the generic update then turns A_ij = w_i d into
+    // -w_i = Z_ij, and rows i <= j get w = 0, an exact no-op, so that all rows of a
+    // warp update in one branch-free block (a row has slots in pair p only when
+    // PR a >= 64 p, known at compile time)
     u64 vh[NP], vl[NP];
 #pragma unroll 16
     for (int p = 0; p < NP; ++p) {
-      const float2 x0 = b[lane + 64 * p], x1 = b[lane + 64 * p + 32];
+      float2 x0 = b[lane + 64 * p], x1 = b[lane + 64 * p + 32];
+      if (lane == (j & 31) && (j >> 6) == p) {
+        const Dfl d1 = df_add1({dv.x, dv.y});
+        if (j & 32)
+          x1 = make_float2(d1.h, d1.l);
+        else
+          x0 = make_float2(d1.h, d1.l);
+      }
       vh[p] = p2(x0.x, x1.x);
       vl[p] = p2(x0.y, x1.y);
     }
-    const int j1 = j + 1;
+    u64 wh[RA], wl[RA], nwh[RA];
 #pragma unroll 16
     for (int a = 0; a < RA; ++a) {
       const int i = w + PR * a;
-      if (i > j && i < n) {  // warp-uniform
       const float2 bi = b[i];
-      const Dfl wi = df_mul({bi.x, bi.y}, rd);
-      const u64 wh = p2(wi.h, wi.h), wl = p2(wi.l, wi.l), nwh = p2(-wi.h, -wi.h);
+      Dfl wi = df_mul({bi.x, bi.y}, rd);
+      if (!(i > j && i < n)) wi = {0.0f, 0.0f};
+      wh[a] = p2(wi.h, wi.h);
+      wl[a] = p2(wi.l, wi.l);
+      nwh[a] = p2(-wi.h, -wi.h);
+    }
+#pragma unroll 16
+    for (int a = 0; a < RA; ++a) {
 #pragma unroll 16
       for (int p = 0; p < NP; ++p) {
-        if (64 * p <= i) {  // some slot of this pair on the row (warp-uniform)
-        // (H, L) -= w v: TwoProduct of the hi parts, TwoSum into H, the rest into L
-        const u64 np = pmul(nwh, vh[p]);
-        u64 pe = pfma(wh, vh[p], np);
-        pe = pfma(wh, vl[p], pe);
-        pe = pfma(wl, vh[p], pe);
-        const u64 s = padd(H[a][p], np);
-        const u64 bb = psub(s, H[a][p]);
-        const u64 e = padd(psub(H[a][p], psub(s, bb)), psub(np, bb));
-        H[a][p] = s;
-        L[a][p] = padd(e, psub(L[a][p], pe));
-        if (j & 1) {  // renormalise every second step: the lo parts' own rounding stays at 2^-48 of hi
-          const u64 s2 = padd(H[a][p], L[a][p]);
-          const u64 b2 = psub(s2, H[a][p]);
-          L[a][p] = padd(psub(H[a][p], psub(s2, b2)), psub(L[a][p], b2));
-          H[a][p] = s2;
-        }
-        if ((j >> 6) == p && lane == (j & 31)) {  // slot (i, j): Z_ij = -w_i
-          float h0 = p2lo(H[a][p]), h1 = p2hi(H[a][p]), l0 = p2lo(L[a][p]), l1 = p2hi(L[a][p]);
-          if (j & 32) {
-            h1 = -wi.h;
-            l1 = -wi.l;
-          } else {
-            h0 = -wi.h;
-            l0 = -wi.l;
-          }
-          H[a][p] = p2(h0, h1);
-          L[a][p] = p2(l0, l1);
-        }
+        if (64 * p <= PR * a) {
+          // (H, L) -= w v: TwoProduct of the hi parts, TwoSum into H, the rest into L
+          const u64 np = pmul(nwh[a], vh[p]);
+          u64 pe = pfma(wh[a], vh[p], np);
+          pe = pfma(wh[a], vl[p], pe);
+          pe = pfma(wl[a], vh[p], pe);
+          const u64 s = padd(H[a][p], np);
+          const u64 bb = psub(s, H[a][p]);
+          const u64 e = padd(psub(H[a][p], psub(s, bb)), psub(np, bb));
+          H[a][p] = s;
+          L[a][p] = padd(e, psub(L[a][p], pe));
         }
       }
-      // the vector of step j + 1: row j + 1 (Z part and pivot), then column j + 1
-      if (i == j1) {
+    }
+    if (j & 1) {  // renormalise every second step: the lo parts' own rounding stays at 2^-48 of hi
 #pragma unroll 16
-        for (int p = 0; p < NP; ++p) {
-          const int q0 = lane + 64 * p;
-          if (q0 <= i) {
-            const Dfl t = df_two_sum(p2lo(H[a][p]), p2lo(L[a][p]));
-            bn[q0] = make_float2(t.h, t.l);
+      for (int a = 0; a < RA; ++a)
+#pragma unroll 16
+        for (int p = 0; p < NP; ++p)
+          if (64 * p <= PR * a) {
+            const u64 s2 = padd(H[a][p], L[a][p]);
+            const u64 b2 = psub(s2, H[a][p]);
+            L[a][p] = padd(psub(H[a][p], psub(s2, b2)), psub(L[a][p], b2));
+            H[a][p] = s2;
           }
-          if (q0 + 32 <= i) {
-            const Dfl t = df_two_sum(p2hi(H[a][p]), p2hi(L[a][p]));
-            bn[q0 + 32] = make_float2(t.h, t.l);
+    }
+    // the vector of step j + 1: row j + 1 (Z part and pivot) from its warp, column
+    // j + 1 from lane (j + 1) mod 32 of every warp
+    const int j1 = j + 1;
+    if (w == j1 % PR) {
+#pragma unroll 16
+      for (int a = 0; a < RA; ++a) {
+        if (w + PR * a == j1) {
+#pragma unroll 16
+          for (int p = 0; p < NP; ++p) {
+            const int q0 = lane + 64 * p;
+            if (q0 <= j1) {
+              const Dfl t = df_two_sum(p2lo(H[a][p]), p2lo(L[a][p]));
+              bn[q0] = make_float2(t.h, t.l);
+            }
+            if (q0 + 32 <= j1) {
+              const Dfl t = df_two_sum(p2hi(H[a][p]), p2hi(L[a][p]));
+              bn[q0 + 32] = make_float2(t.h, t.l);
+            }
           }
         }
-      } else if (lane == (j1 & 31)) {
+      }
+    }
+    if (lane == (j1 & 31)) {
+      const bool up = (j1 & 32) != 0;
+#pragma unroll 16
+      for (int a = 0; a < RA; ++a) {
+        const int i = w + PR * a;
 #pragma unroll 16
         for (int p = 0; p < NP; ++p) {
-          if ((j1 >> 6) == p) {
-            const bool up = (j1 & 32) != 0;
+          if (64 * p <= PR * a && (j1 >> 6) == p && i > j1 && i < n) {
             const Dfl t = df_two_sum(up ? p2hi(H[a][p]) : p2lo(H[a][p]), up ? p2hi(L[a][p]) : p2lo(L[a][p]));
             bn[i] = make_float2(t.h, t.l);
           }
         }
-      }
       }
     }
   }
@@ -653,20 +681,26 @@ __global__ void __launch_bounds__(8 * B) k_chol_diag_df(const double* __restrict
     }
     if (threadIdx.x == 0) piv[j] = dv;
     const Dfl rd = df_rcp({dv.x, dv.y});
-    const float2 vq = b[lane];
+    // entry j of the vector is d + 1: the generic update then turns A_ij = w_i d
+    // into -w_i = Z_ij; rows i <= j get w = 0, an exact no-op, so all rows of the
+    // warp update in one branch-free block
+    const float2 vq2 = b[lane];
+    const Dfl vq = (lane == j) ? df_add1({dv.x, dv.y}) : Dfl{vq2.x, vq2.y};
+    Dfl wv[B / 8];
 #pragma unroll
     for (int a = 0; a < B / 8; ++a) {
       const int i = w + 8 * a;
-      if (i > j && i < m) {  // warp-uniform
-        const float2 bi = b[i];
-        const Dfl wi = df_mul({bi.x, bi.y}, rd);
-        if (lane <= i) M[a] = (lane == j) ? Dfl{-wi.h, -wi.l} : df_sub_mul(M[a], wi, {vq.x, vq.y});
-        if (i == j + 1) {
-          if (lane <= i) bn[lane] = make_float2(M[a].h, M[a].l);
-        } else if (lane == j + 1) {
-          bn[i] = make_float2(M[a].h, M[a].l);
-        }
-      }
+      const float2 bi = b[i];
+      const Dfl t = df_mul({bi.x, bi.y}, rd);
+      wv[a] = (i > j && i < m) ? t : Dfl{0.0f, 0.0f};
+    }
+#pragma unroll
+    for (int a = 0; a < B / 8; ++a) M[a] = df_sub_mul(M[a], wv[a], vq);
+#pragma unroll
+    for (int a = 0; a < B / 8; ++a) {
+      const int i = w + 8 * a;
+      if (i == j + 1 && lane <= i) bn[lane] = make_float2(M[a].h, M[a].l);
+      if (i > j + 1 && i < m && lane == j + 1) bn[i] = make_float2(M[a].h, M[a].l);
     }
   }
   __syncthreads();
