@@ -235,6 +235,32 @@ static int build_geometry(Ctx& c, const int32_t* inyh, const double* hg) {
     if (pos_minus[ig] < 0) pos_minus[ig] = pos_plus[ig];  // G = 0 is its own mirror
   std::vector<double> hgv(hg, hg + ngw);
   std::vector<float> hg32v(hg, hg + ngw);
+  // the four-step Z-stage gather table: one coalesced load per (line, z) instead of
+  // col_start -> col_ent -> c0, and hg without a gather of its own
+  std::vector<int2> zgat;
+  {
+    const int N = n[2], N1 = gbcp::fs_n1(N), L = gbcp::fs_lines(N);
+    if (N1 > 0) {
+      const int N2 = N / N1, nblk = (ncol + L - 1) / L, h = (N + 1) / 2;
+      zgat.assign((size_t)nblk * N * L, int2{0, 0});
+      for (int b = 0; b < nblk; ++b)
+        for (int n1 = 0; n1 < N1; ++n1)
+          for (int n2 = 0; n2 < N2; ++n2)
+            for (int l = 0; l < L; ++l) {
+              const int col = b * L + l;
+              if (col >= ncol) continue;
+              const int i = n2 + N2 * n1, fz = i < h ? i : i - N;
+              const int st = col_start[col], len = col_start[col + 1] - st, off = fz - col_zlo[col];
+              if (off < 0 || off >= len) continue;
+              const int e = col_ent[st + off];
+              float hge = 0.0f;
+              if (e > 0) hge = hg32v[e - 1];
+              int bits;
+              std::memcpy(&bits, &hge, sizeof(bits));
+              zgat[(((size_t)b * N1 + n1) * N2 + n2) * L + l] = int2{e, bits};
+            }
+    }
+  }
   GeoDev& g = c.geo;
   g.geq0 = c.geq0;
   g.n1 = n[0];
@@ -251,7 +277,7 @@ static int build_geometry(Ctx& c, const int32_t* inyh, const double* hg) {
       !upload(c, col_slot, g.col_slot) || !upload(c, col_gy, g.col_gy) || !upload(c, ent_col, g.ent_col) ||
       !upload(c, slot_col0, g.slot_col0) || !upload(c, slot_gylo, g.slot_gylo) ||
       !upload(c, slot_ncol, g.slot_ncol) || !upload(c, pos_plus, g.pos_plus) || !upload(c, pos_minus, g.pos_minus) ||
-      !upload(c, hgv, g.hg) || !upload(c, hg32v, g.hg32)) {
+      !upload(c, hgv, g.hg) || !upload(c, hg32v, g.hg32) || (!zgat.empty() && !upload(c, zgat, g.zgat))) {
     c.err = "geometry upload failed";
     return 6;
   }

@@ -76,33 +76,29 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
   KinAcc<T> kacc;
   load_table(twA, twAg, N);
   __syncthreads();
+  // the gather table: one coalesced 8-byte load per (line, z), then the coefficients
+  const int2* zg = g.zgat + (size_t)blockIdx.x * (P::N1 * P::N2 * P::L);
 #pragma unroll
   for (int ia = 0; ia < P::IA; ++ia) {
     const int t = threadIdx.x + ia * kThreads;
     if (t < P::TA) {
-      const int n2 = t / P::L, l = t - n2 * P::L, col = col0 + l;
+      const int n2 = t / P::L, l = t - n2 * P::L;
       cx<T> v[P::N1];
-      int st = 0, len = 0, zlo = 0;
-      if (col < g.ncol) {
-        st = g.col_start[col];
-        len = g.col_start[col + 1] - st;
-        zlo = g.col_zlo[col];
-      }
+      int2 ce[P::N1];
+#pragma unroll
+      for (int n1 = 0; n1 < P::N1; ++n1) ce[n1] = zg[(n1 * P::N2 + n2) * P::L + l];
 #pragma unroll
       for (int n1 = 0; n1 < P::N1; ++n1) {
-        const int off = freq_split<N, P::N2>(n2, n1) - zlo;
+        const int e = ce[n1].x;
         cx<T> val = mk<T>(0, 0);
-        if (in_range(off, len)) {
-          const int e = g.col_ent[st + off];
-          if (e != 0) {
-            const int ig = (e > 0 ? e : -e) - 1;
-            const cx<double> u = c1[ig];
-            const cx<double> w = two ? c2[ig] : mk<double>(0.0, 0.0);
-            const T ux = from_double<T>(u.x), uy = from_double<T>(u.y);
-            const T wx = from_double<T>(w.x), wy = from_double<T>(w.y);
-            val = (e > 0) ? mk<T>(ux - wy, uy + wx) : mk<T>(ux + wy, wx - uy);
-            if (kpart && e > 0) kin_entry(kacc, g, ig, ux, uy, wx, wy);
-          }
+        if (e != 0) {
+          const int ig = (e > 0 ? e : -e) - 1;
+          const cx<double> u = c1[ig];
+          const cx<double> w = two ? c2[ig] : mk<double>(0.0, 0.0);
+          const T ux = from_double<T>(u.x), uy = from_double<T>(u.y);
+          const T wx = from_double<T>(w.x), wy = from_double<T>(w.y);
+          val = (e > 0) ? mk<T>(ux - wy, uy + wx) : mk<T>(ux + wy, wx - uy);
+          if (kpart && e > 0) kin_entry_t(kacc, g, ig, __int_as_float(ce[n1].y), ux, uy, wx, wy);
         }
         v[n1] = val;
       }

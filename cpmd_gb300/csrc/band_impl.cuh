@@ -149,6 +149,15 @@ __device__ __forceinline__ void kin_entry(KinAcc<float>& acc, const GeoDev& g, i
                                           float wy) {
   acc.add(0.0, g.hg32[ig], g.geq0 && ig == 0, ux, uy, wx, wy);
 }
+// the same with hg taken from the Z-stage gather table (FP32); FP64 reads hg[ig]
+__device__ __forceinline__ void kin_entry_t(KinAcc<double>& acc, const GeoDev& g, int ig, float, double ux, double uy,
+                                            double wx, double wy) {
+  kin_entry(acc, g, ig, ux, uy, wx, wy);
+}
+__device__ __forceinline__ void kin_entry_t(KinAcc<float>& acc, const GeoDev& g, int ig, float hge, float ux, float uy,
+                                            float wx, float wy) {
+  acc.add(0.0, hge, g.geq0 && ig == 0, ux, uy, wx, wy);
+}
 
 // CTA totals weighted by f1, f2 into out[0..1].  Every thread of the CTA calls it.
 __device__ __forceinline__ void kin_flush(KinAcc<double>& acc, double f1, double f2, double* __restrict__ out) {

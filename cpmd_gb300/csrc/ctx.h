@@ -65,6 +65,10 @@ struct GeoDev {
   const int* pos_minus;  // ngw: entry position of -G
   const double* hg;      // ngw
   const float* hg32;     // ngw, hg rounded to FP32 (the FP32 kernels' kinetic sums)
+  // four-step Z-stage gather (z length with a four-step plan): for column block b,
+  // n1, n2 and line l, {col_ent of column b L + l at frequency n2 + N2 n1 (0 for a
+  // hole or no column), hg of that +G entry as FP32 bits}; index ((b N1 + n1) N2 + n2) L + l
+  const int2* zgat;
   int geq0;              // entry 0 is G = 0
 };
 
