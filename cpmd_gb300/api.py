@@ -67,13 +67,14 @@ def _mem(*arrs) -> int:
     return MEM_DEVICE if kinds.pop() else MEM_HOST
 
 
-def _ld_wfn(c, ngw: int) -> tuple[int, int]:
-    """(leading dimension, nstate) of a wavefunction array."""
+def _ld_wfn(c, ngw: int, allow_c64: bool = False) -> tuple[int, int]:
+    """(leading dimension, nstate) of a wavefunction array (complex64 tensors only
+    where allow_c64: the batch's complex64 storage)."""
     if _is_torch(c):
         if c.dim() != 2:
             raise ValueError("wavefunction tensor must be (nstate, ngw)")
         import torch
-        if c.dtype != torch.complex128:
+        if c.dtype != torch.complex128 and not (allow_c64 and c.dtype == torch.complex64):
             raise ValueError("wavefunctions are complex128")
         return int(c.shape[1]), int(c.shape[0])
     if c.dtype != np.complex128 or c.ndim != 2:
@@ -142,7 +143,7 @@ class Context:
         launch), 'fft' (0 four-step, 2 Stockham), 'xchunks' (density x-stage pair chunks,
         0 = automatic) or 'xc' (energy functional: 0 LDA-PZ, 1 PBE)."""
         k = {"gemm": 1, "batch": 2, "fft": 3, "xchunks": 4, "xc": 5, "wfn_cache": 6, "plane": 7, "chol": 8,
-             "test_timeout": 90}[key]
+             "simt_tile": 9, "test_timeout": 90}[key]
         self._check("gbcp_set_option", self.lib.gbcp_set_option(self.h, k, int(value)))
 
     def synchronize(self):
@@ -476,7 +477,7 @@ class Context:
         return terms
 
 
-STEP = {"rhoofr": 1, "vpsi": 2, "ortho": 4}
+STEP = {"rhoofr": 1, "vpsi": 2, "ortho": 4, "psi_c64": 8}
 
 
 def _grid_desc(basis):
@@ -499,9 +500,10 @@ class Batch:
     """Many independent cells per step, one CUDA-graph launch (gbcp_batch_*).
 
     ``cells`` passed to :meth:`tune` / :meth:`step` is a list of dicts with
-    torch CUDA tensors ``c0`` (nstate, ngw) complex128, ``f`` (nstate,),
-    ``vpot`` and ``rhoe`` (kr3, kr2, kr1) float64 and ``c2`` like ``c0``.
-    ``flags``: an int or an iterable of "rhoofr", "vpsi", "ortho".
+    torch CUDA tensors ``c0`` (nstate, ngw) complex128 -- or complex64 in a
+    mixed-precision batch (GBCP_STEP_PSI_C64, added to the flags by itself) --,
+    ``f`` (nstate,), ``vpot`` and ``rhoe`` (kr3, kr2, kr1) float64 and ``c2``
+    like ``c0``.  ``flags``: an int or an iterable of "rhoofr", "vpsi", "ortho".
     """
 
     def __init__(self, bases, precision: str = "mixed", nstreams: int = 8):
@@ -547,8 +549,14 @@ class Batch:
         if len(cells) != len(self.bases):
             raise ValueError("one io entry per cell")
         io = (_lib.CellIO * len(cells))()
+        c64 = {str(x["c0"].dtype) == "torch.complex64" for x in cells}
+        if len(c64) != 1:
+            raise ValueError("all cells complex128, or all complex64")
+        self._c64 = c64.pop()
         for i, (x, b) in enumerate(zip(cells, self.bases)):
-            ldc, n = _ld_wfn(x["c0"], b.ngw)
+            ldc, n = _ld_wfn(x["c0"], b.ngw, allow_c64=True)
+            if x.get("c2") is not None and x["c2"].dtype != x["c0"].dtype:
+                raise ValueError("c2 must have the dtype of c0")
             io[i].c0 = _ptr(x["c0"]).value
             io[i].ldc = ldc
             io[i].nstate = n
@@ -557,14 +565,18 @@ class Batch:
             io[i].rhoe = _ptr(x.get("rhoe")).value if x.get("rhoe") is not None else None
             if x.get("c2") is not None:
                 io[i].c2 = _ptr(x["c2"]).value
-                io[i].ldc2 = _ld_wfn(x["c2"], b.ngw)[0]
+                io[i].ldc2 = _ld_wfn(x["c2"], b.ngw, allow_c64=True)[0]
         return io
+
+    def _step_flags(self, flags) -> int:
+        return self._flags(flags) | (STEP["psi_c64"] if getattr(self, "_c64", False) else 0)
 
     def tune(self, cells, flags=("rhoofr", "vpsi", "ortho")) -> str:
         import torch
         torch.cuda.synchronize()
         buf = C.create_string_buffer(8192)
-        rc = self.lib.gbcp_batch_tune(self.h, C.cast(self._io(cells), C.c_void_p), self._flags(flags), buf, 8192)
+        io = self._io(cells)
+        rc = self.lib.gbcp_batch_tune(self.h, C.cast(io, C.c_void_p), self._step_flags(flags), buf, 8192)
         if rc != 0:
             raise GbcpError("gbcp_batch_tune", rc, self.last_error())
         return buf.value.decode()
@@ -576,7 +588,8 @@ class Batch:
         n = len(self.bases)
         en = np.zeros((n, 2))
         st = np.zeros(n, dtype=np.int32)
-        rc = self.lib.gbcp_batch_step(self.h, C.cast(self._io(cells), C.c_void_p), self._flags(flags),
+        io = self._io(cells)
+        rc = self.lib.gbcp_batch_step(self.h, C.cast(io, C.c_void_p), self._step_flags(flags),
                                       en.ctypes.data_as(C.c_void_p), st.ctypes.data_as(C.c_void_p))
         if rc != 0:
             raise GbcpError("gbcp_batch_step", rc, self.last_error())

@@ -474,6 +474,10 @@ int gbcp_set_option(gbcp_ctx* h, int key, int value) {
     c.plane = value;
     return GBCP_OK;
   }
+  if (key == GBCP_OPT_SIMT_TILE && (value == 32 || value == 64)) {
+    c.simt_tile = value;
+    return GBCP_OK;
+  }
   if (key == GBCP_OPT_CHOL && value >= 0 && value <= 3) {
     c.chol_df = value;
     return GBCP_OK;

@@ -60,8 +60,8 @@ __device__ __forceinline__ void load_table(cx<T>* dst, const cx<T>* __restrict__
 
 // ---------------------------------------------------------------- Z stage (inverse, gather)
 template <typename T, int N>
-__global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>* __restrict__ c0, int ldc, int s0,
-                                                     int nstate, cx<T>* __restrict__ zbuf,
+__global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>* __restrict__ c0, int psi32, int ldc,
+                                                     int s0, int nstate, cx<T>* __restrict__ zbuf,
                                                      const cx<T>* __restrict__ twAg, const double* __restrict__ f,
                                                      double* __restrict__ kpart) {
   using P = FS<T, N>;
@@ -71,8 +71,7 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
   const int col0 = blockIdx.x * P::L, pair = blockIdx.y;
   const int is1 = s0 + 2 * pair, is2 = is1 + 1;
   const bool two = is2 < nstate;
-  const cx<double>* c1 = c0 + (size_t)is1 * ldc;
-  const cx<double>* c2 = c0 + (size_t)(two ? is2 : is1) * ldc;
+  const size_t o1 = (size_t)is1 * ldc, o2 = (size_t)(two ? is2 : is1) * ldc;
   KinAcc<T> kacc;
   load_table(twA, twAg, N);
   __syncthreads();
@@ -93,10 +92,9 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
         cx<T> val = mk<T>(0, 0);
         if (e != 0) {
           const int ig = (e > 0 ? e : -e) - 1;
-          const cx<double> u = c1[ig];
-          const cx<double> w = two ? c2[ig] : mk<double>(0.0, 0.0);
-          const T ux = from_double<T>(u.x), uy = from_double<T>(u.y);
-          const T wx = from_double<T>(w.x), wy = from_double<T>(w.y);
+          T ux, uy, wx = 0, wy = 0;
+          load_coef<T>(c0, psi32, o1 + ig, ux, uy);
+          if (two) load_coef<T>(c0, psi32, o2 + ig, wx, wy);
           val = (e > 0) ? mk<T>(ux - wy, uy + wx) : mk<T>(ux + wy, wx - uy);
           if (kpart && e > 0) kin_entry_t(kacc, g, ig, __int_as_float(ce[n1].y), ux, uy, wx, wy);
         }

@@ -139,6 +139,21 @@ template <> struct KinAcc<float> {
   }
 };
 
+// coefficient idx of c0 as stored (complex128, or complex64 with psi32) in the
+// kernel's precision
+template <typename T>
+__device__ __forceinline__ void load_coef(const cx<double>* __restrict__ c0, int psi32, size_t idx, T& x, T& y) {
+  if (psi32) {
+    const cx<float> a = reinterpret_cast<const cx<float>*>(c0)[idx];
+    x = (T)a.x;
+    y = (T)a.y;
+  } else {
+    const cx<double> a = c0[idx];
+    x = from_double<T>(a.x);
+    y = from_double<T>(a.y);
+  }
+}
+
 // One +G entry (e > 0) of the gather: u, w the two states' coefficients as the
 // kernel holds them (FP64, or FP32-rounded).
 __device__ __forceinline__ void kin_entry(KinAcc<double>& acc, const GeoDev& g, int ig, double ux, double uy,
@@ -214,8 +229,8 @@ __device__ __forceinline__ void kin_flush(KinAcc<float>& acc, double f1, double 
 
 // ---------------------------------------------------------------- Z stage (inverse, gather)
 template <typename T, int NC>
-__global__ void __launch_bounds__(kThreads) k_zinv(GeoDev g, FftPlan p, const cx<double>* __restrict__ c0, int ldc,
-                                                  int s0, int nstate, int nlrt, cx<T>* __restrict__ zbuf,
+__global__ void __launch_bounds__(kThreads) k_zinv(GeoDev g, FftPlan p, const cx<double>* __restrict__ c0, int psi32,
+                                                  int ldc, int s0, int nstate, int nlrt, cx<T>* __restrict__ zbuf,
                                                   const cx<T>* __restrict__ twg, const double* __restrict__ f,
                                                   double* __restrict__ kpart) {
   GBCP_STAGE(g.n3, nlrt)
@@ -223,8 +238,7 @@ __global__ void __launch_bounds__(kThreads) k_zinv(GeoDev g, FftPlan p, const cx
   const int col0 = blockIdx.x * nl;
   const int is1 = s0 + 2 * pair, is2 = is1 + 1;
   const bool two = is2 < nstate;
-  const cx<double>* c1 = c0 + (size_t)is1 * ldc;
-  const cx<double>* c2 = c0 + (size_t)(two ? is2 : is1) * ldc;
+  const size_t o1 = (size_t)is1 * ldc, o2 = (size_t)(two ? is2 : is1) * ldc;
   KinAcc<T> kacc;
   load_tw(tw, twg, N);
   for (int idx = threadIdx.x; idx < nl * N; idx += kThreads) {
@@ -237,11 +251,10 @@ __global__ void __launch_bounds__(kThreads) k_zinv(GeoDev g, FftPlan p, const cx
         const int e = g.col_ent[st + off];
         if (e != 0) {
           const int ig = (e > 0 ? e : -e) - 1;
-          const cx<double> u = c1[ig];
-          const cx<double> w = two ? c2[ig] : mk<double>(0.0, 0.0);
+          T ux, uy, wx = 0, wy = 0;
+          load_coef<T>(c0, psi32, o1 + ig, ux, uy);
+          if (two) load_coef<T>(c0, psi32, o2 + ig, wx, wy);
           // +G: c1 + i c2 ; -G: conj(c1) + i conj(c2)
-          const T ux = from_double<T>(u.x), uy = from_double<T>(u.y);
-          const T wx = from_double<T>(w.x), wy = from_double<T>(w.y);
           v = (e > 0) ? mk<T>(ux - wy, uy + wx) : mk<T>(ux + wy, wx - uy);
           if (kpart && e > 0) kin_entry(kacc, g, ig, ux, uy, wx, wy);
         }
@@ -437,16 +450,41 @@ template <> __device__ __forceinline__ double to_double<float>(float x) { return
 // c2 += -f/2 (tpiba2 hg c0 + (Re fp, Im fm)) for state 1 and -f/2 (... + (Im fp, -Re fm))
 // for state 2; fp/fm in the transform precision, the update in FP64 (two FMAs per
 // component; kin = tpiba2 hg precomputed).
+// psi32 (FP32 kernels only): c0 and c2 stored as complex64, the update in FP32.
 template <typename T>
 __global__ void k_decode(GeoDev g, const cx<T>* __restrict__ qbuf, const cx<double>* __restrict__ c0, int ldc,
                          cx<double>* __restrict__ c2, int ldc2, const double* __restrict__ f, int s0, int nstate,
-                         const double* __restrict__ kin_g) {
+                         const double* __restrict__ kin_g, int psi32) {
   const int ig = blockIdx.x * blockDim.x + threadIdx.x;
   const int pair = blockIdx.y;
   if (ig >= g.ngw) return;
   const int is1 = s0 + 2 * pair, is2 = is1 + 1;
   const cx<T>* qb = qbuf + (size_t)pair * g.nent;
   const cx<T> qp = qb[g.pos_plus[ig]], qm = qb[g.pos_minus[ig]];
+  if (psi32) {
+    const float kin = d2f_int(kin_g[ig]);
+    const cx<float>* a0 = reinterpret_cast<const cx<float>*>(c0);
+    cx<float>* a2 = reinterpret_cast<cx<float>*>(c2);
+    const float q1x = (float)(qp.x + qm.x), q1y = (float)(qp.y - qm.y);
+    const float q2x = (float)(qp.y + qm.y), q2y = (float)(qm.x - qp.x);
+    float fi = d2f_int(f[is1]) * 0.5f;
+    if (fi == 0.0f) fi = 1.0f;
+    {
+      const cx<float> c = a0[(size_t)is1 * ldc + ig];
+      cx<float>& o = a2[(size_t)is1 * ldc2 + ig];
+      o.x = fmaf(-fi, fmaf(kin, c.x, q1x), o.x);
+      o.y = fmaf(-fi, fmaf(kin, c.y, q1y), o.y);
+    }
+    if (is2 < nstate) {
+      float fip1 = d2f_int(f[is2]) * 0.5f;
+      if (fip1 == 0.0f) fip1 = 1.0f;
+      const cx<float> c = a0[(size_t)is2 * ldc + ig];
+      cx<float>& o = a2[(size_t)is2 * ldc2 + ig];
+      o.x = fmaf(-fip1, fmaf(kin, c.x, q2x), o.x);
+      o.y = fmaf(-fip1, fmaf(kin, c.y, q2y), o.y);
+    }
+    return;
+  }
   const double kin = kin_g[ig];
   double fi = f[is1] * 0.5;
   if (fi == 0.0) fi = 1.0;
@@ -552,13 +590,13 @@ int launch_zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int n
   if constexpr (NC > 0) {
     constexpr size_t sm = fs_smem<T, NC>(1, 1);
     allow_smem(k_zinv_fs<T, NC>, sm);
-    k_zinv_fs<T, NC><<<dim3(zinv_blocks_n<T, NC>(c), np), kThreads, sm, c.stream>>>(g, c0, ldc, s0, nstate, zb,
+    k_zinv_fs<T, NC><<<dim3(zinv_blocks_n<T, NC>(c), np), kThreads, sm, c.stream>>>(g, c0, c.psi32, ldc, s0, nstate, zb,
                                                                                     twA_of<T>(c, 2), f, kpart);
   } else {
     const int nl = lines_rt(g.n3);
     const size_t sm = stage_smem<T>(g.n3, nl);
     allow_smem(k_zinv<T, 0>, sm);
-    k_zinv<T, 0><<<dim3(zinv_blocks_n<T, 0>(c), np), kThreads, sm, c.stream>>>(g, c.plan[2], c0, ldc, s0, nstate, nl,
+    k_zinv<T, 0><<<dim3(zinv_blocks_n<T, 0>(c), np), kThreads, sm, c.stream>>>(g, c.plan[2], c0, c.psi32, ldc, s0, nstate, nl,
                                                                                zb, tw_of<T>(c, 2), f, kpart);
   }
   GBCP_LAUNCH_CHECK(c);
@@ -825,7 +863,8 @@ int launch_decode(Ctx& c, int np, const cx<double>* c0, int ldc, cx<double>* c2,
   const GeoDev& g = c.geo;
   ProfScope ps_(c, "k_decode");
   const cx<T>* qb = static_cast<const cx<T>*>(c.qbuf.p) + (size_t)poff * g.nent;  // pair poff of the launch batch
-  k_decode<T><<<dim3((g.ngw + 255) / 256, np), 256, 0, c.stream>>>(g, qb, c0, ldc, c2, ldc2, f, s0, nstate, c.kin);
+  k_decode<T><<<dim3((g.ngw + 255) / 256, np), 256, 0, c.stream>>>(g, qb, c0, ldc, c2, ldc2, f, s0, nstate, c.kin,
+                                                                   c.psi32);
   GBCP_LAUNCH_CHECK(c);
   return 0;
 }

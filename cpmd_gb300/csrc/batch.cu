@@ -16,9 +16,11 @@
 // Autotuner: cells with equal mesh, sphere and state count form a size class.
 // For the first cell of each class it times (CUDA events, copies of that cell's
 // states) every band-loop configuration -- FFT kernels (four-step register
-// codelets or run-time planned Stockham) x state pairs per launch -- and then
-// the overlap/U^-1 GEMM engine of ortho (FP64 SIMT or tcgen05 split precision),
-// and applies the fastest to the whole class.
+// codelets or run-time planned Stockham) x state pairs per launch x plane-fused
+// y/x stages -- and then the ortho GEMMs (FP64 SIMT with 64 x 64 or 32 x 32
+// output tiles, or the tcgen05 split GEMM with its K-split and C M partitions)
+// x the Cholesky (blocked FP64 or double-float), and applies the fastest to the
+// whole class.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -68,10 +70,31 @@ int fail(gbcp_batch* b, int rc, const std::string& msg) {
   return rc;
 }
 
+// complex64 (ld lda) <-> complex128 (ld ngw) for ortho on complex64 storage; the
+// conversions are integer operations on the bit patterns (exact one way, round
+// to nearest the other)
+__global__ void k_c64_to_c128(const cx<float>* __restrict__ a, int lda, cx<double>* __restrict__ b, int ngw, int n) {
+  const size_t tot = (size_t)ngw * n;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t s = e / ngw, g = e - s * ngw;
+    const cx<float> v = a[s * lda + g];
+    b[e] = gbcp::mk<double>(gbcp::f2d_int(v.x), gbcp::f2d_int(v.y));
+  }
+}
+__global__ void k_c128_to_c64(const cx<double>* __restrict__ b, int ngw, int n, cx<float>* __restrict__ a, int lda) {
+  const size_t tot = (size_t)ngw * n;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t s = e / ngw, g = e - s * ngw;
+    const cx<double> v = b[e];
+    a[s * lda + g] = gbcp::mk<float>(gbcp::d2f_int(v.x), gbcp::d2f_int(v.y));
+  }
+}
+
 // all work of one cell, queued on c.stream; no host synchronisation
 int queue_cell(Ctx& c, const gbcp_cell_io& io, int flags, double* dout, int* dstatus) {
   cx<double>* c0 = reinterpret_cast<cx<double>*>(io.c0);
   int rc = 0;
+  c.psi32 = (flags & GBCP_STEP_PSI_C64) ? 1 : 0;
   if (flags & GBCP_STEP_RHOOFR) {
     // E_kin summed in the band loop's gather, as in gbcp_rhoofr (the scalars stay on the device)
     if (!gbcp::ensure(c, c.rho_sc, 4 * sizeof(double))) return 6;
@@ -86,7 +109,19 @@ int queue_cell(Ctx& c, const gbcp_cell_io& io, int flags, double* dout, int* dst
       return rc;
   }
   if (flags & GBCP_STEP_ORTHO) {
-    if ((rc = gbcp::ortho_gs_queue(c, c0, io.ldc, io.nstate))) return rc;
+    if (c.psi32) {
+      // FP64 Gram-Schmidt on a widened copy, rounded back into the complex64 states
+      if (!gbcp::ensure(c, c.st_c0, sizeof(cx<double>) * (size_t)c.ngw * io.nstate)) return 6;
+      cx<double>* w = static_cast<cx<double>*>(c.st_c0.p);
+      const int nb = std::max(1, std::min(1024, (int)(((size_t)c.ngw * io.nstate + 255) / 256)));
+      k_c64_to_c128<<<nb, 256, 0, c.stream>>>(reinterpret_cast<const cx<float>*>(io.c0), io.ldc, w, c.ngw, io.nstate);
+      GBCP_LAUNCH_CHECK(c);
+      if ((rc = gbcp::ortho_gs_queue(c, w, c.ngw, io.nstate))) return rc;
+      k_c128_to_c64<<<nb, 256, 0, c.stream>>>(w, c.ngw, io.nstate, reinterpret_cast<cx<float>*>(io.c0), io.ldc);
+      GBCP_LAUNCH_CHECK(c);
+    } else if ((rc = gbcp::ortho_gs_queue(c, c0, io.ldc, io.nstate))) {
+      return rc;
+    }
     GBCP_CUDA_TRY(c, cudaMemcpyAsync(dstatus, c.d_info, sizeof(int), cudaMemcpyDeviceToDevice, c.stream));
   } else {
     GBCP_CUDA_TRY(c, cudaMemsetAsync(dstatus, 0, sizeof(int), c.stream));
@@ -166,7 +201,9 @@ bool same_class(const Ctx& a, int na, const Ctx& c, int nc) {
 }
 
 int check_io(gbcp_batch* b, const gbcp_cell_io* io, int flags) {
-  if (!io || flags <= 0 || flags > 7) return fail(b, GBCP_ERR_ARG, "batch: bad flags or io");
+  if (!io || (flags & 7) == 0 || flags > 15) return fail(b, GBCP_ERR_ARG, "batch: bad flags or io");
+  if ((flags & GBCP_STEP_PSI_C64) && b->precision != GBCP_PREC_MIXED)
+    return fail(b, GBCP_ERR_ARG, "batch: complex64 states need the MIXED precision");
   for (size_t i = 0; i < b->cells.size(); ++i) {
     const Ctx& c = b->cells[i]->c;
     const gbcp_cell_io& x = io[i];
@@ -289,8 +326,9 @@ int gbcp_batch_tune(gbcp_batch* b, const gbcp_cell_io* io, int flags, char* repo
     Ctx& c = b->cells[i0]->c;
     const gbcp_cell_io& x = io[i0];
     // private copies of the head cell's states and output so tuning leaves the caller's data alone
-    const size_t wbytes = sizeof(cx<double>) * (size_t)x.ldc * x.nstate;
-    const size_t w2bytes = x.c2 ? sizeof(cx<double>) * (size_t)x.ldc2 * x.nstate : 0;
+    const size_t esz = (flags & GBCP_STEP_PSI_C64) ? sizeof(cx<float>) : sizeof(cx<double>);
+    const size_t wbytes = esz * (size_t)x.ldc * x.nstate;
+    const size_t w2bytes = x.c2 ? esz * (size_t)x.ldc2 * x.nstate : 0;
     void *t0 = nullptr, *t2 = nullptr;
     if (cudaMalloc(&t0, wbytes) != cudaSuccess || (w2bytes && cudaMalloc(&t2, w2bytes) != cudaSuccess)) {
       if (t0) cudaFree(t0);
@@ -311,14 +349,14 @@ int gbcp_batch_tune(gbcp_batch* b, const gbcp_cell_io* io, int flags, char* repo
     if (npairs <= gbcp::kMaxBatch) batches.push_back(npairs);
     float best = 1e30f, t = 0.f;
     int best_e = c.fft_engine, best_b = c.batch, best_g = c.gemm_mode, best_p = c.plane;
-    int best_ks = c.oz_ksplit, best_rg = c.oz_rgrid;
-    const int band_flags = flags & (GBCP_STEP_RHOOFR | GBCP_STEP_VPSI);
+    int best_ks = c.oz_ksplit, best_rg = c.oz_rgrid, best_ts = c.simt_tile, best_ch = c.chol_df;
+    const int band_flags = flags & (GBCP_STEP_RHOOFR | GBCP_STEP_VPSI | GBCP_STEP_PSI_C64);
     // plane-fused y/x stages (FP32, four-step meshes whose plane fits): none, vpsi,
     // rhoofr or both
     std::vector<int> planes{0};
     if (c.precision == GBCP_PREC_MIXED) planes = {0, 1, 2, 3};
-    char line[320];
-    if (band_flags) {
+    char line[400];
+    if (band_flags & (GBCP_STEP_RHOOFR | GBCP_STEP_VPSI)) {
       for (int e : engines)
         for (int bt : batches)
           for (int pl : planes) {
@@ -343,39 +381,53 @@ int gbcp_batch_tune(gbcp_batch* b, const gbcp_cell_io* io, int flags, char* repo
       best_o = 1e30f;
       // GEMM engine, and for the split GEMM its partition: K splits of the overlap
       // tiles and persistent CTAs of C U^-1 (many cells share the SMs in a batch)
+      // (FP64 SIMT: output tile 64 or 32), and the Cholesky (blocked FP64 or, in the
+      // mixed precision, double-float)
       struct Part {
-        int g, ks, rg;
+        int g, ks, rg, ts;
       };
-      std::vector<Part> parts{{0, 0, 0}};
+      std::vector<Part> parts{{0, 0, 0, 64}, {0, 0, 0, 32}};
       for (int ks : {0, 1, 2, 4, 8})
-        for (int rg : {0, 16, 38, 76}) parts.push_back({1, ks, rg});
-      for (const Part& q : parts) {
-        c.gemm_mode = q.g;
-        c.oz_ksplit = q.ks;
-        c.oz_rgrid = q.rg;
-        if ((rc = time_cell(b, c, xt, GBCP_STEP_ORTHO, b->d_out + 2 * i0, b->d_status + i0, &t))) break;
-        if (t < best_o) {
-          best_o = t;
-          best_g = q.g;
-          best_ks = q.ks;
-          best_rg = q.rg;
+        for (int rg : {0, 16, 38, 76}) parts.push_back({1, ks, rg, 64});
+      std::vector<int> chols{0};
+      if (c.precision == GBCP_PREC_MIXED) chols.push_back(1);
+      for (const Part& q : parts)
+        for (int ch : chols) {
+          c.gemm_mode = q.g;
+          c.oz_ksplit = q.ks;
+          c.oz_rgrid = q.rg;
+          c.simt_tile = q.ts;
+          c.chol_df = ch;
+          if ((rc = time_cell(b, c, xt, GBCP_STEP_ORTHO | (flags & GBCP_STEP_PSI_C64), b->d_out + 2 * i0,
+                              b->d_status + i0, &t)))
+            break;
+          if (t < best_o) {
+            best_o = t;
+            best_g = q.g;
+            best_ks = q.ks;
+            best_rg = q.rg;
+            best_ts = q.ts;
+            best_ch = ch;
+          }
         }
-      }
       c.gemm_mode = best_g;
       c.oz_ksplit = best_ks;
       c.oz_rgrid = best_rg;
+      c.simt_tile = best_ts;
+      c.chol_df = best_ch;
     }
     cudaStreamSynchronize(b->s0);
     cudaFree(t0);
     if (t2) cudaFree(t2);
     if (rc) return fail(b, rc, "batch tune: " + c.err);
     static const char* plane_name[4] = {"three-stage", "plane vpsi", "plane rhoofr", "plane rhoofr+vpsi"};
-    char gemm[64];
+    char gemm[96];
+    const char* chol = best_ch ? "double-float" : "fp64 blocked";
     if (best_g == 1)
-      std::snprintf(gemm, sizeof(gemm), "tcgen05 (K splits %s%d, C M CTAs %s%d)", best_ks ? "" : "auto ",
-                    best_ks, best_rg ? "" : "auto ", best_rg);
+      std::snprintf(gemm, sizeof(gemm), "tcgen05 (K splits %s%d, C M CTAs %s%d), Cholesky %s", best_ks ? "" : "auto ",
+                    best_ks, best_rg ? "" : "auto ", best_rg, chol);
     else
-      std::snprintf(gemm, sizeof(gemm), "fp64-simt");
+      std::snprintf(gemm, sizeof(gemm), "fp64-simt (tile %dx%d), Cholesky %s", best_ts, best_ts, chol);
     std::snprintf(line, sizeof(line), "mesh %dx%dx%d ngw %d nstate %d (%d cells): fft %s %s, %d pairs/launch, ortho %s; "
                                       "band %.3f ms, ortho %.3f ms\n",
                   c.nr[0], c.nr[1], c.nr[2], c.ngw, x.nstate,
@@ -391,6 +443,8 @@ int gbcp_batch_tune(gbcp_batch* b, const gbcp_cell_io* io, int flags, char* repo
         ci.gemm_mode = best_g;
         ci.oz_ksplit = best_ks;
         ci.oz_rgrid = best_rg;
+        ci.simt_tile = best_ts;
+        ci.chol_df = best_ch;
       }
   }
   if (report && report_len > 0) {

@@ -129,10 +129,12 @@ struct Ctx {
   int xc = 0;          // energy functional: 0 LDA (Slater + Perdew-Zunger), 1 PBE
   int fft_engine = 0;  // band-loop FFTs: 0 four-step where a plan exists, else Stockham; 2 Stockham always
   int plane = 1;       // FP32 band loop, y and x stages fused per z-plane where the plane fits: bit 0 vpsi, bit 1 rhoofr
+  int psi32 = 0;       // batch steps: c0 / c2 stored as complex64 (FP32 band loop only)
   int test_stall = 0;  // test hook: the next tensor-core overlap issues no loads and times out (one call)
   int chol_df = 1;     // double-float Cholesky (one CTA to 64 states, diagonal blocks above): 0 never, 1 mixed, 2 both, 3 one CTA to 128
   int oz_ksplit = 0;   // split GEMM partition: K splits per overlap tile (0 = fill the SMs)
   int oz_rgrid = 0;    // split GEMM partition: persistent CTAs of C M (0 = one per SM)
+  int simt_tile = 64;  // FP64 SIMT overlap / C M GEMMs: output tile 64 or 32
   const char* rmul_name = nullptr;  // profiler name of the next split C M products (Loewdin's n x n ones)
   WfnCache wfn;        // host wavefunction kept on the device between host-memory calls
   cudaStream_t stream = nullptr;  // stream all work is queued on

@@ -34,12 +34,16 @@ constexpr int TS = 64;   // output tile
 constexpr int BK = 16;   // K step
 constexpr int NT = 256;  // threads (16 x 16, 4 x 4 outputs each)
 
-// Partial S over one K-chunk for one upper tile pair (bi <= bj).
+// Partial S over one K-chunk for one upper tile pair (bi <= bj), TT x TT output
+// tiles (TT = 64 or 32: 4 x 4 or 2 x 2 outputs per thread; the batch autotuner
+// picks per size class).
 // A(k, i) = Ar[k + i*lda]  (real view of C, lda = 2*ldc, K = 2*ngw)
+template <int TT = TS>
 __global__ void __launch_bounds__(NT) k_syrk_part(const double* __restrict__ Ar, int lda, int K, int n, int ntb,
                                                   int kchunk, double* __restrict__ part) {
-  __shared__ double As[BK][TS + 1];
-  __shared__ double Bs[BK][TS + 1];
+  constexpr int U = TT / 16;
+  __shared__ double As[BK][TT + 1];
+  __shared__ double Bs[BK][TT + 1];
   // decode tile pair from blockIdx.x over the upper triangle of ntb x ntb tiles
   int t = blockIdx.x, bi = 0;
   while (t >= ntb - bi) {
@@ -50,11 +54,11 @@ __global__ void __launch_bounds__(NT) k_syrk_part(const double* __restrict__ Ar,
   const int split = blockIdx.y;
   const int k0 = split * kchunk, k1 = min(K, k0 + kchunk);
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  double acc[4][4] = {};
-  const int i0 = bi * TS, j0 = bj * TS;
+  double acc[U][U] = {};
+  const int i0 = bi * TT, j0 = bj * TT;
   for (int kb = k0; kb < k1; kb += BK) {
-    // load 16 x 64 for both operands: thread -> (k = tid % 16, col = tid / 16 + 16 q)
-    for (int q = 0; q < 4; ++q) {
+    // load 16 x TT for both operands: thread -> (k = tid % 16, col = tid / 16 + 16 q)
+    for (int q = 0; q < U; ++q) {
       const int kk = threadIdx.x % 16, cc = threadIdx.x / 16 + 16 * q;
       const int k = kb + kk;
       const int ci = i0 + cc, cj = j0 + cc;
@@ -64,25 +68,25 @@ __global__ void __launch_bounds__(NT) k_syrk_part(const double* __restrict__ Ar,
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
-      double a[4], b[4];
+      double a[U], b[U];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < U; ++u) {
         a[u] = As[kk][ty + 16 * u];
         b[u] = Bs[kk][tx + 16 * u];
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
+      for (int u = 0; u < U; ++u)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+        for (int v = 0; v < U; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
     }
     __syncthreads();
   }
   // part[split][i][j] (row-major n x n)
   double* P = part + (size_t)split * n * n;
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < U; ++u)
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
+    for (int v = 0; v < U; ++v) {
       const int i = i0 + ty + 16 * u, j = j0 + tx + 16 * v;
       if (i < n && j < n) P[(size_t)i * n + j] = acc[u][v];
     }
@@ -90,13 +94,13 @@ __global__ void __launch_bounds__(NT) k_syrk_part(const double* __restrict__ Ar,
 
 // S[i][j] = 2 sum_split part - Re c0_i Re c0_j for the upper triangle tiles,
 // mirrored into the lower triangle.  Column-major == row-major (symmetric).
-__global__ void k_syrk_fold(const double* __restrict__ part, int nsplit, int n, int ntb, const double* __restrict__ Ar,
+__global__ void k_syrk_fold(const double* __restrict__ part, int nsplit, int n, int ts, const double* __restrict__ Ar,
                             int lda, int geq0, double* __restrict__ S, unsigned long long* __restrict__ scond_bits) {
   const size_t nn = (size_t)n * n;
   double mx = 0.0;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nn; e += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(e / n), j = (int)(e % n);
-    const int bi = i / TS, bj = j / TS;
+    const int bi = i / ts, bj = j / ts;
     if (bi > bj) continue;  // lower block triangle handled by mirroring
     double s = 0.0;
     for (int p = 0; p < nsplit; ++p) s += part[(size_t)p * nn + e];
@@ -114,49 +118,52 @@ __global__ void k_syrk_fold(const double* __restrict__ part, int nsplit, int n, 
   }
 }
 
-// Cout = A * M.  A real view (rows = 2 ngw, lda), M (n x n) row-major (M[k][j]).
+// Cout = A * M.  A real view (rows = 2 ngw, lda), M (n x n) row-major (M[k][j]),
+// TT x TT output tiles (64 or 32).
 // upper != 0: M is upper triangular, column block j only needs k <= j.
+template <int TT = TS>
 __global__ void __launch_bounds__(NT) k_gemm_right(const double* __restrict__ A, int lda, int rows, int n,
                                                    const double* __restrict__ M, int upper, double* __restrict__ Cout,
                                                    int ldo, const int* __restrict__ status) {
-  __shared__ double As[BK][TS + 1];
-  __shared__ double Ms[BK][TS + 1];
+  constexpr int U = TT / 16, R = NT / TT;  // outputs per thread per dimension, k rows per load pass
+  __shared__ double As[BK][TT + 1];
+  __shared__ double Ms[BK][TT + 1];
   if (*(volatile const int*)status != 0) return;
-  const int r0 = blockIdx.x * TS, j0 = blockIdx.y * TS;
+  const int r0 = blockIdx.x * TT, j0 = blockIdx.y * TT;
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  double acc[4][4] = {};
-  const int kend = upper ? min(n, j0 + TS) : n;
+  double acc[U][U] = {};
+  const int kend = upper ? min(n, j0 + TT) : n;
   for (int kb = 0; kb < kend; kb += BK) {
-    for (int q = 0; q < 4; ++q) {
-      // A tile: 64 rows x 16 k, coalesced along rows
-      const int rr = threadIdx.x % 64, kk = threadIdx.x / 64 + 4 * q;
+    for (int q = 0; q < BK / R; ++q) {
+      // A tile: TT rows x 16 k, coalesced along rows
+      const int rr = threadIdx.x % TT, kk = threadIdx.x / TT + R * q;
       const int r = r0 + rr, k = kb + kk;
       As[kk][rr] = (r < rows && k < n) ? A[r + (size_t)k * lda] : 0.0;
-      // M tile: 16 k x 64 cols
-      const int cc = threadIdx.x % 64, km = threadIdx.x / 64 + 4 * q;
+      // M tile: 16 k x TT cols
+      const int cc = threadIdx.x % TT, km = threadIdx.x / TT + R * q;
       const int c = j0 + cc, k2 = kb + km;
       Ms[km][cc] = (c < n && k2 < n) ? M[(size_t)k2 * n + c] : 0.0;
     }
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
-      double a[4], b[4];
+      double a[U], b[U];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < U; ++u) {
         a[u] = As[kk][tx + 16 * u];
         b[u] = Ms[kk][ty + 16 * u];
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
+      for (int u = 0; u < U; ++u)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
+        for (int v = 0; v < U; ++v) acc[u][v] = fma(a[u], b[v], acc[u][v]);
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < U; ++u)
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
+    for (int v = 0; v < U; ++v) {
       const int r = r0 + tx + 16 * u, c = j0 + ty + 16 * v;
       if (r < rows && c < n) Cout[r + (size_t)c * ldo] = acc[u][v];
     }
@@ -333,7 +340,8 @@ int ovlap_gamma_ex(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S,
   const int n = nstate;
   const int K = 2 * c.ngw;
   const int lda = 2 * ldc;
-  const int ntb = (n + TS - 1) / TS;
+  const int ts = c.simt_tile == 32 ? 32 : TS;
+  const int ntb = (n + ts - 1) / ts;
   const int npairs = ntb * (ntb + 1) / 2;
   // enough CTAs to fill the GPU: ~4 waves of 152 SMs
   int nsplit = std::max(1, std::min(1024, (4 * 152 + npairs - 1) / npairs));
@@ -345,13 +353,16 @@ int ovlap_gamma_ex(Ctx& c, const cx<double>* c0, int ldc, int nstate, double* S,
   double* part = static_cast<double*>(c.sparts.p);
   {
     ProfScope ps_(c, "k_syrk_part");
-    k_syrk_part<<<dim3(npairs, nsplit), NT, 0, c.stream>>>(Ar, lda, K, n, ntb, kchunk, part);
+    if (ts == 32)
+      k_syrk_part<32><<<dim3(npairs, nsplit), NT, 0, c.stream>>>(Ar, lda, K, n, ntb, kchunk, part);
+    else
+      k_syrk_part<TS><<<dim3(npairs, nsplit), NT, 0, c.stream>>>(Ar, lda, K, n, ntb, kchunk, part);
     GBCP_LAUNCH_CHECK(c);
   }
   const int fb = std::max(1, std::min(1024, (n * n + 255) / 256));
   {
     ProfScope ps_(c, "k_syrk_fold");
-    k_syrk_fold<<<fb, 256, 0, c.stream>>>(part, nsplit, n, ntb, Ar, lda, c.geq0, S, bits);
+    k_syrk_fold<<<fb, 256, 0, c.stream>>>(part, nsplit, n, ts, Ar, lda, c.geq0, S, bits);
     GBCP_LAUNCH_CHECK(c);
   }
   return 0;
@@ -376,10 +387,15 @@ static int apply_right(Ctx& c, cx<double>* c0, int ldc, int nstate, const double
   if (!ensure(c, c.cscr, sizeof(double) * (size_t)rows * nstate)) return 6;
   double* tmp = static_cast<double*>(c.cscr.p);
   {
-    dim3 grid((rows + TS - 1) / TS, (nstate + TS - 1) / TS);
+    const int ts = c.simt_tile == 32 ? 32 : TS;
+    dim3 grid((rows + ts - 1) / ts, (nstate + ts - 1) / ts);
     ProfScope ps_(c, "k_gemm_right");
-    k_gemm_right<<<grid, NT, 0, c.stream>>>(reinterpret_cast<const double*>(c0), lda, rows, nstate, M, upper, tmp, rows,
-                                            c.d_info);
+    if (ts == 32)
+      k_gemm_right<32><<<grid, NT, 0, c.stream>>>(reinterpret_cast<const double*>(c0), lda, rows, nstate, M, upper,
+                                                  tmp, rows, c.d_info);
+    else
+      k_gemm_right<TS><<<grid, NT, 0, c.stream>>>(reinterpret_cast<const double*>(c0), lda, rows, nstate, M, upper,
+                                                  tmp, rows, c.d_info);
     GBCP_LAUNCH_CHECK(c);
   }
   {
@@ -766,11 +782,11 @@ extern "C" int gbcp_ovlap_noalloc(const double* c0, int ldc, int ngw, int nstate
   kchunk = ((kchunk + BK - 1) / BK) * BK;
   nsplit = (K + kchunk - 1) / kchunk;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  k_syrk_part<<<dim3(npairs, nsplit), NT, 0, st>>>(c0, lda, K, n, ntb, kchunk, scratch);
+  k_syrk_part<TS><<<dim3(npairs, nsplit), NT, 0, st>>>(c0, lda, K, n, ntb, kchunk, scratch);
   count_launch();
   if (cudaGetLastError() != cudaSuccess) return 5;
   const int fb = std::max(1, std::min(1024, (int)((nn + 255) / 256)));
-  k_syrk_fold<<<fb, 256, 0, st>>>(scratch, nsplit, n, ntb, c0, lda, geq0 ? 1 : 0, smat, nullptr);
+  k_syrk_fold<<<fb, 256, 0, st>>>(scratch, nsplit, n, TS, c0, lda, geq0 ? 1 : 0, smat, nullptr);
   count_launch();
   if (cudaGetLastError() != cudaSuccess) return 5;
   return 0;

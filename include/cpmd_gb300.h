@@ -123,6 +123,9 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  *                   diagonal then reports GBCP_ERR_NOT_SPD (the FP64 chain:
  *                   2^-46); 2 = that in both precisions; 3 = as 2, with the
  *                   one-CTA kernel up to 128 states;
+ *   GBCP_OPT_SIMT_TILE  output tile of the FP64 SIMT overlap and C M GEMMs:
+ *                   64 (the default) or 32 (less padding for small state
+ *                   counts; the batch autotuner chooses per size class);
  *   GBCP_OPT_TEST_TIMEOUT  test hook of the failure path: 1 = the next overlap
  *                   on the tensor cores issues no operand loads, so its first
  *                   bounded wait (no copy in flight towards it) runs out after
@@ -130,7 +133,7 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  *                   c0 untouched and the hook clears itself. */
 enum gbcp_option { GBCP_OPT_GEMM = 1, GBCP_OPT_BATCH = 2, GBCP_OPT_FFT = 3, GBCP_OPT_XCHUNKS = 4, GBCP_OPT_XC = 5,
                    GBCP_OPT_WFN_CACHE = 6, GBCP_OPT_PLANE = 7, GBCP_OPT_CHOL = 8,
-                   GBCP_OPT_TEST_TIMEOUT = 90 };
+                   GBCP_OPT_SIMT_TILE = 9, GBCP_OPT_TEST_TIMEOUT = 90 };
 int gbcp_set_option(gbcp_ctx* ctx, int key, int value);
 /* Queue later work on `stream` (a cudaStream_t; NULL = the context's own
  * stream; the CUDA legacy default stream is cudaStreamLegacy).  Device-pointer calls are ordered only with respect to this stream,
@@ -327,7 +330,13 @@ typedef struct gbcp_cell_io {
   double* c2;          /* (ldc2, nstate) complex, accumulated by GBCP_STEP_VPSI */
   int32_t ldc2;
 } gbcp_cell_io;
-enum gbcp_step_flags { GBCP_STEP_RHOOFR = 1, GBCP_STEP_VPSI = 2, GBCP_STEP_ORTHO = 4 };
+/* GBCP_STEP_PSI_C64 (MIXED batches): c0 and c2 of every cell hold complex64
+ * (pairs of float, ldc / ldc2 in complex elements) instead of complex128.  The
+ * band loop reads and accumulates them directly (half the coefficient traffic);
+ * ortho widens c0 to FP64, runs the FP64-accurate Gram-Schmidt and rounds the
+ * result back, so its orthonormality is that of complex64 (~1e-7); E_kin and
+ * int V rho stay FP64 sums. */
+enum gbcp_step_flags { GBCP_STEP_RHOOFR = 1, GBCP_STEP_VPSI = 2, GBCP_STEP_ORTHO = 4, GBCP_STEP_PSI_C64 = 8 };
 /* `nstreams` worker streams run cells side by side (0 = 8). */
 int gbcp_batch_create(int ncells, const gbcp_grid_desc* grids, int precision, int nstreams, gbcp_batch** out);
 int gbcp_batch_destroy(gbcp_batch* batch);

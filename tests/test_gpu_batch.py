@@ -96,3 +96,39 @@ def test_make_batch_shapes():
         assert nat in (8, 16, 32, 64)
         assert cl.c0.shape[1] == 2 * nat
         assert cl.basis.nr[0] in (32, 36, 40, 48, 60, 64, 72, 80, 96)
+
+
+def test_batch_complex64_states(gpu_lib, cells):
+    """Complex64 storage of the states (GBCP_STEP_PSI_C64, a mixed batch): rho and
+    E_kin are those of a mixed context on the same (complex64-representable)
+    states, C2 agrees to FP32 rounding (the update runs in FP32 into complex64),
+    and ortho gives the oracle's Gram-Schmidt of those states rounded to complex64."""
+    import torch
+    from cpmd_gb300 import Batch
+    bt = Batch([c.basis for c in cells], "mixed", nstreams=4)
+    io = dev_io(cells)
+    for x in io:
+        x["c0"] = x["c0"].to(torch.complex64)
+        x["c2"] = x["c2"].to(torch.complex64)
+    report = bt.tune(io)
+    assert report.count("\n") == 3
+    c0_in = [np.asfortranarray(x["c0"].cpu().numpy().T).astype(np.complex128) for x in io]
+    en, st = bt.step(io)
+    assert (st == 0).all()
+    from cpmd_gb300 import Context
+    for cl, x, e, c in zip(cells, io, en, c0_in):
+        b = cl.basis
+        ctx = Context(b, "mixed")
+        rho, ekin, _, _ = ctx.rhoofr(c, cl.f)
+        c2 = np.zeros_like(c)
+        ctx.vpsi(c, c2, cl.f, cl.vpot)
+        ctx.close()
+        assert rel(x["rhoe"].cpu().numpy(), rho) < 1e-12
+        assert abs(e[0] - ekin) <= 1e-12 * abs(ekin)
+        assert rel(np.asfortranarray(x["c2"].cpu().numpy().T).astype(np.complex128), c2) < 1e-6
+        out = np.asfortranarray(x["c0"].cpu().numpy().T).astype(np.complex128)
+        ref = O.rgs(c, b.geq0)
+        assert rel(out, ref) < 1e-6
+        s = O.overlap(out, b.geq0)
+        assert np.abs(s - np.eye(s.shape[0])).max() < 1e-6
+    bt.close()

@@ -87,3 +87,18 @@ def test_ortho_tensor_cores_match_oracle(gpu_lib, nstate, method):
     ctx.ortho(out, method)
     assert rel(out, ref) < 1e-12
     assert np.all(out[0].imag == 0.0)
+
+
+@pytest.mark.parametrize("nstate", [16, 37, 100])
+def test_simt_tile_32_matches_oracle(gpu_lib, nstate):
+    """The 32 x 32 tile of the FP64 SIMT overlap and C M GEMMs (GBCP_OPT_SIMT_TILE)
+    gives the oracle's overlap and Gram-Schmidt to 1e-12."""
+    from cpmd_gb300 import Context
+    cl = make_small_cell(10.26, 32, 20.0, nstate, seed=500 + nstate)
+    c = perturbed(cl.c0, 0.03, nstate)
+    ctx = Context(cl.basis, "fp64")
+    ctx.set_option("simt_tile", 32)
+    assert rel(ctx.ovlap(c), O.overlap(c, cl.basis.geq0)) < 1e-13
+    out = c.copy(order="F")
+    ctx.ortho(out, "gs")
+    assert rel(out, O.rgs(c, cl.basis.geq0)) < 1e-12
