@@ -728,23 +728,26 @@ def run_extras(args, dev):
     cells = make_batch(64)
     nst = sum(cc.c0.shape[1] for cc in cells)
 
-    def io_of():
+    def io_of(c64=False):
         io = []
+        dt = torch.complex64 if c64 else torch.complex128
         for cc in cells:
             bb = cc.basis
-            io.append(dict(c0=torch.from_numpy(np.ascontiguousarray(cc.c0.T)).to(dev), f=torch.from_numpy(cc.f).to(dev),
-                           vpot=torch.from_numpy(cc.vpot).to(dev),
+            io.append(dict(c0=torch.from_numpy(np.ascontiguousarray(cc.c0.T)).to(dev).to(dt),
+                           f=torch.from_numpy(cc.f).to(dev), vpot=torch.from_numpy(cc.vpot).to(dev),
                            rhoe=torch.empty(tuple(bb.kr[::-1]), dtype=torch.float64, device=dev),
-                           c2=torch.zeros((cc.c0.shape[1], bb.ngw), dtype=torch.complex128, device=dev)))
+                           c2=torch.zeros((cc.c0.shape[1], bb.ngw), dtype=dt, device=dev)))
         return io
 
     r = {}
     en = {}
-    for prec in ("mixed", "fp64"):
-        io = io_of()
+    # the configuration as specified (complex64 states, FP64 energies), then complex128
+    # states in the mixed and FP64 precisions
+    for key, prec, c64 in (("mixed_c64", "mixed", True), ("mixed", "mixed", False), ("fp64", "fp64", False)):
+        io = io_of(c64)
         bt = Batch([cc.basis for cc in cells], prec, nstreams=16)
         report = bt.tune(io)
-        en[prec] = bt.step(io)[0]
+        en[key] = bt.step(io)[0]
         for _ in range(3):
             bt.step(io)
         steps = 10
@@ -753,8 +756,19 @@ def run_extras(args, dev):
         for _ in range(steps):
             bt.step(io)
         ms = (time.perf_counter() - t0) / steps * 1e3
-        r[prec] = {"state_applies_per_s": nst / (ms / 1e3), "ms_per_step": ms,
-                   "kernels_per_graph_launch": bt.graph_kernels(), "autotuner": report.strip().split("\n")}
+        r[key] = {"state_applies_per_s": nst / (ms / 1e3), "ms_per_step": ms, "states": "complex64" if c64 else
+                  "complex128", "kernels_per_graph_launch": bt.graph_kernels(),
+                  "autotuner": report.strip().split("\n")}
+        if c64:
+            # orthonormality of the stored complex64 states after the last step's ortho
+            worst = 0.0
+            for cc, x in zip(cells, io):
+                cm = x["c0"].to(torch.complex128)
+                sm = 2.0 * (cm.conj() @ cm.T).real
+                if cc.basis.geq0:
+                    sm -= torch.outer(cm[:, 0].real, cm[:, 0].real)
+                worst = max(worst, float((sm - torch.eye(sm.shape[0], dtype=sm.dtype, device=dev)).abs().max()))
+            r[key]["orthonormality_after_ortho"] = worst
         bt.close()
         del io
     # the same cells through one context each, no graph, one stream
@@ -776,8 +790,10 @@ def run_extras(args, dev):
         cx_.close()
     nats = np.array([cc.tau.shape[0] for cc in cells])
     de = np.abs(en["mixed"].sum(axis=1) - en["fp64"].sum(axis=1)) / nats
+    de64 = np.abs(en["mixed_c64"].sum(axis=1) - en["fp64"].sum(axis=1)) / nats
     r["mixed_sequential_contexts"] = {"state_applies_per_s": nst / (ms_seq / 1e3), "ms_per_step": ms_seq}
     r["dE_Ha_per_atom_mixed_vs_fp64_max"] = float(de.max())
+    r["dE_Ha_per_atom_mixed_c64_vs_fp64_max"] = float(de64.max())
     # CPU baseline: the C++/OpenMP restatement on one cell of each size class (full steps),
     # weighted by the number of cells in the class
     classes = {}
