@@ -101,8 +101,9 @@ def test_make_batch_shapes():
 def test_batch_complex64_states(gpu_lib, cells):
     """Complex64 storage of the states (GBCP_STEP_PSI_C64, a mixed batch): rho and
     E_kin are those of a mixed context on the same (complex64-representable)
-    states, C2 agrees to FP32 rounding (the update runs in FP32 into complex64),
-    and ortho gives the oracle's Gram-Schmidt of those states rounded to complex64."""
+    states to FP32 rounding (the autotuner may pick other launch shapes), C2 too
+    (the update runs in FP32 into complex64), and ortho gives the oracle's
+    Gram-Schmidt of those states rounded to complex64."""
     import torch
     from cpmd_gb300 import Batch
     bt = Batch([c.basis for c in cells], "mixed", nstreams=4)
@@ -123,8 +124,8 @@ def test_batch_complex64_states(gpu_lib, cells):
         c2 = np.zeros_like(c)
         ctx.vpsi(c, c2, cl.f, cl.vpot)
         ctx.close()
-        assert rel(x["rhoe"].cpu().numpy(), rho) < 1e-12
-        assert abs(e[0] - ekin) <= 1e-12 * abs(ekin)
+        assert rel(x["rhoe"].cpu().numpy(), rho) < 2e-6
+        assert abs(e[0] - ekin) <= 1e-7 * abs(ekin)
         assert rel(np.asfortranarray(x["c2"].cpu().numpy().T).astype(np.complex128), c2) < 1e-6
         out = np.asfortranarray(x["c0"].cpu().numpy().T).astype(np.complex128)
         ref = O.rgs(c, b.geq0)
