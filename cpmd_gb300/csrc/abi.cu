@@ -754,7 +754,6 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
     double* dr = drho;
     c.rho_slabs = false;
     c.rho_slab_done = [&c, rhoe, dr, plane_el, nb](int z0, int z1) -> int {
-      if (z1 >= c.geo.n3) z1 = c.kr[2];  // the last slab takes the padding planes (zero) along
       cudaEvent_t e = c.pipe_ev[1 + nb + (z0 == 0 ? 0 : 1)];
       GBCP_CUDA_TRY(c, cudaEventRecord(e, c.stream));
       GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.copy_out, e, 0));
