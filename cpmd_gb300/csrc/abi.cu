@@ -736,7 +736,7 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
       return GBCP_ERR_NOMEM;
     cx<double>* t = static_cast<cx<double>*>(c.st_c0.p);
     const int nb = stage_plan(c, nstate);
-    if ((rc = pipe_prepare(c, nb + 2))) return rc;  // + the density slab events
+    if ((rc = pipe_prepare(c, nb))) return rc;
     const bool resident = wfn_hit(c, c0, ldc, nstate);
     for (int b = 0; b < nb; ++b) {
       const int s0 = 2 * c.stage_bounds[b], ns = std::min(2 * c.stage_bounds[b + 1], nstate) - s0;
@@ -749,19 +749,6 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
     df = static_cast<double*>(tf);
     drho = static_cast<double*>(c.st_rho.p);
     dld = c.ngw;
-    // the final density goes down in z slabs as the last x-stage group finishes them
-    const size_t plane_el = (size_t)c.kr[0] * c.kr[1];
-    double* dr = drho;
-    c.rho_slabs = false;
-    c.rho_slab_done = [&c, rhoe, dr, plane_el, nb](int z0, int z1) -> int {
-      cudaEvent_t e = c.pipe_ev[1 + nb + (z0 == 0 ? 0 : 1)];
-      GBCP_CUDA_TRY(c, cudaEventRecord(e, c.stream));
-      GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.copy_out, e, 0));
-      gbcp::ProfScope ps_(c, "d2h_rho", c.copy_out, 2);
-      GBCP_CUDA_TRY(c, cudaMemcpyAsync(rhoe + plane_el * z0, dr + plane_el * z0, sizeof(double) * plane_el * (z1 - z0),
-                                       cudaMemcpyDeviceToHost, c.copy_out));
-      return 0;
-    };
   }
   // E_kin and csumg are summed inside the band loop's gather, csumr from the
   // density, all on the device; the host reads the three at the end
@@ -773,15 +760,8 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
   }
   rc = gbcp::band_rhoofr(c, dc0, dld, nstate, df, drho, dsc);
   c.batch_ready = nullptr;
-  c.rho_slab_done = nullptr;
   if (saved_batch) c.batch = saved_batch;
-  if (mem == GBCP_MEM_HOST && c.rho_slabs) {
-    // the context stream (and so finish) waits for the slab downloads
-    cudaEvent_t e = c.pipe_ev[c.pipe_ev.size() - 1];
-    cudaEventRecord(e, c.copy_out);
-    cudaStreamWaitEvent(c.stream, e, 0);
-    c.rho_slabs = false;
-  } else if (!rc && mem == GBCP_MEM_HOST) {
+  if (!rc && mem == GBCP_MEM_HOST) {
     gbcp::ProfScope ps_(c, "d2h_rho", c.stream, 2);
     cudaError_t e = cudaMemcpyAsync(rhoe, drho, sizeof(double) * nnr1, cudaMemcpyDeviceToHost, c.stream);
     if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));

@@ -646,11 +646,8 @@ inline int xrho_chunks(const Ctx& c, int tiles, int np) {
 }
 
 template <typename T, int NC>
-// z planes [z0, z0 + nz) (nz = 0: all); the four-step kernel only splits by z
-int launch_xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho, int poff, int z0 = 0,
-                    int nz = 0) {
+int launch_xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho, int poff) {
   const GeoDev& g = c.geo;
-  if (nz <= 0) nz = g.n3 - z0;
   // pairs poff .. poff+np-1 of the launch batch (states from s0)
   const cx<T>* yb = static_cast<const cx<T>*>(c.ybuf.p) + (size_t)poff * g.n3 * g.n2 * g.nslot;
   if constexpr (NC > 0) {
@@ -678,13 +675,9 @@ int launch_xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double*
     }
     allow_smem(k_xrho_fs<T, NC>, sm);
     ProfScope ps_(c, "k_xinv_rho");
-    k_xrho_fs<T, NC><<<dim3(nchunk, tiles_y, nz), kThreads, sm, c.stream>>>(
-        g, yb, np, s0, nstate, f, 1.0 / c.omega, rho, twA_of<T>(c, 0), pchunk, part, tickets, z0);
+    k_xrho_fs<T, NC><<<dim3(nchunk, tiles_y, g.n3), kThreads, sm, c.stream>>>(
+        g, yb, np, s0, nstate, f, 1.0 / c.omega, rho, twA_of<T>(c, 0), pchunk, part, tickets);
   } else {
-    if (z0 != 0 || nz != g.n3) {
-      c.err = "density x-stage: z ranges need a four-step plan";
-      return 7;
-    }
     int nl = lines_rt(g.n1);
     while (nl > 1 && nl * g.n1 > kMaxAcc * kThreads) --nl;
     if (nl * g.n1 > kMaxAcc * kThreads) {
@@ -886,9 +879,8 @@ template <typename T> int yinv(Ctx& c, int np, int poff = 0) {
   GBCP_DISPATCH(launch_yinv, T, band_len(c, c.nr[1]), c, np, poff)
 }
 template <typename T>
-int xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho, int poff = 0, int z0 = 0,
-             int nz = 0) {
-  GBCP_DISPATCH(launch_xinv_rho, T, band_len(c, c.nr[0]), c, np, s0, nstate, f, rho, poff, z0, nz)
+int xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho, int poff = 0) {
+  GBCP_DISPATCH(launch_xinv_rho, T, band_len(c, c.nr[0]), c, np, s0, nstate, f, rho, poff)
 }
 template <typename T> int xvx(Ctx& c, int np, const double* vpot, const T* vpotT) {
   GBCP_DISPATCH(launch_xvx, T, band_len(c, c.nr[0]), c, np, vpot, vpotT)
@@ -948,16 +940,12 @@ int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f,
       if ((rc = density(p0, p0 + np, p0))) return rc;
     } else {
       // host staging: Z and Y stages of each staging chunk as its states land; the
-      // density x-stage (which gains most from many pairs per launch) in groups of
-      // chunks: all but the last two, then each of those, so that little x work is
-      // left after the last upload.  The last group runs in z slabs, each handed to
-      // rho_slab_done (its download starts while the next slab computes).
+      // density x-stage (which gains most from many pairs per launch) in two groups
+      // of chunks, the first overlapping the later uploads, the second the tail
       const std::vector<int>& b = c.stage_bounds;
-      const int nq = (int)b.size() - 1;
-      const bool last_batch = p0 + np >= npairs_total;
-      const bool slabs = last_batch && c.rho_slab_done && !plane && fs_n1(c.nr[0]) > 0;
+      const size_t nq = b.size() - 1, split = nq > 1 ? (nq + 1) / 2 : nq;
       int g0 = p0;  // first pair of the x-stage group not yet launched
-      for (int q = 0; q < nq; ++q) {
+      for (size_t q = 0; q < nq; ++q) {
         const int q0 = std::max(b[q], p0), q1 = std::min(b[q + 1], p0 + np);
         if (q1 > q0) {
           GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.batch_ready[q], 0));
@@ -965,20 +953,8 @@ int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f,
           if (!plane && (rc = yinv<T>(c, q1 - q0, q0 - p0))) return rc;
         }
         const int gend = std::min(b[q + 1], p0 + np);
-        const bool group_end = q + 1 == nq || q + 1 == nq - 1 || q + 1 == nq - 2;
-        if (group_end && gend > g0) {
-          if (slabs && gend == p0 + np) {
-            const int nzs = 4, n3 = c.geo.n3;
-            for (int r = 0; r < nzs; ++r) {
-              const int z0 = (int)((long long)n3 * r / nzs), z1 = (int)((long long)n3 * (r + 1) / nzs);
-              if (z1 <= z0) continue;
-              if ((rc = xinv_rho<T>(c, gend - g0, 2 * g0, nstate, f, rho, g0 - p0, z0, z1 - z0))) return rc;
-              if ((rc = c.rho_slab_done(z0, z1))) return rc;
-            }
-            c.rho_slabs = true;
-          } else if ((rc = density(g0, gend, p0))) {
-            return rc;
-          }
+        if ((q + 1 == split || q + 1 == nq) && gend > g0) {
+          if ((rc = density(g0, gend, p0))) return rc;
           g0 = gend;
         }
       }

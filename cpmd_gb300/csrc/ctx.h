@@ -188,10 +188,6 @@ struct Ctx {
   const cudaEvent_t* batch_c2_ready = nullptr;  // vpsi: the decode of chunk q waits for its C2 columns
   cudaEvent_t vpot_ready = nullptr;             // vpsi: the first x-stage waits for V(r)
   std::function<int(int)> batch_done;
-  // rhoofr host staging: the final density of z planes [z0, z1) is queued; rho_slabs
-  // records that the slabs went down this way (no download of the whole density)
-  std::function<int(int, int)> rho_slab_done;
-  bool rho_slabs = false;
   std::vector<int> stage_bounds;  // staging chunks as pair ranges [b[q], b[q+1]); each is one launch batch
   // profiling
   bool prof = false;
