@@ -313,9 +313,16 @@ __global__ void __launch_bounds__(kThreads) k_xrho_fs(GeoDev g, const cx<T>* __r
     const T* tp = part + (size_t)tile * nchunk * (P::TB * P::N2);
 #pragma unroll
     for (int k2 = 0; k2 < P::N2; ++k2) {
-      double sum = 0.0;
-      for (int q = 0; q < nchunk; ++q) sum += to_double<T>(__ldcg(tp + (size_t)q * (P::TB * P::N2) + k2 * P::TB + t));
-      rrow[k1 + P::N1 * k2] += sum;
+      if constexpr (sizeof(T) == 4) {
+        // chunk order in double-float (two FP64 additions per element instead of nchunk + 1)
+        float h = 0.f, l = 0.f;
+        for (int q = 0; q < nchunk; ++q) df_add(h, l, __ldcg(tp + (size_t)q * (P::TB * P::N2) + k2 * P::TB + t), 0.f);
+        rrow[k1 + P::N1 * k2] += f2d_int(h) + f2d_int(l);
+      } else {
+        double sum = 0.0;
+        for (int q = 0; q < nchunk; ++q) sum += to_double<T>(__ldcg(tp + (size_t)q * (P::TB * P::N2) + k2 * P::TB + t));
+        rrow[k1 + P::N1 * k2] += sum;
+      }
     }
   }
   if (threadIdx.x == 0) tickets[tile] = 0u;  // ready for the next launch
