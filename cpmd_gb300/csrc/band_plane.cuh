@@ -125,17 +125,26 @@ __global__ void __launch_bounds__(kThreads, 2) k_plane_vx_fs(GeoDev g, cx<float>
   __syncthreads();
   plane_yinv<N>(g, zrow, twy, Pl, X);
   for (int y0 = 0; y0 < N; y0 += P::L) {
+    // this thread's V(r) values of step B, loaded before step A so that their
+    // latency passes during it
+    float vr[P::N2];
+    {
+      const int t = threadIdx.x;
+      const int l = t / P::N1, k1 = t - l * P::N1, y = y0 + l;
+      const float* vrow = vpot + (size_t)g.k1 * ((y < N ? y : 0) + (size_t)g.k2 * z);
+#pragma unroll
+      for (int k2 = 0; k2 < P::N2; ++k2) vr[k2] = (t < P::TB && y < N) ? __ldg(vrow + k1 + P::N1 * k2) : 0.f;
+    }
     plane_xrow_a<N>(g, Pl, y0, twx, X);
     __syncthreads();
     // step B: inverse over k2, x V(r), forward over k2, twiddle, back into row k1
     if (threadIdx.x < P::TB) {
       const int t = threadIdx.x;
-      const int l = t / P::N1, k1 = t - l * P::N1, y = y0 + l;
+      const int l = t / P::N1, k1 = t - l * P::N1;
       cx<float> w[P::N2];
       fs_step_b<1, float, P::N1, P::N2, P::XP>(X + l * P::XS, k1, w);
-      const float* vrow = vpot + (size_t)g.k1 * ((y < N ? y : 0) + (size_t)g.k2 * z);
 #pragma unroll
-      for (int k2 = 0; k2 < P::N2; ++k2) w[k2] = scl(w[k2], (y < N) ? vrow[k1 + P::N1 * k2] : 0.f);
+      for (int k2 = 0; k2 < P::N2; ++k2) w[k2] = scl(w[k2], vr[k2]);
       dftn<-1, P::N2>(w);
       cx<float>* line = X + l * P::XS;
 #pragma unroll
