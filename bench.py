@@ -851,6 +851,43 @@ def run_case_projectors(args):
     ctx.close()
 
 
+def run_case_loewdin(args):
+    """Loewdin ortho of --case-states states (1024 by default for this case) on the
+    64-atom cell's sphere (ngw = 42.7k): the overlap GEMM (K = 85 472) and the
+    Newton-Schulz products S^-1/2 (n x n x n) on the tensor cores, FP64-accurate.
+    About 2 GB on the device."""
+    import torch
+    from cpmd_gb300 import Context
+    from cpmd_gb300.cell import make_basis
+
+    b = make_basis(20.52, 120, 70.0)
+    n = args.case_states if args.case_states != 512 else 1024
+    g = torch.Generator(device="cuda")
+    g.manual_seed(11)
+    c0 = torch.complex(torch.randn(n, b.ngw, generator=g, device="cuda", dtype=torch.float64),
+                       torch.randn(n, b.ngw, generator=g, device="cuda", dtype=torch.float64)) * 0.01
+    ctx = Context(b, "mixed")
+    work = torch.empty_like(c0)
+
+    def step():
+        work.copy_(c0)
+        ctx.ortho(work, "lowdin")
+    ms = _timed_loop(step, args.steps, args.warmup)
+    ctx.profile(True)
+    step()
+    torch.cuda.synchronize()
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    ns_ms, ns_n = prof.get("k_ozaki_ns", (0.0, 0))
+    # every Newton-Schulz product is an n x n x n product of 36 bf16 digit pairs (s + t <= 7)
+    ns_tflops = 36 * 2.0 * n ** 3 * ns_n / (ns_ms / 1e3) / 1e12 if ns_ms else None
+    print(json.dumps({"case": "loewdin", "ms_per_ortho": ms, "states": n, "ngw": b.ngw,
+                      "ns_products": ns_n, "ns_ms": ns_ms, "ns_bf16_issued_tflops": ns_tflops,
+                      "kernels_ms": {k: round(v[0], 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}}),
+          flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -862,13 +899,16 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the 8-, 216- and 512-atom cells")
-    ap.add_argument("--case", default=None, choices=["projectors"],
+    ap.add_argument("--case", default=None, choices=["projectors", "loewdin"],
                     help="run one small case of a single path instead of the benchmark (for profiling)")
     ap.add_argument("--case-states", type=int, default=512)
     ap.add_argument("--case-atoms", type=int, default=128)
     args = ap.parse_args()
     if args.case == "projectors":
         run_case_projectors(args)
+        return
+    if args.case == "loewdin":
+        run_case_loewdin(args)
         return
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":
