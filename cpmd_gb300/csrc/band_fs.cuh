@@ -132,7 +132,6 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
 // E_kin / norm partials taken on the way (hg in order, no gather); then
 // k_zinv_ent_fs runs the z-FFT of every column from that buffer (L2-resident),
 // through the per-line entry-position table.
-constexpr int kEncodePer = 8;
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_encode(GeoDev g, const cx<double>* __restrict__ c0, int psi32, int ldc,
                                                     int s0, int nstate, cx<T>* __restrict__ qbuf,
@@ -143,27 +142,15 @@ __global__ void __launch_bounds__(kThreads) k_encode(GeoDev g, const cx<double>*
   const size_t o1 = (size_t)is1 * ldc, o2 = (size_t)(two ? is2 : is1) * ldc;
   cx<T>* qb = qbuf + (size_t)pair * g.nent;
   KinAcc<T> kacc;
-  // kEncodePer coefficients per thread (coalesced per u), all loads first
-  T ux[kEncodePer], uy[kEncodePer], wx[kEncodePer], wy[kEncodePer];
-  const int base = blockIdx.x * (kThreads * kEncodePer) + threadIdx.x;
-#pragma unroll
-  for (int u = 0; u < kEncodePer; ++u) {
-    const int ig = base + u * kThreads;
-    ux[u] = uy[u] = wx[u] = wy[u] = 0;
-    if (ig < g.ngw) {
-      load_coef<T>(c0, psi32, o1 + ig, ux[u], uy[u]);
-      if (two) load_coef<T>(c0, psi32, o2 + ig, wx[u], wy[u]);
-    }
-  }
-#pragma unroll
-  for (int u = 0; u < kEncodePer; ++u) {
-    const int ig = base + u * kThreads;
-    if (ig < g.ngw) {
-      const int pp = g.pos_plus[ig], pm = g.pos_minus[ig];
-      qb[pp] = mk<T>(ux[u] - wy[u], uy[u] + wx[u]);
-      if (pm != pp) qb[pm] = mk<T>(ux[u] + wy[u], wx[u] - uy[u]);  // G = 0 is its own mirror: the +G value
-      if (kpart) kin_entry(kacc, g, ig, ux[u], uy[u], wx[u], wy[u]);
-    }
+  const int ig = blockIdx.x * kThreads + threadIdx.x;
+  if (ig < g.ngw) {
+    T ux, uy, wx = 0, wy = 0;
+    load_coef<T>(c0, psi32, o1 + ig, ux, uy);
+    if (two) load_coef<T>(c0, psi32, o2 + ig, wx, wy);
+    const int pp = g.pos_plus[ig], pm = g.pos_minus[ig];
+    qb[pp] = mk<T>(ux - wy, uy + wx);
+    if (pm != pp) qb[pm] = mk<T>(ux + wy, wx - uy);  // G = 0 is its own mirror: the +G value
+    if (kpart) kin_entry(kacc, g, ig, ux, uy, wx, wy);
   }
   if (kpart)
     kin_flush(kacc, f[is1], two ? f[is2] : 0.0, kpart + 2 * ((size_t)(s0 / 2 + pair) * gridDim.x + blockIdx.x));

@@ -583,7 +583,7 @@ template <typename T, int NC> int zinv_blocks_n(const Ctx& c) {
 template <typename T, int NC> constexpr bool zinv_encoded() { return NC > 0 && sizeof(T) == 4; }
 // CTAs per pair that write E_kin / norm partials: the encode's, else the gather's
 template <typename T, int NC> int kin_blocks_n(const Ctx& c) {
-  if constexpr (zinv_encoded<T, NC>()) return (c.geo.ngw + kThreads * kEncodePer - 1) / (kThreads * kEncodePer);
+  if constexpr (zinv_encoded<T, NC>()) return (c.geo.ngw + kThreads - 1) / kThreads;
   else return zinv_blocks_n<T, NC>(c);
 }
 
