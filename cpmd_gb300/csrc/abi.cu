@@ -239,15 +239,12 @@ static int build_geometry(Ctx& c, const int32_t* inyh, const double* hg) {
   // col_start -> col_ent -> c0, and hg without a gather of its own
   std::vector<int2> zgat;
   std::vector<int> zent;
-  int zrun = 0;
   {
     const int N = n[2], N1 = gbcp::fs_n1(N), L = gbcp::fs_lines(N);
     if (N1 > 0) {
       const int N2 = N / N1, nblk = (ncol + L - 1) / L, h = (N + 1) / 2;
       zgat.assign((size_t)nblk * N * L, int2{0, 0});
       zent.assign((size_t)nblk * N * L, -1);
-      for (int b = 0; b < nblk; ++b)
-        zrun = std::max(zrun, col_start[std::min(ncol, (b + 1) * L)] - col_start[b * L]);
       for (int b = 0; b < nblk; ++b)
         for (int n1 = 0; n1 < N1; ++n1)
           for (int n2 = 0; n2 < N2; ++n2)
@@ -279,7 +276,6 @@ static int build_geometry(Ctx& c, const int32_t* inyh, const double* hg) {
   g.nslot = nslot;
   g.gxlo = gxlo;
   g.nent = (int)col_ent.size();
-  g.zrun = zrun;
   if (!upload(c, col_start, g.col_start) || !upload(c, col_zlo, g.col_zlo) || !upload(c, col_ent, g.col_ent) ||
       !upload(c, col_slot, g.col_slot) || !upload(c, col_gy, g.col_gy) || !upload(c, ent_col, g.ent_col) ||
       !upload(c, slot_col0, g.slot_col0) || !upload(c, slot_gylo, g.slot_gylo) ||

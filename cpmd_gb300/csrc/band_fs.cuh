@@ -156,9 +156,6 @@ __global__ void __launch_bounds__(kThreads) k_encode(GeoDev g, const cx<double>*
     kin_flush(kacc, f[is1], two ? f[is2] : 0.0, kpart + 2 * ((size_t)(s0 / 2 + pair) * gridDim.x + blockIdx.x));
 }
 
-// The L columns of a block own one contiguous run of entries: it is copied to
-// shared memory with coalesced loads (L2 hits after the encode) and step A reads
-// it there.
 template <int N>
 __global__ void __launch_bounds__(kThreads) k_zinv_ent_fs(GeoDev g, const cx<float>* __restrict__ qbuf,
                                                          cx<float>* __restrict__ zbuf,
@@ -167,11 +164,8 @@ __global__ void __launch_bounds__(kThreads) k_zinv_ent_fs(GeoDev g, const cx<flo
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<float>* twA = reinterpret_cast<cx<float>*>(smem_raw);
   cx<float>* Ts = twA + N;
-  cx<float>* run = Ts + P::L * P::LS;  // g.zrun entries
   const int col0 = blockIdx.x * P::L, pair = blockIdx.y;
-  const int e0 = g.col_start[col0], e1 = g.col_start[min(g.ncol, col0 + P::L)];
-  const cx<float>* qb = qbuf + (size_t)pair * g.nent + e0;
-  for (int e = threadIdx.x; e < e1 - e0; e += kThreads) run[e] = qb[e];
+  const cx<float>* qb = qbuf + (size_t)pair * g.nent;
   load_table(twA, twAg, N);
   __syncthreads();
   const int* ze = g.zent + (size_t)blockIdx.x * (P::N1 * P::N2 * P::L);
@@ -185,7 +179,7 @@ __global__ void __launch_bounds__(kThreads) k_zinv_ent_fs(GeoDev g, const cx<flo
       for (int n1 = 0; n1 < P::N1; ++n1) pos[n1] = ze[(n1 * P::N2 + n2) * P::L + l];
       cx<float> v[P::N1];
 #pragma unroll
-      for (int n1 = 0; n1 < P::N1; ++n1) v[n1] = pos[n1] >= 0 ? run[pos[n1] - e0] : mk<float>(0.f, 0.f);
+      for (int n1 = 0; n1 < P::N1; ++n1) v[n1] = pos[n1] >= 0 ? qb[pos[n1]] : mk<float>(0.f, 0.f);
       fs_step_a<1, float, P::N1, P::N2>(v, n2, twA, Ts + l * P::LS);
     }
   }

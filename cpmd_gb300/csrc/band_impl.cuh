@@ -599,7 +599,7 @@ int launch_zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int n
     k_encode<T><<<dim3(kin_blocks_n<T, NC>(c), np), kThreads, 0, c.stream>>>(g, c0, c.psi32, ldc, s0, nstate, qb, f,
                                                                             kpart);
     GBCP_LAUNCH_CHECK(c);
-    const size_t sm = fs_smem<T, NC>(1, 1) + sizeof(cx<float>) * (size_t)g.zrun;
+    constexpr size_t sm = fs_smem<T, NC>(1, 1);
     allow_smem(k_zinv_ent_fs<NC>, sm);
     k_zinv_ent_fs<NC><<<dim3(zinv_blocks_n<T, NC>(c), np), kThreads, sm, c.stream>>>(
         g, reinterpret_cast<const cx<float>*>(qb), reinterpret_cast<cx<float>*>(zb),

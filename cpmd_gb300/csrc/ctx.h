@@ -70,7 +70,6 @@ struct GeoDev {
   // hole or no column), hg of that +G entry as FP32 bits}; index ((b N1 + n1) N2 + n2) L + l
   const int2* zgat;
   const int* zent;       // the same index: entry position st + off of that (column, z), -1 for none
-  int zrun;              // most sphere entries of one column block (its entries are one contiguous run)
   int geq0;              // entry 0 is G = 0
 };
 
