@@ -238,13 +238,11 @@ static int build_geometry(Ctx& c, const int32_t* inyh, const double* hg) {
   // the four-step Z-stage gather table: one coalesced load per (line, z) instead of
   // col_start -> col_ent -> c0, and hg without a gather of its own
   std::vector<int2> zgat;
-  std::vector<int> zent;
   {
     const int N = n[2], N1 = gbcp::fs_n1(N), L = gbcp::fs_lines(N);
     if (N1 > 0) {
       const int N2 = N / N1, nblk = (ncol + L - 1) / L, h = (N + 1) / 2;
       zgat.assign((size_t)nblk * N * L, int2{0, 0});
-      zent.assign((size_t)nblk * N * L, -1);
       for (int b = 0; b < nblk; ++b)
         for (int n1 = 0; n1 < N1; ++n1)
           for (int n2 = 0; n2 < N2; ++n2)
@@ -260,7 +258,6 @@ static int build_geometry(Ctx& c, const int32_t* inyh, const double* hg) {
               int bits;
               std::memcpy(&bits, &hge, sizeof(bits));
               zgat[(((size_t)b * N1 + n1) * N2 + n2) * L + l] = int2{e, bits};
-              if (e != 0) zent[(((size_t)b * N1 + n1) * N2 + n2) * L + l] = st + off;
             }
     }
   }
@@ -280,7 +277,7 @@ static int build_geometry(Ctx& c, const int32_t* inyh, const double* hg) {
       !upload(c, col_slot, g.col_slot) || !upload(c, col_gy, g.col_gy) || !upload(c, ent_col, g.ent_col) ||
       !upload(c, slot_col0, g.slot_col0) || !upload(c, slot_gylo, g.slot_gylo) ||
       !upload(c, slot_ncol, g.slot_ncol) || !upload(c, pos_plus, g.pos_plus) || !upload(c, pos_minus, g.pos_minus) ||
-      !upload(c, hgv, g.hg) || !upload(c, hg32v, g.hg32) || (!zgat.empty() && (!upload(c, zgat, g.zgat) || !upload(c, zent, g.zent)))) {
+      !upload(c, hgv, g.hg) || !upload(c, hg32v, g.hg32) || (!zgat.empty() && !upload(c, zgat, g.zgat))) {
     c.err = "geometry upload failed";
     return 6;
   }

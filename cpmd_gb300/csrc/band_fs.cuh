@@ -123,83 +123,6 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
               kpart + 2 * ((size_t)(s0 / 2 + pair) * gridDim.x + blockIdx.x));
 }
 
-// ---------------------------------------------------------------- Z stage, FP32: encode + entry gather
-// The G-sphere gather of c0 in CPMD's G order is a random 16-byte read per
-// coefficient (read twice, for +G and -G).  In FP32 it is split in two passes:
-// k_encode reads c0 in order (coalesced), forms the Gamma-packed values of +G and
-// -G (state 1 + i state 2, and its mirror) and scatters them as FP32 pairs into
-// the pair's sphere-entry buffer (column order; the writes merge in L2), with the
-// E_kin / norm partials taken on the way (hg in order, no gather); then
-// k_zinv_ent_fs runs the z-FFT of every column from that buffer (L2-resident),
-// through the per-line entry-position table.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_encode(GeoDev g, const cx<double>* __restrict__ c0, int psi32, int ldc,
-                                                    int s0, int nstate, cx<T>* __restrict__ qbuf,
-                                                    const double* __restrict__ f, double* __restrict__ kpart) {
-  const int pair = blockIdx.y;
-  const int is1 = s0 + 2 * pair, is2 = is1 + 1;
-  const bool two = is2 < nstate;
-  const size_t o1 = (size_t)is1 * ldc, o2 = (size_t)(two ? is2 : is1) * ldc;
-  cx<T>* qb = qbuf + (size_t)pair * g.nent;
-  KinAcc<T> kacc;
-  const int ig = blockIdx.x * kThreads + threadIdx.x;
-  if (ig < g.ngw) {
-    T ux, uy, wx = 0, wy = 0;
-    load_coef<T>(c0, psi32, o1 + ig, ux, uy);
-    if (two) load_coef<T>(c0, psi32, o2 + ig, wx, wy);
-    const int pp = g.pos_plus[ig], pm = g.pos_minus[ig];
-    qb[pp] = mk<T>(ux - wy, uy + wx);
-    if (pm != pp) qb[pm] = mk<T>(ux + wy, wx - uy);  // G = 0 is its own mirror: the +G value
-    if (kpart) kin_entry(kacc, g, ig, ux, uy, wx, wy);
-  }
-  if (kpart)
-    kin_flush(kacc, f[is1], two ? f[is2] : 0.0, kpart + 2 * ((size_t)(s0 / 2 + pair) * gridDim.x + blockIdx.x));
-}
-
-template <int N>
-__global__ void __launch_bounds__(kThreads) k_zinv_ent_fs(GeoDev g, const cx<float>* __restrict__ qbuf,
-                                                         cx<float>* __restrict__ zbuf,
-                                                         const cx<float>* __restrict__ twAg) {
-  using P = FS<float, N>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<float>* twA = reinterpret_cast<cx<float>*>(smem_raw);
-  cx<float>* Ts = twA + N;
-  const int col0 = blockIdx.x * P::L, pair = blockIdx.y;
-  const cx<float>* qb = qbuf + (size_t)pair * g.nent;
-  load_table(twA, twAg, N);
-  __syncthreads();
-  const int* ze = g.zent + (size_t)blockIdx.x * (P::N1 * P::N2 * P::L);
-#pragma unroll
-  for (int ia = 0; ia < P::IA; ++ia) {
-    const int t = threadIdx.x + ia * kThreads;
-    if (t < P::TA) {
-      const int n2 = t / P::L, l = t - n2 * P::L;
-      int pos[P::N1];
-#pragma unroll
-      for (int n1 = 0; n1 < P::N1; ++n1) pos[n1] = ze[(n1 * P::N2 + n2) * P::L + l];
-      cx<float> v[P::N1];
-#pragma unroll
-      for (int n1 = 0; n1 < P::N1; ++n1) v[n1] = pos[n1] >= 0 ? qb[pos[n1]] : mk<float>(0.f, 0.f);
-      fs_step_a<1, float, P::N1, P::N2>(v, n2, twA, Ts + l * P::LS);
-    }
-  }
-  __syncthreads();
-  cx<float>* zb = zbuf + (size_t)pair * N * g.ncol;
-#pragma unroll
-  for (int ib = 0; ib < P::IB; ++ib) {
-    const int t = threadIdx.x + ib * kThreads;
-    if (t < P::TB) {
-      const int k1 = t / P::L, l = t - k1 * P::L, col = col0 + l;
-      cx<float> w[P::N2];
-      fs_step_b<1, float, P::N1, P::N2>(Ts + l * P::LS, k1, w);
-      if (col < g.ncol) {
-#pragma unroll
-        for (int k2 = 0; k2 < P::N2; ++k2) zb[(size_t)(k1 + P::N1 * k2) * g.ncol + col] = w[k2];
-      }
-    }
-  }
-}
-
 // ---------------------------------------------------------------- Y stage (inverse)
 template <typename T, int N>
 __global__ void __launch_bounds__(kThreads) k_yinv_fs(GeoDev g, const cx<T>* __restrict__ zbuf,

@@ -579,13 +579,6 @@ template <typename T, int NC> int zinv_blocks_n(const Ctx& c) {
   if constexpr (NC > 0) return (c.geo.ncol + FS<T, NC>::L - 1) / FS<T, NC>::L;
   else return (c.geo.ncol + lines_rt(c.geo.n3) - 1) / lines_rt(c.geo.n3);
 }
-// the FP32 four-step Z stage runs as k_encode + k_zinv_ent_fs
-template <typename T, int NC> constexpr bool zinv_encoded() { return NC > 0 && sizeof(T) == 4; }
-// CTAs per pair that write E_kin / norm partials: the encode's, else the gather's
-template <typename T, int NC> int kin_blocks_n(const Ctx& c) {
-  if constexpr (zinv_encoded<T, NC>()) return (c.geo.ngw + kThreads - 1) / kThreads;
-  else return zinv_blocks_n<T, NC>(c);
-}
 
 // kpart (may be null): per-CTA partials of E_kin and the norm (rhoofr only)
 template <typename T, int NC>
@@ -594,17 +587,7 @@ int launch_zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int n
   const GeoDev& g = c.geo;
   cx<T>* zb = static_cast<cx<T>*>(c.zbuf.p) + (size_t)poff * g.n3 * g.ncol;  // pair poff of the launch batch
   ProfScope ps_(c, "k_zinv");
-  if constexpr (zinv_encoded<T, NC>()) {
-    cx<T>* qb = static_cast<cx<T>*>(c.qbuf.p) + (size_t)poff * g.nent;
-    k_encode<T><<<dim3(kin_blocks_n<T, NC>(c), np), kThreads, 0, c.stream>>>(g, c0, c.psi32, ldc, s0, nstate, qb, f,
-                                                                            kpart);
-    GBCP_LAUNCH_CHECK(c);
-    constexpr size_t sm = fs_smem<T, NC>(1, 1);
-    allow_smem(k_zinv_ent_fs<NC>, sm);
-    k_zinv_ent_fs<NC><<<dim3(zinv_blocks_n<T, NC>(c), np), kThreads, sm, c.stream>>>(
-        g, reinterpret_cast<const cx<float>*>(qb), reinterpret_cast<cx<float>*>(zb),
-        reinterpret_cast<const cx<float>*>(twA_of<T>(c, 2)));
-  } else if constexpr (NC > 0) {
+  if constexpr (NC > 0) {
     constexpr size_t sm = fs_smem<T, NC>(1, 1);
     allow_smem(k_zinv_fs<T, NC>, sm);
     k_zinv_fs<T, NC><<<dim3(zinv_blocks_n<T, NC>(c), np), kThreads, sm, c.stream>>>(g, c0, c.psi32, ldc, s0, nstate, zb,
@@ -892,7 +875,6 @@ int zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int np, int 
   GBCP_DISPATCH(launch_zinv, T, band_len(c, c.nr[2]), c, c0, ldc, s0, nstate, np, poff, f, kpart)
 }
 template <typename T> int zinv_blocks(const Ctx& c) { GBCP_DISPATCH(zinv_blocks_n, T, band_len(c, c.nr[2]), c) }
-template <typename T> int kin_blocks(const Ctx& c) { GBCP_DISPATCH(kin_blocks_n, T, band_len(c, c.nr[2]), c) }
 template <typename T> int yinv(Ctx& c, int np, int poff = 0) {
   GBCP_DISPATCH(launch_yinv, T, band_len(c, c.nr[1]), c, np, poff)
 }

@@ -69,7 +69,6 @@ struct GeoDev {
   // n1, n2 and line l, {col_ent of column b L + l at frequency n2 + N2 n1 (0 for a
   // hole or no column), hg of that +G entry as FP32 bits}; index ((b N1 + n1) N2 + n2) L + l
   const int2* zgat;
-  const int* zent;       // the same index: entry position st + off of that (column, z), -1 for none
   int geq0;              // entry 0 is G = 0
 };
 
