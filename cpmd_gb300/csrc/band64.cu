@@ -6,7 +6,7 @@ int band_rhoofr_fp64(Ctx& c, const cx<double>* c0, int ldc, int nstate, const do
                      double* kpart) {
   return band::rhoofr_t<double>(c, c0, ldc, nstate, f, rho, kpart);
 }
-int band_zinv_blocks_fp64(const Ctx& c) { return band::zinv_blocks<double>(c); }
+int band_zinv_blocks_fp64(const Ctx& c) { return band::kin_blocks<double>(c); }
 int band_vpsi_fp64(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, const double* f,
                    const double* vpot, int nstate) {
   return band::vpsi_t<double>(c, c0, ldc, c2, ldc2, f, vpot, nstate);

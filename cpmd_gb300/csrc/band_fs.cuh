@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
   }
   if (kpart)
     kin_flush(kacc, f[is1], two ? f[is2] : 0.0,
-              kpart + 2 * ((size_t)(s0 / 2 + pair) * gridDim.x + blockIdx.x));
+              kpart + 2 * kin_slots<T>() * ((size_t)(s0 / 2 + pair) * gridDim.x + blockIdx.x));
 }
 
 // ---------------------------------------------------------------- Y stage (inverse)

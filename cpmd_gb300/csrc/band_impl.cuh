@@ -203,29 +203,23 @@ __device__ __forceinline__ void df_mul_add(float& h, float& l, float ah, float a
   df_add(h, l, p, e);
 }
 __device__ __forceinline__ void kin_flush(KinAcc<float>& acc, double f1, double f2, double* __restrict__ out) {
-  __shared__ float2 wsum[kThreads / 32][4];
+  // one partial per warp (no CTA barrier, no serial CTA sum): out + 2 warp
   float h[4], l[4];
   acc.warp_totals(h, l);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0)
-#pragma unroll
-    for (int q = 0; q < 4; ++q) wsum[warp][q] = make_float2(h[q], l[q]);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    float th[4] = {0.f, 0.f, 0.f, 0.f}, tl[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) df_add(th[q], tl[q], wsum[w][q].x, wsum[w][q].y);
+  if (lane == 0) {
     const float f1h = d2f_int(f1), f1l = d2f_int(f1 - f2d_int(f1h));
     const float f2h = d2f_int(f2), f2l = d2f_int(f2 - f2d_int(f2h));
     float kh = 0.f, kl = 0.f, nh = 0.f, nl = 0.f;
-    df_mul_add(kh, kl, f1h, f1l, th[0], tl[0]);
-    df_mul_add(kh, kl, f2h, f2l, th[2], tl[2]);
-    df_mul_add(nh, nl, f1h, f1l, th[1], tl[1]);
-    df_mul_add(nh, nl, f2h, f2l, th[3], tl[3]);
-    *reinterpret_cast<float4*>(out) = make_float4(kh, kl, nh, nl);
+    df_mul_add(kh, kl, f1h, f1l, h[0], l[0]);
+    df_mul_add(kh, kl, f2h, f2l, h[2], l[2]);
+    df_mul_add(nh, nl, f1h, f1l, h[1], l[1]);
+    df_mul_add(nh, nl, f2h, f2l, h[3], l[3]);
+    reinterpret_cast<float4*>(out)[warp] = make_float4(kh, kl, nh, nl);
   }
 }
+// E_kin / norm partial slots per CTA of a Z-stage kernel: one (FP64), one per warp (FP32)
+template <typename T> __host__ __device__ constexpr int kin_slots() { return sizeof(T) == 4 ? kThreads / 32 : 1; }
 
 // ---------------------------------------------------------------- Z stage (inverse, gather)
 template <typename T, int NC>
@@ -271,7 +265,7 @@ __global__ void __launch_bounds__(kThreads) k_zinv(GeoDev g, FftPlan p, const cx
   }
   if (kpart)
     kin_flush(kacc, f[is1], two ? f[is2] : 0.0,
-              kpart + 2 * ((size_t)(s0 / 2 + pair) * gridDim.x + blockIdx.x));
+              kpart + 2 * kin_slots<T>() * ((size_t)(s0 / 2 + pair) * gridDim.x + blockIdx.x));
 }
 
 // ---------------------------------------------------------------- Y stage (inverse)
@@ -875,6 +869,8 @@ int zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int np, int 
   GBCP_DISPATCH(launch_zinv, T, band_len(c, c.nr[2]), c, c0, ldc, s0, nstate, np, poff, f, kpart)
 }
 template <typename T> int zinv_blocks(const Ctx& c) { GBCP_DISPATCH(zinv_blocks_n, T, band_len(c, c.nr[2]), c) }
+// E_kin / norm partial slots per pair
+template <typename T> int kin_blocks(const Ctx& c) { return zinv_blocks<T>(c) * kin_slots<T>(); }
 template <typename T> int yinv(Ctx& c, int np, int poff = 0) {
   GBCP_DISPATCH(launch_yinv, T, band_len(c, c.nr[1]), c, np, poff)
 }
