@@ -236,7 +236,7 @@ static int build_geometry(Ctx& c, const int32_t* inyh, const double* hg) {
   std::vector<double> hgv(hg, hg + ngw);
   std::vector<float> hg32v(hg, hg + ngw);
   // the four-step Z-stage gather table: one coalesced load per (line, z) instead of
-  // col_start -> col_ent -> c0, and hg without a gather of its own
+  // col_start -> col_ent -> c0, and hg(|G|) of the entry without a gather of its own
   std::vector<int2> zgat;
   {
     const int N = n[2], N1 = gbcp::fs_n1(N), L = gbcp::fs_lines(N);
@@ -253,8 +253,7 @@ static int build_geometry(Ctx& c, const int32_t* inyh, const double* hg) {
               const int st = col_start[col], len = col_start[col + 1] - st, off = fz - col_zlo[col];
               if (off < 0 || off >= len) continue;
               const int e = col_ent[st + off];
-              float hge = 0.0f;
-              if (e > 0) hge = hg32v[e - 1];
+              const float hge = e != 0 ? hg32v[(e > 0 ? e : -e) - 1] : 0.0f;
               int bits;
               std::memcpy(&bits, &hge, sizeof(bits));
               zgat[(((size_t)b * N1 + n1) * N2 + n2) * L + l] = int2{e, bits};
@@ -462,6 +461,12 @@ int gbcp_set_option(gbcp_ctx* h, int key, int value) {
     c.fft_engine = value;
     return GBCP_OK;
   }
+  if (key == GBCP_OPT_STAGES && value >= 0) {
+    c.stage_first = value & 0xFF;
+    c.stage_n = (value >> 8) & 0xFF;
+    c.stage_groups = (value >> 16) & 0xFF;
+    return GBCP_OK;
+  }
   if (key == GBCP_OPT_XCHUNKS && value >= 0 && value <= 8) {
     c.xr_chunks = value;
     return GBCP_OK;
@@ -662,14 +667,34 @@ int pipe_up(Ctx& c, cx<double>* d, const double* h, int ld, int s0, int ns) {
 // stage chain of one chunk overlaps the copies of the next; host-memory calls launch the
 // band loop chunk by chunk (their launch batch is the chunk)
 // Staging chunks of a host-memory band-loop call, as pair ranges, each at most one
-// launch batch: a small first chunk (its upload is the only one the transforms
-// wait for), two large middle ones, and a small last one (its transforms and, in
-// vpsi, its C2 download are the tail nothing overlaps).  Returns the number of chunks.
-int stage_plan(Ctx& c, int nstate) {
+// launch batch.  vpsi: a small first chunk (its upload is the only one the
+// transforms wait for), two large middle ones, and a small last one (its
+// transforms and its C2 download are the tail nothing overlaps).  rhoofr: a small
+// first chunk and three equal ones.  GBCP_OPT_STAGES fixes the plan for both.
+// Returns the number of chunks.
+int stage_plan(Ctx& c, int nstate, bool rho = false) {
   const int npairs = (nstate + 1) / 2;
   std::vector<int>& b = c.stage_bounds;
   b.assign(1, 0);
   if (npairs <= 0) return 0;
+  // rhoofr, whose transforms wait for c0 to land: a small first chunk, then three
+  // equal ones (measured on the 128-state cell: 0.81 ms against 0.87 for the plan below)
+  const int nfix = c.stage_n > 0 ? c.stage_n : (rho ? 4 : 0);
+  if (nfix > 0) {
+    // a fixed plan: the first chunk, then equal chunks of at most one launch batch
+    const int f0 = c.stage_n > 0 ? c.stage_first : npairs / 16;
+    const int first = std::max(1, std::min({f0 > 0 ? f0 : npairs, npairs, c.batch}));
+    b.push_back(first);
+    const int rest = npairs - first;
+    if (rest > 0) {
+      const int k = std::max(std::max(1, nfix - 1), (rest + c.batch - 1) / c.batch);
+      for (int q = 1; q <= k; ++q) {
+        const int e = first + (int)((long long)rest * q / k);
+        if (e > b.back()) b.push_back(e);
+      }
+    }
+    return (int)b.size() - 1;
+  }
   const int first = std::max(1, std::min(c.batch, npairs / 16));
   const int last = (npairs - first >= 3) ? std::max(1, std::min(c.batch, npairs / 6)) : 0;
   int p = first;
@@ -735,7 +760,7 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
         !gbcp::ensure(c, c.st_c0, sizeof(cx<double>) * (size_t)c.ngw * std::max(nstate, 1)))
       return GBCP_ERR_NOMEM;
     cx<double>* t = static_cast<cx<double>*>(c.st_c0.p);
-    const int nb = stage_plan(c, nstate);
+    const int nb = stage_plan(c, nstate, true);
     if ((rc = pipe_prepare(c, nb))) return rc;
     const bool resident = wfn_hit(c, c0, ldc, nstate);
     for (int b = 0; b < nb; ++b) {
@@ -743,7 +768,6 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
       if (!resident && (rc = pipe_up(c, t, c0, ldc, s0, ns))) return rc;
       GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[1 + b], c.copy));
     }
-    wfn_put(c, c0, ldc, nstate);
     c.batch_ready = c.pipe_ev.data() + 1;  // launch batches stay c.batch pairs (see rhoofr_t)
     dc0 = t;
     df = static_cast<double*>(tf);
@@ -760,6 +784,8 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
   }
   rc = gbcp::band_rhoofr(c, dc0, dld, nstate, df, drho, dsc);
   c.batch_ready = nullptr;
+  // the cache key (a host pass over c0's first column) once the GPU has its work
+  if (mem == GBCP_MEM_HOST) wfn_put(c, c0, ldc, nstate);
   if (saved_batch) c.batch = saved_batch;
   if (!rc && mem == GBCP_MEM_HOST) {
     gbcp::ProfScope ps_(c, "d2h_rho", c.stream, 2);

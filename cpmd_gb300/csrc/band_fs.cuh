@@ -59,6 +59,14 @@ __device__ __forceinline__ void load_table(cx<T>* dst, const cx<T>* __restrict__
 }
 
 // ---------------------------------------------------------------- Z stage (inverse, gather)
+// The full sphere's columns, sorted by (gx, gy), form a centrally symmetric set,
+// so the mirror (-gx, -gy) of column c is column ncol - 1 - c and its entry at -z
+// is the -G of the entry at z (code -e).  A CTA takes L primary columns
+// c < ceil(ncol / 2) and their mirrors: each coefficient and each gather-table
+// entry is loaded once and feeds both lines (c1 + i c2 at +G, its conjugate
+// packing at -G).  In the four-step layout the mirror of thread (n2, n1) is
+// (N2 - n2, N1 - 1 - n1), or (0, (N1 - n1) mod N1) for n2 = 0, so the same
+// thread runs step A of both lines.  The column (0, 0), its own mirror, keeps one line.
 template <typename T, int N>
 __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>* __restrict__ c0, int psi32, int ldc,
                                                      int s0, int nstate, cx<T>* __restrict__ zbuf,
@@ -67,8 +75,9 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
   using P = FS<T, N>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* twA = reinterpret_cast<cx<T>*>(smem_raw);
-  cx<T>* Ts = twA + N;
+  cx<T>* Ts = twA + N;  // lines l (primary) and L + l (mirror)
   const int col0 = blockIdx.x * P::L, pair = blockIdx.y;
+  const int half = (g.ncol + 1) / 2;
   const int is1 = s0 + 2 * pair, is2 = is1 + 1;
   const bool two = is2 < nstate;
   const size_t o1 = (size_t)is1 * ldc, o2 = (size_t)(two ? is2 : is1) * ldc;
@@ -81,40 +90,56 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
   for (int ia = 0; ia < P::IA; ++ia) {
     const int t = threadIdx.x + ia * kThreads;
     if (t < P::TA) {
-      const int n2 = t / P::L, l = t - n2 * P::L;
-      cx<T> v[P::N1];
+      const int n2 = t / P::L, l = t - n2 * P::L, col = col0 + l;
+      const bool prim = col < half, mir = prim && g.ncol - 1 - col != col;
+      cx<T> v[P::N1], u[P::N1];
       int2 ce[P::N1];
 #pragma unroll
-      for (int n1 = 0; n1 < P::N1; ++n1) ce[n1] = zg[(n1 * P::N2 + n2) * P::L + l];
+      for (int n1 = 0; n1 < P::N1; ++n1) ce[n1] = prim ? zg[(n1 * P::N2 + n2) * P::L + l] : int2{0, 0};
 #pragma unroll
       for (int n1 = 0; n1 < P::N1; ++n1) {
         const int e = ce[n1].x;
-        cx<T> val = mk<T>(0, 0);
+        cx<T> val = mk<T>(0, 0), mval = mk<T>(0, 0);
         if (e != 0) {
           const int ig = (e > 0 ? e : -e) - 1;
           T ux, uy, wx = 0, wy = 0;
           load_coef<T>(c0, psi32, o1 + ig, ux, uy);
           if (two) load_coef<T>(c0, psi32, o2 + ig, wx, wy);
-          val = (e > 0) ? mk<T>(ux - wy, uy + wx) : mk<T>(ux + wy, wx - uy);
-          if (kpart && e > 0) kin_entry_t(kacc, g, ig, __int_as_float(ce[n1].y), ux, uy, wx, wy);
+          const cx<T> pp = mk<T>(ux - wy, uy + wx), pm = mk<T>(ux + wy, wx - uy);  // at +G, at -G
+          val = e > 0 ? pp : pm;
+          mval = e > 0 ? pm : pp;
+          // each coefficient once: at +G in the self-mirror column, at either sign elsewhere
+          if (kpart && (e > 0 || mir)) kin_entry_t(kacc, g, ig, __int_as_float(ce[n1].y), ux, uy, wx, wy);
         }
         v[n1] = val;
+        u[n1] = mval;
       }
       fs_step_a<1, T, P::N1, P::N2>(v, n2, twA, Ts + l * P::LS);
+      cx<T> vm[P::N1];
+      if (n2 == 0) {  // uniform per warp when L is a multiple of 32
+#pragma unroll
+        for (int n1 = 0; n1 < P::N1; ++n1) vm[(P::N1 - n1) % P::N1] = u[n1];
+      } else {
+#pragma unroll
+        for (int n1 = 0; n1 < P::N1; ++n1) vm[P::N1 - 1 - n1] = u[n1];
+      }
+      fs_step_a<1, T, P::N1, P::N2>(vm, n2 == 0 ? 0 : P::N2 - n2, twA, Ts + (P::L + l) * P::LS);
     }
   }
   __syncthreads();
   cx<T>* zb = zbuf + (size_t)pair * N * g.ncol;
 #pragma unroll
-  for (int ib = 0; ib < P::IB; ++ib) {
-    const int t = threadIdx.x + ib * kThreads;
+  for (int ib = 0; ib < 2 * P::IB; ++ib) {
+    const int t = threadIdx.x + (ib % P::IB) * kThreads, side = ib / P::IB;
     if (t < P::TB) {
       const int k1 = t / P::L, l = t - k1 * P::L, col = col0 + l;
+      const bool ok = side == 0 ? col < half : (col < half && g.ncol - 1 - col != col);
       cx<T> w[P::N2];
-      fs_step_b<1, T, P::N1, P::N2>(Ts + l * P::LS, k1, w);
-      if (col < g.ncol) {
+      fs_step_b<1, T, P::N1, P::N2>(Ts + (side * P::L + l) * P::LS, k1, w);
+      if (ok) {
+        const int oc = side == 0 ? col : g.ncol - 1 - col;
 #pragma unroll
-        for (int k2 = 0; k2 < P::N2; ++k2) zb[(size_t)(k1 + P::N1 * k2) * g.ncol + col] = w[k2];
+        for (int k2 = 0; k2 < P::N2; ++k2) zb[(size_t)(k1 + P::N1 * k2) * g.ncol + oc] = w[k2];
       }
     }
   }

@@ -570,7 +570,8 @@ template <typename T, int N> constexpr size_t fs_smem_x(int tables) {
 // Column blocks of the Z stage (the grid's x extent), for the size of the
 // per-CTA partials of rhoofr's scalars.
 template <typename T, int NC> int zinv_blocks_n(const Ctx& c) {
-  if constexpr (NC > 0) return (c.geo.ncol + FS<T, NC>::L - 1) / FS<T, NC>::L;
+  // four-step: blocks of primary columns, each with its mirrors (k_zinv_fs)
+  if constexpr (NC > 0) return ((c.geo.ncol + 1) / 2 + FS<T, NC>::L - 1) / FS<T, NC>::L;
   else return (c.geo.ncol + lines_rt(c.geo.n3) - 1) / lines_rt(c.geo.n3);
 }
 
@@ -582,7 +583,7 @@ int launch_zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int n
   cx<T>* zb = static_cast<cx<T>*>(c.zbuf.p) + (size_t)poff * g.n3 * g.ncol;  // pair poff of the launch batch
   ProfScope ps_(c, "k_zinv");
   if constexpr (NC > 0) {
-    constexpr size_t sm = fs_smem<T, NC>(1, 1);
+    constexpr size_t sm = fs_smem<T, NC>(2, 1);
     allow_smem(k_zinv_fs<T, NC>, sm);
     k_zinv_fs<T, NC><<<dim3(zinv_blocks_n<T, NC>(c), np), kThreads, sm, c.stream>>>(g, c0, c.psi32, ldc, s0, nstate, zb,
                                                                                     twA_of<T>(c, 2), f, kpart);
@@ -939,7 +940,8 @@ int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f,
       // density x-stage (which gains most from many pairs per launch) in two groups
       // of chunks, the first overlapping the later uploads, the second the tail
       const std::vector<int>& b = c.stage_bounds;
-      const size_t nq = b.size() - 1, split = nq > 1 ? (nq + 1) / 2 : nq;
+      const size_t nq = b.size() - 1;
+      const size_t ng = std::max<size_t>(1, std::min<size_t>(nq, c.stage_groups > 0 ? c.stage_groups : 2));
       int g0 = p0;  // first pair of the x-stage group not yet launched
       for (size_t q = 0; q < nq; ++q) {
         const int q0 = std::max(b[q], p0), q1 = std::min(b[q + 1], p0 + np);
@@ -949,7 +951,9 @@ int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f,
           if (!plane && (rc = yinv<T>(c, q1 - q0, q0 - p0))) return rc;
         }
         const int gend = std::min(b[q + 1], p0 + np);
-        if ((q + 1 == split || q + 1 == nq) && gend > g0) {
+        // group ends after chunks ceil(nq g / ng), g = 1 .. ng
+        const bool group_end = ((q + 1) * ng) / nq != (q * ng) / nq || q + 1 == nq;
+        if (group_end && gend > g0) {
           if ((rc = density(g0, gend, p0))) return rc;
           g0 = gend;
         }

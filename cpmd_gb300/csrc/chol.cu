@@ -620,55 +620,78 @@ __global__ void __launch_bounds__(32 * PR) k_chol_df(const double* __restrict__ 
   }
 }
 
-// The diagonal block k of the blocked chain in double-float (the elimination of
-// k_chol_df on a 32 x 32 block, scalar pairs): X_kk = U_kk^-1 of the block's
-// current Schur complement, without the FP64 pivot chain of k_chol_diag.
-// Scaled by the block's own diagonal; a pivot at or below 2^-40 of the row's
-// original diagonal (diag0) stops with status (global index + 1), a NaN one with
-// -1.  Writes the diagonal block of X (zero below its diagonal) and leaves Uw's
-// diagonal block alone (the panel, update and inverse kernels read only X_kk
-// and Uw's off-diagonal blocks).
-__device__ __forceinline__ Dfl df_sub_mul(Dfl m, Dfl w, Dfl v) {
-  const float np = __fmul_rn(-w.h, v.h);
-  float pe = __fmaf_rn(w.h, v.h, np);
-  pe = __fmaf_rn(w.h, v.l, pe);
-  pe = __fmaf_rn(w.l, v.h, pe);
-  const Dfl s = df_two_sum(m.h, np);
-  return df_two_sum(s.h, __fadd_rn(s.l, __fsub_rn(m.l, pe)));
+// ---- lean double-float elimination: one CTA, up to MMAX = 32 or 64 rows ----
+//
+// The elimination of k_chol_df with less work per step.  The vector of step j
+// (row j of Z, the pivot d, column j of A) is scaled once per lane, u_q = v_q / d,
+// with u_j = 1 + 1/d at the pivot entry; every slot (i, q) of an active row
+// i > j then subtracts b_i u_q, b_i = A_ij taken from the same vector:
+//     A_iq - A_ij A_qj / d   (q > j),   A_ij - A_ij (1 + 1/d) = -A_ij / d = Z_ij,
+//     Z_iq - (A_ij / d) Z_jq (q < j).
+// Finished rows (i <= j) are skipped by warp-uniform branches, 32-column blocks
+// wholly above a warp's rows at compile time, and each update is one 15-operation
+// double-float multiply-subtract, renormalised in place.  Serves the whole matrix
+// up to MMAX states (diag0 == nullptr: thresholds from its own scaled diagonal) and
+// the 32 x 32 diagonal blocks of the blocked chain (base = 32 k, the block's
+// current Schur complement in S, thresholds from the original diagonal diag0);
+// writes the (diagonal block of) X = U^-1, zero below its diagonal.
+
+// m - b u: TwoProduct of the hi parts by FMA, TwoSum into hi, the low-order terms
+// into lo, then Fast2Sum
+__device__ __forceinline__ Dfl df_fms(Dfl m, Dfl b, Dfl u) {
+  const float p = __fmul_rn(b.h, u.h);
+  float pe = __fmaf_rn(b.h, u.h, -p);
+  pe = __fmaf_rn(b.h, u.l, pe);
+  pe = __fmaf_rn(b.l, u.h, pe);
+  const float s = __fsub_rn(m.h, p);
+  const float bb = __fsub_rn(s, m.h);
+  const float e = __fsub_rn(__fsub_rn(m.h, __fsub_rn(s, bb)), __fadd_rn(p, bb));
+  const float l = __fadd_rn(e, __fsub_rn(m.l, pe));
+  const float h = __fadd_rn(s, l);
+  return {h, __fsub_rn(l, __fsub_rn(h, s))};
 }
 
-__global__ void __launch_bounds__(8 * B) k_chol_diag_df(const double* __restrict__ S, double* __restrict__ X,
-                                                        const double* __restrict__ diag0, int n, int k,
-                                                        int* __restrict__ status) {
+template <int MMAX, int NW>
+__global__ void __launch_bounds__(32 * NW) k_chol_lean(const double* __restrict__ S, double* __restrict__ X,
+                                                      const double* __restrict__ diag0, int n, int base,
+                                                      int* __restrict__ status) {
+  constexpr int RA = MMAX / NW, NP = MMAX / 32;
+  static_assert(MMAX % 32 == 0 && MMAX % NW == 0 && NW <= 32, "layout");
   pdl_entry();
-  __shared__ float2 buf[2][B];
-  __shared__ float2 piv[B];
-  __shared__ float thr[B];
-  __shared__ int kx[B];
+  __shared__ float2 buf[2][MMAX];  // the vector of the step (double-buffered)
+  __shared__ float2 piv[MMAX];     // the pivots d_j
+  __shared__ float thr[MMAX];      // 2^-40 of the scaled original diagonal
+  __shared__ int kx[MMAX];         // k_i: A = D S D, D = diag(2^k_i)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int base = k * B, m = min(B, n - base);
+  const int m = min(MMAX, n - base);
   if (failed(status)) return;
-  if (threadIdx.x < B) {
-    const int t = threadIdx.x;
-    int kk = 0;
+  for (int t = threadIdx.x; t < MMAX; t += 32 * NW) {
+    int k = 0;
     float th = 0.0f;
     if (t < m) {
       const int E = (int)((__double_as_longlong(S[(size_t)(base + t) * n + base + t]) >> 52) & 0x7FF);
-      if (E != 0 && E != 0x7FF) kk = -((E - 1023) >> 1);
-      th = 0x1p-40f * df_of_double(diag0[base + t], 2 * kk).h;
+      if (E != 0 && E != 0x7FF) k = -((E - 1023) >> 1);
+      if (diag0) th = 0x1p-40f * df_of_double(diag0[base + t], 2 * k).h;
     }
-    kx[t] = kk;
+    kx[t] = k;
     thr[t] = th;
     buf[0][t] = buf[1][t] = make_float2(0.0f, 0.0f);
   }
   __syncthreads();
-  Dfl M[B / 8];  // slots (i, lane), i = w + 8 a
+  Dfl M[RA][NP];  // slot (i, q): i = w + NW a, q = lane + 32 p
 #pragma unroll
-  for (int a = 0; a < B / 8; ++a) {
-    const int i = w + 8 * a;
-    M[a] = {0.0f, 0.0f};
-    if (i < m && lane <= i) M[a] = df_of_double(S[(size_t)(base + lane) * n + base + i], kx[i] + kx[lane]);
-    if (i < m && lane == 0) buf[0][i] = make_float2(M[a].h, M[a].l);
+  for (int a = 0; a < RA; ++a) {
+    const int i = w + NW * a;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const int q = lane + 32 * p;
+      M[a][p] = {0.0f, 0.0f};
+      if (i < m && q <= i) {
+        M[a][p] = df_of_double(S[(size_t)(base + q) * n + base + i], kx[i] + kx[q]);
+        if (q == 0) buf[0][i] = make_float2(M[a][p].h, M[a][p].l);  // column 0, the first pivot included
+        if (q == i && !diag0) thr[i] = 0x1p-40f * M[a][p].h;
+      }
+    }
   }
   for (int j = 0; j < m; ++j) {
     __syncthreads();
@@ -681,40 +704,71 @@ __global__ void __launch_bounds__(8 * B) k_chol_diag_df(const double* __restrict
     }
     if (threadIdx.x == 0) piv[j] = dv;
     const Dfl rd = df_rcp({dv.x, dv.y});
-    // entry j of the vector is d + 1: the generic update then turns A_ij = w_i d
-    // into -w_i = Z_ij; rows i <= j get w = 0, an exact no-op, so all rows of the
-    // warp update in one branch-free block
-    const float2 vq2 = b[lane];
-    const Dfl vq = (lane == j) ? df_add1({dv.x, dv.y}) : Dfl{vq2.x, vq2.y};
-    Dfl wv[B / 8];
+    Dfl u[NP];
 #pragma unroll
-    for (int a = 0; a < B / 8; ++a) {
-      const int i = w + 8 * a;
-      const float2 bi = b[i];
-      const Dfl t = df_mul({bi.x, bi.y}, rd);
-      wv[a] = (i > j && i < m) ? t : Dfl{0.0f, 0.0f};
+    for (int p = 0; p < NP; ++p) {
+      const int q = lane + 32 * p;
+      const float2 x = b[q];
+      u[p] = (q == j) ? df_add1(rd) : df_mul({x.x, x.y}, rd);
     }
 #pragma unroll
-    for (int a = 0; a < B / 8; ++a) M[a] = df_sub_mul(M[a], wv[a], vq);
+    for (int a = 0; a < RA; ++a) {
+      const int i = w + NW * a;
+      if (i > j && i < m) {  // warp-uniform
+        const float2 bi = b[i];
 #pragma unroll
-    for (int a = 0; a < B / 8; ++a) {
-      const int i = w + 8 * a;
-      if (i == j + 1 && lane <= i) bn[lane] = make_float2(M[a].h, M[a].l);
-      if (i > j + 1 && i < m && lane == j + 1) bn[i] = make_float2(M[a].h, M[a].l);
+        for (int p = 0; p < NP; ++p)
+          if (32 * p <= NW * a + NW - 1) M[a][p] = df_fms(M[a][p], {bi.x, bi.y}, u[p]);
+      }
+    }
+    // the vector of step j + 1: row j + 1 (Z part and pivot) from its warp, column
+    // j + 1 below the diagonal from lane (j + 1) mod 32 of every warp
+    const int j1 = j + 1;
+    if (j1 < m) {
+      if (w == j1 % NW) {
+        const int a1 = j1 / NW;
+#pragma unroll
+        for (int a = 0; a < RA; ++a)
+          if (a == a1) {
+#pragma unroll
+            for (int p = 0; p < NP; ++p)
+              if (lane + 32 * p <= j1) bn[lane + 32 * p] = make_float2(M[a][p].h, M[a][p].l);
+          }
+      }
+      if (lane == (j1 & 31)) {
+        const int p1 = j1 >> 5;
+#pragma unroll
+        for (int a = 0; a < RA; ++a) {
+          const int i = w + NW * a;
+          if (i > j1 && i < m) {
+            Dfl v = M[a][0];
+#pragma unroll
+            for (int p = 1; p < NP; ++p)
+              if (p == p1) v = M[a][p];
+            bn[i] = make_float2(v.h, v.l);
+          }
+        }
+      }
     }
   }
   __syncthreads();
+  // X_qi = 2^k_q d_i^-1/2 Z_iq (q < i), X_ii = 2^k_i d_i^-1/2, zero below the diagonal
+  double* xb = X + (size_t)base * n + base;
 #pragma unroll
-  for (int a = 0; a < B / 8; ++a) {
-    const int i = w + 8 * a;
-    if (i < m && lane < m) {
-      double* xb = X + (size_t)base * n + base;
-      if (lane < i) {
-        const Dfl ri = df_rsqrt({piv[i].x, piv[i].y});
-        xb[(size_t)lane * n + i] = df_to_double(df_mul(M[a], ri), kx[lane]);
-        xb[(size_t)i * n + lane] = 0.0;
-      } else if (lane == i) {
-        xb[(size_t)i * n + i] = df_to_double(df_rsqrt({piv[i].x, piv[i].y}), kx[i]);
+  for (int a = 0; a < RA; ++a) {
+    const int i = w + NW * a;
+    if (i < m) {
+      const float2 pv = piv[i];
+      const Dfl ri = df_rsqrt({pv.x, pv.y});
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        const int q = lane + 32 * p;
+        if (q == i) {
+          xb[(size_t)i * n + i] = df_to_double(ri, kx[i]);
+        } else if (q < i) {
+          xb[(size_t)q * n + i] = df_to_double(df_mul(M[a][p], ri), kx[q]);
+          xb[(size_t)i * n + q] = 0.0;
+        }
       }
     }
   }
@@ -725,17 +779,23 @@ __global__ void __launch_bounds__(8 * B) k_chol_diag_df(const double* __restrict
 // Queue U = chol(S) and X = U^{-1}; no synchronisation.  S is overwritten (the
 // blocked FP64 chain) or left as it was (the one-CTA double-float kernel).
 int chol_inverse(Ctx& c, double* S, double* X, int n) {
-  // double-float: the whole job in one CTA up to 64 states, the diagonal blocks of
-  // the blocked chain above (one CTA for all 128 states is slower than the chain)
-  const bool df = c.chol_df == 2 || (c.chol_df == 1 && c.precision == 1);
-  if (df && n <= 64) {
-    ProfScope ps_(c, "k_chol_df");
-    GBCP_LAUNCH_PDL(c, (k_chol_df<64, 8>), dim3(1), dim3(256), 0, (const double*)S, X, n, c.d_info);
-    return 0;
-  }
+  // double-float: the whole job in one CTA up to 64 states (k_chol_lean), the
+  // diagonal blocks of the blocked chain above (one CTA for all 128 states, option
+  // 3, is slower than the chain)
+  const bool df = c.chol_df >= 2 || (c.chol_df == 1 && c.precision == 1);
   if (c.chol_df == 3 && n <= 128) {
     ProfScope ps_(c, "k_chol_df");
     GBCP_LAUNCH_PDL(c, (k_chol_df<128, 16>), dim3(1), dim3(512), 0, (const double*)S, X, n, c.d_info);
+    return 0;
+  }
+  if (df && n <= 64) {
+    ProfScope ps_(c, "k_chol_df");
+    if (n <= 32)
+      GBCP_LAUNCH_PDL(c, (k_chol_lean<32, 8>), dim3(1), dim3(256), 0, (const double*)S, X, (const double*)nullptr, n,
+                      0, c.d_info);
+    else
+      GBCP_LAUNCH_PDL(c, (k_chol_lean<64, 8>), dim3(1), dim3(256), 0, (const double*)S, X, (const double*)nullptr, n,
+                      0, c.d_info);
     return 0;
   }
   const int nb = (n + B - 1) / B;
@@ -752,8 +812,8 @@ int chol_inverse(Ctx& c, double* S, double* X, int n) {
   for (int k = 0; k < nb; ++k) {
     if (df) {
       ProfScope ps_(c, "k_chol_diag");
-      GBCP_LAUNCH_PDL(c, k_chol_diag_df, dim3(1), dim3(8 * B), 0, (const double*)S, X, (const double*)diag0, n, k,
-                      c.d_info);
+      GBCP_LAUNCH_PDL(c, (k_chol_lean<B, 8>), dim3(1), dim3(8 * B), 0, (const double*)S, X, (const double*)diag0, n,
+                      k * B, c.d_info);
     } else {
       ProfScope ps_(c, "k_chol_diag");
       GBCP_LAUNCH_PDL(c, k_chol_diag, dim3(1), dim3(8 * B), 0, (const double*)S, Uw, X, (const double*)diag0, n, k,

@@ -126,6 +126,9 @@ struct Ctx {
   int gemm_mode = -1;  // overlap GEMM: -1 by precision (mixed -> tensor cores), 0 FP64 SIMT, 1 tensor cores
   int nsm = 0;         // SMs of the device
   int xr_chunks = 0;   // density x-stage pair chunks: 0 = chosen per launch
+  // staging chunks of host-memory band-loop calls (0 = automatic): pairs in the
+  // first chunk, number of chunks, density x-stage groups of rhoofr
+  int stage_first = 0, stage_n = 0, stage_groups = 0;
   int xc = 0;          // energy functional: 0 LDA (Slater + Perdew-Zunger), 1 PBE
   int fft_engine = 0;  // band-loop FFTs: 0 four-step where a plan exists, else Stockham; 2 Stockham always
   int plane = 1;       // FP32 band loop, y and x stages fused per z-plane where the plane fits: bit 0 vpsi, bit 1 rhoofr
