@@ -585,11 +585,12 @@ double wfn_key(const double* h, int rows) {
   for (; i < rows; ++i) s[0] += std::sqrt(h[2 * (size_t)i] * h[2 * (size_t)i] + h[2 * (size_t)i + 1] * h[2 * (size_t)i + 1]);
   return (s[0] + s[1]) + (s[2] + s[3]);
 }
-bool wfn_hit(Ctx& c, const double* h, int ld, int n) {
+// every part of the key but the host pass over c0(:,1)
+bool wfn_maybe(const Ctx& c, const double* h, int ld, int n) {
   const gbcp::WfnCache& w = c.wfn;
-  return w.on && w.valid && w.host == h && w.ldc == ld && w.n == n && w.dev == c.st_c0.p &&
-         wfn_key(h, c.ngw) == w.key;
+  return w.on && w.valid && w.host == h && w.ldc == ld && w.n == n && w.dev == c.st_c0.p;
 }
+bool wfn_hit(Ctx& c, const double* h, int ld, int n) { return wfn_maybe(c, h, ld, n) && wfn_key(h, c.ngw) == c.wfn.key; }
 void wfn_put(Ctx& c, const double* h, int ld, int n) {
   gbcp::WfnCache& w = c.wfn;
   if (!w.on) return;
@@ -924,9 +925,14 @@ int gbcp_ortho(gbcp_ctx* h, double* c0, int ldc, int nstate, int method, double*
   if (mem == GBCP_MEM_HOST && method == GBCP_ORTHO_GS) {
     // copies overlapped with the work where the tensor-core engine runs the step; c0 is
     // rewritten in st_c0 and on the host, so the cached copy ends here
-    const bool resident = wfn_hit(c, c0, ldc, nstate);
+    // on a likely cache hit the read-only part (overlap, Cholesky) starts on the cached
+    // copy while the host checks the key, which is confirmed before C U^-1 rewrites it
+    const bool maybe = wfn_maybe(c, c0, ldc, nstate);
+    const double key = c.wfn.key;
     c.wfn.valid = false;
-    rc = gbcp::ortho_gs_host(c, c0, ldc, nstate, scond, resident ? 1 : 0);
+    const std::function<bool()> confirm = [&c, c0, key]() { return wfn_key(c0, c.ngw) == key; };
+    rc = gbcp::ortho_gs_host(c, c0, ldc, nstate, scond, maybe ? 1 : 0, maybe ? &confirm : nullptr);
+    if (rc == 8) rc = gbcp::ortho_gs_host(c, c0, ldc, nstate, scond, 0, nullptr);
     if (rc != 7) return finish(c, rc);
     rc = 0;
     c.err.clear();

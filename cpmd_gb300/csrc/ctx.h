@@ -277,7 +277,11 @@ int slice_rows_side(Ctx& c, const double* A, int lda, int rows, int n, const int
 // Gram-Schmidt of host-memory c0 with the copies overlapped (tensor-core engine);
 // returns 7 when the engine or size does not allow it (the caller stages instead).
 // resident != 0: st_c0 already holds h (the wavefunction cache), no uploads
-int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host, int resident = 0);
+// resident: the states are already in st_c0 (the wavefunction cache).  confirm
+// (may be null): called once the read-only part of a resident call is queued; false
+// drops that work and returns 8, for a restart with an upload.
+int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host, int resident = 0,
+                  const std::function<bool()>* confirm = nullptr);
 // ---- CP-dynamics constraint (rortho.cu) ----
 // A (row-major n x n) = <X_i|Y_j>; tensor cores in the mixed mode, FP64 SIMT otherwise.
 int xovlap(Ctx& c, const cx<double>* X, int ldx, const cx<double>* Y, int ldy, int n, double* A);

@@ -449,7 +449,8 @@ static int ortho_gs_steps(Ctx& c, cx<double>* c0, int ldc, int n, bool want_scon
 // Cholesky, C U^-1 runs range by range (in place in the staging buffer) and each
 // finished range goes back on the download stream while the next is computed.
 // A failed step skips the GEMM, so the download returns the unchanged states.
-int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host, int resident) {
+int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host, int resident,
+                  const std::function<bool()>* confirm) {
   if (!use_tc_gemm(c) || n > 4096 || n <= 0) return 7;
   const int ngw = c.ngw;
   // G-row ranges: multiples of 64 complex rows (128 real rows: one C M row tile, four S sub-chunks)
@@ -509,6 +510,13 @@ int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host, int res
     if (!rc) rc = ovlap_tc_ranges(c, Ar, 2 * ngw, n, kb, R, up, S, sbits, c.d_info);
   }
   if (!rc) rc = chol_inverse(c, S, X, n);
+  if (!rc && resident && confirm && !(*confirm)()) {
+    // the host array changed under the same key parts: the speculative overlap and
+    // factor (which only read st_c0) are dropped before anything writes the states
+    cudaStreamSynchronize(c.stream);
+    if (c.side) cudaStreamSynchronize(c.side);
+    return 8;
+  }
   if (!rc) rc = rmul_tc_ranges(c, Ar, 2 * ngw, 2 * ngw, n, X, 1, Ar, 2 * ngw, c.geq0, c.d_info, kb, R, done, sliced);
   if (rc) {
     cudaStreamSynchronize(c.copy);

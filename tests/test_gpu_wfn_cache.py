@@ -74,3 +74,29 @@ def test_changed_first_column_is_noticed_and_option_drops_copy(gpu_lib):
     c2r[:] = 0
     ref.vpsi(c0, c2r, cl.f, cl.vpot)
     assert np.array_equal(c2, c2r)
+
+
+def test_ortho_on_changed_first_column_restarts_with_upload(gpu_lib):
+    """On a likely hit (same array, leading dimension and state count) ortho starts
+    the overlap and Cholesky on the cached copy while the host computes the key; a
+    first column changed since rhoofr fails that check, the speculative work is
+    dropped before C U^-1 writes anything, and the call restarts from the caller's
+    array: the result equals that of a context without the cache, bit for bit."""
+    from cpmd_gb300 import Context
+    cl = make_cell("c1", nstate=32)
+    ctx = Context(cl.basis, "mixed")
+    ctx.set_option("wfn_cache", 1)
+    ref = Context(cl.basis, "mixed")
+    c0 = cl.c0.copy(order="F")
+    ctx.rhoofr(c0, cl.f)
+    c0[:, 0] *= 1.5
+    a = c0.copy(order="F")
+    ctx.ortho(c0, "gs")
+    ref.ortho(a, "gs")
+    assert np.array_equal(c0, a)
+    # and a true hit after it still agrees with the uncached call to rounding
+    b = c0.copy(order="F")
+    ctx.rhoofr(c0, cl.f)
+    ctx.ortho(c0, "gs")
+    ref.ortho(b, "gs")
+    assert np.abs(c0 - b).max() <= 1e-13 * np.abs(b).max()
