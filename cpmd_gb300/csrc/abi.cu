@@ -461,10 +461,15 @@ int gbcp_set_option(gbcp_ctx* h, int key, int value) {
     c.fft_engine = value;
     return GBCP_OK;
   }
+  if (key == GBCP_OPT_ZMIRROR && value >= -1 && value <= 1) {
+    c.zmirror = value;
+    return GBCP_OK;
+  }
   if (key == GBCP_OPT_STAGES && value >= 0) {
     c.stage_first = value & 0xFF;
     c.stage_n = (value >> 8) & 0xFF;
     c.stage_groups = (value >> 16) & 0xFF;
+    c.stage_last = (value >> 24) & 0x7F;
     return GBCP_OK;
   }
   if (key == GBCP_OPT_XCHUNKS && value >= 0 && value <= 8) {
@@ -670,30 +675,39 @@ int pipe_up(Ctx& c, cx<double>* d, const double* h, int ld, int s0, int ns) {
 // Staging chunks of a host-memory band-loop call, as pair ranges, each at most one
 // launch batch.  vpsi: a small first chunk (its upload is the only one the
 // transforms wait for), two large middle ones, and a small last one (its
-// transforms and its C2 download are the tail nothing overlaps).  rhoofr: a small
-// first chunk and three equal ones.  GBCP_OPT_STAGES fixes the plan for both.
-// Returns the number of chunks.
-int stage_plan(Ctx& c, int nstate, bool rho = false) {
+// transforms and its C2 download are the tail nothing overlaps); with c0 already
+// on the device, three chunks from large to small.  rhoofr: a small first chunk
+// and three equal ones.  GBCP_OPT_STAGES fixes the plan for both.  Returns the
+// number of chunks.
+enum StageKind { STAGE_VPSI = 0, STAGE_RHOOFR = 1, STAGE_VPSI_CACHED = 2 };
+int stage_plan(Ctx& c, int nstate, int kind) {
   const int npairs = (nstate + 1) / 2;
   std::vector<int>& b = c.stage_bounds;
   b.assign(1, 0);
   if (npairs <= 0) return 0;
   // rhoofr, whose transforms wait for c0 to land: a small first chunk, then three
-  // equal ones (measured on the 128-state cell: 0.81 ms against 0.87 for the plan below)
-  const int nfix = c.stage_n > 0 ? c.stage_n : (rho ? 4 : 0);
+  // equal ones (measured on the 128-state cell: 0.81 ms against 0.87 for the plan
+  // below); vpsi with c0 already on the device, where only C2 moves: 3/8, 3/8 and
+  // 1/4 of the pairs (1.07 ms against 1.11)
+  const bool fixed = c.stage_n > 0;
+  const int nfix = fixed ? c.stage_n : (kind == STAGE_RHOOFR ? 4 : kind == STAGE_VPSI_CACHED ? 3 : 0);
   if (nfix > 0) {
     // a fixed plan: the first chunk, then equal chunks of at most one launch batch
-    const int f0 = c.stage_n > 0 ? c.stage_first : npairs / 16;
+    const int f0 = fixed ? c.stage_first : kind == STAGE_RHOOFR ? npairs / 16 : (3 * npairs + 7) / 8;
     const int first = std::max(1, std::min({f0 > 0 ? f0 : npairs, npairs, c.batch}));
     b.push_back(first);
-    const int rest = npairs - first;
+    // a fixed last chunk (GBCP_OPT_STAGES), the rest in equal chunks between
+    const int l0 = fixed ? c.stage_last : kind == STAGE_VPSI_CACHED ? npairs / 4 : 0;
+    const int lastc = std::min({l0, c.batch, std::max(0, npairs - first - 1)});
+    const int rest = npairs - first - lastc;
     if (rest > 0) {
-      const int k = std::max(std::max(1, nfix - 1), (rest + c.batch - 1) / c.batch);
+      const int k = std::max(std::max(1, nfix - 1 - (lastc > 0 ? 1 : 0)), (rest + c.batch - 1) / c.batch);
       for (int q = 1; q <= k; ++q) {
         const int e = first + (int)((long long)rest * q / k);
         if (e > b.back()) b.push_back(e);
       }
     }
+    if (lastc > 0) b.push_back(npairs);
     return (int)b.size() - 1;
   }
   const int first = std::max(1, std::min(c.batch, npairs / 16));
@@ -761,7 +775,7 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
         !gbcp::ensure(c, c.st_c0, sizeof(cx<double>) * (size_t)c.ngw * std::max(nstate, 1)))
       return GBCP_ERR_NOMEM;
     cx<double>* t = static_cast<cx<double>*>(c.st_c0.p);
-    const int nb = stage_plan(c, nstate, true);
+    const int nb = stage_plan(c, nstate, STAGE_RHOOFR);
     if ((rc = pipe_prepare(c, nb))) return rc;
     const bool resident = wfn_hit(c, c0, ldc, nstate);
     for (int b = 0; b < nb; ++b) {
@@ -841,7 +855,7 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
     void* tv = c.st_vpot.p;
     cx<double>* t0 = static_cast<cx<double>*>(c.st_c0.p);
     cx<double>* t2 = static_cast<cx<double>*>(c.st_c2.p);
-    const int nb = stage_plan(c, nstate);
+    const int nb = stage_plan(c, nstate, wfn_maybe(c, c0, ldc, nstate) ? STAGE_VPSI_CACHED : STAGE_VPSI);
     auto chunk = [&](int b, int* s0, int* ns) {
       *s0 = 2 * c.stage_bounds[b];
       *ns = std::min(2 * c.stage_bounds[b + 1], nstate) - *s0;

@@ -59,15 +59,20 @@ __device__ __forceinline__ void load_table(cx<T>* dst, const cx<T>* __restrict__
 }
 
 // ---------------------------------------------------------------- Z stage (inverse, gather)
-// The full sphere's columns, sorted by (gx, gy), form a centrally symmetric set,
-// so the mirror (-gx, -gy) of column c is column ncol - 1 - c and its entry at -z
-// is the -G of the entry at z (code -e).  A CTA takes L primary columns
-// c < ceil(ncol / 2) and their mirrors: each coefficient and each gather-table
-// entry is loaded once and feeds both lines (c1 + i c2 at +G, its conjugate
-// packing at -G).  In the four-step layout the mirror of thread (n2, n1) is
-// (N2 - n2, N1 - 1 - n1), or (0, (N1 - n1) mod N1) for n2 = 0, so the same
-// thread runs step A of both lines.  The column (0, 0), its own mirror, keeps one line.
-template <typename T, int N>
+// CTA (column block, pair): the gather of its L sphere columns straight from c0
+// through the dense table g.zgat, pair packing, step A and step B.
+// MIR: the full sphere's columns, sorted by (gx, gy), form a centrally symmetric
+// set, so the mirror (-gx, -gy) of column c is column ncol - 1 - c and its entry
+// at -z is the -G of the entry at z (code -e).  A CTA then takes L primary
+// columns c < ceil(ncol / 2) and their mirrors: each coefficient and each
+// gather-table entry is loaded once and feeds both lines (c1 + i c2 at +G, its
+// conjugate packing at -G).  In the four-step layout the mirror of thread
+// (n2, n1) is (N2 - n2, N1 - 1 - n1), or (0, (N1 - n1) mod N1) for n2 = 0, so the
+// same thread runs step A of both lines.  The column (0, 0), its own mirror,
+// keeps one line.  Half the CTAs with twice the work and shared memory each: a
+// gain where the column set is large (a single 120^3 cell: 104 -> 90 us per
+// 64-pair launch), a loss among the small concurrent kernels of a batch.
+template <typename T, int N, bool MIR>
 __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>* __restrict__ c0, int psi32, int ldc,
                                                      int s0, int nstate, cx<T>* __restrict__ zbuf,
                                                      const cx<T>* __restrict__ twAg, const double* __restrict__ f,
@@ -75,9 +80,9 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
   using P = FS<T, N>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* twA = reinterpret_cast<cx<T>*>(smem_raw);
-  cx<T>* Ts = twA + N;  // lines l (primary) and L + l (mirror)
+  cx<T>* Ts = twA + N;  // lines l (primary) and, with MIR, L + l (mirror)
   const int col0 = blockIdx.x * P::L, pair = blockIdx.y;
-  const int half = (g.ncol + 1) / 2;
+  const int half = MIR ? (g.ncol + 1) / 2 : g.ncol;
   const int is1 = s0 + 2 * pair, is2 = is1 + 1;
   const bool two = is2 < nstate;
   const size_t o1 = (size_t)is1 * ldc, o2 = (size_t)(two ? is2 : is1) * ldc;
@@ -91,7 +96,7 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
     const int t = threadIdx.x + ia * kThreads;
     if (t < P::TA) {
       const int n2 = t / P::L, l = t - n2 * P::L, col = col0 + l;
-      const bool prim = col < half, mir = prim && g.ncol - 1 - col != col;
+      const bool prim = col < half, mir = MIR && prim && g.ncol - 1 - col != col;
       cx<T> v[P::N1], u[P::N1];
       int2 ce[P::N1];
 #pragma unroll
@@ -108,28 +113,31 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
           const cx<T> pp = mk<T>(ux - wy, uy + wx), pm = mk<T>(ux + wy, wx - uy);  // at +G, at -G
           val = e > 0 ? pp : pm;
           mval = e > 0 ? pm : pp;
-          // each coefficient once: at +G in the self-mirror column, at either sign elsewhere
+          // each coefficient once: at +G, or with MIR at either sign outside the
+          // self-mirror column
           if (kpart && (e > 0 || mir)) kin_entry_t(kacc, g, ig, __int_as_float(ce[n1].y), ux, uy, wx, wy);
         }
         v[n1] = val;
         u[n1] = mval;
       }
       fs_step_a<1, T, P::N1, P::N2>(v, n2, twA, Ts + l * P::LS);
-      cx<T> vm[P::N1];
-      if (n2 == 0) {  // uniform per warp when L is a multiple of 32
+      if constexpr (MIR) {
+        cx<T> vm[P::N1];
+        if (n2 == 0) {  // uniform per warp when L is a multiple of 32
 #pragma unroll
-        for (int n1 = 0; n1 < P::N1; ++n1) vm[(P::N1 - n1) % P::N1] = u[n1];
-      } else {
+          for (int n1 = 0; n1 < P::N1; ++n1) vm[(P::N1 - n1) % P::N1] = u[n1];
+        } else {
 #pragma unroll
-        for (int n1 = 0; n1 < P::N1; ++n1) vm[P::N1 - 1 - n1] = u[n1];
+          for (int n1 = 0; n1 < P::N1; ++n1) vm[P::N1 - 1 - n1] = u[n1];
+        }
+        fs_step_a<1, T, P::N1, P::N2>(vm, n2 == 0 ? 0 : P::N2 - n2, twA, Ts + (P::L + l) * P::LS);
       }
-      fs_step_a<1, T, P::N1, P::N2>(vm, n2 == 0 ? 0 : P::N2 - n2, twA, Ts + (P::L + l) * P::LS);
     }
   }
   __syncthreads();
   cx<T>* zb = zbuf + (size_t)pair * N * g.ncol;
 #pragma unroll
-  for (int ib = 0; ib < 2 * P::IB; ++ib) {
+  for (int ib = 0; ib < (MIR ? 2 : 1) * P::IB; ++ib) {
     const int t = threadIdx.x + (ib % P::IB) * kThreads, side = ib / P::IB;
     if (t < P::TB) {
       const int k1 = t / P::L, l = t - k1 * P::L, col = col0 + l;

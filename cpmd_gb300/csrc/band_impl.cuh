@@ -569,9 +569,17 @@ template <typename T, int N> constexpr size_t fs_smem_x(int tables) {
 
 // Column blocks of the Z stage (the grid's x extent), for the size of the
 // per-CTA partials of rhoofr's scalars.
+// The four-step gather over column/mirror pairs (k_zinv_fs<.., true>): on by
+// default where the column set spans at least 48 blocks (the 120^3 and larger
+// cells), GBCP_OPT_ZMIRROR forces it on or off (a batch turns it off)
+template <typename T, int NC> bool zmirror_n(const Ctx& c) {
+  if constexpr (NC > 0) return c.zmirror > 0 || (c.zmirror < 0 && (c.geo.ncol + FS<T, NC>::L - 1) / FS<T, NC>::L >= 48);
+  else return false;
+}
 template <typename T, int NC> int zinv_blocks_n(const Ctx& c) {
-  // four-step: blocks of primary columns, each with its mirrors (k_zinv_fs)
-  if constexpr (NC > 0) return ((c.geo.ncol + 1) / 2 + FS<T, NC>::L - 1) / FS<T, NC>::L;
+  // four-step: column blocks, or blocks of primary columns, each with its mirrors
+  if constexpr (NC > 0)
+    return ((zmirror_n<T, NC>(c) ? (c.geo.ncol + 1) / 2 : c.geo.ncol) + FS<T, NC>::L - 1) / FS<T, NC>::L;
   else return (c.geo.ncol + lines_rt(c.geo.n3) - 1) / lines_rt(c.geo.n3);
 }
 
@@ -583,10 +591,18 @@ int launch_zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int n
   cx<T>* zb = static_cast<cx<T>*>(c.zbuf.p) + (size_t)poff * g.n3 * g.ncol;  // pair poff of the launch batch
   ProfScope ps_(c, "k_zinv");
   if constexpr (NC > 0) {
-    constexpr size_t sm = fs_smem<T, NC>(2, 1);
-    allow_smem(k_zinv_fs<T, NC>, sm);
-    k_zinv_fs<T, NC><<<dim3(zinv_blocks_n<T, NC>(c), np), kThreads, sm, c.stream>>>(g, c0, c.psi32, ldc, s0, nstate, zb,
-                                                                                    twA_of<T>(c, 2), f, kpart);
+    const dim3 grid(zinv_blocks_n<T, NC>(c), np);
+    if (zmirror_n<T, NC>(c)) {
+      constexpr size_t sm = fs_smem<T, NC>(2, 1);
+      allow_smem(k_zinv_fs<T, NC, true>, sm);
+      k_zinv_fs<T, NC, true><<<grid, kThreads, sm, c.stream>>>(g, c0, c.psi32, ldc, s0, nstate, zb, twA_of<T>(c, 2), f,
+                                                               kpart);
+    } else {
+      constexpr size_t sm = fs_smem<T, NC>(1, 1);
+      allow_smem(k_zinv_fs<T, NC, false>, sm);
+      k_zinv_fs<T, NC, false><<<grid, kThreads, sm, c.stream>>>(g, c0, c.psi32, ldc, s0, nstate, zb, twA_of<T>(c, 2), f,
+                                                                kpart);
+    }
   } else {
     const int nl = lines_rt(g.n3);
     const size_t sm = stage_smem<T>(g.n3, nl);

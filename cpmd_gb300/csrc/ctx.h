@@ -127,8 +127,9 @@ struct Ctx {
   int nsm = 0;         // SMs of the device
   int xr_chunks = 0;   // density x-stage pair chunks: 0 = chosen per launch
   // staging chunks of host-memory band-loop calls (0 = automatic): pairs in the
-  // first chunk, number of chunks, density x-stage groups of rhoofr
-  int stage_first = 0, stage_n = 0, stage_groups = 0;
+  // first chunk, number of chunks, density x-stage groups of rhoofr, pairs in the last chunk
+  int stage_first = 0, stage_n = 0, stage_groups = 0, stage_last = 0;
+  int zmirror = -1;    // Z-stage gather over column/mirror pairs: -1 by size, 0 off, 1 on
   int xc = 0;          // energy functional: 0 LDA (Slater + Perdew-Zunger), 1 PBE
   int fft_engine = 0;  // band-loop FFTs: 0 four-step where a plan exists, else Stockham; 2 Stockham always
   int plane = 1;       // FP32 band loop, y and x stages fused per z-plane where the plane fits: bit 0 vpsi, bit 1 rhoofr

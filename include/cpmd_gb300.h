@@ -130,7 +130,12 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  *                   overlap the transforms chunk by chunk: 0 (the default) =
  *                   automatic; otherwise (pairs in the first chunk) + 256 x
  *                   (number of chunks) + 65536 x (density x-stage groups of
- *                   rhoofr);
+ *                   rhoofr) + 16777216 x (pairs in the last chunk, 0 = equal
+ *                   to the others);
+ *   GBCP_OPT_ZMIRROR  Z-stage gather of the four-step band loop: -1 (the
+ *                   default) = over pairs of mirror columns (each coefficient
+ *                   loaded once) where the sphere has at least 48 column
+ *                   blocks, 0 = off, 1 = on; a batch turns it off;
  *   GBCP_OPT_TEST_TIMEOUT  test hook of the failure path: 1 = the next overlap
  *                   on the tensor cores issues no operand loads, so its first
  *                   bounded wait (no copy in flight towards it) runs out after
@@ -138,7 +143,8 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  *                   c0 untouched and the hook clears itself. */
 enum gbcp_option { GBCP_OPT_GEMM = 1, GBCP_OPT_BATCH = 2, GBCP_OPT_FFT = 3, GBCP_OPT_XCHUNKS = 4, GBCP_OPT_XC = 5,
                    GBCP_OPT_WFN_CACHE = 6, GBCP_OPT_PLANE = 7, GBCP_OPT_CHOL = 8,
-                   GBCP_OPT_SIMT_TILE = 9, GBCP_OPT_STAGES = 10, GBCP_OPT_TEST_TIMEOUT = 90 };
+                   GBCP_OPT_SIMT_TILE = 9, GBCP_OPT_STAGES = 10, GBCP_OPT_ZMIRROR = 11,
+                   GBCP_OPT_TEST_TIMEOUT = 90 };
 int gbcp_set_option(gbcp_ctx* ctx, int key, int value);
 /* Queue later work on `stream` (a cudaStream_t; NULL = the context's own
  * stream; the CUDA legacy default stream is cudaStreamLegacy).  Device-pointer calls are ordered only with respect to this stream,

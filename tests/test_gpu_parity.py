@@ -167,6 +167,31 @@ def test_band_loop_all_mesh_plans(gpu_lib, nr, ecut, alat, precision, plane):
     assert rel(c2, c2_r) < tol
 
 
+@pytest.mark.parametrize("nr,ecut,alat,nstate", [(32, 20.0, 10.26, 5), (72, 50.0, 10.26, 4), (120, 70.0, 20.52, 5),
+                                                 (240, 70.0, 41.04, 3)])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("zmirror", [0, 1])
+def test_zstage_gather_mirror_pairs(gpu_lib, nr, ecut, alat, nstate, precision, zmirror):
+    """The Z-stage gather over column/mirror pairs (GBCP_OPT_ZMIRROR = 1, the default
+    from 48 column blocks up) and the plain gather (0) give the oracle's rho, E_kin,
+    norm and c2 on small and large meshes, an odd state count included (a single
+    state in the last pair)."""
+    cl = make_small_cell(alat, nr, ecut, nstate, seed=nr + 7)
+    b = cl.basis
+    rho_r, ek_r, cg_r, _ = O.rhoofr(cl.c0, cl.f, b.mill, b.nr, b.kr, b.omega, b.hg, b.tpiba2, b.geq0)
+    c2_r = O.vpsi(cl.c0, np.zeros_like(cl.c0), cl.f, cl.vpot, b.mill, b.nr, b.hg, b.tpiba2, b.geq0)
+    ctx = ctx_for(b, precision)
+    ctx.set_option("zmirror", zmirror)
+    rho, ek, cg, _ = ctx.rhoofr(cl.c0, cl.f)
+    c2 = np.zeros_like(cl.c0)
+    ctx.vpsi(cl.c0, c2, cl.f, cl.vpot)
+    tol = TOL64 if precision == "fp64" else TOL32
+    assert rel(rho, rho_r) < tol
+    assert rel(c2, c2_r) < tol
+    assert abs(ek - ek_r) <= tol * abs(ek_r)
+    assert abs(cg - cg_r) <= tol * abs(cg_r)
+
+
 # ------------------------------------------------------------------ ortho
 def perturbed(cl, scale=0.05, seed=3):
     rng = np.random.default_rng(seed)
