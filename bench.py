@@ -747,7 +747,7 @@ def run_extras(args, dev):
     # states in the mixed and FP64 precisions
     for key, prec, c64 in (("mixed_c64", "mixed", True), ("mixed", "mixed", False), ("fp64", "fp64", False)):
         io = io_of(c64)
-        bt = Batch([cc.basis for cc in cells], prec, nstreams=16)
+        bt = Batch([cc.basis for cc in cells], prec, nstreams=len(cells))
         report = bt.tune(io)
         en[key] = bt.step(io)[0]
         for _ in range(3):
