@@ -119,11 +119,26 @@ __global__ void __launch_bounds__(kThreads, 2) k_plane_vx_fs(GeoDev g, cx<float>
   cx<float>* Pl = X + PL::XEL;
   const int z = blockIdx.x, pair = blockIdx.y;
   cx<float>* zrow = zbuf + ((size_t)pair * g.n3 + z) * g.ncol;
+  // the plane's sphere columns (one contiguous run of zbuf) copied in with cp.async
+  // into the end of Pl, which no y-inverse block writes before the last one has
+  // read them; the y-inverse then reads shared memory instead of scattered HBM
+  // lines.  Where the plane leaves no such room, it reads zbuf directly.
+  const int nblk = (g.nslot + P::L - 1) / P::L;
+  const int zs_off = g.nslot * P::LS - g.ncol;
+  const bool stage = zs_off >= (nblk - 1) * P::L * P::LS;  // the same in every thread
+  const cx<float>* zsrc = zrow;
+  if (stage) {
+    cx<float>* zs = Pl + zs_off;
+    for (int e = threadIdx.x; e < g.ncol; e += kThreads) cp_async_cx(zs + e, zrow + e);
+    cp_async_commit();
+    zsrc = zs;
+  }
   load_table(twy, twAyg, N);
   load_table(twx, twAxg, N);
   load_table(twbx, twBxg, N);
+  if (stage) cp_async_wait<0>();
   __syncthreads();
-  plane_yinv<N>(g, zrow, twy, Pl, X);
+  plane_yinv<N>(g, zsrc, twy, Pl, X);
   for (int y0 = 0; y0 < N; y0 += P::L) {
     // this thread's V(r) values of step B, loaded before step A so that their
     // latency passes during it
@@ -177,7 +192,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_plane_vx_fs(GeoDev g, cx<float>
     }
     __syncthreads();
   }
-  // forward y-transforms of the slot lines; keep the sphere columns
+  // forward y-transforms of the slot lines; keep the sphere columns.  The columns
+  // are gathered in the start of Pl, whose first block of slot lines step A has
+  // consumed before the first step B writes there (ncol <= L LS), then written to
+  // zbuf as one contiguous run; otherwise straight to zbuf.
+  const bool ostage = g.ncol <= P::L * P::LS;  // the same in every thread
+  cx<float>* zdst = ostage ? Pl : zrow;
   for (int sb = 0; sb < g.nslot; sb += P::L) {
 #pragma unroll
     for (int ia = 0; ia < P::IA; ++ia) {
@@ -204,13 +224,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_plane_vx_fs(GeoDev g, cx<float>
 #pragma unroll
           for (int k2 = 0; k2 < P::N2; ++k2) {
             const int off = freq_split<N, P::N1>(k1, k2) - gylo;
-            if (in_range(off, ncs)) zrow[c0s + off] = w[k2];
+            if (in_range(off, ncs)) zdst[c0s + off] = w[k2];
           }
         }
       }
     }
     __syncthreads();
   }
+  if (ostage)
+    for (int e = threadIdx.x; e < g.ncol; e += kThreads) zrow[e] = Pl[e];
 }
 
 // CTA (chunk, z): rhoofr's y-inverse and x-inverse of plane z for the pairs
