@@ -272,6 +272,15 @@ static int build_geometry(Ctx& c, const int32_t* inyh, const double* hg) {
   g.nslot = nslot;
   g.gxlo = gxlo;
   g.nent = (int)col_ent.size();
+  g.yblk_cols = ncol;
+  if (gbcp::fs_lines(n[1]) > 0) {
+    const int L = gbcp::fs_lines(n[1]);
+    g.yblk_cols = 0;
+    for (int sb = 0; sb < nslot; sb += L) {
+      const int ce = sb + L < nslot ? slot_col0[sb + L] : ncol;
+      g.yblk_cols = std::max(g.yblk_cols, ce - slot_col0[sb]);
+    }
+  }
   if (!upload(c, col_start, g.col_start) || !upload(c, col_zlo, g.col_zlo) || !upload(c, col_ent, g.col_ent) ||
       !upload(c, col_slot, g.col_slot) || !upload(c, col_gy, g.col_gy) || !upload(c, ent_col, g.ent_col) ||
       !upload(c, slot_col0, g.slot_col0) || !upload(c, slot_gylo, g.slot_gylo) ||

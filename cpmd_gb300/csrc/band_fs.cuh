@@ -53,6 +53,19 @@ __device__ __forceinline__ void fs_step_b(const cx<T>* line, int k1, cx<T> (&w)[
   dftn<S, N2>(w);
 }
 
+// cp.async copies of complex elements (8 or 16 bytes), their commit and wait
+template <typename T> __device__ __forceinline__ void cp_async_cx(cx<T>* dst, const cx<T>* src) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  if constexpr (sizeof(cx<T>) == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int NPEND> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(NPEND) : "memory");
+}
+
 template <typename T>
 __device__ __forceinline__ void load_table(cx<T>* dst, const cx<T>* __restrict__ src, int n) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
@@ -166,8 +179,19 @@ __global__ void __launch_bounds__(kThreads) k_yinv_fs(GeoDev g, const cx<T>* __r
   cx<T>* Ts = twA + N;
   const int sb = blockIdx.x * P::L, z = blockIdx.y, pair = blockIdx.z;
   const cx<T>* zrow = zbuf + ((size_t)pair * g.n3 + z) * g.ncol;
+  // FP32: the block's sphere columns (one contiguous run of zbuf) copied in with
+  // cp.async, so that the scattered reads of step A hit shared memory
+  constexpr bool STAGE = sizeof(T) == 4;
+  cx<T>* zs = Ts + P::L * P::LS;
+  const int cb = g.slot_col0[sb], ce = sb + P::L < g.nslot ? g.slot_col0[sb + P::L] : g.ncol;
+  if constexpr (STAGE) {
+    for (int e = cb + (int)threadIdx.x; e < ce; e += kThreads) cp_async_cx(zs + (e - cb), zrow + e);
+    cp_async_commit();
+  }
   load_table(twA, twAg, N);
+  if constexpr (STAGE) cp_async_wait<0>();
   __syncthreads();
+  const cx<T>* zsrc = STAGE ? zs - cb : zrow;
 #pragma unroll
   for (int ia = 0; ia < P::IA; ++ia) {
     const int t = threadIdx.x + ia * kThreads;
@@ -183,7 +207,7 @@ __global__ void __launch_bounds__(kThreads) k_yinv_fs(GeoDev g, const cx<T>* __r
 #pragma unroll
       for (int n1 = 0; n1 < P::N1; ++n1) {
         const int off = freq_split<N, P::N2>(n2, n1) - gylo;
-        v[n1] = in_range(off, ncs) ? zrow[c0s + off] : mk<T>(0, 0);
+        v[n1] = in_range(off, ncs) ? zsrc[c0s + off] : mk<T>(0, 0);
       }
       fs_step_a<1, T, P::N1, P::N2>(v, n2, twA, Ts + l * P::LS);
     }
@@ -228,18 +252,6 @@ __device__ __forceinline__ void xline_step_a(const GeoDev& g, const cx<T>* __res
 
 // ---------------------------------------------------------------- X stage + density
 // asynchronous global -> shared copy of one complex (LDGSTS; completes without a wait loop)
-template <typename T> __device__ __forceinline__ void cp_async_cx(cx<T>* dst, const cx<T>* src) {
-  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
-  if constexpr (sizeof(cx<T>) == 16)
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int NPEND> __device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(NPEND) : "memory");
-}
-
 // slab buffers of the density x-stage: two (copy of the next pair overlaps the
 // current one) in FP32, one in FP64 (shared memory)
 template <typename T> __host__ __device__ constexpr int xrho_bufs() { return sizeof(T) == 4 ? 2 : 1; }

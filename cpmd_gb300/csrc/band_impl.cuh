@@ -621,7 +621,8 @@ template <typename T, int NC> int launch_yinv(Ctx& c, int np, int poff) {
   cx<T>* yb = static_cast<cx<T>*>(c.ybuf.p) + (size_t)poff * g.n3 * g.n2 * g.nslot;
   ProfScope ps_(c, "k_yinv");
   if constexpr (NC > 0) {
-    constexpr size_t sm = fs_smem<T, NC>(1, 1);
+    // FP32: plus the staged sphere columns of one block of slots
+    const size_t sm = fs_smem<T, NC>(1, 1) + (sizeof(T) == 4 ? sizeof(cx<T>) * (size_t)g.yblk_cols : 0);
     allow_smem(k_yinv_fs<T, NC>, sm);
     k_yinv_fs<T, NC><<<dim3((g.nslot + FS<T, NC>::L - 1) / FS<T, NC>::L, g.n3, np), kThreads, sm, c.stream>>>(
         g, zb, yb, twA_of<T>(c, 1));

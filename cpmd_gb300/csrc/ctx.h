@@ -52,6 +52,7 @@ struct GeoDev {
   int k1, k2;           // leading dims of real-space arrays
   int ngw;
   int ncol, nslot, gxlo, nent;
+  int yblk_cols;         // most sphere columns of one y-stage block of slots (four-step plan of n2)
   const int* col_start;  // ncol+1
   const int* col_zlo;    // ncol
   const int* col_ent;    // nent
