@@ -272,6 +272,15 @@ static int build_geometry(Ctx& c, const int32_t* inyh, const double* hg) {
   g.nslot = nslot;
   g.gxlo = gxlo;
   g.nent = (int)col_ent.size();
+  {
+    int gymin = 1 << 30, gymax = -(1 << 30);
+    for (int cc = 0; cc < ncol; ++cc) {
+      gymin = std::min(gymin, col_gy[cc]);
+      gymax = std::max(gymax, col_gy[cc]);
+    }
+    g.prune_x = n[0] % 4 == 0 && gxlo >= -n[0] / 4 && gxlo + nslot - 1 <= n[0] / 4 - 1;
+    g.prune_y = n[1] % 4 == 0 && gymin >= -n[1] / 4 && gymax <= n[1] / 4 - 1;
+  }
   g.yblk_cols = ncol;
   if (gbcp::fs_lines(n[1]) > 0) {
     const int L = gbcp::fs_lines(n[1]);

@@ -33,10 +33,15 @@ template <typename T> __device__ __forceinline__ cx<T> twmul(cx<T> v, cx<T> w, b
   return conj ? cmulc(v, w) : cmul(v, w);
 }
 
-// step A on registers v[N1] of line position n2; writes T[k1][n2] = line[k1*PITCH + n2]
-template <int S, typename T, int N1, int N2, int PITCH = N2>
+// step A on registers v[N1] of line position n2; writes T[k1][n2] = line[k1*PITCH + n2].
+// PR (N1 = 8): the line's input lies within frequencies [-N/4, N/4), so v[2] .. v[5]
+// (positions n2 + N2 n1, n1 = 2..5) are zero and are neither loaded nor transformed
+template <int S, typename T, int N1, int N2, int PITCH = N2, bool PR = false>
 __device__ __forceinline__ void fs_step_a(cx<T> (&v)[N1], int n2, const cx<T>* __restrict__ twA, cx<T>* line) {
-  dftn<S, N1>(v);
+  if constexpr (PR && N1 == 8)
+    dft8_lo<S>(v);
+  else
+    dftn<S, N1>(v);
 #pragma unroll
   for (int k1 = 0; k1 < N1; ++k1) {
     cx<T> r = v[k1];
@@ -170,7 +175,7 @@ __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>
 }
 
 // ---------------------------------------------------------------- Y stage (inverse)
-template <typename T, int N>
+template <typename T, int N, bool PR>
 __global__ void __launch_bounds__(kThreads) k_yinv_fs(GeoDev g, const cx<T>* __restrict__ zbuf,
                                                      cx<T>* __restrict__ ybuf, const cx<T>* __restrict__ twAg) {
   using P = FS<T, N>;
@@ -209,7 +214,7 @@ __global__ void __launch_bounds__(kThreads) k_yinv_fs(GeoDev g, const cx<T>* __r
         const int off = freq_split<N, P::N2>(n2, n1) - gylo;
         v[n1] = in_range(off, ncs) ? zsrc[c0s + off] : mk<T>(0, 0);
       }
-      fs_step_a<1, T, P::N1, P::N2>(v, n2, twA, Ts + l * P::LS);
+      fs_step_a<1, T, P::N1, P::N2, P::N2, PR>(v, n2, twA, Ts + l * P::LS);
     }
   }
   __syncthreads();
@@ -264,7 +269,7 @@ template <typename T> __host__ __device__ constexpr int xrho_bufs() { return siz
 // several, each CTA stores its partial tile, and the last CTA of the tile to
 // finish (ticket counter) adds the partials in chunk order: the result does not
 // depend on the order the CTAs run in.
-template <typename T, int N>
+template <typename T, int N, bool PR>
 __global__ void __launch_bounds__(kThreads) k_xrho_fs(GeoDev g, const cx<T>* __restrict__ ybuf, int npairs, int s0,
                                                      int nstate, const double* __restrict__ f, double inv_omega,
                                                      double* __restrict__ rho, const cx<T>* __restrict__ twAg,
@@ -320,7 +325,7 @@ __global__ void __launch_bounds__(kThreads) k_xrho_fs(GeoDev g, const cx<T>* __r
           const int s = freq_split<N, P::N2>(n2, n1) - g.gxlo;
           v[n1] = (y < g.n2 && in_range(s, nslot)) ? sl[l * nslot + s] : mk<T>(0, 0);
         }
-        fs_step_a<1, T, P::N1, P::N2, P::XP>(v, n2, twA, Ts + l * P::XS);
+        fs_step_a<1, T, P::N1, P::N2, P::XP, PR>(v, n2, twA, Ts + l * P::XS);
       }
     }
     __syncthreads();

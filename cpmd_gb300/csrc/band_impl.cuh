@@ -623,9 +623,17 @@ template <typename T, int NC> int launch_yinv(Ctx& c, int np, int poff) {
   if constexpr (NC > 0) {
     // FP32: plus the staged sphere columns of one block of slots
     const size_t sm = fs_smem<T, NC>(1, 1) + (sizeof(T) == 4 ? sizeof(cx<T>) * (size_t)g.yblk_cols : 0);
-    allow_smem(k_yinv_fs<T, NC>, sm);
-    k_yinv_fs<T, NC><<<dim3((g.nslot + FS<T, NC>::L - 1) / FS<T, NC>::L, g.n3, np), kThreads, sm, c.stream>>>(
-        g, zb, yb, twA_of<T>(c, 1));
+    auto go = [&](auto kern) {
+      allow_smem(kern, sm);
+      kern<<<dim3((g.nslot + FS<T, NC>::L - 1) / FS<T, NC>::L, g.n3, np), kThreads, sm, c.stream>>>(g, zb, yb,
+                                                                                                twA_of<T>(c, 1));
+    };
+    if constexpr (FS<T, NC>::N1 == 8) {
+      if (g.prune_y) go(k_yinv_fs<T, NC, true>);
+      else go(k_yinv_fs<T, NC, false>);
+    } else {
+      go(k_yinv_fs<T, NC, false>);
+    }
   } else {
     const int nl = lines_rt(g.n2);
     const size_t sm = stage_smem<T>(g.n2, nl);
@@ -685,10 +693,18 @@ int launch_xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double*
       part = static_cast<T*>(c.xr_part.p);
       tickets = static_cast<unsigned*>(c.xr_tk.p);
     }
-    allow_smem(k_xrho_fs<T, NC>, sm);
     ProfScope ps_(c, "k_xinv_rho");
-    k_xrho_fs<T, NC><<<dim3(nchunk, tiles_y, g.n3), kThreads, sm, c.stream>>>(
-        g, yb, np, s0, nstate, f, 1.0 / c.omega, rho, twA_of<T>(c, 0), pchunk, part, tickets);
+    auto go = [&](auto kern) {
+      allow_smem(kern, sm);
+      kern<<<dim3(nchunk, tiles_y, g.n3), kThreads, sm, c.stream>>>(g, yb, np, s0, nstate, f, 1.0 / c.omega, rho,
+                                                                    twA_of<T>(c, 0), pchunk, part, tickets);
+    };
+    if constexpr (FS<T, NC>::N1 == 8) {
+      if (g.prune_x) go(k_xrho_fs<T, NC, true>);
+      else go(k_xrho_fs<T, NC, false>);
+    } else {
+      go(k_xrho_fs<T, NC, false>);
+    }
   } else {
     int nl = lines_rt(g.n1);
     while (nl > 1 && nl * g.n1 > kMaxAcc * kThreads) --nl;
@@ -794,11 +810,22 @@ template <typename T, int NC> int launch_plane_vx(Ctx& c, int np, int poff, cons
     const GeoDev& g = c.geo;
     cx<float>* zb = static_cast<cx<float>*>(c.zbuf.p) + (size_t)poff * g.n3 * g.ncol;
     const size_t sm = PlaneLayout<NC>::bytes(3, g.nslot);
-    allow_smem(k_plane_vx_fs<NC>, sm);
     ProfScope ps_(c, "k_plane_vx");
-    k_plane_vx_fs<NC><<<dim3(g.n3, np), kThreads, sm, c.stream>>>(g, zb, reinterpret_cast<const float*>(vpotT),
-                                                                  twA_of<float>(c, 1), twA_of<float>(c, 0),
-                                                                  twB_of<float>(c, 0));
+    auto go = [&](auto kern) {
+      allow_smem(kern, sm);
+      kern<<<dim3(g.n3, np), kThreads, sm, c.stream>>>(g, zb, reinterpret_cast<const float*>(vpotT),
+                                                      twA_of<float>(c, 1), twA_of<float>(c, 0), twB_of<float>(c, 0));
+    };
+    // x and y have the same length here; the radix-8 plans prune each axis whose
+    // sphere frequencies allow it
+    if constexpr (FS<float, NC>::N1 == 8) {
+      if (g.prune_x && g.prune_y) go(k_plane_vx_fs<NC, true, true>);
+      else if (g.prune_x) go(k_plane_vx_fs<NC, true, false>);
+      else if (g.prune_y) go(k_plane_vx_fs<NC, false, true>);
+      else go(k_plane_vx_fs<NC, false, false>);
+    } else {
+      go(k_plane_vx_fs<NC, false, false>);
+    }
     GBCP_LAUNCH_CHECK(c);
     return 0;
   } else {

@@ -33,7 +33,7 @@ template <int N> struct PlaneLayout {
 // kThreads threads (tt = thread within the group, h = group); group h transforms
 // the slot-line blocks h, h + nh, ... in its own exchange tile X, every group
 // running the same number of barriers.
-template <int N>
+template <int N, bool PR = false>
 __device__ __forceinline__ void plane_yinv(const GeoDev& g, const cx<float>* __restrict__ zrow, const cx<float>* twy,
                                            cx<float>* Pl, cx<float>* X, int tt = threadIdx.x, int h = 0, int nh = 1) {
   using P = FS<float, N>;
@@ -57,7 +57,7 @@ __device__ __forceinline__ void plane_yinv(const GeoDev& g, const cx<float>* __r
           const int off = freq_split<N, P::N2>(n2, n1) - gylo;
           v[n1] = in_range(off, ncs) ? zrow[c0s + off] : mk<float>(0, 0);
         }
-        fs_step_a<1, float, P::N1, P::N2>(v, n2, twy, X + l * P::LS);
+        fs_step_a<1, float, P::N1, P::N2, P::N2, PR>(v, n2, twy, X + l * P::LS);
       }
     }
     __syncthreads();
@@ -80,7 +80,7 @@ __device__ __forceinline__ void plane_yinv(const GeoDev& g, const cx<float>* __r
 }
 
 // step A of the inverse x-transform of rows y0 .. y0+L-1: the slots of row y from Pl
-template <int N>
+template <int N, bool PR = false>
 __device__ __forceinline__ void plane_xrow_a(const GeoDev& g, const cx<float>* Pl, int y0, const cx<float>* twx,
                                              cx<float>* X, int tt = threadIdx.x) {
   using P = FS<float, N>;
@@ -95,14 +95,14 @@ __device__ __forceinline__ void plane_xrow_a(const GeoDev& g, const cx<float>* P
         const int s = freq_split<N, P::N2>(n2, n1) - g.gxlo;
         v[n1] = (y < N && in_range(s, g.nslot)) ? Pl[(size_t)s * P::LS + y] : mk<float>(0, 0);
       }
-      fs_step_a<1, float, P::N1, P::N2, P::XP>(v, n2, twx, X + l * P::XS);
+      fs_step_a<1, float, P::N1, P::N2, P::XP, PR>(v, n2, twx, X + l * P::XS);
     }
   }
 }
 
 // CTA (z, pair): vpsi's y-inverse, x-inverse, x V(r), x-forward and y-forward of
 // one z-plane, zbuf row in place
-template <int N>
+template <int N, bool PRX, bool PRY>
 __global__ void __launch_bounds__(kThreads, 2) k_plane_vx_fs(GeoDev g, cx<float>* __restrict__ zbuf,
                                                             const float* __restrict__ vpot,
                                                             const cx<float>* __restrict__ twAyg,
@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_plane_vx_fs(GeoDev g, cx<float>
   load_table(twbx, twBxg, N);
   if (stage) cp_async_wait<0>();
   __syncthreads();
-  plane_yinv<N>(g, zsrc, twy, Pl, X);
+  plane_yinv<N, PRY>(g, zsrc, twy, Pl, X);
   for (int y0 = 0; y0 < N; y0 += P::L) {
     // this thread's V(r) values of step B, loaded before step A so that their
     // latency passes during it
@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_plane_vx_fs(GeoDev g, cx<float>
 #pragma unroll
       for (int k2 = 0; k2 < P::N2; ++k2) vr[k2] = (t < P::TB && y < N) ? __ldg(vrow + k1 + P::N1 * k2) : 0.f;
     }
-    plane_xrow_a<N>(g, Pl, y0, twx, X);
+    plane_xrow_a<N, PRX>(g, Pl, y0, twx, X);
     __syncthreads();
     // step B: inverse over k2, x V(r), forward over k2, twiddle, back into row k1
     if (threadIdx.x < P::TB) {

@@ -53,6 +53,9 @@ struct GeoDev {
   int ngw;
   int ncol, nslot, gxlo, nent;
   int yblk_cols;         // most sphere columns of one y-stage block of slots (four-step plan of n2)
+  // the sphere's frequencies along x / y lie within [-n/4, n/4): the inverse step A
+  // of a radix-8 four-step transform skips the zero half of its inputs
+  int prune_x, prune_y;
   const int* col_start;  // ncol+1
   const int* col_zlo;    // ncol
   const int* col_ent;    // nent

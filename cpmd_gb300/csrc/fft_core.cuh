@@ -95,6 +95,26 @@ template <int S, typename T> __device__ __forceinline__ void dft8(cx<T>* v) {
   v[7] = e3 - w3o;
 }
 
+// dft8 for inputs v[2] .. v[5] known to be zero (only v[0], v[1], v[6], v[7] are
+// read): the first butterflies of both length-4 halves reduce to copies, 16 of the
+// 56 real additions go
+template <int S, typename T> __device__ __forceinline__ void dft8_lo(cx<T>* v) {
+  const cx<T> x0 = v[0], x1 = v[1], x6 = v[6], x7 = v[7];
+  const cx<T> e0 = x0 + x6, e2 = x0 - x6, e1 = add_si<-S>(x0, x6), e3 = add_si<S>(x0, x6);
+  const cx<T> o0 = x1 + x7, o2 = x1 - x7, o1 = add_si<-S>(x1, x7), o3 = add_si<S>(x1, x7);
+  const T r = (T)GBCP_R2;
+  const cx<T> w1o = scl(add_si<S>(o1, o1), r);
+  const cx<T> w3o = scl(add_si<S>(mk<T>(-o3.x, -o3.y), o3), r);
+  v[0] = e0 + o0;
+  v[4] = e0 - o0;
+  v[1] = e1 + w1o;
+  v[5] = e1 - w1o;
+  v[2] = add_si<S>(e2, o2);
+  v[6] = add_si<-S>(e2, o2);
+  v[3] = e3 + w3o;
+  v[7] = e3 - w3o;
+}
+
 template <int S, int R, typename T> __device__ __forceinline__ void dft(cx<T>* v) {
   if constexpr (R == 2) dft2<S>(v);
   else if constexpr (R == 3) dft3<S>(v);

@@ -167,6 +167,37 @@ def test_band_loop_all_mesh_plans(gpu_lib, nr, ecut, alat, precision, plane):
     assert rel(c2, c2_r) < tol
 
 
+@pytest.mark.parametrize("nr,ecut", [(40, 60.0), (64, 150.0), (80, 240.0)])
+@pytest.mark.parametrize("precision,plane", [("fp64", 0), ("mixed", 0), ("mixed", 3)])
+def test_radix8_sphere_beyond_quarter_mesh(gpu_lib, nr, ecut, precision, plane):
+    """Radix-8 four-step meshes (40 = 8 x 5, 64 = 8 x 8, 80 = 8 x 10) under a
+    wavefunction sphere that reaches |G| >= N/4 along x and y (a density cutoff of
+    1.2 times the wavefunction cutoff): the inverse step A keeps all eight inputs
+    there (the pruned form, which skips positions n1 = 2..5, applies only while the
+    sphere lies within [-N/4, N/4)), in the three-stage and plane-fused kernels;
+    rho and c2 against the oracle."""
+    from cpmd_gb300.cell import make_basis
+    from cpmd_gb300.synth import atoms, random_states, vloc_grid
+    rng = np.random.default_rng(nr + 11)
+    alat = 10.26
+    tau, _ = atoms(alat, 1, 0.0, rng)
+    b = make_basis(alat, nr, ecut, dual=1.2)
+    assert int(np.abs(b.mill[: b.ngw, :2]).max()) >= nr // 4
+    c0 = random_states(b, 3, rng)
+    vpot = vloc_grid(b, tau)
+    f = np.full(3, 2.0)
+    rho_r, *_ = O.rhoofr(c0, f, b.mill, b.nr, b.kr, b.omega, b.hg, b.tpiba2, b.geq0)
+    c2_r = O.vpsi(c0, np.zeros_like(c0), f, vpot, b.mill, b.nr, b.hg, b.tpiba2, b.geq0)
+    ctx = ctx_for(b, precision)
+    ctx.set_option("plane", plane)
+    rho, *_ = ctx.rhoofr(c0, f)
+    c2 = np.zeros_like(c0)
+    ctx.vpsi(c0, c2, f, vpot)
+    tol = TOL64 if precision == "fp64" else TOL32
+    assert rel(rho, rho_r) < tol
+    assert rel(c2, c2_r) < tol
+
+
 @pytest.mark.parametrize("nr,ecut,alat,nstate", [(32, 20.0, 10.26, 5), (72, 50.0, 10.26, 4), (120, 70.0, 20.52, 5),
                                                  (240, 70.0, 41.04, 3)])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
