@@ -184,8 +184,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_plane_vx_fs(GeoDev g, cx<float>
         if (y < N) {
 #pragma unroll
           for (int j2 = 0; j2 < P::N1; ++j2) {
-            const int s = freq_split<N, P::N2>(j, j2) - g.gxlo;
-            if (in_range(s, g.nslot)) Pl[(size_t)s * P::LS + y] = u[j2];
+            // PRX: outputs 2 .. 5 lie outside the sphere's x range (and go unused)
+            if (!(PRX && P::N1 == 8 && j2 >= 2 && j2 <= 5)) {
+              const int s = freq_split<N, P::N2>(j, j2) - g.gxlo;
+              if (in_range(s, g.nslot)) Pl[(size_t)s * P::LS + y] = u[j2];
+            }
           }
         }
       }
