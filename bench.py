@@ -225,7 +225,7 @@ def run_reference(args, rank, world):
 # script's own command (python bench.py --steps 2 --warmup 3 --fp64-steps 1
 # --e2e-steps 1 --no-cpu --no-extras; k_xrho_fs: -k regex:k_xrho_fs -s 2 -c 1):
 # the density x-stage, and the three-stage vpsi x-stage used with plane = 0.
-NCU_TRAFFIC = {"k_xinv_rho": 419.696128e6 + 32.155648e6, "k_xvx": 412.769536e6 + 348.129792e6}
+NCU_TRAFFIC = {"k_xinv_rho": 419.589632e6 + 31.977216e6, "k_xvx": 412.769536e6 + 348.129792e6}
 
 
 def kernel_bytes(name: str, geo: dict, np_: int, s: int) -> float:
