@@ -100,3 +100,37 @@ def test_ortho_on_changed_first_column_restarts_with_upload(gpu_lib):
     ctx.ortho(c0, "gs")
     ref.ortho(b, "gs")
     assert np.abs(c0 - b).max() <= 1e-13 * np.abs(b).max()
+
+
+@pytest.mark.parametrize("plan", [0, 4 + 256 * 4 + 65536 * 2, 8 + 256 * 3 + 65536 * 3 + 16777216 * 4,
+                                  1 + 256 * 8 + 65536 * 1])
+def test_staging_plans_give_the_device_results(gpu_lib, plan):
+    """Host-memory rhoofr and vpsi under the automatic and fixed staging plans
+    (GBCP_OPT_STAGES: first chunk, chunk count, density groups, last chunk), with and
+    without c0 cached on the device, give the device-memory results: the plans only
+    reorder copies and launches (rho and C2 to rounding, the scalars to 1e-12)."""
+    import torch
+    from cpmd_gb300 import Context
+    cl = make_cell("c1", nstate=40)
+    dev = Context(cl.basis, "fp64")
+    c0d = torch.from_numpy(np.ascontiguousarray(cl.c0.T)).cuda()
+    fd = torch.from_numpy(cl.f).cuda()
+    vd = torch.from_numpy(cl.vpot).cuda()
+    rho_d, ek_d, cg_d, cr_d = dev.rhoofr(c0d, fd)
+    c2d = torch.zeros_like(c0d)
+    dev.vpsi(c0d, c2d, fd, vd)
+    rho_d = rho_d.cpu().numpy()
+    c2_d = c2d.cpu().numpy().T
+    for cache in (0, 1):
+        ctx = Context(cl.basis, "fp64")
+        ctx.set_option("stages", plan)
+        if cache:
+            ctx.set_option("wfn_cache", 1)
+        c0 = cl.c0.copy(order="F")
+        rho, ek, cg, cr = ctx.rhoofr(c0, cl.f)
+        c2 = np.zeros_like(c0)
+        ctx.vpsi(c0, c2, cl.f, cl.vpot)
+        assert np.abs(rho - rho_d).max() <= 1e-13 * np.abs(rho_d).max()
+        assert np.abs(c2 - c2_d).max() <= 1e-13 * np.abs(c2_d).max()
+        for a, r in ((ek, ek_d), (cg, cg_d), (cr, cr_d)):
+            assert abs(a - r) <= 1e-12 * abs(r)
