@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(kThreads) k_yinv_fs(GeoDev g, const cx<T>* __r
 }
 
 // step A of an x-line: gather the sphere slots of row y (l-major thread map)
-template <typename T, int N>
+template <typename T, int N, bool PR = false>
 __device__ __forceinline__ void xline_step_a(const GeoDev& g, const cx<T>* __restrict__ yb, int y0,
                                              const cx<T>* twA, cx<T>* Ts) {
   using P = FS<T, N>;
@@ -250,7 +250,7 @@ __device__ __forceinline__ void xline_step_a(const GeoDev& g, const cx<T>* __res
         const int s = freq_split<N, P::N2>(n2, n1) - g.gxlo;
         v[n1] = (y < g.n2 && in_range(s, g.nslot)) ? yb[(size_t)y * g.nslot + s] : mk<T>(0, 0);
       }
-      fs_step_a<1, T, P::N1, P::N2, P::XP>(v, n2, twA, Ts + l * P::XS);
+      fs_step_a<1, T, P::N1, P::N2, P::XP, PR>(v, n2, twA, Ts + l * P::XS);
     }
   }
 }
@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(kThreads) k_xrho_fs(GeoDev g, const cx<T>* __r
 }
 
 // ---------------------------------------------------------------- X stage: inverse, x V, forward
-template <typename T, int N>
+template <typename T, int N, bool PR>
 __global__ void __launch_bounds__(kThreads) k_xvx_fs(GeoDev g, cx<T>* __restrict__ ybuf,
                                                     const T* __restrict__ vpot, const cx<T>* __restrict__ twAg,
                                                     const cx<T>* __restrict__ twBg) {
@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(kThreads) k_xvx_fs(GeoDev g, cx<T>* __restrict
   load_table(twA, twAg, N);
   load_table(twB, twBg, N);
   __syncthreads();
-  xline_step_a<T, N>(g, yb, y0, twA, Ts);
+  xline_step_a<T, N, PR>(g, yb, y0, twA, Ts);
   __syncthreads();
 #pragma unroll
   for (int ib = 0; ib < P::IB; ++ib) {
@@ -430,8 +430,11 @@ __global__ void __launch_bounds__(kThreads) k_xvx_fs(GeoDev g, cx<T>* __restrict
       if (y < g.n2) {
 #pragma unroll
         for (int j2 = 0; j2 < P::N1; ++j2) {
-          const int s = freq_split<N, P::N2>(j, j2) - g.gxlo;
-          if (in_range(s, g.nslot)) yb[(size_t)y * g.nslot + s] = u[j2];
+          // PR: outputs 2 .. 5 lie outside the sphere's x range (and go unused)
+          if (!(PR && P::N1 == 8 && j2 >= 2 && j2 <= 5)) {
+            const int s = freq_split<N, P::N2>(j, j2) - g.gxlo;
+            if (in_range(s, g.nslot)) yb[(size_t)y * g.nslot + s] = u[j2];
+          }
         }
       }
     }

@@ -728,9 +728,17 @@ template <typename T, int NC> int launch_xvx(Ctx& c, int np, const double* vpot,
   ProfScope ps_(c, "k_xvx");
   if constexpr (NC > 0) {
     constexpr size_t sm = fs_smem_x<T, NC>(2);
-    allow_smem(k_xvx_fs<T, NC>, sm);
-    k_xvx_fs<T, NC><<<dim3((g.n2 + FS<T, NC>::L - 1) / FS<T, NC>::L, g.n3, np), kThreads, sm, c.stream>>>(
-        g, yb, vpotT, twA_of<T>(c, 0), twB_of<T>(c, 0));
+    auto go = [&](auto kern) {
+      allow_smem(kern, sm);
+      kern<<<dim3((g.n2 + FS<T, NC>::L - 1) / FS<T, NC>::L, g.n3, np), kThreads, sm, c.stream>>>(
+          g, yb, vpotT, twA_of<T>(c, 0), twB_of<T>(c, 0));
+    };
+    if constexpr (FS<T, NC>::N1 == 8) {
+      if (g.prune_x) go(k_xvx_fs<T, NC, true>);
+      else go(k_xvx_fs<T, NC, false>);
+    } else {
+      go(k_xvx_fs<T, NC, false>);
+    }
   } else {
     const int nl = lines_rt(g.n1);
     const size_t sm = stage_smem<T>(g.n1, nl);
