@@ -237,6 +237,8 @@ def kernel_bytes(name: str, geo: dict, np_: int, s: int) -> float:
     grid = n1 * n2 * n3
     if name == "k_zinv":
         return np_ * (2 * ngw * 16 + zb)
+    if name == "k_wfn_sum":  # the states' checksum of the kept Z stage: one read of c0
+        return np_ * 2 * ngw * 16
     if name == "k_yinv":
         return np_ * (zb + yb)
     if name == "k_xinv_rho":

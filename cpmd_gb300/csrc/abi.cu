@@ -24,6 +24,10 @@ std::atomic<long long> g_launches{0};
 bool ensure(Ctx& c, Scratch& s, size_t bytes) {
   if (bytes <= s.cap && s.p) return true;
   if (&s == &c.st_c0) c.wfn.valid = false;  // a new buffer holds no cached wavefunction
+  if (&s == &c.zbuf) {  // nor a kept Z stage
+    c.zk.valid = false;
+    c.zk_skip = nullptr;
+  }
   if (s.p) {
     cudaStreamSynchronize(c.stream);
     cudaFree(s.p);
@@ -437,7 +441,7 @@ int gbcp_ctx_destroy(gbcp_ctx* h) {
                           &c.st_misc, &c.st_misc2, &c.st_vf, &c.red, &c.red2, &c.smat, &c.smat2, &c.smat3, &c.sparts, &c.cscr, &c.cdiag, &c.cwork, &c.xr_part, &c.xr_tk, &c.rt_mats, &c.en_g3, &c.oz_a, &c.oz_b,
                           &c.nl_a, &c.nl_b, &c.nl_c, &c.nl_d, &c.nl_ta, &c.nl_tb, &c.nl_tp, &c.en_rho, &c.en_a, &c.en_b, &c.en_veff,
                           &c.en_red, &c.en_ei, &c.en_fp, &c.en_idx, &c.en_in[0], &c.en_in[1], &c.en_in[2],
-                          &c.en_in[3], &c.en_in[4], &c.oz_c, &c.oz_rmax, &c.rho_sc, &c.rho_tk};
+                          &c.en_in[3], &c.en_in[4], &c.oz_c, &c.oz_rmax, &c.rho_sc, &c.rho_tk, &c.zk_sum};
   for (auto* s : all) gbcp::release(*s);
   for (cudaStream_t* st : {&c.copy, &c.copy_out, &c.side})
     if (*st) {
@@ -446,6 +450,8 @@ int gbcp_ctx_destroy(gbcp_ctx* h) {
     }
   for (cudaEvent_t e : c.pipe_ev) cudaEventDestroy(e);
   for (cudaEvent_t e : c.side_ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : c.zk_ev)
+    if (e) cudaEventDestroy(e);
   if (c.d_info) cudaFree(c.d_info);
   gbcp::prof_fold(c);
   for (cudaEvent_t e : c.prof_pool) cudaEventDestroy(e);
@@ -481,6 +487,11 @@ int gbcp_set_option(gbcp_ctx* h, int key, int value) {
   }
   if (key == GBCP_OPT_ZMIRROR && value >= -1 && value <= 1) {
     c.zmirror = value;
+    return GBCP_OK;
+  }
+  if (key == GBCP_OPT_ZKEEP && (value == 0 || value == 1)) {
+    c.zkeep = value;
+    c.zk.valid = false;
     return GBCP_OK;
   }
   if (key == GBCP_OPT_STAGES && value >= 0) {

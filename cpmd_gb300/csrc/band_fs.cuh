@@ -94,7 +94,8 @@ template <typename T, int N, bool MIR>
 __global__ void __launch_bounds__(kThreads) k_zinv_fs(GeoDev g, const cx<double>* __restrict__ c0, int psi32, int ldc,
                                                      int s0, int nstate, cx<T>* __restrict__ zbuf,
                                                      const cx<T>* __restrict__ twAg, const double* __restrict__ f,
-                                                     double* __restrict__ kpart) {
+                                                     double* __restrict__ kpart, const unsigned long long* keep) {
+  if (zk_kept(keep)) return;
   using P = FS<T, N>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* twA = reinterpret_cast<cx<T>*>(smem_raw);

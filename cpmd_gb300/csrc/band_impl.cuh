@@ -226,7 +226,8 @@ template <typename T, int NC>
 __global__ void __launch_bounds__(kThreads) k_zinv(GeoDev g, FftPlan p, const cx<double>* __restrict__ c0, int psi32,
                                                   int ldc, int s0, int nstate, int nlrt, cx<T>* __restrict__ zbuf,
                                                   const cx<T>* __restrict__ twg, const double* __restrict__ f,
-                                                  double* __restrict__ kpart) {
+                                                  double* __restrict__ kpart, const unsigned long long* keep) {
+  if (zk_kept(keep)) return;
   GBCP_STAGE(g.n3, nlrt)
   const int pair = blockIdx.y;
   const int col0 = blockIdx.x * nl;
@@ -589,26 +590,26 @@ int launch_zinv(Ctx& c, const cx<double>* c0, int ldc, int s0, int nstate, int n
                 double* kpart) {
   const GeoDev& g = c.geo;
   cx<T>* zb = static_cast<cx<T>*>(c.zbuf.p) + (size_t)poff * g.n3 * g.ncol;  // pair poff of the launch batch
-  ProfScope ps_(c, "k_zinv");
+  ProfScope ps_(c, c.zk_skip ? "k_zinv_kept" : "k_zinv");  // kept: returns at once if the checksums agree
   if constexpr (NC > 0) {
     const dim3 grid(zinv_blocks_n<T, NC>(c), np);
     if (zmirror_n<T, NC>(c)) {
       constexpr size_t sm = fs_smem<T, NC>(2, 1);
       allow_smem(k_zinv_fs<T, NC, true>, sm);
       k_zinv_fs<T, NC, true><<<grid, kThreads, sm, c.stream>>>(g, c0, c.psi32, ldc, s0, nstate, zb, twA_of<T>(c, 2), f,
-                                                               kpart);
+                                                               kpart, c.zk_skip);
     } else {
       constexpr size_t sm = fs_smem<T, NC>(1, 1);
       allow_smem(k_zinv_fs<T, NC, false>, sm);
       k_zinv_fs<T, NC, false><<<grid, kThreads, sm, c.stream>>>(g, c0, c.psi32, ldc, s0, nstate, zb, twA_of<T>(c, 2), f,
-                                                                kpart);
+                                                                kpart, c.zk_skip);
     }
   } else {
     const int nl = lines_rt(g.n3);
     const size_t sm = stage_smem<T>(g.n3, nl);
     allow_smem(k_zinv<T, 0>, sm);
     k_zinv<T, 0><<<dim3(zinv_blocks_n<T, 0>(c), np), kThreads, sm, c.stream>>>(g, c.plan[2], c0, c.psi32, ldc, s0, nstate, nl,
-                                                                               zb, tw_of<T>(c, 2), f, kpart);
+                                                                               zb, tw_of<T>(c, 2), f, kpart, c.zk_skip);
   }
   GBCP_LAUNCH_CHECK(c);
   return 0;

@@ -134,6 +134,7 @@ struct Ctx {
   // first chunk, number of chunks, density x-stage groups of rhoofr, pairs in the last chunk
   int stage_first = 0, stage_n = 0, stage_groups = 0, stage_last = 0;
   int zmirror = -1;    // Z-stage gather over column/mirror pairs: -1 by size, 0 off, 1 on
+  int zkeep = 1;       // vpsi reuses the Z stage of the rhoofr before it on the same device states: 0 off, 1 on
   int xc = 0;          // energy functional: 0 LDA (Slater + Perdew-Zunger), 1 PBE
   int fft_engine = 0;  // band-loop FFTs: 0 four-step where a plan exists, else Stockham; 2 Stockham always
   int plane = 1;       // FP32 band loop, y and x stages fused per z-plane where the plane fits: bit 0 vpsi, bit 1 rhoofr
@@ -145,6 +146,21 @@ struct Ctx {
   int simt_tile = 64;  // FP64 SIMT overlap / C M GEMMs: output tile 64 or 32
   const char* rmul_name = nullptr;  // profiler name of the next split C M products (Loewdin's n x n ones)
   WfnCache wfn;        // host wavefunction kept on the device between host-memory calls
+  // The Z stage of a device-memory rhoofr over one launch batch, kept for a vpsi on
+  // the same states: zbuf then holds their inverse z-transforms.  The host keeps
+  // what identifies the call; the device compares a checksum of the states taken
+  // by rhoofr (zk_sum[0]) with one taken by vpsi (zk_sum[1]), and vpsi's Z-stage
+  // kernels return at once when they are equal (zk_skip = zk_sum during that vpsi).
+  struct ZKeep {
+    bool valid = false;
+    const void* c0 = nullptr;
+    int ldc = 0, nstate = 0, precision = -1, psi32 = 0;
+    const void* zb = nullptr;
+    size_t zcap = 0;
+  } zk;
+  Scratch zk_sum;
+  const unsigned long long* zk_skip = nullptr;
+  cudaEvent_t zk_ev[2] = {nullptr, nullptr};  // rhoofr's checksum on the side stream: fork, join
   cudaStream_t stream = nullptr;  // stream all work is queued on
   cudaStream_t own = nullptr;     // the context's own stream
   // geometry

@@ -136,6 +136,14 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  *                   default) = over pairs of mirror columns (each coefficient
  *                   loaded once) where the sphere has at least 48 column
  *                   blocks, 0 = off, 1 = on; a batch turns it off;
+ *   GBCP_OPT_ZKEEP  1 (the default) = a device-memory gbcp_vpsi that follows a
+ *                   device-memory gbcp_rhoofr on the same c0 (pointer, leading
+ *                   dimension and state count, both calls one launch batch)
+ *                   reuses rhoofr's inverse z-transforms of the states when a
+ *                   position-keyed 64-bit checksum of all of c0, taken on the
+ *                   device by both calls, is unchanged (the reference reuses its
+ *                   device copy of c0 on a match of SUM(ABS(c0(:,1))),
+ *                   vpsi_utils.mod.F90:278-281); 0 = off;
  *   GBCP_OPT_TEST_TIMEOUT  test hook of the failure path: 1 = the next overlap
  *                   on the tensor cores issues no operand loads, so its first
  *                   bounded wait (no copy in flight towards it) runs out after
@@ -144,6 +152,7 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
 enum gbcp_option { GBCP_OPT_GEMM = 1, GBCP_OPT_BATCH = 2, GBCP_OPT_FFT = 3, GBCP_OPT_XCHUNKS = 4, GBCP_OPT_XC = 5,
                    GBCP_OPT_WFN_CACHE = 6, GBCP_OPT_PLANE = 7, GBCP_OPT_CHOL = 8,
                    GBCP_OPT_SIMT_TILE = 9, GBCP_OPT_STAGES = 10, GBCP_OPT_ZMIRROR = 11,
+                   GBCP_OPT_ZKEEP = 12,
                    GBCP_OPT_TEST_TIMEOUT = 90 };
 int gbcp_set_option(gbcp_ctx* ctx, int key, int value);
 /* Queue later work on `stream` (a cudaStream_t; NULL = the context's own
