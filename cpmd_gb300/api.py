@@ -143,7 +143,7 @@ class Context:
         launch), 'fft' (0 four-step, 2 Stockham), 'xchunks' (density x-stage pair chunks,
         0 = automatic) or 'xc' (energy functional: 0 LDA-PZ, 1 PBE)."""
         k = {"gemm": 1, "batch": 2, "fft": 3, "xchunks": 4, "xc": 5, "wfn_cache": 6, "plane": 7, "chol": 8,
-             "simt_tile": 9, "stages": 10, "zmirror": 11, "zkeep": 12,
+             "simt_tile": 9, "stages": 10, "zmirror": 11, "zkeep": 12, "ortho_columns": 13,
              "test_timeout": 90}[key]
         self._check("gbcp_set_option", self.lib.gbcp_set_option(self.h, k, int(value)))
 

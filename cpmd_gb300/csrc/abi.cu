@@ -450,6 +450,7 @@ int gbcp_ctx_destroy(gbcp_ctx* h) {
     }
   for (cudaEvent_t e : c.pipe_ev) cudaEventDestroy(e);
   for (cudaEvent_t e : c.side_ev) cudaEventDestroy(e);
+  for (cudaEvent_t e : c.col_ev) cudaEventDestroy(e);
   for (cudaEvent_t e : c.zk_ev)
     if (e) cudaEventDestroy(e);
   if (c.d_info) cudaFree(c.d_info);
@@ -487,6 +488,10 @@ int gbcp_set_option(gbcp_ctx* h, int key, int value) {
   }
   if (key == GBCP_OPT_ZMIRROR && value >= -1 && value <= 1) {
     c.zmirror = value;
+    return GBCP_OK;
+  }
+  if (key == GBCP_OPT_ORTHO_COLUMNS && (value == 0 || value == 1)) {
+    c.ortho_cols = value;
     return GBCP_OK;
   }
   if (key == GBCP_OPT_ZKEEP && (value == 0 || value == 1)) {

@@ -23,6 +23,7 @@
 // row-major n x n (symmetric, upper part used; scratch on return); X is row-major
 // n x n, upper triangular, zero below.
 #include <algorithm>
+#include <functional>
 
 #include "ctx.h"
 
@@ -215,17 +216,23 @@ __global__ void __launch_bounds__(RG * B) k_chol_update(double* __restrict__ S, 
 }
 
 // V_ik = X_ii Uw_ik for i < k, into block (i, k) of S; blockIdx.x enumerates the
-// strict upper block triangle, blockIdx.y the row group
+// strict upper block triangle (kcol < 0) or the blocks i = blockIdx.x of block
+// column k = kcol, blockIdx.y the row group
 __global__ void __launch_bounds__(RG * B) k_trtri_v(double* __restrict__ S, const double* __restrict__ Uw,
-                                                    const double* __restrict__ X, int n, int nb,
+                                                    const double* __restrict__ X, int n, int nb, int kcol,
                                                     const int* __restrict__ status) {
   pdl_entry();
   __shared__ double u[B][B + 1];
   __shared__ double xi[RG][B + 1];
   int t = blockIdx.x, bi = 0;
-  while (bi < nb - 1 && t >= nb - 1 - bi) {
-    t -= nb - 1 - bi;
-    ++bi;
+  if (kcol >= 0) {
+    bi = blockIdx.x;
+    t = kcol - 1 - bi;
+  } else {
+    while (bi < nb - 1 && t >= nb - 1 - bi) {
+      t -= nb - 1 - bi;
+      ++bi;
+    }
   }
   const int bk = bi + 1 + t, r0 = blockIdx.y * RG;
   load_rows<B>(Uw, n, bi, bk, 0, u);
@@ -240,13 +247,13 @@ __global__ void __launch_bounds__(RG * B) k_trtri_v(double* __restrict__ S, cons
 }
 
 // X_ij = -sum_{k=i+1..j} V_ik X_kj for the block diagonal j - i = d (V in S);
-// blockIdx.x = i, blockIdx.y the row group
+// i = bi0 + blockIdx.x, blockIdx.y the row group
 __global__ void __launch_bounds__(RG * B) k_trtri_diag(const double* __restrict__ S, double* __restrict__ X, int n,
-                                                       int d, const int* __restrict__ status) {
+                                                       int d, int bi0, const int* __restrict__ status) {
   pdl_entry();
   __shared__ double xk[B][B + 1];
   __shared__ double v[RG][B + 1];
-  const int bi = blockIdx.x, bj = bi + d, r0 = blockIdx.y * RG;
+  const int bi = bi0 + blockIdx.x, bj = bi + d, r0 = blockIdx.y * RG;
   const int rl = threadIdx.x / B, c = threadIdx.x % B, r = r0 + rl;
   double acc = 0.0;
   for (int bk = bi + 1; bk <= bj; ++bk) {
@@ -836,13 +843,101 @@ int chol_inverse(Ctx& c, double* S, double* X, int n) {
   if (nb > 1) {
     ProfScope ps_(c, "k_trtri_v");
     GBCP_LAUNCH_PDL(c, k_trtri_v, dim3(nb * (nb - 1) / 2, B / RG), blk, 0, S, (const double*)Uw, (const double*)X, n,
-                    nb, (const int*)c.d_info);
+                    nb, -1, (const int*)c.d_info);
   }
   for (int d = 1; d < nb; ++d) {
     ProfScope ps_(c, "k_trtri_diag");
-    GBCP_LAUNCH_PDL(c, k_trtri_diag, dim3(nb - d, B / RG), blk, 0, (const double*)S, X, n, d, (const int*)c.d_info);
+    GBCP_LAUNCH_PDL(c, k_trtri_diag, dim3(nb - d, B / RG), blk, 0, (const double*)S, X, n, d, 0, (const int*)c.d_info);
   }
   return 0;
+}
+
+// The blocked chain with X = U^{-1} finished column block by column block, for the
+// host-memory Gram-Schmidt, whose C U^{-1} and download then start one column block
+// at a time while the factorisation goes on.  On the context stream, per block k:
+// the diagonal factor; V_ik = X_ii U_ik (i < k) into S and X_ik for i = k-1 .. 0
+// (the block diagonals of chol_inverse restricted to column k, in the same order);
+// then column(k) is queued on the side stream (the context's stream set to it
+// meanwhile) and the panel and update follow on the context stream.  Element by
+// element the arithmetic of chol_inverse: S blocks (i, k), i < k, are no longer read
+// by the factorisation once diagonal block k is done.  Returns with the context
+// stream waiting for the side stream; 7 if the chain does not apply (one block, or
+// above 8 x 8 blocks).
+int chol_inverse_columns(Ctx& c, double* S, double* X, int n, const std::function<int(int)>& column) {
+  const int nb = (n + B - 1) / B;
+  if (nb < 2 || nb > 8) return 7;
+  const bool df = c.chol_df >= 2 || (c.chol_df == 1 && c.precision == 1);
+  if (!ensure(c, c.cdiag, sizeof(double) * (size_t)n)) return 6;
+  if (!ensure(c, c.cwork, sizeof(double) * (size_t)n * n)) return 6;
+  if (!c.side && cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking) != cudaSuccess) {
+    c.err = "side stream";
+    return 5;
+  }
+  while (c.col_ev.size() < (size_t)nb + 1) {
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      c.err = "events";
+      return 5;
+    }
+    c.col_ev.push_back(e);
+  }
+  double* diag0 = static_cast<double*>(c.cdiag.p);
+  double* Uw = static_cast<double*>(c.cwork.p);
+  const dim3 blk(RG * B);
+  cudaStream_t main = c.stream;
+  int rc = 0;
+  {
+    ProfScope ps_(c, "k_chol_misc");
+    GBCP_LAUNCH_PDL(c, k_zero_lower, dim3(std::max(1, std::min(256, (n * n + 255) / 256))), dim3(256), 0, X,
+                    (const double*)S, diag0, n);
+  }
+  for (int k = 0; k < nb && !rc; ++k) {
+    if (df) {
+      ProfScope ps_(c, "k_chol_diag");
+      GBCP_LAUNCH_PDL(c, (k_chol_lean<B, 8>), dim3(1), dim3(8 * B), 0, (const double*)S, X, (const double*)diag0, n,
+                      k * B, c.d_info);
+    } else {
+      ProfScope ps_(c, "k_chol_diag");
+      GBCP_LAUNCH_PDL(c, k_chol_diag, dim3(1), dim3(8 * B), 0, (const double*)S, Uw, X, (const double*)diag0, n, k,
+                      c.d_info);
+    }
+    // column block k of X: V_ik = X_ii U_ik (i < k), then X_ik for i = k-1 .. 0
+    if (k > 0) {
+      {
+        ProfScope ps_(c, "k_trtri_v");
+        GBCP_LAUNCH_PDL(c, k_trtri_v, dim3(k, B / RG), blk, 0, S, (const double*)Uw, (const double*)X, n, nb, k,
+                        (const int*)c.d_info);
+      }
+      for (int d = 1; d <= k; ++d) {
+        ProfScope ps_(c, "k_trtri_diag");
+        GBCP_LAUNCH_PDL(c, k_trtri_diag, dim3(1, B / RG), blk, 0, (const double*)S, X, n, d, k - d,
+                        (const int*)c.d_info);
+      }
+    }
+    GBCP_CUDA_TRY(c, cudaEventRecord(c.col_ev[k], main));
+    GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.side, c.col_ev[k], 0));
+    c.stream = c.side;
+    rc = column(k);
+    c.stream = main;
+    if (rc) break;
+    const int m0 = nb - k - 1;
+    if (m0 > 0) {
+      {
+        ProfScope ps_(c, "k_chol_panel");
+        GBCP_LAUNCH_PDL(c, k_chol_panel, dim3(m0, B / RG), blk, 0, (const double*)S, (const double*)X, Uw, n, k,
+                        (const int*)c.d_info);
+      }
+      {
+        ProfScope ps_(c, "k_chol_update");
+        GBCP_LAUNCH_PDL(c, k_chol_update, dim3(m0 * (m0 + 1) / 2, B / RG), blk, 0, S, (const double*)Uw, n, nb, k,
+                        (const int*)c.d_info);
+      }
+    }
+  }
+  c.stream = main;
+  // the context stream waits for the side branches (also after an error)
+  if (cudaEventRecord(c.col_ev[nb], c.side) == cudaSuccess) cudaStreamWaitEvent(main, c.col_ev[nb], 0);
+  return rc;
 }
 
 }  // namespace gbcp

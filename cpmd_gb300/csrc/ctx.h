@@ -140,6 +140,7 @@ struct Ctx {
   int plane = 1;       // FP32 band loop, y and x stages fused per z-plane where the plane fits: bit 0 vpsi, bit 1 rhoofr
   int psi32 = 0;       // batch steps: c0 / c2 stored as complex64 (FP32 band loop only)
   int test_stall = 0;  // test hook: the next tensor-core overlap issues no loads and times out (one call)
+  int ortho_cols = 1;  // host-memory Gram-Schmidt: C U^-1 and its download by column blocks as U^-1 finishes them
   int chol_df = 1;     // double-float Cholesky (one CTA to 64 states, diagonal blocks above): 0 never, 1 mixed, 2 both, 3 one CTA to 128
   int oz_ksplit = 0;   // split GEMM partition: K splits per overlap tile (0 = fill the SMs)
   int oz_rgrid = 0;    // split GEMM partition: persistent CTAs of C M (0 = one per SM)
@@ -207,6 +208,7 @@ struct Ctx {
   cudaStream_t copy = nullptr, copy_out = nullptr;  // uploads, downloads (separate copy engines)
   cudaStream_t side = nullptr;                      // ortho: C M row slicing beside S and the Cholesky
   std::vector<cudaEvent_t> side_ev;
+  std::vector<cudaEvent_t> col_ev;  // host Gram-Schmidt: column block k of U^-1 forked to the side stream
   std::vector<cudaEvent_t> pipe_ev;
   const cudaEvent_t* batch_ready = nullptr;
   const cudaEvent_t* batch_c2_ready = nullptr;  // vpsi: the decode of chunk q waits for its C2 columns
@@ -314,6 +316,13 @@ int rortho(Ctx& c, const cx<double>* c0, int ldc0, cx<double>* cm, int ldcm, int
 inline int band_len(const Ctx& c, int n) { return c.fft_engine == 2 ? -1 : n; }
 inline bool use_tc_gemm(const Ctx& c) { return c.gemm_mode == 1 || (c.gemm_mode < 0 && c.precision == 1); }
 int chol_inverse(Ctx& c, double* S, double* X, int n);
+// the blocked chain with U^-1 finished column block by column block; column(k) is
+// called with the context stream set to the side stream, once column block k is queued
+int chol_inverse_columns(Ctx& c, double* S, double* X, int n, const std::function<int(int)>& column);
+// C U^-1 of column block k (32 columns) from the row planes cut by slice_rows_side, on
+// the context stream: the block's digit planes of M, then the tcgen05 split GEMM
+int rmul_tc_column_block(Ctx& c, int rows, int n, const double* M, double* Cout, int ldo, int zero_row1,
+                         int* status, int k);
 int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host);
 // Gram-Schmidt queued on the stream; the status word c.d_info tells the outcome (no synchronisation)
 int ortho_gs_queue(Ctx& c, cx<double>* c0, int ldc, int nstate);

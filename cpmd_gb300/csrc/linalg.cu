@@ -502,28 +502,80 @@ int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host, int res
   const cudaEvent_t* sliced = nullptr;
   unsigned long long* sbits = scond_host ? scond_bits_of(c) : nullptr;
   int rc = 0;
-  if (resident) {
+  const bool cols_ok = c.ortho_cols && n > 64 && n <= 256 && c.chol_df != 3;
+  if (resident && cols_ok) {
+    // by column blocks the first C U^-1 follows the first diagonal block: the row
+    // planes are cut beside the overlap instead of after it
+    rc = slice_rows_side(c, Ar, 2 * ngw, 2 * ngw, n, kb, R, nullptr, &sliced);
+    if (!rc) rc = ovlap_tc(c, d, ngw, n, S, sbits, c.d_info);
+  } else if (resident) {
     rc = ovlap_tc(c, d, ngw, n, S, sbits, c.d_info);
     if (!rc && n <= 256) rc = slice_rows_side(c, Ar, 2 * ngw, 2 * ngw, n, kb, R, nullptr, &sliced);
   } else {
     rc = n <= 256 ? slice_rows_side(c, Ar, 2 * ngw, 2 * ngw, n, kb, R, up, &sliced) : 0;
     if (!rc) rc = ovlap_tc_ranges(c, Ar, 2 * ngw, n, kb, R, up, S, sbits, c.d_info);
   }
-  if (!rc) rc = chol_inverse(c, S, X, n);
-  if (!rc && resident && confirm && !(*confirm)()) {
-    // the host array changed under the same key parts: the speculative overlap and
-    // factor (which only read st_c0) are dropped before anything writes the states
-    cudaStreamSynchronize(c.stream);
-    if (c.side) cudaStreamSynchronize(c.side);
-    return 8;
+  // C U^-1 and the download by column blocks of 32 states as the chain finishes each
+  // block of U^-1 (65 to 256 states; the planes of C cut on the side stream), else
+  // by G-row ranges after the whole chain
+  const int nb = (n + 31) / 32;
+  const bool cols = cols_ok && sliced != nullptr;
+  if (cols) {
+    // the key is confirmed before anything writes the states or the host array
+    if (!rc && resident && confirm && !(*confirm)()) {
+      cudaStreamSynchronize(c.stream);
+      if (c.side) cudaStreamSynchronize(c.side);
+      return 8;
+    }
+    while (!rc && c.col_ev.size() < (size_t)(2 * nb + 1)) {
+      cudaEvent_t e;
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+        c.err = "events";
+        rc = 5;
+      } else {
+        c.col_ev.push_back(e);
+      }
+    }
+    // column block k, queued on the side stream: C U^-1 into st_c2, then its download.
+    // The early blocks reach the host before the factorisation is known to succeed,
+    // so C stays in st_c0 for restoring the host array after a failure
+    if (!rc && !ensure(c, c.st_c2, sizeof(cx<double>) * (size_t)ngw * n)) rc = 6;
+    cx<double>* o = static_cast<cx<double>*>(c.st_c2.p);
+    auto column = [&](int k) -> int {
+      const int r = rmul_tc_column_block(c, 2 * ngw, n, X, reinterpret_cast<double*>(o), 2 * ngw, c.geq0, c.d_info, k);
+      if (r) return r;
+      const cudaEvent_t e = c.col_ev[nb + 1 + k];
+      GBCP_CUDA_TRY(c, cudaEventRecord(e, c.stream));
+      GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.copy_out, e, 0));
+      const int j0 = 32 * k, nj = std::min(n, j0 + 32) - j0;
+      ProfScope ps_(c, "d2h_states", c.copy_out, 2);
+      GBCP_CUDA_TRY(c, cudaMemcpy2DAsync(h + 2 * (size_t)j0 * ldh, sizeof(cx<double>) * (size_t)ldh,
+                                         o + (size_t)j0 * ngw, sizeof(cx<double>) * (size_t)ngw,
+                                         sizeof(cx<double>) * (size_t)ngw, nj, cudaMemcpyDeviceToHost, c.copy_out));
+      return 0;
+    };
+    if (!rc) rc = chol_inverse_columns(c, S, X, n, column);
+  } else {
+    if (!rc) rc = chol_inverse(c, S, X, n);
+    if (!rc && resident && confirm && !(*confirm)()) {
+      // the host array changed under the same key parts: the speculative overlap and
+      // factor (which only read st_c0) are dropped before anything writes the states
+      cudaStreamSynchronize(c.stream);
+      if (c.side) cudaStreamSynchronize(c.side);
+      return 8;
+    }
+    if (!rc) rc = rmul_tc_ranges(c, Ar, 2 * ngw, 2 * ngw, n, X, 1, Ar, 2 * ngw, c.geq0, c.d_info, kb, R, done, sliced);
   }
-  if (!rc) rc = rmul_tc_ranges(c, Ar, 2 * ngw, 2 * ngw, n, X, 1, Ar, 2 * ngw, c.geq0, c.d_info, kb, R, done, sliced);
   if (rc) {
     cudaStreamSynchronize(c.copy);
     if (c.side) cudaStreamSynchronize(c.side);
+    cudaStreamSynchronize(c.copy_out);
+    if (cols && cudaStreamSynchronize(c.stream) == cudaSuccess)  // best effort: the states back to the host
+      cudaMemcpy2D(h, sizeof(cx<double>) * (size_t)ldh, d, sizeof(cx<double>) * (size_t)ngw,
+                   sizeof(cx<double>) * (size_t)ngw, n, cudaMemcpyDeviceToHost);
     return rc;
   }
-  for (int r = 0; r < R; ++r) {
+  for (int r = 0; r < R && !cols; ++r) {
     const int g0 = gb[r], g = gb[r + 1] - gb[r];
     GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.copy_out, done[r], 0));
     ProfScope ps_(c, "d2h_states", c.copy_out, 2);
@@ -533,7 +585,14 @@ int ortho_gs_host(Ctx& c, double* h, int ldh, int n, double* scond_host, int res
                                          cudaMemcpyDeviceToHost, c.copy_out));
   }
   GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.copy_out));
-  return finish_status(c, scond_host);
+  const int st = finish_status(c, scond_host);
+  if (st && cols) {
+    // a failed step by column blocks: the host array gets its states back from st_c0
+    GBCP_CUDA_TRY(c, cudaMemcpy2DAsync(h, sizeof(cx<double>) * (size_t)ldh, d, sizeof(cx<double>) * (size_t)ngw,
+                                       sizeof(cx<double>) * (size_t)ngw, n, cudaMemcpyDeviceToHost, c.stream));
+    GBCP_CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  }
+  return st;
 }
 
 int ortho_gs(Ctx& c, cx<double>* c0, int ldc, int nstate, double* scond_host) {

@@ -201,13 +201,13 @@ __global__ void k_col_max(const double* __restrict__ Ar, int lda, int K, int n, 
   if ((threadIdx.x & 31) == 0 && mx) atomicMax(cmax + j, mx);
 }
 
-// column maxima of a small row-major n x n matrix M over its rows: block = 32
-// columns x 8 row groups, reduced in shared memory
+// column maxima of a small row-major n x n matrix M over its rows, columns j0 ..:
+// block = 32 columns x 8 row groups, reduced in shared memory
 __global__ void __launch_bounds__(256) k_mat_col_max(const double* __restrict__ M, int n,
-                                                     unsigned long long* __restrict__ cmax) {
+                                                     unsigned long long* __restrict__ cmax, int j0) {
   pdl_entry();
   __shared__ unsigned long long red[8][33];
-  const int j = blockIdx.x * 32 + threadIdx.x, g = threadIdx.y;
+  const int j = j0 + blockIdx.x * 32 + threadIdx.x, g = threadIdx.y;
   unsigned long long mx = 0;
   if (j < n) {
     for (int k = g; k < n; k += 8) {
@@ -334,11 +334,11 @@ __global__ void __launch_bounds__(512) k_oz_slice_rows_max(const double* __restr
 
 // C M operand B: plane s, row j (column of M), columns k < n: M[k][j]; exponent per column of M.
 __global__ void k_oz_slice_mat(const double* __restrict__ M, int n, const unsigned long long* __restrict__ emax,
-                               size_t ks, uint4* __restrict__ out) {
+                               size_t ks, uint4* __restrict__ out, int j0, int j1) {
   pdl_entry();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = j0 + blockIdx.x * blockDim.x + threadIdx.x;  // columns j0 .. j1 - 1
   const int k = blockIdx.y * 8;
-  if (j >= n) return;
+  if (j >= j1) return;
   const int e = exp_of_max(emax[j]);
   double x[8];
 #pragma unroll
@@ -369,6 +369,7 @@ struct OzParams {
   int accumulate;                // mode 1: Cout += A M instead of Cout = A M
   int sub_base;                  // mode 0: K offset of this launch, in sub-chunks
   int rt0, nrt;                  // mode 1: row tiles rt0 .. rt0+nrt-1 (nrt = 0: every row tile)
+  int ct0, nct;                  // mode 1: column tiles ct0 .. ct0+nct-1 (nct = 0: every column tile)
   int* status;
   // test of the timeout path: stall != 0 makes the TMA thread issue no loads, so the
   // MMA thread's first wait on a stage (no copy in flight towards it) runs out after
@@ -405,14 +406,14 @@ __device__ __forceinline__ OzUnit oz_unit(const OzParams& p, int u) {
     w.valid = w.nsub > 0;
     return w;
   }
-  const int nrt = p.nrt > 0 ? p.nrt : (p.M + OZ_M - 1) / OZ_M, nct = (p.N + OZ_N - 1) / OZ_N;
+  const int nrt = p.nrt > 0 ? p.nrt : (p.M + OZ_M - 1) / OZ_M, nct = p.nct > 0 ? p.nct : (p.N + OZ_N - 1) / OZ_N;
   // Round k of the persistent loop covers units [k G, k G + G) (G = grid size);
   // odd rounds run the CTAs in reverse order, so that with an upper triangular M
   // (column tile ct costs ct + 1 sub-chunks) each CTA alternates cheap and
   // dear column tiles instead of keeping one for every round.
   const int G = (int)gridDim.x, k = u / G, v = (k & 1) ? k * G + (G - 1 - u % G) : u;
   if (v >= nrt * nct) return w;
-  const int rt = p.rt0 + v / nct, ct = v % nct;  // row tile outer: the CTAs of one row tile share its planes in L2
+  const int rt = p.rt0 + v / nct, ct = p.ct0 + v % nct;  // row tile outer: the CTAs of one row tile share its planes in L2
   w.m0 = rt * OZ_M;
   w.n0 = ct * OZ_N;
   const int kmax = p.upper ? min(p.K, w.n0 + OZ_N) : p.K;
@@ -864,7 +865,7 @@ int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, 
   unsigned long long* mcmax = rmax + rows;
   {
     ProfScope ps_(c, "k_mat_col_max");
-    GBCP_LAUNCH_PDL(c, k_mat_col_max, dim3((n + 31) / 32), dim3(32, 8), 0, M, n, mcmax);
+    GBCP_LAUNCH_PDL(c, k_mat_col_max, dim3((n + 31) / 32), dim3(32, 8), 0, M, n, mcmax, 0);
   }
   if (n <= 256) {
     ProfScope ps_(c, "k_oz_slice");
@@ -882,7 +883,7 @@ int rmul_tc(Ctx& c, const double* A, int lda, int rows, int n, const double* M, 
   {
     ProfScope ps_(c, "k_oz_slice");
     GBCP_LAUNCH_PDL(c, k_oz_slice_mat, dim3((n + 127) / 128, (n + 7) / 8), dim3(128), 0, M, n, mcmax, ks,
-        static_cast<uint4*>(c.oz_b.p));
+        static_cast<uint4*>(c.oz_b.p), 0, n);
   }
   CUtensorMap ma, mb;
   if (!tmap_bf16_2d(&ma, c.oz_a.p, n, (long long)OZ_SL * rows, (int)ks, OZ_KS, OZ_M, 64) ||
@@ -1047,7 +1048,7 @@ int rmul_tc_ranges(Ctx& c, const double* A, int lda, int rows, int n, const doub
   void* planes = sliced ? c.oz_c.p : c.oz_a.p;
   {
     ProfScope ps_(c, "k_mat_col_max");
-    GBCP_LAUNCH_PDL(c, k_mat_col_max, dim3((n + 31) / 32), dim3(32, 8), 0, M, n, mcmax);
+    GBCP_LAUNCH_PDL(c, k_mat_col_max, dim3((n + 31) / 32), dim3(32, 8), 0, M, n, mcmax, 0);
   }
   {
     ProfScope ps_(c, "k_oz_slice");
@@ -1057,7 +1058,7 @@ int rmul_tc_ranges(Ctx& c, const double* A, int lda, int rows, int n, const doub
           rmax, ks, static_cast<uint4*>(c.oz_a.p));
     }
     GBCP_LAUNCH_PDL(c, k_oz_slice_mat, dim3((n + 127) / 128, (n + 7) / 8), dim3(128), 0, M, n, mcmax, ks,
-        static_cast<uint4*>(c.oz_b.p));
+        static_cast<uint4*>(c.oz_b.p), 0, n);
   }
   CUtensorMap ma, mb;
   if (!tmap_bf16_2d(&ma, planes, n, (long long)OZ_SL * rows, (int)ks, OZ_KS, OZ_M, 64) ||
@@ -1098,6 +1099,59 @@ int rmul_tc_ranges(Ctx& c, const double* A, int lda, int rows, int n, const doub
     }
     if (done && done[r]) GBCP_CUDA_TRY(c, cudaEventRecord(done[r], c.stream));
   }
+  return 0;
+}
+
+// C U^-1 of column block k (columns 32 k .. 32 k + 31, K = 32 (k + 1) of the upper
+// triangular M) into Cout, from the row planes and row maxima slice_rows_side cut
+// into oz_c / oz_rmax (queued earlier on the stream this runs on): the block's column
+// maxima and digit planes of M, then the persistent split GEMM over every row tile
+// of that one column tile.  Per output element the arithmetic of rmul_tc_ranges.
+int rmul_tc_column_block(Ctx& c, int rows, int n, const double* M, double* Cout, int ldo, int zero_row1,
+                         int* status, int k) {
+  static_assert(OZ_N == 32, "one column tile per Cholesky block");
+  const size_t ks = ((size_t)n + 7) & ~size_t(7);
+  if (n > 256 || !c.oz_c.p || !c.oz_rmax.p) return 7;
+  if (!ensure(c, c.nl_a, ((size_t)rows + n) * 8) || !ensure(c, c.oz_b, sizeof(uint16_t) * OZ_SL * (size_t)n * ks))
+    return 6;
+  unsigned long long* rmax = static_cast<unsigned long long*>(c.oz_rmax.p);
+  unsigned long long* mcmax = static_cast<unsigned long long*>(c.nl_a.p) + rows;
+  const int j0 = k * OZ_N, j1 = std::min(n, j0 + OZ_N);
+  {
+    ProfScope ps_(c, "k_mat_col_max");
+    GBCP_LAUNCH_PDL(c, k_mat_col_max, dim3(1), dim3(32, 8), 0, M, n, mcmax, j0);
+  }
+  {
+    ProfScope ps_(c, "k_oz_slice");
+    GBCP_LAUNCH_PDL(c, k_oz_slice_mat, dim3(1, (n + 7) / 8), dim3(32), 0, M, n, mcmax, ks,
+        static_cast<uint4*>(c.oz_b.p), j0, j1);
+  }
+  CUtensorMap ma, mb;
+  if (!tmap_bf16_2d(&ma, c.oz_c.p, n, (long long)OZ_SL * rows, (int)ks, OZ_KS, OZ_M, 64) ||
+      !tmap_bf16_2d(&mb, c.oz_b.p, n, (long long)OZ_SL * n, (int)ks, OZ_KS, OZ_N, 64)) {
+    c.err = "C.M: tensor map encoding failed";
+    return 5;
+  }
+  allow_smem(k_oz_tc, OZ_SMEM);
+  OzParams p{};
+  p.M = rows;
+  p.N = n;
+  p.K = n;
+  p.mode = 1;
+  p.upper = 1;
+  p.eA = rmax;
+  p.eB = mcmax;
+  p.Cout = Cout;
+  p.ldo = ldo;
+  p.zero_row1 = zero_row1;
+  p.status = status;
+  p.rt0 = 0;
+  p.nrt = (rows + OZ_M - 1) / OZ_M;
+  p.ct0 = k;
+  p.nct = 1;
+  const int nsm = c.nsm > 0 ? c.nsm : 148;
+  ProfScope ps_(c, "k_ozaki_rmul");
+  GBCP_LAUNCH_PDL(c, k_oz_tc, dim3(std::max(1, std::min(p.nrt, nsm))), dim3(OZ_THREADS), OZ_SMEM, ma, mb, p);
   return 0;
 }
 

@@ -144,6 +144,12 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
  *                   device by both calls, is unchanged (the reference reuses its
  *                   device copy of c0 on a match of SUM(ABS(c0(:,1))),
  *                   vpsi_utils.mod.F90:278-281); 0 = off;
+ *   GBCP_OPT_ORTHO_COLUMNS  host-memory Gram-Schmidt of 65 to 256 states on the
+ *                   tensor cores: 1 (the default) = C U^-1 and its download go
+ *                   column block by column block (32 states) as the Cholesky
+ *                   chain finishes each block of U^-1, so the copy starts after
+ *                   the first diagonal block; 0 = by G-row ranges after the whole
+ *                   chain (the same states bit for bit);
  *   GBCP_OPT_TEST_TIMEOUT  test hook of the failure path: 1 = the next overlap
  *                   on the tensor cores issues no operand loads, so its first
  *                   bounded wait (no copy in flight towards it) runs out after
@@ -152,7 +158,7 @@ int gbcp_set_precision(gbcp_ctx* ctx, int precision);
 enum gbcp_option { GBCP_OPT_GEMM = 1, GBCP_OPT_BATCH = 2, GBCP_OPT_FFT = 3, GBCP_OPT_XCHUNKS = 4, GBCP_OPT_XC = 5,
                    GBCP_OPT_WFN_CACHE = 6, GBCP_OPT_PLANE = 7, GBCP_OPT_CHOL = 8,
                    GBCP_OPT_SIMT_TILE = 9, GBCP_OPT_STAGES = 10, GBCP_OPT_ZMIRROR = 11,
-                   GBCP_OPT_ZKEEP = 12,
+                   GBCP_OPT_ZKEEP = 12, GBCP_OPT_ORTHO_COLUMNS = 13,
                    GBCP_OPT_TEST_TIMEOUT = 90 };
 int gbcp_set_option(gbcp_ctx* ctx, int key, int value);
 /* Queue later work on `stream` (a cudaStream_t; NULL = the context's own
