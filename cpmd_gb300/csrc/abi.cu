@@ -810,7 +810,13 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
       return GBCP_ERR_NOMEM;
     cx<double>* t = static_cast<cx<double>*>(c.st_c0.p);
     const int nb = stage_plan(c, nstate, STAGE_RHOOFR);
-    if ((rc = pipe_prepare(c, nb))) return rc;
+    if ((rc = pipe_prepare(c, nb + 2))) return rc;
+    // events [nb + 1, nb + 2]: the two slabs of rho final; nb + 3: their downloads done.
+    // The first slab 70 % of the planes: its download overlaps the rest, and each
+    // launch stays a few full waves
+    c.rho_slabs = 2;
+    c.rho_zsplit = c.nr[2] * 7 / 10;
+    c.rho_ev = c.pipe_ev.data() + nb + 1;
     const bool resident = wfn_hit(c, c0, ldc, nstate);
     for (int b = 0; b < nb; ++b) {
       const int s0 = 2 * c.stage_bounds[b], ns = std::min(2 * c.stage_bounds[b + 1], nstate) - s0;
@@ -833,13 +839,25 @@ int gbcp_rhoofr(gbcp_ctx* h, const double* c0, int ldc, int nstate, const double
   }
   rc = gbcp::band_rhoofr(c, dc0, dld, nstate, df, drho, dsc);
   c.batch_ready = nullptr;
+  const cudaEvent_t* slab_ev = c.rho_ev;
+  c.rho_ev = nullptr;
+  c.rho_slabs = 0;
   // the cache key (a host pass over c0's first column) once the GPU has its work
   if (mem == GBCP_MEM_HOST) wfn_put(c, c0, ldc, nstate);
   if (saved_batch) c.batch = saved_batch;
   if (!rc && mem == GBCP_MEM_HOST) {
-    gbcp::ProfScope ps_(c, "d2h_rho", c.stream, 2);
-    cudaError_t e = cudaMemcpyAsync(rhoe, drho, sizeof(double) * nnr1, cudaMemcpyDeviceToHost, c.stream);
-    if (e != cudaSuccess) return set_err(h, GBCP_ERR_CUDA, cudaGetErrorString(e));
+    // rho back in two slabs of z planes on the download stream, each once final (the
+    // second with the padding planes), beside the density scalars
+    const size_t plane = (size_t)c.kr[0] * c.kr[1];
+    for (int i = 0; i < 2; ++i) {
+      const size_t p0 = i ? plane * (size_t)c.rho_zsplit : 0, p1 = i ? nnr1 : plane * (size_t)c.rho_zsplit;
+      GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.copy_out, slab_ev[i], 0));
+      gbcp::ProfScope ps_(c, "d2h_rho", c.copy_out, 2);
+      GBCP_CUDA_TRY(c, cudaMemcpyAsync(rhoe + p0, drho + p0, sizeof(double) * (p1 - p0), cudaMemcpyDeviceToHost,
+                                       c.copy_out));
+    }
+    GBCP_CUDA_TRY(c, cudaEventRecord(slab_ev[2], c.copy_out));
+    GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, slab_ev[2], 0));
   }
   if (!rc && scalars) {
     double hs[3] = {0.0, 0.0, 0.0};

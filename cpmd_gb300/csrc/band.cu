@@ -278,9 +278,16 @@ int band_rhoofr(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double*
                 double* scalars) {
   const size_t nnr = (size_t)c.kr[0] * c.kr[1] * c.kr[2];
   GBCP_CUDA_TRY(c, cudaMemsetAsync(rho, 0, sizeof(double) * nnr, c.stream));
+  // the slab events of a host-staged call: recorded here if the band loop did not
+  c.rho_ev_set = false;
+  auto slab_events = [&]() -> int {
+    if (c.rho_ev && !c.rho_ev_set)
+      for (int i = 0; i < c.rho_slabs; ++i) GBCP_CUDA_TRY(c, cudaEventRecord(c.rho_ev[i], c.stream));
+    return 0;
+  };
   if (nstate <= 0) {
     if (scalars) GBCP_CUDA_TRY(c, cudaMemsetAsync(scalars, 0, 3 * sizeof(double), c.stream));
-    return 0;
+    return slab_events();
   }
   // partials of E_kin / norm: one pair of doubles (FP32 gather: four floats, two
   // double-float pairs) per Z-stage CTA of every pair, then three per CTA of the fold
@@ -323,6 +330,7 @@ int band_rhoofr(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double*
   const int rc = c.precision == 0 ? band_rhoofr_fp64(c, c0, ldc, nstate, f, rho, kpart)
                                   : band_rhoofr_fp32(c, c0, ldc, nstate, f, rho, kpart);
   if (keep) GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.zk_ev[1], 0));
+  if (!rc && slab_events()) return 5;
   if (!rc && keep) {
     c.zk.valid = true;
     c.zk.c0 = c0;

@@ -274,7 +274,8 @@ template <typename T, int N, bool PR>
 __global__ void __launch_bounds__(kThreads) k_xrho_fs(GeoDev g, const cx<T>* __restrict__ ybuf, int npairs, int s0,
                                                      int nstate, const double* __restrict__ f, double inv_omega,
                                                      double* __restrict__ rho, const cx<T>* __restrict__ twAg,
-                                                     int pchunk, T* __restrict__ part, unsigned* __restrict__ tickets) {
+                                                     int pchunk, T* __restrict__ part, unsigned* __restrict__ tickets,
+                                                     int z0) {
   using P = FS<T, N>;
   constexpr int NBUF = xrho_bufs<T>();
   static_assert(P::IB == 1, "density tile: one step-B task per thread");
@@ -283,7 +284,7 @@ __global__ void __launch_bounds__(kThreads) k_xrho_fs(GeoDev g, const cx<T>* __r
   cx<T>* Ts = twA + N;
   cx<T>* slab = Ts + P::L * P::XS;
   const int nslot = g.nslot, slab_n = P::L * nslot;
-  const int nchunk = gridDim.x, chunk = blockIdx.x, y0 = blockIdx.y * P::L, z = blockIdx.z;
+  const int nchunk = gridDim.x, chunk = blockIdx.x, y0 = blockIdx.y * P::L, z = z0 + blockIdx.z;  // planes z0 ..
   const int p0 = chunk * pchunk, p1 = min(npairs, p0 + pchunk);
   const int nel = min(P::L, g.n2 - y0) * nslot;
   load_table(twA, twAg, N);
@@ -348,7 +349,7 @@ __global__ void __launch_bounds__(kThreads) k_xrho_fs(GeoDev g, const cx<T>* __r
     }
     return;
   }
-  const int tile = blockIdx.z * gridDim.y + blockIdx.y;
+  const int tile = z * gridDim.y + blockIdx.y;
   T* mine = part + ((size_t)tile * nchunk + chunk) * (P::TB * P::N2);
   if (t < P::TB) {
 #pragma unroll

@@ -667,8 +667,9 @@ inline int xrho_chunks(const Ctx& c, int tiles, int np) {
 }
 
 template <typename T, int NC>
-int launch_xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho, int poff) {
+int launch_xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho, int poff, int z0, int z1) {
   const GeoDev& g = c.geo;
+  if (z1 < 0) z1 = g.n3;
   // pairs poff .. poff+np-1 of the launch batch (states from s0)
   const cx<T>* yb = static_cast<const cx<T>*>(c.ybuf.p) + (size_t)poff * g.n3 * g.n2 * g.nslot;
   if constexpr (NC > 0) {
@@ -697,8 +698,8 @@ int launch_xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double*
     ProfScope ps_(c, "k_xinv_rho");
     auto go = [&](auto kern) {
       allow_smem(kern, sm);
-      kern<<<dim3(nchunk, tiles_y, g.n3), kThreads, sm, c.stream>>>(g, yb, np, s0, nstate, f, 1.0 / c.omega, rho,
-                                                                    twA_of<T>(c, 0), pchunk, part, tickets);
+      kern<<<dim3(nchunk, tiles_y, z1 - z0), kThreads, sm, c.stream>>>(g, yb, np, s0, nstate, f, 1.0 / c.omega, rho,
+                                                                         twA_of<T>(c, 0), pchunk, part, tickets, z0);
     };
     if constexpr (FS<T, NC>::N1 == 8) {
       if (g.prune_x) go(k_xrho_fs<T, NC, true>);
@@ -707,6 +708,7 @@ int launch_xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double*
       go(k_xrho_fs<T, NC, false>);
     }
   } else {
+    if (z0 != 0 || z1 != g.n3) return 7;  // planes are split in the four-step kernel only
     int nl = lines_rt(g.n1);
     while (nl > 1 && nl * g.n1 > kMaxAcc * kThreads) --nl;
     if (nl * g.n1 > kMaxAcc * kThreads) {
@@ -928,9 +930,16 @@ template <typename T> int kin_blocks(const Ctx& c) { return zinv_blocks<T>(c) * 
 template <typename T> int yinv(Ctx& c, int np, int poff = 0) {
   GBCP_DISPATCH(launch_yinv, T, band_len(c, c.nr[1]), c, np, poff)
 }
+// planes z0 .. z1-1 (z1 < 0: to the last plane; other than all planes only in the four-step kernels)
 template <typename T>
-int xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho, int poff = 0) {
-  GBCP_DISPATCH(launch_xinv_rho, T, band_len(c, c.nr[0]), c, np, s0, nstate, f, rho, poff)
+int xinv_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho, int poff = 0, int z0 = 0, int z1 = -1) {
+  GBCP_DISPATCH(launch_xinv_rho, T, band_len(c, c.nr[0]), c, np, s0, nstate, f, rho, poff, z0, z1)
+}
+// the density x-stage's z planes can be launched in slabs (four-step kernels)
+template <typename T> bool xrho_slabs(const Ctx& c) {
+  const int n = band_len(c, c.nr[0]);
+  return c.fft_engine != 2 && (n == 32 || n == 36 || n == 40 || n == 48 || n == 60 || n == 64 || n == 72 || n == 80 ||
+                               n == 96 || n == 120 || n == 144 || n == 240);
 }
 template <typename T> int xvx(Ctx& c, int np, const double* vpot, const T* vpotT) {
   GBCP_DISPATCH(launch_xvx, T, band_len(c, c.nr[0]), c, np, vpot, vpotT)
@@ -981,6 +990,25 @@ int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f,
     return plane ? plane_rho<T>(c, g1 - g0, 2 * g0, nstate, f, rho, g0 - p0b)
                  : xinv_rho<T>(c, g1 - g0, 2 * g0, nstate, f, rho, g0 - p0b);
   };
+  // host staging, the call's last x-stage launch: in slabs of z planes, each followed
+  // by its event, so that rho goes back slab by slab while the later ones compute
+  // (band_rhoofr records the events at its end if no such launch ran)
+  auto density_final = [&](int g0, int g1, int p0b) -> int {
+    const int ns = c.rho_ev ? c.rho_slabs : 0;
+    int r = 0;
+    if (ns == 2 && !plane && xrho_slabs<T>(c) && c.rho_zsplit > 0 && c.rho_zsplit < c.geo.n3) {
+      for (int i = 0; i < ns && !r; ++i) {
+        r = xinv_rho<T>(c, g1 - g0, 2 * g0, nstate, f, rho, g0 - p0b, i ? c.rho_zsplit : 0,
+                        i ? c.geo.n3 : c.rho_zsplit);
+        if (!r) GBCP_CUDA_TRY(c, cudaEventRecord(c.rho_ev[i], c.stream));
+      }
+    } else {
+      r = density(g0, g1, p0b);
+      for (int i = 0; i < ns && !r; ++i) GBCP_CUDA_TRY(c, cudaEventRecord(c.rho_ev[i], c.stream));
+    }
+    c.rho_ev_set = !r;
+    return r;
+  };
   for (int p0 = 0, np = 0; p0 < npairs_total; p0 += np) {
     np = std::min(c.batch, npairs_total - p0);
     const int s0 = 2 * p0;
@@ -995,6 +1023,7 @@ int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f,
       const std::vector<int>& b = c.stage_bounds;
       const size_t nq = b.size() - 1;
       const size_t ng = std::max<size_t>(1, std::min<size_t>(nq, c.stage_groups > 0 ? c.stage_groups : 2));
+      const bool last_batch = p0 + np >= npairs_total;
       int g0 = p0;  // first pair of the x-stage group not yet launched
       for (size_t q = 0; q < nq; ++q) {
         const int q0 = std::max(b[q], p0), q1 = std::min(b[q + 1], p0 + np);
@@ -1007,11 +1036,12 @@ int rhoofr_t(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double* f,
         // group ends after chunks ceil(nq g / ng), g = 1 .. ng
         const bool group_end = ((q + 1) * ng) / nq != (q * ng) / nq || q + 1 == nq;
         if (group_end && gend > g0) {
-          if ((rc = density(g0, gend, p0))) return rc;
+          const bool fin = last_batch && gend == p0 + np;
+          if ((rc = fin ? density_final(g0, gend, p0) : density(g0, gend, p0))) return rc;
           g0 = gend;
         }
       }
-      if (g0 < p0 + np && (rc = density(g0, p0 + np, p0))) return rc;
+      if (g0 < p0 + np && (rc = last_batch ? density_final(g0, p0 + np, p0) : density(g0, p0 + np, p0))) return rc;
     }
   }
   return 0;

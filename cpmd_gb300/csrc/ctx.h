@@ -213,6 +213,12 @@ struct Ctx {
   const cudaEvent_t* batch_ready = nullptr;
   const cudaEvent_t* batch_c2_ready = nullptr;  // vpsi: the decode of chunk q waits for its C2 columns
   cudaEvent_t vpot_ready = nullptr;             // vpsi: the first x-stage waits for V(r)
+  // rhoofr with host staging: the last density x-stage in two slabs of z planes,
+  // [0, rho_zsplit) and [rho_zsplit, n3); rho_ev[i] recorded once slab i is final
+  int rho_slabs = 0;
+  int rho_zsplit = 0;
+  const cudaEvent_t* rho_ev = nullptr;
+  bool rho_ev_set = false;  // the slab events were recorded by the call's last x-stage
   std::function<int(int)> batch_done;
   std::vector<int> stage_bounds;  // staging chunks as pair ranges [b[q], b[q+1]); each is one launch batch
   // profiling
