@@ -27,6 +27,7 @@ bool ensure(Ctx& c, Scratch& s, size_t bytes) {
   if (&s == &c.zbuf) {  // nor a kept Z stage
     c.zk.valid = false;
     c.zk_skip = nullptr;
+    c.zk_host = false;
   }
   if (s.p) {
     cudaStreamSynchronize(c.stream);
@@ -925,6 +926,7 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
       GBCP_CUDA_TRY(c, cudaEventRecord(c.pipe_ev[3 * nb + 1], c.copy));
     }
     const bool resident = wfn_hit(c, c0, ldc, nstate);  // c0 still on the device from rhoofr
+    c.zk_resident = resident;
     for (int b = 0; b <= nb; ++b) {
       int s0, ns;
       if (b < nb) {
@@ -962,6 +964,7 @@ int gbcp_vpsi(gbcp_ctx* h, const double* c0, int ldc, double* c2, int ldc2, cons
     l0 = l2 = c.ngw;
   }
   rc = gbcp::band_vpsi(c, dc0, l0, dc2, l2, df, dv, nstate);
+  c.zk_resident = false;
   c.batch_ready = nullptr;
   c.batch_c2_ready = nullptr;
   c.vpot_ready = nullptr;

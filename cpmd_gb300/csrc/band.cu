@@ -305,9 +305,11 @@ int band_rhoofr(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double*
   }
   // device states in one launch batch: checksum them for a vpsi that may reuse the Z
   // stage, on the side stream beside the Z stage (which waits on scattered loads, not
-  // on HBM bandwidth)
+  // on HBM bandwidth).  Host staging over one launch batch: the Z stage is kept for a
+  // vpsi on the same staging copy, recognised by the wavefunction cache's key
   c.zk.valid = false;
   const bool keep = c.zkeep && !c.batch_ready && npairs <= c.batch;
+  const bool keep_host = c.zkeep && c.batch_ready && npairs <= c.batch;
   if (keep) {
     if (!c.side && cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking) != cudaSuccess) {
       c.err = "side stream";
@@ -331,7 +333,7 @@ int band_rhoofr(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double*
                                   : band_rhoofr_fp32(c, c0, ldc, nstate, f, rho, kpart);
   if (keep) GBCP_CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.zk_ev[1], 0));
   if (!rc && slab_events()) return 5;
-  if (!rc && keep) {
+  if (!rc && (keep || keep_host)) {
     c.zk.valid = true;
     c.zk.c0 = c0;
     c.zk.ldc = ldc;
@@ -340,6 +342,7 @@ int band_rhoofr(Ctx& c, const cx<double>* c0, int ldc, int nstate, const double*
     c.zk.psi32 = c.psi32;
     c.zk.zb = c.zbuf.p;
     c.zk.zcap = c.zbuf.cap;
+    c.zk.host = keep_host;
   }
   if (rc || !scalars) return rc;
   {
@@ -360,9 +363,12 @@ int band_vpsi(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, c
   // the Z stage of the rhoofr before it on the same device states, one launch batch
   // in both calls and zbuf untouched since: the Z-stage kernels return at once if
   // the states' checksum is unchanged (a reallocation of zbuf drops zk_skip)
-  const bool kept = c.zkeep && c.zk.valid && !c.batch_ready && (nstate + 1) / 2 <= c.batch && c.zk.c0 == c0 &&
-                    c.zk.ldc == ldc && c.zk.nstate == nstate && c.zk.precision == c.precision &&
-                    c.zk.psi32 == c.psi32 && c.zk.zb == c.zbuf.p && c.zk.zcap == c.zbuf.cap;
+  const bool same = c.zkeep && c.zk.valid && c.zk.c0 == c0 && c.zk.ldc == ldc && c.zk.nstate == nstate &&
+                    c.zk.precision == c.precision && c.zk.psi32 == c.psi32 && c.zk.zb == c.zbuf.p &&
+                    c.zk.zcap == c.zbuf.cap;
+  const bool kept = same && !c.zk.host && !c.batch_ready && (nstate + 1) / 2 <= c.batch;
+  // host staging: the staging copy still holds rhoofr's states (the cache's hit)
+  c.zk_host = same && c.zk.host && c.batch_ready && c.zk_resident;
   c.zk.valid = false;  // vpsi's y-forward overwrites zbuf
   if (kept) {
     const int r = zk_checksum(c, c0, ldc, nstate, 1);
@@ -372,6 +378,7 @@ int band_vpsi(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, c
   const int rc = c.precision == 0 ? band_vpsi_fp64(c, c0, ldc, c2, ldc2, f, vpot, nstate)
                                   : band_vpsi_fp32(c, c0, ldc, c2, ldc2, f, vpot, nstate);
   c.zk_skip = nullptr;
+  c.zk_host = false;
   return rc;
 }
 

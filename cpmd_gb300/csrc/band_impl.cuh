@@ -774,9 +774,9 @@ template <typename T, int NC> int launch_yfwd(Ctx& c, int np) {
   return 0;
 }
 
-template <typename T, int NC> int launch_zfwd(Ctx& c, int np) {
+template <typename T, int NC> int launch_zfwd(Ctx& c, int np, int poff) {
   const GeoDev& g = c.geo;
-  const cx<T>* zb = static_cast<const cx<T>*>(c.zbuf.p);
+  const cx<T>* zb = static_cast<const cx<T>*>(c.zbuf.p) + (size_t)poff * g.n3 * g.ncol;  // pairs poff ..
   cx<T>* qb = static_cast<cx<T>*>(c.qbuf.p);
   const T scale = (T)(1.0 / ((double)g.n1 * g.n2 * g.n3));
   ProfScope ps_(c, "k_zfwd");
@@ -945,14 +945,16 @@ template <typename T> int xvx(Ctx& c, int np, const double* vpot, const T* vpotT
   GBCP_DISPATCH(launch_xvx, T, band_len(c, c.nr[0]), c, np, vpot, vpotT)
 }
 template <typename T> int yfwd(Ctx& c, int np) { GBCP_DISPATCH(launch_yfwd, T, band_len(c, c.nr[1]), c, np) }
-template <typename T> int plane_vx(Ctx& c, int np, const T* vpotT) {
-  GBCP_DISPATCH(launch_plane_vx, T, c.nr[0], c, np, 0, vpotT)
+template <typename T> int plane_vx(Ctx& c, int np, const T* vpotT, int poff = 0) {
+  GBCP_DISPATCH(launch_plane_vx, T, c.nr[0], c, np, poff, vpotT)
 }
 template <typename T>
 int plane_rho(Ctx& c, int np, int s0, int nstate, const double* f, double* rho, int poff = 0) {
   GBCP_DISPATCH(launch_plane_rho, T, c.nr[0], c, np, s0, nstate, f, rho, poff)
 }
-template <typename T> int zfwd(Ctx& c, int np) { GBCP_DISPATCH(launch_zfwd, T, band_len(c, c.nr[2]), c, np) }
+template <typename T> int zfwd(Ctx& c, int np, int poff = 0) {
+  GBCP_DISPATCH(launch_zfwd, T, band_len(c, c.nr[2]), c, np, poff)
+}
 
 // Z stage of pairs [p0, p0 + np): one launch, or, with host staging, one launch per
 // staging chunk after that chunk's columns have arrived
@@ -1070,20 +1072,23 @@ int vpsi_t(Ctx& c, const cx<double>* c0, int ldc, cx<double>* c2, int ldc2, cons
     }
     return 0;
   };
+  // host staging with the Z stage kept from rhoofr (all pairs in zbuf at their own
+  // positions): no Z stage, each staging chunk's stages on its pairs of zbuf
+  const bool hkeep = c.zk_host && plane;
   for (int p0 = 0, np = 0; p0 < npairs_total; p0 += np) {
     np = launch_pairs(c, p0, npairs_total);
     const int s0 = 2 * p0;
-    if ((rc = zinv_staged<T>(c, c0, ldc, p0, nstate, np))) return rc;
+    if (!hkeep && (rc = zinv_staged<T>(c, c0, ldc, p0, nstate, np))) return rc;
     if (plane) {
       if (p0 == 0 && (rc = prepare_v())) return rc;
-      if ((rc = plane_vx<T>(c, np, vT))) return rc;
+      if ((rc = plane_vx<T>(c, np, vT, hkeep ? p0 : 0))) return rc;
     } else {
       if ((rc = yinv<T>(c, np))) return rc;
       if (p0 == 0 && (rc = prepare_v())) return rc;
       if ((rc = xvx<T>(c, np, vpot, vT))) return rc;
       if ((rc = yfwd<T>(c, np))) return rc;
     }
-    if ((rc = zfwd<T>(c, np))) return rc;
+    if ((rc = zfwd<T>(c, np, hkeep ? p0 : 0))) return rc;
     if (!c.batch_ready) {
       if ((rc = launch_decode<T>(c, np, c0, ldc, c2, ldc2, f, s0, nstate))) return rc;
     } else {

@@ -158,7 +158,12 @@ struct Ctx {
     int ldc = 0, nstate = 0, precision = -1, psi32 = 0;
     const void* zb = nullptr;
     size_t zcap = 0;
+    bool host = false;  // a host-staged rhoofr: zbuf holds its pairs, c0 its staging copy
   } zk;
+  // vpsi with host staging: c0 is the staging copy rhoofr uploaded (the wavefunction
+  // cache's hit, set by the caller) and, if zk matches, zk_host skips the Z stage
+  bool zk_resident = false;
+  bool zk_host = false;
   Scratch zk_sum;
   const unsigned long long* zk_skip = nullptr;
   cudaEvent_t zk_ev[2] = {nullptr, nullptr};  // rhoofr's checksum on the side stream: fork, join

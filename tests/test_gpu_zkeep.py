@@ -8,7 +8,9 @@ reuses its device copy of c0 on a match of SUM(ABS(c0(:,1))) (vpsi_utils.mod.F90
 278-281).  C2 must equal that of a context with the option off bit for bit, on every
 Z-stage kernel (four-step with and without the mirror-pair gather, Stockham); a change
 of c0 between the calls (one coefficient, two states exchanged), a second vpsi, or a
-rhoofr on another array in between must be noticed.
+rhoofr on another array in between must be noticed.  Host-memory calls keep the Z
+stage only through the wavefunction cache: a vpsi on the staging copy the rhoofr
+uploaded (its key confirmed) runs no Z stage.
 """
 import numpy as np
 import pytest
@@ -122,3 +124,34 @@ def test_host_memory_calls_keep_nothing(gpu_lib):
     c2dr = torch.zeros_like(c0)
     off.vpsi(c0, c2dr, f, v)
     assert torch.equal(c2d, c2dr)
+
+
+def test_host_staged_vpsi_on_the_cached_copy_skips_the_z_stage(gpu_lib):
+    """With the wavefunction cache, a host-memory vpsi on the array the host-memory
+    rhoofr just uploaded finds rhoofr's inverse z-transforms of all pairs in zbuf and
+    runs no Z stage; C2 equals that of the option off bit for bit.  A changed first
+    column (a new key) uploads and transforms again."""
+    from cpmd_gb300 import Context
+    cl = make_cell("c1", nstate=64)
+    on, off = pair(cl.basis, "mixed", wfn_cache=1)
+    res = []
+    for ctx in (on, off):
+        c0 = cl.c0.copy(order="F")
+        ctx.rhoofr(c0, cl.f)
+        ctx.profile(True)
+        c2 = np.zeros_like(c0)
+        ctx.vpsi(c0, c2, cl.f, cl.vpot)
+        names = [r[0] for r in ctx.profile_timeline()]
+        ctx.profile(False)
+        res.append((c2, names))
+    assert np.array_equal(res[0][0], res[1][0])
+    assert "k_zinv" not in res[0][1] and "k_zinv" in res[1][1]
+    # a new key: the Z stage runs again and C2 is that of the changed states
+    c0 = cl.c0.copy(order="F")
+    on.rhoofr(c0, cl.f)
+    c0[:, 0] *= 1.5
+    c2 = np.zeros_like(c0)
+    on.vpsi(c0, c2, cl.f, cl.vpot)
+    c2r = np.zeros_like(c0)
+    Context(cl.basis, "mixed").vpsi(c0, c2r, cl.f, cl.vpot)
+    assert np.array_equal(c2, c2r)
