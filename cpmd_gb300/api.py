@@ -39,6 +39,10 @@ import numpy as np
 from . import _lib
 from ._lib import MEM_DEVICE, MEM_HOST, ORTHO, PREC, GbcpError
 
+# gbcp_set_option keys: GBCP_OPT_<NAME> of include/cpmd_gb300.h, by lower-case name
+OPTIONS = {"gemm": 1, "batch": 2, "fft": 3, "xchunks": 4, "xc": 5, "wfn_cache": 6, "plane": 7, "chol": 8,
+           "simt_tile": 9, "stages": 10, "zmirror": 11, "zkeep": 12, "ortho_columns": 13, "test_timeout": 90}
+
 
 def _is_torch(x) -> bool:
     return type(x).__module__.startswith("torch")
@@ -139,13 +143,11 @@ class Context:
         self.precision = precision
 
     def set_option(self, key: str, value: int):
-        """key 'gemm' (-1 by precision, 0 FP64 SIMT, 1 tensor cores), 'batch' (pairs per
-        launch), 'fft' (0 four-step, 2 Stockham), 'xchunks' (density x-stage pair chunks,
-        0 = automatic) or 'xc' (energy functional: 0 LDA-PZ, 1 PBE)."""
-        k = {"gemm": 1, "batch": 2, "fft": 3, "xchunks": 4, "xc": 5, "wfn_cache": 6, "plane": 7, "chol": 8,
-             "simt_tile": 9, "stages": 10, "zmirror": 11, "zkeep": 12, "ortho_columns": 13,
-             "test_timeout": 90}[key]
-        self._check("gbcp_set_option", self.lib.gbcp_set_option(self.h, k, int(value)))
+        """key: a name of OPTIONS (GBCP_OPT_<NAME> of the C header, lower case), e.g.
+        'gemm' (-1 by precision, 0 FP64 SIMT, 1 tensor cores), 'batch' (pairs per
+        launch), 'fft' (0 four-step, 2 Stockham), 'xc' (0 LDA-PZ, 1 PBE), 'wfn_cache',
+        'zkeep', 'ortho_columns'; the values are those the header documents."""
+        self._check("gbcp_set_option", self.lib.gbcp_set_option(self.h, OPTIONS[key], int(value)))
 
     def synchronize(self):
         self._check("gbcp_synchronize", self.lib.gbcp_synchronize(self.h))

@@ -72,3 +72,13 @@ def test_create_rejects_bad_arguments_without_gpu(lib):
 def test_built_for_sm103a():
     from cpmd_gb300 import build as B
     assert "arch=compute_103a,code=sm_103a" in " ".join(B.ARCH)
+
+
+def test_python_options_match_header_enum():
+    """Every GBCP_OPT_* of the header is reachable from Context.set_option under its
+    lower-case name, with the header's value, and nothing else is."""
+    from cpmd_gb300.api import OPTIONS
+    txt = (ROOT / "include" / "cpmd_gb300.h").read_text()
+    body = re.search(r"enum gbcp_option\s*\{(.*?)\}", txt, flags=re.S).group(1)
+    enum = {m.group(1).lower(): int(m.group(2)) for m in re.finditer(r"GBCP_OPT_([A-Z0-9_]+)\s*=\s*(\d+)", body)}
+    assert enum == OPTIONS
