@@ -46,7 +46,7 @@ def step(ctx, c0, f, v, c2in=None):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("opts", [{}, {"zmirror": 1}, {"zmirror": 0}, {"fft": 2}])
+@pytest.mark.parametrize("opts", [{}, {"zmirror": 1}, {"zmirror": 0}, {"fft": 2}, {"plane": 3}])
 def test_kept_z_stage_gives_the_same_rho_and_c2(gpu_lib, precision, opts):
     cl = make_cell("c0")
     on, off = pair(cl.basis, precision, **opts)
