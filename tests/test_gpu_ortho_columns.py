@@ -66,3 +66,25 @@ def test_column_blocks_failed_factorisation_leaves_host_states(gpu_lib):
     ref = O.rgs(ok, cl.basis.geq0)
     ctx.ortho(ok, "gs")
     assert rel(ok, ref) < 1e-12
+
+
+@pytest.mark.parametrize("cached", [False, True])
+def test_column_blocks_with_upload_ranges(gpu_lib, cached):
+    """ngw = 42 736: four G-row upload ranges, whose overlap parts and row planes start
+    as each range lands (uncached), or one pass on the cached copy."""
+    from cpmd_gb300 import Context
+    from cpmd_gb300.synth import make_cell
+    cl = make_cell("c1", nstate=100)
+    c = perturbed(cl.c0, 0.02, 100)
+    outs = []
+    for cols in (0, 1):
+        ctx = Context(cl.basis, "mixed")
+        ctx.set_option("ortho_columns", cols)
+        out = c.copy(order="F")
+        if cached:
+            ctx.set_option("wfn_cache", 1)
+            ctx.rhoofr(out, cl.f)
+        ctx.ortho(out, "gs")
+        outs.append(out)
+    assert np.array_equal(outs[0], outs[1])
+    assert rel(outs[1], O.rgs(c, cl.basis.geq0)) < 1e-12
