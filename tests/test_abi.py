@@ -82,3 +82,15 @@ def test_python_options_match_header_enum():
     body = re.search(r"enum gbcp_option\s*\{(.*?)\}", txt, flags=re.S).group(1)
     enum = {m.group(1).lower(): int(m.group(2)) for m in re.finditer(r"GBCP_OPT_([A-Z0-9_]+)\s*=\s*(\d+)", body)}
     assert enum == OPTIONS
+
+
+def test_fortran_module_options_match_header_enum():
+    """The option constants of the Fortran module in INTEGRATION.md are the header's
+    (the test hook GBCP_OPT_TEST_TIMEOUT is left out there)."""
+    txt = (ROOT / "include" / "cpmd_gb300.h").read_text()
+    body = re.search(r"enum gbcp_option\s*\{(.*?)\}", txt, flags=re.S).group(1)
+    enum = {m.group(1): int(m.group(2)) for m in re.finditer(r"(GBCP_OPT_[A-Z0-9_]+)\s*=\s*(\d+)", body)}
+    enum.pop("GBCP_OPT_TEST_TIMEOUT")
+    fort = (ROOT / "INTEGRATION.md").read_text()
+    got = {m.group(1): int(m.group(2)) for m in re.finditer(r"(GBCP_OPT_[A-Z0-9_]+) = (\d+)", fort)}
+    assert got == enum
