@@ -890,6 +890,55 @@ def run_case_loewdin(args):
     ctx.close()
 
 
+def run_case_timeline(args):
+    """One config-1 step through the C ABI with pinned host buffers (rhoofr, vpsi,
+    Gram-Schmidt ortho; the wavefunction cache on), after 5 warm-up steps, with the
+    library's per-launch event timers: one JSON line per kernel or copy (name, lane:
+    0 kernels, 1 uploads, 2 downloads; start and end in ms from the first record).
+    The timers add a few microseconds per launch."""
+    import torch
+    from cpmd_gb300 import Context
+    from cpmd_gb300.synth import make_cell
+    cell = make_cell("c1")
+    b, n = cell.basis, cell.nstate
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()  # noqa: E731
+    c0h = pin((n, b.ngw), torch.complex128)
+    c0h[:] = cell.c0.T
+    c0h = c0h.T
+    c2h = pin((n, b.ngw), torch.complex128)
+    c2h[:] = 0
+    c2h = c2h.T
+    fh = pin((n,), torch.float64)
+    fh[:] = cell.f
+    vh = pin(tuple(b.kr[::-1]), torch.float64)
+    vh[:] = cell.vpot
+    rhoh = pin(tuple(b.kr[::-1]), torch.float64)
+    ctx = Context(b, "mixed")
+    ctx.set_option("wfn_cache", 1)
+
+    def step():
+        t = [time.perf_counter()]
+        ctx.rhoofr(c0h, fh, rhoh, energies=True)
+        t.append(time.perf_counter())
+        ctx.vpsi(c0h, c2h, fh, vh)
+        t.append(time.perf_counter())
+        ctx.ortho(c0h, "gs")
+        t.append(time.perf_counter())
+        return [round((t[i + 1] - t[i]) * 1e3, 3) for i in range(3)]
+    for _ in range(5):
+        step()
+    plain = step()
+    ctx.profile(True)
+    timed = step()
+    tl = ctx.profile_timeline()
+    ctx.profile(False)
+    t0 = min(r[2] for r in tl)
+    print(json.dumps({"case": "timeline", "host_ms_per_call": plain, "host_ms_per_call_with_timers": timed}))
+    for name, lane, a, e in sorted(tl, key=lambda r: r[2]):
+        print(json.dumps({"name": name, "lane": lane, "start_ms": round(a - t0, 4), "end_ms": round(e - t0, 4)}))
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -901,7 +950,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the 8-, 216- and 512-atom cells")
-    ap.add_argument("--case", default=None, choices=["projectors", "loewdin"],
+    ap.add_argument("--case", default=None, choices=["projectors", "loewdin", "timeline"],
                     help="run one small case of a single path instead of the benchmark (for profiling)")
     ap.add_argument("--case-states", type=int, default=512)
     ap.add_argument("--case-atoms", type=int, default=128)
@@ -911,6 +960,9 @@ def main():
         return
     if args.case == "loewdin":
         run_case_loewdin(args)
+        return
+    if args.case == "timeline":
+        run_case_timeline(args)
         return
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":
